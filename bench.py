@@ -1,0 +1,333 @@
+"""Benchmark of the GB300 photon-packet Monte Carlo loop.
+
+Workload: the full-3D precision model (grid 400 x 199 x 64 with a seeded
+3-level fractal envelope, 80 peel-off directions = 20 inclinations x 4
+azimuths, 301^2 broadband Stokes I,Q,U,V images, 50 wavelength bins).  Its
+temperatures are first brought up by two Lucy iterations (untimed set-up).
+One step is one call of disk() for the final, peeled iteration on a batch of
+packets: zero the tallies, run the packet loop, solve the Lucy temperatures.
+
+  value  packets/s with the model resident in HBM (CUDA events on the
+         library's stream around each step; L2 flushed between steps)
+  e2e    the same through the C-ABI with host buffers: run parameters in,
+         every tally and the temperature grid back to host each step
+  roofline  algorithmic bytes of the transport kernel per launch (propagation
+         crossings x (4S+16) B + peel crossings x 4S B, S = 3 active species)
+         over its event-timed duration, against the measured HBM peak
+  cpu_baseline  the CPU oracle (C restatement, FP64) on the host cores, on
+         a bounded sample of the same workload
+
+``--impl reference`` times the CPU oracle alone (the reference cannot be
+built here: no Fortran compiler and 14 modules missing).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "packets/s mixed vs FP64 on 1 GB300 at ≤1% SED err; models/hr; serving p99 latency"
+WORKLOAD = "full3d"
+S_ACTIVE = 3
+B_PROP = 4 * S_ACTIVE + 16
+B_PEEL = 4 * S_ACTIVE
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--id={self.device}",
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def build_model(tmp: Path, name: str):
+    from hochunk3d_gb300 import configs, hc3d
+
+    par = configs.write_par(tmp, name)
+    return hc3d.Model(par)
+
+
+def warm_up_temperatures(model, ctx, n_lucy: int, iters: int = 2):
+    """Untimed set-up: Lucy iterations (no peel-off) to a realistic dust field."""
+    td = None
+    for it in range(1, iters + 1):
+        p = model.run_params(np=n_lucy, iter=it, ipeel=0)
+        ctx.zero()
+        ctx.run(p)
+        td, rel, conv = ctx.lucy_update(model.info.ltot, n_lucy)
+    model.set_tdust(td)
+    return td
+
+
+def run_cpu_oracle(model, np_, threads, iter_=9, seed_offset=0):
+    import oracle.oracle as O
+
+    p = model.run_params(np=np_, iter=iter_, ipeel=1, packet_offset=seed_offset)
+    t0 = time.perf_counter()
+    r = O.run(model, p, nthreads=threads)
+    return time.perf_counter() - t0, r
+
+
+def cpu_baseline(model, budget_s: float = 15.0):
+    threads = os.cpu_count() or 1
+    n = max(threads, 16)
+    dt, _ = run_cpu_oracle(model, n, threads)
+    while dt < 1.0 and n < 1 << 22:
+        n *= 4
+        dt, _ = run_cpu_oracle(model, n, threads)
+    n = int(max(threads, min(n * budget_s / max(dt, 1e-3), 1 << 24)))
+    dt, r = run_cpu_oracle(model, n, threads, seed_offset=1 << 40)
+    return {"value": n / dt, "unit": "packets/s", "cores": threads, "kind": "port",
+            "sample": f"{n} packets of the {WORKLOAD} peeled iteration (oracle C restatement, FP64, "
+                      f"{threads} threads, {dt:.1f} s)"}
+
+
+def reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as td:
+        from hochunk3d_gb300.build import build_library, build_oracle
+
+        build_library()
+        build_oracle()
+        model = build_model(Path(td), WORKLOAD)
+        # same dust field as the GPU arm would start from: a warm profile
+        from tests.helpers import warm_tdust
+
+        model.set_tdust(warm_tdust(model))
+        threads = os.cpu_count() or 1
+        n = max(threads * 2, 32)
+        dt, _ = run_cpu_oracle(model, n, threads)
+        n = int(max(threads, n * 20.0 / max(dt, 1e-3)))
+        times = []
+        for s in range(args.warmup + args.steps):
+            dt, _ = run_cpu_oracle(model, n, threads, seed_offset=(s + 1) << 32)
+            if s >= args.warmup:
+                times.append(dt)
+        v = n * len(times) / sum(times)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "packets/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": WORKLOAD, "packets_per_step": n},
+                "cpu_baseline": {"value": v, "unit": "packets/s", "cores": threads, "kind": "port",
+                                 "sample": f"{n} packets per step, oracle C restatement with {threads} threads"},
+                "e2e": {"value": v, "unit": "packets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--step-seconds", type=float, default=2.0)
+    ap.add_argument("--packets", type=int, default=0, help="packets per step (0 = calibrate)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lucy-packets", type=int, default=2_000_000)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from hochunk3d_gb300 import hc3d
+    from hochunk3d_gb300.build import build_library, build_oracle
+
+    if rank == 0:
+        build_library()
+        build_oracle()
+    if world > 1:
+        torch.distributed.barrier()
+
+    with tempfile.TemporaryDirectory() as td:
+        model = build_model(Path(td), WORKLOAD)
+        ctx = hc3d.Context(hc3d.PREC_MIXED, device=local).load(model)
+        warm_up_temperatures(model, ctx, args.lucy_packets)
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+        def step(np_, it, off, e2e=False, T=None):
+            p = model.run_params(np=np_, iter=it, ipeel=1, packet_offset=off)
+            ctx.zero()
+            ctx.run(p)
+            if e2e:
+                T = ctx.tallies(p)
+                td_, rel, conv = ctx.lucy_update(model.info.ltot, np_, want_tdust=True)
+                return T, td_
+            ctx.lucy_update(model.info.ltot, np_, want_tdust=False)
+            return None
+
+        # calibrate the batch so one step takes about --step-seconds
+        n = args.packets
+        if n <= 0:
+            n = 20000
+            t0 = time.perf_counter()
+            step(n, 100, 0)
+            dt = time.perf_counter() - t0
+            n = int(min(max(n * args.step_seconds / max(dt, 1e-3), 1000), 50_000_000))
+        for w in range(args.warmup):
+            step(n, 200 + w, rank * n)
+        ev = []
+        kern_ms, cross_prop, cross_peel = [], 0, 0
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for s in range(args.steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step(n, 300 + s, (s * world + rank) * n)
+                e1.record(stream)
+                e1.synchronize()
+                ev.append(e0.elapsed_time(e1))
+                kern_ms.append(ctx.last_kernel_ms())
+                c = ctx.tallies(model.run_params(np=n, ipeel=1), grid=False)["counters"]
+                cross_prop += int(c[hc3d.CNT["cross_prop"]])
+                cross_peel += int(c[hc3d.CNT["cross_peel"]])
+        torch.cuda.synchronize()
+        step_ms = sum(ev) / len(ev)
+        if world > 1:
+            t = torch.tensor([step_ms], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            step_ms = float(t.item())
+        value = n * world / (step_ms / 1000.0)
+
+        # end to end through the C-ABI with host buffers
+        e2e_times = []
+        h2d = d2h = 0
+        for s in range(max(2, args.steps // 2)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            T, tdh = step(n, 400 + s, (1 << 36) + s * n, e2e=True)
+            torch.cuda.synchronize()
+            e2e_times.append(time.perf_counter() - t0)
+            d2h = sum(v.nbytes for k, v in T.items() if isinstance(v, np.ndarray)) + tdh.nbytes
+            h2d = 8 * 4 * model.npeel + 8 * len(model.aperture2)
+        e2e = n * world / (sum(e2e_times) / len(e2e_times))
+
+        # the all-FP64 form on the same model and temperatures, for the speed-up
+        ctx64 = hc3d.Context(hc3d.PREC_FP64, device=local).load(model)
+        n64 = max(1000, n // 16)
+        p64 = model.run_params(np=n64, iter=500, ipeel=1)
+        ctx64.zero(); ctx64.run(p64)
+        t64 = []
+        for s in range(2):
+            ctx64.zero()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ctx64.run(model.run_params(np=n64, iter=501 + s, ipeel=1))
+            t64.append(time.perf_counter() - t0)
+        fp64_value = n64 / (sum(t64) / len(t64))
+        ctx64.close()
+
+        kms = sum(kern_ms) / len(kern_ms)
+        bytes_per_launch = (cross_prop * B_PROP + cross_peel * B_PEEL) / args.steps
+        peak, peak_kind = measured_peaks()
+        achieved = bytes_per_launch / (kms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": None, "kernel": "k_transport<float>",
+                "kernel_ms": kms, "crossings_per_step": {"prop": cross_prop // args.steps,
+                                                         "peel": cross_peel // args.steps}}
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            cpu = cpu_baseline(model)
+        if rank == 0:
+            line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                    "config": {"workload": WORKLOAD, "grid": [400, 199, 64], "peel_directions": 80,
+                               "image": [301, 301, 4], "nfreq": 50, "packets_per_step": n,
+                               "l2": "256 MiB buffer written between timed steps",
+                               "lucy_setup": f"2 iterations x {args.lucy_packets} packets"},
+                    "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),
+                            "d2h_bytes_per_step": int(d2h)},
+                    "fp64": {"value": fp64_value, "unit": "packets/s", "packets_per_step": n64,
+                             "speedup_mixed_over_fp64": value / world / fp64_value},
+                    "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
+                    "gpu_launches": 2 * args.steps}
+            print(json.dumps(line))
+        ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,108 @@
+"""Build recipe of the GB300 library (sm_103a) and of the CPU oracle.
+
+``build_library()`` compiles the CUDA kernels, the C-ABI and the host driver
+into ``hochunk3d_gb300/libhc3d.so`` with nvcc; ``build_oracle()`` compiles the
+CPU restatement used by the tests into ``oracle/_build/libhc3d_oracle.so``.
+Translation units are compiled in parallel; a unit is rebuilt when its source
+or any header is newer than its object file.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libhc3d.so"
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_LIB = ORACLE_DIR / "_build" / "libhc3d_oracle.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+
+# (source, extra flags); the all-FP64 kernel keeps multiplies and adds
+# separately rounded so that it reproduces the CPU restatement
+UNITS = [
+    ("hc3d_kernel_mixed.cu", []),
+    ("hc3d_kernel_fp64.cu", ["--fmad=false"]),
+    ("hc3d_capi.cu", []),
+    ("hc3d_model.cpp", []),
+    ("hc3d_driver.cpp", []),
+]
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or Path(c).exists()):
+            return c
+    return "nvcc"
+
+
+def _headers() -> list[Path]:
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+
+
+def _stale(obj: Path, src: Path) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in [src, *_headers(), Path(__file__)])
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def build_library(verbose: bool = False, force: bool = False) -> Path:
+    """Compile every translation unit for sm_103a and link libhc3d.so."""
+    BUILD.mkdir(exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    objs = []
+    for src_name, extra in UNITS:
+        src = CSRC / src_name
+        obj = BUILD / (src.stem + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src):
+            lang = ["-x", "cu"] if src.suffix == ".cu" else []
+            cmd = [nvcc, *ARCH, *NVCC_COMMON, *extra, *lang, "-c", str(src), "-o", str(obj)]
+            jobs.append(cmd)
+    if jobs:
+        with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for _ in ex.map(_run, jobs):
+                pass
+    if force or jobs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
+        os.replace(tmp, LIB)
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+def build_oracle(verbose: bool = False, force: bool = False) -> Path:
+    """Compile the CPU restatement (test infrastructure) with gcc."""
+    src = ORACLE_DIR / "hc3d_oracle.c"
+    ORACLE_LIB.parent.mkdir(exist_ok=True)
+    deps = [src, ORACLE_DIR / "philox.h", ROOT / "include" / "hc3d.h"]
+    if force or not ORACLE_LIB.exists() or any(p.stat().st_mtime > ORACLE_LIB.stat().st_mtime for p in deps):
+        tmp = ORACLE_LIB.with_suffix(".so.tmp")
+        _run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu11", "-o", str(tmp), str(src),
+              "-lm", "-lpthread"])
+        os.replace(tmp, ORACLE_LIB)
+    if verbose:
+        print(f"built {ORACLE_LIB}")
+    return ORACLE_LIB
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    build_library(verbose=True, force=force)
+    build_oracle(verbose=True, force=force)

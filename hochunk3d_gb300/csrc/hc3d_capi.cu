@@ -1,0 +1,736 @@
+// hc3d_capi.cu -- the C-ABI of include/hc3d.h: context, device layouts,
+// the Lucy temperature solve and tally read-back.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/hc3d.h"
+#include "hc3d_device.h"
+
+using namespace hc3d;
+
+struct hc3d_ctx {
+  int device = 0, precision = HC3D_PREC_MIXED, block_size = 128, grid_blocks = 0;
+  int sm_count = 0;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  bool tables = false, grid = false;
+  // model
+  DevModel dm{};
+  std::vector<void*> model_allocs;
+  std::vector<void*> grid_allocs;
+  double tsub = 1600.0;
+  double kappav[kSlots] = {0, 0, 0, 0};
+  double* d_kappap = nullptr;  // (nT, kSlots)
+  double* d_massarr = nullptr; // (ncell*4)
+  double* d_tdust = nullptr;   // (ncell*4), also dm.tdust
+  unsigned char* d_peelmask = nullptr;
+  int ndg_in = 0;
+  // tallies
+  DevTallies dt{};
+  TallyDims dims{};
+  bool run_tallies = false;
+  std::vector<void*> run_allocs;
+  bool scales_set = false;
+  int64_t epoch_np = 0, epoch_budget = 0;
+  int status_seen = 0;
+  unsigned long long* d_work = nullptr;
+  int* d_status = nullptr;
+  double* d_peeldir = nullptr;
+  double* d_ap2 = nullptr;
+  unsigned long long* d_maxrel = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+};
+
+namespace {
+
+int fail(hc3d_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(c, HC3D_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(hc3d_ctx* c, std::vector<void*>& owner, T** p, size_t n) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  owner.push_back(q);
+  *p = (T*)q;
+  return HC3D_OK;
+}
+
+template <class T>
+int dupload(hc3d_ctx* c, std::vector<void*>& owner, T** p, const T* src, size_t n) {
+  int r = dalloc(c, owner, p, n);
+  if (r) return r;
+  if (n) {
+    cudaError_t e = cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  }
+  return HC3D_OK;
+}
+
+void free_all(std::vector<void*>& v) {
+  for (void* p : v) cudaFree(p);
+  v.clear();
+}
+
+int ceil_log2(double x) {
+  int k = 0;
+  while ((double)(1ull << k) < x && k < 62) ++k;
+  return k;
+}
+
+// ---- Lucy temperature (tfinal restated; dusttemp.f90:30-50 fixed point) ----
+struct LucyArgs {
+  int64_t ncell;
+  int nT;
+  const double* lTint;
+  const double* kappap;  // (nT, kSlots)
+  double kappav[kSlots];
+  double ltot, nphot, path_scale, tsub, na_min;
+  int nslots;
+};
+
+__device__ double kapp_dev(const LucyArgs& a, double T, int s) {
+  // KapP, dust.f90:114-141
+  const double lT = log(T);
+  const double l1 = a.lTint[0], lN = a.lTint[a.nT - 1];
+  const int k = (int)((double)(a.nT - 1) * (lT - l1) / (lN - l1)) + 1;
+  const double* kp = a.kappap + (size_t)s * a.nT;
+  if (k < 1) return kp[0];
+  if (k > a.nT - 1) return kp[a.nT - 1];
+  const double f = (lT - a.lTint[k - 1]) / (a.lTint[k] - a.lTint[k - 1]);
+  return (1.0 - f) * kp[k - 1] + f * kp[k];
+}
+
+__device__ double dusttemp_dev(const LucyArgs& a, double na, double T0, int s, double massarr) {
+  const double eps = 1.e-5, sigt = 5.670400e-5;
+  double Td = T0 != 0.0 ? T0 : 0.1 / 11605.0;
+  double Told = 0.5 * Td;
+  int it = 0;
+  while (fabs(Td - Told) > eps * Td && it < 1000) {
+    ++it;
+    Told = Td;
+    Td = pow((na * a.ltot) / (4.0 * sigt * a.nphot * a.kappav[s] * kapp_dev(a, Td, s)), 0.25) / 11605.0;
+    if (massarr > 0.0) Td = Td / massarr;
+    else Td = 0.1 / 11605.0;
+    if (Td > 1600.0 / 11605.0) Td = 1600.0 / 11605.0;
+    if (Td < 0.1 / 11605.0) Td = 0.1 / 11605.0;
+  }
+  return Td;
+}
+
+__global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const double* rho4d, const double* massarr,
+                       double* tdust, unsigned char* peelmask, unsigned long long* maxrel) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.ncell; c += (int64_t)gridDim.x * blockDim.x) {
+    unsigned mask = 0;
+    for (int s = 0; s < kSlots; ++s) {
+      double T = tdust[4 * c + s];
+      if (s < a.nslots && rho4d[4 * c + s] > 0.0) {
+        const double na = (double)(long long)dtauabs[(int64_t)s * a.ncell + c] / a.path_scale;
+        const double Td = dusttemp_dev(a, na, T, s, massarr[4 * c + s]);
+        if (na >= a.na_min) {
+          const double rel = fabs(Td - T) / Td;
+          atomicMax(maxrel, (unsigned long long)__double_as_longlong(rel));
+        }
+        T = Td;
+        tdust[4 * c + s] = Td;
+      }
+      if (T < a.tsub / 11605.0) mask |= 1u << s;
+    }
+    peelmask[c] = (unsigned char)mask;
+  }
+}
+
+__global__ void k_peelmask(int64_t ncell, const double* tdust, double tsub, unsigned char* peelmask) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
+    unsigned mask = 0;
+    for (int s = 0; s < kSlots; ++s)
+      if (tdust[4 * c + s] < tsub / 11605.0) mask |= 1u << s;
+    peelmask[c] = (unsigned char)mask;
+  }
+}
+
+int grid_blocks_for(hc3d_ctx* c, int64_t n) {
+  int64_t b = (n + 255) / 256;
+  int64_t cap = (int64_t)c->sm_count * 8;
+  return (int)std::max<int64_t>(1, std::min(b, cap));
+}
+
+int alloc_run_tallies(hc3d_ctx* c, const TallyDims& d) {
+  free_all(c->run_allocs);
+  c->run_tallies = false;
+  int r;
+  if ((r = dalloc(c, c->run_allocs, &c->dt.sed, (size_t)9 * d.nsed))) return r;
+  if ((r = dalloc(c, c->run_allocs, &c->dt.psed, (size_t)9 * std::max<int64_t>(d.npsed, 1)))) return r;
+  if ((r = dalloc(c, c->run_allocs, &c->dt.img, (size_t)4 * std::max<int64_t>(d.nimg, 1)))) return r;
+  CK(cudaMemset(c->dt.sed, 0, sizeof(unsigned long long) * 9 * d.nsed));
+  CK(cudaMemset(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(d.npsed, 1)));
+  CK(cudaMemset(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(d.nimg, 1)));
+  c->dims = d;
+  c->run_tallies = true;
+  return HC3D_OK;
+}
+
+bool same_dims(const TallyDims& a, const TallyDims& b) {
+  return a.nfreq == b.nfreq && a.nmu == b.nmu && a.nph == b.nph && a.nap == b.nap && a.npeel == b.npeel &&
+         a.nx == b.nx;
+}
+
+TallyDims dims_of(const hc3d_run_params* p) {
+  TallyDims d;
+  d.nfreq = p->nfreq; d.nmu = p->nmu; d.nph = p->nph; d.nap = p->nap;
+  d.npeel = p->ipeel ? p->npeel : 0;
+  d.nx = p->nxhst;
+  d.nsed = (int64_t)p->nfreq * p->nmu * p->nph * p->nap * kNo;
+  d.npsed = (int64_t)p->nfreq * d.npeel * p->nap * kNo;
+  d.nimg = (int64_t)d.npeel * p->nxhst * p->nxhst;
+  return d;
+}
+
+int check_params(hc3d_ctx* c, const hc3d_run_params* p) {
+  if (!p) return fail(c, HC3D_ERR_INVALID, "params is NULL");
+  if (p->np < 0 || p->packet_offset < 0) return fail(c, HC3D_ERR_INVALID, "np and packet_offset must be >= 0");
+  if (p->nfreq < 1 || p->nmu < 1 || p->nph < 1 || p->nap < 1)
+    return fail(c, HC3D_ERR_INVALID, "nfreq, nmu, nph and nap must be >= 1");
+  if (!p->aperture2) return fail(c, HC3D_ERR_INVALID, "aperture2 is NULL");
+  if (p->ipeel) {
+    if (p->npeel < 1 || p->npeel > kMaxPeel) return fail(c, HC3D_ERR_INVALID, "npeel must be in 1..256");
+    if (!p->thete || !p->phie) return fail(c, HC3D_ERR_INVALID, "thete/phie are NULL");
+    if (p->nxhst < 1) return fail(c, HC3D_ERR_INVALID, "nxhst must be >= 1");
+  }
+  if (p->limb != 0) return fail(c, HC3D_ERR_UNSUPPORTED, "limb-darkening table (CLIMB=YES) is not supported");
+  if (!(p->numin > 0.0) || !(p->numax > p->numin)) return fail(c, HC3D_ERR_INVALID, "need 0 < numin < numax");
+  if (!(p->rstar_cm > 0.0) || !(p->rmaxi > 0.0 || !p->ipeel)) return fail(c, HC3D_ERR_INVALID, "bad rstar_cm/rmaxi");
+  return HC3D_OK;
+}
+
+int set_scales(hc3d_ctx* c, int64_t np) {
+  const double budget = (double)std::max<int64_t>(np, 1 << 20) * 16.0;
+  const int L = ceil_log2(budget);
+  const int sb = std::max(16, std::min(40, 58 - L));
+  const int qb = sb - 8;
+  const int pb = std::max(12, std::min(32, 52 - L));
+  c->dt.stokes_scale = std::ldexp(1.0, sb);
+  c->dt.square_scale = std::ldexp(1.0, qb);
+  c->dt.path_scale = std::ldexp(1.0, pb);
+  c->epoch_budget = (int64_t)budget;
+  c->scales_set = true;
+  return HC3D_OK;
+}
+
+int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
+  int r = check_params(c, p);
+  if (r) return r;
+  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid before running");
+  TallyDims d = dims_of(p);
+  if (!c->run_tallies || !same_dims(d, c->dims)) {
+    if (c->scales_set && c->epoch_np > 0 && c->run_tallies)
+      return fail(c, HC3D_ERR_STATE, "tally shape changed without hc3d_zero_tallies()");
+    if ((r = alloc_run_tallies(c, d))) return r;
+  }
+  if (!c->scales_set) set_scales(c, p->np);
+  if (c->epoch_np + p->np > c->epoch_budget)
+    return fail(c, HC3D_ERR_INVALID, "fixed-point tally budget exceeded: call hc3d_zero_tallies() first");
+  std::vector<double> pdir(4 * (size_t)std::max(1, d.npeel));
+  for (int k = 0; k < d.npeel; ++k) {
+    pdir[4 * k + 0] = std::cos(p->thete[k]);
+    pdir[4 * k + 1] = std::sin(p->thete[k]);
+    pdir[4 * k + 2] = std::cos(p->phie[k]);
+    pdir[4 * k + 3] = std::sin(p->phie[k]);
+  }
+  CK(cudaMemcpyAsync(c->d_peeldir, pdir.data(), sizeof(double) * pdir.size(), cudaMemcpyHostToDevice, c->stream));
+  if (p->nap > 64) return fail(c, HC3D_ERR_INVALID, "nap must be <= 64");
+  CK(cudaMemcpyAsync(c->d_ap2, p->aperture2, sizeof(double) * p->nap, cudaMemcpyHostToDevice, c->stream));
+  std::memset(a, 0, sizeof(*a));
+  a->np = p->np;
+  a->packet_offset = p->packet_offset;
+  a->key0 = (uint32_t)p->seed ^ ((uint32_t)p->iter * 0x9E3779B9u);
+  a->key1 = (uint32_t)(p->seed >> 32);
+  a->ipeel = p->ipeel ? 1 : 0;
+  a->npeel = d.npeel;
+  a->image = p->ipeel && p->image ? 1 : 0;
+  a->nfreq = p->nfreq; a->nmu = p->nmu; a->nph = p->nph; a->nap = p->nap; a->nx = p->nxhst;
+  a->rmaxi = p->rmaxi;
+  a->fractxh = p->nxhst > 0 ? 2.0 * p->rmaxi / (double)p->nxhst : 1.0;
+  a->numin = p->numin;
+  a->lnurat = std::log(p->numax / p->numin);
+  a->rstar_cm = p->rstar_cm;
+  a->iintmax = p->iintmax > 0 ? p->iintmax : 10000;
+  a->max_interactions = p->max_interactions;
+  a->peeldir = c->d_peeldir;
+  a->aperture2 = c->d_ap2;
+  a->work = c->d_work;
+  a->status = c->d_status;
+  return HC3D_OK;
+}
+
+int finish_run(hc3d_ctx* c) {
+  CK(cudaStreamSynchronize(c->stream));
+  int st = 0;
+  CK(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st && !c->status_seen) c->status_seen = st;
+  return HC3D_OK;
+}
+
+}  // namespace
+
+extern "C" const char* hc3d_version(void) { return "hc3d 0.1 sm_103a"; }
+
+extern "C" int hc3d_create(hc3d_ctx** out, const hc3d_device_opts* opts) {
+  if (!out) return HC3D_ERR_INVALID;
+  *out = nullptr;
+  hc3d_ctx* c = new (std::nothrow) hc3d_ctx();
+  if (!c) return HC3D_ERR_NOMEM;
+  if (opts) {
+    c->device = opts->device;
+    c->precision = opts->precision;
+    if (opts->block_size > 0) c->block_size = opts->block_size;
+    c->grid_blocks = opts->grid_blocks;
+  }
+  if (c->precision != HC3D_PREC_MIXED && c->precision != HC3D_PREC_FP64) {
+    delete c;
+    return HC3D_ERR_INVALID;
+  }
+  if (c->block_size % 32 != 0 || c->block_size > 128) {
+    delete c;
+    return HC3D_ERR_INVALID;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || c->device < 0 || c->device >= ndev) {
+    delete c;
+    return HC3D_ERR_CUDA;
+  }
+  if (cudaSetDevice(c->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return HC3D_ERR_CUDA;
+  }
+  std::vector<void*>& own = c->model_allocs;
+  if (dalloc(c, own, &c->d_work, 1) || dalloc(c, own, &c->d_status, 1) ||
+      dalloc(c, own, &c->d_peeldir, 4 * kMaxPeel) || dalloc(c, own, &c->d_ap2, 64) ||
+      dalloc(c, own, &c->d_maxrel, 1) || dalloc(c, own, &c->dt.counters, 16)) {
+    free_all(own);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return HC3D_ERR_NOMEM;
+  }
+  cudaMemset(c->dt.counters, 0, 16 * sizeof(unsigned long long));
+  cudaMemset(c->d_status, 0, sizeof(int));
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    free_all(own);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return HC3D_ERR_CUDA;
+  }
+  *out = c;
+  return HC3D_OK;
+}
+
+extern "C" void hc3d_destroy(hc3d_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c->run_allocs);
+  free_all(c->grid_allocs);
+  free_all(c->model_allocs);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" void* hc3d_get_stream(hc3d_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int hc3d_last_kernel_ms(hc3d_ctx* c, double* ms) {
+  if (!c || !ms) return HC3D_ERR_INVALID;
+  *ms = c->last_ms;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_get_error(const hc3d_ctx* c, char* buf, size_t len) {
+  if (!c || !buf || !len) return HC3D_ERR_INVALID;
+  std::snprintf(buf, len, "%s", c->err.c_str());
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
+  if (!c || !t) return HC3D_ERR_INVALID;
+  if (t->ndg < 1 || t->ndg > HC3D_NDG || t->nlammax < 2 || t->nT < 2 || t->nnu < 2 || t->nhnu < 3)
+    return fail(c, HC3D_ERR_INVALID, "bad table dimensions");
+  if (!t->nlambda || !t->nudust || !t->kappad || !t->adust || !t->gdust || !t->pldust || !t->kappav || !t->lTint ||
+      !t->nuint || !t->kapBint || !t->kappap || !t->hnuint || !t->atmosnu || !t->lognu || !t->loghnu)
+    return fail(c, HC3D_ERR_INVALID, "a table pointer is NULL");
+  CK(cudaSetDevice(c->device));
+  if (c->tables) {
+    // tables own their allocations at the front of model_allocs; rebuild the context tables
+    return fail(c, HC3D_ERR_STATE, "tables already loaded in this context");
+  }
+  const int ns = std::min(t->ndg, kSlots);
+  std::vector<double> nud((size_t)t->nlammax * kSlots), kap(nud.size()), alb(nud.size()), gg(nud.size()),
+      pl(nud.size());
+  std::vector<double> kB((size_t)t->nT * t->nnu * kSlots), kp((size_t)t->nT * kSlots);
+  for (int s = 0; s < kSlots; ++s) {
+    const int src = s < ns ? s : 0;
+    const int nl = t->nlambda[src];
+    if (nl < 2 || nl > t->nlammax) return fail(c, HC3D_ERR_INVALID, "nlambda out of range");
+    c->dm.nlambda[s] = nl;
+    for (int i = 0; i < t->nlammax; ++i) {
+      const size_t o = (size_t)src * t->nlammax + i, q = (size_t)s * t->nlammax + i;
+      nud[q] = t->nudust[o]; kap[q] = t->kappad[o]; alb[q] = t->adust[o]; gg[q] = t->gdust[o]; pl[q] = t->pldust[o];
+    }
+    std::memcpy(&kB[(size_t)s * t->nT * t->nnu], t->kapBint + (size_t)src * t->nT * t->nnu,
+                sizeof(double) * t->nT * t->nnu);
+    std::memcpy(&kp[(size_t)s * t->nT], t->kappap + (size_t)src * t->nT, sizeof(double) * t->nT);
+    c->dm.kappav[s] = t->kappav[src];
+    c->kappav[s] = t->kappav[src];
+  }
+  std::vector<void*>& own = c->model_allocs;
+  int r;
+  double *d_nud, *d_kap, *d_alb, *d_g, *d_pl, *d_lT, *d_nuint, *d_kB, *d_hn, *d_an, *d_ln, *d_lh;
+  if ((r = dupload(c, own, &d_nud, nud.data(), nud.size())) || (r = dupload(c, own, &d_kap, kap.data(), kap.size())) ||
+      (r = dupload(c, own, &d_alb, alb.data(), alb.size())) || (r = dupload(c, own, &d_g, gg.data(), gg.size())) ||
+      (r = dupload(c, own, &d_pl, pl.data(), pl.size())) || (r = dupload(c, own, &d_lT, t->lTint, (size_t)t->nT)) ||
+      (r = dupload(c, own, &d_nuint, t->nuint, (size_t)t->nnu)) || (r = dupload(c, own, &d_kB, kB.data(), kB.size())) ||
+      (r = dupload(c, own, &c->d_kappap, kp.data(), kp.size())) ||
+      (r = dupload(c, own, &d_hn, t->hnuint, (size_t)t->nhnu)) ||
+      (r = dupload(c, own, &d_an, t->atmosnu, (size_t)t->nhnu)) ||
+      (r = dupload(c, own, &d_ln, t->lognu, (size_t)t->nhnu)) ||
+      (r = dupload(c, own, &d_lh, t->loghnu, (size_t)t->nhnu)))
+    return r;
+  c->dm.nlammax = t->nlammax;
+  c->dm.nudust = d_nud; c->dm.kappad = d_kap; c->dm.adust = d_alb; c->dm.gdust = d_g; c->dm.pldust = d_pl;
+  c->dm.nT = t->nT; c->dm.nnu = t->nnu; c->dm.lTint = d_lT; c->dm.nuint = d_nuint; c->dm.kapBint = d_kB;
+  c->dm.nhnu = t->nhnu; c->dm.hnuint = d_hn; c->dm.atmosnu = d_an; c->dm.lognu = d_ln; c->dm.loghnu = d_lh;
+  c->tsub = t->tsub > 0.0 ? t->tsub : 1600.0;
+  c->tables = true;
+  if (c->grid) {
+    k_peelmask<<<grid_blocks_for(c, c->dm.ncell), 256, 0, c->stream>>>(c->dm.ncell, c->d_tdust, c->tsub, c->d_peelmask);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
+  if (!c || !g) return HC3D_ERR_INVALID;
+  if (g->nrg < 3 || g->ntg < 3 || g->npg < 2 || g->ndg < 1 || g->ndg > HC3D_NDG)
+    return fail(c, HC3D_ERR_INVALID, "bad grid dimensions");
+  if (!g->rarr || !g->r2arr || !g->thetarr || !g->costarr || !g->tan2arr || !g->phiarr || !g->aarr || !g->barr ||
+      !g->densarr || !g->massarr || !g->tdust)
+    return fail(c, HC3D_ERR_INVALID, "a grid pointer is NULL");
+  CK(cudaSetDevice(c->device));
+  const int nrg = g->nrg, ntg = g->ntg, npg = g->npg;
+  const int64_t n4 = (int64_t)nrg * ntg * npg;
+  const int64_t ncell = (int64_t)(nrg - 1) * (ntg - 1) * (npg - 1);
+  // species slots beyond the device's four must be empty
+  for (int s = kSlots; s < g->ndg; ++s)
+    for (int64_t k = 0; k < n4; ++k)
+      if (g->densarr[k + n4 * s] != 0.0)
+        return fail(c, HC3D_ERR_UNSUPPORTED, "species slots 5-8 (small grains) are not supported");
+  for (int64_t k = 0; k < n4 * g->ndg; ++k)
+    if (!(g->densarr[k] >= 0.0) || std::isinf(g->densarr[k]))
+      return fail(c, HC3D_ERR_INVALID, "densarr holds a negative, NaN or infinite value");
+  for (int i = 1; i < nrg; ++i)
+    if (!(g->rarr[i] > g->rarr[i - 1])) return fail(c, HC3D_ERR_INVALID, "rarr must increase");
+  free_all(c->grid_allocs);
+  c->grid = false;
+  std::vector<float> tan2f(ntg), hemi(ntg), af(npg), bf(npg);
+  for (int i = 0; i < ntg; ++i) {
+    tan2f[i] = (float)g->tan2arr[i];
+    hemi[i] = g->costarr[i] > 0.0 ? 1.0f : -1.0f;
+  }
+  for (int i = 0; i < npg; ++i) {
+    af[i] = (float)g->aarr[i];
+    bf[i] = (float)g->barr[i];
+  }
+  const int ns = std::min(g->ndg, kSlots);
+  std::vector<float4> rf(ncell);
+  std::vector<double> rd(4 * ncell, 0.0), td(4 * ncell, 0.1 / 11605.0), ma(4 * ncell, 0.0);
+  for (int ip = 1; ip < npg; ++ip)
+    for (int it = 1; it < ntg; ++it)
+      for (int ir = 1; ir < nrg; ++ir) {
+        const int64_t c4 = (int64_t)(ir - 1) + (int64_t)nrg * ((it - 1) + (int64_t)ntg * (ip - 1));
+        const int64_t cc = (int64_t)(ir - 1) + (int64_t)(nrg - 1) * ((it - 1) + (int64_t)(ntg - 1) * (ip - 1));
+        float v[4] = {0, 0, 0, 0};
+        for (int s = 0; s < ns; ++s) {
+          const double d = g->densarr[c4 + n4 * s];
+          v[s] = (float)d;
+          rd[4 * cc + s] = d;
+          td[4 * cc + s] = g->tdust[c4 + n4 * s];
+          ma[4 * cc + s] = g->massarr[c4 + n4 * s];
+        }
+        rf[cc] = make_float4(v[0], v[1], v[2], v[3]);
+      }
+  std::vector<void*>& own = c->grid_allocs;
+  int r;
+  double *d_r, *d_r2, *d_th, *d_ph, *d_t2, *d_a, *d_b, *d_rd;
+  float *d_t2f, *d_hemi, *d_af, *d_bf;
+  float4* d_rf;
+  if ((r = dupload(c, own, &d_r, g->rarr, (size_t)nrg)) || (r = dupload(c, own, &d_r2, g->r2arr, (size_t)nrg)) ||
+      (r = dupload(c, own, &d_th, g->thetarr, (size_t)ntg)) || (r = dupload(c, own, &d_ph, g->phiarr, (size_t)npg)) ||
+      (r = dupload(c, own, &d_t2, g->tan2arr, (size_t)ntg)) || (r = dupload(c, own, &d_a, g->aarr, (size_t)npg)) ||
+      (r = dupload(c, own, &d_b, g->barr, (size_t)npg)) || (r = dupload(c, own, &d_t2f, tan2f.data(), tan2f.size())) ||
+      (r = dupload(c, own, &d_hemi, hemi.data(), hemi.size())) || (r = dupload(c, own, &d_af, af.data(), af.size())) ||
+      (r = dupload(c, own, &d_bf, bf.data(), bf.size())) || (r = dupload(c, own, &d_rf, rf.data(), rf.size())) ||
+      (r = dupload(c, own, &d_rd, rd.data(), rd.size())) || (r = dupload(c, own, &c->d_tdust, td.data(), td.size())) ||
+      (r = dupload(c, own, &c->d_massarr, ma.data(), ma.size())) || (r = dalloc(c, own, &c->d_peelmask, (size_t)ncell)))
+    return r;
+  DevTallies& t = c->dt;
+  if ((r = dalloc(c, own, &t.nabs, (size_t)kSlots * ncell)) || (r = dalloc(c, own, &t.dtauabs, (size_t)kSlots * ncell)) ||
+      (r = dalloc(c, own, &t.jmean, (size_t)ncell)) || (r = dalloc(c, own, &t.killed, (size_t)ncell)) ||
+      (r = dalloc(c, own, &t.dbig, (size_t)ncell)))
+    return r;
+  DevModel& m = c->dm;
+  m.nrg = nrg; m.ntg = ntg; m.npg = npg; m.ncell = ncell;
+  m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
+  m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
+  m.peelmask = c->d_peelmask; m.tdust = c->d_tdust;
+  c->ndg_in = g->ndg;
+  k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  c->grid = true;
+  return hc3d_zero_tallies(c);
+}
+
+extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
+  if (!c) return HC3D_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  if (c->grid) {
+    const int64_t n = c->dm.ncell;
+    CK(cudaMemsetAsync(c->dt.nabs, 0, sizeof(unsigned long long) * kSlots * n, c->stream));
+    CK(cudaMemsetAsync(c->dt.dtauabs, 0, sizeof(unsigned long long) * kSlots * n, c->stream));
+    CK(cudaMemsetAsync(c->dt.jmean, 0, sizeof(unsigned long long) * n, c->stream));
+    CK(cudaMemsetAsync(c->dt.killed, 0, sizeof(unsigned int) * n, c->stream));
+    CK(cudaMemsetAsync(c->dt.dbig, 0, sizeof(unsigned int) * n, c->stream));
+  }
+  if (c->run_tallies) {
+    CK(cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * c->dims.nsed, c->stream));
+    CK(cudaMemsetAsync(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(c->dims.npsed, 1), c->stream));
+    CK(cudaMemsetAsync(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(c->dims.nimg, 1), c->stream));
+  }
+  CK(cudaMemsetAsync(c->dt.counters, 0, sizeof(unsigned long long) * 16, c->stream));
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->scales_set = false;
+  c->epoch_np = 0;
+  c->status_seen = 0;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
+  if (!c) return HC3D_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  RunArgs a;
+  int r = prepare_run(c, p, &a);
+  if (r) return r;
+  if (p->np == 0) return HC3D_OK;
+  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), c->stream));
+  LaunchCfg cfg;
+  cfg.threads = c->block_size;
+  cfg.stream = c->stream;
+  if (c->grid_blocks > 0) {
+    cfg.blocks = c->grid_blocks;
+  } else {
+    int per_sm = 0;
+    cudaError_t e;
+    if (c->precision == HC3D_PREC_FP64) {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_fp64(), cfg.threads, 0);
+    } else {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_mixed(), cfg.threads, 0);
+    }
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    cfg.blocks = c->sm_count * per_sm;
+    const int64_t need = (p->np + cfg.threads - 1) / cfg.threads;
+    if (need < cfg.blocks) cfg.blocks = (int)std::max<int64_t>(1, need);
+  }
+  CK(cudaEventRecord(c->ev0, c->stream));
+  cudaError_t e = c->precision == HC3D_PREC_FP64 ? launch_transport_fp64(c->dm, c->dt, c->dims, a, cfg)
+                                                 : launch_transport_mixed(c->dm, c->dt, c->dims, a, cfg);
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("transport launch: ") + cudaGetErrorString(e));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  if ((r = finish_run(c))) return r;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last_ms = ms;
+  c->epoch_np += p->np;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tallies* out) {
+  if (!c || !out) return HC3D_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (!c->grid) return fail(c, HC3D_ERR_STATE, "no grid loaded");
+  if (p && c->run_tallies && !same_dims(dims_of(p), c->dims))
+    return fail(c, HC3D_ERR_INVALID, "params do not match the tally shape of the runs");
+  out->stokes_scale = c->dt.stokes_scale;
+  out->square_scale = c->dt.square_scale;
+  out->path_scale = c->dt.path_scale;
+  if (c->run_tallies) {
+    int64_t* sed[9] = {out->si, out->sq, out->su, out->sv, out->si2, out->sq2, out->su2, out->sv2, out->nums};
+    for (int k = 0; k < 9; ++k)
+      if (sed[k]) CK(cudaMemcpy(sed[k], c->dt.sed + k * c->dims.nsed, sizeof(int64_t) * c->dims.nsed, cudaMemcpyDeviceToHost));
+    int64_t* ps[9] = {out->ti, out->tq, out->tu, out->tv, out->ti2, out->tq2, out->tu2, out->tv2, out->numt};
+    if (c->dims.npsed > 0)
+      for (int k = 0; k < 9; ++k)
+        if (ps[k]) CK(cudaMemcpy(ps[k], c->dt.psed + k * c->dims.npsed, sizeof(int64_t) * c->dims.npsed, cudaMemcpyDeviceToHost));
+    int64_t* im[4] = {out->image_i, out->image_q, out->image_u, out->image_v};
+    if (c->dims.nimg > 0)
+      for (int k = 0; k < 4; ++k)
+        if (im[k]) CK(cudaMemcpy(im[k], c->dt.img + k * c->dims.nimg, sizeof(int64_t) * c->dims.nimg, cudaMemcpyDeviceToHost));
+  }
+  const DevModel& m = c->dm;
+  const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
+  const int ndg = c->ndg_in;
+  auto scatter = [&](const std::vector<unsigned long long>& src, int slots, int64_t* dst) {
+    std::fill(dst, dst + n4 * slots, 0);
+    for (int s = 0; s < std::min(slots, kSlots); ++s)
+      for (int ip = 1; ip < m.npg; ++ip)
+        for (int it = 1; it < m.ntg; ++it)
+          for (int ir = 1; ir < m.nrg; ++ir) {
+            const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+            const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+            dst[c4 + n4 * s] = (int64_t)src[(size_t)s * n + cc];
+          }
+  };
+  std::vector<unsigned long long> buf;
+  if (out->nabs) {
+    buf.resize((size_t)kSlots * n);
+    CK(cudaMemcpy(buf.data(), c->dt.nabs, sizeof(unsigned long long) * buf.size(), cudaMemcpyDeviceToHost));
+    scatter(buf, ndg, out->nabs);
+  }
+  if (out->dtauabs) {
+    buf.resize((size_t)kSlots * n);
+    CK(cudaMemcpy(buf.data(), c->dt.dtauabs, sizeof(unsigned long long) * buf.size(), cudaMemcpyDeviceToHost));
+    scatter(buf, ndg, out->dtauabs);
+  }
+  if (out->jmean) {
+    buf.resize((size_t)n);
+    CK(cudaMemcpy(buf.data(), c->dt.jmean, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    scatter(buf, 1, out->jmean);
+  }
+  auto scatter32 = [&](const unsigned int* dsrc, int32_t* dst) -> int {
+    std::vector<unsigned int> b32((size_t)n);
+    CK(cudaMemcpy(b32.data(), dsrc, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost));
+    std::fill(dst, dst + n4, 0);
+    for (int ip = 1; ip < m.npg; ++ip)
+      for (int it = 1; it < m.ntg; ++it)
+        for (int ir = 1; ir < m.nrg; ++ir) {
+          const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+          const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+          dst[c4] = (int32_t)b32[cc];
+        }
+    return HC3D_OK;
+  };
+  int r;
+  if (out->killed && (r = scatter32(c->dt.killed, out->killed))) return r;
+  if (out->dbig && (r = scatter32(c->dt.dbig, out->dbig))) return r;
+  unsigned long long cnt[16];
+  CK(cudaMemcpy(cnt, c->dt.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 16; ++k) out->counters[k] = (int64_t)cnt[k];
+  out->counters[HC3D_CNT_STATUS] = c->status_seen;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* tdust_out, double* max_rel_change,
+                                int* converged) {
+  if (!c) return HC3D_ERR_INVALID;
+  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
+  if (!(ltot > 0.0) || np <= 0) return fail(c, HC3D_ERR_INVALID, "need ltot > 0 and np > 0");
+  if (!c->scales_set) return fail(c, HC3D_ERR_STATE, "no packets were run since the last hc3d_zero_tallies()");
+  CK(cudaSetDevice(c->device));
+  LucyArgs a;
+  a.ncell = c->dm.ncell;
+  a.nT = c->dm.nT;
+  a.lTint = c->dm.lTint;
+  a.kappap = c->d_kappap;
+  for (int s = 0; s < kSlots; ++s) a.kappav[s] = c->kappav[s];
+  a.ltot = ltot;
+  a.nphot = (double)np;
+  a.path_scale = c->dt.path_scale;
+  a.tsub = c->tsub;
+  a.na_min = 1.0e4;
+  a.nslots = std::min(c->ndg_in, kSlots);
+  CK(cudaMemsetAsync(c->d_maxrel, 0, sizeof(unsigned long long), c->stream));
+  k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust,
+                                                           c->d_peelmask, c->d_maxrel);
+  CK(cudaGetLastError());
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, c->d_maxrel, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double rel;
+  std::memcpy(&rel, &bits, sizeof(rel));
+  if (max_rel_change) *max_rel_change = rel;
+  if (converged) *converged = rel < 0.01 ? 1 : 0;
+  if (tdust_out) {
+    const DevModel& m = c->dm;
+    const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
+    std::vector<double> td((size_t)4 * n);
+    CK(cudaMemcpy(td.data(), c->d_tdust, sizeof(double) * td.size(), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < std::min(c->ndg_in, kSlots); ++s)
+      for (int ip = 1; ip < m.npg; ++ip)
+        for (int it = 1; it < m.ntg; ++it)
+          for (int ir = 1; ir < m.nrg; ++ir) {
+            const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+            const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+            tdust_out[c4 + n4 * s] = td[4 * cc + s];
+          }
+  }
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_trace_packets(hc3d_ctx* c, const hc3d_run_params* p, int npkt, const double* uniforms, int nu,
+                                  hc3d_trace_rec* recs, int max_rec, int32_t* nrec) {
+  if (!c || !uniforms || !recs || !nrec || npkt < 1 || nu < 1 || max_rec < 1) return HC3D_ERR_INVALID;
+  if ((int64_t)npkt * nu > (int64_t)1 << 28 || (int64_t)npkt * max_rec > (int64_t)1 << 26)
+    return fail(c, HC3D_ERR_INVALID, "trace request too large");
+  CK(cudaSetDevice(c->device));
+  hc3d_run_params q = *p;
+  q.np = npkt;
+  RunArgs a;
+  int r = prepare_run(c, &q, &a);
+  if (r) return r;
+  std::vector<void*> tmp;
+  double* d_u;
+  hc3d_trace_rec* d_rec;
+  int* d_n;
+  if ((r = dupload(c, tmp, &d_u, uniforms, (size_t)npkt * nu)) || (r = dalloc(c, tmp, &d_rec, (size_t)npkt * max_rec)) ||
+      (r = dalloc(c, tmp, &d_n, (size_t)npkt))) {
+    free_all(tmp);
+    return r;
+  }
+  a.inj = d_u;
+  a.ninj = nu;
+  a.trace = d_rec;
+  a.max_rec = max_rec;
+  a.nrec = d_n;
+  LaunchCfg cfg;
+  cfg.threads = 128;
+  cfg.blocks = (npkt + 127) / 128;
+  cfg.stream = c->stream;
+  cudaError_t e = c->precision == HC3D_PREC_FP64 ? launch_transport_fp64(c->dm, c->dt, c->dims, a, cfg)
+                                                 : launch_transport_mixed(c->dm, c->dt, c->dims, a, cfg);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(recs, d_rec, sizeof(hc3d_trace_rec) * (size_t)npkt * max_rec, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(nrec, d_n, sizeof(int32_t) * npkt, cudaMemcpyDeviceToHost);
+  free_all(tmp);
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("trace: ") + cudaGetErrorString(e));
+  c->epoch_np += npkt;
+  return HC3D_OK;
+}

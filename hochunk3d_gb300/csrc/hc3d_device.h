@@ -1,0 +1,103 @@
+// hc3d_device.h -- device-side data layout shared by the transport kernels
+// and the C-ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/hc3d.h"
+
+namespace hc3d {
+
+constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2, envelope, cavity)
+constexpr int kNo = 8;      // SED components (output.F90:232-239)
+constexpr int kMaxPeel = 256;
+
+// Fortran-layout sizes of the tally arrays of one run configuration.
+struct TallyDims {
+  int nfreq, nmu, nph, nap, npeel, nx;
+  int64_t nsed;    // nfreq*nmu*nph*nap*no
+  int64_t npsed;   // nfreq*npeel*nap*no
+  int64_t nimg;    // npeel*nx*nx
+};
+
+// Device tallies (int64 fixed point).  Grid tallies use the compact cell
+// index c = (ir-1) + (nrg-1)*((it-1) + (ntg-1)*(ip-1)).
+struct DevTallies {
+  unsigned long long* sed;    // [9][nsed]: si sq su sv si2 sq2 su2 sv2 nums
+  unsigned long long* psed;   // [9][npsed]: ti .. numt
+  unsigned long long* img;    // [4][nimg]: I Q U V
+  unsigned long long* nabs;   // [kSlots][ncell]
+  unsigned long long* dtauabs;// [kSlots][ncell]
+  unsigned long long* jmean;  // [ncell]
+  unsigned int* killed;       // [ncell]
+  unsigned int* dbig;         // [ncell]
+  unsigned long long* counters; // [16]
+  double stokes_scale, square_scale, path_scale;
+};
+
+// Read-only model data on the device.
+struct DevModel {
+  // grid
+  int nrg, ntg, npg;
+  int64_t ncell;
+  const double* rarr;     // (nrg)
+  const double* r2arr;    // (nrg)
+  const double* thetarr;  // (ntg)
+  const double* phiarr;   // (npg)
+  const double* tan2d;    // (ntg)
+  const float* tan2f;     // (ntg)
+  const float* hemi;      // (ntg) +1 upper, -1 lower (cone nappe)
+  const double* aarrd; const double* barrd;  // (npg)
+  const float* aarrf; const float* barrf;    // (npg)
+  const float4* rho4f;    // (ncell) species slots x,y,z,w  (mixed form)
+  const double* rho4d;    // (ncell*4)                     (FP64 form)
+  const unsigned char* peelmask;  // (ncell) bit s: tdust(s) < Tsub
+  const double* tdust;    // (ncell*4) K/11605
+  // dust tables
+  int nlammax;
+  int nlambda[kSlots];
+  const double* nudust; const double* kappad; const double* adust; const double* gdust; const double* pldust;
+  double kappav[kSlots];
+  int nT, nnu;
+  const double* lTint; const double* nuint; const double* kapBint;  // kapBint (nT,nnu,kSlots)
+  int nhnu;
+  const double* hnuint; const double* atmosnu; const double* lognu; const double* loghnu;
+};
+
+// One call of the packet loop.
+struct RunArgs {
+  int64_t np, packet_offset;
+  uint32_t key0, key1;
+  int ipeel, npeel, image;
+  int nfreq, nmu, nph, nap, nx;
+  double rmaxi, fractxh;
+  double numin, lnurat;
+  double rstar_cm;
+  int iintmax;
+  int64_t max_interactions;
+  const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
+  const double* aperture2;   // [nap]
+  unsigned long long* work;  // packet counter
+  int* status;               // first fault code
+  // trace harness
+  const double* inj; int ninj;
+  void* trace; int max_rec; int* nrec;
+};
+
+struct LaunchCfg {
+  int blocks, threads;
+  cudaStream_t stream;
+};
+
+// entry points of the two instantiations
+cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                   const LaunchCfg& cfg);
+cudaError_t launch_transport_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                  const LaunchCfg& cfg);
+int transport_regs_mixed();
+int transport_regs_fp64();
+const void* transport_fn_mixed();
+const void* transport_fn_fp64();
+
+}  // namespace hc3d

@@ -1,0 +1,1074 @@
+// hc3d_model.cpp -- the Fortran host's setup work, restated in C++:
+// reapar/setup (input and units), dustinit/setemiss (opacity and Planck
+// tables), atmosinit (stellar spectrum CDF), setup_wave (disk rho0) and
+// gridset (walls, cell volumes, densities).  Each function cites the
+// reference lines it follows.
+#include "hc3d_model.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <thread>
+
+namespace hc3d {
+
+// ---------------------------------------------------------------------------
+// configuration.f90:28-56 -- value = NAME = comment; the value is the text
+// before the first '=', the name the trimmed text between the first two.
+// ---------------------------------------------------------------------------
+static std::string trim(const std::string& s) {
+  size_t b = s.find_first_not_of(" \t\r\n");
+  if (b == std::string::npos) return "";
+  size_t e = s.find_last_not_of(" \t\r\n");
+  return s.substr(b, e - b + 1);
+}
+
+bool ParFile::load(const std::string& path, std::string* err) {
+  std::ifstream f(path);
+  if (!f) {
+    *err = "cannot open parameter file " + path;
+    return false;
+  }
+  std::string line;
+  while (std::getline(f, line)) {
+    size_t p1 = line.find('=');
+    if (p1 == std::string::npos) continue;
+    size_t p2 = line.find('=', p1 + 1);
+    if (p2 == std::string::npos) continue;
+    std::string value = trim(line.substr(0, p1));
+    std::string name = trim(line.substr(p1 + 1, p2 - p1 - 1));
+    kv_[name] = value;  // later duplicates win, like the Fortran key() scan order
+  }
+  return true;
+}
+
+// Fortran list-directed read of the first item: quotes stripped, stops at
+// blank or comma.
+static std::string first_item(const std::string& v) {
+  std::string s = trim(v);
+  if (!s.empty() && (s[0] == '\'' || s[0] == '"')) {
+    char q = s[0];
+    size_t e = s.find(q, 1);
+    return e == std::string::npos ? s.substr(1) : s.substr(1, e - 1);
+  }
+  size_t e = s.find_first_of(" \t,");
+  return e == std::string::npos ? s : s.substr(0, e);
+}
+
+static bool parse_real(const std::string& tok, double* out) {
+  std::string t = tok;
+  for (auto& ch : t)
+    if (ch == 'd' || ch == 'D') ch = 'e';
+  char* end = nullptr;
+  errno = 0;
+  double v = std::strtod(t.c_str(), &end);
+  if (end == t.c_str() || errno != 0) return false;
+  *out = v;
+  return true;
+}
+
+bool ParFile::str(const std::string& key, std::string* out, std::string* err) const {
+  auto it = kv_.find(key);
+  if (it == kv_.end()) {
+    *err = "ERROR: parameter " + key + " not found";
+    return false;
+  }
+  *out = first_item(it->second);
+  return true;
+}
+
+bool ParFile::real(const std::string& key, double* out, std::string* err) const {
+  std::string s;
+  if (!str(key, &s, err)) return false;
+  if (!parse_real(s, out)) {
+    *err = "Parameter " + key + " is not a real";
+    return false;
+  }
+  return true;
+}
+
+bool ParFile::integer(const std::string& key, int64_t* out, std::string* err) const {
+  std::string s;
+  if (!str(key, &s, err)) return false;
+  if (s == "YES") { *out = 1; return true; }
+  if (s == "NO") { *out = 0; return true; }
+  double v;
+  if (!parse_real(s, &v)) {
+    *err = "Parameter " + key + " is not an integer";
+    return false;
+  }
+  *out = (int64_t)v;
+  return true;
+}
+
+bool ParFile::reals(const std::string& key, std::vector<double>* out, std::string* err) const {
+  auto it = kv_.find(key);
+  if (it == kv_.end()) {
+    *err = "ERROR: parameter " + key + " not found";
+    return false;
+  }
+  out->clear();
+  std::string s = it->second;
+  for (auto& ch : s)
+    if (ch == ',') ch = ' ';
+  std::istringstream is(s);
+  std::string tok;
+  while (is >> tok) {
+    double v;
+    if (!parse_real(tok, &v)) {
+      *err = "Parameter " + key + " is not a list of reals";
+      return false;
+    }
+    out->push_back(v);
+  }
+  return true;
+}
+
+bool ParFile::ints(const std::string& key, std::vector<int64_t>* out, std::string* err) const {
+  std::vector<double> v;
+  if (!reals(key, &v, err)) return false;
+  out->clear();
+  for (double x : v) out->push_back((int64_t)x);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// mathsubs.f90: expm1 (Abramowitz & Stegun 4.2.45 polynomial) and the
+// normalised Planck function Bnu.
+// ---------------------------------------------------------------------------
+static double expm1_as(double x) {
+  static const double coef[7] = {0.9999999995, 0.4999999206, 0.1666653019, 0.0416573475,
+                                 0.0083013598, 0.0013298820, 0.0001413161};
+  if (std::fabs(x) > 0.6931472) return std::exp(x) - 1.0;
+  double sum = 0.0;
+  for (int i = 6; i >= 0; --i) sum = x * (coef[i] + sum);
+  return sum;
+}
+
+static double Bnu(double nu, double T) {
+  const double norm = 0.1539897;  // 15/pi^4
+  double x = nu / T;
+  if (x == 0.0) return 0.0;
+  return norm * x * x * x / expm1_as(x);
+}
+
+// ---------------------------------------------------------------------------
+// opacset for one species (dust.f90:9-80), host copy used by setemiss.
+// ---------------------------------------------------------------------------
+static void opacset1(const Model& m, int id, double nu, double* kappa, double* albedo) {
+  const int nl = m.nlambda[id];
+  const double* nud = &m.nudust[(size_t)id * m.nlammax];
+  const double* kap = &m.kappad[(size_t)id * m.nlammax];
+  const double* alb = &m.adust[(size_t)id * m.nlammax];
+  if (nu >= nud[0]) {
+    *kappa = kap[0];
+    *albedo = alb[0];
+  } else if (nu <= nud[nl - 1]) {
+    *kappa = kap[nl - 1];
+    *albedo = alb[nl - 1];
+  } else {
+    int i0 = 1, i1 = nl;
+    while (i1 - i0 > 1) {
+      int i = (i1 + i0) / 2;
+      if (nu <= nud[i - 1]) i0 = i; else i1 = i;
+    }
+    double f = (nu - nud[i1 - 1]) / (nud[i0 - 1] - nud[i1 - 1]);
+    double fm1 = 1.0 - f;
+    *kappa = fm1 * kap[i1 - 1] + f * kap[i0 - 1];
+    *albedo = fm1 * alb[i1 - 1] + f * alb[i0 - 1];
+  }
+}
+
+// nr.f qsimp/trapzd (nr.f:183-225); returns the last estimate instead of
+// stopping when JMAX is reached.
+template <class F>
+static double qsimp(F func, double a, double b) {
+  const double EPS = 1.e-5;
+  const int JMAX = 20;
+  double ost = -1.e30, os = -1.e30, st = 0.0, s = 0.0;
+  for (int j = 1; j <= JMAX; ++j) {
+    if (j == 1) {
+      st = 0.5 * (b - a) * (func(a) + func(b));
+    } else {
+      int it = 1 << (j - 2);
+      double tnm = (double)it, del = (b - a) / tnm, x = a + 0.5 * del, sum = 0.0;
+      for (int k = 0; k < it; ++k) {
+        sum += func(x);
+        x += del;
+      }
+      st = 0.5 * (st + (b - a) * sum / tnm);
+    }
+    s = (4.0 * st - ost) / 3.0;
+    if (std::fabs(s - os) < EPS * std::fabs(os)) return s;
+    os = s;
+    ost = st;
+  }
+  return s;
+}
+
+// setemiss, dust.f90:394-474: cumulative kappa*B_nu integrals over the
+// nuint grid (scaled by T) for every temperature; kapBint normalised to 1 at
+// nnu and kappap = the unnormalised total (Planck-mean kappa / kappa_V).
+void setemiss_species(const Model& m, int id, double* kapB, double* kapp) {
+  const int nT = m.nT, nnu = m.nnu;
+  auto rows = [&](int i_begin, int i_end) {
+    for (int i = i_begin; i < i_end; ++i) {
+      const double Teff = std::exp(m.lTint[i]);
+      double nu1 = 0.0, kappa, albedo;
+      opacset1(m, id, nu1, &kappa, &albedo);
+      double kappa1 = (1.0 - albedo) * kappa;
+      double acc = 0.0;
+      for (int j = 0; j < nnu; ++j) {
+        double nu0 = nu1;
+        nu1 = m.nuint[j] * Teff;
+        double dnu = nu1 - nu0;
+        double dx = dnu / Teff;
+        double kappa0 = kappa1;
+        opacset1(m, id, nu1, &kappa, &albedo);
+        kappa1 = (1.0 - albedo) * kappa;
+        double v = 0.0;
+        if (nu0 / Teff < 50.0) {
+          v = qsimp([&](double f) { return ((1.0 - f) * kappa0 + f * kappa1) * Bnu(nu0 + f * dnu, Teff); }, 0.0,
+                    1.0);
+        }
+        acc = (j == 0) ? dx * v : dx * v + acc;
+        kapB[(size_t)i + (size_t)nT * j] = acc;
+      }
+      kapp[i] = kapB[(size_t)i + (size_t)nT * (nnu - 1)];
+      for (int j = 0; j < nnu - 1; ++j) kapB[(size_t)i + (size_t)nT * j] /= kapp[i];
+      kapB[(size_t)i + (size_t)nT * (nnu - 1)] = 1.0;
+    }
+  };
+  unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (unsigned k = 0; k < nth; ++k) th.emplace_back(rows, (int)(nT * k / nth), (int)(nT * (k + 1) / nth));
+  for (auto& t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// dustinit, dust.f90:314-391: 7-column file lam(um) cext csca kap g pmax thet
+// ---------------------------------------------------------------------------
+static bool read_dust(Model* m, int id, const std::string& path, std::string* err) {
+  std::ifstream f(path);
+  if (!f) {
+    *err = "cannot open dust file " + path;
+    return false;
+  }
+  int i = 0, iv = 0;
+  std::string line;
+  const size_t o = (size_t)id * m->nlammax;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    double lam, cext, csca, kap, hgg, pmax, thet;
+    if (!(is >> lam >> cext >> csca >> kap >> hgg >> pmax >> thet)) {
+      if (trim(line).empty()) continue;
+      break;
+    }
+    if (i >= m->nlammax) {
+      *err = "error, too many wavelengths in dust opacity file";
+      return false;
+    }
+    if (lam <= 0.55) iv = i + 1;
+    m->lamdust[o + i] = 10000.0 * lam;
+    m->nudust[o + i] = 12398.0 / m->lamdust[o + i];
+    m->kappad[o + i] = kap;
+    m->adust[o + i] = csca / cext;
+    m->gdust[o + i] = hgg;
+    m->pldust[o + i] = pmax;
+    if (i == 0) m->kappad[o + i] = 0.00001 * m->kappad[o + i];
+    ++i;
+  }
+  if (i < 2 || iv < 1 || iv >= i) {
+    *err = "dust file " + path + " has too few rows or no row at 0.55um";
+    return false;
+  }
+  m->nlambda[id] = i;
+  double f5 = (5500.0 - m->lamdust[o + iv - 1]) / (m->lamdust[o + iv] - m->lamdust[o + iv - 1]);
+  m->kappav[id] = (1.0 - f5) * m->kappad[o + iv - 1] + f5 * m->kappad[o + iv];
+  for (int k = 0; k < i; ++k) m->kappad[o + k] /= m->kappav[id];
+  return true;
+}
+
+// atmosinit, starbarb.f90:3-110 (the parts the photon loop reads).
+static bool atmosinit(Model* m, const std::string& path, std::string* err) {
+  std::ifstream f(path);
+  if (!f) {
+    *err = "cannot open atmosphere file " + path;
+    return false;
+  }
+  std::string line;
+  std::getline(f, line);  // header
+  std::vector<double> w, fl;
+  while (std::getline(f, line)) {
+    std::istringstream is(line);
+    double wtmp, ftmp;
+    if (!(is >> wtmp >> ftmp)) break;
+    if (m->iplanckst == 1) ftmp = Bnu(1.2398 / wtmp, m->tstar_k / 11605.0);
+    w.push_back(wtmp);
+    fl.push_back(ftmp);
+  }
+  const int nh = (int)w.size();
+  if (nh < 3) {
+    *err = "atmosphere file has fewer than 3 samples";
+    return false;
+  }
+  std::vector<double> winv(nh), ff(nh);
+  for (int i = 0; i < nh; ++i) {
+    winv[nh - 1 - i] = 1.0 / w[i];
+    ff[nh - 1 - i] = fl[i];
+  }
+  m->hnuint.assign(nh, 0.0);
+  m->atmosnu.assign(nh, 0.0);
+  m->lognu.assign(nh, 0.0);
+  m->loghnu.assign(nh, 0.0);
+  for (int i = 0; i < nh; ++i) {
+    m->atmosnu[i] = 1.2398 * winv[i];
+    m->lognu[i] = std::log10(m->atmosnu[i]);
+    m->hnuint[i] = i == 0 ? 0.0 : m->hnuint[i - 1] + 0.5 * (ff[i] + ff[i - 1]) * (winv[i] - winv[i - 1]);
+  }
+  double fbol = m->hnuint[nh - 1];
+  if (fbol == 0.0) {
+    *err = "error, atmosphere file is all zeros";
+    return false;
+  }
+  for (int i = 0; i < nh; ++i) {
+    m->hnuint[i] /= fbol;
+    if (i > 0) m->loghnu[i] = std::log10(m->hnuint[i]);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// zerod (module not shipped): root mu0 in [mu,1] of the Ulrich streamline
+// equation mu0^3 + (r/Rc - 1) mu0 - (r/Rc) mu = 0 (Ulrich 1976), by the
+// closed form of the depressed cubic, polished by Newton steps.
+// ---------------------------------------------------------------------------
+double zerod(double mu, double rx) {
+  const double p = rx - 1.0, q = -rx * mu;
+  double x;
+  double disc = 0.25 * q * q + p * p * p / 27.0;
+  if (disc > 0.0) {
+    double sd = std::sqrt(disc);
+    x = std::cbrt(-0.5 * q + sd) + std::cbrt(-0.5 * q - sd);
+  } else if (p < 0.0) {
+    double r = std::sqrt(-p / 3.0);
+    double arg = std::max(-1.0, std::min(1.0, (3.0 * q) / (2.0 * p) * std::sqrt(-3.0 / p)));
+    x = 2.0 * r * std::cos(std::acos(arg) / 3.0);  // the largest real root
+  } else {
+    x = 0.0;
+  }
+  for (int k = 0; k < 3; ++k) {
+    double fx = x * x * x + p * x + q, d = 3.0 * x * x + p;
+    if (d != 0.0) x -= fx / d;
+  }
+  return std::max(0.0, std::min(1.0, x));
+}
+
+// densdisk, densdiskg.f90:1-155 for an unwarped, ungapped, unspiralled disk.
+double densdisk(const Model& m, double rad, double sint, double cost, int id) {
+  const double rp = rad * sint, zp = rad * cost;
+  const double rcoord = m.idiskcurve == 1 ? rad : rp;
+  const double rmin = 1.0;
+  double zmr = m.z1[id] * std::pow(rcoord / rmin, m.b[id]);
+  if (rcoord > m.rmaxd[id] || m.rho0[id] == 0.0 || rcoord < m.rddust[id] || zmr < 1.e-10) return 0.0;
+  double gexp = (zp / zmr) * (zp / zmr);
+  if (gexp > 1.e-15) {
+    if (gexp < 120.0) return m.rho0[id] * std::pow(rcoord / rmin, -m.a[id]) * std::exp(-0.5 * gexp);
+    return 0.0;
+  }
+  return m.rho0[id] * std::pow(rcoord / rmin, -m.a[id]);
+}
+
+// densenv, densenv.f90:1-128: Ulrich envelope (or power law) with a
+// polynomial bipolar cavity; species id is the envelope (slot 3) or cavity
+// (slot 4).
+double densenv(const Model& m, double rad, double thetin, double costin, double sina, int id) {
+  const bool is_env = (id == 2 || id == 6), is_cav = (id == 3 || id == 7);
+  int inhole = 0;
+  double thet = thetin;
+  double cosa = std::fabs(costin);
+  if (thet > kPiHalf) thet = kPi - thet;
+  (void)thet;
+  const double rp = rad * sina, zp = rad * cosa;
+  const double zup = m.c1e * std::pow(rp, m.ex1) + m.z01;
+  const double xmu = zp / rad;
+  double dens;
+  if (rad > m.rmine) {
+    if (m.ienvtype == 1) {
+      double rx = rad / m.rc;
+      double xmu0 = zerod(xmu, rx);
+      double ratio = xmu0 > 0.0 ? xmu / xmu0 : 1.0;
+      double factor = 1.0 / (ratio + 2.0 * (xmu0 * xmu0) / rx);
+      dens = m.rhoe0 * std::pow(rx, -1.5) * factor / std::sqrt(1.0 + ratio);
+    } else {
+      dens = m.rhodens1 * std::pow(rad, -m.envexp);  // densenvpw.f90
+    }
+  } else {
+    dens = 0.0;
+  }
+  if (rad > m.rmine && dens < m.rhoamb) dens = m.rhoamb;
+  if (m.ihole == 1 && m.ipoly == 1) {
+    double zlo = m.c2e * std::pow(rp, m.ex2) + m.z02;
+    if (zp > zlo) {
+      inhole = 1;
+      dens = m.rhoconst2 * std::pow(rad, -m.exf);
+    }
+    if (zp > zup) {
+      inhole = 1;
+      dens = m.rhoconst1 * std::pow(rad, -m.exf);
+    }
+  }
+  if (rad >= m.rmax) dens = 0.0;
+  if (rad <= m.rmine) dens = 0.0;
+  if (is_cav && inhole == 0) dens = 0.0;
+  if (is_env && inhole == 1) dens = 0.0;
+  return dens;
+}
+
+// ---------------------------------------------------------------------------
+// The project fractal generator (CFRACTAL=YES; the reference's fractal_sph is
+// not reproduced): fractlev levels of hierarchical clumps, fractn level-1
+// centres in cell-index space and fractn/8+1 children per parent, each level
+// closer to its parent.  Clump cells get density factor a, the rest b, with
+// a/b = fractcontrast, the cell average of the factor 1 (the normalisation of
+// gridset.f90:842-851) and a share densratio of the mass in clumps; the clump
+// radius is set by bisection to the volume fraction these imply.
+// ---------------------------------------------------------------------------
+static uint64_t splitmix(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double u01(uint64_t* s) { return ((double)(splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+static void fractal_field(Model* m) {
+  const int nr = m->nrg - 1, nt = m->ntg - 1, np = m->npg - 1;
+  const int64_t nc = (int64_t)nr * nt * np;
+  uint64_t s = (uint64_t)m->ifseed * 0x2545F4914F6CDD1Dull + 12345;
+  struct C { double r, t, p; };
+  std::vector<C> cur;
+  for (int k = 0; k < m->fractn; ++k) cur.push_back({u01(&s) * nr, u01(&s) * nt, u01(&s) * np});
+  double spread = 0.25;
+  for (int lev = 2; lev <= m->fractlev; ++lev) {
+    std::vector<C> nxt;
+    for (const C& c : cur)
+      for (int k = 0; k < m->fractn / 8 + 1; ++k)
+        nxt.push_back({c.r + (u01(&s) - 0.5) * 2 * spread * nr, c.t + (u01(&s) - 0.5) * 2 * spread * nt,
+                       c.p + (u01(&s) - 0.5) * 2 * spread * np});
+    cur.swap(nxt);
+    spread *= 0.35;
+  }
+  std::vector<uint8_t> in(nc, 0);
+  auto mark = [&](double rad) {
+    std::fill(in.begin(), in.end(), 0);
+    const double cr = std::max(0.5, rad * nr), ct = std::max(0.5, rad * nt), cp = std::max(0.5, rad * np);
+    int64_t count = 0;
+    for (const C& c : cur) {
+      int r0 = (int)std::floor(c.r - cr), r1 = (int)std::ceil(c.r + cr);
+      int t0 = (int)std::floor(c.t - ct), t1 = (int)std::ceil(c.t + ct);
+      int p0 = (int)std::floor(c.p - cp), p1 = (int)std::ceil(c.p + cp);
+      for (int ir = std::max(0, r0); ir <= std::min(nr - 1, r1); ++ir)
+        for (int it = std::max(0, t0); it <= std::min(nt - 1, t1); ++it)
+          for (int ipp = p0; ipp <= p1; ++ipp) {
+            int ip = ((ipp % np) + np) % np;
+            double dr = (ir + 0.5 - c.r) / cr, dt = (it + 0.5 - c.t) / ct, dp = (ipp + 0.5 - c.p) / cp;
+            int64_t k = ir + (int64_t)nr * (it + (int64_t)nt * ip);
+            if (dr * dr + dt * dt + dp * dp <= 1.0 && !in[k]) { in[k] = 1; ++count; }
+          }
+    }
+    return (double)count / (double)nc;
+  };
+  const double K = m->fractcontrast, fm = m->densratio;
+  const double fv_target = fm / (K * (1.0 - fm) + fm);
+  double lo = 0.0, hi = 0.5;
+  for (int k = 0; k < 30; ++k) {
+    double mid = 0.5 * (lo + hi);
+    if (mark(mid) < fv_target) lo = mid; else hi = mid;
+  }
+  const double fv = std::max(mark(hi), 1.0 / (double)nc);
+  const double b = 1.0 / (K * fv + 1.0 - fv), a = K * b;
+  m->densvar.assign(nc, 1.0);
+  for (int64_t k = 0; k < nc; ++k) m->densvar[k] = in[k] ? a : b;
+}
+
+// ---------------------------------------------------------------------------
+// reapar + setup: read the keys the photon loop depends on and convert units
+// (reapar.f90:32-535, setup.f90:26-231).
+// ---------------------------------------------------------------------------
+#define REQ(call) \
+  do {            \
+    if (!(call)) return false; \
+  } while (0)
+
+static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std::string* err) {
+  int64_t iv;
+  double dv;
+  std::string sv;
+  REQ(P.integer("NP", &m->np, err));
+  REQ(P.integer("NPMIN", &m->npmin, err));
+  REQ(P.integer("NIMIN", &iv, err)); m->nimin = (int)iv;
+  REQ(P.integer("NIMAX", &iv, err)); m->nimax = (int)iv;
+  REQ(P.integer("CPEEL", &iv, err)); m->ipeel = (int)iv;
+  REQ(P.integer("CLUCY", &iv, err)); m->ilucy = (int)iv;
+  if (m->ilucy != 1) { *err = "CLUCY=NO (Bjorkman & Wood temperatures) is not supported; use CLUCY=YES"; return false; }
+  if (P.has("SEED")) { REQ(P.integer("SEED", &iv, err)); m->seed = (uint64_t)iv; }
+  else { REQ(P.integer("I1", &iv, err)); m->seed = (uint64_t)(iv < 0 ? -iv : iv); }
+  REQ(P.str("PARDIR", &m->pardir, err));
+  if (par_dir) m->pardir = *par_dir;
+  REQ(P.integer("COUTILLUM", &iv, err));
+  if (iv != 0) { *err = "COUTILLUM=YES (external illumination) is not supported"; return false; }
+  REQ(P.integer("CLIMB", &iv, err)); m->limb = (int)iv;
+  if (m->limb != 0) { *err = "CLIMB=YES (limb-darkening table) is not supported"; return false; }
+  REQ(P.integer("CPLANCKST", &iv, err)); m->iplanckst = (int)iv;
+  REQ(P.str("ATNAME", &sv, err)); m->atname = m->pardir + "/" + sv;
+  REQ(P.real("RSTAR", &m->rstar, err));
+  REQ(P.real("TSTAR", &m->tstar_k, err));
+  REQ(P.real("MASSC", &m->massc, err));
+  REQ(P.integer("CSPOT", &iv, err));
+  if (iv != 0) { *err = "CSPOT=YES (stellar hotspots) is not supported"; return false; }
+  REQ(P.real("MASSD", &m->massd, err));
+  REQ(P.str("CRMIN", &sv, err));
+  int irminsub = sv == "RSTAR" ? 0 : sv == "RSUB" ? 1 : sv == "AU" ? 2 : -1;
+  if (irminsub < 0) { *err = "CRMIN should be one of RSTAR/RSUB/AU"; return false; }
+  std::string czmin;
+  REQ(P.str("CZMIN", &czmin, err));
+  double fmassd1;
+  REQ(P.real("FMASSD1", &fmassd1, err));
+  if (P.has("CDISKCURV")) { REQ(P.str("CDISKCURV", &sv, err)); m->idiskcurve = sv == "SPH" ? 1 : 0; }
+  const char* off_keys[] = {"CHSEQ", "CGAPD", "CSPIRAL", "CDISKWARP", "CRIMPUFF", "CGAPPUFF",
+                            "CRIMCURVE", "CGAPCURVE", "CMISALIGN", "CRADEXP", "CDISKACC", "DIFFUSION",
+                            "DENSINPUT", "CGAPE"};
+  for (const char* k : off_keys) {
+    if (P.has(k)) {
+      REQ(P.integer(k, &iv, err));
+      if (iv != 0) { *err = std::string(k) + "=YES is not supported by this build"; return false; }
+    }
+  }
+  double rmind_in[HC3D_NDG] = {0}, fsg[4] = {0};
+  for (int d = 1; d <= 2; ++d) {
+    char key[64];
+    snprintf(key, sizeof key, "DUSTNAME(%d)", d);
+    REQ(P.str(key, &sv, err)); m->dustname[d - 1] = sv;
+    snprintf(key, sizeof key, "FSG(%d)", d); REQ(P.real(key, &fsg[d - 1], err));
+    snprintf(key, sizeof key, "ZSCALE(%d)", d); REQ(P.real(key, &m->z1[d - 1], err));
+    snprintf(key, sizeof key, "RMIND(%d)", d); REQ(P.real(key, &rmind_in[d - 1], err));
+    snprintf(key, sizeof key, "RMAXD(%d)", d); REQ(P.real(key, &m->rmaxd[d - 1], err));
+    snprintf(key, sizeof key, "A(%d)", d); REQ(P.real(key, &m->a[d - 1], err));
+    snprintf(key, sizeof key, "B(%d)", d); REQ(P.real(key, &m->b[d - 1], err));
+  }
+  REQ(P.str("DUSTNAME(3)", &sv, err)); m->dustname[2] = sv;
+  REQ(P.str("DUSTNAME(4)", &sv, err)); m->dustname[3] = sv;
+  REQ(P.real("FSG(3)", &fsg[2], err));
+  REQ(P.real("FSG(4)", &fsg[3], err));
+  for (int k = 0; k < 4; ++k)
+    if (fsg[k] != 0.0) { *err = "FSG > 0 (small-grain emission) is not supported"; return false; }
+  m->fmass[0] = fmassd1; m->fmass[1] = 1.0 - fmassd1; m->fmass[2] = 1.0; m->fmass[3] = 1.0;
+  for (int d = 0; d < 2; ++d) m->rddust[d] = rmind_in[d];
+  REQ(P.real("RMAX", &m->rmax, err));
+  double rmine_in;
+  REQ(P.real("RMINE", &rmine_in, err));
+  REQ(P.str("ENVTYPE", &sv, err));
+  m->ienvtype = sv == "ULRICH" ? 1 : sv == "POWLAW" ? 0 : -1;
+  if (m->ienvtype < 0) { *err = "ERROR: ENVTYPE should be set to ULRICH or POWLAW"; return false; }
+  REQ(P.real("RATE", &m->rate, err));
+  REQ(P.real("RC", &m->rc, err));
+  if (m->ienvtype == 0) { REQ(P.real("RHODENS1", &m->rhodens1, err)); REQ(P.real("ENVEXP", &m->envexp, err)); }
+  REQ(P.real("RHOAMB", &m->rhoamb, err));
+  REQ(P.integer("CFRACTAL", &iv, err)); m->ifractal = (int)iv;
+  if (m->ifractal) {
+    std::vector<int64_t> fm;
+    REQ(P.real("DENSRATIO", &m->densratio, err));
+    REQ(P.ints("FRACTMASK", &fm, err));
+    REQ(P.integer("IFSEED", &m->ifseed, err));
+    for (size_t k = 0; k < 4 && k < fm.size(); ++k) m->fractmask[k] = (int)fm[k];
+    if (P.has("FRACTLEV")) { REQ(P.integer("FRACTLEV", &iv, err)); m->fractlev = (int)iv; }
+    if (P.has("FRACTN")) { REQ(P.integer("FRACTN", &iv, err)); m->fractn = (int)iv; }
+    if (P.has("FRACTCONTRAST")) REQ(P.real("FRACTCONTRAST", &m->fractcontrast, err));
+  }
+  REQ(P.integer("CHOLE", &iv, err)); m->ihole = (int)iv;
+  if (m->ihole) {
+    REQ(P.str("CSHAPE", &sv, err));
+    if (sv == "STREAM") { *err = "CSHAPE=STREAM is not supported; use POLYN"; return false; }
+    m->ipoly = 1;
+    REQ(P.real("EX1", &m->ex1, err)); REQ(P.real("EX2", &m->ex2, err));
+    REQ(P.real("THET1", &m->thet1, err)); REQ(P.real("Z01", &m->z01, err));
+    REQ(P.real("THET2", &m->thet2, err)); REQ(P.real("Z02", &m->z02, err));
+    REQ(P.real("EXF", &m->exf, err));
+    REQ(P.real("RHOCONST1", &m->rhoconst1, err)); REQ(P.real("RHOCONST2", &m->rhoconst2, err));
+  }
+  REQ(P.integer("NPEEL", &iv, err)); m->npeel = (int)iv;
+  REQ(P.integer("NAP", &iv, err)); m->nap = (int)iv;
+  REQ(P.integer("NXIMG", &iv, err)); m->nxhst = (int)iv;
+  REQ(P.real("RMAXI", &m->rmaxi, err));
+  double apmin, apmax;
+  REQ(P.real("APMIN", &apmin, err)); REQ(P.real("APMAX", &apmax, err));
+  REQ(P.reals("THETE", &m->thete, err)); REQ(P.reals("PHIE", &m->phie, err));
+  if ((int)m->thete.size() < m->npeel || (int)m->phie.size() < m->npeel) {
+    *err = "THETE/PHIE list shorter than NPEEL"; return false;
+  }
+  m->thete.resize(m->npeel); m->phie.resize(m->npeel);
+  for (double t : m->thete)
+    if (t == 0.0) { *err = "ERROR: THETE has to be <> 0"; return false; }
+  REQ(P.integer("NRG", &iv, err)); m->nrg = (int)iv;
+  REQ(P.integer("NTG", &iv, err)); m->ntg = (int)iv;
+  REQ(P.integer("NPG", &iv, err)); m->npg = (int)iv;
+  REQ(P.integer("NMU", &iv, err)); m->nmu = (int)iv;
+  REQ(P.integer("NPH", &iv, err)); m->nph = (int)iv;
+  REQ(P.integer("NFREQ", &iv, err)); m->nfreq = (int)iv;
+  if (m->nrg < 3 || m->ntg < 3 || m->npg < 2 || m->ntg % 2 == 0) {
+    *err = "grid needs NRG>=3, NPG>=2 and an odd NTG>=3"; return false;
+  }
+  if ((double)m->nrg * m->ntg * m->npg > 1e9) { *err = "Number of grid cells requested is too large"; return false; }
+  double lmin = 0.01, lmax = 5000.0;
+  if (P.has("SEDLMIN")) REQ(P.real("SEDLMIN", &lmin, err));
+  if (P.has("SEDLMAX")) REQ(P.real("SEDLMAX", &lmax, err));
+  if (P.has("IMAGE")) { REQ(P.integer("IMAGE", &iv, err)); m->image = (int)iv; }
+  if (P.has("MAXINT")) REQ(P.integer("MAXINT", &m->maxint, err));
+
+  // ---- setup.f90:26-231 ----
+  m->numin = 1.2398 / lmax;
+  m->numax = 1.2398 / lmin;
+  m->autors = kAu / kRsun / m->rstar;
+  m->tsub_k = 1600.0;
+  m->rminsub = std::pow(m->tsub_k / m->tstar_k, -2.10);
+  if (irminsub == 1) {
+    m->rmine = m->rminsub * rmine_in;
+    for (int d = 0; d < 2; ++d) m->rddust[d] = m->rminsub * rmind_in[d];
+  } else if (irminsub == 2) {
+    m->rmine = rmine_in * m->autors;
+    for (int d = 0; d < 2; ++d) m->rddust[d] = rmind_in[d] * m->autors;
+  } else {
+    m->rmine = rmine_in;
+  }
+  if (czmin == "RSUB") {
+    const double muc = 2.3, rcgs = m->rminsub * m->rstar * kRsun, mcgs = m->massc * kMsun;
+    const double honr = std::sqrt(kBoltz * m->tsub_k / kGn / mcgs * rcgs / muc / kMH);
+    for (int d = 0; d < 2; ++d) m->z1[d] = m->z1[d] * honr * m->rminsub / std::pow(m->rminsub, m->b[d]);
+  } else if (czmin == "R100") {
+    for (int d = 0; d < 2; ++d) m->z1[d] = m->z1[d] * m->autors / std::pow(100.0 * m->autors, m->b[d]);
+  }
+  m->rmax *= m->autors;
+  for (int d = 0; d < 2; ++d) m->rmaxd[d] *= m->autors;
+  m->rmaxi *= m->autors;
+  m->rc *= m->autors;
+  m->z01 *= m->autors;
+  m->z02 *= m->autors;
+  m->aperture2.resize(m->nap);
+  for (int i = 0; i < m->nap; ++i) {
+    double ap = m->nap == 1 ? apmin
+                            : std::pow(10.0, (double)i / (double)(m->nap - 1) * (std::log10(apmax) - std::log10(apmin)) +
+                                                 std::log10(apmin));
+    ap *= m->autors;
+    m->aperture2[i] = ap * ap;
+  }
+  for (int d = 0; d < 2; ++d) {
+    if (m->rddust[d] > m->rmaxd[d] && m->fmass[d] > 0.0) { *err = "ERROR, rddust > rmaxd"; return false; }
+    if (m->rmaxd[d] > m->rmax) m->rmax = m->rmaxd[d] * 1.001;
+  }
+  m->rddustmin = std::min(m->rddust[0], m->rddust[1]);
+  for (int k = 0; k < m->npeel; ++k) {
+    m->thete[k] *= kR2p / 360.0;
+    m->phie[k] *= kR2p / 360.0;
+  }
+  return true;
+}
+
+// envset, envset.f90:18-80
+static void envset(Model* m) {
+  const double rdcgs = m->rc * m->rstar * kRsun;
+  const double cst = 1.0 / 3.15576e7 * std::sqrt(kMsun) / (4.0 * kPi) / std::sqrt(kGn);
+  m->rhoe0 = cst * m->rate / std::sqrt(m->massc) / std::pow(rdcgs, 1.5);
+  const double z1max = m->rmax;
+  if (m->thet1 < 89.999) {
+    double r1max = z1max * std::tan(m->thet1 * kPi / 180.0);
+    m->c1e = (z1max - m->z01) / std::pow(r1max, m->ex1);
+    double r2max = z1max * std::tan(m->thet2 * kPi / 180.0);
+    m->c2e = (z1max - m->z02) / std::pow(r2max, m->ex2);
+  } else {
+    m->c1e = 0.0;
+    m->c2e = 0.0;
+  }
+}
+
+// setup_wave, setup_wave.f90:46-80: disk rho0 before gridset rescales it.
+static void setup_rho0(Model* m) {
+  const double rmincgs = m->rstar * kRsun;
+  for (int id = 0; id < 2; ++id) {
+    const double z1cgs = rmincgs * m->z1[id];
+    const double p = m->b[id] - m->a[id];
+    const double rmind = m->rddust[id];
+    if (m->rmaxd[id] > 0.0 && m->fmass[id] > 0.0) {
+      const double cst = std::pow(kR2p, 1.5) * rmincgs * rmincgs * z1cgs;
+      double denom;
+      if (p != -2.0 && p != -1.5)
+        denom = 1.0 / (p + 2.0) * (std::pow(m->rmaxd[id], p + 2.0) - std::pow(rmind, p + 2.0)) -
+                1.0 / (p + 1.5) * (std::pow(m->rmaxd[id], p + 1.5) - std::pow(rmind, p + 1.5));
+      else if (p == -2.0)
+        denom = std::log(m->rmaxd[id] / rmind) -
+                1.0 / (p + 1.5) * (std::pow(m->rmaxd[id], p + 1.5) - std::pow(rmind, p + 1.5));
+      else
+        denom = 1.0 / (p + 2.0) * (std::pow(m->rmaxd[id], p + 2.0) - std::pow(rmind, p + 2.0)) -
+                std::log(m->rmaxd[id] / rmind);
+      m->rho0[id] = m->massd * kMsun / cst / denom * m->fmass[id];
+    } else {
+      m->rho0[id] = 0.0;
+    }
+  }
+}
+
+// gridset walls and densities, gridset.f90:411-664 and 954-1098
+static bool gridset(Model* m, std::string* err) {
+  const int nrg = m->nrg, ntg = m->ntg, npg = m->npg;
+  const double rmin = 1.0, rmincgs = m->rstar * kRsun;
+  m->rarr.assign(nrg, 0.0);
+  m->r2arr.assign(nrg, 0.0);
+  m->ravearr.assign(nrg - 1, 0.0);
+  // radial walls (gridset.f90:423-455)
+  m->rarr[0] = rmin;
+  if (m->massd == 0.0) {
+    const double rexpnew = 3.0;  // grid_mod rexp
+    const double dr = (m->rmax - m->rmine) / std::pow((double)(nrg - 1), rexpnew);
+    for (int ir = 2; ir <= nrg; ++ir) m->rarr[ir - 1] = m->rmine + dr * std::pow((double)(ir - 1), rexpnew);
+  } else {
+    const double rdduste = std::min(std::min(m->rddust[0], m->rddust[1]), m->rmine);
+    const double rfac = std::pow(m->rmax / rdduste, 1.0 / (double)(nrg - 2));
+    for (int ir = 2; ir <= nrg; ++ir) m->rarr[ir - 1] = rdduste * std::pow(rfac, ir - 2);
+  }
+  auto locate = [](const std::vector<double>& xx, double x) {
+    int n = (int)xx.size(), jl = 0, ju = n + 1;
+    bool asc = xx[n - 1] > xx[0];
+    while (ju - jl > 1) {
+      int jm = (ju + jl) / 2;
+      if (asc == (x > xx[jm - 1])) jl = jm; else ju = jm;
+    }
+    if (jl == 0 && x == xx[0]) jl = 1;
+    return jl;
+  };
+  if (m->rddustmin < m->rmine) {
+    int ir = locate(m->rarr, m->rmine);
+    if (ir >= 1 && ir < nrg) m->rarr[ir] = m->rmine;
+  }
+  if (m->rmine < m->rddustmin) {
+    int ir = locate(m->rarr, m->rddustmin);
+    if (ir >= 1 && ir < nrg) m->rarr[ir] = m->rddustmin;
+  }
+  for (int ir = 0; ir < nrg; ++ir) m->r2arr[ir] = std::pow(m->rarr[ir], 2.0);
+  for (int ir = 0; ir < nrg - 1; ++ir) {
+    double r1 = std::log10(m->rarr[ir]), r2 = std::log10(m->rarr[ir + 1]);
+    m->ravearr[ir] = std::pow(10.0, 0.5 * (r1 + r2));
+  }
+  for (int ir = 1; ir < nrg; ++ir)
+    if (!(m->rarr[ir] > m->rarr[ir - 1])) { *err = "radial walls are not increasing"; return false; }
+  // polar walls, power law pexp=2 (gridset.f90:529-604)
+  const int nttmp = ntg / 2;
+  const int pexp = 2;
+  m->thetarr.assign(ntg, 0.0);
+  std::vector<double> tmpth(nttmp + 1);
+  const double mm = kPi / 2.0 / std::pow((double)nttmp, pexp);
+  for (int it = 1; it <= nttmp; ++it) tmpth[it] = mm * std::pow((double)it, pexp);
+  for (int it = 1; it <= nttmp; ++it) m->thetarr[nttmp + 1 + it - 1] = tmpth[it] + kPiHalf;
+  m->thetarr[nttmp] = kPiHalf;
+  for (int it = 1; it <= nttmp; ++it) m->thetarr[it - 1] = kPi - m->thetarr[ntg - it];
+  for (double te : m->thete)
+    for (double tw : m->thetarr)
+      if (te == tw) { *err = "ERROR: peeloff angle is exactly the same as one of the wall angles"; return false; }
+  m->costarr.assign(ntg, 0.0);
+  m->sintarr.assign(ntg, 0.0);
+  m->tan2arr.assign(ntg, 0.0);
+  for (int it = 1; it <= ntg; ++it) {
+    double& th = m->thetarr[it - 1];
+    if (it == 1) {
+      th = 0.0; m->costarr[0] = 1.0; m->sintarr[0] = 0.0; m->tan2arr[0] = 0.0;
+    } else if (it == ntg) {
+      th = kPi; m->costarr[it - 1] = -1.0; m->sintarr[it - 1] = 0.0; m->tan2arr[it - 1] = 0.0;
+    } else if (it == nttmp + 1) {
+      th = kPiHalf; m->costarr[it - 1] = 0.0; m->sintarr[it - 1] = 1.0; m->tan2arr[it - 1] = -1.0;
+    } else {
+      m->costarr[it - 1] = std::cos(th);
+      m->sintarr[it - 1] = std::sin(th);
+      m->tan2arr[it - 1] = std::pow(std::tan(th), 2.0);
+    }
+  }
+  m->thetavearr.assign(ntg - 1, 0.0);
+  for (int it = 0; it < ntg - 1; ++it) {
+    if (m->thetarr[it + 1] < m->thetarr[it]) { *err = "Error - thetarr is not monotonically increasing"; return false; }
+    double th1 = std::pow(m->thetarr[it], pexp), th2 = std::pow(m->thetarr[it + 1], pexp);
+    m->thetavearr[it] = std::pow(0.5 * (th1 + th2), 1.0 / pexp);
+  }
+  // azimuthal walls (gridset.f90:642-650)
+  m->phiarr.assign(npg, 0.0);
+  m->aarr.assign(npg, 0.0);
+  m->barr.assign(npg, 0.0);
+  const double dp = kR2p / (double)(npg - 1);
+  for (int ip = 0; ip < npg; ++ip) {
+    m->phiarr[ip] = dp * (double)ip;
+    m->aarr[ip] = std::sin(m->phiarr[ip]);
+    m->barr[ip] = -std::cos(m->phiarr[ip]);
+  }
+  if (m->ifractal) fractal_field(m);
+
+  // ---- densities (gridset.f90:954-1098) ----
+  m->ndg = 4;  // disk1, disk2, envelope, cavity slots; small-grain slots 5-8 are empty
+  const int64_t n4 = m->n4();
+  m->densarr.assign(n4 * m->ndg, 0.0);
+  m->massarr.assign(n4 * m->ndg, 0.0);
+  m->vcell.assign(n4, 0.0);
+  auto cell = [&](int ir, int it, int ip) { return (int64_t)ir + (int64_t)nrg * (it + (int64_t)ntg * ip); };
+  // disk mass normalisation: diskscl = massd*fmass / mass on the grid
+  double diskscl[2] = {1.0, 1.0};
+  if (m->massd > 0.0) {
+    double tmpmass[2] = {0, 0};
+    for (int id = 0; id < 2; ++id) {
+      if (m->rho0[id] == 0.0) continue;
+      for (int ir = 0; ir < nrg - 1; ++ir) {
+        const double rad = m->ravearr[ir];
+        const double dr3 = std::pow(m->rarr[ir + 1], 3.0) - std::pow(m->rarr[ir], 3.0);
+        for (int it = 0; it < ntg - 1; ++it) {
+          const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
+          const double dcost = std::cos(m->thetarr[it + 1]) - std::cos(m->thetarr[it]);
+          const double dd = densdisk(*m, rad, sint, cost, id);
+          if (dd == 0.0) continue;
+          for (int ip = 0; ip < npg - 1; ++ip) {
+            const double dpp = m->phiarr[ip + 1] - m->phiarr[ip];
+            const double vol = -dr3 * dcost * dpp / 3.0 * std::pow(rmincgs, 3.0);
+            tmpmass[id] += dd * vol;
+          }
+        }
+      }
+      tmpmass[id] /= kMsun;
+      if (tmpmass[id] > 0.0) diskscl[id] = m->massd * m->fmass[id] / tmpmass[id];
+    }
+  }
+  m->massdisk = 0.0;
+  m->massenv = 0.0;
+  const double r3 = std::pow(rmincgs, 3.0);
+  for (int ir = 0; ir < nrg - 1; ++ir) {
+    const double rad = m->ravearr[ir];
+    const double dr3 = std::pow(m->rarr[ir + 1], 3.0) - std::pow(m->rarr[ir], 3.0);
+    for (int it = 0; it < ntg - 1; ++it) {
+      const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
+      const double dcost = std::cos(m->thetarr[it + 1]) - std::cos(m->thetarr[it]);
+      double dens_r[4];
+      for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, id) * diskscl[id];
+      for (int id = 2; id < 4; ++id) dens_r[id] = densenv(*m, rad, thet, cost, sint, id) * m->fmass[id];
+      for (int ip = 0; ip < npg - 1; ++ip) {
+        const double dpp = m->phiarr[ip + 1] - m->phiarr[ip];
+        const double vol = -dr3 * dcost * dpp / 3.0 * r3;
+        const int64_t c = cell(ir, it, ip);
+        m->vcell[c] = vol;
+        for (int id = 0; id < 4; ++id) {
+          double d = dens_r[id];
+          if (m->ifractal && m->fractmask[id] == 1)
+            d *= m->densvar[ir + (int64_t)(nrg - 1) * (it + (int64_t)(ntg - 1) * ip)];
+          m->densarr[c + n4 * id] = d;
+          m->massarr[c + n4 * id] = std::pow(d * vol, 0.25);
+          if (id < 2) m->massdisk += d * vol; else m->massenv += d * vol;
+        }
+      }
+    }
+  }
+  m->massdisk /= kMsun;
+  m->massenv /= kMsun;
+  m->ndg_active = 0;
+  for (int id = 0; id < m->ndg; ++id) {
+    bool any = false;
+    for (int64_t k = 0; k < n4 && !any; ++k) any = m->densarr[k + n4 * id] > 0.0;
+    if (any) m->ndg_active++;
+  }
+  // initarr(.true.): tdust2 = 0.1 K, tdust = tdust2 (initarr.f90:50,78-84)
+  m->tdust.assign(n4 * m->ndg, 0.1 / 11605.0);
+  // ltot without accretion or ISRF (gridset.f90:165-180)
+  m->ltot = 4.0 * kPi * kSigt * std::pow(m->tstar_k, 4.0) * rmincgs * rmincgs;
+  // Lucy packets per iteration (newtts.F90:159-182)
+  const int64_t ncells = m->ncells();
+  int64_t npl = (ntg < 10 && npg < 10) ? 100 * ncells : (int64_t)(3.0 * (double)ncells);
+  if (npl > m->np) npl = m->np;
+  if (npl < m->npmin) npl = m->npmin;
+  m->np_lucy = npl;
+  return true;
+}
+
+bool build_model(Model* m, const std::string& par_path, const std::string* par_dir, std::string* err) {
+  ParFile P;
+  if (!P.load(par_path, err)) return false;
+  if (!read_par(m, P, par_dir, err)) return false;
+  envset(m);
+  // dustinit: one table per slot; identical files are read and integrated once
+  m->ndg = 4;
+  m->nlambda.assign(m->ndg, 0);
+  const size_t nl = (size_t)m->nlammax * m->ndg;
+  m->nudust.assign(nl, 0); m->kappad.assign(nl, 0); m->adust.assign(nl, 0);
+  m->gdust.assign(nl, 0); m->pldust.assign(nl, 0); m->lamdust.assign(nl, 0);
+  m->kappav.assign(m->ndg, 0);
+  for (int id = 0; id < m->ndg; ++id)
+    if (!read_dust(m, id, m->pardir + "/" + m->dustname[id], err)) return false;
+  const double Tmin = 0.1, Tmax = 2100.0;
+  m->lTint.resize(m->nT);
+  for (int i = 0; i < m->nT; ++i)
+    m->lTint[i] = std::log(Tmin / 11605.0) + (double)i * std::log(Tmax / Tmin) / (double)(m->nT - 1);
+  const double numax = 32.0, numin = numax / 1024.0;
+  m->nuint.resize(m->nnu);
+  for (int i = 0; i < m->nnu; ++i) m->nuint[i] = numin + (double)i * (numax - numin) / (double)(m->nnu - 1);
+  m->kapBint.assign((size_t)m->nT * m->nnu * m->ndg, 0.0);
+  m->kappap.assign((size_t)m->nT * m->ndg, 0.0);
+  for (int id = 0; id < m->ndg; ++id) {
+    int same = -1;
+    for (int j = 0; j < id; ++j)
+      if (m->dustname[j] == m->dustname[id]) { same = j; break; }
+    double* kb = &m->kapBint[(size_t)id * m->nT * m->nnu];
+    double* kp = &m->kappap[(size_t)id * m->nT];
+    if (same >= 0) {
+      std::copy(&m->kapBint[(size_t)same * m->nT * m->nnu], &m->kapBint[(size_t)(same + 1) * m->nT * m->nnu], kb);
+      std::copy(&m->kappap[(size_t)same * m->nT], &m->kappap[(size_t)(same + 1) * m->nT], kp);
+    } else {
+      setemiss_species(*m, id, kb, kp);
+    }
+  }
+  if (!atmosinit(m, m->atname, err)) return false;
+  setup_rho0(m);
+  if (!gridset(m, err)) return false;
+  return true;
+}
+
+hc3d_dust_tables Model::tables_view() const {
+  hc3d_dust_tables t;
+  std::memset(&t, 0, sizeof t);
+  t.ndg = ndg; t.nlammax = nlammax; t.nlambda = nlambda.data();
+  t.nudust = nudust.data(); t.kappad = kappad.data(); t.adust = adust.data();
+  t.gdust = gdust.data(); t.pldust = pldust.data(); t.kappav = kappav.data();
+  t.nT = nT; t.nnu = nnu; t.lTint = lTint.data(); t.nuint = nuint.data();
+  t.kapBint = kapBint.data(); t.kappap = kappap.data(); t.tsub = tsub_k;
+  t.nhnu = (int)hnuint.size(); t.hnuint = hnuint.data(); t.atmosnu = atmosnu.data();
+  t.lognu = lognu.data(); t.loghnu = loghnu.data();
+  return t;
+}
+
+hc3d_grid Model::grid_view() const {
+  hc3d_grid g;
+  std::memset(&g, 0, sizeof g);
+  g.nrg = nrg; g.ntg = ntg; g.npg = npg; g.ndg = ndg;
+  g.rarr = rarr.data(); g.r2arr = r2arr.data(); g.thetarr = thetarr.data(); g.costarr = costarr.data();
+  g.tan2arr = tan2arr.data(); g.phiarr = phiarr.data(); g.aarr = aarr.data(); g.barr = barr.data();
+  g.densarr = densarr.data(); g.massarr = massarr.data(); g.vcell = vcell.data(); g.tdust = tdust.data();
+  return g;
+}
+
+hc3d_run_params Model::params_view() const {
+  hc3d_run_params p;
+  std::memset(&p, 0, sizeof p);
+  p.np = np; p.packet_offset = 0; p.seed = seed; p.iter = 1; p.ipeel = ipeel; p.npeel = npeel;
+  p.thete = thete.data(); p.phie = phie.data(); p.nfreq = nfreq; p.nmu = nmu; p.nph = nph; p.nap = nap;
+  p.nxhst = nxhst; p.rmaxi = rmaxi; p.aperture2 = aperture2.data(); p.numin = numin; p.numax = numax;
+  p.rstar_cm = rstar * kRsun; p.tstar = tstar_k / 11605.0; p.limb = limb; p.iintmax = 10000;
+  p.max_interactions = maxint; p.image = image;
+  return p;
+}
+
+hc3d_model_info Model::info() const {
+  hc3d_model_info i;
+  std::memset(&i, 0, sizeof i);
+  i.np = np; i.npmin = npmin; i.np_lucy = np_lucy; i.nimin = nimin; i.nimax = nimax; i.ipeel = ipeel;
+  i.ilucy = ilucy; i.ndg_active = ndg_active; i.ltot = ltot; i.tstar_k = tstar_k; i.rstar_rsun = rstar;
+  i.autors = autors; i.rminsub = rminsub; i.massdisk = massdisk; i.massenv = massenv; i.ncells = ncells();
+  return i;
+}
+
+}  // namespace hc3d
+
+// ---------------------------------------------------------------------------
+// C entry points of hc3d_host.h (model part)
+// ---------------------------------------------------------------------------
+
+static void put_err(char* err, size_t len, const std::string& s) {
+  if (err && len) {
+    std::snprintf(err, len, "%s", s.c_str());
+  }
+}
+
+extern "C" int hc3d_model_create(hc3d_model** out, const char* par_path, const char* par_dir, char* err,
+                                 size_t errlen) {
+  if (!out || !par_path) return HC3D_ERR_INVALID;
+  *out = nullptr;
+  hc3d_model* m = new (std::nothrow) hc3d_model();
+  if (!m) return HC3D_ERR_NOMEM;
+  std::string e;
+  std::string pd = par_dir ? par_dir : "";
+  try {
+    if (!hc3d::build_model(&m->m, par_path, par_dir ? &pd : nullptr, &e)) {
+      put_err(err, errlen, e);
+      delete m;
+      bool unsup = e.find("not supported") != std::string::npos;
+      bool io = e.find("cannot open") != std::string::npos;
+      return unsup ? HC3D_ERR_UNSUPPORTED : io ? HC3D_ERR_IO : HC3D_ERR_INVALID;
+    }
+  } catch (const std::bad_alloc&) {
+    put_err(err, errlen, "host allocation failed");
+    delete m;
+    return HC3D_ERR_NOMEM;
+  }
+  *out = m;
+  return HC3D_OK;
+}
+
+extern "C" void hc3d_model_destroy(hc3d_model* m) { delete m; }
+
+extern "C" int hc3d_model_views(hc3d_model* m, hc3d_dust_tables* t, hc3d_grid* g, hc3d_run_params* p,
+                                hc3d_model_info* info) {
+  if (!m) return HC3D_ERR_INVALID;
+  if (t) *t = m->m.tables_view();
+  if (g) *g = m->m.grid_view();
+  if (p) *p = m->m.params_view();
+  if (info) *info = m->m.info();
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_model_set_tdust(hc3d_model* m, const double* tdust) {
+  if (!m || !tdust) return HC3D_ERR_INVALID;
+  std::copy(tdust, tdust + m->m.tdust.size(), m->m.tdust.begin());
+  return HC3D_OK;
+}
+
+// Fixture writers ------------------------------------------------------------
+extern "C" int hc3d_write_synthetic_dust(const char* path) {
+  // kappa: kV*(0.55/lam) below 100 um, continued as lam^-1.7 beyond, flat
+  // below 0.1 um; albedo 0.5 -> 0 and g 0.6 -> 0 linear in log(lam) over
+  // 0.1-10 um; pmax = 0.5.
+  FILE* f = std::fopen(path, "w");
+  if (!f) return HC3D_ERR_IO;
+  const int n = 241;
+  const double kV = 100.0;
+  for (int i = 0; i < n; ++i) {
+    double lam = std::pow(10.0, -2.0 + 6.0 * i / (double)(n - 1));  // 0.01 .. 10000 um
+    double l = std::max(lam, 0.1);
+    double kap = l <= 100.0 ? kV * (0.55 / l) : kV * (0.55 / 100.0) * std::pow(l / 100.0, -1.7);
+    double x = (std::log10(lam) - std::log10(0.1)) / 2.0;
+    x = std::max(0.0, std::min(1.0, x));
+    double alb = 0.5 * (1.0 - x), g = 0.6 * (1.0 - x);
+    double cext = kap * 1.0e-22;
+    std::fprintf(f, " %.6e %.6e %.6e %.6e %.6e %.6e %.6e\n", lam, cext, alb * cext, kap, g, 0.5, 0.0);
+  }
+  std::fclose(f);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_write_wavelength_grid(const char* path, double tstar_k) {
+  // 1321 log-spaced wavelengths over 0.0091-1e6 um (the span of the shipped
+  // Kurucz tables); the flux column is the Planck function at tstar_k.
+  FILE* f = std::fopen(path, "w");
+  if (!f) return HC3D_ERR_IO;
+  std::fprintf(f, "# synthetic wavelength grid, Planck Teff = %.1f K\n", tstar_k);
+  const int n = 1321;
+  for (int i = 0; i < n; ++i) {
+    double lam = std::pow(10.0, std::log10(0.0091) + (std::log10(1.0e6) - std::log10(0.0091)) * i / (double)(n - 1));
+    double x = 1.2398 / lam / (tstar_k / 11605.0);
+    double b = x < 700.0 ? x * x * x / std::expm1(x) : 0.0;
+    std::fprintf(f, " %14.4f  %.4e\n", lam, b);
+  }
+  std::fclose(f);
+  return HC3D_OK;
+}

@@ -1,0 +1,115 @@
+// hc3d_model.h -- host model: the data newtts.F90 builds before calling disk().
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hc3d.h"
+#include "../../include/hc3d_host.h"
+
+namespace hc3d {
+
+// physical constants, constants.f90:11-26
+constexpr double kPi = 3.1415926535897932384626433;
+constexpr double kR2p = 2.0 * kPi;
+constexpr double kPiHalf = 0.5 * kPi;
+constexpr double kRsun = 6.9598e10;
+constexpr double kMsun = 1.989e33;
+constexpr double kLsun = 3.839e33;
+constexpr double kGn = 6.67428e-8;
+constexpr double kSigt = 5.670400e-5;
+constexpr double kBoltz = 1.3806503e-16;
+constexpr double kMH = 1.67262158e-24;
+constexpr double kC = 2.99792458e10;
+constexpr double kAu = 1.49598e13;
+constexpr double kPc = 3.0857e18;
+
+// ".par" file: value = KEY = comment (configuration.f90:28-56)
+class ParFile {
+ public:
+  bool load(const std::string& path, std::string* err);
+  bool has(const std::string& key) const { return kv_.count(key) != 0; }
+  bool str(const std::string& key, std::string* out, std::string* err) const;
+  bool real(const std::string& key, double* out, std::string* err) const;
+  bool integer(const std::string& key, int64_t* out, std::string* err) const;  // YES/NO -> 1/0
+  bool reals(const std::string& key, std::vector<double>* out, std::string* err) const;
+  bool ints(const std::string& key, std::vector<int64_t>* out, std::string* err) const;
+
+ private:
+  std::map<std::string, std::string> kv_;
+};
+
+struct Model {
+  // ---- reapar/setup scalars (units after setup.f90) ----
+  int64_t np = 0, npmin = 0, np_lucy = 0;
+  int nimin = 0, nimax = 0, ipeel = 0, ilucy = 1, limb = 0, iplanckst = 1;
+  double rstar = 1, tstar_k = 4000, massc = 0.5, massd = 0;
+  double rmax = 0, rmaxi = 0, rc = 0, rate = 0, rhoamb = 0;
+  double rmine = 0, rminsub = 0, autors = 1, rddustmin = 0;
+  double rmaxd[HC3D_NDG] = {0}, rddust[HC3D_NDG] = {0};
+  double z1[HC3D_NDG] = {0}, a[HC3D_NDG] = {0}, b[HC3D_NDG] = {0}, fmass[HC3D_NDG] = {0}, rho0[HC3D_NDG] = {0};
+  int ihole = 0, ipoly = 1, istream = 0, ienvtype = 1;
+  double thet1 = 0, thet2 = 0, ex1 = 1, ex2 = 1, z01 = 0, z02 = 0, exf = 0, rhoconst1 = 0, rhoconst2 = 0;
+  double c1e = 0, c2e = 0, rhoe0 = 0, rhodens1 = 0, envexp = 0;
+  int idiskcurve = 0;
+  int ifractal = 0, fractlev = 3, fractn = 32;
+  double densratio = 0.5, fractcontrast = 100.0;
+  int fractmask[HC3D_NDG] = {0};
+  int64_t ifseed = 0;
+  int nfreq = 0, nmu = 0, nph = 0, nap = 0, npeel = 0, nxhst = 0;
+  std::vector<double> thete, phie, aperture2;
+  double numin = 0, numax = 0;
+  double ltot = 0;
+  double massdisk = 0, massenv = 0;
+  int image = 1;
+  int64_t maxint = 1000000;
+  uint64_t seed = 0;
+  std::string atname, pardir;
+  std::string dustname[HC3D_NDG];
+
+  // ---- dust_mod ----
+  int ndg = 0;  // slots carried across the boundary
+  int nlammax = 1001;
+  std::vector<int> nlambda;
+  std::vector<double> nudust, kappad, adust, gdust, pldust, lamdust, kappav;
+  int nT = 1000, nnu = 1025;
+  std::vector<double> lTint, nuint, kapBint, kappap;
+  double tsub_k = 1600.0;
+  std::vector<double> hnuint, atmosnu, lognu, loghnu;
+
+  // ---- grid_mod ----
+  int nrg = 0, ntg = 0, npg = 0;
+  std::vector<double> rarr, r2arr, ravearr, thetarr, costarr, sintarr, tan2arr, thetavearr, phiarr, aarr, barr;
+  std::vector<double> densarr, massarr, vcell, tdust;
+  std::vector<double> densvar;
+  int ndg_active = 0;
+
+  hc3d_dust_tables tables_view() const;
+  hc3d_grid grid_view() const;
+  hc3d_run_params params_view() const;  // pointers into this model
+  hc3d_model_info info() const;
+  int64_t ncells() const { return (int64_t)(nrg - 1) * (ntg - 1) * (npg - 1); }
+  int64_t n4() const { return (int64_t)nrg * ntg * npg; }
+};
+
+// setup.f90 + reapar.f90 + dustinit + atmosinit + setup_wave + gridset
+bool build_model(Model* m, const std::string& par_path, const std::string* par_dir, std::string* err);
+
+// setemiss (dust.f90:394-474) for one species table, kapBint and kappap only
+void setemiss_species(const Model& m, int id, double* kapB /*(nT,nnu)*/, double* kapp /*(nT)*/);
+
+// densdisk (densdiskg.f90:1-155) and densenv (densenv.f90:1-128) for the
+// options the benchmark models use
+double densdisk(const Model& m, double rad, double sint, double cost, int id);
+double densenv(const Model& m, double rad, double thetin, double costin, double sina, int id);
+// zerod: the Ulrich streamline root mu0 (module not shipped; restated)
+double zerod(double mu, double rx);
+
+}  // namespace hc3d
+
+// opaque handle of hc3d_host.h
+struct hc3d_model {
+  hc3d::Model m;
+};

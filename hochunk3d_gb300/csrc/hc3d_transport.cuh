@@ -1,0 +1,983 @@
+// hc3d_transport.cuh -- the photon-packet loop as sm_103a device code.
+//
+// One templated implementation, instantiated twice:
+//   R = double : the all-FP64 form.  Its translation unit is compiled with
+//                --fmad=false so that it rounds like the CPU restatement of
+//                the reference and can be compared with it packet by packet.
+//   R = float  : the mixed form.  Directions, Stokes vectors, angles, cone and
+//                plane roots, opacities and the propagation tau integral are
+//                FP32.  FP64 is kept for the position, the radial-face
+//                quadratic (cancellation-free form), the cumulative peel-off
+//                escape tau and the per-event table lookups (opacset,
+//                lucydustfreq, atmosfreq).
+//
+// The routine-by-routine structure follows the reference: disk() packet loop
+// (newdisktherm.F90:256-377), propagate (propagate.f90:27-319), the cell walk
+// (radface.f90:44-62, phiface.f90:48-56, closest_wall.f90:13-66, thetaface and
+// tauint restated from their call sites peeloff_3d.f90:88-154), scattering
+// (stokes.f90:46-388, dustmat.f90:40-65, select_dust.f90:16-42), re-emission
+// (reemit.f90:17-34, lucydustfreq.f90:19-157) and peel-off (peeloff_3d.f90:
+// 52-286, findangle3.f90:31-67, stokespeel.f90:49-376).  Random draws are
+// taken in the same order as the Fortran; the stream is counter-based
+// Philox4x32-10 keyed by (seed, iteration, packet id).
+//
+// Execution: a persistent grid; every thread takes the next packet id from a
+// global counter when its packet ends (regeneration), so the cost of long
+// packet histories is balanced across the device.  All tallies are int64
+// fixed-point atomics: sums do not depend on the order packets finish in.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hc3d_device.h"
+
+namespace hc3d {
+namespace dev {
+
+constexpr double kPi = 3.1415926535897932384626433;
+constexpr double kR2p = 2.0 * kPi;
+constexpr double kTauMax = 25.0;  // peeloff_3d.f90:40
+
+// ---- math overloads ---------------------------------------------------------
+__device__ __forceinline__ float xsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float xcos(float x) { return cosf(x); }
+__device__ __forceinline__ double xcos(double x) { return cos(x); }
+__device__ __forceinline__ float xsin(float x) { return sinf(x); }
+__device__ __forceinline__ double xsin(double x) { return sin(x); }
+__device__ __forceinline__ float xacos(float x) { return acosf(x); }
+__device__ __forceinline__ double xacos(double x) { return acos(x); }
+__device__ __forceinline__ float xlog(float x) { return logf(x); }
+__device__ __forceinline__ double xlog(double x) { return log(x); }
+__device__ __forceinline__ float xabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double xabs(double x) { return fabs(x); }
+template <class R> __device__ __forceinline__ R rhuge();
+template <> __device__ __forceinline__ float rhuge<float>() { return 3.402823466e38f; }
+template <> __device__ __forceinline__ double rhuge<double>() { return 1.7976931348623157e308; }
+
+// ---- Philox4x32-10 (Salmon et al., SC'11) -------------------------------------
+struct Rng {
+  uint32_t k0, k1, c0, c2, c3;
+  uint32_t b[4];
+  int left;
+  const double* inj;
+  int ninj, pos;
+};
+
+__device__ __forceinline__ void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                       uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+__device__ __forceinline__ void rng_init(Rng& r, uint32_t key0, uint32_t key1, uint64_t pid) {
+  r.k0 = key0; r.k1 = key1; r.c0 = 0;
+  r.c2 = (uint32_t)pid; r.c3 = (uint32_t)(pid >> 32);
+  r.left = 0; r.inj = nullptr; r.ninj = 0; r.pos = 0;
+}
+
+__device__ __forceinline__ uint32_t next_u32(Rng& r) {
+  if (r.left == 0) {
+    philox(r.c0, 0u, r.c2, r.c3, r.k0, r.k1, r.b);
+    r.c0++;
+    r.left = 4;
+  }
+  uint32_t u = r.b[4 - r.left];
+  r.left--;
+  return u;
+}
+
+template <class R> __device__ __forceinline__ R ran(Rng& r);
+template <> __device__ __forceinline__ double ran<double>(Rng& r) {
+  if (r.inj) return r.pos < r.ninj ? r.inj[r.pos++] : 0.5;
+  return ((double)next_u32(r) + 0.5) * (1.0 / 4294967296.0);
+}
+template <> __device__ __forceinline__ float ran<float>(Rng& r) {
+  if (r.inj) return r.pos < r.ninj ? (float)r.inj[r.pos++] : 0.5f;
+  return ((float)(next_u32(r) >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+// ---- packet state: the tts_mod/stokesvar_mod globals of one packet ------------
+template <class R>
+struct Pkt {
+  double x, y, z;
+  R ux, uy, uz;
+  R cost, sint, cosp, sinp, phi;
+  R sip, sqp, sup, svp;
+  double nub;
+  R cosb, sinb, lp;
+  int ir, it, ip;
+  int on_wall;
+  int i_orig;
+  R kapd[kSlots], albedo[kSlots], g[kSlots], pl[kSlots];
+};
+
+// per-thread counters, flushed once per thread
+struct Local {
+  unsigned long long c[16];
+};
+
+// trace record (hc3d_trace_rec of hc3d.h)
+struct TraceRec {
+  int32_t kind, ir, it, ip, iface, pad;
+  double tsum, x, y, z;
+};
+struct Tracer {
+  TraceRec* recs;
+  int max_rec;
+  int n;
+  __device__ __forceinline__ void add(int kind, int ir, int it, int ip, int iface, double tsum, double x, double y,
+                                      double z) {
+    if (recs && n < max_rec) {
+      TraceRec& r = recs[n++];
+      r.kind = kind; r.ir = ir; r.it = it; r.ip = ip; r.iface = iface; r.pad = 0;
+      r.tsum = tsum; r.x = x; r.y = y; r.z = z;
+    }
+  }
+};
+
+// ---- closest_wall.f90:13-66 ----------------------------------------------------
+template <class R>
+struct Walls {
+  R tn1, tp1, tp2;
+  int in1, ip1, ip2;
+  __device__ __forceinline__ void reset() {
+    tn1 = -rhuge<R>(); tp1 = rhuge<R>(); tp2 = rhuge<R>();
+    in1 = 0; ip1 = 0; ip2 = 0;
+  }
+  __device__ __forceinline__ void insert(R t, int i) {
+    if (t < R(0)) {
+      if (t > tn1) { tn1 = t; in1 = i; }
+    } else {
+      if (t < tp1) { tp2 = tp1; ip2 = ip1; tp1 = t; ip1 = i; }
+      else if (t < tp2) { tp2 = t; ip2 = i; }
+    }
+  }
+  __device__ __forceinline__ bool next(int on_wall, R& t, int& i) const {
+    if (on_wall) {
+      if (xabs(tn1) < xabs(tp1)) { t = tp1; i = ip1; }
+      else { t = tp2; i = ip2; }
+    } else {
+      t = tp1; i = ip1;
+    }
+    return t != rhuge<R>();
+  }
+};
+
+// radface.f90:44-62.  FP64 form: the reference's (-b +- sqrt(D))/2.  Mixed
+// form: the same roots in FP64 by the cancellation-free q = -(b+sign(b)sqrt D)/2,
+// roots q and c/q.
+template <class R>
+__device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, double uz, double x, double y, double z,
+                                        double R2_1, double R2_2) {
+  const double bb = 2.0 * (x * ux + y * uy + uz * z);
+  const double rr = x * x + y * y + z * z;
+  if (sizeof(R) == 8) {
+    double cc = rr - R2_1;
+    double descr = bb * bb - 4.0 * cc;
+    if (descr > 0.0) {
+      descr = sqrt(descr);
+      w.insert((R)((-bb + descr) * 0.5), 1);
+      w.insert((R)((-bb - descr) * 0.5), 1);
+    }
+    cc = rr - R2_2;
+    descr = bb * bb - 4.0 * cc;
+    if (descr > 0.0) {
+      descr = sqrt(descr);
+      w.insert((R)((-bb + descr) * 0.5), 2);
+      w.insert((R)((-bb - descr) * 0.5), 2);
+    }
+  } else {
+    double cc = rr - R2_1;
+    double descr = bb * bb - 4.0 * cc;
+    if (descr > 0.0) {
+      double q = -0.5 * (bb + copysign(sqrt(descr), bb));
+      w.insert((R)q, 1);
+      w.insert((R)(cc / q), 1);
+    }
+    cc = rr - R2_2;
+    descr = bb * bb - 4.0 * cc;
+    if (descr > 0.0) {
+      double q = -0.5 * (bb + copysign(sqrt(descr), bb));
+      w.insert((R)q, 2);
+      w.insert((R)(cc / q), 2);
+    }
+  }
+}
+
+// thetaface (module not shipped; restated): one cone wall on the nappe of its
+// hemisphere; tan2 < 0 is the midplane plane z = 0; tan2 == 0 is a pole.
+template <class R>
+__device__ __forceinline__ void cone_roots(Walls<R>& w, R ux, R uy, R uz, R x, R y, R z, R tan2, R hemi, int id) {
+  if (tan2 == R(0)) return;
+  if (tan2 < R(0)) {
+    if (uz != R(0)) w.insert(-z / uz, id);
+    return;
+  }
+  const R a = ux * ux + uy * uy - tan2 * uz * uz;
+  const R b = R(2) * (x * ux + y * uy - tan2 * z * uz);
+  const R cq = x * x + y * y - tan2 * z * z;
+  if (a == R(0)) {
+    if (b != R(0)) {
+      R t = -cq / b;
+      if ((z + t * uz) * hemi > R(0)) w.insert(t, id);
+    }
+    return;
+  }
+  R descr = b * b - R(4) * a * cq;
+  if (descr > R(0)) {
+    descr = xsqrt(descr);
+    const R t1 = (-b + descr) / (R(2) * a);
+    const R t2 = (-b - descr) / (R(2) * a);
+    if ((z + t1 * uz) * hemi > R(0)) w.insert(t1, id);
+    if ((z + t2 * uz) * hemi > R(0)) w.insert(t2, id);
+  }
+}
+
+template <class R> __device__ __forceinline__ R tan2_of(const DevModel& m, int i);
+template <> __device__ __forceinline__ float tan2_of<float>(const DevModel& m, int i) { return __ldg(m.tan2f + i); }
+template <> __device__ __forceinline__ double tan2_of<double>(const DevModel& m, int i) { return __ldg(m.tan2d + i); }
+template <class R> __device__ __forceinline__ R aarr_of(const DevModel& m, int i);
+template <> __device__ __forceinline__ float aarr_of<float>(const DevModel& m, int i) { return __ldg(m.aarrf + i); }
+template <> __device__ __forceinline__ double aarr_of<double>(const DevModel& m, int i) { return __ldg(m.aarrd + i); }
+template <class R> __device__ __forceinline__ R barr_of(const DevModel& m, int i);
+template <> __device__ __forceinline__ float barr_of<float>(const DevModel& m, int i) { return __ldg(m.barrf + i); }
+template <> __device__ __forceinline__ double barr_of<double>(const DevModel& m, int i) { return __ldg(m.barrd + i); }
+
+// The wall machinery of one step (peeloff_3d.f90:92-115).
+template <class R>
+__device__ __forceinline__ bool next_wall(const DevModel& m, R ux, R uy, R uz, double x, double y, double z, int ir,
+                                          int it, int ip, int on_wall, R& dt, int& iface) {
+  Walls<R> w;
+  w.reset();
+  radface<R>(w, (double)ux, (double)uy, (double)uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir));
+  if (m.ntg > 2) {
+    const R xr = (R)x, yr = (R)y, zr = (R)z;
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3);
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4);
+    if (m.npg > 2) {
+      // phiface.f90:48-56 with C = D = 0
+      const R A1 = aarr_of<R>(m, ip - 1), B1 = barr_of<R>(m, ip - 1);
+      const R A2 = aarr_of<R>(m, ip), B2 = barr_of<R>(m, ip);
+      const R d1 = A1 * ux + B1 * uy;
+      if (d1 != R(0)) w.insert(-(A1 * xr + B1 * yr) / d1, 5);
+      const R d2 = A2 * ux + B2 * uy;
+      if (d2 != R(0)) w.insert(-(A2 * xr + B2 * yr) / d2, 6);
+    }
+  }
+  return w.next(on_wall, dt, iface);
+}
+
+// wall -> index step, peeloff_3d.f90:120-139
+__device__ __forceinline__ void step_index(int npg, int iface, int& ir, int& it, int& ip) {
+  switch (iface) {
+    case 1: ir--; break;
+    case 2: ir++; break;
+    case 3: it--; break;
+    case 4: it++; break;
+    case 5: ip--; break;
+    case 6: ip++; break;
+  }
+  if (ip == 0) ip = npg - 1;
+  if (ip == npg) ip = 1;
+}
+
+__device__ __forceinline__ int64_t cidx(const DevModel& m, int ir, int it, int ip) {
+  return (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+}
+
+template <class R> struct Rho { R v[kSlots]; };
+template <class R> __device__ __forceinline__ Rho<R> load_rho(const DevModel& m, int64_t c);
+template <> __device__ __forceinline__ Rho<float> load_rho<float>(const DevModel& m, int64_t c) {
+  float4 q = __ldg(m.rho4f + c);
+  Rho<float> r;
+  r.v[0] = q.x; r.v[1] = q.y; r.v[2] = q.z; r.v[3] = q.w;
+  return r;
+}
+template <> __device__ __forceinline__ Rho<double> load_rho<double>(const DevModel& m, int64_t c) {
+  const double2* p = reinterpret_cast<const double2*>(m.rho4d + 4 * c);
+  double2 a = __ldg(p), b = __ldg(p + 1);
+  Rho<double> r;
+  r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
+  return r;
+}
+
+__device__ __forceinline__ unsigned long long fx(double v, double scale) {
+  return (unsigned long long)llround(v * scale);
+}
+
+// ---- opacset, dust.f90:9-80 (FP64 lookups; results stored in R) ---------------
+template <class R>
+__device__ void opacset(const DevModel& m, Pkt<R>& p, double nu, double rstar_cm) {
+#pragma unroll
+  for (int id = 0; id < kSlots; ++id) {
+    const int nl = m.nlambda[id];
+    const size_t o = (size_t)id * m.nlammax;
+    const double* nud = m.nudust + o;
+    double g, pl, kappa, albedo;
+    if (nu >= __ldg(nud)) {
+      g = __ldg(m.gdust + o); pl = __ldg(m.pldust + o); kappa = __ldg(m.kappad + o); albedo = __ldg(m.adust + o);
+    } else if (nu <= __ldg(nud + nl - 1)) {
+      const size_t k = o + nl - 1;
+      g = __ldg(m.gdust + k); pl = __ldg(m.pldust + k); kappa = __ldg(m.kappad + k); albedo = __ldg(m.adust + k);
+    } else {
+      int i0 = 1, i1 = nl;
+      while (i1 - i0 > 1) {
+        int i = (i1 + i0) / 2;
+        if (nu <= __ldg(nud + i - 1)) i0 = i; else i1 = i;
+      }
+      const double n1 = __ldg(nud + i1 - 1), n0 = __ldg(nud + i0 - 1);
+      const double f = (nu - n1) / (n0 - n1), fm1 = 1.0 - f;
+      const size_t k1 = o + i1 - 1, k0 = o + i0 - 1;
+      g = fm1 * __ldg(m.gdust + k1) + f * __ldg(m.gdust + k0);
+      pl = fm1 * __ldg(m.pldust + k1) + f * __ldg(m.pldust + k0);
+      kappa = fm1 * __ldg(m.kappad + k1) + f * __ldg(m.kappad + k0);
+      albedo = fm1 * __ldg(m.adust + k1) + f * __ldg(m.adust + k0);
+    }
+    p.g[id] = (R)g; p.pl[id] = (R)pl; p.albedo[id] = (R)albedo;
+    p.kapd[id] = (R)(kappa * rstar_cm * m.kappav[id]);
+  }
+}
+
+// ---- tauint (restated; module not shipped) -------------------------------------
+enum { TI_INTERACT = 0, TI_ESCAPE = 1, TI_STAR = 2, TI_FAULT = 3 };
+
+template <class R>
+__device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
+  R tsum = R(0);
+  const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  for (int n = 0;; ++n) {
+    if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) return TI_FAULT;
+    R dt;
+    int iface;
+    if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) return TI_FAULT;
+    const int64_t c = cidx(m, p.ir, p.it, p.ip);
+    const Rho<R> rho = load_rho<R>(m, c);
+    R opac = R(0);
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
+    const R dtau = opac * dt;
+    const double rout = __ldg(m.rarr + p.ir);
+    L.c[HC3D_CNT_CROSS_PROP]++;
+    if (tsum + dtau > tau) {
+      const R ds = (tau - tsum) / opac;
+      p.x += (double)ds * (double)p.ux;
+      p.y += (double)ds * (double)p.uy;
+      p.z += (double)ds * (double)p.uz;
+      p.on_wall = 0;
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s)
+        if (rho.v[s] > R(0)) {
+          const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * ds;
+          atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
+        }
+      atomicAdd(t.jmean + c, fx((double)ds / rout, t.path_scale));
+      tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, p.x, p.y, p.z);
+      return TI_INTERACT;
+    }
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s)
+      if (rho.v[s] > R(0)) {
+        const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * dt;
+        atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
+      }
+    atomicAdd(t.jmean + c, fx((double)dt / rout, t.path_scale));
+    tsum += dtau;
+    step_index(m.npg, iface, p.ir, p.it, p.ip);
+    p.x += (double)dt * (double)p.ux;
+    p.y += (double)dt * (double)p.uy;
+    p.z += (double)dt * (double)p.uz;
+    p.on_wall = 1;
+    tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
+    if (p.ir == m.nrg) return TI_ESCAPE;
+    if (p.ir == 0) return TI_STAR;
+  }
+}
+
+// ---- select_dust.f90:16-42 ---------------------------------------------------
+template <class R>
+__device__ int select_dust(const DevModel& m, const Pkt<R>& p, Rng& rng) {
+  const R xran = ran<R>(rng);
+  const Rho<R> rho = load_rho<R>(m, cidx(m, p.ir, p.it, p.ip));
+  R opac = R(0), frac = R(0);
+#pragma unroll
+  for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
+  if (opac == R(0)) return -1;
+  for (int s = 0; s < kSlots; ++s) {
+    frac += p.kapd[s] * rho.v[s] / opac;
+    if (xran <= frac + (R)(double)1.e-10f) return s;
+  }
+  return -1;
+}
+
+// ---- dustmat.f90:40-65 -----------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void dustmat(R g, R pl, R cost, R cost2, R& p1, R& p2, R& p3) {
+  const R g2 = g * g;
+  const R temp = (g2 + R(1)) - (R(2) * g) * cost;
+  p1 = R(1.5) * (R(1) - g2) / (R(2) + g2) * (R(1) + cost2) / (temp * xsqrt(temp));
+  p2 = -pl * p1 * (R(1) - cost2) / (R(1) + cost2);
+  p3 = p1 * R(2) * cost / (R(1) + cost2);
+}
+
+template <class R>
+__device__ __forceinline__ R peak_of(R g) {
+  const R g2 = g * g;
+  R temp;
+  if (g > R(0)) temp = (g2 + R(1)) - R(2) * g;
+  else temp = (g2 + R(1)) + R(2) * g;
+  const R peak = R(1.5) * (R(1) - g2) / (R(2) + g2) * R(2) / temp / xsqrt(temp);
+  return peak * R(1.01);
+}
+
+// Mueller rotation of a Stokes vector (the a21..a44 blocks of stokes.f90 and
+// stokespeel.f90); s2x/c2x: double angle of i1 (or i3), sin2i2/cos2i2 of i2.
+template <class R>
+__device__ __forceinline__ void mueller(bool upper, R p1, R p2, R p3, R s2x, R c2x, R sini2, R cosi2, R& si, R& sq,
+                                        R& su, R& sv) {
+  const R sin2i2 = R(2) * sini2 * cosi2, cos2i2 = R(2) * cosi2 * cosi2 - R(1);
+  const R sin2 = sin2i2 * s2x, cos2 = cos2i2 * c2x;
+  const R sin2cos1 = sin2i2 * c2x, cos2sin1 = cos2i2 * s2x;
+  R a11, a12, a13, a21, a22, a23, a31, a32, a33, a44;
+  if (upper) {
+    a11 = p1; a12 = p2 * c2x; a13 = p2 * s2x;
+    a21 = p2 * cos2i2; a22 = p1 * cos2 - p3 * sin2; a23 = p1 * cos2sin1 + p3 * sin2cos1;
+    a31 = -p2 * sin2i2; a32 = -p1 * sin2cos1 - p3 * cos2sin1; a33 = -p1 * sin2 + p3 * cos2;
+    a44 = p3;
+  } else {
+    a11 = p1; a12 = p2 * c2x; a13 = -p2 * s2x;
+    a21 = p2 * cos2i2; a22 = p1 * cos2 - p3 * sin2; a23 = -p1 * cos2sin1 - p3 * sin2cos1;
+    a31 = p2 * sin2i2; a32 = p1 * sin2cos1 + p3 * cos2sin1; a33 = -p1 * sin2 + p3 * cos2;
+    a44 = p3;
+  }
+  // p4 = 0 (dustmat.f90:65): a24 = a34 = a42 = a43 = 0
+  const R i = a11 * si + a12 * sq + a13 * su;
+  const R q = a21 * si + a22 * sq + a23 * su + R(0) * sv;
+  const R u = a31 * si + a32 * sq + a33 * su + R(0) * sv;
+  const R v = R(0) * sq + R(0) * su + a44 * sv;
+  si = i; sq = q; su = u; sv = v;
+}
+
+// ---- stokes.f90:46-388 --------------------------------------------------------------
+template <class R>
+__device__ void stokes(Pkt<R>& p, int id, Rng& rng) {
+  const R costp = p.cost, sintp = p.sint, phip = p.phi;
+  const R g = p.g[id], pl = p.pl[id];
+  R peak = peak_of<R>(g);
+  R bmu, cosb2, sinbt, p1, p2, p3, rprob, ci, si_;
+  bool upper;
+  for (;;) {
+    bmu = R(1) - R(2) * ran<R>(rng);
+    cosb2 = bmu * bmu;
+    dustmat<R>(g, pl, bmu, cosb2, p1, p2, p3);
+    if (xabs(bmu) > R(1)) { bmu = bmu > R(1) ? R(1) : R(-1); cosb2 = R(1); }
+    sinbt = xsqrt(R(1) - cosb2);
+    const R ri1 = (R)kR2p * ran<R>(rng);
+    upper = ri1 > (R)kPi;
+    const R ang = upper ? (R)kR2p - ri1 : ri1;
+    ci = xcos(ang);
+    si_ = xsin(ang);
+    const R s2 = R(2) * si_ * ci, c2 = R(2) * ci * ci - R(1);
+    const R a12 = p2 * c2, a13 = upper ? p2 * s2 : -p2 * s2;
+    rprob = (p1 * p.sip + a12 * p.sqp + a13 * p.sup) / p.sip;
+    if (rprob > peak) peak = rprob;
+    const R xran = ran<R>(rng);
+    if (!(peak * xran > rprob)) break;
+  }
+  const R a = rprob;
+  if (bmu == R(1)) return;
+  const R s2x = R(2) * si_ * ci, c2x = R(2) * ci * ci - R(1);
+  R cosi2 = R(0), sini2 = R(0);
+  if (bmu == R(-1)) {
+    si_ = R(1); sini2 = R(1); ci = R(0); cosi2 = R(0);
+    p.cost = -costp; p.sint = sintp;
+  } else {
+    p.cost = costp * bmu + sintp * sinbt * ci;
+    if (xabs(p.cost) < R(1)) {
+      p.sint = xabs(xsqrt(R(1) - p.cost * p.cost));
+      sini2 = si_ * sintp / p.sint;
+      const R bott = p.sint * sinbt;
+      cosi2 = costp / bott - p.cost * bmu / bott;
+      if (cosi2 >= R(1)) { cosi2 = R(1); sini2 = R(0); }
+      if (cosi2 <= R(-1)) { cosi2 = R(-1); sini2 = R(0); }
+    } else {
+      if (p.cost >= R(1)) { p.cost = R(1); cosi2 = R(-1); }
+      if (p.cost <= R(-1)) { p.cost = R(-1); cosi2 = R(1); }
+      p.sint = R(0); sini2 = R(0);
+    }
+  }
+  R cosdph = upper ? -cosi2 * ci + sini2 * si_ * bmu : -ci * cosi2 + si_ * sini2 * bmu;
+  if (xabs(cosdph) > R(1)) cosdph = cosdph > R(1) ? R(1) : R(-1);
+  p.phi = upper ? phip + xacos(cosdph) : phip - xacos(cosdph);
+  if (p.phi > (R)kR2p) p.phi -= (R)kR2p;
+  if (p.phi < R(0)) p.phi += (R)kR2p;
+  R si = p.sip, sq = p.sqp, su = p.sup, sv = p.svp;
+  mueller<R>(upper, p1, p2, p3, s2x, c2x, sini2, cosi2, si, sq, su, sv);
+  p.sip = si / a; p.sqp = sq / a; p.sup = su / a; p.svp = sv / a;
+  p.cosp = xcos(p.phi);
+  p.sinp = xsin(p.phi);
+}
+
+__device__ __forceinline__ float xcheck(float x) { return x > 1.f ? 1.f : (x < -1.f ? -1.f : x); }
+__device__ __forceinline__ double xcheck(double x) { return x > 1.0 ? 1.0 : (x < -1.0 ? -1.0 : x); }
+
+// ---- findangle3.f90:31-67 (phi2 = the module phie = 0, as the reference calls it)
+template <class R>
+__device__ __forceinline__ void findangle3(R cost1, R sint1, R phi1, R cosp1, R sinp1, R cost2, R sint2, R phi2,
+                                           R cosp2, R sinp2, R& costnew, R& ri1) {
+  costnew = xcheck(cost1 * cost2 + (sint1 * sint2 * (cosp1 * cosp2 + sinp1 * sinp2)));
+  const R sintnew = xsqrt(R(1) - costnew * costnew);
+  ri1 = R(0);
+  if (sint1 > R(1.e-8) && sintnew > R(1.e-8)) {
+    const R cosx = xcheck((cost2 - (cost1 * costnew)) / (sint1 * sintnew));
+    const R x = xacos(cosx);
+    if (phi2 > phi1) ri1 = (phi2 - phi1) > (R)kPi ? x : (R)kR2p - x;
+    else ri1 = (phi1 - phi2) > (R)kPi ? (R)kR2p - x : x;
+  }
+}
+
+// ---- stokespeel.f90:49-376 -----------------------------------------------------------
+template <class R>
+__device__ __forceinline__ void stokespeel(R g, R pl, R& sip, R& sqp, R& sup, R& svp, R cost, R sint, R ri1, R bmu,
+                                           R costp, R sintp) {
+  R cosb2 = bmu * bmu;
+  R p1, p2, p3;
+  dustmat<R>(g, pl, bmu, cosb2, p1, p2, p3);
+  if (xabs(bmu) > R(1)) { bmu = bmu > R(1) ? R(1) : R(-1); cosb2 = R(1); }
+  const R sinbt = xsqrt(R(1) - cosb2);
+  const bool upper = ri1 > (R)kPi;
+  const R ang = upper ? (R)kR2p - ri1 : ri1;
+  R ci = xcos(ang), si_ = xsin(ang);
+  if (bmu == R(1)) return;
+  const R s2x = R(2) * si_ * ci, c2x = R(2) * ci * ci - R(1);
+  R cosi2 = R(0), sini2 = R(0);
+  if (bmu == R(-1)) {
+    si_ = R(1); sini2 = R(1); ci = R(0); cosi2 = R(0);
+  } else if (xabs(cost) < R(1)) {
+    sini2 = si_ * sintp / sint;
+    const R bott = sint * sinbt;
+    cosi2 = costp / bott - cost * bmu / bott;
+    if (cosi2 >= R(1)) { cosi2 = R(1); sini2 = R(0); }
+    if (cosi2 <= R(-1)) { cosi2 = R(-1); sini2 = R(0); }
+  } else {
+    if (cost >= R(1)) cosi2 = R(-1);
+    if (cost <= R(-1)) cosi2 = R(1);
+    sini2 = R(0);
+  }
+  mueller<R>(upper, p1, p2, p3, s2x, c2x, sini2, cosi2, sip, sqp, sup, svp);
+}
+
+__device__ __forceinline__ int nu_bin(const RunArgs& a, double nub) {
+  int inub = (int)((double)a.nfreq * log(nub / a.numin) / a.lnurat) + 1;
+  return inub < 1 ? 1 : (inub > a.nfreq ? a.nfreq : inub);
+}
+
+__device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, int64_t b, double i, double q, double u,
+                                     double v, double ss, double sq) {
+  atomicAdd(base + b, fx(i, ss));
+  atomicAdd(base + stride + b, fx(q, ss));
+  atomicAdd(base + 2 * stride + b, fx(u, ss));
+  atomicAdd(base + 3 * stride + b, fx(v, ss));
+  atomicAdd(base + 4 * stride + b, fx(i * i, sq));
+  atomicAdd(base + 5 * stride + b, fx(q * q, sq));
+  atomicAdd(base + 6 * stride + b, fx(u * u, sq));
+  atomicAdd(base + 7 * stride + b, fx(v * v, sq));
+  atomicAdd(base + 8 * stride + b, 1ull);
+}
+
+// ---- peeloff_3d.f90:52-286: one observer direction ------------------------------------
+template <class R>
+__device__ void peeloff(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                        const Pkt<R>& p, R sip, int iflag, int idust2, int k, Local& L) {
+  double xp1 = p.x, yp1 = p.y, zp1 = p.z;
+  int ir = p.ir, it = p.it, ip = p.ip;
+  int on_wall = p.on_wall;
+  R sqp = p.sqp, sup = p.sup, svp = p.svp;
+  const double* pd = a.peeldir + 4 * k;
+  const R coste = (R)__ldg(pd), sinte = (R)__ldg(pd + 1), cospe = (R)__ldg(pd + 2), sinpe = (R)__ldg(pd + 3);
+  const R ux1 = sinte * cospe, uy1 = sinte * sinpe, uz1 = coste;
+  L.c[HC3D_CNT_PEELS]++;
+  if (on_wall) {
+    const double rsq1 = xp1 * xp1 + yp1 * yp1 + zp1 * zp1;
+    const bool inner_wall = fabs(rsq1 - __ldg(m.r2arr + ir - 1)) < fabs(rsq1 - __ldg(m.r2arr + ir));
+    const bool outwards = (double)ux1 * xp1 + (double)uy1 * yp1 + (double)uz1 * zp1 > 0.0;
+    if (inner_wall && !outwards) {
+      if (ir == 1) return;
+      ir = ir - 1;
+    }
+    if (!inner_wall && outwards) ir = ir + 1;
+  }
+  double tsum = 0.0;  // FP64 escape tau in both forms
+  const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  for (int n = 0;; ++n) {
+    if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
+      L.c[HC3D_CNT_STUCK]++;
+      return;
+    }
+    R dt;
+    int iface;
+    if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
+      L.c[HC3D_CNT_STUCK]++;
+      return;
+    }
+    const int64_t c = cidx(m, ir, it, ip);
+    const Rho<R> rho = load_rho<R>(m, c);
+    const unsigned mask = __ldg(m.peelmask + c);
+    R opac = R(0);
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s)
+      if (mask & (1u << s)) opac += p.kapd[s] * rho.v[s];
+    tsum += (double)(opac * dt);
+    L.c[HC3D_CNT_CROSS_PEEL]++;
+    if (tsum > kTauMax) return;
+    step_index(m.npg, iface, ir, it, ip);
+    xp1 += (double)dt * (double)ux1;
+    yp1 += (double)dt * (double)uy1;
+    zp1 += (double)dt * (double)uz1;
+    on_wall = 1;
+    if (ir == m.nrg) break;
+    if (ir == 0) return;
+  }
+  const R factor = (R)exp(-tsum);
+  sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
+  if (iflag == 1) {
+    R bmu, ri1;
+    findangle3<R>(p.cost, p.sint, p.phi, p.cosp, p.sinp, coste, sinte, R(0), cospe, sinpe, bmu, ri1);
+    stokespeel<R>(p.g[idust2], p.pl[idust2], sip, sqp, sup, svp, coste, sinte, ri1, bmu, p.cost, p.sint);
+  }
+  const double cte = (double)coste, ste = (double)sinte, cpe = (double)cospe, spe = (double)sinpe;
+  const double yimage = zp1 * ste - yp1 * cte * spe - xp1 * cte * cpe;
+  const double ximage = yp1 * cpe - xp1 * spe;
+  const int ix = (int)((ximage + a.rmaxi) / a.fractxh) + 1;
+  const int iy = (int)((yimage + a.rmaxi) / a.fractxh) + 1;
+  const double rho2 = ximage * ximage + yimage * yimage;
+  const int inub = nu_bin(a, p.nub);
+  const int i_inter = iflag == 1 ? 2 : (p.i_orig == 1 ? 1 : 3);
+  const int indx[3] = {1, 1 + p.i_orig, 5 + i_inter};
+  const double dsip = (double)sip, dsqp = (double)sqp, dsup = (double)sup, dsvp = (double)svp;
+  for (int ia = 1; ia <= a.nap; ++ia) {
+    if (rho2 < __ldg(a.aperture2 + ia - 1)) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int64_t b = (int64_t)(inub - 1) + (int64_t)a.nfreq * (k + (int64_t)a.npeel * ((ia - 1) + (int64_t)a.nap * (indx[q] - 1)));
+        add9(t.psed, d.npsed, b, dsip, dsqp, dsup, dsvp, t.stokes_scale, t.square_scale);
+      }
+    }
+  }
+  if (a.image && ix <= a.nx && iy <= a.nx && ix > 0 && iy > 0) {
+    const int64_t b = (int64_t)k + (int64_t)a.npeel * ((ix - 1) + (int64_t)a.nx * (iy - 1));
+    atomicAdd(t.img + b, fx(dsip, t.stokes_scale));
+    atomicAdd(t.img + d.nimg + b, fx(dsqp, t.stokes_scale));
+    atomicAdd(t.img + 2 * d.nimg + b, fx(dsup, t.stokes_scale));
+    atomicAdd(t.img + 3 * d.nimg + b, fx(dsvp, t.stokes_scale));
+  }
+}
+
+// ---- lucydustfreq.f90:19-157 (FP64) --------------------------------------------------
+template <class R>
+__device__ double lucydustfreq(const DevModel& m, double T0, int id, Rng& rng) {
+  const int nT = m.nT, nnu = m.nnu;
+  const double* K = m.kapBint + (size_t)id * nT * nnu;
+  const double lT0 = log(T0);
+  const double xi = (double)ran<R>(rng);
+  const double l1 = __ldg(m.lTint), lN = __ldg(m.lTint + nT - 1);
+  int j = (int)((double)(nT - 1) * (lT0 - l1) / (lN - l1)) + 1;
+  j = j < 1 ? 1 : (j > nT - 1 ? nT - 1 : j);
+  double f = (lT0 - __ldg(m.lTint + j - 1)) / (__ldg(m.lTint + j) - __ldg(m.lTint + j - 1));
+  f = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
+#define KB(jj, ii) __ldg(K + (size_t)((jj) - 1) + (size_t)nT * ((ii) - 1))
+  int i0 = 1, i1 = nnu;
+  double P0 = (1.0 - f) * KB(j, i0) + f * KB(j + 1, i0);
+  if (xi < P0) return P0 > 0.0 ? T0 * xi * __ldg(m.nuint) / P0 : T0 * __ldg(m.nuint);
+  double P1 = (1.0 - f) * KB(j, i1) + f * KB(j + 1, i1);
+  if (P1 > 1.0) P1 = 1.0;
+  if (xi >= P1) {
+    if (P1 < 1.0 && xi < 1.0) return T0 * __ldg(m.nuint + nnu - 1) * (1.0 - P1) / (1.0 - xi);
+    return T0 * __ldg(m.nuint + nnu - 1);
+  }
+  while (i1 - i0 > 1) {
+    const int i = (i0 + i1) / 2;
+    double P = (1.0 - f) * KB(j, i) + f * KB(j + 1, i);
+    if (P > 1.0) P = 1.0;
+    if (P < P0) { P0 = P; i0 = i; }
+    if (P > P1) { P1 = P; i1 = 1; }
+    if (P > xi) { i1 = i; P1 = P; }
+    else { i0 = i; P0 = P; }
+  }
+#undef KB
+  if (xi < P0) f = 0.0;
+  else if (xi > P1) f = 1.0;
+  else if (P0 <= 0.0) f = 0.5;
+  else if (P1 <= 0.0 || xi <= 0.0) { }
+  else f = log(xi / P0) / log(P1 / P0);
+  const double n0 = __ldg(m.nuint + i0 - 1), n1 = __ldg(m.nuint + i1 - 1);
+  return T0 * n0 * pow(n1 / n0, f);
+}
+
+// ---- atmosfreq, starbarb.f90:120-156 (FP64) -------------------------------------------
+template <class R>
+__device__ double atmosfreq(const DevModel& m, Rng& rng) {
+  const double xi = (double)ran<R>(rng);
+  // locate2 (nr.f:152-171) on the increasing hnuint
+  const int n = m.nhnu;
+  int jl = 0, ju = n + 1;
+  while (ju - jl > 1) {
+    const int jm = (ju + jl) / 2;
+    if (xi > __ldg(m.hnuint + jm - 1)) jl = jm; else ju = jm;
+  }
+  int i = jl < 1 ? 1 : (jl > n - 1 ? n - 1 : jl);
+  if (i > 1) {
+    const double l0 = __ldg(m.lognu + i - 1), l1 = __ldg(m.lognu + i);
+    const double h0 = __ldg(m.loghnu + i - 1), h1 = __ldg(m.loghnu + i);
+    return pow(10.0, l0 + (l1 - l0) * (log10(xi) - h0) / (h1 - h0));
+  }
+  const double a0 = __ldg(m.atmosnu + i - 1), a1 = __ldg(m.atmosnu + i);
+  const double c0 = __ldg(m.hnuint + i - 1), c1 = __ldg(m.hnuint + i);
+  return a0 + (a1 - a0) * (xi - c0) / (c1 - c0);
+}
+
+__device__ __forceinline__ int locate_dev(const double* xx, int n, double x) {
+  int jl = 0, ju = n + 1;
+  const bool asc = __ldg(xx + n - 1) > __ldg(xx);
+  while (ju - jl > 1) {
+    const int jm = (ju + jl) / 2;
+    if (asc == (x > __ldg(xx + jm - 1))) jl = jm; else ju = jm;
+  }
+  if (jl == 0 && x == __ldg(xx)) jl = 1;
+  return jl;
+}
+
+// ---- propagate.f90:206-319 escape binning ----------------------------------------
+template <class R>
+__device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArgs& a, const Pkt<R>& p, double xpold,
+                           double ypold, double zpold, int iflag, int iscat, Local& L) {
+  int it = (int)((double)a.nmu * (1.0 - (double)p.cost) / 2.0) + 1;
+  it = it > a.nmu ? a.nmu : (it < 1 ? 1 : it);
+  double phi = (double)p.phi;
+  if (phi < 0.0) phi += kR2p;
+  int ip = (int)((double)a.nph * phi / kR2p) + 1;
+  ip = ip > a.nph ? a.nph : (ip < 1 ? 1 : ip);
+  const double dmu = 2.0 / (double)a.nmu;
+  const double u = 1.0 - dmu * ((double)it - 0.5);
+  const double sini = sqrt(1.0 - u * u);
+  const double cp = (double)p.cosp, sp = (double)p.sinp;
+  const double x = ypold * cp - xpold * sp;
+  const double y = zpold * sini - ypold * u * sp - xpold * u * cp;
+  const double rho2 = x * x + y * y;
+  if (rho2 < __ldg(a.aperture2 + a.nap - 1) * 1.0001) {
+    L.c[HC3D_CNT_FLUX]++;
+    if (iflag == 1) {
+      L.c[HC3D_CNT_SFLUX]++;
+      L.c[HC3D_CNT_NSCAT] += (unsigned long long)iscat;
+    }
+  }
+  const int inub = nu_bin(a, p.nub);
+  const int i_inter = iflag == 1 ? 2 : (p.i_orig == 1 ? 1 : 3);
+  const int indx[3] = {1, 1 + p.i_orig, 5 + i_inter};
+  const double si = (double)p.sip, sq = (double)p.sqp, su = (double)p.sup, sv = (double)p.svp;
+  const bool count = !(iflag == 0 && p.i_orig == 4);
+  for (int ia = 1; ia <= a.nap; ++ia) {
+    if (rho2 < __ldg(a.aperture2 + ia - 1) && count) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int64_t b = (int64_t)(inub - 1) +
+                          (int64_t)a.nfreq * ((it - 1) + (int64_t)a.nmu * ((ip - 1) + (int64_t)a.nph * ((ia - 1) + (int64_t)a.nap * (indx[q] - 1))));
+        add9(t.sed, d.nsed, b, si, sq, su, sv, t.stokes_scale, t.square_scale);
+      }
+    }
+  }
+  if (count) L.c[HC3D_CNT_SUMSUB] += fx(si, t.stokes_scale);
+  L.c[HC3D_CNT_SUMALL] += fx(si, t.stokes_scale);
+  if (iflag == 1) L.c[HC3D_CNT_SCOUNT]++;
+  L.c[HC3D_CNT_ESCAPED]++;
+}
+
+__device__ __forceinline__ void set_status(const RunArgs& a, int code) {
+  if (a.status) atomicCAS(a.status, 0, code);
+}
+
+// ---- one stellar packet: newdisktherm.F90:256-377 + propagate.f90:27-204 ------------
+template <class R>
+__device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
+                           Local& L, Tracer& tr) {
+  Pkt<R> p;
+  p.on_wall = 0;
+  // initpspot (spot-free) + initp_sample (limb = 0) + initp_transform
+  p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+  for (;;) {
+    const R xran = ran<R>(rng);
+    p.cosb = R(1) - R(2) * xran;
+    p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
+    if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
+  }
+  p.lp = (R)kR2p * ran<R>(rng);
+  p.cost = xsqrt(ran<R>(rng));
+  p.sint = xsqrt(R(1) - p.cost * p.cost);
+  p.phi = (R)kR2p * ran<R>(rng);
+  p.cosp = xcos(p.phi);
+  p.sinp = xsin(p.phi);
+  if (xabs(p.cosb) < R(0.9999999)) {
+    R costi = p.cost * p.cosb - p.sint * p.sinb * p.cosp;
+    if (xabs(costi) > R(1)) {
+      if (costi > R(1)) costi = R(1);
+      if (p.cost < R(-1)) costi = R(-1);
+    }
+    const R sinti = xsqrt(R(1) - costi * costi);
+    R phinew;
+    if (sinti > R(0.0000001)) {
+      R cospn = (p.cost - costi * p.cosb) / (sinti * p.sinb);
+      if (xabs(cospn) > R(1)) cospn = cospn < R(0) ? R(-1) : R(1);
+      if (p.phi < (R)kPi) {
+        phinew = xacos(cospn);
+        if (phinew > (R)kPi) phinew = (R)kPi;
+      } else {
+        phinew = (R)kR2p - xacos(cospn);
+        if (phinew < (R)kPi) phinew = (R)kPi;
+      }
+    } else {
+      phinew = R(0);
+    }
+    p.phi = phinew; p.cost = costi; p.sint = sinti;
+  } else if (p.cosb < R(0)) {
+    p.cost = -p.cost;
+  }
+  p.phi = p.phi + p.lp;
+  if (p.phi > (R)kR2p) p.phi -= (R)kR2p;
+  if (p.phi < R(0)) p.phi += (R)kR2p;
+  p.sinp = xsin(p.phi);
+  p.cosp = xcos(p.phi);
+  p.nub = atmosfreq<R>(m, rng);
+  p.i_orig = 1;
+  opacset<R>(m, p, p.nub, a.rstar_cm);
+  const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
+  p.z = (double)p.cosb;
+  const double rp_ = (double)p.sinb;
+  p.x = rp_ * (double)coslp;
+  p.y = rp_ * (double)sinlp;
+  p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
+  p.ir = 1;
+  p.on_wall = 1;
+  p.it = locate_dev(m.thetarr, m.ntg, acos((double)p.cosb));
+  p.ip = locate_dev(m.phiarr, m.npg, (double)p.lp);
+  p.it = p.it < 1 ? 1 : (p.it > m.ntg - 1 ? m.ntg - 1 : p.it);
+  p.ip = p.ip < 1 ? 1 : (p.ip > m.npg - 1 ? m.npg - 1 : p.ip);
+  tr.add(0, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+  if (a.ipeel == 1) {
+    for (int k = 0; k < a.npeel; ++k) {
+      const double* pd = a.peeldir + 4 * k;
+      const R coste = (R)__ldg(pd), sinte = (R)__ldg(pd + 1), cospe = (R)__ldg(pd + 2), sinpe = (R)__ldg(pd + 3);
+      const R cosnorm = p.cosb * coste + (p.sinb * sinte * (cospe * coslp + sinpe * sinlp));
+      const R sipnew = R(4) * p.sip * cosnorm;
+      if (cosnorm > R(0)) peeloff<R>(m, t, d, a, p, sipnew, 0, 0, k, L);
+    }
+  }
+
+  // ---- propagate ----
+  double xpold = p.x, ypold = p.y, zpold = p.z;
+  int iflag = 0, iscat = 0, iint = 0;
+  int64_t ntot = 0;
+  R tau = -xlog(ran<R>(rng));
+  int st = tauint<R>(m, t, p, tau, L, tr);
+  if (st == TI_ESCAPE) {
+    tr.add(3, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    bin_escape<R>(t, d, a, p, xpold, ypold, zpold, iflag, iscat, L);
+    return;
+  }
+  if (st == TI_STAR) { L.c[HC3D_CNT_AFLUX]++; tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z); return; }
+  if (st == TI_FAULT) { L.c[HC3D_CNT_STUCK]++; set_status(a, 1); return; }
+  int idust2 = select_dust<R>(m, p, rng);
+  if (idust2 < 0) { set_status(a, 2); return; }
+  L.c[HC3D_CNT_TOT]++;
+  for (;;) {
+    const int64_t c = cidx(m, p.ir, p.it, p.ip);
+    L.c[HC3D_CNT_EVENTS]++;
+    ntot++;
+    if (ran<R>(rng) <= p.albedo[idust2]) {  // scattered
+      iflag = 1; iscat++; iint++;
+      if (a.ipeel == 1)
+        for (int k = 0; k < a.npeel; ++k) peeloff<R>(m, t, d, a, p, p.sip, 1, idust2, k, L);
+      stokes<R>(p, idust2, rng);
+      tr.add(5, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
+      atomicAdd(t.dbig + c, 1u);
+      p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
+      atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
+      const double tave = __ldg(m.tdust + 4 * c + idust2);
+      p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+      p.cost = R(1) - R(2) * ran<R>(rng);
+      p.sint = xsqrt(R(1) - p.cost * p.cost);
+      p.phi = (R)kR2p * ran<R>(rng);
+      p.cosp = xcos(p.phi);
+      p.sinp = xsin(p.phi);
+      p.nub = lucydustfreq<R>(m, tave, idust2, rng);
+      iflag = 0;
+      opacset<R>(m, p, p.nub, a.rstar_cm);
+      if (a.ipeel == 1)
+        for (int k = 0; k < a.npeel; ++k) peeloff<R>(m, t, d, a, p, p.sip, 0, idust2, k, L);
+      iint++;
+      tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    }
+    tau = -xlog(ran<R>(rng));
+    xpold = p.x; ypold = p.y; zpold = p.z;
+    p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
+    const int pir = p.ir, pit = p.it, pip = p.ip;
+    st = tauint<R>(m, t, p, tau, L, tr);
+    if (st == TI_ESCAPE) break;
+    if (st == TI_STAR) { L.c[HC3D_CNT_AFLUX]++; tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z); return; }
+    if (st == TI_FAULT) { L.c[HC3D_CNT_STUCK]++; set_status(a, 1); return; }
+    if (p.ir != pir || p.it != pit || p.ip != pip) iint = 0;
+    if (iint > a.iintmax || (a.max_interactions > 0 && ntot >= a.max_interactions)) {
+      atomicAdd(t.killed + cidx(m, p.ir, p.it, p.ip), 1u);
+      L.c[HC3D_CNT_ABFLUX]++;
+      tr.add(7, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+      return;
+    }
+    idust2 = select_dust<R>(m, p, rng);
+    if (idust2 < 0) { set_status(a, 2); return; }
+  }
+  tr.add(3, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+  bin_escape<R>(t, d, a, p, xpold, ypold, zpold, iflag, iscat, L);
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, TallyDims d, RunArgs a) {
+  Local L;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  if (a.inj) {
+    // trace harness: one thread per traced packet, draws from the injected list
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < a.np) {
+      Rng rng;
+      rng_init(rng, a.key0, a.key1, (uint64_t)(a.packet_offset + k));
+      rng.inj = a.inj + (size_t)k * a.ninj;
+      rng.ninj = a.ninj;
+      Tracer tr{reinterpret_cast<TraceRec*>(a.trace) + (size_t)k * a.max_rec, a.max_rec, 0};
+      run_packet<R>(m, t, d, a, rng, L, tr);
+      a.nrec[k] = tr.n;
+    }
+  } else {
+    Tracer tr{nullptr, 0, 0};
+    for (;;) {
+      const unsigned long long pid = atomicAdd(a.work, 1ull);
+      if (pid >= (unsigned long long)a.np) break;
+      Rng rng;
+      rng_init(rng, a.key0, a.key1, (uint64_t)(a.packet_offset + (int64_t)pid));
+      run_packet<R>(m, t, d, a, rng, L, tr);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 15; ++i)
+    if (L.c[i]) atomicAdd(t.counters + i, L.c[i]);
+}
+
+}  // namespace dev
+}  // namespace hc3d

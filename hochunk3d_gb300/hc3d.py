@@ -1,0 +1,433 @@
+"""ctypes binding of the GB300 photon-packet Monte Carlo library (libhc3d.so).
+
+The Python host mirrors the Fortran caller of ``disk()``:
+
+* :class:`Model` -- setup/reapar/dustinit/atmosinit/gridset of a ``.par``
+  file (newtts.F90:141-290), built by the library's C++ host code;
+* :class:`Context` -- one GPU context holding tables, grid and tallies;
+  :meth:`Context.disk` is one call of ``disk(converge, iter, i1)``
+  (newdisktherm.F90:1): the packet loop on the GPU followed by the Lucy
+  temperature update (``tfinal``, newdisktherm.F90:557);
+* :func:`tts` -- the whole program ``tts`` (newtts.F90) in the library.
+
+There is no CPU fallback: every function that computes needs ``libhc3d.so``
+and a CUDA device, and raises :class:`Hc3dError` otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libhc3d.so"
+
+NDG = 8
+NO = 8
+PREC_MIXED = 0
+PREC_FP64 = 1
+
+ERRORS = {
+    -1: "HC3D_ERR_INVALID", -2: "HC3D_ERR_CUDA", -3: "HC3D_ERR_NOMEM", -4: "HC3D_ERR_STATE",
+    -5: "HC3D_ERR_DEVICE", -6: "HC3D_ERR_IO", -7: "HC3D_ERR_UNSUPPORTED", -8: "HC3D_ERR_TIMEOUT",
+}
+
+CNT = {
+    "flux": 0, "sflux": 1, "nscat": 2, "scount": 3, "tot": 4, "abflux": 5, "aflux": 6, "sumsub": 7,
+    "sumall": 8, "escaped": 9, "cross_prop": 10, "cross_peel": 11, "events": 12, "peels": 13, "stuck": 14,
+    "status": 15,
+}
+
+P = C.POINTER
+dp = P(C.c_double)
+ip_ = P(C.c_int)
+i64p = P(C.c_int64)
+i32p = P(C.c_int32)
+
+
+class Hc3dError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        self.code = code
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+
+
+class DeviceOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("block_size", C.c_int), ("grid_blocks", C.c_int)]
+
+
+class DustTables(C.Structure):
+    _fields_ = [
+        ("ndg", C.c_int), ("nlammax", C.c_int), ("nlambda", ip_),
+        ("nudust", dp), ("kappad", dp), ("adust", dp), ("gdust", dp), ("pldust", dp), ("kappav", dp),
+        ("nT", C.c_int), ("nnu", C.c_int), ("lTint", dp), ("nuint", dp), ("kapBint", dp), ("kappap", dp),
+        ("tsub", C.c_double), ("nhnu", C.c_int), ("hnuint", dp), ("atmosnu", dp), ("lognu", dp), ("loghnu", dp),
+    ]
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("nrg", C.c_int), ("ntg", C.c_int), ("npg", C.c_int), ("ndg", C.c_int),
+        ("rarr", dp), ("r2arr", dp), ("thetarr", dp), ("costarr", dp), ("tan2arr", dp),
+        ("phiarr", dp), ("aarr", dp), ("barr", dp),
+        ("densarr", dp), ("massarr", dp), ("vcell", dp), ("tdust", dp),
+    ]
+
+
+class RunParams(C.Structure):
+    _fields_ = [
+        ("np", C.c_int64), ("packet_offset", C.c_int64), ("seed", C.c_uint64), ("iter", C.c_int),
+        ("ipeel", C.c_int), ("npeel", C.c_int), ("thete", dp), ("phie", dp),
+        ("nfreq", C.c_int), ("nmu", C.c_int), ("nph", C.c_int), ("nap", C.c_int), ("nxhst", C.c_int),
+        ("rmaxi", C.c_double), ("aperture2", dp), ("numin", C.c_double), ("numax", C.c_double),
+        ("rstar_cm", C.c_double), ("tstar", C.c_double), ("limb", C.c_int), ("iintmax", C.c_int),
+        ("max_interactions", C.c_int64), ("image", C.c_int),
+    ]
+
+
+class Tallies(C.Structure):
+    _fields_ = [(n, i64p) for n in ("si", "sq", "su", "sv", "si2", "sq2", "su2", "sv2", "nums",
+                                     "ti", "tq", "tu", "tv", "ti2", "tq2", "tu2", "tv2", "numt",
+                                     "image_i", "image_q", "image_u", "image_v",
+                                     "nabs", "dtauabs", "jmean")] + [
+        ("killed", i32p), ("dbig", i32p), ("counters", C.c_int64 * 16),
+        ("stokes_scale", C.c_double), ("square_scale", C.c_double), ("path_scale", C.c_double),
+    ]
+
+
+class TraceRec(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ir", C.c_int32), ("it", C.c_int32), ("ip", C.c_int32),
+                ("iface", C.c_int32), ("pad", C.c_int32), ("tsum", C.c_double),
+                ("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+TRACE_DTYPE = np.dtype([("kind", "<i4"), ("ir", "<i4"), ("it", "<i4"), ("ip", "<i4"), ("iface", "<i4"),
+                        ("pad", "<i4"), ("tsum", "<f8"), ("x", "<f8"), ("y", "<f8"), ("z", "<f8")])
+
+
+class ModelInfo(C.Structure):
+    _fields_ = [
+        ("np", C.c_int64), ("npmin", C.c_int64), ("np_lucy", C.c_int64), ("nimin", C.c_int), ("nimax", C.c_int),
+        ("ipeel", C.c_int), ("ilucy", C.c_int), ("ndg_active", C.c_int), ("ltot", C.c_double),
+        ("tstar_k", C.c_double), ("rstar_rsun", C.c_double), ("autors", C.c_double), ("rminsub", C.c_double),
+        ("massdisk", C.c_double), ("massenv", C.c_double), ("ncells", C.c_int64),
+    ]
+
+
+class TtsStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int), ("max_rel_change", C.c_double),
+                ("seconds_lucy", C.c_double), ("seconds_final", C.c_double), ("packets_total", C.c_int64),
+                ("counters", C.c_int64 * 16)]
+
+
+# every symbol the public headers declare, with its ctypes signature
+SIGNATURES = {
+    "hc3d_create": (C.c_int, [P(C.c_void_p), P(DeviceOpts)]),
+    "hc3d_destroy": (None, [C.c_void_p]),
+    "hc3d_get_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "hc3d_version": (C.c_char_p, []),
+    "hc3d_load_tables": (C.c_int, [C.c_void_p, P(DustTables)]),
+    "hc3d_load_grid": (C.c_int, [C.c_void_p, P(Grid)]),
+    "hc3d_zero_tallies": (C.c_int, [C.c_void_p]),
+    "hc3d_run_iteration": (C.c_int, [C.c_void_p, P(RunParams)]),
+    "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
+    "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
+    "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
+    "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
+    "hc3d_trace_packets": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, dp, C.c_int, P(TraceRec), C.c_int, i32p]),
+    "hc3d_model_create": (C.c_int, [P(C.c_void_p), C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t]),
+    "hc3d_model_destroy": (None, [C.c_void_p]),
+    "hc3d_model_views": (C.c_int, [C.c_void_p, P(DustTables), P(Grid), P(RunParams), P(ModelInfo)]),
+    "hc3d_model_set_tdust": (C.c_int, [C.c_void_p, dp]),
+    "hc3d_tts": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P(DeviceOpts), P(TtsStats), C.c_char_p, C.c_size_t]),
+    "hc3d_write_synthetic_dust": (C.c_int, [C.c_char_p]),
+    "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
+}
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    """Load libhc3d.so (built by ``__graft_entry__.build()``); fail loudly if absent."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise Hc3dError(-4, f"{LIB_PATH} is not built; run hochunk3d_gb300.build.build_library()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a: np.ndarray, t=C.c_double):
+    return a.ctypes.data_as(P(t))
+
+
+def _arr(ptr, n: int, dtype=np.float64) -> np.ndarray:
+    if not ptr or n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+def tally_scales(np_: int) -> tuple[float, float, float]:
+    """Fixed-point scales the library picks for an epoch whose first call runs np_ packets."""
+    budget = max(int(np_), 1 << 20) * 16.0
+    L = 0
+    while float(1 << L) < budget and L < 62:
+        L += 1
+    sb = max(16, min(40, 58 - L))
+    pb = max(12, min(32, 52 - L))
+    return math.ldexp(1.0, sb), math.ldexp(1.0, sb - 8), math.ldexp(1.0, pb)
+
+
+# ---------------------------------------------------------------------------
+class Model:
+    """A model built from a .par file by the library's host setup code.
+
+    The numpy attributes are copies of the library's arrays in the reference's
+    Fortran (column-major) layout; ``tables``/``grid``/``params`` are ctypes
+    views that point into arrays this object keeps alive.
+    """
+
+    def __init__(self, par_path: str | os.PathLike, par_dir: str | os.PathLike | None = None):
+        L = lib()
+        h = C.c_void_p()
+        err = C.create_string_buffer(1024)
+        rc = L.hc3d_model_create(C.byref(h), str(par_path).encode(),
+                                 None if par_dir is None else str(par_dir).encode(), err, 1024)
+        if rc != 0:
+            raise Hc3dError(rc, err.value.decode())
+        self._h = h
+        t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
+        L.hc3d_model_views(h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
+        self.info = info
+        nrg, ntg, npg, ndg = g.nrg, g.ntg, g.npg, g.ndg
+        n4 = nrg * ntg * npg
+        self.shape4 = (nrg, ntg, npg, ndg)
+        self.shape3 = (nrg, ntg, npg)
+        # grid arrays (copies, Fortran order)
+        self.rarr = _arr(g.rarr, nrg); self.r2arr = _arr(g.r2arr, nrg)
+        self.thetarr = _arr(g.thetarr, ntg); self.costarr = _arr(g.costarr, ntg); self.tan2arr = _arr(g.tan2arr, ntg)
+        self.phiarr = _arr(g.phiarr, npg); self.aarr = _arr(g.aarr, npg); self.barr = _arr(g.barr, npg)
+        self.densarr = _arr(g.densarr, n4 * ndg).reshape(self.shape4, order="F")
+        self.massarr = _arr(g.massarr, n4 * ndg).reshape(self.shape4, order="F")
+        self.vcell = _arr(g.vcell, n4).reshape(self.shape3, order="F")
+        self.tdust = _arr(g.tdust, n4 * ndg).reshape(self.shape4, order="F")
+        # dust tables
+        self.ndg_tab, self.nlammax, self.nT, self.nnu, self.nhnu = t.ndg, t.nlammax, t.nT, t.nnu, t.nhnu
+        nl = t.nlammax * t.ndg
+        self.nlambda = _arr(t.nlambda, t.ndg, np.int32)
+        self.nudust = _arr(t.nudust, nl); self.kappad = _arr(t.kappad, nl); self.adust = _arr(t.adust, nl)
+        self.gdust = _arr(t.gdust, nl); self.pldust = _arr(t.pldust, nl); self.kappav = _arr(t.kappav, t.ndg)
+        self.lTint = _arr(t.lTint, t.nT); self.nuint = _arr(t.nuint, t.nnu)
+        self.kapBint = _arr(t.kapBint, t.nT * t.nnu * t.ndg); self.kappap = _arr(t.kappap, t.nT * t.ndg)
+        self.tsub = t.tsub
+        self.hnuint = _arr(t.hnuint, t.nhnu); self.atmosnu = _arr(t.atmosnu, t.nhnu)
+        self.lognu = _arr(t.lognu, t.nhnu); self.loghnu = _arr(t.loghnu, t.nhnu)
+        # run parameters
+        self.npeel = p.npeel
+        self.thete = _arr(p.thete, p.npeel); self.phie = _arr(p.phie, p.npeel)
+        self.aperture2 = _arr(p.aperture2, p.nap)
+        self._p = p
+        self.params = self.run_params()
+
+    # ctypes views over this object's numpy copies
+    @property
+    def tables(self) -> DustTables:
+        t = DustTables()
+        t.ndg, t.nlammax, t.nT, t.nnu, t.nhnu, t.tsub = self.ndg_tab, self.nlammax, self.nT, self.nnu, self.nhnu, self.tsub
+        t.nlambda = _ptr(self.nlambda, C.c_int)
+        for n in ("nudust", "kappad", "adust", "gdust", "pldust", "kappav", "lTint", "nuint", "kapBint", "kappap",
+                  "hnuint", "atmosnu", "lognu", "loghnu"):
+            setattr(t, n, _ptr(getattr(self, n)))
+        return t
+
+    @property
+    def grid(self) -> Grid:
+        g = Grid()
+        g.nrg, g.ntg, g.npg, g.ndg = self.shape4
+        for n in ("rarr", "r2arr", "thetarr", "costarr", "tan2arr", "phiarr", "aarr", "barr"):
+            setattr(g, n, _ptr(getattr(self, n)))
+        for n in ("densarr", "massarr", "vcell", "tdust"):
+            a = getattr(self, n)
+            assert a.flags.f_contiguous
+            setattr(g, n, a.ctypes.data_as(dp))
+        return g
+
+    def run_params(self, **over) -> RunParams:
+        q = RunParams()
+        for f, _ in RunParams._fields_:
+            setattr(q, f, getattr(self._p, f))
+        q.thete = _ptr(self.thete)
+        q.phie = _ptr(self.phie)
+        q.aperture2 = _ptr(self.aperture2)
+        for k, v in over.items():
+            setattr(q, k, v)
+        return q
+
+    def set_tdust(self, tdust: np.ndarray) -> None:
+        self.tdust = np.asfortranarray(tdust, dtype=np.float64).copy(order="F")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().hc3d_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+class Context:
+    """One GPU context: device tables, grid and tallies of the photon loop."""
+
+    def __init__(self, precision: int = PREC_MIXED, device: int = 0, block_size: int = 0, grid_blocks: int = 0):
+        L = lib()
+        h = C.c_void_p()
+        o = DeviceOpts(device, precision, block_size, grid_blocks)
+        rc = L.hc3d_create(C.byref(h), C.byref(o))
+        if rc != 0:
+            raise Hc3dError(rc, "hc3d_create failed (is a CUDA device visible?)")
+        self._h = h
+        self.precision = precision
+        self.model: Model | None = None
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            buf = C.create_string_buffer(1024)
+            lib().hc3d_get_error(self._h, buf, 1024)
+            raise Hc3dError(rc, buf.value.decode())
+
+    def load(self, model: Model) -> "Context":
+        t, g = model.tables, model.grid
+        self._check(lib().hc3d_load_tables(self._h, C.byref(t)))
+        self._check(lib().hc3d_load_grid(self._h, C.byref(g)))
+        self.model = model
+        return self
+
+    def zero(self) -> None:
+        self._check(lib().hc3d_zero_tallies(self._h))
+
+    def run(self, params: RunParams) -> None:
+        self._check(lib().hc3d_run_iteration(self._h, C.byref(params)))
+
+    def tallies(self, params: RunParams, grid: bool = True) -> dict:
+        m = self.model
+        nrg, ntg, npg, ndg = m.shape4
+        npeel = params.npeel if params.ipeel else 0
+        sed_shape = (params.nfreq, params.nmu, params.nph, params.nap, NO)
+        psed_shape = (params.nfreq, npeel, params.nap, NO)
+        img_shape = (npeel, params.nxhst, params.nxhst)
+        out = {}
+        T = Tallies()
+        keep = []
+
+        def buf(name, shape, dtype=np.int64, ctype=C.c_int64):
+            a = np.zeros(int(np.prod(shape)) if len(shape) else 0, dtype=dtype)
+            keep.append(a)
+            out[name] = (a, shape)
+            setattr(T, name, a.ctypes.data_as(P(ctype)))
+
+        for n in ("si", "sq", "su", "sv", "si2", "sq2", "su2", "sv2", "nums"):
+            buf(n, sed_shape)
+        if npeel:
+            for n in ("ti", "tq", "tu", "tv", "ti2", "tq2", "tu2", "tv2", "numt"):
+                buf(n, psed_shape)
+            if params.image:
+                for n in ("image_i", "image_q", "image_u", "image_v"):
+                    buf(n, img_shape)
+        if grid:
+            buf("nabs", (nrg, ntg, npg, ndg))
+            buf("dtauabs", (nrg, ntg, npg, ndg))
+            buf("jmean", (nrg, ntg, npg))
+            buf("killed", (nrg, ntg, npg), np.int32, C.c_int32)
+            buf("dbig", (nrg, ntg, npg), np.int32, C.c_int32)
+        self._check(lib().hc3d_get_tallies(self._h, C.byref(params), C.byref(T)))
+        res = {k: a.reshape(s, order="F") for k, (a, s) in out.items()}
+        res["counters"] = np.array(T.counters[:], dtype=np.int64)
+        res["stokes_scale"], res["square_scale"], res["path_scale"] = T.stokes_scale, T.square_scale, T.path_scale
+        return res
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t (as an int) of this context's kernels."""
+        return lib().hc3d_get_stream(self._h) or 0
+
+    def last_kernel_ms(self) -> float:
+        v = C.c_double(0)
+        self._check(lib().hc3d_last_kernel_ms(self._h, C.byref(v)))
+        return v.value
+
+    def lucy_update(self, ltot: float, np_: int, want_tdust: bool = True):
+        m = self.model
+        td = np.zeros(m.shape4, dtype=np.float64, order="F") if want_tdust else None
+        rel = C.c_double(0)
+        conv = C.c_int(0)
+        self._check(lib().hc3d_lucy_update(self._h, ltot, int(np_), None if td is None else td.ctypes.data_as(dp),
+                                           C.byref(rel), C.byref(conv)))
+        return td, rel.value, bool(conv.value)
+
+    def trace(self, params: RunParams, uniforms: np.ndarray, max_rec: int = 4096):
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        if u.ndim == 1:
+            u = u[None, :]
+        npkt, nu = u.shape
+        recs = np.zeros(npkt * max_rec, dtype=TRACE_DTYPE)
+        nrec = np.zeros(npkt, dtype=np.int32)
+        self._check(lib().hc3d_trace_packets(self._h, C.byref(params), npkt, _ptr(u), nu,
+                                             recs.ctypes.data_as(P(TraceRec)), max_rec, _ptr(nrec, C.c_int32)))
+        return [recs[k * max_rec: k * max_rec + nrec[k]] for k in range(npkt)]
+
+    def disk(self, converge: str, iter_: int, np_: int | None = None, ipeel: int | None = None,
+             packet_offset: int = 0):
+        """One call of disk(converge, iter, i1) (newdisktherm.F90:1): zero the
+        tallies (initarr(.false.)), run the packet loop, read the tallies and
+        solve the Lucy temperatures (tfinal).  Returns (tallies, converge,
+        max_rel_change, tdust)."""
+        m = self.model
+        n = m.info.np if np_ is None else np_
+        pe = (m.info.ipeel if converge == "yes" else 0) if ipeel is None else ipeel
+        params = m.run_params(np=n, iter=iter_, ipeel=pe, packet_offset=packet_offset)
+        self.zero()
+        self.run(params)
+        tal = self.tallies(params)
+        td, rel, conv = self.lucy_update(m.info.ltot, n)
+        m.set_tdust(td)
+        new = "yes" if (converge == "yes" or conv) else "no"
+        return tal, new, rel, td
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().hc3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tts(par_path, out_dir, par_dir=None, precision: int = PREC_MIXED, device: int = 0) -> TtsStats:
+    """Run program tts (newtts.F90) on the GPU and write its ASCII outputs."""
+    st = TtsStats()
+    err = C.create_string_buffer(1024)
+    o = DeviceOpts(device, precision, 0, 0)
+    Path(out_dir).mkdir(parents=True, exist_ok=True)
+    rc = lib().hc3d_tts(str(par_path).encode(), None if par_dir is None else str(par_dir).encode(),
+                        str(out_dir).encode(), C.byref(o), C.byref(st), err, 1024)
+    if rc != 0:
+        raise Hc3dError(rc, err.value.decode())
+    return st
+
+
+def version() -> str:
+    return lib().hc3d_version().decode()

@@ -1,0 +1,245 @@
+/*
+ * hc3d.h -- C-ABI of the GB300 photon-packet Monte Carlo loop.
+ *
+ * This library stands in for one Fortran subroutine of Hochunk3d:
+ *
+ *     subroutine disk(converge, iter, i1)            (newdisktherm.F90:1)
+ *
+ * called from the Lucy loop and the final peeled iteration of the driver
+ * (newtts.F90:312 and newtts.F90:349).  In the reference every input of
+ * disk() reaches it through Fortran module globals (tts_mod, grid_mod,
+ * dust_mod, opacin_mod, stokesvar_mod, out_mod).  Here the same data crosses
+ * the boundary explicitly, as plain pointers and sizes:
+ *
+ *   hc3d_load_tables   <- dust_mod / atmos_interp arrays built by dustinit
+ *                         (dust.f90:314), setemiss (dust.f90:394) and
+ *                         atmosinit (starbarb.f90:3)
+ *   hc3d_load_grid     <- grid_mod arrays built by gridset (gridset.f90:1)
+ *                         and initarr (initarr.f90:1)
+ *   hc3d_run_iteration <- the packet loop of disk() (newdisktherm.F90:194-449)
+ *                         with propagate (propagate.f90:1) and peeloff
+ *                         (peeloff_3d.f90:5)
+ *   hc3d_lucy_update   <- tfinal (called at newdisktherm.F90:557; the module
+ *                         is not shipped, restated from dusttemp.f90:30-50)
+ *                         followed by initarr(.false.) (initarr.f90:58-89)
+ *
+ * Conventions (the same as the Fortran arrays they replace):
+ *   - arrays are column-major (Fortran order), the first index fastest;
+ *   - grid indices are 1-based at the boundary (wall ir = 1..nrg);
+ *   - temperatures are in the reference's internal unit K/11605 (eV);
+ *   - lengths are in stellar radii, densities in g/cm^3;
+ *   - every entry point returns 0 on success and a negative HC3D_ERR_* code
+ *     otherwise; no C++ exception crosses the boundary; hc3d_get_error()
+ *     returns the last message of a context.
+ *
+ * Tallies are int64 fixed point: a value v is stored as llround(v * scale),
+ * so sums are exact and independent of the order in which packets finish.
+ * The scales are reported by hc3d_get_tallies().
+ */
+#ifndef HC3D_H
+#define HC3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HC3D_NDG 8  /* species slots, ndg in grid_mod.f90:13 */
+#define HC3D_NO 8   /* SED components all/star/disk/envelope/outside/direct/scattered/thermal, output.F90:232-239 */
+
+#define HC3D_OK 0
+#define HC3D_ERR_INVALID (-1)     /* bad argument or size */
+#define HC3D_ERR_CUDA (-2)        /* CUDA runtime error */
+#define HC3D_ERR_NOMEM (-3)       /* device or host allocation failed */
+#define HC3D_ERR_STATE (-4)       /* call out of order (e.g. run before load) */
+#define HC3D_ERR_DEVICE (-5)      /* a kernel reported a fault in its status word */
+#define HC3D_ERR_IO (-6)          /* file could not be read or written */
+#define HC3D_ERR_UNSUPPORTED (-7) /* option of the reference that this build leaves out */
+#define HC3D_ERR_TIMEOUT (-8)     /* a bounded wait ran out */
+
+#define HC3D_PREC_MIXED 0 /* FP32 walk/scatter/peel; FP64 radial quadratic, peel tau sum, Lucy root */
+#define HC3D_PREC_FP64 1  /* everything FP64: the all-FP64 GPU form */
+
+typedef struct hc3d_ctx hc3d_ctx;
+
+typedef struct hc3d_device_opts {
+  int device;      /* CUDA device ordinal */
+  int precision;   /* HC3D_PREC_MIXED or HC3D_PREC_FP64 */
+  int block_size;  /* threads per block of the transport kernel; 0 = default */
+  int grid_blocks; /* blocks of the persistent transport kernel; 0 = SMs x resident blocks */
+} hc3d_device_opts;
+
+/* dust_mod (dust_mod.f90:7-17) plus the stellar-spectrum CDF of atmos_interp
+ * (starbarb.f90:57-110).  All species slots 1..ndg must be described; a slot
+ * whose density is zero everywhere may repeat another slot's table. */
+typedef struct hc3d_dust_tables {
+  int ndg;                /* species slots described, 1..8 */
+  int nlammax;            /* leading dimension of the per-wavelength tables */
+  const int *nlambda;     /* (ndg) rows used per species */
+  const double *nudust;   /* (nlammax,ndg) frequency, decreasing with row */
+  const double *kappad;   /* (nlammax,ndg) kappa / kappa_V */
+  const double *adust;    /* (nlammax,ndg) albedo */
+  const double *gdust;    /* (nlammax,ndg) HG asymmetry g */
+  const double *pldust;   /* (nlammax,ndg) peak linear polarisation */
+  const double *kappav;   /* (ndg) kappa_V in cm^2/g */
+  int nT, nnu;            /* 1000, 1025 in the reference */
+  const double *lTint;    /* (nT) log temperature grid */
+  const double *nuint;    /* (nnu) frequency grid in units of T */
+  const double *kapBint;  /* (nT,nnu,ndg) normalised cumulative kappa*B_nu */
+  const double *kappap;   /* (nT,ndg) Planck-mean kappa / kappa_V */
+  double tsub;            /* dust sublimation temperature, K */
+  int nhnu;               /* stellar spectrum samples */
+  const double *hnuint;   /* (nhnu) cumulative distribution, increasing */
+  const double *atmosnu;  /* (nhnu) frequency */
+  const double *lognu;    /* (nhnu) log10 frequency */
+  const double *loghnu;   /* (nhnu) log10 cumulative distribution */
+} hc3d_dust_tables;
+
+/* grid_mod (grid_mod.f90:20-50) as gridset leaves it. */
+typedef struct hc3d_grid {
+  int nrg, ntg, npg;      /* wall counts; cells are (nrg-1)(ntg-1)(npg-1) */
+  int ndg;                /* species slots in densarr/tdust/massarr, 1..8 */
+  const double *rarr;     /* (nrg) radial walls, R* */
+  const double *r2arr;    /* (nrg) squares of rarr */
+  const double *thetarr;  /* (ntg) polar walls, rad */
+  const double *costarr;  /* (ntg) */
+  const double *tan2arr;  /* (ntg) tan^2; 0 at the poles, -1 for the midplane */
+  const double *phiarr;   /* (npg) azimuthal walls, rad */
+  const double *aarr;     /* (npg) sin(phi) */
+  const double *barr;     /* (npg) -cos(phi) */
+  const double *densarr;  /* (nrg,ntg,npg,ndg) g/cm^3 */
+  const double *massarr;  /* (nrg,ntg,npg,ndg) (rho*V)^(1/4), cgs */
+  const double *vcell;    /* (nrg,ntg,npg) cm^3 */
+  const double *tdust;    /* (nrg,ntg,npg,ndg) temperature used by re-emission, K/11605 */
+} hc3d_grid;
+
+/* The scalars and small arrays of tts_mod/out_mod that one call of disk()
+ * reads (setup.f90:37-43,118-130,196-202; initarr.f90:17-21). */
+typedef struct hc3d_run_params {
+  int64_t np;             /* packets of this call */
+  int64_t packet_offset;  /* global id of the first packet (sharding across processes) */
+  uint64_t seed;          /* run seed; packet streams are keyed by (seed, iter, packet id) */
+  int iter;               /* Lucy iteration number, 1-based */
+  int ipeel;              /* 1 = peel-off images and SEDs (CPEEL) */
+  int npeel;              /* peel-off directions */
+  const double *thete;    /* (npeel) peel-off theta, rad */
+  const double *phie;     /* (npeel) peel-off phi, rad */
+  int nfreq, nmu, nph, nap;
+  int nxhst;              /* image pixels per side (NXIMG) */
+  double rmaxi;           /* image half size, R* */
+  const double *aperture2;/* (nap) squared aperture radii, R*^2 */
+  double numin, numax;    /* SED frequency range, units of 1.2398/lambda[um] */
+  double rstar_cm;        /* stellar radius in cm (rmincgs) */
+  double tstar;           /* stellar temperature, K/11605 */
+  int limb;               /* 0 = uniform disk; 1 (limb-darkening table) is not supported */
+  int iintmax;            /* interactions in one cell before a packet is killed (10000) */
+  int64_t max_interactions; /* per-packet cap on interactions; 0 = no cap */
+  int image;              /* 1 = accumulate broadband I,Q,U,V images of the peeled packets */
+} hc3d_run_params;
+
+/* Host copies of the device tallies.  Any pointer may be NULL.  Shapes are
+ * those of the reference arrays (initarr.f90:24-43, initimages, grid_mod). */
+typedef struct hc3d_tallies {
+  int64_t *si, *sq, *su, *sv;      /* (nfreq,nmu,nph,nap,no) Stokes sums, x stokes_scale */
+  int64_t *si2, *sq2, *su2, *sv2;  /* (nfreq,nmu,nph,nap,no) squares, x square_scale */
+  int64_t *nums;                   /* (nfreq,nmu,nph,nap,no) packet counts */
+  int64_t *ti, *tq, *tu, *tv;      /* (nfreq,npeel,nap,no) peeled Stokes sums, x stokes_scale */
+  int64_t *ti2, *tq2, *tu2, *tv2;  /* (nfreq,npeel,nap,no) peeled squares, x square_scale */
+  int64_t *numt;                   /* (nfreq,npeel,nap,no) peeled counts */
+  int64_t *image_i, *image_q, *image_u, *image_v; /* (npeel,nxhst,nxhst) broadband, x stokes_scale */
+  int64_t *nabs;                   /* (nrg,ntg,npg,ndg) absorption counts */
+  int64_t *dtauabs;                /* (nrg,ntg,npg,ndg) absorption path estimator, x path_scale */
+  int64_t *jmean;                  /* (nrg,ntg,npg) path length, x path_scale */
+  int32_t *killed;                 /* (nrg,ntg,npg) */
+  int32_t *dbig;                   /* (nrg,ntg,npg) thermal-grain absorptions */
+  int64_t counters[16];            /* see HC3D_CNT_* */
+  double stokes_scale;             /* fixed-point scale of Stokes sums and images */
+  double square_scale;             /* fixed-point scale of squared Stokes sums */
+  double path_scale;               /* fixed-point scale of dtauabs and jmean */
+} hc3d_tallies;
+
+/* counters[] of hc3d_tallies (newdisktherm.F90:122-141, propagate.f90:296-318) */
+#define HC3D_CNT_FLUX 0       /* packets binned inside the largest aperture */
+#define HC3D_CNT_SFLUX 1      /* of those, scattered at least once */
+#define HC3D_CNT_NSCAT 2      /* scatterings of the packets in SFLUX */
+#define HC3D_CNT_SCOUNT 3     /* escaped packets that scattered last */
+#define HC3D_CNT_TOT 4        /* packets that interacted at least once */
+#define HC3D_CNT_ABFLUX 5     /* packets killed (iint > iintmax or the interaction cap) */
+#define HC3D_CNT_AFLUX 6      /* packets absorbed by the star */
+#define HC3D_CNT_SUMSUB 7     /* sum of escaping Stokes I, x stokes_scale */
+#define HC3D_CNT_SUMALL 8     /* same, including non-interacting external packets */
+#define HC3D_CNT_ESCAPED 9    /* packets that left the grid */
+#define HC3D_CNT_CROSS_PROP 10 /* cell crossings of the propagation walk */
+#define HC3D_CNT_CROSS_PEEL 11 /* cell crossings of the peel-off walks */
+#define HC3D_CNT_EVENTS 12    /* scatterings + absorptions */
+#define HC3D_CNT_PEELS 13     /* peel-off rays started */
+#define HC3D_CNT_STUCK 14     /* walks stopped by the crossing cap (geometry fault) */
+#define HC3D_CNT_STATUS 15    /* first device status word != 0 */
+
+/* ---- context ----------------------------------------------------------- */
+int hc3d_create(hc3d_ctx **ctx, const hc3d_device_opts *opts);
+void hc3d_destroy(hc3d_ctx *ctx);
+int hc3d_get_error(const hc3d_ctx *ctx, char *buf, size_t len);
+/* Library version string and build architecture, e.g. "hc3d 0.1 sm_103a". */
+const char *hc3d_version(void);
+
+/* dustinit/setemiss/atmosinit outputs (dust.f90:314-474, starbarb.f90:3-110) */
+int hc3d_load_tables(hc3d_ctx *ctx, const hc3d_dust_tables *tables);
+
+/* gridset/initarr outputs (gridset.f90:411-1098, initarr.f90:11-56) */
+int hc3d_load_grid(hc3d_ctx *ctx, const hc3d_grid *grid);
+
+/* initarr(.false.) tally reset (initarr.f90:58-89): zero every tally. */
+int hc3d_zero_tallies(hc3d_ctx *ctx);
+
+/* One call of the packet loop of disk() (newdisktherm.F90:194-449) for
+ * params->np packets, accumulating into the device tallies.  Blocks until the
+ * packets are done. */
+int hc3d_run_iteration(hc3d_ctx *ctx, const hc3d_run_params *params);
+
+/* Copy the device tallies to the non-NULL host buffers of *out. */
+int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies *out);
+
+/* tfinal (newdisktherm.F90:557, restated) + initarr(.false.) temperature copy
+ * (initarr.f90:78-84): solve the Lucy energy balance of every cell and
+ * species in FP64 from the dtauabs tally of the packets run since the last
+ * hc3d_zero_tallies(), with ltot in erg/s and np the packets that produced
+ * it.  The new temperatures become the device tdust used by the next
+ * iteration and are copied to tdust_out (nrg,ntg,npg,ndg) when non-NULL.
+ * *max_rel_change receives max |T_new-T_old|/T_new over the cells counted
+ * by the convergence test and *converged is 1 when it is below 1%. */
+int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
+                     double *max_rel_change, int *converged);
+
+/* ---- measurement helpers (no counterpart in the reference) -------------- */
+/* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
+void *hc3d_get_stream(hc3d_ctx *ctx);
+/* Device time in ms of the transport kernel of the last hc3d_run_iteration,
+ * from CUDA events recorded on that stream around the launch. */
+int hc3d_last_kernel_ms(hc3d_ctx *ctx, double *ms);
+
+/* ---- single-packet trace harness ---------------------------------------- */
+/* One record per propagation cell crossing / interaction of a traced packet. */
+typedef struct hc3d_trace_rec {
+  int32_t kind;    /* 1 = crossing, 2 = interaction point, 3 = escape, 4 = star, 5 = scatter, 6 = absorb, 7 = kill */
+  int32_t ir, it, ip; /* cell after the event, 1-based */
+  int32_t iface;   /* wall crossed (1..6) or 0 */
+  int32_t pad;
+  double tsum;     /* optical depth integrated in the current tauint call */
+  double x, y, z;  /* position after the event */
+} hc3d_trace_rec;
+
+/* Replay packets 0..npkt-1 of params with their uniform draws taken from
+ * uniforms[k*nu + j] (packet k, draw j) instead of the counter-based stream,
+ * writing up to max_rec trace records per packet to recs[k*max_rec + ...]
+ * and the record count to nrec[k].  Tallies are accumulated as usual. */
+int hc3d_trace_packets(hc3d_ctx *ctx, const hc3d_run_params *params, int npkt,
+                       const double *uniforms, int nu, hc3d_trace_rec *recs,
+                       int max_rec, int32_t *nrec);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HC3D_H */

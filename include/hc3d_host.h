@@ -1,0 +1,91 @@
+/*
+ * hc3d_host.h -- host-side model setup and run driver of the GB300 photon loop.
+ *
+ * These entry points replace the Fortran caller of disk() -- the work that
+ * newtts.F90 does before, between and after the calls of disk():
+ *
+ *   hc3d_model_create  <- setup (setup.f90:3) + reapar (reapar.f90:1)
+ *                         + dustinit/setemiss (dust.f90:314,394)
+ *                         + atmosinit (starbarb.f90:3) + setup_wave
+ *                         (setup_wave.f90:46-115) + gridset (gridset.f90:1)
+ *                         + initarr(.true.) (initarr.f90:11-56)
+ *   hc3d_tts           <- program tts (newtts.F90:141-368): Lucy iterations,
+ *                         the final peeled iteration, diskflux (flux.f90:1)
+ *                         and the ASCII writers of output (output.F90:166-503)
+ *
+ * The .par format and keys are those of configuration.f90/reapar.f90, with
+ * these extensions (all optional):
+ *   SEDLMIN, SEDLMAX  SED wavelength range in microns (setup.f90:37-39
+ *                     hard-codes 0.01 and 5000)
+ *   IMAGE             YES/NO broadband I,Q,U,V peel-off images (default YES)
+ *   MAXINT            per-packet interaction cap (default 1000000; 0 = none)
+ *   SEED              64-bit run seed of the counter-based packet streams
+ *   FRACTLEV, FRACTN, FRACTCONTRAST  levels, clumps per level and density
+ *                     contrast of the project fractal generator (CFRACTAL=YES)
+ */
+#ifndef HC3D_HOST_H
+#define HC3D_HOST_H
+
+#include "hc3d.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hc3d_model hc3d_model;
+
+/* Scalars of tts_mod/opacin_mod that the driver needs besides the views. */
+typedef struct hc3d_model_info {
+  int64_t np;          /* NP */
+  int64_t npmin;       /* NPMIN */
+  int64_t np_lucy;     /* packets per Lucy iteration (newtts.F90:159-182) */
+  int nimin, nimax;    /* NIMIN, NIMAX */
+  int ipeel, ilucy;    /* CPEEL, CLUCY */
+  int ndg_active;      /* species slots with nonzero density */
+  double ltot;         /* erg/s (gridset.f90:165-180) */
+  double tstar_k;      /* K */
+  double rstar_rsun;
+  double autors;       /* AU in stellar radii */
+  double rminsub;      /* sublimation radius, R* */
+  double massdisk, massenv; /* Msun on the grid */
+  int64_t ncells;      /* (nrg-1)(ntg-1)(npg-1) */
+} hc3d_model_info;
+
+/* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
+ * err receives a message on failure. */
+int hc3d_model_create(hc3d_model **m, const char *par_path, const char *par_dir, char *err, size_t errlen);
+void hc3d_model_destroy(hc3d_model *m);
+
+/* Views of the model's arrays (owned by the model; valid until destroy). */
+int hc3d_model_views(hc3d_model *m, hc3d_dust_tables *tables, hc3d_grid *grid, hc3d_run_params *params,
+                     hc3d_model_info *info);
+
+/* Replace the model's tdust (nrg,ntg,npg,ndg), e.g. after hc3d_lucy_update. */
+int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
+
+typedef struct hc3d_tts_stats {
+  int iterations;            /* Lucy iterations + the final one */
+  int converged;
+  double max_rel_change;     /* of the last Lucy update */
+  double seconds_lucy;       /* wall time of the Lucy iterations */
+  double seconds_final;      /* wall time of the final peeled iteration */
+  int64_t packets_total;
+  int64_t counters[16];      /* final iteration, see HC3D_CNT_* */
+} hc3d_tts_stats;
+
+/* program tts: run the whole model on the GPU and write the reference's ASCII
+ * output files (flux*.dat, peel_flux*.dat, e_ALL_*_img.dat, tmidplane*.dat,
+ * tave*.dat) into out_dir. */
+int hc3d_tts(const char *par_path, const char *par_dir, const char *out_dir, const hc3d_device_opts *opts,
+             hc3d_tts_stats *stats, char *err, size_t errlen);
+
+/* Write a synthetic 7-column dust file (dustinit's format, dust.f90:336)
+ * and a 2-column stellar wavelength grid (atmosinit's format,
+ * starbarb.f90:24-36): the fixtures of the benchmark models. */
+int hc3d_write_synthetic_dust(const char *path);
+int hc3d_write_wavelength_grid(const char *path, double tstar_k);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

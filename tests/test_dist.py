@@ -1,0 +1,74 @@
+"""Multi-process packet sharding on CPU (gloo, world_size 2).
+
+The packet loop shards by packet id (the reference splits np over MPI ranks,
+newtts.F90:185-188).  Tallies are int64 fixed point, so the all-reduce of the
+shards equals the single-process run exactly.  The ranks run the oracle on
+CPU; on GPUs each rank runs the library on its own device with the same
+packet_offset arithmetic.
+"""
+from __future__ import annotations
+
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+from tests.helpers import make_model
+
+KEYS = ("si", "sq", "nums", "ti", "tv", "numt", "image_i", "nabs", "dtauabs", "jmean")
+
+
+def _free_port() -> int:
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _rank(rank, world, port, directory, n, q):
+    import torch
+    import torch.distributed as dist
+
+    import oracle.oracle as O
+    from hochunk3d_gb300 import hc3d
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    m = make_model(directory, "tiny3d")
+    lo, hi = n * rank // world, n * (rank + 1) // world
+    p = m.run_params(np=hi - lo, packet_offset=lo, iter=2, ipeel=1)
+    r = O.run(m, p, scales=hc3d.tally_scales(n))
+    out = {}
+    for k in KEYS + ("counters",):
+        t = torch.from_numpy(np.ascontiguousarray(r[k]).astype(np.int64))
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        out[k] = t.numpy()
+    if rank == 0:
+        q.put(out)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_shards_sum_to_the_single_run(tmp_path, built):
+    import oracle.oracle as O
+    from hochunk3d_gb300 import hc3d
+
+    n = 1500
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, tmp_path / "m", n, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    m = make_model(tmp_path / "single", "tiny3d")
+    ref = O.run(m, m.run_params(np=n, iter=2, ipeel=1), scales=hc3d.tally_scales(n))
+    for k in KEYS + ("counters",):
+        np.testing.assert_array_equal(got[k], np.ascontiguousarray(ref[k]).astype(np.int64), err_msg=k)

@@ -1,0 +1,223 @@
+"""CPU tests of the oracle: known answers, physics checks and golden traces."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from hochunk3d_gb300 import hc3d
+from tests.helpers import splitmix_uniforms, trace_key
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def O(built):
+    import oracle.oracle as orc
+
+    return orc
+
+
+def test_philox_known_answers(O):
+    # Random123 known-answer vectors of Philox4x32-10 (Salmon et al., SC'11)
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_stream_is_open_uniform(O):
+    u = O.stream(7, 1, 123456789012, 200000)
+    assert u.min() > 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 4 * np.sqrt(1 / 12 / len(u))
+    # distinct packets and iterations give distinct streams
+    assert not np.array_equal(u[:8], O.stream(7, 1, 123456789013, 8))
+    assert not np.array_equal(u[:8], O.stream(7, 2, 123456789012, 8))
+
+
+def test_radface_closed_form(O):
+    import ctypes as C
+
+    out = np.zeros(6)
+    ids = np.zeros(3, dtype=np.int32)
+    # point at r=2 on the x axis moving along +x: spheres r=1 and r=3
+    O.lib().orc_radface_roots(1.0, 0.0, 0.0, 2.0, 0.0, 0.0, 1.0, 9.0, out.ctypes.data_as(C.POINTER(C.c_double)),
+                              ids.ctypes.data_as(C.POINTER(C.c_int)))
+    tn1, tp1, tp2 = out[:3]
+    assert tn1 == pytest.approx(-1.0) and ids[0] == 1  # back through r=1 at t=-1
+    assert tp1 == pytest.approx(1.0) and ids[1] == 2   # r=3 at t=+1
+    assert tp2 == ORC_HUGE  # no second non-negative root
+
+
+def test_locate_numerical_recipes(O):
+    import ctypes as C
+
+    xx = np.array([0.0, 1.0, 2.0, 3.0])
+    f = lambda x: O.lib().orc_locate_c(xx.ctypes.data_as(C.POINTER(C.c_double)), 4, x)
+    assert f(-1.0) == 0 and f(0.0) == 1 and f(0.5) == 1 and f(1.0) == 1 and f(1.5) == 2 and f(3.0) == 3
+    assert f(4.0) == 4
+
+
+def test_findangle3_scattering_angle(O):
+    import ctypes as C
+
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        t1, t2 = rng.uniform(0.05, np.pi - 0.05, 2)
+        p1, p2 = rng.uniform(0, 2 * np.pi, 2)
+        out = np.zeros(3)
+        O.lib().orc_findangle3_c(np.cos(t1), np.sin(t1), p1, np.cos(p1), np.sin(p1), np.cos(t2), np.sin(t2), p2,
+                                 np.cos(p2), np.sin(p2), out.ctypes.data_as(C.POINTER(C.c_double)))
+        u1 = np.array([np.sin(t1) * np.cos(p1), np.sin(t1) * np.sin(p1), np.cos(t1)])
+        u2 = np.array([np.sin(t2) * np.cos(p2), np.sin(t2) * np.sin(p2), np.cos(t2)])
+        assert out[0] == pytest.approx(u1 @ u2, abs=1e-12)
+        assert 0.0 <= out[2] <= 2 * np.pi
+
+
+def test_phase_function_mean_cosine(O, model_factory):
+    """<cos Theta> of the modified Cornette-Shanks phase function sampled by
+    stokes: 3g(4+g^2) / (5(2+g^2))."""
+    import ctypes as C
+
+    m = model_factory("tiny", warm=False)
+    for lam in (0.1, 0.55, 2.0):
+        nu = 1.2398 / lam
+        t = m.tables
+        n = 200000
+        cs = np.zeros(n)
+        q = np.zeros(n)
+        O.lib().orc_sample_stokes(C.byref(t), C.byref(m.grid), nu, 11, n, cs.ctypes.data_as(C.POINTER(C.c_double)),
+                                  q.ctypes.data_as(C.POINTER(C.c_double)))
+        x = (np.log10(lam) + 1.0) / 2.0
+        g = 0.6 * (1 - min(max(x, 0), 1))
+        expect = 3 * g * (4 + g * g) / (5 * (2 + g * g))
+        assert cs.mean() == pytest.approx(expect, abs=5 * cs.std() / np.sqrt(n) + 2e-3)
+
+
+def test_trace_golden_oracle(O, model_factory):
+    """The oracle reproduces the committed single-packet traces exactly."""
+    for name in ("tiny", "tiny3d"):
+        g = np.load(GOLDEN / f"trace_{name}.npz")
+        m = model_factory(name)
+        p = m.run_params(np=32, iter=3, ipeel=1)
+        U = splitmix_uniforms(len(g["nrec"]), int(g["nu"]), seed=int(g["seed"]))
+        off = 0
+        for k, n in enumerate(g["nrec"]):
+            recs, ex, _ = O.trace(m, p, k, U[k], max_rec=2048)
+            assert not ex
+            want = np.stack([g[f][off:off + n] for f in ("kind", "ir", "it", "ip", "iface")], axis=1)
+            np.testing.assert_array_equal(trace_key(recs), want)
+            np.testing.assert_allclose(recs["tsum"], g["tsum"][off:off + n], rtol=1e-12, atol=0)
+            off += n
+
+
+def test_run_golden_oracle(O, model_factory):
+    for name in ("tiny", "tiny3d"):
+        g = np.load(GOLDEN / f"trace_{name}.npz")
+        m = model_factory(name)
+        r = O.run(m, m.run_params(np=int(g["run_np"]), iter=3, ipeel=1))
+        np.testing.assert_array_equal(r["nums"].sum(axis=(1, 2, 3)), g["run_nums"])
+        np.testing.assert_array_equal(r["numt"].sum(axis=(1, 2)), g["run_numt"])
+        np.testing.assert_array_equal(r["nabs"].sum(axis=(0, 1, 2)), g["run_nabs"])
+        np.testing.assert_array_equal(r["counters"], g["run_counters"])
+
+
+def test_threads_give_identical_tallies(O, model_factory):
+    m = model_factory("tiny")
+    p = m.run_params(np=3000, iter=2, ipeel=1)
+    a = O.run(m, p, nthreads=1)
+    b = O.run(m, p, nthreads=4)
+    for k in ("si", "sq", "nums", "ti", "tu", "numt", "image_i", "nabs", "dtauabs", "jmean", "counters"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_packet_bookkeeping(O, model_factory):
+    """Every packet ends exactly once: escaped, absorbed by the star or killed."""
+    m = model_factory("tiny3d")
+    n = 4000
+    r = O.run(m, m.run_params(np=n, iter=2, ipeel=0))
+    c = r["counters"]
+    assert c[hc3d.CNT["escaped"]] + c[hc3d.CNT["aflux"]] + c[hc3d.CNT["abflux"]] + r["errors"] == n
+    assert r["errors"] == 0 and c[hc3d.CNT["stuck"]] == 0
+    # luminosity closure (output.F90:381): no external packets, so sumsub == sumall
+    assert c[hc3d.CNT["sumsub"]] == c[hc3d.CNT["sumall"]]
+    # escaping Stokes I is conserved by scattering: every binned packet carries I=1
+    assert r["si"][..., 0].sum() == r["nums"][..., 0].sum() * int(r["stokes_scale"])
+
+
+def test_optically_thin_star_spectrum(O, model_factory):
+    """With no dust the escaping SED is the stellar spectrum of atmosinit."""
+    m = model_factory("tiny", warm=False)
+    m.densarr[...] = 0.0
+    n = 60000
+    p = m.run_params(np=n, iter=1, ipeel=0)
+    r = O.run(m, p, nthreads=4)
+    assert r["counters"][hc3d.CNT["escaped"]] == n
+    counts = r["nums"][:, :, :, :, 0].sum(axis=(1, 2, 3)).astype(float)
+    # expected bin probabilities from the CDF of the frequency sampler
+    nf = p.nfreq
+    edges = p.numin * (p.numax / p.numin) ** (np.arange(nf + 1) / nf)
+    cdf = np.interp(np.log10(edges), m.lognu, np.concatenate([[0.0], np.power(10.0, m.loghnu[1:])]))
+    prob = np.diff(cdf)
+    prob[0] += cdf[0]
+    prob[-1] += 1.0 - cdf[-1]
+    exp = prob * n
+    ok = exp > 50
+    chi2 = (((counts - exp) ** 2) / exp)[ok].sum() / ok.sum()
+    assert chi2 < 2.0
+
+
+def test_pure_absorber_escape_fraction(O, model_factory):
+    """Uniform non-scattering shell: fraction escaping without interaction is
+    <exp(-tau L)> over the emission directions (cos = sqrt(xi) about the normal)."""
+    m = model_factory("tiny", warm=False)
+    m.densarr[...] = 0.0
+    rho = 1.0e-19
+    m.densarr[1:-1, :-1, :-1, 2] = rho
+    n = 40000
+    p = m.run_params(np=n, iter=1, ipeel=0)
+    r = O.run(m, p, nthreads=4)
+    interacted = r["counters"][hc3d.CNT["tot"]]
+    frac = 1.0 - interacted / n
+    # expected: average over photon frequencies of exp(-kappa rho L)
+    r1, r2 = m.rarr[1], m.rarr[-1]
+    mu = np.sqrt((np.arange(4000) + 0.5) / 4000)  # emission cosine about the surface normal
+    # path inside the shell from the surface r=1 along direction with radial cosine mu
+    s = lambda R: -mu + np.sqrt(mu * mu - 1 + R * R)
+    L = s(r2) - s(r1)
+    # frequency distribution of stellar packets: sample the CDF
+    xi = (np.arange(2000) + 0.5) / 2000
+    lnu = np.interp(np.log10(xi), m.loghnu[1:], m.lognu[1:])
+    nu = 10 ** lnu
+    nud = m.nudust[: m.nlambda[2]]
+    kap = np.interp(nu, nud[::-1], m.kappad[: m.nlambda[2]][::-1])
+    kapd = kap * p.rstar_cm * m.kappav[2]
+    expect = np.mean(np.exp(-np.outer(kapd * rho, L)))
+    sig = np.sqrt(expect * (1 - expect) / n)
+    assert abs(frac - expect) < 5 * sig + 2e-3
+
+
+def test_tfinal_energy_balance(O, model_factory):
+    """The Lucy temperature balances emission and the absorbed-path estimator:
+    4 sigma T^4 kappa_V kappa_P(T) rho V = na L / N (dusttemp.f90:35)."""
+    m = model_factory("tiny", warm=False)
+    na = np.zeros(m.shape4, order="F")
+    sel = m.densarr > 0
+    rng = np.random.default_rng(5)
+    na[sel] = 10 ** rng.uniform(-2, 3, sel.sum())
+    L, N = m.info.ltot, 1.0e5
+    T = O.tfinal(m, na, L, N)
+    kp = m.kappap.reshape(m.ndg_tab, m.nT)
+    idx = np.argwhere(sel)[:500]
+    for ir, it, ip, s in idx:
+        Tk = T[ir, it, ip, s]
+        if not (0.11 / 11605 < Tk < 1599 / 11605):
+            continue
+        lT = np.log(Tk)
+        kap = np.interp(lT, m.lTint, kp[s])
+        lhs = 4 * 5.6704e-5 * (Tk * 11605) ** 4 * m.kappav[s] * kap * m.massarr[ir, it, ip, s] ** 4
+        assert lhs == pytest.approx(na[ir, it, ip, s] * L / N, rel=2e-4)
+
+
+ORC_HUGE = 1.7976931348623157e308
