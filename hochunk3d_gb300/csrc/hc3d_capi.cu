@@ -44,7 +44,16 @@ struct hc3d_ctx {
   double* d_ap2 = nullptr;
   unsigned long long* d_maxrel = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double last_ms = 0.0;
+  cudaEvent_t wev[3] = {nullptr, nullptr, nullptr};
+  double last_ms = 0.0, last_transport_ms = 0.0, last_peel_ms = 0.0;
+  int last_launches = 0;
+  // wavefront form
+  std::vector<void*> wave_allocs;
+  WaveBufs wave{};
+  int64_t pool_threads = 0, qcap = 0;
+  int wave_blocks = 0, peel_blocks = 0;
+  int64_t queue_records = 1 << 22;  // peel-off events held per wave
+  bool use_waves = true;            // peeled runs use the wavefront form
 };
 
 namespace {
@@ -278,6 +287,75 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   return HC3D_OK;
 }
 
+// Allocate the packet pool and event queue of the wavefront form once per context.
+int ensure_wave(hc3d_ctx* c) {
+  if (c->wave.pool) return HC3D_OK;
+  const bool f64 = c->precision == HC3D_PREC_FP64;
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f64 ? wave_fn_fp64() : wave_fn_mixed(), 128, 0));
+  if (per_sm < 1) per_sm = 1;
+  c->wave_blocks = c->sm_count * per_sm;
+  c->pool_threads = (int64_t)c->wave_blocks * 128;
+  int per_sm_p = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, f64 ? peel_fn_fp64() : peel_fn_mixed(), 256, 0));
+  c->peel_blocks = c->sm_count * std::max(1, per_sm_p);
+  c->qcap = std::max<int64_t>(c->queue_records, c->pool_threads);
+  const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
+  const size_t rec = f64 ? rec_bytes_fp64() : rec_bytes_mixed();
+  int r;
+  unsigned char *pool, *queue;
+  if ((r = dalloc(c, c->wave_allocs, &pool, slot * (size_t)c->pool_threads)) ||
+      (r = dalloc(c, c->wave_allocs, &queue, rec * (size_t)c->qcap)) ||
+      (r = dalloc(c, c->wave_allocs, &c->wave.qcount, 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.alive, 1)))
+    return r;
+  c->wave.pool = pool;
+  c->wave.queue = queue;
+  for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&c->wev[i]));
+  return HC3D_OK;
+}
+
+// The wavefront loop of one peeled run: waves until the batch is exhausted
+// and no packet is alive.  The per-wave event budget E keeps the queue within
+// its capacity: at most min(pool, alive + unstarted) threads append, each at
+// most E records.
+int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
+  int r;
+  if ((r = ensure_wave(c))) return r;
+  const bool f64 = c->precision == HC3D_PREC_FP64;
+  const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
+  CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
+  LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->stream};
+  int64_t alive_prev = 0;
+  unsigned long long work = 0;
+  c->last_transport_ms = c->last_peel_ms = 0.0;
+  c->last_launches = 0;
+  for (int wave = 0;; ++wave) {
+    const int64_t remaining = p->np - (int64_t)std::min<unsigned long long>(work, (unsigned long long)p->np);
+    const int64_t active = std::min<int64_t>(c->pool_threads, alive_prev + remaining);
+    if (active <= 0) break;
+    const int E = (int)std::max<int64_t>(1, std::min<int64_t>(c->qcap / active, 1 << 20));
+    CK(cudaMemsetAsync(c->wave.qcount, 0, sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->wave.alive, 0, sizeof(unsigned int), c->stream));
+    cudaError_t e = f64 ? launch_wave_fp64(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev)
+                        : launch_wave_mixed(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev);
+    if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("wave launch: ") + cudaGetErrorString(e));
+    unsigned int alive = 0;
+    CK(cudaMemcpyAsync(&alive, c->wave.alive, sizeof(alive), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float t0 = 0.f, t1 = 0.f;
+    CK(cudaEventElapsedTime(&t0, c->wev[0], c->wev[1]));
+    CK(cudaEventElapsedTime(&t1, c->wev[1], c->wev[2]));
+    c->last_transport_ms += t0;
+    c->last_peel_ms += t1;
+    c->last_launches += 2;
+    alive_prev = alive;
+    if (alive == 0 && work >= (unsigned long long)p->np) break;
+  }
+  c->last_ms = c->last_transport_ms + c->last_peel_ms;
+  return HC3D_OK;
+}
+
 int finish_run(hc3d_ctx* c) {
   CK(cudaStreamSynchronize(c->stream));
   int st = 0;
@@ -350,6 +428,9 @@ extern "C" void hc3d_destroy(hc3d_ctx* c) {
   free_all(c->model_allocs);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (int i = 0; i < 3; ++i)
+    if (c->wev[i]) cudaEventDestroy(c->wev[i]);
+  free_all(c->wave_allocs);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -541,6 +622,12 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   if (r) return r;
   if (p->np == 0) return HC3D_OK;
   CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), c->stream));
+  if (p->ipeel && c->use_waves) {
+    if ((r = run_waves(c, p, a))) return r;
+    if ((r = finish_run(c))) return r;
+    c->epoch_np += p->np;
+    return HC3D_OK;
+  }
   LaunchCfg cfg;
   cfg.threads = c->block_size;
   cfg.stream = c->stream;
@@ -568,7 +655,18 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   c->last_ms = ms;
+  c->last_transport_ms = ms;
+  c->last_peel_ms = 0.0;
+  c->last_launches = 1;
   c->epoch_np += p->np;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_last_launch_stats(hc3d_ctx* c, int* launches, double* transport_ms, double* peel_ms) {
+  if (!c) return HC3D_ERR_INVALID;
+  if (launches) *launches = c->last_launches;
+  if (transport_ms) *transport_ms = c->last_transport_ms;
+  if (peel_ms) *peel_ms = c->last_peel_ms;
   return HC3D_OK;
 }
 

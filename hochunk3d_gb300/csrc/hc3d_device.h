@@ -95,6 +95,32 @@ cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const
                                    const LaunchCfg& cfg);
 cudaError_t launch_transport_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                   const LaunchCfg& cfg);
+// Buffers of the wavefront form: the packet pool (one slot per thread of
+// k_wave) and the peel-off event queue.
+struct WaveBufs {
+  void* pool;
+  void* queue;
+  unsigned long long* qcount;
+  unsigned int* alive;
+};
+
+// One wave: k_wave (advance every live packet by up to E events) then k_peel
+// (walk the queued peel-off rays); ev[0..2] bracket the two kernels.
+cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                              const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
+                              cudaEvent_t ev[3]);
+cudaError_t launch_wave_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                             const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
+                             cudaEvent_t ev[3]);
+size_t slot_bytes_mixed();
+size_t slot_bytes_fp64();
+size_t rec_bytes_mixed();
+size_t rec_bytes_fp64();
+const void* wave_fn_mixed();
+const void* wave_fn_fp64();
+const void* peel_fn_mixed();
+const void* peel_fn_fp64();
+
 int transport_regs_mixed();
 int transport_regs_fp64();
 const void* transport_fn_mixed();

@@ -20,3 +20,28 @@ int transport_regs_fp64() {
 const void* transport_fn_fp64() { return (const void*)dev::k_transport<double>; }
 
 }  // namespace hc3d
+
+namespace hc3d {
+
+cudaError_t launch_wave_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                              const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
+                              cudaEvent_t ev[3]) {
+  cudaError_t e;
+  if (ev && (e = cudaEventRecord(ev[0], wave.stream)) != cudaSuccess) return e;
+  dev::k_wave<double><<<wave.blocks, wave.threads, 0, wave.stream>>>(
+      m, t, d, a, static_cast<dev::Slot<double>*>(w.pool), static_cast<dev::PeelRec<double>*>(w.queue), w.qcount, E, w.alive);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;
+  dev::k_peel<double><<<peel.blocks, peel.threads, 0, peel.stream>>>(
+      m, t, d, a, static_cast<const dev::PeelRec<double>*>(w.queue), w.qcount);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[2], wave.stream)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+size_t slot_bytes_fp64() { return sizeof(dev::Slot<double>); }
+size_t rec_bytes_fp64() { return sizeof(dev::PeelRec<double>); }
+const void* wave_fn_fp64() { return (const void*)dev::k_wave<double>; }
+const void* peel_fn_fp64() { return (const void*)dev::k_peel<double>; }
+
+}  // namespace hc3d

@@ -20,3 +20,28 @@ int transport_regs_mixed() {
 const void* transport_fn_mixed() { return (const void*)dev::k_transport<float>; }
 
 }  // namespace hc3d
+
+namespace hc3d {
+
+cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                              const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
+                              cudaEvent_t ev[3]) {
+  cudaError_t e;
+  if (ev && (e = cudaEventRecord(ev[0], wave.stream)) != cudaSuccess) return e;
+  dev::k_wave<float><<<wave.blocks, wave.threads, 0, wave.stream>>>(
+      m, t, d, a, static_cast<dev::Slot<float>*>(w.pool), static_cast<dev::PeelRec<float>*>(w.queue), w.qcount, E, w.alive);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;
+  dev::k_peel<float><<<peel.blocks, peel.threads, 0, peel.stream>>>(
+      m, t, d, a, static_cast<const dev::PeelRec<float>*>(w.queue), w.qcount);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[2], wave.stream)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+size_t slot_bytes_mixed() { return sizeof(dev::Slot<float>); }
+size_t rec_bytes_mixed() { return sizeof(dev::PeelRec<float>); }
+const void* wave_fn_mixed() { return (const void*)dev::k_wave<float>; }
+const void* peel_fn_mixed() { return (const void*)dev::k_peel<float>; }
+
+}  // namespace hc3d

@@ -28,6 +28,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "hc3d_device.h"
@@ -575,9 +576,39 @@ __device__ __forceinline__ void stokespeel(R g, R pl, R& sip, R& sqp, R& sup, R&
   mueller<R>(upper, p1, p2, p3, s2x, c2x, sini2, cosi2, sip, sqp, sup, svp);
 }
 
+// ---- peel-off events -------------------------------------------------------------------
+// Everything a peel-off ray needs from the event that spawns it: the packet
+// state at a scattering (before stokes), at a re-emission (after reemit) or at
+// its emission from the stellar surface.  Peel-off rays draw no random numbers,
+// so they can run after the event, in any order and on any thread.
+template <class R>
+struct PeelRec {
+  double x, y, z;
+  int ir, it, ip;
+  int flags;  // bit0 on_wall, bit1 scattered, bits2-4 i_orig, bits5-6 idust2, bit7 stellar-surface emission
+  int inub;
+  R sip, sqp, sup, svp;
+  R d0, d1, d2, d3, d4;  // scattered: cost, sint, phi, cosp, sinp of the incident packet; stellar: cosb, sinb, coslp, sinlp
+  R g, pl;               // phase-matrix parameters of the scattering species
+  R kapd[kSlots];
+};
+
 __device__ __forceinline__ int nu_bin(const RunArgs& a, double nub) {
   int inub = (int)((double)a.nfreq * log(nub / a.numin) / a.lnurat) + 1;
   return inub < 1 ? 1 : (inub > a.nfreq ? a.nfreq : inub);
+}
+
+template <class R>
+__device__ __forceinline__ void make_rec(PeelRec<R>& e, const Pkt<R>& p, const RunArgs& a, int iflag, int idust2) {
+  e.x = p.x; e.y = p.y; e.z = p.z;
+  e.ir = p.ir; e.it = p.it; e.ip = p.ip;
+  e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5);
+  e.inub = nu_bin(a, p.nub);
+  e.sip = p.sip; e.sqp = p.sqp; e.sup = p.sup; e.svp = p.svp;
+  e.d0 = p.cost; e.d1 = p.sint; e.d2 = p.phi; e.d3 = p.cosp; e.d4 = p.sinp;
+  e.g = p.g[idust2]; e.pl = p.pl[idust2];
+#pragma unroll
+  for (int s = 0; s < kSlots; ++s) e.kapd[s] = p.kapd[s];
 }
 
 __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, int64_t b, double i, double q, double u,
@@ -593,16 +624,25 @@ __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, i
   atomicAdd(base + 8 * stride + b, 1ull);
 }
 
-// ---- peeloff_3d.f90:52-286: one observer direction ------------------------------------
+// ---- peeloff_3d.f90:52-286: one observer direction k of one event ----------------------
 template <class R>
-__device__ void peeloff(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
-                        const Pkt<R>& p, R sip, int iflag, int idust2, int k, Local& L) {
-  double xp1 = p.x, yp1 = p.y, zp1 = p.z;
-  int ir = p.ir, it = p.it, ip = p.ip;
-  int on_wall = p.on_wall;
-  R sqp = p.sqp, sup = p.sup, svp = p.svp;
+__device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                         const PeelRec<R>& e, int k, Local& L) {
   const double* pd = a.peeldir + 4 * k;
   const R coste = (R)__ldg(pd), sinte = (R)__ldg(pd + 1), cospe = (R)__ldg(pd + 2), sinpe = (R)__ldg(pd + 3);
+  const int flags = e.flags;
+  const int iflag = (flags >> 1) & 1;
+  const int i_orig = (flags >> 2) & 7;
+  R sip = e.sip, sqp = e.sqp, sup = e.sup, svp = e.svp;
+  if (flags & 128) {
+    // newdisktherm.F90:342-360: limb = 0 weight of a stellar-surface packet
+    const R cosnorm = e.d0 * coste + (e.d1 * sinte * (cospe * e.d2 + sinpe * e.d3));
+    if (!(cosnorm > R(0))) return;
+    sip = R(4) * e.sip * cosnorm;
+  }
+  double xp1 = e.x, yp1 = e.y, zp1 = e.z;
+  int ir = e.ir, it = e.it, ip = e.ip;
+  int on_wall = flags & 1;
   const R ux1 = sinte * cospe, uy1 = sinte * sinpe, uz1 = coste;
   L.c[HC3D_CNT_PEELS]++;
   if (on_wall) {
@@ -634,7 +674,7 @@ __device__ void peeloff(const DevModel& m, const DevTallies& t, const TallyDims&
     R opac = R(0);
 #pragma unroll
     for (int s = 0; s < kSlots; ++s)
-      if (mask & (1u << s)) opac += p.kapd[s] * rho.v[s];
+      if (mask & (1u << s)) opac += e.kapd[s] * rho.v[s];
     tsum += (double)(opac * dt);
     L.c[HC3D_CNT_CROSS_PEEL]++;
     if (tsum > kTauMax) return;
@@ -650,8 +690,8 @@ __device__ void peeloff(const DevModel& m, const DevTallies& t, const TallyDims&
   sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
   if (iflag == 1) {
     R bmu, ri1;
-    findangle3<R>(p.cost, p.sint, p.phi, p.cosp, p.sinp, coste, sinte, R(0), cospe, sinpe, bmu, ri1);
-    stokespeel<R>(p.g[idust2], p.pl[idust2], sip, sqp, sup, svp, coste, sinte, ri1, bmu, p.cost, p.sint);
+    findangle3<R>(e.d0, e.d1, e.d2, e.d3, e.d4, coste, sinte, R(0), cospe, sinpe, bmu, ri1);
+    stokespeel<R>(e.g, e.pl, sip, sqp, sup, svp, coste, sinte, ri1, bmu, e.d0, e.d1);
   }
   const double cte = (double)coste, ste = (double)sinte, cpe = (double)cospe, spe = (double)sinpe;
   const double yimage = zp1 * ste - yp1 * cte * spe - xp1 * cte * cpe;
@@ -659,9 +699,9 @@ __device__ void peeloff(const DevModel& m, const DevTallies& t, const TallyDims&
   const int ix = (int)((ximage + a.rmaxi) / a.fractxh) + 1;
   const int iy = (int)((yimage + a.rmaxi) / a.fractxh) + 1;
   const double rho2 = ximage * ximage + yimage * yimage;
-  const int inub = nu_bin(a, p.nub);
-  const int i_inter = iflag == 1 ? 2 : (p.i_orig == 1 ? 1 : 3);
-  const int indx[3] = {1, 1 + p.i_orig, 5 + i_inter};
+  const int inub = e.inub;
+  const int i_inter = iflag == 1 ? 2 : (i_orig == 1 ? 1 : 3);
+  const int indx[3] = {1, 1 + i_orig, 5 + i_inter};
   const double dsip = (double)sip, dsqp = (double)sqp, dsup = (double)sup, dsvp = (double)svp;
   for (int ia = 1; ia <= a.nap; ++ia) {
     if (rho2 < __ldg(a.aperture2 + ia - 1)) {
@@ -800,17 +840,22 @@ __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArg
   L.c[HC3D_CNT_ESCAPED]++;
 }
 
-__device__ __forceinline__ void set_status(const RunArgs& a, int code) {
-  if (a.status) atomicCAS(a.status, 0, code);
-}
+// ---- the packet history, split at its events ----------------------------------------
+// propagate.f90 keeps these in locals; they persist across the waves below.
+struct Flow {
+  double xpold, ypold, zpold;
+  int iflag, iscat, iint, idust2;
+  int64_t ntot;
+};
 
-// ---- one stellar packet: newdisktherm.F90:256-377 + propagate.f90:27-204 ------------
+enum { ST_DONE = 0, ST_INTERACT = 1 };
+
+// Stellar packet emission, newdisktherm.F90:256-337 with initpspot (spot-free),
+// initp_sample (limb = 0) and initp_transform (initp_common.f90:1-94).  rec
+// receives the stellar-surface peel-off event.
 template <class R>
-__device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
-                           Local& L, Tracer& tr) {
-  Pkt<R> p;
+__device__ void emit(const DevModel& m, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
   p.on_wall = 0;
-  // initpspot (spot-free) + initp_sample (limb = 0) + initp_transform
   p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
   for (;;) {
     const R xran = ran<R>(rng);
@@ -870,81 +915,120 @@ __device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDi
   p.it = p.it < 1 ? 1 : (p.it > m.ntg - 1 ? m.ntg - 1 : p.it);
   p.ip = p.ip < 1 ? 1 : (p.ip > m.npg - 1 ? m.npg - 1 : p.ip);
   tr.add(0, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-  if (a.ipeel == 1) {
-    for (int k = 0; k < a.npeel; ++k) {
-      const double* pd = a.peeldir + 4 * k;
-      const R coste = (R)__ldg(pd), sinte = (R)__ldg(pd + 1), cospe = (R)__ldg(pd + 2), sinpe = (R)__ldg(pd + 3);
-      const R cosnorm = p.cosb * coste + (p.sinb * sinte * (cospe * coslp + sinpe * sinlp));
-      const R sipnew = R(4) * p.sip * cosnorm;
-      if (cosnorm > R(0)) peeloff<R>(m, t, d, a, p, sipnew, 0, 0, k, L);
-    }
-  }
+  make_rec<R>(rec, p, a, 0, 0);
+  rec.flags |= 128;
+  rec.d0 = p.cosb; rec.d1 = p.sinb; rec.d2 = coslp; rec.d3 = sinlp;
+}
 
-  // ---- propagate ----
-  double xpold = p.x, ypold = p.y, zpold = p.z;
-  int iflag = 0, iscat = 0, iint = 0;
-  int64_t ntot = 0;
-  R tau = -xlog(ran<R>(rng));
-  int st = tauint<R>(m, t, p, tau, L, tr);
+__device__ __forceinline__ void set_status(const RunArgs& a, int code) {
+  if (a.status) atomicCAS(a.status, 0, code);
+}
+
+// tau sample + tauint + outcome, propagate.f90:46-62 (first) and 169-202.
+template <class R>
+__device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                    Flow& f, Local& L, Tracer& tr, bool first) {
+  const R tau = -xlog(ran<R>(rng));
+  if (!first) {
+    f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
+    p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
+  }
+  const int pir = p.ir, pit = p.it, pip = p.ip;
+  const int st = tauint<R>(m, t, p, tau, L, tr);
   if (st == TI_ESCAPE) {
     tr.add(3, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-    bin_escape<R>(t, d, a, p, xpold, ypold, zpold, iflag, iscat, L);
-    return;
+    bin_escape<R>(t, d, a, p, f.xpold, f.ypold, f.zpold, f.iflag, f.iscat, L);
+    return ST_DONE;
   }
-  if (st == TI_STAR) { L.c[HC3D_CNT_AFLUX]++; tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z); return; }
-  if (st == TI_FAULT) { L.c[HC3D_CNT_STUCK]++; set_status(a, 1); return; }
-  int idust2 = select_dust<R>(m, p, rng);
-  if (idust2 < 0) { set_status(a, 2); return; }
-  L.c[HC3D_CNT_TOT]++;
-  for (;;) {
-    const int64_t c = cidx(m, p.ir, p.it, p.ip);
-    L.c[HC3D_CNT_EVENTS]++;
-    ntot++;
-    if (ran<R>(rng) <= p.albedo[idust2]) {  // scattered
-      iflag = 1; iscat++; iint++;
-      if (a.ipeel == 1)
-        for (int k = 0; k < a.npeel; ++k) peeloff<R>(m, t, d, a, p, p.sip, 1, idust2, k, L);
-      stokes<R>(p, idust2, rng);
-      tr.add(5, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-    } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
-      atomicAdd(t.dbig + c, 1u);
-      p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
-      atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
-      const double tave = __ldg(m.tdust + 4 * c + idust2);
-      p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
-      p.cost = R(1) - R(2) * ran<R>(rng);
-      p.sint = xsqrt(R(1) - p.cost * p.cost);
-      p.phi = (R)kR2p * ran<R>(rng);
-      p.cosp = xcos(p.phi);
-      p.sinp = xsin(p.phi);
-      p.nub = lucydustfreq<R>(m, tave, idust2, rng);
-      iflag = 0;
-      opacset<R>(m, p, p.nub, a.rstar_cm);
-      if (a.ipeel == 1)
-        for (int k = 0; k < a.npeel; ++k) peeloff<R>(m, t, d, a, p, p.sip, 0, idust2, k, L);
-      iint++;
-      tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-    }
-    tau = -xlog(ran<R>(rng));
-    xpold = p.x; ypold = p.y; zpold = p.z;
-    p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
-    const int pir = p.ir, pit = p.it, pip = p.ip;
-    st = tauint<R>(m, t, p, tau, L, tr);
-    if (st == TI_ESCAPE) break;
-    if (st == TI_STAR) { L.c[HC3D_CNT_AFLUX]++; tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z); return; }
-    if (st == TI_FAULT) { L.c[HC3D_CNT_STUCK]++; set_status(a, 1); return; }
-    if (p.ir != pir || p.it != pit || p.ip != pip) iint = 0;
-    if (iint > a.iintmax || (a.max_interactions > 0 && ntot >= a.max_interactions)) {
+  if (st == TI_STAR) {
+    L.c[HC3D_CNT_AFLUX]++;
+    tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    return ST_DONE;
+  }
+  if (st == TI_FAULT) {
+    L.c[HC3D_CNT_STUCK]++;
+    set_status(a, 1);
+    return ST_DONE;
+  }
+  if (!first) {
+    if (p.ir != pir || p.it != pit || p.ip != pip) f.iint = 0;
+    if (f.iint > a.iintmax || (a.max_interactions > 0 && f.ntot >= a.max_interactions)) {
       atomicAdd(t.killed + cidx(m, p.ir, p.it, p.ip), 1u);
       L.c[HC3D_CNT_ABFLUX]++;
       tr.add(7, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-      return;
+      return ST_DONE;
     }
-    idust2 = select_dust<R>(m, p, rng);
-    if (idust2 < 0) { set_status(a, 2); return; }
   }
-  tr.add(3, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-  bin_escape<R>(t, d, a, p, xpold, ypold, zpold, iflag, iscat, L);
+  f.idust2 = select_dust<R>(m, p, rng);
+  if (f.idust2 < 0) {
+    set_status(a, 2);
+    return ST_DONE;
+  }
+  if (first) L.c[HC3D_CNT_TOT]++;
+  return ST_INTERACT;
+}
+
+// One interaction, propagate.f90:70-166: scattering (rec = the state before
+// stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
+template <class R>
+__device__ void interact(const DevModel& m, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
+                         Local& L, Tracer& tr, PeelRec<R>& rec) {
+  const int64_t c = cidx(m, p.ir, p.it, p.ip);
+  const int idust2 = f.idust2;
+  L.c[HC3D_CNT_EVENTS]++;
+  f.ntot++;
+  if (ran<R>(rng) <= p.albedo[idust2]) {  // scattered
+    f.iflag = 1; f.iscat++; f.iint++;
+    make_rec<R>(rec, p, a, 1, idust2);
+    stokes<R>(p, idust2, rng);
+    tr.add(5, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+  } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
+    atomicAdd(t.dbig + c, 1u);
+    p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
+    atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
+    const double tave = __ldg(m.tdust + 4 * c + idust2);
+    p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+    p.cost = R(1) - R(2) * ran<R>(rng);
+    p.sint = xsqrt(R(1) - p.cost * p.cost);
+    p.phi = (R)kR2p * ran<R>(rng);
+    p.cosp = xcos(p.phi);
+    p.sinp = xsin(p.phi);
+    p.nub = lucydustfreq<R>(m, tave, idust2, rng);
+    f.iflag = 0;
+    opacset<R>(m, p, p.nub, a.rstar_cm);
+    make_rec<R>(rec, p, a, 0, idust2);
+    f.iint++;
+    tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+  }
+}
+
+__device__ __forceinline__ void flush(const DevTallies& t, Local& L) {
+#pragma unroll
+  for (int i = 0; i < 15; ++i)
+    if (L.c[i]) atomicAdd(t.counters + i, L.c[i]);
+}
+
+// ---- per-thread form: one packet at a time, its peel-off rays inline --------------
+// Used for the trace harness and for runs without peel-off (the Lucy
+// iterations), where a packet's history is its only work.
+template <class R>
+__device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
+                           Local& L, Tracer& tr) {
+  Pkt<R> p;
+  PeelRec<R> rec;
+  emit<R>(m, a, p, rng, rec, tr);
+  if (a.ipeel == 1)
+    for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
+  Flow f;
+  f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
+  f.iflag = 0; f.iscat = 0; f.iint = 0; f.idust2 = 0; f.ntot = 0;
+  int st = walk<R>(m, t, d, a, p, rng, f, L, tr, true);
+  while (st == ST_INTERACT) {
+    interact<R>(m, t, a, p, rng, f, L, tr, rec);
+    if (a.ipeel == 1)
+      for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
+    st = walk<R>(m, t, d, a, p, rng, f, L, tr, false);
+  }
 }
 
 template <class R>
@@ -974,9 +1058,89 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
       run_packet<R>(m, t, d, a, rng, L, tr);
     }
   }
+  flush(t, L);
+}
+
+// ---- wavefront form: packet pool + peel-off event queue ----------------------------
+// Each thread owns one pool slot.  A wave advances every live packet by up
+// to E events (taking new packets from the batch as slots free up) and
+// appends each event's peel-off record to a queue; k_peel then walks every
+// (event, direction) ray of the queue across the whole device.  A packet
+// with a very long history therefore costs only its own chain of
+// interactions, not that chain times the peel-off rays.
+template <class R>
+struct Slot {
+  Pkt<R> p;
+  Flow f;
+  uint64_t pid;
+  uint32_t c0;
+  int left;
+  int stage;  // 0 = empty, 1 = an interaction is pending
+};
+
+template <class R>
+__global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDims d, RunArgs a, Slot<R>* pool,
+                                               PeelRec<R>* queue, unsigned long long* qcount, int E,
+                                               unsigned int* alive) {
+  namespace cg = cooperative_groups;
+  Local L;
 #pragma unroll
-  for (int i = 0; i < 15; ++i)
-    if (L.c[i]) atomicAdd(t.counters + i, L.c[i]);
+  for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Slot<R> s = pool[gid];
+  Rng rng;
+  rng_init(rng, a.key0, a.key1, s.pid);
+  if (s.stage) {
+    rng.c0 = s.c0;
+    rng.left = s.left;
+    if (rng.left > 0) philox(rng.c0 - 1, 0u, rng.c2, rng.c3, rng.k0, rng.k1, rng.b);
+  }
+  Tracer tr{nullptr, 0, 0};
+  PeelRec<R> rec;
+  for (int nrec = 0; nrec < E; ++nrec) {
+    if (s.stage == 0) {
+      const unsigned long long pid = atomicAdd(a.work, 1ull);
+      if (pid >= (unsigned long long)a.np) break;
+      s.pid = (uint64_t)(a.packet_offset + (int64_t)pid);
+      rng_init(rng, a.key0, a.key1, s.pid);
+      emit<R>(m, a, s.p, rng, rec, tr);
+      s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
+      s.f.iflag = 0; s.f.iscat = 0; s.f.iint = 0; s.f.idust2 = 0; s.f.ntot = 0;
+      s.stage = 2;  // emitted: walk to the first interaction after the record
+    } else {
+      interact<R>(m, t, a, s.p, rng, s.f, L, tr, rec);
+    }
+    if (a.ipeel) {
+      cg::coalesced_group g = cg::coalesced_threads();
+      unsigned long long base = 0;
+      if (g.thread_rank() == 0) base = atomicAdd(qcount, (unsigned long long)g.size());
+      base = g.shfl(base, 0);
+      queue[base + g.thread_rank()] = rec;
+    }
+    const int st = walk<R>(m, t, d, a, s.p, rng, s.f, L, tr, s.stage == 2);
+    s.stage = st == ST_INTERACT ? 1 : 0;
+  }
+  s.c0 = rng.c0;
+  s.left = rng.left;
+  pool[gid] = s;
+  if (s.stage) atomicAdd(alive, 1u);
+  flush(t, L);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_peel(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+                                               const PeelRec<R>* queue, const unsigned long long* qcount) {
+  Local L;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  const unsigned long long n = *qcount * (unsigned long long)a.npeel;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned long long e = i / (unsigned)a.npeel;
+    const int k = (int)(i - e * (unsigned)a.npeel);
+    peel_ray<R>(m, t, d, a, queue[e], k, L);
+  }
+  flush(t, L);
 }
 
 }  // namespace dev

@@ -136,6 +136,7 @@ SIGNATURES = {
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
+    "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),
     "hc3d_trace_packets": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, dp, C.c_int, P(TraceRec), C.c_int, i32p]),
     "hc3d_model_create": (C.c_int, [P(C.c_void_p), C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t]),
     "hc3d_model_destroy": (None, [C.c_void_p]),
@@ -365,6 +366,12 @@ class Context:
         v = C.c_double(0)
         self._check(lib().hc3d_last_kernel_ms(self._h, C.byref(v)))
         return v.value
+
+    def last_launch_stats(self) -> tuple[int, float, float]:
+        """(launches, transport ms, peel-off ms) of the last run."""
+        n, a, b = C.c_int(0), C.c_double(0), C.c_double(0)
+        self._check(lib().hc3d_last_launch_stats(self._h, C.byref(n), C.byref(a), C.byref(b)))
+        return n.value, a.value, b.value
 
     def lucy_update(self, ltot: float, np_: int, want_tdust: bool = True):
         m = self.model

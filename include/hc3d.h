@@ -219,6 +219,9 @@ void *hc3d_get_stream(hc3d_ctx *ctx);
 /* Device time in ms of the transport kernel of the last hc3d_run_iteration,
  * from CUDA events recorded on that stream around the launch. */
 int hc3d_last_kernel_ms(hc3d_ctx *ctx, double *ms);
+/* Kernel launches of the last hc3d_run_iteration and their device time, split
+ * into packet transport and peel-off ray walks (CUDA events on the stream). */
+int hc3d_last_launch_stats(hc3d_ctx *ctx, int *launches, double *transport_ms, double *peel_ms);
 
 /* ---- single-packet trace harness ---------------------------------------- */
 /* One record per propagation cell crossing / interaction of a traced packet. */
