@@ -47,6 +47,7 @@ struct hc3d_ctx {
   cudaEvent_t wev[3] = {nullptr, nullptr, nullptr};
   double last_ms = 0.0, last_transport_ms = 0.0, last_peel_ms = 0.0;
   int last_launches = 0;
+  std::vector<double> wave_log;  // per wave: E, active, alive after, transport ms, peel ms
   // wavefront form
   std::vector<void*> wave_allocs;
   WaveBufs wave{};
@@ -329,6 +330,7 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
   unsigned long long work = 0;
   c->last_transport_ms = c->last_peel_ms = 0.0;
   c->last_launches = 0;
+  c->wave_log.clear();
   for (int wave = 0;; ++wave) {
     const int64_t remaining = p->np - (int64_t)std::min<unsigned long long>(work, (unsigned long long)p->np);
     const int64_t active = std::min<int64_t>(c->pool_threads, alive_prev + remaining);
@@ -349,6 +351,7 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     c->last_transport_ms += t0;
     c->last_peel_ms += t1;
     c->last_launches += 2;
+    c->wave_log.insert(c->wave_log.end(), {(double)E, (double)active, (double)alive, (double)t0, (double)t1});
     alive_prev = alive;
     if (alive == 0 && work >= (unsigned long long)p->np) break;
   }
@@ -401,7 +404,8 @@ extern "C" int hc3d_create(hc3d_ctx** out, const hc3d_device_opts* opts) {
   std::vector<void*>& own = c->model_allocs;
   if (dalloc(c, own, &c->d_work, 1) || dalloc(c, own, &c->d_status, 1) ||
       dalloc(c, own, &c->d_peeldir, 4 * kMaxPeel) || dalloc(c, own, &c->d_ap2, 64) ||
-      dalloc(c, own, &c->d_maxrel, 1) || dalloc(c, own, &c->dt.counters, 16)) {
+      dalloc(c, own, &c->d_maxrel, 1) || dalloc(c, own, &c->dt.counters, 16) ||
+      dalloc(c, own, &c->dt.fault_log, kFaultLog) || dalloc(c, own, &c->dt.fault_count, 1)) {
     free_all(own);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -606,6 +610,7 @@ extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
     CK(cudaMemsetAsync(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(c->dims.nimg, 1), c->stream));
   }
   CK(cudaMemsetAsync(c->dt.counters, 0, sizeof(unsigned long long) * 16, c->stream));
+  CK(cudaMemsetAsync(c->dt.fault_count, 0, sizeof(unsigned long long), c->stream));
   CK(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
   CK(cudaStreamSynchronize(c->stream));
   c->scales_set = false;
@@ -659,6 +664,27 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   c->last_peel_ms = 0.0;
   c->last_launches = 1;
   c->epoch_np += p->np;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_get_fault_log(hc3d_ctx* c, uint64_t* entries, int max, int* n) {
+  if (!c || !n) return HC3D_ERR_INVALID;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpy(&cnt, c->dt.fault_count, sizeof(cnt), cudaMemcpyDeviceToHost));
+  *n = (int)std::min<unsigned long long>(cnt, (unsigned long long)kFaultLog);
+  if (entries && max > 0) {
+    const int k = std::min(*n, max);
+    if (k) CK(cudaMemcpy(entries, c->dt.fault_log, sizeof(uint64_t) * k, cudaMemcpyDeviceToHost));
+  }
+  *n = (int)std::min<unsigned long long>(cnt, (unsigned long long)0x7fffffff);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_get_wave_log(hc3d_ctx* c, double* out, int max_waves, int* n) {
+  if (!c || !n) return HC3D_ERR_INVALID;
+  *n = (int)(c->wave_log.size() / 5);
+  if (out)
+    std::copy(c->wave_log.begin(), c->wave_log.begin() + 5 * std::min(*n, std::max(max_waves, 0)), out);
   return HC3D_OK;
 }
 

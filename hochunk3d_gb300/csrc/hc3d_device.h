@@ -12,6 +12,7 @@ namespace hc3d {
 constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2, envelope, cavity)
 constexpr int kNo = 8;      // SED components (output.F90:232-239)
 constexpr int kMaxPeel = 256;
+constexpr int kFaultLog = 256;
 
 // Fortran-layout sizes of the tally arrays of one run configuration.
 struct TallyDims {
@@ -34,6 +35,8 @@ struct DevTallies {
   unsigned int* dbig;         // [ncell]
   unsigned long long* counters; // [16]
   double stokes_scale, square_scale, path_scale;
+  unsigned long long* fault_log;   // [kFaultLog]: packet id | code << 56
+  unsigned long long* fault_count;
 };
 
 // Read-only model data on the device.

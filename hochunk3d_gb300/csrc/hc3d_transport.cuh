@@ -124,6 +124,7 @@ struct Pkt {
 // per-thread counters, flushed once per thread
 struct Local {
   unsigned long long c[16];
+  int fault;
 };
 
 // trace record (hc3d_trace_rec of hc3d.h)
@@ -350,16 +351,25 @@ __device__ void opacset(const DevModel& m, Pkt<R>& p, double nu, double rstar_cm
 
 // ---- tauint (restated; module not shipped) -------------------------------------
 enum { TI_INTERACT = 0, TI_ESCAPE = 1, TI_STAR = 2, TI_FAULT = 3 };
+// fault codes of the fault log: walk left the index range, found no wall,
+// exceeded the crossing cap; species selection found no opacity
+enum { F_RANGE = 1, F_NOWALL = 2, F_CAP = 3, F_SELECT = 4 };
 
 template <class R>
 __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
   R tsum = R(0);
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   for (int n = 0;; ++n) {
-    if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) return TI_FAULT;
+    if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
+      L.fault = n > cap ? F_CAP : F_RANGE;
+      return TI_FAULT;
+    }
     R dt;
     int iface;
-    if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) return TI_FAULT;
+    if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+      L.fault = F_NOWALL;
+      return TI_FAULT;
+    }
     const int64_t c = cidx(m, p.ir, p.it, p.ip);
     const Rho<R> rho = load_rho<R>(m, c);
     R opac = R(0);
@@ -924,6 +934,14 @@ __device__ __forceinline__ void set_status(const RunArgs& a, int code) {
   if (a.status) atomicCAS(a.status, 0, code);
 }
 
+// Record a faulted packet (global id and fault code) in the fault log.
+__device__ __forceinline__ void log_fault(const DevTallies& t, const Rng& rng, int code) {
+  if (!t.fault_log) return;
+  const unsigned long long k = atomicAdd(t.fault_count, 1ull);
+  if (k < (unsigned long long)kFaultLog)
+    t.fault_log[k] = ((unsigned long long)rng.c2 | ((unsigned long long)rng.c3 << 32)) | ((unsigned long long)code << 56);
+}
+
 // tau sample + tauint + outcome, propagate.f90:46-62 (first) and 169-202.
 template <class R>
 __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Pkt<R>& p, Rng& rng,
@@ -948,6 +966,7 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
   if (st == TI_FAULT) {
     L.c[HC3D_CNT_STUCK]++;
     set_status(a, 1);
+    log_fault(t, rng, L.fault);
     return ST_DONE;
   }
   if (!first) {
@@ -961,7 +980,9 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
   }
   f.idust2 = select_dust<R>(m, p, rng);
   if (f.idust2 < 0) {
+    L.c[HC3D_CNT_STUCK]++;
     set_status(a, 2);
+    log_fault(t, rng, F_SELECT);
     return ST_DONE;
   }
   if (first) L.c[HC3D_CNT_TOT]++;
@@ -1036,6 +1057,7 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  L.fault = 0;
   if (a.inj) {
     // trace harness: one thread per traced packet, draws from the injected list
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1086,6 +1108,7 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  L.fault = 0;
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   Slot<R> s = pool[gid];
   Rng rng;
@@ -1133,6 +1156,7 @@ __global__ void __launch_bounds__(256) k_peel(DevModel m, DevTallies t, TallyDim
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  L.fault = 0;
   const unsigned long long n = *qcount * (unsigned long long)a.npeel;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {

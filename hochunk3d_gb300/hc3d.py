@@ -137,6 +137,8 @@ SIGNATURES = {
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),
+    "hc3d_get_fault_log": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_int, ip_]),
+    "hc3d_get_wave_log": (C.c_int, [C.c_void_p, dp, C.c_int, ip_]),
     "hc3d_trace_packets": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, dp, C.c_int, P(TraceRec), C.c_int, i32p]),
     "hc3d_model_create": (C.c_int, [P(C.c_void_p), C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t]),
     "hc3d_model_destroy": (None, [C.c_void_p]),
@@ -366,6 +368,22 @@ class Context:
         v = C.c_double(0)
         self._check(lib().hc3d_last_kernel_ms(self._h, C.byref(v)))
         return v.value
+
+    def fault_log(self) -> tuple[int, list[tuple[int, int]]]:
+        """(count, [(packet id, fault code), ...]) of packets stopped by a fault."""
+        buf = np.zeros(256, dtype=np.uint64)
+        n = C.c_int(0)
+        self._check(lib().hc3d_get_fault_log(self._h, buf.ctypes.data_as(P(C.c_uint64)), 256, C.byref(n)))
+        k = min(n.value, 256)
+        return n.value, [(int(v) & ((1 << 56) - 1), int(v) >> 56) for v in buf[:k]]
+
+    def wave_log(self) -> np.ndarray:
+        """Per wave of the last peeled run: E, active, alive, transport ms, peel ms."""
+        n = C.c_int(0)
+        lib().hc3d_get_wave_log(self._h, None, 0, C.byref(n))
+        out = np.zeros((max(n.value, 1), 5))
+        self._check(lib().hc3d_get_wave_log(self._h, _ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
 
     def last_launch_stats(self) -> tuple[int, float, float]:
         """(launches, transport ms, peel-off ms) of the last run."""

@@ -222,6 +222,15 @@ int hc3d_last_kernel_ms(hc3d_ctx *ctx, double *ms);
 /* Kernel launches of the last hc3d_run_iteration and their device time, split
  * into packet transport and peel-off ray walks (CUDA events on the stream). */
 int hc3d_last_launch_stats(hc3d_ctx *ctx, int *launches, double *transport_ms, double *peel_ms);
+/* Packets stopped by a fault since the last hc3d_zero_tallies(): *n receives
+ * the count and entries[0..min(n,max,256)-1] the global packet id in the low
+ * 56 bits and the fault code in the high 8 (1 index range, 2 no wall found,
+ * 3 crossing cap, 4 no opacity to select a species).  Replaying a logged id
+ * through hc3d_trace_packets with its counter-based uniforms reproduces it. */
+int hc3d_get_fault_log(hc3d_ctx *ctx, uint64_t *entries, int max, int *n);
+/* Per wave of the last peeled run: event budget E, threads that could run,
+ * packets alive after the wave, transport ms, peel-off ms (5 doubles each). */
+int hc3d_get_wave_log(hc3d_ctx *ctx, double *out, int max_waves, int *n);
 
 /* ---- single-packet trace harness ---------------------------------------- */
 /* One record per propagation cell crossing / interaction of a traced packet. */

@@ -839,7 +839,7 @@ static void orc_propagate(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, o
   if (st == TI_STAR) { t->fx.counters[HC3D_CNT_AFLUX]++; trace_add(tr, 4, p->ir, p->it, p->ip, 0, 0, p->xp, p->yp, p->zp); return; }
   if (st == TI_FAULT) { t->fx.counters[HC3D_CNT_STUCK]++; t->errors++; return; }
   int idust2 = orc_select_dust(c, p, rng);
-  if (idust2 < 0) { t->errors++; return; }
+  if (idust2 < 0) { t->fx.counters[HC3D_CNT_STUCK]++; t->errors++; return; }
   t->fx.counters[HC3D_CNT_TOT]++;
   for (;;) {
     const int64_t cell = cidx(c, p->ir, p->it, p->ip);
@@ -887,7 +887,7 @@ static void orc_propagate(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, o
       return;
     }
     idust2 = orc_select_dust(c, p, rng);
-    if (idust2 < 0) { t->errors++; return; }
+    if (idust2 < 0) { t->fx.counters[HC3D_CNT_STUCK]++; t->errors++; return; }
   }
 bin:
   trace_add(tr, 3, p->ir, p->it, p->ip, 0, 0, p->xp, p->yp, p->zp);
