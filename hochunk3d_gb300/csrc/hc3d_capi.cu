@@ -293,7 +293,7 @@ int ensure_wave(hc3d_ctx* c) {
   if (c->wave.pool) return HC3D_OK;
   const bool f64 = c->precision == HC3D_PREC_FP64;
   int per_sm = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f64 ? wave_fn_fp64() : wave_fn_mixed(), 128, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f64 ? wave_fn_fp64() : wave_fn_mixed(), 128, c->dm.dust_smem));
   if (per_sm < 1) per_sm = 1;
   c->wave_blocks = c->sm_count * per_sm;
   c->pool_threads = (int64_t)c->wave_blocks * 128;
@@ -484,6 +484,38 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
     c->dm.kappav[s] = t->kappav[src];
     c->kappav[s] = t->kappav[src];
   }
+  // unique dust tables: slots whose rows are identical share one table
+  {
+    const size_t L = (size_t)t->nlammax;
+    std::vector<double> un(L * kSlots), uk(un.size()), ua(un.size()), ug(un.size()), up(un.size());
+    int ntab = 0;
+    size_t smem = 0;
+    for (int s = 0; s < kSlots; ++s) {
+      const int nl = c->dm.nlambda[s];
+      int found = -1;
+      for (int u = 0; u < ntab && found < 0; ++u) {
+        if (c->dm.tab_nl[u] != nl) continue;
+        const size_t so = (size_t)s * L, uo = (size_t)u * L, b = sizeof(double) * nl;
+        if (!std::memcmp(&nud[so], &un[uo], b) && !std::memcmp(&kap[so], &uk[uo], b) &&
+            !std::memcmp(&alb[so], &ua[uo], b) && !std::memcmp(&gg[so], &ug[uo], b) && !std::memcmp(&pl[so], &up[uo], b))
+          found = u;
+      }
+      if (found < 0) {
+        found = ntab++;
+        const size_t so = (size_t)s * L, uo = (size_t)found * L;
+        std::copy(&nud[so], &nud[so] + L, &un[uo]); std::copy(&kap[so], &kap[so] + L, &uk[uo]);
+        std::copy(&alb[so], &alb[so] + L, &ua[uo]); std::copy(&gg[so], &gg[so] + L, &ug[uo]);
+        std::copy(&pl[so], &pl[so] + L, &up[uo]);
+        c->dm.tab_nl[found] = nl;
+        smem += 5 * sizeof(double) * (size_t)nl;
+      }
+      c->dm.table_of[s] = found;
+    }
+    c->dm.ntab = ntab;
+    c->dm.dust_smem = smem <= 48 * 1024 ? (int)smem : 0;
+    un.resize(L * ntab); uk.resize(un.size()); ua.resize(un.size()); ug.resize(un.size()); up.resize(un.size());
+    nud.swap(un); kap.swap(uk); alb.swap(ua); gg.swap(ug); pl.swap(up);
+  }
   std::vector<void*>& own = c->model_allocs;
   int r;
   double *d_nud, *d_kap, *d_alb, *d_g, *d_pl, *d_lT, *d_nuint, *d_kB, *d_hn, *d_an, *d_ln, *d_lh;
@@ -642,9 +674,9 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
     int per_sm = 0;
     cudaError_t e;
     if (c->precision == HC3D_PREC_FP64) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_fp64(), cfg.threads, 0);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_fp64(), cfg.threads, c->dm.dust_smem);
     } else {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_mixed(), cfg.threads, 0);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_mixed(), cfg.threads, c->dm.dust_smem);
     }
     if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     cfg.blocks = c->sm_count * per_sm;

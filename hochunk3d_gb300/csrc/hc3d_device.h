@@ -60,7 +60,11 @@ struct DevModel {
   // dust tables
   int nlammax;
   int nlambda[kSlots];
-  const double* nudust; const double* kappad; const double* adust; const double* gdust; const double* pldust;
+  int ntab;               // unique dust tables (species slots reading the same file share one)
+  int table_of[kSlots];   // slot -> table
+  int tab_nl[kSlots];     // rows of each table
+  int dust_smem;          // bytes of dynamic shared memory staging the tables; 0 = global memory
+  const double* nudust; const double* kappad; const double* adust; const double* gdust; const double* pldust;  // (nlammax, ntab)
   double kappav[kSlots];
   int nT, nnu;
   const double* lTint; const double* nuint; const double* kapBint;  // kapBint (nT,nnu,kSlots)

@@ -7,7 +7,7 @@ namespace hc3d {
 
 cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                    const LaunchCfg& cfg) {
-  dev::k_transport<float><<<cfg.blocks, cfg.threads, 0, cfg.stream>>>(m, t, d, a);
+  dev::k_transport<float><<<cfg.blocks, cfg.threads, m.dust_smem, cfg.stream>>>(m, t, d, a);
   return cudaGetLastError();
 }
 
@@ -28,7 +28,7 @@ cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const Tall
                               cudaEvent_t ev[3]) {
   cudaError_t e;
   if (ev && (e = cudaEventRecord(ev[0], wave.stream)) != cudaSuccess) return e;
-  dev::k_wave<float><<<wave.blocks, wave.threads, 0, wave.stream>>>(
+  dev::k_wave<float><<<wave.blocks, wave.threads, m.dust_smem, wave.stream>>>(
       m, t, d, a, static_cast<dev::Slot<float>*>(w.pool), static_cast<dev::PeelRec<float>*>(w.queue), w.qcount, E, w.alive);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;

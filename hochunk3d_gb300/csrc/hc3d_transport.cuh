@@ -176,10 +176,11 @@ struct Walls {
 
 // radface.f90:44-62.  FP64 form: the reference's (-b +- sqrt(D))/2.  Mixed
 // form: the same roots in FP64 by the cancellation-free q = -(b+sign(b)sqrt D)/2,
-// roots q and c/q.
+// roots q and c/q; on the sphere the packet stands on (own) the roots are
+// exactly 0 and -b.
 template <class R>
 __device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, double uz, double x, double y, double z,
-                                        double R2_1, double R2_2) {
+                                        double R2_1, double R2_2, int own) {
   const double bb = 2.0 * (x * ux + y * uy + uz * z);
   const double rr = x * x + y * y + z * z;
   if (sizeof(R) == 8) {
@@ -198,34 +199,48 @@ __device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, doubl
       w.insert((R)((-bb - descr) * 0.5), 2);
     }
   } else {
-    double cc = rr - R2_1;
-    double descr = bb * bb - 4.0 * cc;
-    if (descr > 0.0) {
-      double q = -0.5 * (bb + copysign(sqrt(descr), bb));
-      w.insert((R)q, 1);
-      w.insert((R)(cc / q), 1);
-    }
-    cc = rr - R2_2;
-    descr = bb * bb - 4.0 * cc;
-    if (descr > 0.0) {
-      double q = -0.5 * (bb + copysign(sqrt(descr), bb));
-      w.insert((R)q, 2);
-      w.insert((R)(cc / q), 2);
+#pragma unroll
+    for (int id = 1; id <= 2; ++id) {
+      if (own == id) {
+        w.insert(R(0), id);
+        w.insert((R)(-bb), id);
+        continue;
+      }
+      const double cc = rr - (id == 1 ? R2_1 : R2_2);
+      const double descr = bb * bb - 4.0 * cc;
+      if (descr > 0.0) {
+        const double q = -0.5 * (bb + copysign(sqrt(descr), bb));
+        w.insert((R)q, id);
+        w.insert((R)(cc / q), id);
+      }
     }
   }
 }
 
 // thetaface (module not shipped; restated): one cone wall on the nappe of its
-// hemisphere; tan2 < 0 is the midplane plane z = 0; tan2 == 0 is a pole.
+// hemisphere; tan2 < 0 is the midplane plane z = 0; tan2 == 0 is a pole.  In
+// the mixed form the cone the packet stands on has the exact root 0 and the
+// second root -b/a: FP32 would otherwise place two roots of that cone within
+// rounding of zero at grazing incidence and let the walk re-cross it.
 template <class R>
-__device__ __forceinline__ void cone_roots(Walls<R>& w, R ux, R uy, R uz, R x, R y, R z, R tan2, R hemi, int id) {
+__device__ __forceinline__ void cone_roots(Walls<R>& w, R ux, R uy, R uz, R x, R y, R z, R tan2, R hemi, int id,
+                                           bool own) {
   if (tan2 == R(0)) return;
   if (tan2 < R(0)) {
-    if (uz != R(0)) w.insert(-z / uz, id);
+    if (own) w.insert(R(0), id);
+    else if (uz != R(0)) w.insert(-z / uz, id);
     return;
   }
   const R a = ux * ux + uy * uy - tan2 * uz * uz;
   const R b = R(2) * (x * ux + y * uy - tan2 * z * uz);
+  if (own) {
+    w.insert(R(0), id);
+    if (a != R(0)) {
+      const R t = -b / a;
+      if ((z + t * uz) * hemi > R(0)) w.insert(t, id);
+    }
+    return;
+  }
   const R cq = x * x + y * y - tan2 * z * z;
   if (a == R(0)) {
     if (b != R(0)) {
@@ -254,28 +269,37 @@ template <class R> __device__ __forceinline__ R barr_of(const DevModel& m, int i
 template <> __device__ __forceinline__ float barr_of<float>(const DevModel& m, int i) { return __ldg(m.barrf + i); }
 template <> __device__ __forceinline__ double barr_of<double>(const DevModel& m, int i) { return __ldg(m.barrd + i); }
 
-// The wall machinery of one step (peeloff_3d.f90:92-115).
+// The wall a packet stands on after crossing wall iface of its old cell, as a
+// wall id of the new cell (1<->2, 3<->4, 5<->6).
+__device__ __forceinline__ int own_after(int iface) { return ((iface - 1) ^ 1) + 1; }
+
+// The wall machinery of one step (peeloff_3d.f90:92-115).  on_wall is 0 off
+// the walls, else the id (1..6) of the wall of the current cell the packet
+// stands on; the FP64 form uses it only as the reference's on_wall flag.
 template <class R>
 __device__ __forceinline__ bool next_wall(const DevModel& m, R ux, R uy, R uz, double x, double y, double z, int ir,
                                           int it, int ip, int on_wall, R& dt, int& iface) {
   Walls<R> w;
   w.reset();
-  radface<R>(w, (double)ux, (double)uy, (double)uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir));
+  const int own = sizeof(R) == 4 ? on_wall : 0;
+  radface<R>(w, (double)ux, (double)uy, (double)uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir), own);
   if (m.ntg > 2) {
     const R xr = (R)x, yr = (R)y, zr = (R)z;
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3);
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4);
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3, own == 3);
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4, own == 4);
     if (m.npg > 2) {
       // phiface.f90:48-56 with C = D = 0
       const R A1 = aarr_of<R>(m, ip - 1), B1 = barr_of<R>(m, ip - 1);
       const R A2 = aarr_of<R>(m, ip), B2 = barr_of<R>(m, ip);
       const R d1 = A1 * ux + B1 * uy;
-      if (d1 != R(0)) w.insert(-(A1 * xr + B1 * yr) / d1, 5);
+      if (own == 5) w.insert(R(0), 5);
+      else if (d1 != R(0)) w.insert(-(A1 * xr + B1 * yr) / d1, 5);
       const R d2 = A2 * ux + B2 * uy;
-      if (d2 != R(0)) w.insert(-(A2 * xr + B2 * yr) / d2, 6);
+      if (own == 6) w.insert(R(0), 6);
+      else if (d2 != R(0)) w.insert(-(A2 * xr + B2 * yr) / d2, 6);
     }
   }
-  return w.next(on_wall, dt, iface);
+  return w.next(on_wall != 0, dt, iface);
 }
 
 // wall -> index step, peeloff_3d.f90:120-139
@@ -316,36 +340,76 @@ __device__ __forceinline__ unsigned long long fx(double v, double scale) {
   return (unsigned long long)llround(v * scale);
 }
 
+// ---- dust tables: unique per-species tables, staged in shared memory ---------------
+struct DustView {
+  const double* nud[kSlots];
+  const double* kap[kSlots];
+  const double* alb[kSlots];
+  const double* g[kSlots];
+  const double* pl[kSlots];
+};
+
+// Copy the unique dust tables into the block's dynamic shared memory (when
+// the host sized it, DevModel::dust_smem > 0) and point the view at them;
+// otherwise read them from global memory.  Called by every thread of the
+// block before any divergence.
+__device__ __forceinline__ void dust_view(const DevModel& m, double* smem, DustView& v) {
+  size_t off = 0;
+  for (int u = 0; u < m.ntab; ++u) {
+    const int nl = m.tab_nl[u];
+    const size_t go = (size_t)u * m.nlammax;
+    if (m.dust_smem > 0) {
+      double* base = smem + off;
+      for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+        base[i] = m.nudust[go + i];
+        base[nl + i] = m.kappad[go + i];
+        base[2 * nl + i] = m.adust[go + i];
+        base[3 * nl + i] = m.gdust[go + i];
+        base[4 * nl + i] = m.pldust[go + i];
+      }
+      v.nud[u] = base; v.kap[u] = base + nl; v.alb[u] = base + 2 * nl; v.g[u] = base + 3 * nl; v.pl[u] = base + 4 * nl;
+      off += 5 * (size_t)nl;
+    } else {
+      v.nud[u] = m.nudust + go; v.kap[u] = m.kappad + go; v.alb[u] = m.adust + go; v.g[u] = m.gdust + go;
+      v.pl[u] = m.pldust + go;
+    }
+  }
+  if (m.dust_smem > 0) __syncthreads();
+}
+
 // ---- opacset, dust.f90:9-80 (FP64 lookups; results stored in R) ---------------
+// Computed once per unique table; species slots sharing a dust file share
+// the result (only kappa_V differs), which is what the per-slot loop of the
+// reference computes for them.
 template <class R>
-__device__ void opacset(const DevModel& m, Pkt<R>& p, double nu, double rstar_cm) {
-#pragma unroll
-  for (int id = 0; id < kSlots; ++id) {
-    const int nl = m.nlambda[id];
-    const size_t o = (size_t)id * m.nlammax;
-    const double* nud = m.nudust + o;
-    double g, pl, kappa, albedo;
-    if (nu >= __ldg(nud)) {
-      g = __ldg(m.gdust + o); pl = __ldg(m.pldust + o); kappa = __ldg(m.kappad + o); albedo = __ldg(m.adust + o);
-    } else if (nu <= __ldg(nud + nl - 1)) {
-      const size_t k = o + nl - 1;
-      g = __ldg(m.gdust + k); pl = __ldg(m.pldust + k); kappa = __ldg(m.kappad + k); albedo = __ldg(m.adust + k);
+__device__ void opacset(const DevModel& m, const DustView& v, Pkt<R>& p, double nu, double rstar_cm) {
+  double gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
+  for (int u = 0; u < m.ntab; ++u) {
+    const int nl = m.tab_nl[u];
+    const double* nud = v.nud[u];
+    if (nu >= nud[0]) {
+      gt[u] = v.g[u][0]; plt[u] = v.pl[u][0]; kt[u] = v.kap[u][0]; at[u] = v.alb[u][0];
+    } else if (nu <= nud[nl - 1]) {
+      gt[u] = v.g[u][nl - 1]; plt[u] = v.pl[u][nl - 1]; kt[u] = v.kap[u][nl - 1]; at[u] = v.alb[u][nl - 1];
     } else {
       int i0 = 1, i1 = nl;
       while (i1 - i0 > 1) {
-        int i = (i1 + i0) / 2;
-        if (nu <= __ldg(nud + i - 1)) i0 = i; else i1 = i;
+        const int i = (i1 + i0) / 2;
+        if (nu <= nud[i - 1]) i0 = i; else i1 = i;
       }
-      const double n1 = __ldg(nud + i1 - 1), n0 = __ldg(nud + i0 - 1);
+      const double n1 = nud[i1 - 1], n0 = nud[i0 - 1];
       const double f = (nu - n1) / (n0 - n1), fm1 = 1.0 - f;
-      const size_t k1 = o + i1 - 1, k0 = o + i0 - 1;
-      g = fm1 * __ldg(m.gdust + k1) + f * __ldg(m.gdust + k0);
-      pl = fm1 * __ldg(m.pldust + k1) + f * __ldg(m.pldust + k0);
-      kappa = fm1 * __ldg(m.kappad + k1) + f * __ldg(m.kappad + k0);
-      albedo = fm1 * __ldg(m.adust + k1) + f * __ldg(m.adust + k0);
+      gt[u] = fm1 * v.g[u][i1 - 1] + f * v.g[u][i0 - 1];
+      plt[u] = fm1 * v.pl[u][i1 - 1] + f * v.pl[u][i0 - 1];
+      kt[u] = fm1 * v.kap[u][i1 - 1] + f * v.kap[u][i0 - 1];
+      at[u] = fm1 * v.alb[u][i1 - 1] + f * v.alb[u][i0 - 1];
     }
-    p.g[id] = (R)g; p.pl[id] = (R)pl; p.albedo[id] = (R)albedo;
-    p.kapd[id] = (R)(kappa * rstar_cm * m.kappav[id]);
+  }
+#pragma unroll
+  for (int id = 0; id < kSlots; ++id) {
+    const int u = m.table_of[id];
+    p.g[id] = (R)gt[u]; p.pl[id] = (R)plt[u]; p.albedo[id] = (R)at[u];
+    p.kapd[id] = (R)(kt[u] * rstar_cm * m.kappav[id]);
   }
 }
 
@@ -406,7 +470,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     p.x += (double)dt * (double)p.ux;
     p.y += (double)dt * (double)p.uy;
     p.z += (double)dt * (double)p.uz;
-    p.on_wall = 1;
+    p.on_wall = own_after(iface);
     tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
     if (p.ir == m.nrg) return TI_ESCAPE;
     if (p.ir == 0) return TI_STAR;
@@ -422,11 +486,15 @@ __device__ int select_dust(const DevModel& m, const Pkt<R>& p, Rng& rng) {
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
   if (opac == R(0)) return -1;
+  int last = -1;
   for (int s = 0; s < kSlots; ++s) {
     frac += p.kapd[s] * rho.v[s] / opac;
+    if (p.kapd[s] * rho.v[s] > R(0)) last = s;
     if (xran <= frac + (R)(double)1.e-10f) return s;
   }
-  return -1;
+  // FP32 fractions can sum to just below 1; the draw then belongs to the
+  // last species with opacity (the FP64 form keeps the reference's stop)
+  return sizeof(R) == 4 ? last : -1;
 }
 
 // ---- dustmat.f90:40-65 -----------------------------------------------------------
@@ -595,7 +663,8 @@ template <class R>
 struct PeelRec {
   double x, y, z;
   int ir, it, ip;
-  int flags;  // bit0 on_wall, bit1 scattered, bits2-4 i_orig, bits5-6 idust2, bit7 stellar-surface emission
+  int flags;  // bit0 on_wall, bit1 scattered, bits2-4 i_orig, bits5-6 idust2, bit7 stellar-surface emission,
+              // bits8-10 id of the wall the event sits on
   int inub;
   R sip, sqp, sup, svp;
   R d0, d1, d2, d3, d4;  // scattered: cost, sint, phi, cosp, sinp of the incident packet; stellar: cosb, sinb, coslp, sinlp
@@ -612,7 +681,7 @@ template <class R>
 __device__ __forceinline__ void make_rec(PeelRec<R>& e, const Pkt<R>& p, const RunArgs& a, int iflag, int idust2) {
   e.x = p.x; e.y = p.y; e.z = p.z;
   e.ir = p.ir; e.it = p.it; e.ip = p.ip;
-  e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5);
+  e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5) | (p.on_wall << 8);
   e.inub = nu_bin(a, p.nub);
   e.sip = p.sip; e.sqp = p.sqp; e.sup = p.sup; e.svp = p.svp;
   e.d0 = p.cost; e.d1 = p.sint; e.d2 = p.phi; e.d3 = p.cosp; e.d4 = p.sinp;
@@ -652,7 +721,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   }
   double xp1 = e.x, yp1 = e.y, zp1 = e.z;
   int ir = e.ir, it = e.it, ip = e.ip;
-  int on_wall = flags & 1;
+  int on_wall = (flags >> 8) & 7;
   const R ux1 = sinte * cospe, uy1 = sinte * sinpe, uz1 = coste;
   L.c[HC3D_CNT_PEELS]++;
   if (on_wall) {
@@ -662,8 +731,12 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     if (inner_wall && !outwards) {
       if (ir == 1) return;
       ir = ir - 1;
+      on_wall = 2;
     }
-    if (!inner_wall && outwards) ir = ir + 1;
+    if (!inner_wall && outwards) {
+      ir = ir + 1;
+      on_wall = 1;
+    }
   }
   double tsum = 0.0;  // FP64 escape tau in both forms
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
@@ -692,7 +765,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     xp1 += (double)dt * (double)ux1;
     yp1 += (double)dt * (double)uy1;
     zp1 += (double)dt * (double)uz1;
-    on_wall = 1;
+    on_wall = own_after(iface);
     if (ir == m.nrg) break;
     if (ir == 0) return;
   }
@@ -864,7 +937,7 @@ enum { ST_DONE = 0, ST_INTERACT = 1 };
 // initp_sample (limb = 0) and initp_transform (initp_common.f90:1-94).  rec
 // receives the stellar-surface peel-off event.
 template <class R>
-__device__ void emit(const DevModel& m, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
+__device__ void emit(const DevModel& m, const DustView& dv, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
   p.on_wall = 0;
   p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
   for (;;) {
@@ -911,7 +984,7 @@ __device__ void emit(const DevModel& m, const RunArgs& a, Pkt<R>& p, Rng& rng, P
   p.cosp = xcos(p.phi);
   p.nub = atmosfreq<R>(m, rng);
   p.i_orig = 1;
-  opacset<R>(m, p, p.nub, a.rstar_cm);
+  opacset<R>(m, dv, p, p.nub, a.rstar_cm);
   const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
   p.z = (double)p.cosb;
   const double rp_ = (double)p.sinb;
@@ -992,7 +1065,7 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
 // One interaction, propagate.f90:70-166: scattering (rec = the state before
 // stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
 template <class R>
-__device__ void interact(const DevModel& m, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
+__device__ void interact(const DevModel& m, const DustView& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
                          Local& L, Tracer& tr, PeelRec<R>& rec) {
   const int64_t c = cidx(m, p.ir, p.it, p.ip);
   const int idust2 = f.idust2;
@@ -1016,7 +1089,7 @@ __device__ void interact(const DevModel& m, const DevTallies& t, const RunArgs& 
     p.sinp = xsin(p.phi);
     p.nub = lucydustfreq<R>(m, tave, idust2, rng);
     f.iflag = 0;
-    opacset<R>(m, p, p.nub, a.rstar_cm);
+    opacset<R>(m, dv, p, p.nub, a.rstar_cm);
     make_rec<R>(rec, p, a, 0, idust2);
     f.iint++;
     tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
@@ -1033,11 +1106,11 @@ __device__ __forceinline__ void flush(const DevTallies& t, Local& L) {
 // Used for the trace harness and for runs without peel-off (the Lucy
 // iterations), where a packet's history is its only work.
 template <class R>
-__device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
+__device__ void run_packet(const DevModel& m, const DustView& dv, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
                            Local& L, Tracer& tr) {
   Pkt<R> p;
   PeelRec<R> rec;
-  emit<R>(m, a, p, rng, rec, tr);
+  emit<R>(m, dv, a, p, rng, rec, tr);
   if (a.ipeel == 1)
     for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
   Flow f;
@@ -1045,7 +1118,7 @@ __device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDi
   f.iflag = 0; f.iscat = 0; f.iint = 0; f.idust2 = 0; f.ntot = 0;
   int st = walk<R>(m, t, d, a, p, rng, f, L, tr, true);
   while (st == ST_INTERACT) {
-    interact<R>(m, t, a, p, rng, f, L, tr, rec);
+    interact<R>(m, dv, t, a, p, rng, f, L, tr, rec);
     if (a.ipeel == 1)
       for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
     st = walk<R>(m, t, d, a, p, rng, f, L, tr, false);
@@ -1054,6 +1127,9 @@ __device__ void run_packet(const DevModel& m, const DevTallies& t, const TallyDi
 
 template <class R>
 __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, TallyDims d, RunArgs a) {
+  extern __shared__ double dust_smem[];
+  DustView dv;
+  dust_view(m, dust_smem, dv);
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
@@ -1067,7 +1143,7 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
       rng.inj = a.inj + (size_t)k * a.ninj;
       rng.ninj = a.ninj;
       Tracer tr{reinterpret_cast<TraceRec*>(a.trace) + (size_t)k * a.max_rec, a.max_rec, 0};
-      run_packet<R>(m, t, d, a, rng, L, tr);
+      run_packet<R>(m, dv, t, d, a, rng, L, tr);
       a.nrec[k] = tr.n;
     }
   } else {
@@ -1077,7 +1153,7 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
       if (pid >= (unsigned long long)a.np) break;
       Rng rng;
       rng_init(rng, a.key0, a.key1, (uint64_t)(a.packet_offset + (int64_t)pid));
-      run_packet<R>(m, t, d, a, rng, L, tr);
+      run_packet<R>(m, dv, t, d, a, rng, L, tr);
     }
   }
   flush(t, L);
@@ -1105,6 +1181,9 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
                                                PeelRec<R>* queue, unsigned long long* qcount, int E,
                                                unsigned int* alive) {
   namespace cg = cooperative_groups;
+  extern __shared__ double dust_smem[];
+  DustView dv;
+  dust_view(m, dust_smem, dv);
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
@@ -1126,12 +1205,12 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
       if (pid >= (unsigned long long)a.np) break;
       s.pid = (uint64_t)(a.packet_offset + (int64_t)pid);
       rng_init(rng, a.key0, a.key1, s.pid);
-      emit<R>(m, a, s.p, rng, rec, tr);
+      emit<R>(m, dv, a, s.p, rng, rec, tr);
       s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
       s.f.iflag = 0; s.f.iscat = 0; s.f.iint = 0; s.f.idust2 = 0; s.f.ntot = 0;
       s.stage = 2;  // emitted: walk to the first interaction after the record
     } else {
-      interact<R>(m, t, a, s.p, rng, s.f, L, tr, rec);
+      interact<R>(m, dv, t, a, s.p, rng, s.f, L, tr, rec);
     }
     if (a.ipeel) {
       cg::coalesced_group g = cg::coalesced_threads();
