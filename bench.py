@@ -187,7 +187,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--step-seconds", type=float, default=2.0)
-    ap.add_argument("--packets", type=int, default=0, help="packets per step (0 = calibrate)")
+    ap.add_argument("--packets", type=int, default=100000, help="packets per step (0 = calibrate)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
     args = ap.parse_args()

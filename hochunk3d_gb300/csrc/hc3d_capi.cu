@@ -533,6 +533,24 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
   c->dm.nudust = d_nud; c->dm.kappad = d_kap; c->dm.adust = d_alb; c->dm.gdust = d_g; c->dm.pldust = d_pl;
   c->dm.nT = t->nT; c->dm.nnu = t->nnu; c->dm.lTint = d_lT; c->dm.nuint = d_nuint; c->dm.kapBint = d_kB;
   c->dm.nhnu = t->nhnu; c->dm.hnuint = d_hn; c->dm.atmosnu = d_an; c->dm.lognu = d_ln; c->dm.loghnu = d_lh;
+  // FP32 copies for the mixed form
+  {
+    auto f32 = [](const double* p, size_t n) { return std::vector<float>(p, p + n); };
+    const float* fp[12] = {};
+    const std::vector<float> h[12] = {
+        f32(nud.data(), nud.size()), f32(kap.data(), kap.size()), f32(alb.data(), alb.size()),
+        f32(gg.data(), gg.size()),   f32(pl.data(), pl.size()),   f32(t->lTint, (size_t)t->nT),
+        f32(t->nuint, (size_t)t->nnu), f32(kB.data(), kB.size()), f32(t->hnuint, (size_t)t->nhnu),
+        f32(t->atmosnu, (size_t)t->nhnu), f32(t->lognu, (size_t)t->nhnu), f32(t->loghnu, (size_t)t->nhnu)};
+    for (int k = 0; k < 12; ++k) {
+      float* d = nullptr;
+      if ((r = dupload(c, own, &d, h[k].data(), h[k].size()))) return r;
+      fp[k] = d;
+    }
+    c->dm.nudustf = fp[0]; c->dm.kappadf = fp[1]; c->dm.adustf = fp[2]; c->dm.gdustf = fp[3]; c->dm.pldustf = fp[4];
+    c->dm.lTintf = fp[5]; c->dm.nuintf = fp[6]; c->dm.kapBintf = fp[7]; c->dm.hnuintf = fp[8];
+    c->dm.atmosnuf = fp[9]; c->dm.lognuf = fp[10]; c->dm.loghnuf = fp[11];
+  }
   c->tsub = t->tsub > 0.0 ? t->tsub : 1600.0;
   c->tables = true;
   if (c->grid) {
@@ -800,7 +818,6 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   unsigned long long cnt[16];
   CK(cudaMemcpy(cnt, c->dt.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
   for (int k = 0; k < 16; ++k) out->counters[k] = (int64_t)cnt[k];
-  out->counters[HC3D_CNT_STATUS] = c->status_seen;
   return HC3D_OK;
 }
 

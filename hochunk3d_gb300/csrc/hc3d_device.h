@@ -70,6 +70,10 @@ struct DevModel {
   const double* lTint; const double* nuint; const double* kapBint;  // kapBint (nT,nnu,kSlots)
   int nhnu;
   const double* hnuint; const double* atmosnu; const double* lognu; const double* loghnu;
+  // FP32 copies of the per-event tables, read by the mixed form
+  const float* nudustf; const float* kappadf; const float* adustf; const float* gdustf; const float* pldustf;
+  const float* lTintf; const float* nuintf; const float* kapBintf;
+  const float* hnuintf; const float* atmosnuf; const float* lognuf; const float* loghnuf;
 };
 
 // One call of the packet loop.

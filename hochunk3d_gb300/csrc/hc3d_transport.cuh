@@ -199,19 +199,29 @@ __device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, doubl
       w.insert((R)((-bb - descr) * 0.5), 2);
     }
   } else {
+    // With the wall the packet stands on given the exact root 0, negative
+    // roots never decide the next wall, so only the nearest non-negative
+    // root of each sphere is formed: outside a sphere moving away there is
+    // none; inside it one square root, and a division only when b > 0.
 #pragma unroll
     for (int id = 1; id <= 2; ++id) {
       if (own == id) {
         w.insert(R(0), id);
-        w.insert((R)(-bb), id);
+        if (bb < 0.0) w.insert((R)(-bb), id);
         continue;
       }
       const double cc = rr - (id == 1 ? R2_1 : R2_2);
+      if (cc > 0.0 && bb >= 0.0) continue;
       const double descr = bb * bb - 4.0 * cc;
       if (descr > 0.0) {
-        const double q = -0.5 * (bb + copysign(sqrt(descr), bb));
-        w.insert((R)q, id);
-        w.insert((R)(cc / q), id);
+        const double sd = sqrt(descr);
+        if (cc > 0.0) {
+          w.insert((R)(cc / (0.5 * (sd - bb))), id);  // near root, entering the sphere
+        } else if (bb > 0.0) {
+          w.insert((R)(cc / (-0.5 * (bb + sd))), id);
+        } else {
+          w.insert((R)(0.5 * (sd - bb)), id);
+        }
       }
     }
   }
@@ -341,52 +351,64 @@ __device__ __forceinline__ unsigned long long fx(double v, double scale) {
 }
 
 // ---- dust tables: unique per-species tables, staged in shared memory ---------------
+// R-typed: the FP64 form reads the FP64 tables, the mixed form their FP32 copies.
+template <class R>
 struct DustView {
-  const double* nud[kSlots];
-  const double* kap[kSlots];
-  const double* alb[kSlots];
-  const double* g[kSlots];
-  const double* pl[kSlots];
+  const R* nud[kSlots];
+  const R* kap[kSlots];
+  const R* alb[kSlots];
+  const R* g[kSlots];
+  const R* pl[kSlots];
 };
+
+template <class R> __device__ __forceinline__ const R* tab(const double* d, const float* f);
+template <> __device__ __forceinline__ const double* tab<double>(const double* d, const float*) { return d; }
+template <> __device__ __forceinline__ const float* tab<float>(const double*, const float* f) { return f; }
 
 // Copy the unique dust tables into the block's dynamic shared memory (when
 // the host sized it, DevModel::dust_smem > 0) and point the view at them;
 // otherwise read them from global memory.  Called by every thread of the
 // block before any divergence.
-__device__ __forceinline__ void dust_view(const DevModel& m, double* smem, DustView& v) {
+template <class R>
+__device__ __forceinline__ void dust_view(const DevModel& m, R* smem, DustView<R>& v) {
+  const R* nud = tab<R>(m.nudust, m.nudustf);
+  const R* kap = tab<R>(m.kappad, m.kappadf);
+  const R* alb = tab<R>(m.adust, m.adustf);
+  const R* gg = tab<R>(m.gdust, m.gdustf);
+  const R* pl = tab<R>(m.pldust, m.pldustf);
   size_t off = 0;
   for (int u = 0; u < m.ntab; ++u) {
     const int nl = m.tab_nl[u];
     const size_t go = (size_t)u * m.nlammax;
     if (m.dust_smem > 0) {
-      double* base = smem + off;
+      R* base = smem + off;
       for (int i = threadIdx.x; i < nl; i += blockDim.x) {
-        base[i] = m.nudust[go + i];
-        base[nl + i] = m.kappad[go + i];
-        base[2 * nl + i] = m.adust[go + i];
-        base[3 * nl + i] = m.gdust[go + i];
-        base[4 * nl + i] = m.pldust[go + i];
+        base[i] = nud[go + i];
+        base[nl + i] = kap[go + i];
+        base[2 * nl + i] = alb[go + i];
+        base[3 * nl + i] = gg[go + i];
+        base[4 * nl + i] = pl[go + i];
       }
       v.nud[u] = base; v.kap[u] = base + nl; v.alb[u] = base + 2 * nl; v.g[u] = base + 3 * nl; v.pl[u] = base + 4 * nl;
       off += 5 * (size_t)nl;
     } else {
-      v.nud[u] = m.nudust + go; v.kap[u] = m.kappad + go; v.alb[u] = m.adust + go; v.g[u] = m.gdust + go;
-      v.pl[u] = m.pldust + go;
+      v.nud[u] = nud + go; v.kap[u] = kap + go; v.alb[u] = alb + go; v.g[u] = gg + go; v.pl[u] = pl + go;
     }
   }
   if (m.dust_smem > 0) __syncthreads();
 }
 
-// ---- opacset, dust.f90:9-80 (FP64 lookups; results stored in R) ---------------
+// ---- opacset, dust.f90:9-80 ---------------------------------------------------------
 // Computed once per unique table; species slots sharing a dust file share
 // the result (only kappa_V differs), which is what the per-slot loop of the
 // reference computes for them.
 template <class R>
-__device__ void opacset(const DevModel& m, const DustView& v, Pkt<R>& p, double nu, double rstar_cm) {
-  double gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
+__device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, double nu_in, double rstar_cm) {
+  const R nu = (R)nu_in;
+  R gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
   for (int u = 0; u < m.ntab; ++u) {
     const int nl = m.tab_nl[u];
-    const double* nud = v.nud[u];
+    const R* nud = v.nud[u];
     if (nu >= nud[0]) {
       gt[u] = v.g[u][0]; plt[u] = v.pl[u][0]; kt[u] = v.kap[u][0]; at[u] = v.alb[u][0];
     } else if (nu <= nud[nl - 1]) {
@@ -397,8 +419,8 @@ __device__ void opacset(const DevModel& m, const DustView& v, Pkt<R>& p, double 
         const int i = (i1 + i0) / 2;
         if (nu <= nud[i - 1]) i0 = i; else i1 = i;
       }
-      const double n1 = nud[i1 - 1], n0 = nud[i0 - 1];
-      const double f = (nu - n1) / (n0 - n1), fm1 = 1.0 - f;
+      const R n1 = nud[i1 - 1], n0 = nud[i0 - 1];
+      const R f = (nu - n1) / (n0 - n1), fm1 = R(1) - f;
       gt[u] = fm1 * v.g[u][i1 - 1] + f * v.g[u][i0 - 1];
       plt[u] = fm1 * v.pl[u][i1 - 1] + f * v.pl[u][i0 - 1];
       kt[u] = fm1 * v.kap[u][i1 - 1] + f * v.kap[u][i0 - 1];
@@ -408,8 +430,8 @@ __device__ void opacset(const DevModel& m, const DustView& v, Pkt<R>& p, double 
 #pragma unroll
   for (int id = 0; id < kSlots; ++id) {
     const int u = m.table_of[id];
-    p.g[id] = (R)gt[u]; p.pl[id] = (R)plt[u]; p.albedo[id] = (R)at[u];
-    p.kapd[id] = (R)(kt[u] * rstar_cm * m.kappav[id]);
+    p.g[id] = gt[u]; p.pl[id] = plt[u]; p.albedo[id] = at[u];
+    p.kapd[id] = (R)((double)kt[u] * rstar_cm * m.kappav[id]);
   }
 }
 
@@ -742,13 +764,13 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
-      L.c[HC3D_CNT_STUCK]++;
+      L.c[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
     R dt;
     int iface;
     if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
-      L.c[HC3D_CNT_STUCK]++;
+      L.c[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
     const int64_t c = cidx(m, ir, it, ip);
@@ -804,67 +826,81 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   }
 }
 
-// ---- lucydustfreq.f90:19-157 (FP64) --------------------------------------------------
+// ---- lucydustfreq.f90:19-157 -------------------------------------------------------------
+// R-typed: FP64 tables and arithmetic in the FP64 form, FP32 in the mixed one.
+template <class R> __device__ __forceinline__ R xpow(R a, R b);
+template <> __device__ __forceinline__ float xpow<float>(float a, float b) { return powf(a, b); }
+template <> __device__ __forceinline__ double xpow<double>(double a, double b) { return pow(a, b); }
+__device__ __forceinline__ float xlog10(float x) { return log10f(x); }
+__device__ __forceinline__ double xlog10(double x) { return log10(x); }
+
 template <class R>
-__device__ double lucydustfreq(const DevModel& m, double T0, int id, Rng& rng) {
+__device__ double lucydustfreq(const DevModel& m, double T0in, int id, Rng& rng) {
   const int nT = m.nT, nnu = m.nnu;
-  const double* K = m.kapBint + (size_t)id * nT * nnu;
-  const double lT0 = log(T0);
-  const double xi = (double)ran<R>(rng);
-  const double l1 = __ldg(m.lTint), lN = __ldg(m.lTint + nT - 1);
-  int j = (int)((double)(nT - 1) * (lT0 - l1) / (lN - l1)) + 1;
+  const R* lTint = tab<R>(m.lTint, m.lTintf);
+  const R* nuint = tab<R>(m.nuint, m.nuintf);
+  const R* K = tab<R>(m.kapBint, m.kapBintf) + (size_t)id * nT * nnu;
+  const R T0 = (R)T0in;
+  const R lT0 = xlog(T0);
+  const R xi = ran<R>(rng);
+  const R l1 = __ldg(lTint), lN = __ldg(lTint + nT - 1);
+  int j = (int)((R)(nT - 1) * (lT0 - l1) / (lN - l1)) + 1;
   j = j < 1 ? 1 : (j > nT - 1 ? nT - 1 : j);
-  double f = (lT0 - __ldg(m.lTint + j - 1)) / (__ldg(m.lTint + j) - __ldg(m.lTint + j - 1));
-  f = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
+  R f = (lT0 - __ldg(lTint + j - 1)) / (__ldg(lTint + j) - __ldg(lTint + j - 1));
+  f = f < R(0) ? R(0) : (f > R(1) ? R(1) : f);
 #define KB(jj, ii) __ldg(K + (size_t)((jj) - 1) + (size_t)nT * ((ii) - 1))
   int i0 = 1, i1 = nnu;
-  double P0 = (1.0 - f) * KB(j, i0) + f * KB(j + 1, i0);
-  if (xi < P0) return P0 > 0.0 ? T0 * xi * __ldg(m.nuint) / P0 : T0 * __ldg(m.nuint);
-  double P1 = (1.0 - f) * KB(j, i1) + f * KB(j + 1, i1);
-  if (P1 > 1.0) P1 = 1.0;
+  R P0 = (R(1) - f) * KB(j, i0) + f * KB(j + 1, i0);
+  if (xi < P0) return (double)(P0 > R(0) ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint));
+  R P1 = (R(1) - f) * KB(j, i1) + f * KB(j + 1, i1);
+  if (P1 > R(1)) P1 = R(1);
   if (xi >= P1) {
-    if (P1 < 1.0 && xi < 1.0) return T0 * __ldg(m.nuint + nnu - 1) * (1.0 - P1) / (1.0 - xi);
-    return T0 * __ldg(m.nuint + nnu - 1);
+    if (P1 < R(1) && xi < R(1)) return (double)(T0 * __ldg(nuint + nnu - 1) * (R(1) - P1) / (R(1) - xi));
+    return (double)(T0 * __ldg(nuint + nnu - 1));
   }
   while (i1 - i0 > 1) {
     const int i = (i0 + i1) / 2;
-    double P = (1.0 - f) * KB(j, i) + f * KB(j + 1, i);
-    if (P > 1.0) P = 1.0;
+    R P = (R(1) - f) * KB(j, i) + f * KB(j + 1, i);
+    if (P > R(1)) P = R(1);
     if (P < P0) { P0 = P; i0 = i; }
     if (P > P1) { P1 = P; i1 = 1; }
     if (P > xi) { i1 = i; P1 = P; }
     else { i0 = i; P0 = P; }
   }
 #undef KB
-  if (xi < P0) f = 0.0;
-  else if (xi > P1) f = 1.0;
-  else if (P0 <= 0.0) f = 0.5;
-  else if (P1 <= 0.0 || xi <= 0.0) { }
-  else f = log(xi / P0) / log(P1 / P0);
-  const double n0 = __ldg(m.nuint + i0 - 1), n1 = __ldg(m.nuint + i1 - 1);
-  return T0 * n0 * pow(n1 / n0, f);
+  if (xi < P0) f = R(0);
+  else if (xi > P1) f = R(1);
+  else if (P0 <= R(0)) f = R(0.5);
+  else if (P1 <= R(0) || xi <= R(0)) { }
+  else f = xlog(xi / P0) / xlog(P1 / P0);
+  const R n0 = __ldg(nuint + i0 - 1), n1 = __ldg(nuint + i1 - 1);
+  return (double)(T0 * n0 * xpow<R>(n1 / n0, f));
 }
 
-// ---- atmosfreq, starbarb.f90:120-156 (FP64) -------------------------------------------
+// ---- atmosfreq, starbarb.f90:120-156 ---------------------------------------------------
 template <class R>
 __device__ double atmosfreq(const DevModel& m, Rng& rng) {
-  const double xi = (double)ran<R>(rng);
+  const R* hnuint = tab<R>(m.hnuint, m.hnuintf);
+  const R* lognu = tab<R>(m.lognu, m.lognuf);
+  const R* loghnu = tab<R>(m.loghnu, m.loghnuf);
+  const R* atmosnu = tab<R>(m.atmosnu, m.atmosnuf);
+  const R xi = ran<R>(rng);
   // locate2 (nr.f:152-171) on the increasing hnuint
   const int n = m.nhnu;
   int jl = 0, ju = n + 1;
   while (ju - jl > 1) {
     const int jm = (ju + jl) / 2;
-    if (xi > __ldg(m.hnuint + jm - 1)) jl = jm; else ju = jm;
+    if (xi > __ldg(hnuint + jm - 1)) jl = jm; else ju = jm;
   }
   int i = jl < 1 ? 1 : (jl > n - 1 ? n - 1 : jl);
   if (i > 1) {
-    const double l0 = __ldg(m.lognu + i - 1), l1 = __ldg(m.lognu + i);
-    const double h0 = __ldg(m.loghnu + i - 1), h1 = __ldg(m.loghnu + i);
-    return pow(10.0, l0 + (l1 - l0) * (log10(xi) - h0) / (h1 - h0));
+    const R l0 = __ldg(lognu + i - 1), l1 = __ldg(lognu + i);
+    const R h0 = __ldg(loghnu + i - 1), h1 = __ldg(loghnu + i);
+    return (double)xpow<R>(R(10), l0 + (l1 - l0) * (xlog10(xi) - h0) / (h1 - h0));
   }
-  const double a0 = __ldg(m.atmosnu + i - 1), a1 = __ldg(m.atmosnu + i);
-  const double c0 = __ldg(m.hnuint + i - 1), c1 = __ldg(m.hnuint + i);
-  return a0 + (a1 - a0) * (xi - c0) / (c1 - c0);
+  const R a0 = __ldg(atmosnu + i - 1), a1 = __ldg(atmosnu + i);
+  const R c0 = __ldg(hnuint + i - 1), c1 = __ldg(hnuint + i);
+  return (double)(a0 + (a1 - a0) * (xi - c0) / (c1 - c0));
 }
 
 __device__ __forceinline__ int locate_dev(const double* xx, int n, double x) {
@@ -937,7 +973,7 @@ enum { ST_DONE = 0, ST_INTERACT = 1 };
 // initp_sample (limb = 0) and initp_transform (initp_common.f90:1-94).  rec
 // receives the stellar-surface peel-off event.
 template <class R>
-__device__ void emit(const DevModel& m, const DustView& dv, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
+__device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
   p.on_wall = 0;
   p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
   for (;;) {
@@ -1065,7 +1101,7 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
 // One interaction, propagate.f90:70-166: scattering (rec = the state before
 // stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
 template <class R>
-__device__ void interact(const DevModel& m, const DustView& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
+__device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
                          Local& L, Tracer& tr, PeelRec<R>& rec) {
   const int64_t c = cidx(m, p.ir, p.it, p.ip);
   const int idust2 = f.idust2;
@@ -1098,7 +1134,7 @@ __device__ void interact(const DevModel& m, const DustView& dv, const DevTallies
 
 __device__ __forceinline__ void flush(const DevTallies& t, Local& L) {
 #pragma unroll
-  for (int i = 0; i < 15; ++i)
+  for (int i = 0; i < 16; ++i)
     if (L.c[i]) atomicAdd(t.counters + i, L.c[i]);
 }
 
@@ -1106,7 +1142,7 @@ __device__ __forceinline__ void flush(const DevTallies& t, Local& L) {
 // Used for the trace harness and for runs without peel-off (the Lucy
 // iterations), where a packet's history is its only work.
 template <class R>
-__device__ void run_packet(const DevModel& m, const DustView& dv, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
+__device__ void run_packet(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const TallyDims& d, const RunArgs& a, Rng& rng,
                            Local& L, Tracer& tr) {
   Pkt<R> p;
   PeelRec<R> rec;
@@ -1128,8 +1164,8 @@ __device__ void run_packet(const DevModel& m, const DustView& dv, const DevTalli
 template <class R>
 __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, TallyDims d, RunArgs a) {
   extern __shared__ double dust_smem[];
-  DustView dv;
-  dust_view(m, dust_smem, dv);
+  DustView<R> dv;
+  dust_view<R>(m, reinterpret_cast<R*>(dust_smem), dv);
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
@@ -1182,8 +1218,8 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
                                                unsigned int* alive) {
   namespace cg = cooperative_groups;
   extern __shared__ double dust_smem[];
-  DustView dv;
-  dust_view(m, dust_smem, dv);
+  DustView<R> dv;
+  dust_view<R>(m, reinterpret_cast<R*>(dust_smem), dv);
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;

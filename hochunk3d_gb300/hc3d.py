@@ -38,7 +38,7 @@ ERRORS = {
 CNT = {
     "flux": 0, "sflux": 1, "nscat": 2, "scount": 3, "tot": 4, "abflux": 5, "aflux": 6, "sumsub": 7,
     "sumall": 8, "escaped": 9, "cross_prop": 10, "cross_peel": 11, "events": 12, "peels": 13, "stuck": 14,
-    "status": 15,
+    "peel_stuck": 15,
 }
 
 P = C.POINTER

@@ -175,8 +175,8 @@ typedef struct hc3d_tallies {
 #define HC3D_CNT_CROSS_PEEL 11 /* cell crossings of the peel-off walks */
 #define HC3D_CNT_EVENTS 12    /* scatterings + absorptions */
 #define HC3D_CNT_PEELS 13     /* peel-off rays started */
-#define HC3D_CNT_STUCK 14     /* walks stopped by the crossing cap (geometry fault) */
-#define HC3D_CNT_STATUS 15    /* first device status word != 0 */
+#define HC3D_CNT_STUCK 14     /* packets stopped by a fault (see hc3d_get_fault_log) */
+#define HC3D_CNT_PEEL_STUCK 15 /* peel-off rays stopped by a fault (their contribution is dropped) */
 
 /* ---- context ----------------------------------------------------------- */
 int hc3d_create(hc3d_ctx **ctx, const hc3d_device_opts *opts);

@@ -599,13 +599,13 @@ static void orc_peeloff(const orc_ctx *c, const hc3d_run_params *rp, const pkt *
   const int cap = crossing_cap(c);
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > c->g.ntg - 1 || ir < 1 || ir > c->g.nrg - 1) {
-      t->fx.counters[HC3D_CNT_STUCK]++;
+      t->fx.counters[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
     double dt;
     int iface;
     if (!next_wall(c, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, &dt, &iface)) {
-      t->fx.counters[HC3D_CNT_STUCK]++;
+      t->fx.counters[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
     const int64_t cell = cidx(c, ir, it, ip);
