@@ -205,7 +205,7 @@ __device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, doubl
     // none; inside it one square root, and a division only when b > 0.
 #pragma unroll
     for (int id = 1; id <= 2; ++id) {
-      if (own == id) {
+      if (own & (1 << id)) {
         w.insert(R(0), id);
         if (bb < 0.0) w.insert((R)(-bb), id);
         continue;
@@ -283,6 +283,20 @@ template <> __device__ __forceinline__ double barr_of<double>(const DevModel& m,
 // wall id of the new cell (1<->2, 3<->4, 5<->6).
 __device__ __forceinline__ int own_after(int iface) { return ((iface - 1) ^ 1) + 1; }
 
+// The set of walls (bit id) a packet stands on after crossing wall iface with
+// step dt.  A step of (near) zero length is a crossing at an edge where two
+// walls meet: the packet still stands on the walls of the other families it
+// stood on before, and the FP32 walk must not re-cross them.
+template <class R>
+__device__ __forceinline__ int walls_after(int iface, int before, R dt, double x, double y, double z) {
+  int m = 1 << own_after(iface);
+  if (sizeof(R) == 4) {
+    const float scale = fabsf((float)x) + fabsf((float)y) + fabsf((float)z);
+    if ((float)dt <= 2.0e-7f * scale) m |= before & ~(6 << (2 * ((iface - 1) >> 1)));
+  }
+  return m;
+}
+
 // The wall machinery of one step (peeloff_3d.f90:92-115).  on_wall is 0 off
 // the walls, else the id (1..6) of the wall of the current cell the packet
 // stands on; the FP64 form uses it only as the reference's on_wall flag.
@@ -295,17 +309,17 @@ __device__ __forceinline__ bool next_wall(const DevModel& m, R ux, R uy, R uz, d
   radface<R>(w, (double)ux, (double)uy, (double)uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir), own);
   if (m.ntg > 2) {
     const R xr = (R)x, yr = (R)y, zr = (R)z;
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3, own == 3);
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4, own == 4);
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3, (own & 8) != 0);
+    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4, (own & 16) != 0);
     if (m.npg > 2) {
       // phiface.f90:48-56 with C = D = 0
       const R A1 = aarr_of<R>(m, ip - 1), B1 = barr_of<R>(m, ip - 1);
       const R A2 = aarr_of<R>(m, ip), B2 = barr_of<R>(m, ip);
       const R d1 = A1 * ux + B1 * uy;
-      if (own == 5) w.insert(R(0), 5);
+      if (own & 32) w.insert(R(0), 5);
       else if (d1 != R(0)) w.insert(-(A1 * xr + B1 * yr) / d1, 5);
       const R d2 = A2 * ux + B2 * uy;
-      if (own == 6) w.insert(R(0), 6);
+      if (own & 64) w.insert(R(0), 6);
       else if (d2 != R(0)) w.insert(-(A2 * xr + B2 * yr) / d2, 6);
     }
   }
@@ -492,7 +506,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     p.x += (double)dt * (double)p.ux;
     p.y += (double)dt * (double)p.uy;
     p.z += (double)dt * (double)p.uz;
-    p.on_wall = own_after(iface);
+    p.on_wall = walls_after<R>(iface, p.on_wall, dt, p.x, p.y, p.z);
     tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
     if (p.ir == m.nrg) return TI_ESCAPE;
     if (p.ir == 0) return TI_STAR;
@@ -743,7 +757,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   }
   double xp1 = e.x, yp1 = e.y, zp1 = e.z;
   int ir = e.ir, it = e.it, ip = e.ip;
-  int on_wall = (flags >> 8) & 7;
+  int on_wall = (flags >> 8) & 127;
   const R ux1 = sinte * cospe, uy1 = sinte * sinpe, uz1 = coste;
   L.c[HC3D_CNT_PEELS]++;
   if (on_wall) {
@@ -753,11 +767,11 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     if (inner_wall && !outwards) {
       if (ir == 1) return;
       ir = ir - 1;
-      on_wall = 2;
+      on_wall = 1 << 2;
     }
     if (!inner_wall && outwards) {
       ir = ir + 1;
-      on_wall = 1;
+      on_wall = 1 << 1;
     }
   }
   double tsum = 0.0;  // FP64 escape tau in both forms
@@ -787,7 +801,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     xp1 += (double)dt * (double)ux1;
     yp1 += (double)dt * (double)uy1;
     zp1 += (double)dt * (double)uz1;
-    on_wall = own_after(iface);
+    on_wall = walls_after<R>(iface, on_wall, dt, xp1, yp1, zp1);
     if (ir == m.nrg) break;
     if (ir == 0) return;
   }
@@ -1028,7 +1042,7 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   p.y = rp_ * (double)sinlp;
   p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
   p.ir = 1;
-  p.on_wall = 1;
+  p.on_wall = 1 << 1;  // on the stellar surface: the inner radial wall (id 1) of cell 1
   p.it = locate_dev(m.thetarr, m.ntg, acos((double)p.cosb));
   p.ip = locate_dev(m.phiarr, m.npg, (double)p.lp);
   p.it = p.it < 1 ? 1 : (p.it > m.ntg - 1 ? m.ntg - 1 : p.it);
