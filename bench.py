@@ -132,7 +132,7 @@ def run_cpu_oracle(model, np_, threads, iter_=9, seed_offset=0):
     return time.perf_counter() - t0, r
 
 
-def cpu_baseline(model, budget_s: float = 15.0):
+def cpu_baseline(model, workload, budget_s: float = 15.0):
     threads = os.cpu_count() or 1
     n = max(threads, 16)
     dt, _ = run_cpu_oracle(model, n, threads)
@@ -142,7 +142,7 @@ def cpu_baseline(model, budget_s: float = 15.0):
     n = int(max(threads, min(n * budget_s / max(dt, 1e-3), 1 << 24)))
     dt, r = run_cpu_oracle(model, n, threads, seed_offset=1 << 40)
     return {"value": n / dt, "unit": "packets/s", "cores": threads, "kind": "port",
-            "sample": f"{n} packets of the {WORKLOAD} peeled iteration (oracle C restatement, FP64, "
+            "sample": f"{n} packets of the {workload} peeled iteration (oracle C restatement, FP64, "
                       f"{threads} threads, {dt:.1f} s)"}
 
 
@@ -190,6 +190,8 @@ def main():
     ap.add_argument("--packets", type=int, default=100000, help="packets per step (0 = calibrate)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
+    ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -215,7 +217,7 @@ def main():
         torch.distributed.barrier()
 
     with tempfile.TemporaryDirectory() as td:
-        model = build_model(Path(td), WORKLOAD)
+        model = build_model(Path(td), args.workload)
         ctx = hc3d.Context(hc3d.PREC_MIXED, device=local).load(model)
         warm_up_temperatures(model, ctx, args.lucy_packets)
         stream = torch.cuda.ExternalStream(ctx.stream)
@@ -283,20 +285,26 @@ def main():
             h2d = 8 * 4 * model.npeel + 8 * len(model.aperture2)
         e2e = n * world / (sum(e2e_times) / len(e2e_times))
 
-        # the all-FP64 form on the same model and temperatures, for the speed-up
-        ctx64 = hc3d.Context(hc3d.PREC_FP64, device=local).load(model)
-        n64 = max(1000, n // 16)
-        p64 = model.run_params(np=n64, iter=500, ipeel=1)
-        ctx64.zero(); ctx64.run(p64)
-        t64 = []
-        for s in range(2):
-            ctx64.zero()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            ctx64.run(model.run_params(np=n64, iter=501 + s, ipeel=1))
-            t64.append(time.perf_counter() - t0)
-        fp64_value = n64 / (sum(t64) / len(t64))
-        ctx64.close()
+        # the all-FP64 form on the same model, temperatures and packets, for the
+        # speed-up: both forms time the same batch (packet loop only)
+        fp64 = None
+        if not args.no_fp64:
+            n64 = max(1000, n // 4)
+
+            def timed_run(c, it):
+                c.zero()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                c.run(model.run_params(np=n64, iter=it, ipeel=1))
+                return time.perf_counter() - t0
+
+            ctx64 = hc3d.Context(hc3d.PREC_FP64, device=local).load(model)
+            timed_run(ctx64, 500)
+            t64 = timed_run(ctx64, 501)
+            ctx64.close()
+            t32 = timed_run(ctx, 501)
+            fp64 = {"value": n64 / t64, "unit": "packets/s", "packets_per_step": n64,
+                    "mixed_same_batch": n64 / t32, "speedup_mixed_over_fp64": t64 / t32}
 
         launches = sum(k[0] for k in kern_ms)
         tms = sum(k[1] for k in kern_ms) / len(kern_ms)
@@ -315,19 +323,20 @@ def main():
                 "crossings_per_step": {"prop": cross_prop // args.steps, "peel": cross_peel // args.steps}}
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:
-            cpu = cpu_baseline(model)
+            cpu = cpu_baseline(model, args.workload)
         if rank == 0:
             line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
                     "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-                    "config": {"workload": WORKLOAD, "grid": [400, 199, 64], "peel_directions": 80,
-                               "image": [301, 301, 4], "nfreq": 50, "packets_per_step": n,
+                    "config": {"workload": args.workload,
+                               "grid": [model.shape4[0], model.shape4[1], model.shape4[2] - 1],
+                               "peel_directions": int(model.npeel), "image": [int(model._p.nxhst)] * 2 + [4],
+                               "nfreq": int(model._p.nfreq), "packets_per_step": n,
                                "l2": "256 MiB buffer written between timed steps",
                                "lucy_setup": f"2 iterations x {args.lucy_packets} packets"},
                     "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),
                             "d2h_bytes_per_step": int(d2h)},
-                    "fp64": {"value": fp64_value, "unit": "packets/s", "packets_per_step": n64,
-                             "speedup_mixed_over_fp64": value / world / fp64_value},
+                    "fp64": fp64,
                     "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
                     "gpu_launches": launches + args.steps}
             print(json.dumps(line))
