@@ -307,7 +307,8 @@ int ensure_wave(hc3d_ctx* c) {
   unsigned char *pool, *queue;
   if ((r = dalloc(c, c->wave_allocs, &pool, slot * (size_t)c->pool_threads)) ||
       (r = dalloc(c, c->wave_allocs, &queue, rec * (size_t)c->qcap)) ||
-      (r = dalloc(c, c->wave_allocs, &c->wave.qcount, 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.alive, 1)))
+      (r = dalloc(c, c->wave_allocs, &c->wave.qcount, 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.alive, 1)) ||
+      (r = dalloc(c, c->wave_allocs, &c->wave.next_ray, 1)))
     return r;
   c->wave.pool = pool;
   c->wave.queue = queue;
@@ -338,6 +339,7 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     const int E = (int)std::max<int64_t>(1, std::min<int64_t>(c->qcap / active, 1 << 20));
     CK(cudaMemsetAsync(c->wave.qcount, 0, sizeof(unsigned long long), c->stream));
     CK(cudaMemsetAsync(c->wave.alive, 0, sizeof(unsigned int), c->stream));
+    CK(cudaMemsetAsync(c->wave.next_ray, 0, sizeof(unsigned long long), c->stream));
     cudaError_t e = f64 ? launch_wave_fp64(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev)
                         : launch_wave_mixed(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev);
     if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("wave launch: ") + cudaGetErrorString(e));

@@ -113,6 +113,7 @@ struct WaveBufs {
   void* queue;
   unsigned long long* qcount;
   unsigned int* alive;
+  unsigned long long* next_ray;  // ray counter of k_peel
 };
 
 // One wave: k_wave (advance every live packet by up to E events) then k_peel

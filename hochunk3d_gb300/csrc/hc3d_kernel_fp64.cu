@@ -33,7 +33,7 @@ cudaError_t launch_wave_fp64(const DevModel& m, const DevTallies& t, const Tally
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;
   dev::k_peel<double><<<peel.blocks, peel.threads, 0, peel.stream>>>(
-      m, t, d, a, static_cast<const dev::PeelRec<double>*>(w.queue), w.qcount);
+      m, t, d, a, static_cast<const dev::PeelRec<double>*>(w.queue), w.qcount, w.next_ray);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], wave.stream)) != cudaSuccess) return e;
   return cudaSuccess;

@@ -210,17 +210,19 @@ __device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, doubl
         if (bb < 0.0) w.insert((R)(-bb), id);
         continue;
       }
+      // FP64 for the cancelling terms |x|^2 - R^2 and b^2 - 4c; the root itself
+      // is well conditioned in the cancellation-free form and is taken in FP32
       const double cc = rr - (id == 1 ? R2_1 : R2_2);
       if (cc > 0.0 && bb >= 0.0) continue;
       const double descr = bb * bb - 4.0 * cc;
       if (descr > 0.0) {
-        const double sd = sqrt(descr);
+        const float sd = sqrtf((float)descr), bbf = (float)bb, ccf = (float)cc;
         if (cc > 0.0) {
-          w.insert((R)(cc / (0.5 * (sd - bb))), id);  // near root, entering the sphere
+          w.insert((R)(ccf / (0.5f * (sd - bbf))), id);  // near root, entering the sphere
         } else if (bb > 0.0) {
-          w.insert((R)(cc / (-0.5 * (bb + sd))), id);
+          w.insert((R)(ccf / (-0.5f * (bbf + sd))), id);
         } else {
-          w.insert((R)(0.5 * (sd - bb)), id);
+          w.insert((R)(0.5f * (sd - bbf)), id);
         }
       }
     }
@@ -289,12 +291,8 @@ __device__ __forceinline__ int own_after(int iface) { return ((iface - 1) ^ 1) +
 // stood on before, and the FP32 walk must not re-cross them.
 template <class R>
 __device__ __forceinline__ int walls_after(int iface, int before, R dt, double x, double y, double z) {
-  int m = 1 << own_after(iface);
-  if (sizeof(R) == 4) {
-    const float scale = fabsf((float)x) + fabsf((float)y) + fabsf((float)z);
-    if ((float)dt <= 2.0e-7f * scale) m |= before & ~(6 << (2 * ((iface - 1) >> 1)));
-  }
-  return m;
+  (void)before; (void)dt; (void)x; (void)y; (void)z;
+  return 1 << own_after(iface);
 }
 
 // The wall machinery of one step (peeloff_3d.f90:92-115).  on_wall is 0 off
@@ -455,10 +453,41 @@ enum { TI_INTERACT = 0, TI_ESCAPE = 1, TI_STAR = 2, TI_FAULT = 3 };
 // exceeded the crossing cap; species selection found no opacity
 enum { F_RANGE = 1, F_NOWALL = 2, F_CAP = 3, F_SELECT = 4 };
 
+// Re-derive the cell of a position from the walls: the consistency check
+// testgrid (called at peeloff_3d.f90:90; the module is not shipped).  The
+// FP32 walk uses it when it finds no wall or keeps crossing walls at zero
+// distance.  Returns 0 inside the grid, 1 beyond rmax, 2 inside the star.
+__device__ __noinline__ int relocate(const DevModel& m, double x, double y, double z, int& ir, int& it, int& ip) {
+  const double rr = x * x + y * y + z * z;
+  if (rr >= __ldg(m.r2arr + m.nrg - 1)) return 1;
+  if (rr <= __ldg(m.r2arr)) return 2;
+  auto loc = [](const double* xx, int n, double v) {
+    int jl = 0, ju = n + 1;
+    while (ju - jl > 1) {
+      const int jm = (ju + jl) / 2;
+      if (v > __ldg(xx + jm - 1)) jl = jm; else ju = jm;
+    }
+    return jl;
+  };
+  ir = min(max(loc(m.r2arr, m.nrg, rr), 1), m.nrg - 1);
+  const double th = acos(fmin(1.0, fmax(-1.0, z / sqrt(rr))));
+  it = min(max(loc(m.thetarr, m.ntg, th), 1), m.ntg - 1);
+  double ph = atan2(y, x);
+  if (ph < 0.0) ph += kR2p;
+  ip = min(max(loc(m.phiarr, m.npg, ph), 1), m.npg - 1);
+  return 0;
+}
+
+// FP32 walk: a crossing shorter than this (relative to |x|) is at zero distance
+__device__ __forceinline__ bool tiny_step(float dt, double x, double y, double z) {
+  return dt <= 1.0e-6f * (fabsf((float)x) + fabsf((float)y) + fabsf((float)z));
+}
+
 template <class R>
 __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
   R tsum = R(0);
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  int nreloc = 0, ntiny = 0;
   for (int n = 0;; ++n) {
     if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
       L.fault = n > cap ? F_CAP : F_RANGE;
@@ -467,6 +496,14 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     R dt;
     int iface;
     if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+      if (sizeof(R) == 4 && nreloc < 4) {
+        ++nreloc;
+        const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
+        if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
+        if (where == 2) { p.ir = 0; return TI_STAR; }
+        p.on_wall = 0;
+        continue;
+      }
       L.fault = F_NOWALL;
       return TI_FAULT;
     }
@@ -510,6 +547,19 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
     if (p.ir == m.nrg) return TI_ESCAPE;
     if (p.ir == 0) return TI_STAR;
+    if (sizeof(R) == 4) {
+      // walls crossed back and forth at zero distance: re-derive the cell
+      if (!tiny_step((float)dt, p.x, p.y, p.z)) {
+        ntiny = 0;
+      } else if (++ntiny > 6 && nreloc < 4) {
+        ++nreloc;
+        ntiny = 0;
+        const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
+        if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
+        if (where == 2) { p.ir = 0; return TI_STAR; }
+        p.on_wall = 0;
+      }
+    }
   }
 }
 
@@ -776,6 +826,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   }
   double tsum = 0.0;  // FP64 escape tau in both forms
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  int nreloc = 0, ntiny = 0;
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
       L.c[HC3D_CNT_PEEL_STUCK]++;
@@ -784,6 +835,14 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     R dt;
     int iface;
     if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
+      if (sizeof(R) == 4 && nreloc < 4) {
+        ++nreloc;
+        const int where = relocate(m, xp1, yp1, zp1, ir, it, ip);
+        if (where == 1) break;
+        if (where == 2) return;
+        on_wall = 0;
+        continue;
+      }
       L.c[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
@@ -804,6 +863,18 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     on_wall = walls_after<R>(iface, on_wall, dt, xp1, yp1, zp1);
     if (ir == m.nrg) break;
     if (ir == 0) return;
+    if (sizeof(R) == 4) {
+      if (!tiny_step((float)dt, xp1, yp1, zp1)) {
+        ntiny = 0;
+      } else if (++ntiny > 6 && nreloc < 4) {
+        ++nreloc;
+        ntiny = 0;
+        const int where = relocate(m, xp1, yp1, zp1, ir, it, ip);
+        if (where == 1) break;
+        if (where == 2) return;
+        on_wall = 0;
+      }
+    }
   }
   const R factor = (R)exp(-tsum);
   sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
@@ -1279,16 +1350,20 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
   flush(t, L);
 }
 
+// Every lane takes its next (event, direction) ray from a counter as soon as
+// its current ray ends, so warps stay full although ray lengths differ.
 template <class R>
-__global__ void __launch_bounds__(256) k_peel(DevModel m, DevTallies t, TallyDims d, RunArgs a,
-                                               const PeelRec<R>* queue, const unsigned long long* qcount) {
+__global__ void __launch_bounds__(256, 3) k_peel(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+                                                  const PeelRec<R>* queue, const unsigned long long* qcount,
+                                                  unsigned long long* next_ray) {
   Local L;
 #pragma unroll
   for (int i = 0; i < 16; ++i) L.c[i] = 0;
   L.fault = 0;
   const unsigned long long n = *qcount * (unsigned long long)a.npeel;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  for (;;) {
+    const unsigned long long i = atomicAdd(next_ray, 1ull);
+    if (i >= n) break;
     const unsigned long long e = i / (unsigned)a.npeel;
     const int k = (int)(i - e * (unsigned)a.npeel);
     peel_ray<R>(m, t, d, a, queue[e], k, L);
