@@ -78,7 +78,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for _ in ex.map(_run, jobs):
                 pass
-    if force or jobs or not LIB.exists():
+    if force or jobs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
         _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
         os.replace(tmp, LIB)

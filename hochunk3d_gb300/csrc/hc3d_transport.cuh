@@ -457,7 +457,8 @@ enum { F_RANGE = 1, F_NOWALL = 2, F_CAP = 3, F_SELECT = 4 };
 // testgrid (called at peeloff_3d.f90:90; the module is not shipped).  The
 // FP32 walk uses it when it finds no wall or keeps crossing walls at zero
 // distance.  Returns 0 inside the grid, 1 beyond rmax, 2 inside the star.
-__device__ __noinline__ int relocate(const DevModel& m, double x, double y, double z, int& ir, int& it, int& ip) {
+static __device__ __noinline__ int relocate(const DevModel& m, double x, double y, double z, int& ir, int& it,
+                                            int& ip) {
   const double rr = x * x + y * y + z * z;
   if (rr >= __ldg(m.r2arr + m.nrg - 1)) return 1;
   if (rr <= __ldg(m.r2arr)) return 2;
