@@ -635,6 +635,12 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   DevModel& m = c->dm;
   m.nrg = nrg; m.ntg = ntg; m.npg = npg; m.ncell = ncell;
   m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
+  {
+    std::vector<float> rf32(g->rarr, g->rarr + nrg);
+    float* d_rarrf = nullptr;
+    if ((r = dupload(c, own, &d_rarrf, rf32.data(), rf32.size()))) return r;
+    m.rarrf = d_rarrf;
+  }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
   m.peelmask = c->d_peelmask; m.tdust = c->d_tdust;
   c->ndg_in = g->ndg;

@@ -45,6 +45,7 @@ struct DevModel {
   int nrg, ntg, npg;
   int64_t ncell;
   const double* rarr;     // (nrg)
+  const float* rarrf;     // (nrg)
   const double* r2arr;    // (nrg)
   const double* thetarr;  // (ntg)
   const double* phiarr;   // (npg)

@@ -324,6 +324,99 @@ __device__ __forceinline__ bool next_wall(const DevModel& m, R ux, R uy, R uz, d
   return w.next(on_wall != 0, dt, iface);
 }
 
+// Mixed form of the wall search.  The reference keeps the roots of every wall
+// in closest_wall and skips the root of the wall it stands on by the on_wall
+// rule; here the walls in `own` (bit id) contribute only their far
+// intersection and the next wall is the smallest non-negative root of the
+// rest, a minimum over at most six candidates.  FP64 enters only |x|^2, x.u and
+// |x|^2 - R^2 of the two spheres (the cancelling terms); the sphere roots are
+// then taken in FP32 by the cancellation-free forms, cones and planes in FP32.
+__device__ __forceinline__ bool next_wall_f32(const DevModel& m, float ux, float uy, float uz, double uxd, double uyd,
+                                              double uzd, double x, double y, double z, int ir, int it, int ip,
+                                              int own, float& dt, int& iface) {
+  float best = 3.402823466e38f;
+  int bi = 0;
+  auto cand = [&](float t, int id) {
+    if (t >= 0.f && t < best) {
+      best = t;
+      bi = id;
+    }
+  };
+  // spheres: t^2 + 2 hb t + c = 0 with hb = x.u, c = |x|^2 - R^2
+  const double hb = x * uxd + y * uyd + z * uzd;
+  const double rr = x * x + y * y + z * z;
+  const float hbf = (float)hb;
+  if (own & 2) {
+    if (hbf < 0.f) cand(-2.f * hbf, 1);
+  } else if (hbf < 0.f) {  // inner sphere: reached only moving inwards
+    const float c = (float)(rr - __ldg(m.r2arr + ir - 1));
+    const float disc = hbf * hbf - c;
+    if (disc > 0.f) cand(fmaxf(c, 0.f) / (sqrtf(disc) - hbf), 1);
+  }
+  if (own & 4) {
+    if (hbf < 0.f) cand(-2.f * hbf, 2);
+  } else {  // outer sphere: the exit root
+    const float c = (float)(rr - __ldg(m.r2arr + ir));
+    const float disc = hbf * hbf - c;
+    if (disc > 0.f) {
+      const float s = sqrtf(disc);
+      cand(hbf > 0.f ? fmaxf(-c, 0.f) / (hbf + s) : s - hbf, 2);
+    }
+  }
+  if (m.ntg > 2) {
+    const float xr = (float)x, yr = (float)y, zr = (float)z;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int id = 3 + k;
+      const float tan2 = __ldg(m.tan2f + it - 1 + k);
+      if (tan2 == 0.f) continue;  // a pole: no crossing
+      const bool mine = (own >> id) & 1;
+      if (tan2 < 0.f) {  // the midplane z = 0
+        if (!mine && uz != 0.f) cand(-zr / uz, id);
+        continue;
+      }
+      const float hemi = __ldg(m.hemi + it - 1 + k);
+      const float a = ux * ux + uy * uy - tan2 * uz * uz;
+      const float b = 2.f * (xr * ux + yr * uy - tan2 * zr * uz);
+      if (mine) {
+        if (a != 0.f) {
+          const float t = -b / a;
+          if ((zr + t * uz) * hemi > 0.f) cand(t, id);
+        }
+        continue;
+      }
+      const float cq = xr * xr + yr * yr - tan2 * zr * zr;
+      if (a == 0.f) {
+        if (b != 0.f) {
+          const float t = -cq / b;
+          if ((zr + t * uz) * hemi > 0.f) cand(t, id);
+        }
+        continue;
+      }
+      const float disc = b * b - 4.f * a * cq;
+      if (disc > 0.f) {
+        const float s = sqrtf(disc), inv = 0.5f / a;
+        const float t1 = (-b + s) * inv, t2 = (-b - s) * inv;
+        if ((zr + t1 * uz) * hemi > 0.f) cand(t1, id);
+        if ((zr + t2 * uz) * hemi > 0.f) cand(t2, id);
+      }
+    }
+    if (m.npg > 2) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int id = 5 + k;
+        if ((own >> id) & 1) continue;  // a plane is crossed once
+        const float A = __ldg(m.aarrf + ip - 1 + k), B = __ldg(m.barrf + ip - 1 + k);
+        const float d = A * ux + B * uy;
+        if (d != 0.f) cand(-(A * xr + B * yr) / d, id);
+      }
+    }
+  }
+  dt = best;
+  iface = bi;
+  return bi != 0;
+}
+
 // wall -> index step, peeloff_3d.f90:120-139
 __device__ __forceinline__ void step_index(int npg, int iface, int& ir, int& it, int& ip) {
   switch (iface) {
@@ -480,8 +573,21 @@ static __device__ __noinline__ int relocate(const DevModel& m, double x, double 
 }
 
 // FP32 walk: a crossing shorter than this (relative to |x|) is at zero distance
-__device__ __forceinline__ bool tiny_step(float dt, double x, double y, double z) {
-  return dt <= 1.0e-6f * (fabsf((float)x) + fabsf((float)y) + fabsf((float)z));
+__device__ __forceinline__ bool tiny_step(const DevModel& m, float dt, int ir) {
+  return dt <= 1.0e-6f * __ldg(m.rarrf + min(ir, m.nrg - 1));
+}
+
+// One wall search in either form: the reference's closest_wall machinery in
+// FP64, the candidate minimum in the mixed form (uxd..: the direction in FP64).
+template <class R>
+__device__ __forceinline__ bool find_wall(const DevModel& m, R ux, R uy, R uz, double uxd, double uyd, double uzd,
+                                          double x, double y, double z, int ir, int it, int ip, int on_wall, R& dt,
+                                          int& iface) {
+  if constexpr (sizeof(R) == 4) {
+    return next_wall_f32(m, ux, uy, uz, uxd, uyd, uzd, x, y, z, ir, it, ip, on_wall, dt, iface);
+  } else {
+    return next_wall<R>(m, ux, uy, uz, x, y, z, ir, it, ip, on_wall, dt, iface);
+  }
 }
 
 template <class R>
@@ -489,6 +595,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
   R tsum = R(0);
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nreloc = 0, ntiny = 0;
+  const double uxd = (double)p.ux, uyd = (double)p.uy, uzd = (double)p.uz;
   for (int n = 0;; ++n) {
     if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
       L.fault = n > cap ? F_CAP : F_RANGE;
@@ -496,7 +603,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     }
     R dt;
     int iface;
-    if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+    if (!find_wall<R>(m, p.ux, p.uy, p.uz, uxd, uyd, uzd, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
       if (sizeof(R) == 4 && nreloc < 4) {
         ++nreloc;
         const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
@@ -518,9 +625,9 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     L.c[HC3D_CNT_CROSS_PROP]++;
     if (tsum + dtau > tau) {
       const R ds = (tau - tsum) / opac;
-      p.x += (double)ds * (double)p.ux;
-      p.y += (double)ds * (double)p.uy;
-      p.z += (double)ds * (double)p.uz;
+      p.x += (double)ds * uxd;
+      p.y += (double)ds * uyd;
+      p.z += (double)ds * uzd;
       p.on_wall = 0;
 #pragma unroll
       for (int s = 0; s < kSlots; ++s)
@@ -541,16 +648,16 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
     atomicAdd(t.jmean + c, fx((double)dt / rout, t.path_scale));
     tsum += dtau;
     step_index(m.npg, iface, p.ir, p.it, p.ip);
-    p.x += (double)dt * (double)p.ux;
-    p.y += (double)dt * (double)p.uy;
-    p.z += (double)dt * (double)p.uz;
+    p.x += (double)dt * uxd;
+    p.y += (double)dt * uyd;
+    p.z += (double)dt * uzd;
     p.on_wall = walls_after<R>(iface, p.on_wall, dt, p.x, p.y, p.z);
     tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
     if (p.ir == m.nrg) return TI_ESCAPE;
     if (p.ir == 0) return TI_STAR;
     if (sizeof(R) == 4) {
       // walls crossed back and forth at zero distance: re-derive the cell
-      if (!tiny_step((float)dt, p.x, p.y, p.z)) {
+      if (!tiny_step(m, (float)dt, p.ir)) {
         ntiny = 0;
       } else if (++ntiny > 6 && nreloc < 4) {
         ++nreloc;
@@ -828,6 +935,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   double tsum = 0.0;  // FP64 escape tau in both forms
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nreloc = 0, ntiny = 0;
+  const double uxd = (double)ux1, uyd = (double)uy1, uzd = (double)uz1;
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
       L.c[HC3D_CNT_PEEL_STUCK]++;
@@ -835,7 +943,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     }
     R dt;
     int iface;
-    if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
+    if (!find_wall<R>(m, ux1, uy1, uz1, uxd, uyd, uzd, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
       if (sizeof(R) == 4 && nreloc < 4) {
         ++nreloc;
         const int where = relocate(m, xp1, yp1, zp1, ir, it, ip);
@@ -858,14 +966,14 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     L.c[HC3D_CNT_CROSS_PEEL]++;
     if (tsum > kTauMax) return;
     step_index(m.npg, iface, ir, it, ip);
-    xp1 += (double)dt * (double)ux1;
-    yp1 += (double)dt * (double)uy1;
-    zp1 += (double)dt * (double)uz1;
+    xp1 += (double)dt * uxd;
+    yp1 += (double)dt * uyd;
+    zp1 += (double)dt * uzd;
     on_wall = walls_after<R>(iface, on_wall, dt, xp1, yp1, zp1);
     if (ir == m.nrg) break;
     if (ir == 0) return;
     if (sizeof(R) == 4) {
-      if (!tiny_step((float)dt, xp1, yp1, zp1)) {
+      if (!tiny_step(m, (float)dt, ir)) {
         ntiny = 0;
       } else if (++ntiny > 6 && nreloc < 4) {
         ++nreloc;
