@@ -37,8 +37,14 @@ def _rank(rank, world, port, directory, n, q):
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
+    try:
+        # each rank writes its own copy of the model files: two ranks writing
+        # one directory at once could read each other's half-written files
+        m = make_model(directory / f"rank{rank}", "tiny3d")
+    except Exception as e:  # report instead of leaving the parent waiting
+        q.put(e)
+        raise
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    m = make_model(directory, "tiny3d")
     lo, hi = n * rank // world, n * (rank + 1) // world
     p = m.run_params(np=hi - lo, packet_offset=lo, iter=2, ipeel=1)
     r = O.run(m, p, scales=hc3d.tally_scales(n))
@@ -65,6 +71,8 @@ def test_two_rank_shards_sum_to_the_single_run(tmp_path, built):
     for p in procs:
         p.start()
     got = q.get(timeout=300)
+    if isinstance(got, Exception):
+        raise got
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
