@@ -31,6 +31,7 @@ UNITS = [
     ("hc3d_kernel_mixed.cu", []),
     ("hc3d_kernel_fp64.cu", ["--fmad=false"]),
     ("hc3d_capi.cu", []),
+    ("hc3d_noalloc.cu", []),
     ("hc3d_model.cpp", []),
     ("hc3d_driver.cpp", []),
 ]

@@ -10,6 +10,7 @@
 
 #include "../../include/hc3d.h"
 #include "hc3d_device.h"
+#include "hc3d_lucy.cuh"
 
 using namespace hc3d;
 
@@ -114,33 +115,8 @@ struct LucyArgs {
   int nslots;
 };
 
-__device__ double kapp_dev(const LucyArgs& a, double T, int s) {
-  // KapP, dust.f90:114-141
-  const double lT = log(T);
-  const double l1 = a.lTint[0], lN = a.lTint[a.nT - 1];
-  const int k = (int)((double)(a.nT - 1) * (lT - l1) / (lN - l1)) + 1;
-  const double* kp = a.kappap + (size_t)s * a.nT;
-  if (k < 1) return kp[0];
-  if (k > a.nT - 1) return kp[a.nT - 1];
-  const double f = (lT - a.lTint[k - 1]) / (a.lTint[k] - a.lTint[k - 1]);
-  return (1.0 - f) * kp[k - 1] + f * kp[k];
-}
-
 __device__ double dusttemp_dev(const LucyArgs& a, double na, double T0, int s, double massarr) {
-  const double eps = 1.e-5, sigt = 5.670400e-5;
-  double Td = T0 != 0.0 ? T0 : 0.1 / 11605.0;
-  double Told = 0.5 * Td;
-  int it = 0;
-  while (fabs(Td - Told) > eps * Td && it < 1000) {
-    ++it;
-    Told = Td;
-    Td = pow((na * a.ltot) / (4.0 * sigt * a.nphot * a.kappav[s] * kapp_dev(a, Td, s)), 0.25) / 11605.0;
-    if (massarr > 0.0) Td = Td / massarr;
-    else Td = 0.1 / 11605.0;
-    if (Td > 1600.0 / 11605.0) Td = 1600.0 / 11605.0;
-    if (Td < 0.1 / 11605.0) Td = 0.1 / 11605.0;
-  }
-  return Td;
+  return lucy_dusttemp(a.lTint, a.nT, a.kappap + (size_t)s * a.nT, a.kappav[s], a.ltot, a.nphot, na, T0, massarr);
 }
 
 __global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const double* rho4d, const double* massarr,

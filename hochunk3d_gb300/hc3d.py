@@ -97,6 +97,18 @@ class Tallies(C.Structure):
     ]
 
 
+class LucyBuffers(C.Structure):
+    """hc3d_lucy_buffers: caller-owned device buffers of hc3d_lucy_update_noalloc."""
+    _fields_ = [
+        ("device", C.c_int), ("stream", C.c_void_p),
+        ("nrg", C.c_int), ("ntg", C.c_int), ("npg", C.c_int), ("ndg", C.c_int),
+        ("dtauabs", C.c_void_p), ("path_scale", C.c_double),
+        ("densarr", C.c_void_p), ("massarr", C.c_void_p), ("tdust_in", C.c_void_p), ("tdust_out", C.c_void_p),
+        ("nT", C.c_int), ("lTint", C.c_void_p), ("kappap", C.c_void_p),
+        ("kappav", C.c_double * 8), ("ltot", C.c_double), ("np", C.c_int64),
+    ]
+
+
 class TraceRec(C.Structure):
     _fields_ = [("kind", C.c_int32), ("ir", C.c_int32), ("it", C.c_int32), ("ip", C.c_int32),
                 ("iface", C.c_int32), ("pad", C.c_int32), ("tsum", C.c_double),
@@ -134,6 +146,7 @@ SIGNATURES = {
     "hc3d_run_iteration": (C.c_int, [C.c_void_p, P(RunParams)]),
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
+    "hc3d_lucy_update_noalloc": (C.c_int, [P(LucyBuffers), dp, ip_]),
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),

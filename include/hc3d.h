@@ -213,6 +213,50 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
+/* ---- Lucy update that allocates nothing (no counterpart in the reference) --
+ * hc3d_lucy_update() needs a context, and a context obtains its device
+ * buffers with cudaMalloc.  Callers that cannot allocate device memory when
+ * the temperatures are due -- a host code that has reserved all of its device
+ * memory up front or hands it out from a pool it does not own, or a coupling
+ * that runs inside another code's stream work and may not add allocations to
+ * it -- call hc3d_lucy_update_noalloc() instead, with every array already on
+ * the device.  It computes what hc3d_lucy_update() computes, in the same
+ * FP64 arithmetic, from caller-owned buffers in the Fortran layouts above.
+ *
+ * Its only working memory is a fixed array of 1 MiB + 16 bytes in the
+ * library's device image: the per-block maxima of the convergence test and a
+ * completion counter.  Every GPU that loads the library holds that array until
+ * the process exits.  Grids are limited to nrg*ntg*npg*ndg <=
+ * HC3D_NOALLOC_MAX_ELEMENTS; a larger one returns HC3D_ERR_INVALID with a
+ * message on stderr.  The first call on each device looks the array's device
+ * address up (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array, which keeps the
+ * last call's contents, so calls that overlap on the GPU (different streams
+ * without ordering between them) race and must not be issued.  The call
+ * returns after the update on `stream` is complete. */
+#define HC3D_NOALLOC_MAX_ELEMENTS 134217728LL /* 2^27 grid elements */
+
+typedef struct hc3d_lucy_buffers {
+  int device;                /* CUDA device ordinal the buffers live on */
+  void *stream;              /* cudaStream_t to run on (NULL = legacy default stream) */
+  int nrg, ntg, npg, ndg;    /* wall counts and species slots of the arrays below */
+  const int64_t *dtauabs;    /* device (nrg,ntg,npg,ndg) absorbed-path tally, x path_scale */
+  double path_scale;         /* fixed-point scale of dtauabs (hc3d_tallies.path_scale) */
+  const double *densarr;     /* device (nrg,ntg,npg,ndg) g/cm^3; cells with 0 are left as they are */
+  const double *massarr;     /* device (nrg,ntg,npg,ndg) (rho*V)^(1/4) */
+  const double *tdust_in;    /* device (nrg,ntg,npg,ndg) temperatures of the last iteration, K/11605 */
+  double *tdust_out;         /* device (nrg,ntg,npg,ndg) new temperatures; may equal tdust_in */
+  int nT;                    /* rows of lTint */
+  const double *lTint;       /* device (nT) log temperature grid */
+  const double *kappap;      /* device (nT,ndg) Planck-mean kappa / kappa_V */
+  double kappav[HC3D_NDG];   /* kappa_V of each slot, cm^2/g (host values) */
+  double ltot;               /* luminosity of the packets, erg/s */
+  int64_t np;                /* packets that produced dtauabs */
+} hc3d_lucy_buffers;
+
+int hc3d_lucy_update_noalloc(const hc3d_lucy_buffers *buffers, double *max_rel_change,
+                             int *converged);
+
 /* ---- measurement helpers (no counterpart in the reference) -------------- */
 /* The CUDA stream (cudaStream_t) every kernel of this context is launched on. */
 void *hc3d_get_stream(hc3d_ctx *ctx);
