@@ -11,9 +11,12 @@ packets: zero the tallies, run the packet loop, solve the Lucy temperatures.
          library's stream around each step; L2 flushed between steps)
   e2e    the same through the C-ABI with host buffers: run parameters in,
          every tally and the temperature grid back to host each step
-  roofline  algorithmic bytes of the transport kernel per launch (propagation
-         crossings x (4S+16) B + peel crossings x 4S B, S = 3 active species)
-         over its event-timed duration, against the measured HBM peak
+  roofline  the dominant kernel (transport k_wave or peel-off k_peel_mixed):
+         algorithmic bytes per launch (propagation crossings x (4S+16) B, or
+         peel crossings x 4S B; S = 3 active species) over its event-timed
+         duration, against the measured HBM peak; traffic = DRAM bytes per
+         launch from the ncu capture in profiles/traffic_<workload>.txt,
+         scaled by crossings
   cpu_baseline  the CPU oracle (C restatement, FP64) on the host cores, on
          a bounded sample of the same workload
 
@@ -44,6 +47,22 @@ WORKLOAD = "full3d"
 S_ACTIVE = 3
 B_PROP = 4 * S_ACTIVE + 16
 B_PEEL = 4 * S_ACTIVE
+
+
+def profiled_traffic(workload: str) -> dict:
+    """DRAM bytes per cell crossing of each kernel, from the ncu capture
+    summarised in profiles/traffic_<workload>.txt (lines "kernel bytes")."""
+    p = ROOT / "profiles" / f"traffic_{workload}.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
 
 
 def env_rank():
@@ -155,15 +174,15 @@ def reference_arm(args):
 
         build_library()
         build_oracle()
-        model = build_model(Path(td), WORKLOAD)
-        # same dust field as the GPU arm would start from: a warm profile
+        model = build_model(Path(td), args.workload)
+        # the warm dust profile of the tests (the GPU arm's Lucy set-up needs a GPU)
         from tests.helpers import warm_tdust
 
         model.set_tdust(warm_tdust(model))
         threads = os.cpu_count() or 1
         n = max(threads * 2, 32)
         dt, _ = run_cpu_oracle(model, n, threads)
-        n = int(max(threads, n * 20.0 / max(dt, 1e-3)))
+        n = int(max(threads, n * 10.0 / max(dt, 1e-3)))  # about 10 s of CPU work per step
         times = []
         for s in range(args.warmup + args.steps):
             dt, _ = run_cpu_oracle(model, n, threads, seed_offset=(s + 1) << 32)
@@ -173,7 +192,7 @@ def reference_arm(args):
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "packets/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": WORKLOAD, "packets_per_step": n},
+                "data": "synthetic", "config": {"workload": args.workload, "packets_per_step": n},
                 "cpu_baseline": {"value": v, "unit": "packets/s", "cores": threads, "kind": "port",
                                  "sample": f"{n} packets per step, oracle C restatement with {threads} threads"},
                 "e2e": {"value": v, "unit": "packets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -309,17 +328,21 @@ def main():
         launches = sum(k[0] for k in kern_ms)
         tms = sum(k[1] for k in kern_ms) / len(kern_ms)
         pms = sum(k[2] for k in kern_ms) / len(kern_ms)
+        waves = launches / 2 / args.steps  # one k_wave and one k_peel launch per wave
         peak, peak_kind = measured_peaks()
-        # the dominant kernel: peel-off walks (k_peel) unless transport takes longer
+        # the dominant kernel: peel-off walks unless transport takes longer
         if pms >= tms:
-            kname, kms, kbytes = "k_peel<float>", pms, cross_peel * B_PEEL / args.steps
+            kname, kms, kcross, kb = "k_peel_mixed<float>", pms, cross_peel / args.steps, B_PEEL
         else:
-            kname, kms, kbytes = "k_wave<float>", tms, cross_prop * B_PROP / args.steps
+            kname, kms, kcross, kb = "k_wave<float>", tms, cross_prop / args.steps, B_PROP
+        kbytes = kcross * kb
         achieved = kbytes / (kms / 1000.0) / 1e9
+        per_cross = profiled_traffic(args.workload).get(kname)
+        traffic = per_cross * kcross / waves if per_cross is not None else None
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind, "traffic": None, "kernel": kname,
+                "peak_source": peak_kind, "traffic": traffic, "kernel": kname,
+                "algorithmic_bytes_per_launch": kbytes / waves, "launches_per_step": waves,
                 "kernel_ms_per_step": kms, "transport_ms_per_step": tms, "peel_ms_per_step": pms,
-                "algorithmic_bytes_per_step": kbytes,
                 "crossings_per_step": {"prop": cross_prop // args.steps, "peel": cross_peel // args.steps}}
         cpu = None
         if rank == 0 and not args.no_cpu_baseline:

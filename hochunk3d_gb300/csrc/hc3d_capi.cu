@@ -255,6 +255,7 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   a->numin = p->numin;
   a->lnurat = std::log(p->numax / p->numin);
   a->rstar_cm = p->rstar_cm;
+  for (int s = 0; s < kSlots; ++s) a->kapfac[s] = (float)(p->rstar_cm * c->kappav[s]);
   a->iintmax = p->iintmax > 0 ? p->iintmax : 10000;
   a->max_interactions = p->max_interactions;
   a->peeldir = c->d_peeldir;
@@ -529,6 +530,47 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
     c->dm.lTintf = fp[5]; c->dm.nuintf = fp[6]; c->dm.kapBintf = fp[7]; c->dm.hnuintf = fp[8];
     c->dm.atmosnuf = fp[9]; c->dm.lognuf = fp[10]; c->dm.loghnuf = fp[11];
   }
+  // Lucy CDF of the mixed form: row pairs interleaved per frequency, and the
+  // guide of index brackets per probability level (see DevModel)
+  {
+    const int nT = t->nT, nnu = t->nnu;
+    if (nnu > 32767) return fail(c, HC3D_ERR_INVALID, "nnu too large for the CDF guide");
+    std::vector<float2> pair((size_t)kSlots * (nT - 1) * nnu);
+    std::vector<short2> guide((size_t)kSlots * (nT - 1) * kGuide);
+    std::vector<int> last((size_t)nT * (kGuide + 1));
+    for (int s = 0; s < kSlots; ++s) {
+      const double* K = kB.data() + (size_t)s * nT * nnu;
+      auto kf = [&](int j, int i) { return (float)K[(size_t)(j - 1) + (size_t)nT * (i - 1)]; };
+      // last[j][b]: the last index i with K(j,i) <= b/kGuide (0 if none), for a non-decreasing row
+      for (int j = 1; j <= nT; ++j) {
+        int i = 0;
+        for (int b = 0; b <= kGuide; ++b) {
+          const float lev = (float)b / (float)kGuide;
+          while (i < nnu && kf(j, i + 1) <= lev) ++i;
+          last[(size_t)(j - 1) * (kGuide + 1) + b] = i;
+        }
+      }
+      for (int j = 1; j < nT; ++j) {
+        float2* row = &pair[((size_t)s * (nT - 1) + (j - 1)) * nnu];
+        for (int i = 1; i <= nnu; ++i) row[i - 1] = make_float2(kf(j, i), kf(j + 1, i));
+        const int* a = &last[(size_t)(j - 1) * (kGuide + 1)];
+        const int* b2 = &last[(size_t)j * (kGuide + 1)];
+        short2* g = &guide[((size_t)s * (nT - 1) + (j - 1)) * kGuide];
+        for (int b = 0; b < kGuide; ++b) {
+          const int lo = std::max(1, std::min(a[b], b2[b]));
+          const int hi = std::min(nnu, std::max(a[b + 1], b2[b + 1]) + 1);
+          g[b] = make_short2((short)lo, (short)hi);
+        }
+      }
+    }
+    float2* d_pair = nullptr;
+    short2* d_guide = nullptr;
+    if ((r = dupload(c, own, &d_pair, pair.data(), pair.size())) ||
+        (r = dupload(c, own, &d_guide, guide.data(), guide.size())))
+      return r;
+    c->dm.kpairf = d_pair;
+    c->dm.kguide = d_guide;
+  }
   c->tsub = t->tsub > 0.0 ? t->tsub : 1600.0;
   c->tables = true;
   if (c->grid) {
@@ -612,10 +654,13 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   m.nrg = nrg; m.ntg = ntg; m.npg = npg; m.ncell = ncell;
   m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
   {
-    std::vector<float> rf32(g->rarr, g->rarr + nrg);
-    float* d_rarrf = nullptr;
-    if ((r = dupload(c, own, &d_rarrf, rf32.data(), rf32.size()))) return r;
+    std::vector<float> rf32(g->rarr, g->rarr + nrg), r2f32(g->r2arr, g->r2arr + nrg);
+    float *d_rarrf = nullptr, *d_r2arrf = nullptr;
+    if ((r = dupload(c, own, &d_rarrf, rf32.data(), rf32.size())) ||
+        (r = dupload(c, own, &d_r2arrf, r2f32.data(), r2f32.size())))
+      return r;
     m.rarrf = d_rarrf;
+    m.r2arrf = d_r2arrf;
   }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
   m.peelmask = c->d_peelmask; m.tdust = c->d_tdust;

@@ -13,6 +13,7 @@ constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2
 constexpr int kNo = 8;      // SED components (output.F90:232-239)
 constexpr int kMaxPeel = 256;
 constexpr int kFaultLog = 256;
+constexpr int kGuide = 64;  // probability levels of the Lucy-CDF guide table
 
 // Fortran-layout sizes of the tally arrays of one run configuration.
 struct TallyDims {
@@ -46,6 +47,7 @@ struct DevModel {
   int64_t ncell;
   const double* rarr;     // (nrg)
   const float* rarrf;     // (nrg)
+  const float* r2arrf;    // (nrg) squares of rarr rounded to FP32
   const double* r2arr;    // (nrg)
   const double* thetarr;  // (ntg)
   const double* phiarr;   // (npg)
@@ -75,6 +77,11 @@ struct DevModel {
   const float* nudustf; const float* kappadf; const float* adustf; const float* gdustf; const float* pldustf;
   const float* lTintf; const float* nuintf; const float* kapBintf;
   const float* hnuintf; const float* atmosnuf; const float* lognuf; const float* loghnuf;
+  // Lucy CDF of the mixed form: kpairf[(slot*(nT-1) + j-1)*nnu + i-1] = (K(j,i), K(j+1,i)) of the
+  // FP32 kapBint rows j and j+1; kguide[(slot*(nT-1) + j-1)*kGuide + b] = (lo, hi) brackets the
+  // frequency index where the interpolated CDF of rows j, j+1 crosses a level in [b, b+1)/kGuide
+  const float2* kpairf;
+  const short2* kguide;
 };
 
 // One call of the packet loop.
@@ -86,6 +93,7 @@ struct RunArgs {
   double rmaxi, fractxh;
   double numin, lnurat;
   double rstar_cm;
+  float kapfac[kSlots];      // rstar_cm * kappa_V of each slot, FP32 (mixed-form opacities)
   int iintmax;
   int64_t max_interactions;
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe

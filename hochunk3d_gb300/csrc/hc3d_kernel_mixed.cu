@@ -32,7 +32,7 @@ cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const Tall
       m, t, d, a, static_cast<dev::Slot<float>*>(w.pool), static_cast<dev::PeelRec<float>*>(w.queue), w.qcount, E, w.alive);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;
-  dev::k_peel<float><<<peel.blocks, peel.threads, 0, peel.stream>>>(
+  dev::k_peel_mixed<float><<<peel.blocks, dev::kPeelThreads, 0, peel.stream>>>(
       m, t, d, a, static_cast<const dev::PeelRec<float>*>(w.queue), w.qcount, w.next_ray);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], wave.stream)) != cudaSuccess) return e;
@@ -42,6 +42,6 @@ cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const Tall
 size_t slot_bytes_mixed() { return sizeof(dev::Slot<float>); }
 size_t rec_bytes_mixed() { return sizeof(dev::PeelRec<float>); }
 const void* wave_fn_mixed() { return (const void*)dev::k_wave<float>; }
-const void* peel_fn_mixed() { return (const void*)dev::k_peel<float>; }
+const void* peel_fn_mixed() { return (const void*)dev::k_peel_mixed<float>; }
 
 }  // namespace hc3d

@@ -28,7 +28,6 @@
 #pragma once
 
 #include <cstdint>
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "hc3d_device.h"
@@ -174,165 +173,148 @@ struct Walls {
   }
 };
 
-// radface.f90:44-62.  FP64 form: the reference's (-b +- sqrt(D))/2.  Mixed
-// form: the same roots in FP64 by the cancellation-free q = -(b+sign(b)sqrt D)/2,
-// roots q and c/q; on the sphere the packet stands on (own) the roots are
-// exactly 0 and -b.
-template <class R>
-__device__ __forceinline__ void radface(Walls<R>& w, double ux, double uy, double uz, double x, double y, double z,
-                                        double R2_1, double R2_2, int own) {
+// radface.f90:44-62: both roots (-b +- sqrt(D))/2 of each sphere (FP64 form)
+__device__ __forceinline__ void radface(Walls<double>& w, double ux, double uy, double uz, double x, double y,
+                                        double z, double R2_1, double R2_2) {
   const double bb = 2.0 * (x * ux + y * uy + uz * z);
   const double rr = x * x + y * y + z * z;
-  if (sizeof(R) == 8) {
-    double cc = rr - R2_1;
-    double descr = bb * bb - 4.0 * cc;
-    if (descr > 0.0) {
-      descr = sqrt(descr);
-      w.insert((R)((-bb + descr) * 0.5), 1);
-      w.insert((R)((-bb - descr) * 0.5), 1);
-    }
-    cc = rr - R2_2;
-    descr = bb * bb - 4.0 * cc;
-    if (descr > 0.0) {
-      descr = sqrt(descr);
-      w.insert((R)((-bb + descr) * 0.5), 2);
-      w.insert((R)((-bb - descr) * 0.5), 2);
-    }
-  } else {
-    // With the wall the packet stands on given the exact root 0, negative
-    // roots never decide the next wall, so only the nearest non-negative
-    // root of each sphere is formed: outside a sphere moving away there is
-    // none; inside it one square root, and a division only when b > 0.
-#pragma unroll
-    for (int id = 1; id <= 2; ++id) {
-      if (own & (1 << id)) {
-        w.insert(R(0), id);
-        if (bb < 0.0) w.insert((R)(-bb), id);
-        continue;
-      }
-      // FP64 for the cancelling terms |x|^2 - R^2 and b^2 - 4c; the root itself
-      // is well conditioned in the cancellation-free form and is taken in FP32
-      const double cc = rr - (id == 1 ? R2_1 : R2_2);
-      if (cc > 0.0 && bb >= 0.0) continue;
-      const double descr = bb * bb - 4.0 * cc;
-      if (descr > 0.0) {
-        const float sd = sqrtf((float)descr), bbf = (float)bb, ccf = (float)cc;
-        if (cc > 0.0) {
-          w.insert((R)(ccf / (0.5f * (sd - bbf))), id);  // near root, entering the sphere
-        } else if (bb > 0.0) {
-          w.insert((R)(ccf / (-0.5f * (bbf + sd))), id);
-        } else {
-          w.insert((R)(0.5f * (sd - bbf)), id);
-        }
-      }
-    }
+  double cc = rr - R2_1;
+  double descr = bb * bb - 4.0 * cc;
+  if (descr > 0.0) {
+    descr = sqrt(descr);
+    w.insert((-bb + descr) * 0.5, 1);
+    w.insert((-bb - descr) * 0.5, 1);
+  }
+  cc = rr - R2_2;
+  descr = bb * bb - 4.0 * cc;
+  if (descr > 0.0) {
+    descr = sqrt(descr);
+    w.insert((-bb + descr) * 0.5, 2);
+    w.insert((-bb - descr) * 0.5, 2);
   }
 }
 
 // thetaface (module not shipped; restated): one cone wall on the nappe of its
-// hemisphere; tan2 < 0 is the midplane plane z = 0; tan2 == 0 is a pole.  In
-// the mixed form the cone the packet stands on has the exact root 0 and the
-// second root -b/a: FP32 would otherwise place two roots of that cone within
-// rounding of zero at grazing incidence and let the walk re-cross it.
-template <class R>
-__device__ __forceinline__ void cone_roots(Walls<R>& w, R ux, R uy, R uz, R x, R y, R z, R tan2, R hemi, int id,
-                                           bool own) {
-  if (tan2 == R(0)) return;
-  if (tan2 < R(0)) {
-    if (own) w.insert(R(0), id);
-    else if (uz != R(0)) w.insert(-z / uz, id);
+// hemisphere; tan2 < 0 is the midplane plane z = 0; tan2 == 0 is a pole.
+__device__ __forceinline__ void cone_roots(Walls<double>& w, double ux, double uy, double uz, double x, double y,
+                                           double z, double tan2, double hemi, int id) {
+  if (tan2 == 0.0) return;
+  if (tan2 < 0.0) {
+    if (uz != 0.0) w.insert(-z / uz, id);
     return;
   }
-  const R a = ux * ux + uy * uy - tan2 * uz * uz;
-  const R b = R(2) * (x * ux + y * uy - tan2 * z * uz);
-  if (own) {
-    w.insert(R(0), id);
-    if (a != R(0)) {
-      const R t = -b / a;
-      if ((z + t * uz) * hemi > R(0)) w.insert(t, id);
+  const double a = ux * ux + uy * uy - tan2 * uz * uz;
+  const double b = 2.0 * (x * ux + y * uy - tan2 * z * uz);
+  const double cq = x * x + y * y - tan2 * z * z;
+  if (a == 0.0) {
+    if (b != 0.0) {
+      const double t = -cq / b;
+      if ((z + t * uz) * hemi > 0.0) w.insert(t, id);
     }
     return;
   }
-  const R cq = x * x + y * y - tan2 * z * z;
-  if (a == R(0)) {
-    if (b != R(0)) {
-      R t = -cq / b;
-      if ((z + t * uz) * hemi > R(0)) w.insert(t, id);
-    }
-    return;
-  }
-  R descr = b * b - R(4) * a * cq;
-  if (descr > R(0)) {
-    descr = xsqrt(descr);
-    const R t1 = (-b + descr) / (R(2) * a);
-    const R t2 = (-b - descr) / (R(2) * a);
-    if ((z + t1 * uz) * hemi > R(0)) w.insert(t1, id);
-    if ((z + t2 * uz) * hemi > R(0)) w.insert(t2, id);
+  double descr = b * b - 4.0 * a * cq;
+  if (descr > 0.0) {
+    descr = sqrt(descr);
+    const double t1 = (-b + descr) / (2.0 * a);
+    const double t2 = (-b - descr) / (2.0 * a);
+    if ((z + t1 * uz) * hemi > 0.0) w.insert(t1, id);
+    if ((z + t2 * uz) * hemi > 0.0) w.insert(t2, id);
   }
 }
-
-template <class R> __device__ __forceinline__ R tan2_of(const DevModel& m, int i);
-template <> __device__ __forceinline__ float tan2_of<float>(const DevModel& m, int i) { return __ldg(m.tan2f + i); }
-template <> __device__ __forceinline__ double tan2_of<double>(const DevModel& m, int i) { return __ldg(m.tan2d + i); }
-template <class R> __device__ __forceinline__ R aarr_of(const DevModel& m, int i);
-template <> __device__ __forceinline__ float aarr_of<float>(const DevModel& m, int i) { return __ldg(m.aarrf + i); }
-template <> __device__ __forceinline__ double aarr_of<double>(const DevModel& m, int i) { return __ldg(m.aarrd + i); }
-template <class R> __device__ __forceinline__ R barr_of(const DevModel& m, int i);
-template <> __device__ __forceinline__ float barr_of<float>(const DevModel& m, int i) { return __ldg(m.barrf + i); }
-template <> __device__ __forceinline__ double barr_of<double>(const DevModel& m, int i) { return __ldg(m.barrd + i); }
 
 // The wall a packet stands on after crossing wall iface of its old cell, as a
 // wall id of the new cell (1<->2, 3<->4, 5<->6).
 __device__ __forceinline__ int own_after(int iface) { return ((iface - 1) ^ 1) + 1; }
 
-// The set of walls (bit id) a packet stands on after crossing wall iface with
-// step dt.  A step of (near) zero length is a crossing at an edge where two
-// walls meet: the packet still stands on the walls of the other families it
-// stood on before, and the FP32 walk must not re-cross them.
-template <class R>
-__device__ __forceinline__ int walls_after(int iface, int before, R dt, double x, double y, double z) {
-  (void)before; (void)dt; (void)x; (void)y; (void)z;
-  return 1 << own_after(iface);
-}
-
-// The wall machinery of one step (peeloff_3d.f90:92-115).  on_wall is 0 off
-// the walls, else the id (1..6) of the wall of the current cell the packet
-// stands on; the FP64 form uses it only as the reference's on_wall flag.
+// The wall machinery of one step (peeloff_3d.f90:92-115), FP64 form.
+// on_wall is the reference's on_wall flag (nonzero on a wall).
 template <class R>
 __device__ __forceinline__ bool next_wall(const DevModel& m, R ux, R uy, R uz, double x, double y, double z, int ir,
                                           int it, int ip, int on_wall, R& dt, int& iface) {
+  static_assert(sizeof(R) == 8, "next_wall is the FP64 form");
   Walls<R> w;
   w.reset();
-  const int own = sizeof(R) == 4 ? on_wall : 0;
-  radface<R>(w, (double)ux, (double)uy, (double)uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir), own);
+  radface(w, ux, uy, uz, x, y, z, __ldg(m.r2arr + ir - 1), __ldg(m.r2arr + ir));
   if (m.ntg > 2) {
-    const R xr = (R)x, yr = (R)y, zr = (R)z;
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it - 1), (R)__ldg(m.hemi + it - 1), 3, (own & 8) != 0);
-    cone_roots<R>(w, ux, uy, uz, xr, yr, zr, tan2_of<R>(m, it), (R)__ldg(m.hemi + it), 4, (own & 16) != 0);
+    cone_roots(w, ux, uy, uz, x, y, z, __ldg(m.tan2d + it - 1), (double)__ldg(m.hemi + it - 1), 3);
+    cone_roots(w, ux, uy, uz, x, y, z, __ldg(m.tan2d + it), (double)__ldg(m.hemi + it), 4);
     if (m.npg > 2) {
       // phiface.f90:48-56 with C = D = 0
-      const R A1 = aarr_of<R>(m, ip - 1), B1 = barr_of<R>(m, ip - 1);
-      const R A2 = aarr_of<R>(m, ip), B2 = barr_of<R>(m, ip);
-      const R d1 = A1 * ux + B1 * uy;
-      if (own & 32) w.insert(R(0), 5);
-      else if (d1 != R(0)) w.insert(-(A1 * xr + B1 * yr) / d1, 5);
-      const R d2 = A2 * ux + B2 * uy;
-      if (own & 64) w.insert(R(0), 6);
-      else if (d2 != R(0)) w.insert(-(A2 * xr + B2 * yr) / d2, 6);
+      const double A1 = __ldg(m.aarrd + ip - 1), B1 = __ldg(m.barrd + ip - 1);
+      const double A2 = __ldg(m.aarrd + ip), B2 = __ldg(m.barrd + ip);
+      const double d1 = A1 * ux + B1 * uy;
+      if (d1 != 0.0) w.insert(-(A1 * x + B1 * y) / d1, 5);
+      const double d2 = A2 * ux + B2 * uy;
+      if (d2 != 0.0) w.insert(-(A2 * x + B2 * y) / d2, 6);
     }
   }
   return w.next(on_wall != 0, dt, iface);
 }
 
-// Mixed form of the wall search.  The reference keeps the roots of every wall
-// in closest_wall and skips the root of the wall it stands on by the on_wall
-// rule; here the walls in `own` (bit id) contribute only their far
-// intersection and the next wall is the smallest non-negative root of the
-// rest, a minimum over at most six candidates.  FP64 enters only |x|^2, x.u and
-// |x|^2 - R^2 of the two spheres (the cancelling terms); the sphere roots are
-// then taken in FP32 by the cancellation-free forms, cones and planes in FP32.
-__device__ __forceinline__ bool next_wall_f32(const DevModel& m, float ux, float uy, float uz, double uxd, double uyd,
-                                              double uzd, double x, double y, double z, int ir, int it, int ip,
+// A straight ray of the mixed form, parametrised by its path length S from
+// the start point.  S is an unevaluated FP32 pair (hi + lo) advanced by an
+// error-free FP32 sum, so the FP32 position x0 + S u carries no error that
+// grows along the ray.  The FP64 radial terms |x|^2 and x.u are formed from
+// the FP64 start point only when a sphere root needs them (first use).
+struct PathLen {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void path_add(PathLen& s, float d) {
+  const float t = s.hi + d;
+  const float bp = t - s.hi;
+  s.lo += (s.hi - (t - bp)) + (d - bp);
+  s.hi = t;
+}
+
+__device__ __forceinline__ double path_f64(const PathLen& s) { return (double)s.hi + (double)s.lo; }
+
+struct Ray {
+  float x0, y0, z0, ux, uy, uz;  // FP32 start point and direction
+  double xd, yd, zd;             // FP64 start point
+  double rr0, hb0, u2;           // FP64 |x0|^2, x0.u, |u|^2 once `dbl` is set
+  bool dbl;
+};
+
+__device__ __forceinline__ void ray_init(Ray& r, double x, double y, double z, float xf, float yf, float zf, float ux,
+                                         float uy, float uz) {
+  r.x0 = xf; r.y0 = yf; r.z0 = zf;
+  r.ux = ux; r.uy = uy; r.uz = uz;
+  r.xd = x; r.yd = y; r.zd = z;
+  r.dbl = false;
+}
+
+__device__ __forceinline__ void ray_f64(Ray& r) {
+  if (r.dbl) return;
+  const double uxd = r.ux, uyd = r.uy, uzd = r.uz;
+  r.rr0 = r.xd * r.xd + r.yd * r.yd + r.zd * r.zd;
+  r.hb0 = r.xd * uxd + r.yd * uyd + r.zd * uzd;
+  r.u2 = uxd * uxd + uyd * uyd + uzd * uzd;
+  r.dbl = true;
+}
+
+// FP64 point of the ray at path length S
+__device__ __forceinline__ void ray_at(const Ray& r, const PathLen& S, double& x, double& y, double& z) {
+  const double s = path_f64(S);
+  x = fma(s, (double)r.ux, r.xd);
+  y = fma(s, (double)r.uy, r.yd);
+  z = fma(s, (double)r.uz, r.zd);
+}
+
+// A sphere root from FP32 |x|^2 - R^2 is exact enough unless the point lies
+// within 2^-12 R^2 of the sphere (|x|^2 - R^2 cancels) or the ray grazes it
+// (hb^2 - c within 2^-8 R^2 of zero); those cases are redone in FP64.
+constexpr float kNearSphere = 1.0f / 4096.0f;
+constexpr float kGrazeSphere = 1.0f / 256.0f;
+
+// The mixed-form wall search on a Ray at path length S.  The reference keeps
+// the roots of every wall in closest_wall and skips the root of the wall it
+// stands on by the on_wall rule; here the walls in `own` (bit id) contribute
+// only their far root, and the next wall is the smallest non-negative root
+// of the rest, a minimum over at most six candidates.  FP32, except the
+// near-sphere and grazing sphere roots (FP64).
+__device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const PathLen& S, int ir, int it, int ip,
                                               int own, float& dt, int& iface) {
   float best = 3.402823466e38f;
   int bi = 0;
@@ -342,36 +324,48 @@ __device__ __forceinline__ bool next_wall_f32(const DevModel& m, float ux, float
       bi = id;
     }
   };
-  // spheres: t^2 + 2 hb t + c = 0 with hb = x.u, c = |x|^2 - R^2
-  const double hb = x * uxd + y * uyd + z * uzd;
-  const double rr = x * x + y * y + z * z;
-  const float hbf = (float)hb;
-  if (own & 2) {
-    if (hbf < 0.f) cand(-2.f * hbf, 1);
-  } else if (hbf < 0.f) {  // inner sphere: reached only moving inwards
-    const float c = (float)(rr - __ldg(m.r2arr + ir - 1));
-    const float disc = hbf * hbf - c;
-    if (disc > 0.f) cand(fmaxf(c, 0.f) / (sqrtf(disc) - hbf), 1);
+  const float ux = r.ux, uy = r.uy, uz = r.uz;
+  const float xr = fmaf(S.hi, ux, fmaf(S.lo, ux, r.x0));
+  const float yr = fmaf(S.hi, uy, fmaf(S.lo, uy, r.y0));
+  const float zr = fmaf(S.hi, uz, fmaf(S.lo, uz, r.z0));
+  // spheres: t^2 + 2 hb t + c = 0 with hb = x.u, c = |x|^2 - R^2, disc = hb^2 - c
+  const bool in_own = (own & 2) != 0, out_own = (own & 4) != 0;
+  float hb = xr * ux + yr * uy + zr * uz;
+  const float rr = xr * xr + yr * yr + zr * zr;
+  const float r2i = __ldg(m.r2arrf + ir - 1), r2o = __ldg(m.r2arrf + ir);
+  float ci = rr - r2i, co = rr - r2o;
+  float di = hb * hb - ci, dq = hb * hb - co;
+  const bool fix = (!in_own && (fabsf(ci) < kNearSphere * r2i || fabsf(di) < kGrazeSphere * r2i)) ||
+                   (!out_own && (fabsf(co) < kNearSphere * r2o || fabsf(dq) < kGrazeSphere * r2o));
+  if (fix) {
+    ray_f64(r);
+    const double s = path_f64(S);
+    const double hbd = fma(s, r.u2, r.hb0);
+    const double rrd = fma(s, fma(s, r.u2, r.hb0 + r.hb0), r.rr0);
+    const double cid = rrd - __ldg(m.r2arr + ir - 1), cod = rrd - __ldg(m.r2arr + ir);
+    hb = (float)hbd;
+    ci = (float)cid; co = (float)cod;
+    di = (float)(hbd * hbd - cid); dq = (float)(hbd * hbd - cod);
   }
-  if (own & 4) {
-    if (hbf < 0.f) cand(-2.f * hbf, 2);
-  } else {  // outer sphere: the exit root
-    const float c = (float)(rr - __ldg(m.r2arr + ir));
-    const float disc = hbf * hbf - c;
-    if (disc > 0.f) {
-      const float s = sqrtf(disc);
-      cand(hbf > 0.f ? fmaxf(-c, 0.f) / (hbf + s) : s - hbf, 2);
-    }
+  if (in_own) {
+    if (hb < 0.f) cand(-2.f * hb, 1);
+  } else if (hb < 0.f && di > 0.f) {  // inner sphere: reached only moving inwards
+    cand(fmaxf(ci, 0.f) / (sqrtf(di) - hb), 1);
+  }
+  if (out_own) {
+    if (hb < 0.f) cand(-2.f * hb, 2);
+  } else if (dq > 0.f) {  // outer sphere: the exit root
+    const float sq = sqrtf(dq);
+    cand(hb > 0.f ? fmaxf(-co, 0.f) / (hb + sq) : sq - hb, 2);
   }
   if (m.ntg > 2) {
-    const float xr = (float)x, yr = (float)y, zr = (float)z;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int id = 3 + k;
       const float tan2 = __ldg(m.tan2f + it - 1 + k);
-      if (tan2 == 0.f) continue;  // a pole: no crossing
+      if (tan2 == 0.f) continue;
       const bool mine = (own >> id) & 1;
-      if (tan2 < 0.f) {  // the midplane z = 0
+      if (tan2 < 0.f) {
         if (!mine && uz != 0.f) cand(-zr / uz, id);
         continue;
       }
@@ -395,8 +389,8 @@ __device__ __forceinline__ bool next_wall_f32(const DevModel& m, float ux, float
       }
       const float disc = b * b - 4.f * a * cq;
       if (disc > 0.f) {
-        const float s = sqrtf(disc), inv = 0.5f / a;
-        const float t1 = (-b + s) * inv, t2 = (-b - s) * inv;
+        const float sq = sqrtf(disc), inv = 0.5f / a;
+        const float t1 = (-b + sq) * inv, t2 = (-b - sq) * inv;
         if ((zr + t1 * uz) * hemi > 0.f) cand(t1, id);
         if ((zr + t2 * uz) * hemi > 0.f) cand(t2, id);
       }
@@ -405,7 +399,7 @@ __device__ __forceinline__ bool next_wall_f32(const DevModel& m, float ux, float
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
         const int id = 5 + k;
-        if ((own >> id) & 1) continue;  // a plane is crossed once
+        if ((own >> id) & 1) continue;
         const float A = __ldg(m.aarrf + ip - 1 + k), B = __ldg(m.barrf + ip - 1 + k);
         const float d = A * ux + B * uy;
         if (d != 0.f) cand(-(A * xr + B * yr) / d, id);
@@ -508,7 +502,7 @@ __device__ __forceinline__ void dust_view(const DevModel& m, R* smem, DustView<R
 // the result (only kappa_V differs), which is what the per-slot loop of the
 // reference computes for them.
 template <class R>
-__device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, double nu_in, double rstar_cm) {
+__device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, double nu_in, const RunArgs& a) {
   const R nu = (R)nu_in;
   R gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
   for (int u = 0; u < m.ntab; ++u) {
@@ -536,7 +530,8 @@ __device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, doub
   for (int id = 0; id < kSlots; ++id) {
     const int u = m.table_of[id];
     p.g[id] = gt[u]; p.pl[id] = plt[u]; p.albedo[id] = at[u];
-    p.kapd[id] = (R)((double)kt[u] * rstar_cm * m.kappav[id]);
+    if constexpr (sizeof(R) == 4) p.kapd[id] = kt[u] * a.kapfac[id];
+    else p.kapd[id] = (R)((double)kt[u] * a.rstar_cm * m.kappav[id]);
   }
 }
 
@@ -577,34 +572,50 @@ __device__ __forceinline__ bool tiny_step(const DevModel& m, float dt, int ir) {
   return dt <= 1.0e-6f * __ldg(m.rarrf + min(ir, m.nrg - 1));
 }
 
-// One wall search in either form: the reference's closest_wall machinery in
-// FP64, the candidate minimum in the mixed form (uxd..: the direction in FP64).
-template <class R>
-__device__ __forceinline__ bool find_wall(const DevModel& m, R ux, R uy, R uz, double uxd, double uyd, double uzd,
-                                          double x, double y, double z, int ir, int it, int ip, int on_wall, R& dt,
-                                          int& iface) {
-  if constexpr (sizeof(R) == 4) {
-    return next_wall_f32(m, ux, uy, uz, uxd, uyd, uzd, x, y, z, ir, it, ip, on_wall, dt, iface);
-  } else {
-    return next_wall<R>(m, ux, uy, uz, x, y, z, ir, it, ip, on_wall, dt, iface);
-  }
+// Round a float to the nearest int64 (halves away from zero) with integer
+// operations only: the fixed-point conversion of the mixed form.  |v| must be
+// below 2^63; the tally scales keep it far below.
+__device__ __forceinline__ long long f2ll(float v) {
+  const unsigned b = __float_as_uint(v);
+  const int ex = (int)((b >> 23) & 0xffu);
+  const unsigned mant = (b & 0x7fffffu) | 0x800000u;
+  const int e = ex - 150;  // |v| = mant * 2^e
+  long long r;
+  if (ex == 0 || e < -24) r = 0;
+  else if (e >= 0) r = e > 39 ? 0x7fffffffffffffffll : (long long)mant << e;
+  else r = (long long)((mant + (1u << (-e - 1))) >> (-e));
+  return (b >> 31) ? -r : r;
 }
 
-template <class R>
-__device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
-  R tsum = R(0);
+// scale is a power of two, so v * scale is exact
+__device__ __forceinline__ unsigned long long fxf(float v, float scale) {
+  return (unsigned long long)f2ll(v * scale);
+}
+
+// Mixed form of tauint: the step of one event is a Ray from the event point;
+// the walk, the tau integral and the Lucy tallies are FP32, the FP64 point
+// where the walk stops is formed once, at the end.
+static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<float>& p, float tau, Local& L,
+                                   Tracer& tr) {
+  float tsum = 0.f;
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nreloc = 0, ntiny = 0;
-  const double uxd = (double)p.ux, uyd = (double)p.uy, uzd = (double)p.uz;
+  Ray ray;
+  ray_init(ray, p.x, p.y, p.z, (float)p.x, (float)p.y, (float)p.z, p.ux, p.uy, p.uz);
+  PathLen S{0.f, 0.f};
+  const float ps = (float)t.path_scale;
+  auto at = [&]() { ray_at(ray, S, p.x, p.y, p.z); };
   for (int n = 0;; ++n) {
     if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
       L.fault = n > cap ? F_CAP : F_RANGE;
+      at();
       return TI_FAULT;
     }
-    R dt;
+    float dt;
     int iface;
-    if (!find_wall<R>(m, p.ux, p.uy, p.uz, uxd, uyd, uzd, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
-      if (sizeof(R) == 4 && nreloc < 4) {
+    if (!next_wall_ray(m, ray, S, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+      at();
+      if (nreloc < 4) {
         ++nreloc;
         const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
         if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
@@ -616,57 +627,112 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
       return TI_FAULT;
     }
     const int64_t c = cidx(m, p.ir, p.it, p.ip);
-    const Rho<R> rho = load_rho<R>(m, c);
-    R opac = R(0);
+    const Rho<float> rho = load_rho<float>(m, c);
+    float opac = 0.f;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
-    const R dtau = opac * dt;
-    const double rout = __ldg(m.rarr + p.ir);
+    const float dtau = opac * dt;
+    const float rout = __ldg(m.rarrf + p.ir);
     L.c[HC3D_CNT_CROSS_PROP]++;
-    if (tsum + dtau > tau) {
-      const R ds = (tau - tsum) / opac;
-      p.x += (double)ds * uxd;
-      p.y += (double)ds * uyd;
-      p.z += (double)ds * uzd;
-      p.on_wall = 0;
+    const bool stop = tsum + dtau > tau;
+    const float ds = stop ? (tau - tsum) / opac : dt;
 #pragma unroll
-      for (int s = 0; s < kSlots; ++s)
-        if (rho.v[s] > R(0)) {
-          const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * ds;
-          atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
-        }
-      atomicAdd(t.jmean + c, fx((double)ds / rout, t.path_scale));
+    for (int s = 0; s < kSlots; ++s)
+      if (rho.v[s] > 0.f)
+        atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fxf(p.kapd[s] * (1.f - p.albedo[s]) * rho.v[s] * ds, ps));
+    atomicAdd(t.jmean + c, fxf(ds / rout, ps));
+    if (stop) {
+      path_add(S, ds);
+      at();
+      p.on_wall = 0;
       tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, p.x, p.y, p.z);
       return TI_INTERACT;
     }
-#pragma unroll
-    for (int s = 0; s < kSlots; ++s)
-      if (rho.v[s] > R(0)) {
-        const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * dt;
-        atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
-      }
-    atomicAdd(t.jmean + c, fx((double)dt / rout, t.path_scale));
     tsum += dtau;
     step_index(m.npg, iface, p.ir, p.it, p.ip);
-    p.x += (double)dt * uxd;
-    p.y += (double)dt * uyd;
-    p.z += (double)dt * uzd;
-    p.on_wall = walls_after<R>(iface, p.on_wall, dt, p.x, p.y, p.z);
-    tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
-    if (p.ir == m.nrg) return TI_ESCAPE;
-    if (p.ir == 0) return TI_STAR;
-    if (sizeof(R) == 4) {
-      // walls crossed back and forth at zero distance: re-derive the cell
-      if (!tiny_step(m, (float)dt, p.ir)) {
-        ntiny = 0;
-      } else if (++ntiny > 6 && nreloc < 4) {
-        ++nreloc;
-        ntiny = 0;
-        const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
-        if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
-        if (where == 2) { p.ir = 0; return TI_STAR; }
-        p.on_wall = 0;
+    path_add(S, dt);
+    p.on_wall = 1 << own_after(iface);
+    if (tr.recs) {
+      at();
+      tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
+    }
+    if (p.ir == m.nrg) { at(); return TI_ESCAPE; }
+    if (p.ir == 0) { at(); return TI_STAR; }
+    if (!tiny_step(m, dt, p.ir)) {
+      ntiny = 0;
+    } else if (++ntiny > 6 && nreloc < 4) {
+      ++nreloc;
+      ntiny = 0;
+      at();
+      const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
+      if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
+      if (where == 2) { p.ir = 0; return TI_STAR; }
+      p.on_wall = 0;
+    }
+  }
+}
+
+// tauint in either form: the FP64 form walks with the reference's wall
+// machinery (closest_wall rule), the mixed form with tauint_mixed.
+template <class R>
+__device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
+  if constexpr (sizeof(R) == 4) {
+    return tauint_mixed(m, t, p, tau, L, tr);
+  } else {
+    R tsum = R(0);
+    const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+    const double uxd = (double)p.ux, uyd = (double)p.uy, uzd = (double)p.uz;
+    for (int n = 0;; ++n) {
+      if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
+        L.fault = n > cap ? F_CAP : F_RANGE;
+        return TI_FAULT;
       }
+      R dt;
+      int iface;
+      if (!next_wall<R>(m, p.ux, p.uy, p.uz, p.x, p.y, p.z, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+        L.fault = F_NOWALL;
+        return TI_FAULT;
+      }
+      const int64_t c = cidx(m, p.ir, p.it, p.ip);
+      const Rho<R> rho = load_rho<R>(m, c);
+      R opac = R(0);
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
+      const R dtau = opac * dt;
+      const double rout = __ldg(m.rarr + p.ir);
+      L.c[HC3D_CNT_CROSS_PROP]++;
+      if (tsum + dtau > tau) {
+        const R ds = (tau - tsum) / opac;
+        p.x += (double)ds * uxd;
+        p.y += (double)ds * uyd;
+        p.z += (double)ds * uzd;
+        p.on_wall = 0;
+#pragma unroll
+        for (int s = 0; s < kSlots; ++s)
+          if (rho.v[s] > R(0)) {
+            const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * ds;
+            atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
+          }
+        atomicAdd(t.jmean + c, fx((double)ds / rout, t.path_scale));
+        tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, p.x, p.y, p.z);
+        return TI_INTERACT;
+      }
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s)
+        if (rho.v[s] > R(0)) {
+          const R v = p.kapd[s] * (R(1) - p.albedo[s]) * rho.v[s] * dt;
+          atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
+        }
+      atomicAdd(t.jmean + c, fx((double)dt / rout, t.path_scale));
+      tsum += dtau;
+      step_index(m.npg, iface, p.ir, p.it, p.ip);
+      p.x += (double)dt * uxd;
+      p.y += (double)dt * uyd;
+      p.z += (double)dt * uzd;
+      p.on_wall = 1 << own_after(iface);
+      tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
+      if (p.ir == m.nrg) return TI_ESCAPE;
+      if (p.ir == 0) return TI_STAR;
     }
   }
 }
@@ -864,10 +930,16 @@ struct PeelRec {
   R d0, d1, d2, d3, d4;  // scattered: cost, sint, phi, cosp, sinp of the incident packet; stellar: cosb, sinb, coslp, sinlp
   R g, pl;               // phase-matrix parameters of the scattering species
   R kapd[kSlots];
+  float xf, yf, zf;      // the event point in FP32 (mixed form)
 };
 
+template <class R>
 __device__ __forceinline__ int nu_bin(const RunArgs& a, double nub) {
-  int inub = (int)((double)a.nfreq * log(nub / a.numin) / a.lnurat) + 1;
+  int inub;
+  if constexpr (sizeof(R) == 4)
+    inub = (int)((float)a.nfreq * logf((float)nub / (float)a.numin) / (float)a.lnurat) + 1;
+  else
+    inub = (int)((double)a.nfreq * log(nub / a.numin) / a.lnurat) + 1;
   return inub < 1 ? 1 : (inub > a.nfreq ? a.nfreq : inub);
 }
 
@@ -876,12 +948,13 @@ __device__ __forceinline__ void make_rec(PeelRec<R>& e, const Pkt<R>& p, const R
   e.x = p.x; e.y = p.y; e.z = p.z;
   e.ir = p.ir; e.it = p.it; e.ip = p.ip;
   e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5) | (p.on_wall << 8);
-  e.inub = nu_bin(a, p.nub);
+  e.inub = nu_bin<R>(a, p.nub);
   e.sip = p.sip; e.sqp = p.sqp; e.sup = p.sup; e.svp = p.svp;
   e.d0 = p.cost; e.d1 = p.sint; e.d2 = p.phi; e.d3 = p.cosp; e.d4 = p.sinp;
   e.g = p.g[idust2]; e.pl = p.pl[idust2];
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) e.kapd[s] = p.kapd[s];
+  e.xf = (float)p.x; e.yf = (float)p.y; e.zf = (float)p.z;
 }
 
 __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, int64_t b, double i, double q, double u,
@@ -897,10 +970,25 @@ __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, i
   atomicAdd(base + 8 * stride + b, 1ull);
 }
 
-// ---- peeloff_3d.f90:52-286: one observer direction k of one event ----------------------
+__device__ __forceinline__ void add9f(unsigned long long* base, int64_t stride, int64_t b, float i, float q, float u,
+                                      float v, float ss, float sq) {
+  atomicAdd(base + b, fxf(i, ss));
+  atomicAdd(base + stride + b, fxf(q, ss));
+  atomicAdd(base + 2 * stride + b, fxf(u, ss));
+  atomicAdd(base + 3 * stride + b, fxf(v, ss));
+  atomicAdd(base + 4 * stride + b, fxf(i * i, sq));
+  atomicAdd(base + 5 * stride + b, fxf(q * q, sq));
+  atomicAdd(base + 6 * stride + b, fxf(u * u, sq));
+  atomicAdd(base + 7 * stride + b, fxf(v * v, sq));
+  atomicAdd(base + 8 * stride + b, 1ull);
+}
+
+// ---- peeloff_3d.f90:52-286: one observer direction k of one event (FP64 form) ----------
+// The mixed form walks its peel-off rays in k_peel_mixed.
 template <class R>
 __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                          const PeelRec<R>& e, int k, Local& L) {
+  static_assert(sizeof(R) == 8, "peel_ray is the FP64 form");
   const double* pd = a.peeldir + 4 * k;
   const R coste = (R)__ldg(pd), sinte = (R)__ldg(pd + 1), cospe = (R)__ldg(pd + 2), sinpe = (R)__ldg(pd + 3);
   const int flags = e.flags;
@@ -920,8 +1008,8 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   L.c[HC3D_CNT_PEELS]++;
   if (on_wall) {
     const double rsq1 = xp1 * xp1 + yp1 * yp1 + zp1 * zp1;
-    const bool inner_wall = fabs(rsq1 - __ldg(m.r2arr + ir - 1)) < fabs(rsq1 - __ldg(m.r2arr + ir));
     const bool outwards = (double)ux1 * xp1 + (double)uy1 * yp1 + (double)uz1 * zp1 > 0.0;
+    const bool inner_wall = fabs(rsq1 - __ldg(m.r2arr + ir - 1)) < fabs(rsq1 - __ldg(m.r2arr + ir));
     if (inner_wall && !outwards) {
       if (ir == 1) return;
       ir = ir - 1;
@@ -932,9 +1020,8 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
       on_wall = 1 << 1;
     }
   }
-  double tsum = 0.0;  // FP64 escape tau in both forms
+  double tsum = 0.0;
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
-  int nreloc = 0, ntiny = 0;
   const double uxd = (double)ux1, uyd = (double)uy1, uzd = (double)uz1;
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
@@ -943,15 +1030,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     }
     R dt;
     int iface;
-    if (!find_wall<R>(m, ux1, uy1, uz1, uxd, uyd, uzd, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
-      if (sizeof(R) == 4 && nreloc < 4) {
-        ++nreloc;
-        const int where = relocate(m, xp1, yp1, zp1, ir, it, ip);
-        if (where == 1) break;
-        if (where == 2) return;
-        on_wall = 0;
-        continue;
-      }
+    if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
       L.c[HC3D_CNT_PEEL_STUCK]++;
       return;
     }
@@ -969,21 +1048,9 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     xp1 += (double)dt * uxd;
     yp1 += (double)dt * uyd;
     zp1 += (double)dt * uzd;
-    on_wall = walls_after<R>(iface, on_wall, dt, xp1, yp1, zp1);
+    on_wall = 1 << own_after(iface);
     if (ir == m.nrg) break;
     if (ir == 0) return;
-    if (sizeof(R) == 4) {
-      if (!tiny_step(m, (float)dt, ir)) {
-        ntiny = 0;
-      } else if (++ntiny > 6 && nreloc < 4) {
-        ++nreloc;
-        ntiny = 0;
-        const int where = relocate(m, xp1, yp1, zp1, ir, it, ip);
-        if (where == 1) break;
-        if (where == 2) return;
-        on_wall = 0;
-      }
-    }
   }
   const R factor = (R)exp(-tsum);
   sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
@@ -1020,6 +1087,223 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   }
 }
 
+// ---- peel-off rays of the mixed form: a warp-synchronous ray pool --------------
+// Each lane of a warp holds one (event, direction) ray.  A loop iteration
+// refills the lanes whose ray ended (one atomic per warp), advances every
+// live ray by one cell crossing, and parks the rays that left the grid in a
+// per-warp buffer; the buffer is tallied 32 rays at a time, so the long
+// tally code (peeloff_3d.f90:155-282) runs with every lane busy instead of
+// one lane at a time.
+struct PeelDir {
+  float ux, uy, uz, coste, sinte, cospe, sinpe;
+};
+
+struct PeelEsc {
+  unsigned long long e;
+  float tsum, xf, yf, zf;
+  int k;
+};
+
+constexpr int kPeelThreads = 256;
+constexpr int kPeelBuf = 64;
+constexpr int kPeelChunk = 256;  // rays a warp reserves per atomic
+
+// peeloff_3d.f90:155-282 for one ray of the mixed form that reached the grid
+// edge: attenuation, the Stokes rotation of a scattered packet, image pixel
+// and aperture binning
+__device__ __forceinline__ void peel_tally_mixed(const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                                 const PeelRec<float>& e, const PeelDir& dd, int k, float tsum,
+                                                 float xf, float yf, float zf) {
+  const int flags = e.flags;
+  const int iflag = (flags >> 1) & 1;
+  const int i_orig = (flags >> 2) & 7;
+  const float coste = dd.coste, sinte = dd.sinte, cospe = dd.cospe, sinpe = dd.sinpe;
+  float sip = e.sip, sqp = e.sqp, sup = e.sup, svp = e.svp;
+  if (flags & 128) sip = 4.f * e.sip * (e.d0 * coste + (e.d1 * sinte * (cospe * e.d2 + sinpe * e.d3)));
+  const float factor = expf(-tsum);
+  sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
+  if (iflag == 1) {
+    float bmu, ri1;
+    findangle3<float>(e.d0, e.d1, e.d2, e.d3, e.d4, coste, sinte, 0.f, cospe, sinpe, bmu, ri1);
+    stokespeel<float>(e.g, e.pl, sip, sqp, sup, svp, coste, sinte, ri1, bmu, e.d0, e.d1);
+  }
+  const float yimage = zf * sinte - yf * coste * sinpe - xf * coste * cospe;
+  const float ximage = yf * cospe - xf * sinpe;
+  const float rmaxi = (float)a.rmaxi, fractxh = (float)a.fractxh;
+  const int ix = (int)((ximage + rmaxi) / fractxh) + 1;
+  const int iy = (int)((yimage + rmaxi) / fractxh) + 1;
+  const float rho2 = ximage * ximage + yimage * yimage;
+  const int i_inter = iflag == 1 ? 2 : (i_orig == 1 ? 1 : 3);
+  const int indx[3] = {1, 1 + i_orig, 5 + i_inter};
+  const float ss = (float)t.stokes_scale, sq = (float)t.square_scale;
+  for (int ia = 1; ia <= a.nap; ++ia) {
+    if (rho2 < (float)__ldg(a.aperture2 + ia - 1)) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int64_t b = (int64_t)(e.inub - 1) +
+                          (int64_t)a.nfreq * (k + (int64_t)a.npeel * ((ia - 1) + (int64_t)a.nap * (indx[q] - 1)));
+        add9f(t.psed, d.npsed, b, sip, sqp, sup, svp, ss, sq);
+      }
+    }
+  }
+  if (a.image && ix <= a.nx && iy <= a.nx && ix > 0 && iy > 0) {
+    const int64_t b = (int64_t)k + (int64_t)a.npeel * ((ix - 1) + (int64_t)a.nx * (iy - 1));
+    atomicAdd(t.img + b, fxf(sip, ss));
+    atomicAdd(t.img + d.nimg + b, fxf(sqp, ss));
+    atomicAdd(t.img + 2 * d.nimg + b, fxf(sup, ss));
+    atomicAdd(t.img + 3 * d.nimg + b, fxf(svp, ss));
+  }
+}
+
+// The walk of one peel-off ray of the mixed form (peeloff_3d.f90:52-154):
+// start() sets it up from an event record and a direction, step() crosses
+// one cell wall.
+struct PeelWalk {
+  Ray ray;
+  PathLen S;
+  double tsum;  // FP64 escape tau
+  float tf;     // FP32 copy of the sum for the taumax test only
+  int ir, it, ip, on_wall, nstep, nreloc, ntiny;
+  float kap[kSlots];
+
+  // false when the ray is not walked (the star's far side, or it enters the star)
+  __device__ __forceinline__ bool start(const DevModel& m, const PeelRec<float>& r, const PeelDir& dd) {
+    const int flags = r.flags;
+    if (flags & 128) {  // newdisktherm.F90:342-360: the star's surface faces the observer
+      const float cosnorm = r.d0 * dd.coste + (r.d1 * dd.sinte * (dd.cospe * r.d2 + dd.sinpe * r.d3));
+      if (!(cosnorm > 0.f)) return false;
+    }
+    ray_init(ray, r.x, r.y, r.z, r.xf, r.yf, r.zf, dd.ux, dd.uy, dd.uz);
+    ir = r.ir; it = r.it; ip = r.ip;
+    on_wall = (flags >> 8) & 127;
+    bool go = true;
+    if (on_wall) {  // peeloff_3d.f90:60-87: leave the radial wall the event sits on
+      ray_f64(ray);
+      const bool inner_wall = fabs(ray.rr0 - __ldg(m.r2arr + ir - 1)) < fabs(ray.rr0 - __ldg(m.r2arr + ir));
+      const bool outwards = ray.hb0 > 0.0;
+      if (inner_wall && !outwards) {
+        if (ir == 1) go = false;
+        ir = ir - 1;
+        on_wall = 1 << 2;
+      }
+      if (!inner_wall && outwards) {
+        ir = ir + 1;
+        on_wall = 1 << 1;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) kap[s] = r.kapd[s];
+    S = PathLen{0.f, 0.f};
+    tsum = 0.0;
+    tf = 0.f;
+    nstep = 0; nreloc = 0; ntiny = 0;
+    return go;
+  }
+
+  enum { GOING = 0, OUT = 1, ENDED = 2 };  // OUT: left the grid, to be tallied
+
+  __device__ __forceinline__ int step(const DevModel& m, int cap, Local& L) {
+    if (nstep > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
+      L.c[HC3D_CNT_PEEL_STUCK]++;
+      return ENDED;
+    }
+    ++nstep;
+    float dt;
+    int iface;
+    if (!next_wall_ray(m, ray, S, ir, it, ip, on_wall, dt, iface)) {
+      if (nreloc < 4) {
+        ++nreloc;
+        return relocate_here(m);
+      }
+      L.c[HC3D_CNT_PEEL_STUCK]++;
+      return ENDED;
+    }
+    const int64_t c = cidx(m, ir, it, ip);
+    const Rho<float> rho = load_rho<float>(m, c);
+    const unsigned mask = __ldg(m.peelmask + c);
+    float opac = 0.f;
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s)
+      if (mask & (1u << s)) opac += kap[s] * rho.v[s];
+    const float dtau = opac * dt;
+    tsum += (double)dtau;
+    tf += dtau;
+    L.c[HC3D_CNT_CROSS_PEEL]++;
+    if (tf > (float)kTauMax) return ENDED;
+    step_index(m.npg, iface, ir, it, ip);
+    path_add(S, dt);
+    on_wall = 1 << own_after(iface);
+    if (ir == m.nrg) return OUT;
+    if (ir == 0) return ENDED;
+    if (!tiny_step(m, dt, ir)) {
+      ntiny = 0;
+    } else if (++ntiny > 6 && nreloc < 4) {
+      ++nreloc;
+      ntiny = 0;
+      return relocate_here(m);
+    }
+    return GOING;
+  }
+
+  __device__ __forceinline__ int relocate_here(const DevModel& m) {
+    double x, y, z;
+    ray_at(ray, S, x, y, z);
+    int jr = ir, jt = it, jp = ip;  // locals: the walk's fields stay in registers
+    const int where = relocate(m, x, y, z, jr, jt, jp);
+    ir = jr; it = jt; ip = jp;
+    if (where == 1) return OUT;
+    if (where == 2) return ENDED;
+    on_wall = 0;
+    return GOING;
+  }
+
+  // FP32 point of the ray where it left the grid
+  __device__ __forceinline__ void end_point(float& x, float& y, float& z) const {
+    x = fmaf(S.hi, ray.ux, fmaf(S.lo, ray.ux, ray.x0));
+    y = fmaf(S.hi, ray.uy, fmaf(S.lo, ray.uy, ray.y0));
+    z = fmaf(S.hi, ray.uz, fmaf(S.lo, ray.uz, ray.z0));
+  }
+};
+
+__device__ __forceinline__ PeelDir peel_dir(const RunArgs& a, int k) {
+  const double* pd = a.peeldir + 4 * k;
+  PeelDir q;
+  q.coste = (float)__ldg(pd); q.sinte = (float)__ldg(pd + 1);
+  q.cospe = (float)__ldg(pd + 2); q.sinpe = (float)__ldg(pd + 3);
+  q.ux = q.sinte * q.cospe; q.uy = q.sinte * q.sinpe; q.uz = q.coste;
+  return q;
+}
+
+// One peel-off ray of the mixed form walked by one thread (the per-packet
+// loop of k_transport: trace harness and unwaved runs)
+__device__ __forceinline__ void peel_ray_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d,
+                                               const RunArgs& a, const PeelRec<float>& e, int k, Local& L) {
+  const PeelDir dd = peel_dir(a, k);
+  PeelWalk w;
+  if (!w.start(m, e, dd)) return;
+  L.c[HC3D_CNT_PEELS]++;
+  const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  int st;
+  while ((st = w.step(m, cap, L)) == PeelWalk::GOING) {
+  }
+  if (st == PeelWalk::OUT) {
+    float x, y, z;
+    w.end_point(x, y, z);
+    peel_tally_mixed(t, d, a, e, dd, k, (float)w.tsum, x, y, z);
+  }
+}
+
+// The peel-off rays of one event walked by the thread that made it (the
+// per-packet loop of k_transport)
+template <class R>
+__device__ __forceinline__ void peel_all(const DevModel& m, const DevTallies& t, const TallyDims& d,
+                                         const RunArgs& a, const PeelRec<R>& rec, Local& L) {
+  for (int k = 0; k < a.npeel; ++k) {
+    if constexpr (sizeof(R) == 4) peel_ray_mixed(m, t, d, a, rec, k, L);
+    else peel_ray<R>(m, t, d, a, rec, k, L);
+  }
+}
+
 // ---- lucydustfreq.f90:19-157 -------------------------------------------------------------
 // R-typed: FP64 tables and arithmetic in the FP64 form, FP32 in the mixed one.
 template <class R> __device__ __forceinline__ R xpow(R a, R b);
@@ -1042,6 +1326,44 @@ __device__ double lucydustfreq(const DevModel& m, double T0in, int id, Rng& rng)
   j = j < 1 ? 1 : (j > nT - 1 ? nT - 1 : j);
   R f = (lT0 - __ldg(lTint + j - 1)) / (__ldg(lTint + j) - __ldg(lTint + j - 1));
   f = f < R(0) ? R(0) : (f > R(1) ? R(1) : f);
+  if constexpr (sizeof(R) == 4) {
+    // mixed form: the same bracket of the interpolated CDF (it is
+    // non-decreasing, so the bracket is unique) from the guide table, then a
+    // short bisection over the interleaved rows j, j+1
+    const size_t pr = (size_t)id * (nT - 1) + (j - 1);
+    const float2* KP = m.kpairf + pr * nnu;
+    const short2 g = __ldg(m.kguide + pr * kGuide + min((int)(xi * (float)kGuide), kGuide - 1));
+    auto P = [&](int i) {
+      const float2 k = __ldg(KP + i - 1);
+      const float v = (1.f - f) * k.x + f * k.y;
+      return v > 1.f ? 1.f : v;
+    };
+    float P0 = P(1), P1 = P(nnu);
+    if (xi < P0) return (double)(P0 > 0.f ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint));
+    if (xi >= P1) {
+      if (P1 < 1.f && xi < 1.f) return (double)(T0 * __ldg(nuint + nnu - 1) * (1.f - P1) / (1.f - xi));
+      return (double)(T0 * __ldg(nuint + nnu - 1));
+    }
+    int i0 = g.x, i1 = g.y;
+    const float Pa = P(i0), Pb = P(i1);
+    if (Pa <= xi) P0 = Pa; else i0 = 1;
+    if (Pb > xi) P1 = Pb; else i1 = nnu;
+    if (i1 <= i0) { i0 = 1; i1 = nnu; P0 = P(1); P1 = P(nnu); }
+    while (i1 - i0 > 1) {
+      const int i = (i0 + i1) / 2;
+      const float v = P(i);
+      if (v > xi) { i1 = i; P1 = v; }
+      else { i0 = i; P0 = v; }
+    }
+    float w;
+    if (xi < P0) w = 0.f;
+    else if (xi > P1) w = 1.f;
+    else if (P0 <= 0.f) w = 0.5f;
+    else if (P1 <= 0.f || xi <= 0.f) w = f;
+    else w = logf(xi / P0) / logf(P1 / P0);
+    const float n0 = __ldg(nuint + i0 - 1), n1 = __ldg(nuint + i1 - 1);
+    return (double)(T0 * n0 * powf(n1 / n0, w));
+  }
 #define KB(jj, ii) __ldg(K + (size_t)((jj) - 1) + (size_t)nT * ((ii) - 1))
   int i0 = 1, i1 = nnu;
   R P0 = (R(1) - f) * KB(j, i0) + f * KB(j + 1, i0);
@@ -1132,7 +1454,7 @@ __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArg
       L.c[HC3D_CNT_NSCAT] += (unsigned long long)iscat;
     }
   }
-  const int inub = nu_bin(a, p.nub);
+  const int inub = nu_bin<R>(a, p.nub);
   const int i_inter = iflag == 1 ? 2 : (p.i_orig == 1 ? 1 : 3);
   const int indx[3] = {1, 1 + p.i_orig, 5 + i_inter};
   const double si = (double)p.sip, sq = (double)p.sqp, su = (double)p.sup, sv = (double)p.svp;
@@ -1214,7 +1536,7 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   p.cosp = xcos(p.phi);
   p.nub = atmosfreq<R>(m, rng);
   p.i_orig = 1;
-  opacset<R>(m, dv, p, p.nub, a.rstar_cm);
+  opacset<R>(m, dv, p, p.nub, a);
   const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
   p.z = (double)p.cosb;
   const double rp_ = (double)p.sinb;
@@ -1301,6 +1623,8 @@ __device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTall
   const int idust2 = f.idust2;
   L.c[HC3D_CNT_EVENTS]++;
   f.ntot++;
+  // issued before the albedo test so that its latency overlaps the draw
+  const double tave = __ldg(m.tdust + 4 * c + idust2);
   if (ran<R>(rng) <= p.albedo[idust2]) {  // scattered
     f.iflag = 1; f.iscat++; f.iint++;
     make_rec<R>(rec, p, a, 1, idust2);
@@ -1310,7 +1634,6 @@ __device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTall
     atomicAdd(t.dbig + c, 1u);
     p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
     atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
-    const double tave = __ldg(m.tdust + 4 * c + idust2);
     p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
     p.cost = R(1) - R(2) * ran<R>(rng);
     p.sint = xsqrt(R(1) - p.cost * p.cost);
@@ -1319,7 +1642,7 @@ __device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTall
     p.sinp = xsin(p.phi);
     p.nub = lucydustfreq<R>(m, tave, idust2, rng);
     f.iflag = 0;
-    opacset<R>(m, dv, p, p.nub, a.rstar_cm);
+    opacset<R>(m, dv, p, p.nub, a);
     make_rec<R>(rec, p, a, 0, idust2);
     f.iint++;
     tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
@@ -1341,16 +1664,14 @@ __device__ void run_packet(const DevModel& m, const DustView<R>& dv, const DevTa
   Pkt<R> p;
   PeelRec<R> rec;
   emit<R>(m, dv, a, p, rng, rec, tr);
-  if (a.ipeel == 1)
-    for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
+  if (a.ipeel == 1) peel_all<R>(m, t, d, a, rec, L);
   Flow f;
   f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
   f.iflag = 0; f.iscat = 0; f.iint = 0; f.idust2 = 0; f.ntot = 0;
   int st = walk<R>(m, t, d, a, p, rng, f, L, tr, true);
   while (st == ST_INTERACT) {
     interact<R>(m, dv, t, a, p, rng, f, L, tr, rec);
-    if (a.ipeel == 1)
-      for (int k = 0; k < a.npeel; ++k) peel_ray<R>(m, t, d, a, rec, k, L);
+    if (a.ipeel == 1) peel_all<R>(m, t, d, a, rec, L);
     st = walk<R>(m, t, d, a, p, rng, f, L, tr, false);
   }
 }
@@ -1410,7 +1731,6 @@ template <class R>
 __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDims d, RunArgs a, Slot<R>* pool,
                                                PeelRec<R>* queue, unsigned long long* qcount, int E,
                                                unsigned int* alive) {
-  namespace cg = cooperative_groups;
   extern __shared__ double dust_smem[];
   DustView<R> dv;
   dust_view<R>(m, reinterpret_cast<R*>(dust_smem), dv);
@@ -1442,14 +1762,13 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     } else {
       interact<R>(m, dv, t, a, s.p, rng, s.f, L, tr, rec);
     }
-    if (a.ipeel) {
-      cg::coalesced_group g = cg::coalesced_threads();
-      unsigned long long base = 0;
-      if (g.thread_rank() == 0) base = atomicAdd(qcount, (unsigned long long)g.size());
-      base = g.shfl(base, 0);
-      queue[base + g.thread_rank()] = rec;
-    }
+    // The queue slot of this event's record, reserved before the walk and
+    // written after it, so that the atomic's round trip overlaps the walk
+    // (a per-thread atomic: no lane waits for the walks of the others).
+    unsigned long long slot = 0;
+    if (a.ipeel) slot = atomicAdd(qcount, 1ull);
     const int st = walk<R>(m, t, d, a, s.p, rng, s.f, L, tr, s.stage == 2);
+    if (a.ipeel) queue[slot] = rec;
     s.stage = st == ST_INTERACT ? 1 : 0;
   }
   s.c0 = rng.c0;
@@ -1476,6 +1795,93 @@ __global__ void __launch_bounds__(256, 3) k_peel(DevModel m, DevTallies t, Tally
     const unsigned long long e = i / (unsigned)a.npeel;
     const int k = (int)(i - e * (unsigned)a.npeel);
     peel_ray<R>(m, t, d, a, queue[e], k, L);
+  }
+  flush(t, L);
+}
+
+
+template <class R>
+__global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+                                                                  const PeelRec<R>* queue,
+                                                                  const unsigned long long* qcount,
+                                                                  unsigned long long* next_ray) {
+  static_assert(sizeof(R) == 4, "the warp-synchronous ray pool is the mixed form");
+  __shared__ PeelDir dirs[kMaxPeel];
+  __shared__ PeelEsc esc[kPeelThreads / 32][kPeelBuf];
+  for (int k = threadIdx.x; k < a.npeel; k += blockDim.x) dirs[k] = peel_dir(a, k);
+  __syncthreads();
+  Local L;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) L.c[i] = 0;
+  L.fault = 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  PeelEsc* buf = esc[warp];
+  const unsigned npeel = (unsigned)a.npeel;
+  const unsigned long long n = *qcount * (unsigned long long)npeel;
+  const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
+  int nbuf = 0;
+  bool have = false, more = n > 0;
+  unsigned long long rbase = 0, rend = 0;  // rays reserved by this warp, not yet started
+  unsigned long long e = 0;                // the ray of this lane: event e, direction k
+  int k = 0;
+  PeelWalk w;
+  for (;;) {
+    if (more || rbase < rend) {
+      const unsigned need = __ballot_sync(0xffffffffu, !have);
+      if (need) {
+        if (rbase >= rend) {  // reserve the next chunk of rays for this warp
+          unsigned long long b = 0;
+          if (lane == 0) b = atomicAdd(next_ray, (unsigned long long)kPeelChunk);
+          b = __shfl_sync(0xffffffffu, b, 0);
+          if (b >= n) {
+            more = false;
+          } else {
+            rbase = b;
+            rend = b + kPeelChunk < n ? b + kPeelChunk : n;
+            if (rend >= n) more = false;
+          }
+        }
+        const unsigned long long avail = rend - rbase;
+        const unsigned long long i = rbase + (unsigned long long)__popc(need & lt);
+        rbase += (unsigned long long)__popc(need) < avail ? (unsigned long long)__popc(need) : avail;
+        if (!have && i < rend) {
+          e = i / npeel;
+          k = (int)(i - e * npeel);
+          have = w.start(m, queue[e], dirs[k]);
+          if (have) L.c[HC3D_CNT_PEELS]++;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have) && !more && rbase >= rend) break;
+    bool out = false;
+    if (have) {
+      const int st = w.step(m, cap, L);
+      out = st == PeelWalk::OUT;
+      if (st != PeelWalk::GOING) have = false;
+    }
+    // park the rays that left the grid; tally them 32 at a time
+    const unsigned outm = __ballot_sync(0xffffffffu, out);
+    if (out) {
+      PeelEsc& q = buf[nbuf + __popc(outm & lt)];
+      q.e = e; q.k = k; q.tsum = (float)w.tsum;
+      w.end_point(q.xf, q.yf, q.zf);
+    }
+    nbuf += __popc(outm);
+    if (nbuf >= 32) {
+      __syncwarp();
+      const PeelEsc q = buf[lane];
+      peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
+      __syncwarp();
+      if (lane < nbuf - 32) buf[lane] = buf[lane + 32];
+      __syncwarp();
+      nbuf -= 32;
+    }
+  }
+  __syncwarp();
+  for (int j = lane; j < nbuf; j += 32) {
+    const PeelEsc q = buf[j];
+    peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
   }
   flush(t, L);
 }
