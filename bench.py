@@ -211,6 +211,9 @@ def main():
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
     ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison run")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run one untimed peeled step after the Lucy set-up and print its crossing and launch "
+                         "counts (the command a DRAM-traffic capture of k_wave / k_peel_mixed runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -252,6 +255,18 @@ def main():
                 return T, td_
             ctx.lucy_update(model.info.ltot, np_, want_tdust=False)
             return None
+
+        if args.profile_step:
+            n = args.packets
+            step(n, 300, 0)
+            c = ctx.tallies(model.run_params(np=n, ipeel=1), grid=False)["counters"]
+            waves = ctx.last_launch_stats()[0] // 2
+            print(json.dumps({"workload": args.workload, "packets": n,
+                              "crossings": {"prop": int(c[hc3d.CNT["cross_prop"]]),
+                                            "peel": int(c[hc3d.CNT["cross_peel"]])},
+                              "launches": {"k_wave<float>": waves, "k_peel_mixed<float>": waves}}))
+            ctx.close()
+            return
 
         # calibrate the batch so one step takes about --step-seconds
         n = args.packets

@@ -29,6 +29,7 @@ struct hc3d_ctx {
   double* d_kappap = nullptr;  // (nT, kSlots)
   double* d_massarr = nullptr; // (ncell*4)
   double* d_tdust = nullptr;   // (ncell*4), also dm.tdust
+  float* d_tdustf = nullptr;   // (ncell*4) FP32 copy, also dm.tdustf
   unsigned char* d_peelmask = nullptr;
   int ndg_in = 0;
   // tallies
@@ -48,7 +49,7 @@ struct hc3d_ctx {
   cudaEvent_t wev[3] = {nullptr, nullptr, nullptr};
   double last_ms = 0.0, last_transport_ms = 0.0, last_peel_ms = 0.0;
   int last_launches = 0;
-  std::vector<double> wave_log;  // per wave: E, active, alive after, transport ms, peel ms
+  std::vector<double> wave_log;  // per wave: E, active, alive after, transport ms, peel ms, events
   // wavefront form
   std::vector<void*> wave_allocs;
   WaveBufs wave{};
@@ -120,7 +121,7 @@ __device__ double dusttemp_dev(const LucyArgs& a, double na, double T0, int s, d
 }
 
 __global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const double* rho4d, const double* massarr,
-                       double* tdust, unsigned char* peelmask, unsigned long long* maxrel) {
+                       double* tdust, float* tdustf, unsigned char* peelmask, unsigned long long* maxrel) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.ncell; c += (int64_t)gridDim.x * blockDim.x) {
     unsigned mask = 0;
     for (int s = 0; s < kSlots; ++s) {
@@ -134,6 +135,7 @@ __global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const doub
         }
         T = Td;
         tdust[4 * c + s] = Td;
+        tdustf[4 * c + s] = (float)Td;
       }
       if (T < a.tsub / 11605.0) mask |= 1u << s;
     }
@@ -305,7 +307,9 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
   CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
   LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->stream};
   int64_t alive_prev = 0;
-  unsigned long long work = 0;
+  unsigned long long work = 0, events_prev = 0;
+  CK(cudaMemcpyAsync(&events_prev, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events_prev), cudaMemcpyDeviceToHost,
+                     c->stream));
   c->last_transport_ms = c->last_peel_ms = 0.0;
   c->last_launches = 0;
   c->wave_log.clear();
@@ -321,8 +325,11 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
                         : launch_wave_mixed(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev);
     if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("wave launch: ") + cudaGetErrorString(e));
     unsigned int alive = 0;
+    unsigned long long events = 0;
     CK(cudaMemcpyAsync(&alive, c->wave.alive, sizeof(alive), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&work, c->d_work, sizeof(work), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&events, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events), cudaMemcpyDeviceToHost,
+                       c->stream));
     CK(cudaStreamSynchronize(c->stream));
     float t0 = 0.f, t1 = 0.f;
     CK(cudaEventElapsedTime(&t0, c->wev[0], c->wev[1]));
@@ -330,7 +337,9 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     c->last_transport_ms += t0;
     c->last_peel_ms += t1;
     c->last_launches += 2;
-    c->wave_log.insert(c->wave_log.end(), {(double)E, (double)active, (double)alive, (double)t0, (double)t1});
+    c->wave_log.insert(c->wave_log.end(),
+                       {(double)E, (double)active, (double)alive, (double)t0, (double)t1, (double)(events - events_prev)});
+    events_prev = events;
     alive_prev = alive;
     if (alive == 0 && work >= (unsigned long long)p->np) break;
   }
@@ -530,6 +539,33 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
     c->dm.lTintf = fp[5]; c->dm.nuintf = fp[6]; c->dm.kapBintf = fp[7]; c->dm.hnuintf = fp[8];
     c->dm.atmosnuf = fp[9]; c->dm.lognuf = fp[10]; c->dm.loghnuf = fp[11];
   }
+  // dust-table guide of the mixed form (see DevModel), on the FP32 tables
+  {
+    const size_t L = (size_t)t->nlammax;
+    std::vector<short2> dg((size_t)kSlots * kDustGuide, make_short2(1, 1));
+    for (int u = 0; u < c->dm.ntab; ++u) {
+      const int nl = c->dm.tab_nl[u];
+      std::vector<float> f(nl);
+      for (int i = 0; i < nl; ++i) f[i] = (float)nud[(size_t)u * L + i];
+      // i0(nu): the last row (1-based) with f[i-1] >= nu, for f[nl-1] < nu < f[0]
+      auto i0 = [&](double nu) {
+        int k = 1;
+        while (k < nl - 1 && (double)f[k] >= nu) ++k;
+        return k;
+      };
+      const double lo = std::log((double)f[nl - 1]), hi = std::log((double)f[0]);
+      const double w = (hi - lo) / kDustGuide;
+      for (int b = 0; b < kDustGuide; ++b) {
+        const int a = i0(std::exp(lo + (b + 1) * w)), z = i0(std::exp(lo + b * w));
+        dg[(size_t)u * kDustGuide + b] = make_short2((short)std::max(1, a - 1), (short)std::min(nl - 1, z + 1));
+      }
+      c->dm.dlnlo[u] = (float)lo;
+      c->dm.dginv[u] = (float)(kDustGuide / (hi - lo));
+    }
+    short2* d_dg = nullptr;
+    if ((r = dupload(c, own, &d_dg, dg.data(), dg.size()))) return r;
+    c->dm.dguide = d_dg;
+  }
   // Lucy CDF of the mixed form: row pairs interleaved per frequency, and the
   // guide of index brackets per probability level (see DevModel)
   {
@@ -645,6 +681,10 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       (r = dupload(c, own, &d_rd, rd.data(), rd.size())) || (r = dupload(c, own, &c->d_tdust, td.data(), td.size())) ||
       (r = dupload(c, own, &c->d_massarr, ma.data(), ma.size())) || (r = dalloc(c, own, &c->d_peelmask, (size_t)ncell)))
     return r;
+  {
+    const std::vector<float> tdf(td.begin(), td.end());
+    if ((r = dupload(c, own, &c->d_tdustf, tdf.data(), tdf.size()))) return r;
+  }
   DevTallies& t = c->dt;
   if ((r = dalloc(c, own, &t.nabs, (size_t)kSlots * ncell)) || (r = dalloc(c, own, &t.dtauabs, (size_t)kSlots * ncell)) ||
       (r = dalloc(c, own, &t.jmean, (size_t)ncell)) || (r = dalloc(c, own, &t.killed, (size_t)ncell)) ||
@@ -661,9 +701,14 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       return r;
     m.rarrf = d_rarrf;
     m.r2arrf = d_r2arrf;
+    std::vector<float2> cs(ntg);
+    for (int i = 0; i < ntg; ++i) cs[i] = make_float2((float)std::cos(g->thetarr[i]), (float)std::sin(g->thetarr[i]));
+    float2* d_cs = nullptr;
+    if ((r = dupload(c, own, &d_cs, cs.data(), cs.size()))) return r;
+    m.thcs = d_cs;
   }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
-  m.peelmask = c->d_peelmask; m.tdust = c->d_tdust;
+  m.peelmask = c->d_peelmask; m.tdust = c->d_tdust; m.tdustf = c->d_tdustf;
   c->ndg_in = g->ndg;
   k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask);
   CK(cudaGetLastError());
@@ -761,9 +806,9 @@ extern "C" int hc3d_get_fault_log(hc3d_ctx* c, uint64_t* entries, int max, int* 
 
 extern "C" int hc3d_get_wave_log(hc3d_ctx* c, double* out, int max_waves, int* n) {
   if (!c || !n) return HC3D_ERR_INVALID;
-  *n = (int)(c->wave_log.size() / 5);
+  *n = (int)(c->wave_log.size() / 6);
   if (out)
-    std::copy(c->wave_log.begin(), c->wave_log.begin() + 5 * std::min(*n, std::max(max_waves, 0)), out);
+    std::copy(c->wave_log.begin(), c->wave_log.begin() + 6 * std::min(*n, std::max(max_waves, 0)), out);
   return HC3D_OK;
 }
 
@@ -870,7 +915,7 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
   a.na_min = 1.0e4;
   a.nslots = std::min(c->ndg_in, kSlots);
   CK(cudaMemsetAsync(c->d_maxrel, 0, sizeof(unsigned long long), c->stream));
-  k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust,
+  k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust, c->d_tdustf,
                                                            c->d_peelmask, c->d_maxrel);
   CK(cudaGetLastError());
   unsigned long long bits = 0;

@@ -13,7 +13,8 @@ constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2
 constexpr int kNo = 8;      // SED components (output.F90:232-239)
 constexpr int kMaxPeel = 256;
 constexpr int kFaultLog = 256;
-constexpr int kGuide = 64;  // probability levels of the Lucy-CDF guide table
+constexpr int kGuide = 64;      // probability levels of the Lucy-CDF guide table
+constexpr int kDustGuide = 64;  // ln(nu) buckets of the dust-table guide
 
 // Fortran-layout sizes of the tally arrays of one run configuration.
 struct TallyDims {
@@ -54,12 +55,14 @@ struct DevModel {
   const double* tan2d;    // (ntg)
   const float* tan2f;     // (ntg)
   const float* hemi;      // (ntg) +1 upper, -1 lower (cone nappe)
+  const float2* thcs;     // (ntg) cos, sin of the polar walls (mixed-form safe distance)
   const double* aarrd; const double* barrd;  // (npg)
   const float* aarrf; const float* barrf;    // (npg)
   const float4* rho4f;    // (ncell) species slots x,y,z,w  (mixed form)
   const double* rho4d;    // (ncell*4)                     (FP64 form)
   const unsigned char* peelmask;  // (ncell) bit s: tdust(s) < Tsub
   const double* tdust;    // (ncell*4) K/11605
+  const float* tdustf;    // (ncell*4) FP32 copy (mixed form)
   // dust tables
   int nlammax;
   int nlambda[kSlots];
@@ -82,6 +85,10 @@ struct DevModel {
   // frequency index where the interpolated CDF of rows j, j+1 crosses a level in [b, b+1)/kGuide
   const float2* kpairf;
   const short2* kguide;
+  // dust-table guide of the mixed form: dguide[u*kDustGuide + b] = (lo, hi) brackets the row i0 of
+  // table u (nud(i0) >= nu > nud(i0+1)) for ln(nu) in bucket b of [dlnlo[u], dlnlo[u] + kDustGuide/dginv[u])
+  const short2* dguide;
+  float dlnlo[kSlots], dginv[kSlots];
 };
 
 // One call of the packet loop.

@@ -84,13 +84,20 @@ __device__ __forceinline__ void rng_init(Rng& r, uint32_t key0, uint32_t key1, u
   r.left = 0; r.inj = nullptr; r.ninj = 0; r.pos = 0;
 }
 
+// a[i] of a four-element array by selects, so that the array stays in
+// registers (a runtime index would place it in local memory)
+template <class T>
+__device__ __forceinline__ T pick4(const T (&a)[4], int i) {
+  return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
+
 __device__ __forceinline__ uint32_t next_u32(Rng& r) {
   if (r.left == 0) {
     philox(r.c0, 0u, r.c2, r.c3, r.k0, r.k1, r.b);
     r.c0++;
     r.left = 4;
   }
-  uint32_t u = r.b[4 - r.left];
+  uint32_t u = pick4(r.b, 4 - r.left);
   r.left--;
   return u;
 }
@@ -106,24 +113,67 @@ template <> __device__ __forceinline__ float ran<float>(Rng& r) {
 }
 
 // ---- packet state: the tts_mod/stokesvar_mod globals of one packet ------------
+// Positions: FP64 in the FP64 form.  The mixed form carries each coordinate
+// as an unevaluated FP32 pair hi + lo (about 44 significant bits), advanced
+// with error-free FP32 transformations, so no FP64 instruction -- 64 cycles
+// of latency each on this GPU -- sits on the per-event critical path.
+struct Pos2 {
+  float hi, lo;
+};
+template <class R> struct PosOf { using T = double; };
+template <> struct PosOf<float> { using T = Pos2; };
+__device__ __forceinline__ double dval(double v) { return v; }
+__device__ __forceinline__ double dval(const Pos2& v) { return (double)v.hi + (double)v.lo; }
+__device__ __forceinline__ void set_pos(double& d, double v) { d = v; }
+__device__ __forceinline__ void set_pos(Pos2& d, double v) {
+  d.hi = (float)v;
+  d.lo = (float)(v - (double)d.hi);
+}
+
+// Lucy CDF rows of one cell and species slot (mixed form, lucy_freq_mixed)
+struct LucyRow {
+  int key;  // 4 * cell + slot; -1 = empty
+  int pr;   // row pair: slot * (nT - 1) + j - 1
+  float T0, f, P0, P1;
+};
+
 template <class R>
 struct Pkt {
-  double x, y, z;
+  typename PosOf<R>::T x, y, z;
   R ux, uy, uz;
   R cost, sint, cosp, sinp, phi;
   R sip, sqp, sup, svp;
-  double nub;
+  R nub;
   R cosb, sinb, lp;
   int ir, it, ip;
   int on_wall;
   int i_orig;
   R kapd[kSlots], albedo[kSlots], g[kSlots], pl[kSlots];
+  float safe;  // mixed form: a step shorter than this from here stays in the cell (0 = unknown)
+  LucyRow lrow;  // mixed form: cached Lucy CDF rows of the current cell
 };
 
-// per-thread counters, flushed once per thread
+// Event counters (HC3D_CNT_*) of a thread and its last fault code.  The
+// counters live in the block's shared memory, so they take no registers on
+// the packet's chain of events; local_init() clears them, flush() adds them
+// to the device counters once per block.  The peel-off walks count in
+// registers instead (PeelCount): their crossings would make every lane hit
+// the same shared counter.
 struct Local {
-  unsigned long long c[16];
+  unsigned long long* sc;  // the block's 16 counters
   int fault;
+  __device__ __forceinline__ void add(int k, unsigned long long v = 1ull) const { atomicAdd(sc + k, v); }
+};
+
+__device__ __forceinline__ void local_init(Local& L, unsigned long long* sc) {
+  if (threadIdx.x < 16) sc[threadIdx.x] = 0ull;
+  __syncthreads();
+  L.sc = sc;
+  L.fault = 0;
+}
+
+struct PeelCount {
+  unsigned peels, cross, stuck;
 };
 
 // trace record (hc3d_trace_rec of hc3d.h)
@@ -272,24 +322,25 @@ __device__ __forceinline__ double path_f64(const PathLen& s) { return (double)s.
 
 struct Ray {
   float x0, y0, z0, ux, uy, uz;  // FP32 start point and direction
-  double xd, yd, zd;             // FP64 start point
+  Pos2 xs, ys, zs;               // the start point as pairs
   double rr0, hb0, u2;           // FP64 |x0|^2, x0.u, |u|^2 once `dbl` is set
   bool dbl;
 };
 
-__device__ __forceinline__ void ray_init(Ray& r, double x, double y, double z, float xf, float yf, float zf, float ux,
-                                         float uy, float uz) {
-  r.x0 = xf; r.y0 = yf; r.z0 = zf;
+__device__ __forceinline__ void ray_init(Ray& r, const Pos2& x, const Pos2& y, const Pos2& z, float ux, float uy,
+                                         float uz) {
+  r.x0 = x.hi; r.y0 = y.hi; r.z0 = z.hi;
   r.ux = ux; r.uy = uy; r.uz = uz;
-  r.xd = x; r.yd = y; r.zd = z;
+  r.xs = x; r.ys = y; r.zs = z;
   r.dbl = false;
 }
 
 __device__ __forceinline__ void ray_f64(Ray& r) {
   if (r.dbl) return;
   const double uxd = r.ux, uyd = r.uy, uzd = r.uz;
-  r.rr0 = r.xd * r.xd + r.yd * r.yd + r.zd * r.zd;
-  r.hb0 = r.xd * uxd + r.yd * uyd + r.zd * uzd;
+  const double x = dval(r.xs), y = dval(r.ys), z = dval(r.zs);
+  r.rr0 = x * x + y * y + z * z;
+  r.hb0 = x * uxd + y * uyd + z * uzd;
   r.u2 = uxd * uxd + uyd * uyd + uzd * uzd;
   r.dbl = true;
 }
@@ -297,9 +348,27 @@ __device__ __forceinline__ void ray_f64(Ray& r) {
 // FP64 point of the ray at path length S
 __device__ __forceinline__ void ray_at(const Ray& r, const PathLen& S, double& x, double& y, double& z) {
   const double s = path_f64(S);
-  x = fma(s, (double)r.ux, r.xd);
-  y = fma(s, (double)r.uy, r.yd);
-  z = fma(s, (double)r.uz, r.zd);
+  x = fma(s, (double)r.ux, dval(r.xs));
+  y = fma(s, (double)r.uy, dval(r.ys));
+  z = fma(s, (double)r.uz, dval(r.zs));
+}
+
+// x + S u as a pair: x a pair, S a pair, u FP32 (error-free product and sum)
+__device__ __forceinline__ Pos2 pos_step(const Pos2& x, const PathLen& S, float u) {
+  const float pr = S.hi * u;
+  const float pe = fmaf(S.hi, u, -pr) + S.lo * u;
+  const float sm = x.hi + pr;
+  const float bp = sm - x.hi;
+  const float e = ((x.hi - (sm - bp)) + (pr - bp)) + (x.lo + pe);
+  const float hi = sm + e;
+  return Pos2{hi, e - (hi - sm)};
+}
+
+// the point of the ray at path length S, as pairs
+__device__ __forceinline__ void ray_pos(const Ray& r, const PathLen& S, Pos2& x, Pos2& y, Pos2& z) {
+  x = pos_step(r.xs, S, r.ux);
+  y = pos_step(r.ys, S, r.uy);
+  z = pos_step(r.zs, S, r.uz);
 }
 
 // A sphere root from FP32 |x|^2 - R^2 is exact enough unless the point lies
@@ -476,7 +545,10 @@ __device__ __forceinline__ void dust_view(const DevModel& m, R* smem, DustView<R
   const R* gg = tab<R>(m.gdust, m.gdustf);
   const R* pl = tab<R>(m.pldust, m.pldustf);
   size_t off = 0;
-  for (int u = 0; u < m.ntab; ++u) {
+#pragma unroll
+  for (int u = 0; u < kSlots; ++u) {  // unrolled: the view's pointers stay in registers
+    v.nud[u] = v.kap[u] = v.alb[u] = v.g[u] = v.pl[u] = nullptr;
+    if (u >= m.ntab) continue;
     const int nl = m.tab_nl[u];
     const size_t go = (size_t)u * m.nlammax;
     if (m.dust_smem > 0) {
@@ -502,8 +574,55 @@ __device__ __forceinline__ void dust_view(const DevModel& m, R* smem, DustView<R
 // the result (only kappa_V differs), which is what the per-slot loop of the
 // reference computes for them.
 template <class R>
-__device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, double nu_in, const RunArgs& a) {
-  const R nu = (R)nu_in;
+__device__ __forceinline__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, R nu, const RunArgs& a) {
+  if constexpr (sizeof(R) == 4) {
+    // mixed form: the same bracket from the ln(nu) guide of each table, then
+    // a short bisection inside it; values kept in registers
+    const float lnu = logf(nu);
+    float gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
+#pragma unroll
+    for (int u = 0; u < kSlots; ++u) {
+      gt[u] = plt[u] = kt[u] = at[u] = 0.f;
+      if (u >= m.ntab) continue;
+      const int nl = m.tab_nl[u];
+      const float* nud = v.nud[u];
+      int i0 = 1, i1 = nl;
+      if (nu >= nud[0]) {
+        i0 = i1 = 1;
+      } else if (nu <= nud[nl - 1]) {
+        i0 = i1 = nl;
+      } else {
+        const int b = min(max((int)((lnu - m.dlnlo[u]) * m.dginv[u]), 0), kDustGuide - 1);
+        const short2 gb = __ldg(m.dguide + u * kDustGuide + b);
+        if (nud[gb.x - 1] >= nu && nu > nud[gb.y]) { i0 = gb.x; i1 = gb.y + 1; }
+        while (i1 - i0 > 1) {
+          const int i = (i1 + i0) / 2;
+          if (nu <= nud[i - 1]) i0 = i; else i1 = i;
+        }
+      }
+      if (i0 == i1) {
+        gt[u] = v.g[u][i0 - 1]; plt[u] = v.pl[u][i0 - 1]; kt[u] = v.kap[u][i0 - 1]; at[u] = v.alb[u][i0 - 1];
+      } else {
+        const float n1 = nud[i1 - 1], n0 = nud[i0 - 1];
+        const float f = (nu - n1) / (n0 - n1), fm1 = 1.f - f;
+        gt[u] = fm1 * v.g[u][i1 - 1] + f * v.g[u][i0 - 1];
+        plt[u] = fm1 * v.pl[u][i1 - 1] + f * v.pl[u][i0 - 1];
+        kt[u] = fm1 * v.kap[u][i1 - 1] + f * v.kap[u][i0 - 1];
+        at[u] = fm1 * v.alb[u][i1 - 1] + f * v.alb[u][i0 - 1];
+      }
+    }
+#pragma unroll
+    for (int id = 0; id < kSlots; ++id) {
+      const int u = m.table_of[id];
+      float g_ = gt[0], pl_ = plt[0], k_ = kt[0], a_ = at[0];
+#pragma unroll
+      for (int q = 1; q < kSlots; ++q)
+        if (u == q) { g_ = gt[q]; pl_ = plt[q]; k_ = kt[q]; a_ = at[q]; }
+      p.g[id] = g_; p.pl[id] = pl_; p.albedo[id] = a_;
+      p.kapd[id] = k_ * a.kapfac[id];
+    }
+    return;
+  }
   R gt[kSlots], plt[kSlots], kt[kSlots], at[kSlots];
   for (int u = 0; u < m.ntab; ++u) {
     const int nl = m.tab_nl[u];
@@ -530,8 +649,7 @@ __device__ void opacset(const DevModel& m, const DustView<R>& v, Pkt<R>& p, doub
   for (int id = 0; id < kSlots; ++id) {
     const int u = m.table_of[id];
     p.g[id] = gt[u]; p.pl[id] = plt[u]; p.albedo[id] = at[u];
-    if constexpr (sizeof(R) == 4) p.kapd[id] = kt[u] * a.kapfac[id];
-    else p.kapd[id] = (R)((double)kt[u] * a.rstar_cm * m.kappav[id]);
+    p.kapd[id] = (R)((double)kt[u] * a.rstar_cm * m.kappav[id]);
   }
 }
 
@@ -592,19 +710,79 @@ __device__ __forceinline__ unsigned long long fxf(float v, float scale) {
   return (unsigned long long)f2ll(v * scale);
 }
 
+// A lower bound on the distance from a point inside cell (ir, it, ip) to
+// every wall of the cell: the spheres |r - R|, the cones r|sin(theta - theta_w)|
+// = |rho cos(theta_w) - z sin(theta_w)| (rho the cylindrical radius; the
+// midplane gives |z|, a pole is no wall) and the planes |A x + B y|, less a
+// margin for FP32 rounding of the point and of the walls.
+__device__ __forceinline__ float safe_dist(const DevModel& m, float x, float y, float z, int ir, int it, int ip) {
+  const float rc2 = x * x + y * y;
+  const float r = sqrtf(rc2 + z * z), rc = sqrtf(rc2);
+  float d = fminf(r - __ldg(m.rarrf + ir - 1), __ldg(m.rarrf + ir) - r);
+  if (m.ntg > 2) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (__ldg(m.tan2f + it - 1 + k) == 0.f) continue;
+      const float2 cs = __ldg(m.thcs + it - 1 + k);
+      d = fminf(d, fabsf(rc * cs.x - z * cs.y));
+    }
+    if (m.npg > 2) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+        d = fminf(d, fabsf(__ldg(m.aarrf + ip - 1 + k) * x + __ldg(m.barrf + ip - 1 + k) * y));
+    }
+  }
+  return d - 1.0e-6f * r;
+}
+
 // Mixed form of tauint: the step of one event is a Ray from the event point;
 // the walk, the tau integral and the Lucy tallies are FP32, the FP64 point
 // where the walk stops is formed once, at the end.
-static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<float>& p, float tau, Local& L,
+static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<float>& p, float tau, Local& L,
                                    Tracer& tr) {
   float tsum = 0.f;
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nreloc = 0, ntiny = 0;
   Ray ray;
-  ray_init(ray, p.x, p.y, p.z, (float)p.x, (float)p.y, (float)p.z, p.ux, p.uy, p.uz);
+  ray_init(ray, p.x, p.y, p.z, p.ux, p.uy, p.uz);
   PathLen S{0.f, 0.f};
   const float ps = (float)t.path_scale;
-  auto at = [&]() { ray_at(ray, S, p.x, p.y, p.z); };
+  if (p.on_wall == 0 && p.ir >= 1 && p.ir <= m.nrg - 1 && p.it >= 1 && p.it <= m.ntg - 1) {
+    // From a point inside the cell, a step shorter than the safe distance
+    // ends in the cell: the interaction the walk would find, without the
+    // wall search.  The safe distance holds for a ball around the point
+    // where it was formed; each such step uses up its length.
+    const int64_t c = cidx(m, p.ir, p.it, p.ip);
+    const Rho<float> rho = load_rho<float>(m, c);
+    float opac = 0.f;
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
+    const float ds = tau / opac;
+    if (opac > 0.f && !(ds < p.safe)) p.safe = safe_dist(m, p.x.hi, p.y.hi, p.z.hi, p.ir, p.it, p.ip);
+    if (opac > 0.f && ds < p.safe) {
+      p.safe -= ds;
+      L.add(HC3D_CNT_CROSS_PROP);
+#pragma unroll
+      for (int s = 0; s < kSlots; ++s)
+        if (rho.v[s] > 0.f)
+          atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fxf(p.kapd[s] * (1.f - p.albedo[s]) * rho.v[s] * ds, ps));
+      atomicAdd(t.jmean + c, fxf(ds / __ldg(m.rarrf + p.ir), ps));
+      path_add(S, ds);
+      ray_pos(ray, S, p.x, p.y, p.z);
+      tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, dval(p.x), dval(p.y), dval(p.z));
+      return TI_INTERACT;
+    }
+  }
+  p.safe = 0.f;
+  auto at = [&]() { ray_pos(ray, S, p.x, p.y, p.z); };
+  auto reloc = [&]() {
+    double x, y, z;
+    ray_at(ray, S, x, y, z);
+    int jr = p.ir, jt = p.it, jp = p.ip;
+    const int where = relocate(m, x, y, z, jr, jt, jp);
+    p.ir = jr; p.it = jt; p.ip = jp;
+    return where;
+  };
   for (int n = 0;; ++n) {
     if (n > cap || p.it < 1 || p.it > m.ntg - 1 || p.ir < 1 || p.ir > m.nrg - 1) {
       L.fault = n > cap ? F_CAP : F_RANGE;
@@ -617,7 +795,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
       at();
       if (nreloc < 4) {
         ++nreloc;
-        const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
+        const int where = reloc();
         if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
         if (where == 2) { p.ir = 0; return TI_STAR; }
         p.on_wall = 0;
@@ -633,7 +811,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
     for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
     const float dtau = opac * dt;
     const float rout = __ldg(m.rarrf + p.ir);
-    L.c[HC3D_CNT_CROSS_PROP]++;
+    L.add(HC3D_CNT_CROSS_PROP);
     const bool stop = tsum + dtau > tau;
     const float ds = stop ? (tau - tsum) / opac : dt;
 #pragma unroll
@@ -645,7 +823,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
       path_add(S, ds);
       at();
       p.on_wall = 0;
-      tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, p.x, p.y, p.z);
+      tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, dval(p.x), dval(p.y), dval(p.z));
       return TI_INTERACT;
     }
     tsum += dtau;
@@ -654,7 +832,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
     p.on_wall = 1 << own_after(iface);
     if (tr.recs) {
       at();
-      tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, p.x, p.y, p.z);
+      tr.add(1, p.ir, p.it, p.ip, iface, (double)tsum, dval(p.x), dval(p.y), dval(p.z));
     }
     if (p.ir == m.nrg) { at(); return TI_ESCAPE; }
     if (p.ir == 0) { at(); return TI_STAR; }
@@ -664,7 +842,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
       ++nreloc;
       ntiny = 0;
       at();
-      const int where = relocate(m, p.x, p.y, p.z, p.ir, p.it, p.ip);
+      const int where = reloc();
       if (where == 1) { p.ir = m.nrg; return TI_ESCAPE; }
       if (where == 2) { p.ir = 0; return TI_STAR; }
       p.on_wall = 0;
@@ -675,7 +853,7 @@ static __device__ int tauint_mixed(const DevModel& m, const DevTallies& t, Pkt<f
 // tauint in either form: the FP64 form walks with the reference's wall
 // machinery (closest_wall rule), the mixed form with tauint_mixed.
 template <class R>
-__device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
+__device__ __forceinline__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, Local& L, Tracer& tr) {
   if constexpr (sizeof(R) == 4) {
     return tauint_mixed(m, t, p, tau, L, tr);
   } else {
@@ -700,7 +878,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
       for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
       const R dtau = opac * dt;
       const double rout = __ldg(m.rarr + p.ir);
-      L.c[HC3D_CNT_CROSS_PROP]++;
+      L.add(HC3D_CNT_CROSS_PROP);
       if (tsum + dtau > tau) {
         const R ds = (tau - tsum) / opac;
         p.x += (double)ds * uxd;
@@ -739,7 +917,7 @@ __device__ int tauint(const DevModel& m, const DevTallies& t, Pkt<R>& p, R tau, 
 
 // ---- select_dust.f90:16-42 ---------------------------------------------------
 template <class R>
-__device__ int select_dust(const DevModel& m, const Pkt<R>& p, Rng& rng) {
+__device__ __forceinline__ int select_dust(const DevModel& m, const Pkt<R>& p, Rng& rng) {
   const R xran = ran<R>(rng);
   const Rho<R> rho = load_rho<R>(m, cidx(m, p.ir, p.it, p.ip));
   R opac = R(0), frac = R(0);
@@ -747,8 +925,11 @@ __device__ int select_dust(const DevModel& m, const Pkt<R>& p, Rng& rng) {
   for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
   if (opac == R(0)) return -1;
   int last = -1;
+  const R inv = R(1) / opac;  // mixed form: one division
+#pragma unroll
   for (int s = 0; s < kSlots; ++s) {
-    frac += p.kapd[s] * rho.v[s] / opac;
+    if constexpr (sizeof(R) == 4) frac += p.kapd[s] * rho.v[s] * inv;
+    else frac += p.kapd[s] * rho.v[s] / opac;
     if (p.kapd[s] * rho.v[s] > R(0)) last = s;
     if (xran <= frac + (R)(double)1.e-10f) return s;
   }
@@ -807,9 +988,9 @@ __device__ __forceinline__ void mueller(bool upper, R p1, R p2, R p3, R s2x, R c
 
 // ---- stokes.f90:46-388 --------------------------------------------------------------
 template <class R>
-__device__ void stokes(Pkt<R>& p, int id, Rng& rng) {
+__device__ __forceinline__ void stokes(Pkt<R>& p, int id, Rng& rng) {
   const R costp = p.cost, sintp = p.sint, phip = p.phi;
-  const R g = p.g[id], pl = p.pl[id];
+  const R g = pick4(p.g, id), pl = pick4(p.pl, id);
   R peak = peak_of<R>(g);
   R bmu, cosb2, sinbt, p1, p2, p3, rprob, ci, si_;
   bool upper;
@@ -921,7 +1102,7 @@ __device__ __forceinline__ void stokespeel(R g, R pl, R& sip, R& sqp, R& sup, R&
 // so they can run after the event, in any order and on any thread.
 template <class R>
 struct PeelRec {
-  double x, y, z;
+  typename PosOf<R>::T x, y, z;
   int ir, it, ip;
   int flags;  // bit0 on_wall, bit1 scattered, bits2-4 i_orig, bits5-6 idust2, bit7 stellar-surface emission,
               // bits8-10 id of the wall the event sits on
@@ -930,31 +1111,30 @@ struct PeelRec {
   R d0, d1, d2, d3, d4;  // scattered: cost, sint, phi, cosp, sinp of the incident packet; stellar: cosb, sinb, coslp, sinlp
   R g, pl;               // phase-matrix parameters of the scattering species
   R kapd[kSlots];
-  float xf, yf, zf;      // the event point in FP32 (mixed form)
 };
 
 template <class R>
-__device__ __forceinline__ int nu_bin(const RunArgs& a, double nub) {
+__device__ __forceinline__ int nu_bin(const RunArgs& a, R nub) {
   int inub;
   if constexpr (sizeof(R) == 4)
-    inub = (int)((float)a.nfreq * logf((float)nub / (float)a.numin) / (float)a.lnurat) + 1;
+    inub = (int)((float)a.nfreq * logf(nub / (float)a.numin) / (float)a.lnurat) + 1;
   else
     inub = (int)((double)a.nfreq * log(nub / a.numin) / a.lnurat) + 1;
   return inub < 1 ? 1 : (inub > a.nfreq ? a.nfreq : inub);
 }
 
 template <class R>
-__device__ __forceinline__ void make_rec(PeelRec<R>& e, const Pkt<R>& p, const RunArgs& a, int iflag, int idust2) {
+__device__ __forceinline__ void make_rec(PeelRec<R>& e, const Pkt<R>& p, const RunArgs& a, int iflag, int idust2,
+                                         int extra = 0) {
   e.x = p.x; e.y = p.y; e.z = p.z;
   e.ir = p.ir; e.it = p.it; e.ip = p.ip;
-  e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5) | (p.on_wall << 8);
+  e.flags = (p.on_wall ? 1 : 0) | (iflag << 1) | (p.i_orig << 2) | (idust2 << 5) | (p.on_wall << 8) | extra;
   e.inub = nu_bin<R>(a, p.nub);
   e.sip = p.sip; e.sqp = p.sqp; e.sup = p.sup; e.svp = p.svp;
   e.d0 = p.cost; e.d1 = p.sint; e.d2 = p.phi; e.d3 = p.cosp; e.d4 = p.sinp;
-  e.g = p.g[idust2]; e.pl = p.pl[idust2];
+  e.g = pick4(p.g, idust2); e.pl = pick4(p.pl, idust2);
 #pragma unroll
   for (int s = 0; s < kSlots; ++s) e.kapd[s] = p.kapd[s];
-  e.xf = (float)p.x; e.yf = (float)p.y; e.zf = (float)p.z;
 }
 
 __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, int64_t b, double i, double q, double u,
@@ -1005,7 +1185,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   int ir = e.ir, it = e.it, ip = e.ip;
   int on_wall = (flags >> 8) & 127;
   const R ux1 = sinte * cospe, uy1 = sinte * sinpe, uz1 = coste;
-  L.c[HC3D_CNT_PEELS]++;
+  L.add(HC3D_CNT_PEELS);
   if (on_wall) {
     const double rsq1 = xp1 * xp1 + yp1 * yp1 + zp1 * zp1;
     const bool outwards = (double)ux1 * xp1 + (double)uy1 * yp1 + (double)uz1 * zp1 > 0.0;
@@ -1025,13 +1205,13 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   const double uxd = (double)ux1, uyd = (double)uy1, uzd = (double)uz1;
   for (int n = 0;; ++n) {
     if (n > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
-      L.c[HC3D_CNT_PEEL_STUCK]++;
+      L.add(HC3D_CNT_PEEL_STUCK);
       return;
     }
     R dt;
     int iface;
     if (!next_wall<R>(m, ux1, uy1, uz1, xp1, yp1, zp1, ir, it, ip, on_wall, dt, iface)) {
-      L.c[HC3D_CNT_PEEL_STUCK]++;
+      L.add(HC3D_CNT_PEEL_STUCK);
       return;
     }
     const int64_t c = cidx(m, ir, it, ip);
@@ -1042,7 +1222,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     for (int s = 0; s < kSlots; ++s)
       if (mask & (1u << s)) opac += e.kapd[s] * rho.v[s];
     tsum += (double)(opac * dt);
-    L.c[HC3D_CNT_CROSS_PEEL]++;
+    L.add(HC3D_CNT_CROSS_PEEL);
     if (tsum > kTauMax) return;
     step_index(m.npg, iface, ir, it, ip);
     xp1 += (double)dt * uxd;
@@ -1173,7 +1353,7 @@ struct PeelWalk {
       const float cosnorm = r.d0 * dd.coste + (r.d1 * dd.sinte * (dd.cospe * r.d2 + dd.sinpe * r.d3));
       if (!(cosnorm > 0.f)) return false;
     }
-    ray_init(ray, r.x, r.y, r.z, r.xf, r.yf, r.zf, dd.ux, dd.uy, dd.uz);
+    ray_init(ray, r.x, r.y, r.z, dd.ux, dd.uy, dd.uz);
     ir = r.ir; it = r.it; ip = r.ip;
     on_wall = (flags >> 8) & 127;
     bool go = true;
@@ -1202,9 +1382,9 @@ struct PeelWalk {
 
   enum { GOING = 0, OUT = 1, ENDED = 2 };  // OUT: left the grid, to be tallied
 
-  __device__ __forceinline__ int step(const DevModel& m, int cap, Local& L) {
+  __device__ __forceinline__ int step(const DevModel& m, int cap, PeelCount& pc) {
     if (nstep > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
-      L.c[HC3D_CNT_PEEL_STUCK]++;
+      pc.stuck++;
       return ENDED;
     }
     ++nstep;
@@ -1215,7 +1395,7 @@ struct PeelWalk {
         ++nreloc;
         return relocate_here(m);
       }
-      L.c[HC3D_CNT_PEEL_STUCK]++;
+      pc.stuck++;
       return ENDED;
     }
     const int64_t c = cidx(m, ir, it, ip);
@@ -1228,7 +1408,7 @@ struct PeelWalk {
     const float dtau = opac * dt;
     tsum += (double)dtau;
     tf += dtau;
-    L.c[HC3D_CNT_CROSS_PEEL]++;
+    pc.cross++;
     if (tf > (float)kTauMax) return ENDED;
     step_index(m.npg, iface, ir, it, ip);
     path_add(S, dt);
@@ -1281,11 +1461,14 @@ __device__ __forceinline__ void peel_ray_mixed(const DevModel& m, const DevTalli
   const PeelDir dd = peel_dir(a, k);
   PeelWalk w;
   if (!w.start(m, e, dd)) return;
-  L.c[HC3D_CNT_PEELS]++;
+  PeelCount pc{1u, 0u, 0u};
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int st;
-  while ((st = w.step(m, cap, L)) == PeelWalk::GOING) {
+  while ((st = w.step(m, cap, pc)) == PeelWalk::GOING) {
   }
+  L.add(HC3D_CNT_PEELS);
+  L.add(HC3D_CNT_CROSS_PEEL, pc.cross);
+  if (pc.stuck) L.add(HC3D_CNT_PEEL_STUCK, pc.stuck);
   if (st == PeelWalk::OUT) {
     float x, y, z;
     w.end_point(x, y, z);
@@ -1305,7 +1488,67 @@ __device__ __forceinline__ void peel_all(const DevModel& m, const DevTallies& t,
 }
 
 // ---- lucydustfreq.f90:19-157 -------------------------------------------------------------
-// R-typed: FP64 tables and arithmetic in the FP64 form, FP32 in the mixed one.
+// Mixed form.  The row pair j, j+1 of the Lucy CDF and the weight f follow
+// from the cell temperature, which is fixed during a run: they are cached in
+// the packet while it stays in the cell and species slot.  The frequency
+// index is the same bracket of the interpolated CDF as the reference's
+// bisection (the CDF is non-decreasing, so the bracket is unique), found
+// from the guide table and a short bisection over the interleaved rows.
+__device__ __forceinline__ float lucy_freq_mixed(const DevModel& m, LucyRow& lr, int64_t c, int id, Rng& rng) {
+  const int nT = m.nT, nnu = m.nnu;
+  const float* nuint = m.nuintf;
+  const int key = (int)(4 * c + id);
+  if (key != lr.key) {
+    const float T0 = __ldg(m.tdustf + 4 * c + id);
+    const float* lTint = m.lTintf;
+    const float lT0 = logf(T0);
+    const float l1 = __ldg(lTint), lN = __ldg(lTint + nT - 1);
+    int j = (int)((float)(nT - 1) * (lT0 - l1) / (lN - l1)) + 1;
+    j = j < 1 ? 1 : (j > nT - 1 ? nT - 1 : j);
+    float f = (lT0 - __ldg(lTint + j - 1)) / (__ldg(lTint + j) - __ldg(lTint + j - 1));
+    f = f < 0.f ? 0.f : (f > 1.f ? 1.f : f);
+    const int pr = id * (nT - 1) + (j - 1);
+    const float2 k1 = __ldg(m.kpairf + (size_t)pr * nnu), kn = __ldg(m.kpairf + (size_t)pr * nnu + nnu - 1);
+    lr.key = key;
+    lr.pr = pr;
+    lr.T0 = T0;
+    lr.f = f;
+    lr.P0 = fminf((1.f - f) * k1.x + f * k1.y, 1.f);
+    lr.P1 = fminf((1.f - f) * kn.x + f * kn.y, 1.f);
+  }
+  const float T0 = lr.T0, f = lr.f;
+  const float xi = ran<float>(rng);
+  float P0 = lr.P0, P1 = lr.P1;
+  if (xi < P0) return P0 > 0.f ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint);
+  if (xi >= P1) {
+    if (P1 < 1.f && xi < 1.f) return T0 * __ldg(nuint + nnu - 1) * (1.f - P1) / (1.f - xi);
+    return T0 * __ldg(nuint + nnu - 1);
+  }
+  const float2* KP = m.kpairf + (size_t)lr.pr * nnu;
+  auto P = [&](int i) { return fminf((1.f - f) * __ldg(KP + i - 1).x + f * __ldg(KP + i - 1).y, 1.f); };
+  const short2 g = __ldg(m.kguide + (size_t)lr.pr * kGuide + min((int)(xi * (float)kGuide), kGuide - 1));
+  int i0 = g.x, i1 = g.y;
+  const float Pa = P(i0), Pb = P(i1);
+  if (Pa <= xi) P0 = Pa; else i0 = 1;
+  if (Pb > xi) P1 = Pb; else i1 = nnu;
+  if (i1 <= i0) { i0 = 1; i1 = nnu; P0 = lr.P0; P1 = lr.P1; }
+  while (i1 - i0 > 1) {
+    const int i = (i0 + i1) / 2;
+    const float v = P(i);
+    if (v > xi) { i1 = i; P1 = v; }
+    else { i0 = i; P0 = v; }
+  }
+  float w;
+  if (xi < P0) w = 0.f;
+  else if (xi > P1) w = 1.f;
+  else if (P0 <= 0.f) w = 0.5f;
+  else if (P1 <= 0.f || xi <= 0.f) w = f;
+  else w = logf(xi / P0) / logf(P1 / P0);
+  const float n0 = __ldg(nuint + i0 - 1), n1 = __ldg(nuint + i1 - 1);
+  return T0 * n0 * powf(n1 / n0, w);
+}
+
+// FP64 form: the reference's bisection.
 template <class R> __device__ __forceinline__ R xpow(R a, R b);
 template <> __device__ __forceinline__ float xpow<float>(float a, float b) { return powf(a, b); }
 template <> __device__ __forceinline__ double xpow<double>(double a, double b) { return pow(a, b); }
@@ -1313,12 +1556,11 @@ __device__ __forceinline__ float xlog10(float x) { return log10f(x); }
 __device__ __forceinline__ double xlog10(double x) { return log10(x); }
 
 template <class R>
-__device__ double lucydustfreq(const DevModel& m, double T0in, int id, Rng& rng) {
+__device__ __forceinline__ R lucydustfreq(const DevModel& m, R T0, int id, Rng& rng) {
   const int nT = m.nT, nnu = m.nnu;
   const R* lTint = tab<R>(m.lTint, m.lTintf);
   const R* nuint = tab<R>(m.nuint, m.nuintf);
   const R* K = tab<R>(m.kapBint, m.kapBintf) + (size_t)id * nT * nnu;
-  const R T0 = (R)T0in;
   const R lT0 = xlog(T0);
   const R xi = ran<R>(rng);
   const R l1 = __ldg(lTint), lN = __ldg(lTint + nT - 1);
@@ -1326,53 +1568,15 @@ __device__ double lucydustfreq(const DevModel& m, double T0in, int id, Rng& rng)
   j = j < 1 ? 1 : (j > nT - 1 ? nT - 1 : j);
   R f = (lT0 - __ldg(lTint + j - 1)) / (__ldg(lTint + j) - __ldg(lTint + j - 1));
   f = f < R(0) ? R(0) : (f > R(1) ? R(1) : f);
-  if constexpr (sizeof(R) == 4) {
-    // mixed form: the same bracket of the interpolated CDF (it is
-    // non-decreasing, so the bracket is unique) from the guide table, then a
-    // short bisection over the interleaved rows j, j+1
-    const size_t pr = (size_t)id * (nT - 1) + (j - 1);
-    const float2* KP = m.kpairf + pr * nnu;
-    const short2 g = __ldg(m.kguide + pr * kGuide + min((int)(xi * (float)kGuide), kGuide - 1));
-    auto P = [&](int i) {
-      const float2 k = __ldg(KP + i - 1);
-      const float v = (1.f - f) * k.x + f * k.y;
-      return v > 1.f ? 1.f : v;
-    };
-    float P0 = P(1), P1 = P(nnu);
-    if (xi < P0) return (double)(P0 > 0.f ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint));
-    if (xi >= P1) {
-      if (P1 < 1.f && xi < 1.f) return (double)(T0 * __ldg(nuint + nnu - 1) * (1.f - P1) / (1.f - xi));
-      return (double)(T0 * __ldg(nuint + nnu - 1));
-    }
-    int i0 = g.x, i1 = g.y;
-    const float Pa = P(i0), Pb = P(i1);
-    if (Pa <= xi) P0 = Pa; else i0 = 1;
-    if (Pb > xi) P1 = Pb; else i1 = nnu;
-    if (i1 <= i0) { i0 = 1; i1 = nnu; P0 = P(1); P1 = P(nnu); }
-    while (i1 - i0 > 1) {
-      const int i = (i0 + i1) / 2;
-      const float v = P(i);
-      if (v > xi) { i1 = i; P1 = v; }
-      else { i0 = i; P0 = v; }
-    }
-    float w;
-    if (xi < P0) w = 0.f;
-    else if (xi > P1) w = 1.f;
-    else if (P0 <= 0.f) w = 0.5f;
-    else if (P1 <= 0.f || xi <= 0.f) w = f;
-    else w = logf(xi / P0) / logf(P1 / P0);
-    const float n0 = __ldg(nuint + i0 - 1), n1 = __ldg(nuint + i1 - 1);
-    return (double)(T0 * n0 * powf(n1 / n0, w));
-  }
 #define KB(jj, ii) __ldg(K + (size_t)((jj) - 1) + (size_t)nT * ((ii) - 1))
   int i0 = 1, i1 = nnu;
   R P0 = (R(1) - f) * KB(j, i0) + f * KB(j + 1, i0);
-  if (xi < P0) return (double)(P0 > R(0) ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint));
+  if (xi < P0) return (P0 > R(0) ? T0 * xi * __ldg(nuint) / P0 : T0 * __ldg(nuint));
   R P1 = (R(1) - f) * KB(j, i1) + f * KB(j + 1, i1);
   if (P1 > R(1)) P1 = R(1);
   if (xi >= P1) {
-    if (P1 < R(1) && xi < R(1)) return (double)(T0 * __ldg(nuint + nnu - 1) * (R(1) - P1) / (R(1) - xi));
-    return (double)(T0 * __ldg(nuint + nnu - 1));
+    if (P1 < R(1) && xi < R(1)) return (T0 * __ldg(nuint + nnu - 1) * (R(1) - P1) / (R(1) - xi));
+    return (T0 * __ldg(nuint + nnu - 1));
   }
   while (i1 - i0 > 1) {
     const int i = (i0 + i1) / 2;
@@ -1390,12 +1594,12 @@ __device__ double lucydustfreq(const DevModel& m, double T0in, int id, Rng& rng)
   else if (P1 <= R(0) || xi <= R(0)) { }
   else f = xlog(xi / P0) / xlog(P1 / P0);
   const R n0 = __ldg(nuint + i0 - 1), n1 = __ldg(nuint + i1 - 1);
-  return (double)(T0 * n0 * xpow<R>(n1 / n0, f));
+  return (T0 * n0 * xpow<R>(n1 / n0, f));
 }
 
 // ---- atmosfreq, starbarb.f90:120-156 ---------------------------------------------------
 template <class R>
-__device__ double atmosfreq(const DevModel& m, Rng& rng) {
+__device__ R atmosfreq(const DevModel& m, Rng& rng) {
   const R* hnuint = tab<R>(m.hnuint, m.hnuintf);
   const R* lognu = tab<R>(m.lognu, m.lognuf);
   const R* loghnu = tab<R>(m.loghnu, m.loghnuf);
@@ -1412,11 +1616,11 @@ __device__ double atmosfreq(const DevModel& m, Rng& rng) {
   if (i > 1) {
     const R l0 = __ldg(lognu + i - 1), l1 = __ldg(lognu + i);
     const R h0 = __ldg(loghnu + i - 1), h1 = __ldg(loghnu + i);
-    return (double)xpow<R>(R(10), l0 + (l1 - l0) * (xlog10(xi) - h0) / (h1 - h0));
+    return xpow<R>(R(10), l0 + (l1 - l0) * (xlog10(xi) - h0) / (h1 - h0));
   }
   const R a0 = __ldg(atmosnu + i - 1), a1 = __ldg(atmosnu + i);
   const R c0 = __ldg(hnuint + i - 1), c1 = __ldg(hnuint + i);
-  return (double)(a0 + (a1 - a0) * (xi - c0) / (c1 - c0));
+  return a0 + (a1 - a0) * (xi - c0) / (c1 - c0);
 }
 
 __device__ __forceinline__ int locate_dev(const double* xx, int n, double x) {
@@ -1448,10 +1652,10 @@ __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArg
   const double y = zpold * sini - ypold * u * sp - xpold * u * cp;
   const double rho2 = x * x + y * y;
   if (rho2 < __ldg(a.aperture2 + a.nap - 1) * 1.0001) {
-    L.c[HC3D_CNT_FLUX]++;
+    L.add(HC3D_CNT_FLUX);
     if (iflag == 1) {
-      L.c[HC3D_CNT_SFLUX]++;
-      L.c[HC3D_CNT_NSCAT] += (unsigned long long)iscat;
+      L.add(HC3D_CNT_SFLUX);
+      L.add(HC3D_CNT_NSCAT, (unsigned long long)iscat);
     }
   }
   const int inub = nu_bin<R>(a, p.nub);
@@ -1469,16 +1673,17 @@ __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArg
       }
     }
   }
-  if (count) L.c[HC3D_CNT_SUMSUB] += fx(si, t.stokes_scale);
-  L.c[HC3D_CNT_SUMALL] += fx(si, t.stokes_scale);
-  if (iflag == 1) L.c[HC3D_CNT_SCOUNT]++;
-  L.c[HC3D_CNT_ESCAPED]++;
+  if (count) L.add(HC3D_CNT_SUMSUB, fx(si, t.stokes_scale));
+  L.add(HC3D_CNT_SUMALL, fx(si, t.stokes_scale));
+  if (iflag == 1) L.add(HC3D_CNT_SCOUNT);
+  L.add(HC3D_CNT_ESCAPED);
 }
 
 // ---- the packet history, split at its events ----------------------------------------
 // propagate.f90 keeps these in locals; they persist across the waves below.
+template <class R>
 struct Flow {
-  double xpold, ypold, zpold;
+  typename PosOf<R>::T xpold, ypold, zpold;
   int iflag, iscat, iint, idust2;
   int64_t ntot;
 };
@@ -1491,6 +1696,8 @@ enum { ST_DONE = 0, ST_INTERACT = 1 };
 template <class R>
 __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
   p.on_wall = 0;
+  p.safe = 0.f;
+  p.lrow.key = -1;
   p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
   for (;;) {
     const R xran = ran<R>(rng);
@@ -1538,10 +1745,10 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   p.i_orig = 1;
   opacset<R>(m, dv, p, p.nub, a);
   const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
-  p.z = (double)p.cosb;
   const double rp_ = (double)p.sinb;
-  p.x = rp_ * (double)coslp;
-  p.y = rp_ * (double)sinlp;
+  set_pos(p.z, (double)p.cosb);
+  set_pos(p.x, rp_ * (double)coslp);
+  set_pos(p.y, rp_ * (double)sinlp);
   p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
   p.ir = 1;
   p.on_wall = 1 << 1;  // on the stellar surface: the inner radial wall (id 1) of cell 1
@@ -1549,9 +1756,8 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   p.ip = locate_dev(m.phiarr, m.npg, (double)p.lp);
   p.it = p.it < 1 ? 1 : (p.it > m.ntg - 1 ? m.ntg - 1 : p.it);
   p.ip = p.ip < 1 ? 1 : (p.ip > m.npg - 1 ? m.npg - 1 : p.ip);
-  tr.add(0, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-  make_rec<R>(rec, p, a, 0, 0);
-  rec.flags |= 128;
+  tr.add(0, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
+  make_rec<R>(rec, p, a, 0, 0, 128);
   rec.d0 = p.cosb; rec.d1 = p.sinb; rec.d2 = coslp; rec.d3 = sinlp;
 }
 
@@ -1569,8 +1775,8 @@ __device__ __forceinline__ void log_fault(const DevTallies& t, const Rng& rng, i
 
 // tau sample + tauint + outcome, propagate.f90:46-62 (first) and 169-202.
 template <class R>
-__device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Pkt<R>& p, Rng& rng,
-                    Flow& f, Local& L, Tracer& tr, bool first) {
+__device__ __forceinline__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                    Flow<R>& f, Local& L, Tracer& tr, bool first) {
   const R tau = -xlog(ran<R>(rng));
   if (!first) {
     f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
@@ -1579,17 +1785,17 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
   const int pir = p.ir, pit = p.it, pip = p.ip;
   const int st = tauint<R>(m, t, p, tau, L, tr);
   if (st == TI_ESCAPE) {
-    tr.add(3, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
-    bin_escape<R>(t, d, a, p, f.xpold, f.ypold, f.zpold, f.iflag, f.iscat, L);
+    tr.add(3, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
+    bin_escape<R>(t, d, a, p, dval(f.xpold), dval(f.ypold), dval(f.zpold), f.iflag, f.iscat, L);
     return ST_DONE;
   }
   if (st == TI_STAR) {
-    L.c[HC3D_CNT_AFLUX]++;
-    tr.add(4, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    L.add(HC3D_CNT_AFLUX);
+    tr.add(4, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
     return ST_DONE;
   }
   if (st == TI_FAULT) {
-    L.c[HC3D_CNT_STUCK]++;
+    L.add(HC3D_CNT_STUCK);
     set_status(a, 1);
     log_fault(t, rng, L.fault);
     return ST_DONE;
@@ -1598,38 +1804,39 @@ __device__ int walk(const DevModel& m, const DevTallies& t, const TallyDims& d, 
     if (p.ir != pir || p.it != pit || p.ip != pip) f.iint = 0;
     if (f.iint > a.iintmax || (a.max_interactions > 0 && f.ntot >= a.max_interactions)) {
       atomicAdd(t.killed + cidx(m, p.ir, p.it, p.ip), 1u);
-      L.c[HC3D_CNT_ABFLUX]++;
-      tr.add(7, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+      L.add(HC3D_CNT_ABFLUX);
+      tr.add(7, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
       return ST_DONE;
     }
   }
   f.idust2 = select_dust<R>(m, p, rng);
   if (f.idust2 < 0) {
-    L.c[HC3D_CNT_STUCK]++;
+    L.add(HC3D_CNT_STUCK);
     set_status(a, 2);
     log_fault(t, rng, F_SELECT);
     return ST_DONE;
   }
-  if (first) L.c[HC3D_CNT_TOT]++;
+  if (first) L.add(HC3D_CNT_TOT);
   return ST_INTERACT;
 }
 
 // One interaction, propagate.f90:70-166: scattering (rec = the state before
 // stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
 template <class R>
-__device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow& f,
+__device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow<R>& f,
                          Local& L, Tracer& tr, PeelRec<R>& rec) {
   const int64_t c = cidx(m, p.ir, p.it, p.ip);
   const int idust2 = f.idust2;
-  L.c[HC3D_CNT_EVENTS]++;
+  L.add(HC3D_CNT_EVENTS);
   f.ntot++;
   // issued before the albedo test so that its latency overlaps the draw
-  const double tave = __ldg(m.tdust + 4 * c + idust2);
-  if (ran<R>(rng) <= p.albedo[idust2]) {  // scattered
+  R tave = R(0);
+  if constexpr (sizeof(R) == 8) tave = __ldg(m.tdust + 4 * c + idust2);
+  if (ran<R>(rng) <= pick4(p.albedo, idust2)) {  // scattered
     f.iflag = 1; f.iscat++; f.iint++;
     make_rec<R>(rec, p, a, 1, idust2);
     stokes<R>(p, idust2, rng);
-    tr.add(5, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    tr.add(5, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
     atomicAdd(t.dbig + c, 1u);
     p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
@@ -1640,19 +1847,20 @@ __device__ void interact(const DevModel& m, const DustView<R>& dv, const DevTall
     p.phi = (R)kR2p * ran<R>(rng);
     p.cosp = xcos(p.phi);
     p.sinp = xsin(p.phi);
-    p.nub = lucydustfreq<R>(m, tave, idust2, rng);
+    if constexpr (sizeof(R) == 4) p.nub = lucy_freq_mixed(m, p.lrow, c, idust2, rng);
+    else p.nub = lucydustfreq<R>(m, tave, idust2, rng);
     f.iflag = 0;
     opacset<R>(m, dv, p, p.nub, a);
     make_rec<R>(rec, p, a, 0, idust2);
     f.iint++;
-    tr.add(6, p.ir, p.it, p.ip, 0, 0.0, p.x, p.y, p.z);
+    tr.add(6, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   }
 }
 
+// every thread of the block calls it, after its last event
 __device__ __forceinline__ void flush(const DevTallies& t, Local& L) {
-#pragma unroll
-  for (int i = 0; i < 16; ++i)
-    if (L.c[i]) atomicAdd(t.counters + i, L.c[i]);
+  __syncthreads();
+  if (threadIdx.x < 16 && L.sc[threadIdx.x]) atomicAdd(t.counters + threadIdx.x, L.sc[threadIdx.x]);
 }
 
 // ---- per-thread form: one packet at a time, its peel-off rays inline --------------
@@ -1665,7 +1873,7 @@ __device__ void run_packet(const DevModel& m, const DustView<R>& dv, const DevTa
   PeelRec<R> rec;
   emit<R>(m, dv, a, p, rng, rec, tr);
   if (a.ipeel == 1) peel_all<R>(m, t, d, a, rec, L);
-  Flow f;
+  Flow<R> f;
   f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
   f.iflag = 0; f.iscat = 0; f.iint = 0; f.idust2 = 0; f.ntot = 0;
   int st = walk<R>(m, t, d, a, p, rng, f, L, tr, true);
@@ -1681,10 +1889,9 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
   extern __shared__ double dust_smem[];
   DustView<R> dv;
   dust_view<R>(m, reinterpret_cast<R*>(dust_smem), dv);
+  __shared__ unsigned long long block_counters[16];
   Local L;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) L.c[i] = 0;
-  L.fault = 0;
+  local_init(L, block_counters);
   if (a.inj) {
     // trace harness: one thread per traced packet, draws from the injected list
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1720,7 +1927,7 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
 template <class R>
 struct Slot {
   Pkt<R> p;
-  Flow f;
+  Flow<R> f;
   uint64_t pid;
   uint32_t c0;
   int left;
@@ -1734,10 +1941,9 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
   extern __shared__ double dust_smem[];
   DustView<R> dv;
   dust_view<R>(m, reinterpret_cast<R*>(dust_smem), dv);
+  __shared__ unsigned long long block_counters[16];
   Local L;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) L.c[i] = 0;
-  L.fault = 0;
+  local_init(L, block_counters);
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   Slot<R> s = pool[gid];
   Rng rng;
@@ -1748,13 +1954,18 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     if (rng.left > 0) philox(rng.c0 - 1, 0u, rng.c2, rng.c3, rng.k0, rng.k1, rng.b);
   }
   Tracer tr{nullptr, 0, 0};
-  PeelRec<R> rec;
   for (int nrec = 0; nrec < E; ++nrec) {
     if (s.stage == 0) {
       const unsigned long long pid = atomicAdd(a.work, 1ull);
       if (pid >= (unsigned long long)a.np) break;
       s.pid = (uint64_t)(a.packet_offset + (int64_t)pid);
       rng_init(rng, a.key0, a.key1, s.pid);
+    }
+    // The event's record is written field by field into its queue slot as
+    // emission or the interaction produces it: the slot's atomic overlaps
+    // that work, and the record occupies no registers across the walk.
+    PeelRec<R>& rec = queue[atomicAdd(qcount, 1ull)];
+    if (s.stage == 0) {
       emit<R>(m, dv, a, s.p, rng, rec, tr);
       s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
       s.f.iflag = 0; s.f.iscat = 0; s.f.iint = 0; s.f.idust2 = 0; s.f.ntot = 0;
@@ -1762,13 +1973,7 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     } else {
       interact<R>(m, dv, t, a, s.p, rng, s.f, L, tr, rec);
     }
-    // The queue slot of this event's record, reserved before the walk and
-    // written after it, so that the atomic's round trip overlaps the walk
-    // (a per-thread atomic: no lane waits for the walks of the others).
-    unsigned long long slot = 0;
-    if (a.ipeel) slot = atomicAdd(qcount, 1ull);
     const int st = walk<R>(m, t, d, a, s.p, rng, s.f, L, tr, s.stage == 2);
-    if (a.ipeel) queue[slot] = rec;
     s.stage = st == ST_INTERACT ? 1 : 0;
   }
   s.c0 = rng.c0;
@@ -1784,10 +1989,9 @@ template <class R>
 __global__ void __launch_bounds__(256, 3) k_peel(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                   const PeelRec<R>* queue, const unsigned long long* qcount,
                                                   unsigned long long* next_ray) {
+  __shared__ unsigned long long block_counters[16];
   Local L;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) L.c[i] = 0;
-  L.fault = 0;
+  local_init(L, block_counters);
   const unsigned long long n = *qcount * (unsigned long long)a.npeel;
   for (;;) {
     const unsigned long long i = atomicAdd(next_ray, 1ull);
@@ -1810,10 +2014,9 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
   __shared__ PeelEsc esc[kPeelThreads / 32][kPeelBuf];
   for (int k = threadIdx.x; k < a.npeel; k += blockDim.x) dirs[k] = peel_dir(a, k);
   __syncthreads();
+  __shared__ unsigned long long block_counters[16];
   Local L;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) L.c[i] = 0;
-  L.fault = 0;
+  local_init(L, block_counters);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   PeelEsc* buf = esc[warp];
@@ -1826,6 +2029,7 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
   unsigned long long e = 0;                // the ray of this lane: event e, direction k
   int k = 0;
   PeelWalk w;
+  PeelCount pc{0u, 0u, 0u};
   for (;;) {
     if (more || rbase < rend) {
       const unsigned need = __ballot_sync(0xffffffffu, !have);
@@ -1849,14 +2053,14 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
           e = i / npeel;
           k = (int)(i - e * npeel);
           have = w.start(m, queue[e], dirs[k]);
-          if (have) L.c[HC3D_CNT_PEELS]++;
+          if (have) pc.peels++;
         }
       }
     }
     if (!__any_sync(0xffffffffu, have) && !more && rbase >= rend) break;
     bool out = false;
     if (have) {
-      const int st = w.step(m, cap, L);
+      const int st = w.step(m, cap, pc);
       out = st == PeelWalk::OUT;
       if (st != PeelWalk::GOING) have = false;
     }
@@ -1883,6 +2087,9 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
     const PeelEsc q = buf[j];
     peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
   }
+  if (pc.peels) L.add(HC3D_CNT_PEELS, pc.peels);
+  if (pc.cross) L.add(HC3D_CNT_CROSS_PEEL, pc.cross);
+  if (pc.stuck) L.add(HC3D_CNT_PEEL_STUCK, pc.stuck);
   flush(t, L);
 }
 

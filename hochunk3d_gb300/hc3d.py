@@ -391,10 +391,10 @@ class Context:
         return n.value, [(int(v) & ((1 << 56) - 1), int(v) >> 56) for v in buf[:k]]
 
     def wave_log(self) -> np.ndarray:
-        """Per wave of the last peeled run: E, active, alive, transport ms, peel ms."""
+        """Per wave of the last peeled run: E, active, alive, transport ms, peel ms, interactions."""
         n = C.c_int(0)
         lib().hc3d_get_wave_log(self._h, None, 0, C.byref(n))
-        out = np.zeros((max(n.value, 1), 5))
+        out = np.zeros((max(n.value, 1), 6))
         self._check(lib().hc3d_get_wave_log(self._h, _ptr(out), n.value, C.byref(n)))
         return out[: n.value]
 

@@ -273,7 +273,8 @@ int hc3d_last_launch_stats(hc3d_ctx *ctx, int *launches, double *transport_ms, d
  * through hc3d_trace_packets with its counter-based uniforms reproduces it. */
 int hc3d_get_fault_log(hc3d_ctx *ctx, uint64_t *entries, int max, int *n);
 /* Per wave of the last peeled run: event budget E, threads that could run,
- * packets alive after the wave, transport ms, peel-off ms (5 doubles each). */
+ * packets alive after the wave, transport ms, peel-off ms, interactions
+ * (6 doubles each). */
 int hc3d_get_wave_log(hc3d_ctx *ctx, double *out, int max_waves, int *n);
 
 /* ---- single-packet trace harness ---------------------------------------- */
