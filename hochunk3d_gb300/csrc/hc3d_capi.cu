@@ -628,6 +628,9 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   const int nrg = g->nrg, ntg = g->ntg, npg = g->npg;
   const int64_t n4 = (int64_t)nrg * ntg * npg;
   const int64_t ncell = (int64_t)(nrg - 1) * (ntg - 1) * (npg - 1);
+  // the kernels index cells with 32-bit arithmetic
+  if (ncell >= ((int64_t)1 << 31) || 4 * ncell >= ((int64_t)1 << 31))
+    return fail(c, HC3D_ERR_INVALID, "grid has 2^29 or more cells");
   // species slots beyond the device's four must be empty
   for (int s = kSlots; s < g->ndg; ++s)
     for (int64_t k = 0; k < n4; ++k)

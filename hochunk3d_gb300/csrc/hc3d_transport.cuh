@@ -377,6 +377,10 @@ __device__ __forceinline__ void ray_pos(const Ray& r, const PathLen& S, Pos2& x,
 constexpr float kNearSphere = 1.0f / 4096.0f;
 constexpr float kGrazeSphere = 1.0f / 256.0f;
 
+// square root of a positive FP32 value by the reciprocal square root (the
+// wall searches take it of discriminants already tested > 0)
+__device__ __forceinline__ float fsqrt_pos(float x) { return x * rsqrtf(x); }
+
 // The mixed-form wall search on a Ray at path length S.  The reference keeps
 // the roots of every wall in closest_wall and skips the root of the wall it
 // stands on by the on_wall rule; here the walls in `own` (bit id) contribute
@@ -419,13 +423,13 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
   if (in_own) {
     if (hb < 0.f) cand(-2.f * hb, 1);
   } else if (hb < 0.f && di > 0.f) {  // inner sphere: reached only moving inwards
-    cand(fmaxf(ci, 0.f) / (sqrtf(di) - hb), 1);
+    cand(__fdividef(fmaxf(ci, 0.f), fsqrt_pos(di) - hb), 1);
   }
   if (out_own) {
     if (hb < 0.f) cand(-2.f * hb, 2);
   } else if (dq > 0.f) {  // outer sphere: the exit root
-    const float sq = sqrtf(dq);
-    cand(hb > 0.f ? fmaxf(-co, 0.f) / (hb + sq) : sq - hb, 2);
+    const float sq = fsqrt_pos(dq);
+    cand(hb > 0.f ? __fdividef(fmaxf(-co, 0.f), hb + sq) : sq - hb, 2);
   }
   if (m.ntg > 2) {
 #pragma unroll
@@ -435,7 +439,7 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
       if (tan2 == 0.f) continue;
       const bool mine = (own >> id) & 1;
       if (tan2 < 0.f) {
-        if (!mine && uz != 0.f) cand(-zr / uz, id);
+        if (!mine && uz != 0.f) cand(__fdividef(-zr, uz), id);
         continue;
       }
       const float hemi = __ldg(m.hemi + it - 1 + k);
@@ -443,7 +447,7 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
       const float b = 2.f * (xr * ux + yr * uy - tan2 * zr * uz);
       if (mine) {
         if (a != 0.f) {
-          const float t = -b / a;
+          const float t = __fdividef(-b, a);
           if ((zr + t * uz) * hemi > 0.f) cand(t, id);
         }
         continue;
@@ -451,14 +455,14 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
       const float cq = xr * xr + yr * yr - tan2 * zr * zr;
       if (a == 0.f) {
         if (b != 0.f) {
-          const float t = -cq / b;
+          const float t = __fdividef(-cq, b);
           if ((zr + t * uz) * hemi > 0.f) cand(t, id);
         }
         continue;
       }
       const float disc = b * b - 4.f * a * cq;
       if (disc > 0.f) {
-        const float sq = sqrtf(disc), inv = 0.5f / a;
+        const float sq = fsqrt_pos(disc), inv = __fdividef(0.5f, a);
         const float t1 = (-b + sq) * inv, t2 = (-b - sq) * inv;
         if ((zr + t1 * uz) * hemi > 0.f) cand(t1, id);
         if ((zr + t2 * uz) * hemi > 0.f) cand(t2, id);
@@ -471,7 +475,7 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
         if ((own >> id) & 1) continue;
         const float A = __ldg(m.aarrf + ip - 1 + k), B = __ldg(m.barrf + ip - 1 + k);
         const float d = A * ux + B * uy;
-        if (d != 0.f) cand(-(A * xr + B * yr) / d, id);
+        if (d != 0.f) cand(__fdividef(-(A * xr + B * yr), d), id);
       }
     }
   }
@@ -482,20 +486,15 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
 
 // wall -> index step, peeloff_3d.f90:120-139
 __device__ __forceinline__ void step_index(int npg, int iface, int& ir, int& it, int& ip) {
-  switch (iface) {
-    case 1: ir--; break;
-    case 2: ir++; break;
-    case 3: it--; break;
-    case 4: it++; break;
-    case 5: ip--; break;
-    case 6: ip++; break;
-  }
-  if (ip == 0) ip = npg - 1;
-  if (ip == npg) ip = 1;
+  ir += (int)(iface == 2) - (int)(iface == 1);
+  it += (int)(iface == 4) - (int)(iface == 3);
+  ip += (int)(iface == 6) - (int)(iface == 5);
+  ip = ip == 0 ? npg - 1 : (ip == npg ? 1 : ip);
 }
 
+// compact cell index; hc3d_load_grid keeps the cell count below 2^31
 __device__ __forceinline__ int64_t cidx(const DevModel& m, int ir, int it, int ip) {
-  return (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+  return (int64_t)((ir - 1) + (m.nrg - 1) * ((it - 1) + (m.ntg - 1) * (ip - 1)));
 }
 
 template <class R> struct Rho { R v[kSlots]; };
@@ -2020,13 +2019,14 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   PeelEsc* buf = esc[warp];
+  // ray indices of one wave fit 32 bits: at most 2^22 records x 256 directions
   const unsigned npeel = (unsigned)a.npeel;
-  const unsigned long long n = *qcount * (unsigned long long)npeel;
+  const unsigned n = (unsigned)(*qcount) * npeel;
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nbuf = 0;
   bool have = false, more = n > 0;
-  unsigned long long rbase = 0, rend = 0;  // rays reserved by this warp, not yet started
-  unsigned long long e = 0;                // the ray of this lane: event e, direction k
+  unsigned rbase = 0, rend = 0;  // rays reserved by this warp, not yet started
+  unsigned e = 0;                // the ray of this lane: event e, direction k
   int k = 0;
   PeelWalk w;
   PeelCount pc{0u, 0u, 0u};
@@ -2041,14 +2041,14 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
           if (b >= n) {
             more = false;
           } else {
-            rbase = b;
-            rend = b + kPeelChunk < n ? b + kPeelChunk : n;
+            rbase = (unsigned)b;
+            rend = b + kPeelChunk < n ? (unsigned)b + kPeelChunk : n;
             if (rend >= n) more = false;
           }
         }
-        const unsigned long long avail = rend - rbase;
-        const unsigned long long i = rbase + (unsigned long long)__popc(need & lt);
-        rbase += (unsigned long long)__popc(need) < avail ? (unsigned long long)__popc(need) : avail;
+        const unsigned avail = rend - rbase;
+        const unsigned i = rbase + (unsigned)__popc(need & lt);
+        rbase += (unsigned)__popc(need) < avail ? (unsigned)__popc(need) : avail;
         if (!have && i < rend) {
           e = i / npeel;
           k = (int)(i - e * npeel);
