@@ -322,6 +322,7 @@ __device__ __forceinline__ double path_f64(const PathLen& s) { return (double)s.
 
 struct Ray {
   float x0, y0, z0, ux, uy, uz;  // FP32 start point and direction
+  float urho2, uz2;              // ux^2 + uy^2, uz^2
   Pos2 xs, ys, zs;               // the start point as pairs
   double rr0, hb0, u2;           // FP64 |x0|^2, x0.u, |u|^2 once `dbl` is set
   bool dbl;
@@ -331,6 +332,8 @@ __device__ __forceinline__ void ray_init(Ray& r, const Pos2& x, const Pos2& y, c
                                          float uz) {
   r.x0 = x.hi; r.y0 = y.hi; r.z0 = z.hi;
   r.ux = ux; r.uy = uy; r.uz = uz;
+  r.urho2 = ux * ux + uy * uy;
+  r.uz2 = uz * uz;
   r.xs = x; r.ys = y; r.zs = z;
   r.dbl = false;
 }
@@ -401,10 +404,13 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
   const float xr = fmaf(S.hi, ux, fmaf(S.lo, ux, r.x0));
   const float yr = fmaf(S.hi, uy, fmaf(S.lo, uy, r.y0));
   const float zr = fmaf(S.hi, uz, fmaf(S.lo, uz, r.z0));
+  // terms shared by the spheres and the cones
+  const float pxy = xr * ux + yr * uy, pz = zr * uz;
+  const float rho2 = xr * xr + yr * yr, z2 = zr * zr;
   // spheres: t^2 + 2 hb t + c = 0 with hb = x.u, c = |x|^2 - R^2, disc = hb^2 - c
   const bool in_own = (own & 2) != 0, out_own = (own & 4) != 0;
-  float hb = xr * ux + yr * uy + zr * uz;
-  const float rr = xr * xr + yr * yr + zr * zr;
+  float hb = pxy + pz;
+  const float rr = rho2 + z2;
   const float r2i = __ldg(m.r2arrf + ir - 1), r2o = __ldg(m.r2arrf + ir);
   float ci = rr - r2i, co = rr - r2o;
   float di = hb * hb - ci, dq = hb * hb - co;
@@ -432,6 +438,7 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
     cand(hb > 0.f ? __fdividef(fmaxf(-co, 0.f), hb + sq) : sq - hb, 2);
   }
   if (m.ntg > 2) {
+    // cones x^2 + y^2 = tan2 z^2: a t^2 + b t + cq = 0
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int id = 3 + k;
@@ -443,8 +450,8 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
         continue;
       }
       const float hemi = __ldg(m.hemi + it - 1 + k);
-      const float a = ux * ux + uy * uy - tan2 * uz * uz;
-      const float b = 2.f * (xr * ux + yr * uy - tan2 * zr * uz);
+      const float a = fmaf(-tan2, r.uz2, r.urho2);
+      const float b = 2.f * fmaf(-tan2, pz, pxy);
       if (mine) {
         if (a != 0.f) {
           const float t = __fdividef(-b, a);
@@ -452,7 +459,7 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
         }
         continue;
       }
-      const float cq = xr * xr + yr * yr - tan2 * zr * zr;
+      const float cq = fmaf(-tan2, z2, rho2);
       if (a == 0.f) {
         if (b != 0.f) {
           const float t = __fdividef(-cq, b);
@@ -469,10 +476,12 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
       }
     }
     if (m.npg > 2) {
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int id = 5 + k;
-        if ((own >> id) & 1) continue;
+      // The azimuth of a straight line changes monotonically (by less than
+      // pi), so only the plane on the side it turns towards can be met:
+      // phi(ip) (id 6) when (x cross u)_z > 0, phi(ip-1) (id 5) otherwise.
+      const int k = xr * uy - yr * ux > 0.f ? 1 : 0;
+      const int id = 5 + k;
+      if (!((own >> id) & 1)) {
         const float A = __ldg(m.aarrf + ip - 1 + k), B = __ldg(m.barrf + ip - 1 + k);
         const float d = A * ux + B * uy;
         if (d != 0.f) cand(__fdividef(-(A * xr + B * yr), d), id);
@@ -2004,7 +2013,7 @@ __global__ void __launch_bounds__(256, 3) k_peel(DevModel m, DevTallies t, Tally
 
 
 template <class R>
-__global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+__global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                                   const PeelRec<R>* queue,
                                                                   const unsigned long long* qcount,
                                                                   unsigned long long* next_ray) {
@@ -2057,7 +2066,7 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
         }
       }
     }
-    if (!__any_sync(0xffffffffu, have) && !more && rbase >= rend) break;
+    const bool idle = !__any_sync(0xffffffffu, have) && !more && rbase >= rend;
     bool out = false;
     if (have) {
       const int st = w.step(m, cap, pc);
@@ -2072,20 +2081,22 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
       w.end_point(q.xf, q.yf, q.zf);
     }
     nbuf += __popc(outm);
-    if (nbuf >= 32) {
+    // One call site of the tally: a ray's arithmetic does not depend on
+    // whether a full buffer or the final drain tallies it, so runs repeat
+    // bit for bit.
+    if (nbuf >= 32 || (idle && nbuf > 0)) {
       __syncwarp();
-      const PeelEsc q = buf[lane];
-      peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
+      const int take = nbuf < 32 ? nbuf : 32;
+      if (lane < take) {
+        const PeelEsc q = buf[lane];
+        peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
+      }
       __syncwarp();
-      if (lane < nbuf - 32) buf[lane] = buf[lane + 32];
+      if (lane < nbuf - take) buf[lane] = buf[lane + take];
       __syncwarp();
-      nbuf -= 32;
+      nbuf -= take;
     }
-  }
-  __syncwarp();
-  for (int j = lane; j < nbuf; j += 32) {
-    const PeelEsc q = buf[j];
-    peel_tally_mixed(t, d, a, queue[q.e], dirs[q.k], q.k, q.tsum, q.xf, q.yf, q.zf);
+    if (idle && nbuf == 0) break;
   }
   if (pc.peels) L.add(HC3D_CNT_PEELS, pc.peels);
   if (pc.cross) L.add(HC3D_CNT_CROSS_PEEL, pc.cross);
