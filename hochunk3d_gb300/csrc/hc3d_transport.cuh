@@ -797,6 +797,9 @@ static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevT
       at();
       return TI_FAULT;
     }
+    // the cell's density, loaded before the wall search (latency overlap)
+    const int64_t c = cidx(m, p.ir, p.it, p.ip);
+    const Rho<float> rho = load_rho<float>(m, c);
     float dt;
     int iface;
     if (!next_wall_ray(m, ray, S, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
@@ -812,8 +815,6 @@ static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevT
       L.fault = F_NOWALL;
       return TI_FAULT;
     }
-    const int64_t c = cidx(m, p.ir, p.it, p.ip);
-    const Rho<float> rho = load_rho<float>(m, c);
     float opac = 0.f;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) opac += p.kapd[s] * rho.v[s];
@@ -1294,7 +1295,8 @@ struct PeelEsc {
 
 constexpr int kPeelThreads = 256;
 constexpr int kPeelBuf = 64;
-constexpr int kPeelChunk = 256;  // rays a warp reserves per atomic
+constexpr int kPeelChunk = 256;  // rays a warp reserves per atomic, at most
+constexpr int kPeelStage = 4;    // records a warp stages in shared memory
 
 // peeloff_3d.f90:155-282 for one ray of the mixed form that reached the grid
 // edge: attenuation, the Stokes rotation of a scattered packet, image pixel
@@ -1396,6 +1398,11 @@ struct PeelWalk {
       return ENDED;
     }
     ++nstep;
+    // the cell's density and peel mask, loaded before the wall search so
+    // that their latency overlaps it
+    const int64_t c = cidx(m, ir, it, ip);
+    const Rho<float> rho = load_rho<float>(m, c);
+    const unsigned mask = __ldg(m.peelmask + c);
     float dt;
     int iface;
     if (!next_wall_ray(m, ray, S, ir, it, ip, on_wall, dt, iface)) {
@@ -1406,9 +1413,6 @@ struct PeelWalk {
       pc.stuck++;
       return ENDED;
     }
-    const int64_t c = cidx(m, ir, it, ip);
-    const Rho<float> rho = load_rho<float>(m, c);
-    const unsigned mask = __ldg(m.peelmask + c);
     float opac = 0.f;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s)
@@ -2020,6 +2024,8 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
   static_assert(sizeof(R) == 4, "the warp-synchronous ray pool is the mixed form");
   __shared__ PeelDir dirs[kMaxPeel];
   __shared__ PeelEsc esc[kPeelThreads / 32][kPeelBuf];
+  __shared__ PeelRec<float> stage[kPeelThreads / 32][kPeelStage];
+  static_assert(sizeof(PeelRec<float>) % 4 == 0, "records are staged as 32-bit words");
   for (int k = threadIdx.x; k < a.npeel; k += blockDim.x) dirs[k] = peel_dir(a, k);
   __syncthreads();
   __shared__ unsigned long long block_counters[16];
@@ -2031,6 +2037,12 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
   // ray indices of one wave fit 32 bits: at most 2^22 records x 256 directions
   const unsigned npeel = (unsigned)a.npeel;
   const unsigned n = (unsigned)(*qcount) * npeel;
+  // a warp reserves whole records: kPeelStage of them, or fewer when
+  // npeel is large, and stages them in shared memory for its lanes
+  const unsigned nrec = min((unsigned)kPeelStage, max(1u, (unsigned)kPeelChunk / npeel));
+  const unsigned chunk = nrec * npeel;
+  PeelRec<float>* st = stage[warp];
+  unsigned e0 = 0;  // first record staged
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int nbuf = 0;
   bool have = false, more = n > 0;
@@ -2045,14 +2057,21 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
       if (need) {
         if (rbase >= rend) {  // reserve the next chunk of rays for this warp
           unsigned long long b = 0;
-          if (lane == 0) b = atomicAdd(next_ray, (unsigned long long)kPeelChunk);
+          if (lane == 0) b = atomicAdd(next_ray, (unsigned long long)chunk);
           b = __shfl_sync(0xffffffffu, b, 0);
           if (b >= n) {
             more = false;
           } else {
             rbase = (unsigned)b;
-            rend = b + kPeelChunk < n ? (unsigned)b + kPeelChunk : n;
+            rend = b + chunk < n ? (unsigned)b + chunk : n;
             if (rend >= n) more = false;
+            // stage the chunk's records (whole records: chunks are multiples of npeel)
+            e0 = rbase / npeel;
+            const int words = (int)((rend - rbase) / npeel) * (int)(sizeof(PeelRec<float>) / 4);
+            const unsigned* src = reinterpret_cast<const unsigned*>(queue + e0);
+            unsigned* dst = reinterpret_cast<unsigned*>(st);
+            for (int j = lane; j < words; j += 32) dst[j] = __ldg(src + j);
+            __syncwarp();
           }
         }
         const unsigned avail = rend - rbase;
@@ -2061,7 +2080,7 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
         if (!have && i < rend) {
           e = i / npeel;
           k = (int)(i - e * npeel);
-          have = w.start(m, queue[e], dirs[k]);
+          have = w.start(m, st[e - e0], dirs[k]);
           if (have) pc.peels++;
         }
       }
