@@ -709,6 +709,17 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
     float2* d_cs = nullptr;
     if ((r = dupload(c, own, &d_cs, cs.data(), cs.size()))) return r;
     m.thcs = d_cs;
+    std::vector<float2> r2p(nrg - 1), cf(ntg), pf(npg);
+    for (int i = 0; i < nrg - 1; ++i) r2p[i] = make_float2(r2f32[i], r2f32[i + 1]);
+    for (int i = 0; i < ntg; ++i) cf[i] = make_float2(tan2f[i], hemi[i]);
+    for (int i = 0; i < npg; ++i) pf[i] = make_float2(af[i], bf[i]);
+    float2 *d_r2p = nullptr, *d_cf = nullptr, *d_pf = nullptr;
+    if ((r = dupload(c, own, &d_r2p, r2p.data(), r2p.size())) || (r = dupload(c, own, &d_cf, cf.data(), cf.size())) ||
+        (r = dupload(c, own, &d_pf, pf.data(), pf.size())))
+      return r;
+    m.r2pair = d_r2p;
+    m.conef = d_cf;
+    m.planef = d_pf;
   }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
   m.peelmask = c->d_peelmask; m.tdust = c->d_tdust; m.tdustf = c->d_tdustf;

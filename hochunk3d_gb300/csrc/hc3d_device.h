@@ -56,6 +56,10 @@ struct DevModel {
   const float* tan2f;     // (ntg)
   const float* hemi;      // (ntg) +1 upper, -1 lower (cone nappe)
   const float2* thcs;     // (ntg) cos, sin of the polar walls (mixed-form safe distance)
+  // interleaved FP32 wall data of the mixed-form wall search (one load per family)
+  const float2* r2pair;   // (nrg-1) squared inner and outer radius of radial cell ir (index ir-1)
+  const float2* conef;    // (ntg) tan^2 and hemisphere sign of polar wall it (index it-1)
+  const float2* planef;   // (npg) A = sin(phi), B = -cos(phi) of azimuthal wall ip (index ip-1)
   const double* aarrd; const double* barrd;  // (npg)
   const float* aarrf; const float* barrf;    // (npg)
   const float4* rho4f;    // (ncell) species slots x,y,z,w  (mixed form)

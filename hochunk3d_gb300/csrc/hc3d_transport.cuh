@@ -376,9 +376,11 @@ __device__ __forceinline__ void ray_pos(const Ray& r, const PathLen& S, Pos2& x,
 
 // A sphere root from FP32 |x|^2 - R^2 is exact enough unless the point lies
 // within 2^-12 R^2 of the sphere (|x|^2 - R^2 cancels) or the ray grazes it
-// (hb^2 - c within 2^-8 R^2 of zero); those cases are redone in FP64.
+// (hb^2 - c within 2^-10 R^2 of zero); those cases are redone in FP64.  The
+// inner sphere counts only for a ray moving inwards, the one case whose root
+// is used.
 constexpr float kNearSphere = 1.0f / 4096.0f;
-constexpr float kGrazeSphere = 1.0f / 256.0f;
+constexpr float kGrazeSphere = 1.0f / 1024.0f;
 
 // square root of a positive FP32 value by the reciprocal square root (the
 // wall searches take it of discriminants already tested > 0)
@@ -411,10 +413,11 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
   const bool in_own = (own & 2) != 0, out_own = (own & 4) != 0;
   float hb = pxy + pz;
   const float rr = rho2 + z2;
-  const float r2i = __ldg(m.r2arrf + ir - 1), r2o = __ldg(m.r2arrf + ir);
+  const float2 r2io = __ldg(m.r2pair + ir - 1);
+  const float r2i = r2io.x, r2o = r2io.y;
   float ci = rr - r2i, co = rr - r2o;
   float di = hb * hb - ci, dq = hb * hb - co;
-  const bool fix = (!in_own && (fabsf(ci) < kNearSphere * r2i || fabsf(di) < kGrazeSphere * r2i)) ||
+  const bool fix = (!in_own && hb < 0.f && (fabsf(ci) < kNearSphere * r2i || fabsf(di) < kGrazeSphere * r2i)) ||
                    (!out_own && (fabsf(co) < kNearSphere * r2o || fabsf(dq) < kGrazeSphere * r2o));
   if (fix) {
     ray_f64(r);
@@ -442,14 +445,14 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const int id = 3 + k;
-      const float tan2 = __ldg(m.tan2f + it - 1 + k);
+      const float2 cw = __ldg(m.conef + it - 1 + k);
+      const float tan2 = cw.x, hemi = cw.y;
       if (tan2 == 0.f) continue;
       const bool mine = (own >> id) & 1;
       if (tan2 < 0.f) {
         if (!mine && uz != 0.f) cand(__fdividef(-zr, uz), id);
         continue;
       }
-      const float hemi = __ldg(m.hemi + it - 1 + k);
       const float a = fmaf(-tan2, r.uz2, r.urho2);
       const float b = 2.f * fmaf(-tan2, pz, pxy);
       if (mine) {
@@ -482,7 +485,8 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
       const int k = xr * uy - yr * ux > 0.f ? 1 : 0;
       const int id = 5 + k;
       if (!((own >> id) & 1)) {
-        const float A = __ldg(m.aarrf + ip - 1 + k), B = __ldg(m.barrf + ip - 1 + k);
+        const float2 ab = __ldg(m.planef + ip - 1 + k);
+        const float A = ab.x, B = ab.y;
         const float d = A * ux + B * uy;
         if (d != 0.f) cand(__fdividef(-(A * xr + B * yr), d), id);
       }
@@ -1159,18 +1163,6 @@ __device__ __forceinline__ void add9(unsigned long long* base, int64_t stride, i
   atomicAdd(base + 8 * stride + b, 1ull);
 }
 
-__device__ __forceinline__ void add9f(unsigned long long* base, int64_t stride, int64_t b, float i, float q, float u,
-                                      float v, float ss, float sq) {
-  atomicAdd(base + b, fxf(i, ss));
-  atomicAdd(base + stride + b, fxf(q, ss));
-  atomicAdd(base + 2 * stride + b, fxf(u, ss));
-  atomicAdd(base + 3 * stride + b, fxf(v, ss));
-  atomicAdd(base + 4 * stride + b, fxf(i * i, sq));
-  atomicAdd(base + 5 * stride + b, fxf(q * q, sq));
-  atomicAdd(base + 6 * stride + b, fxf(u * u, sq));
-  atomicAdd(base + 7 * stride + b, fxf(v * v, sq));
-  atomicAdd(base + 8 * stride + b, 1ull);
-}
 
 // ---- peeloff_3d.f90:52-286: one observer direction k of one event (FP64 form) ----------
 // The mixed form walks its peel-off rays in k_peel_mixed.
@@ -1325,23 +1317,25 @@ __device__ __forceinline__ void peel_tally_mixed(const DevTallies& t, const Tall
   const float rho2 = ximage * ximage + yimage * yimage;
   const int i_inter = iflag == 1 ? 2 : (i_orig == 1 ? 1 : 3);
   const int indx[3] = {1, 1 + i_orig, 5 + i_inter};
+  // the fixed-point values, converted once for all the bins they go to
   const float ss = (float)t.stokes_scale, sq = (float)t.square_scale;
+  const unsigned long long v[9] = {fxf(sip, ss), fxf(sqp, ss), fxf(sup, ss), fxf(svp, ss),
+                                   fxf(sip * sip, sq), fxf(sqp * sqp, sq), fxf(sup * sup, sq), fxf(svp * svp, sq), 1ull};
   for (int ia = 1; ia <= a.nap; ++ia) {
     if (rho2 < (float)__ldg(a.aperture2 + ia - 1)) {
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const int64_t b = (int64_t)(e.inub - 1) +
                           (int64_t)a.nfreq * (k + (int64_t)a.npeel * ((ia - 1) + (int64_t)a.nap * (indx[q] - 1)));
-        add9f(t.psed, d.npsed, b, sip, sqp, sup, svp, ss, sq);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) atomicAdd(t.psed + j * d.npsed + b, v[j]);
       }
     }
   }
   if (a.image && ix <= a.nx && iy <= a.nx && ix > 0 && iy > 0) {
     const int64_t b = (int64_t)k + (int64_t)a.npeel * ((ix - 1) + (int64_t)a.nx * (iy - 1));
-    atomicAdd(t.img + b, fxf(sip, ss));
-    atomicAdd(t.img + d.nimg + b, fxf(sqp, ss));
-    atomicAdd(t.img + 2 * d.nimg + b, fxf(sup, ss));
-    atomicAdd(t.img + 3 * d.nimg + b, fxf(svp, ss));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) atomicAdd(t.img + j * d.nimg + b, v[j]);
   }
 }
 
@@ -1675,13 +1669,18 @@ __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArg
   const int indx[3] = {1, 1 + p.i_orig, 5 + i_inter};
   const double si = (double)p.sip, sq = (double)p.sqp, su = (double)p.sup, sv = (double)p.svp;
   const bool count = !(iflag == 0 && p.i_orig == 4);
+  // the fixed-point values, converted once for all the bins they go to
+  const unsigned long long v[9] = {fx(si, t.stokes_scale), fx(sq, t.stokes_scale), fx(su, t.stokes_scale),
+                                   fx(sv, t.stokes_scale), fx(si * si, t.square_scale), fx(sq * sq, t.square_scale),
+                                   fx(su * su, t.square_scale), fx(sv * sv, t.square_scale), 1ull};
   for (int ia = 1; ia <= a.nap; ++ia) {
     if (rho2 < __ldg(a.aperture2 + ia - 1) && count) {
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
         const int64_t b = (int64_t)(inub - 1) +
                           (int64_t)a.nfreq * ((it - 1) + (int64_t)a.nmu * ((ip - 1) + (int64_t)a.nph * ((ia - 1) + (int64_t)a.nap * (indx[q] - 1))));
-        add9(t.sed, d.nsed, b, si, sq, su, sv, t.stokes_scale, t.square_scale);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) atomicAdd(t.sed + j * d.nsed + b, v[j]);
       }
     }
   }
