@@ -392,6 +392,10 @@ __device__ __forceinline__ float fsqrt_pos(float x) { return x * rsqrtf(x); }
 // only their far root, and the next wall is the smallest non-negative root
 // of the rest, a minimum over at most six candidates.  FP32, except the
 // near-sphere and grazing sphere roots (FP64).
+// kCache: keep the FP64 terms of the start point in the Ray once formed (the
+// transport walk, where one event's steps repeat the refinement); the
+// peel-off walk forms them afresh each time and keeps its registers.
+template <bool kCache>
 __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const PathLen& S, int ir, int it, int ip,
                                               int own, float& dt, int& iface) {
   float best = 3.402823466e38f;
@@ -420,10 +424,20 @@ __device__ __forceinline__ bool next_wall_ray(const DevModel& m, Ray& r, const P
   const bool fix = (!in_own && hb < 0.f && (fabsf(ci) < kNearSphere * r2i || fabsf(di) < kGrazeSphere * r2i)) ||
                    (!out_own && (fabsf(co) < kNearSphere * r2o || fabsf(dq) < kGrazeSphere * r2o));
   if (fix) {
-    ray_f64(r);
+    double rr0, hb0, u2;
+    if constexpr (kCache) {
+      ray_f64(r);
+      rr0 = r.rr0; hb0 = r.hb0; u2 = r.u2;
+    } else {
+      const double uxd = ux, uyd = uy, uzd = uz;
+      const double x = dval(r.xs), y = dval(r.ys), z = dval(r.zs);
+      rr0 = x * x + y * y + z * z;
+      hb0 = x * uxd + y * uyd + z * uzd;
+      u2 = uxd * uxd + uyd * uyd + uzd * uzd;
+    }
     const double s = path_f64(S);
-    const double hbd = fma(s, r.u2, r.hb0);
-    const double rrd = fma(s, fma(s, r.u2, r.hb0 + r.hb0), r.rr0);
+    const double hbd = fma(s, u2, hb0);
+    const double rrd = fma(s, fma(s, u2, hb0 + hb0), rr0);
     const double cid = rrd - __ldg(m.r2arr + ir - 1), cod = rrd - __ldg(m.r2arr + ir);
     hb = (float)hbd;
     ci = (float)cid; co = (float)cod;
@@ -806,7 +820,7 @@ static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevT
     const Rho<float> rho = load_rho<float>(m, c);
     float dt;
     int iface;
-    if (!next_wall_ray(m, ray, S, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
+    if (!next_wall_ray<true>(m, ray, S, p.ir, p.it, p.ip, p.on_wall, dt, iface)) {
       at();
       if (nreloc < 4) {
         ++nreloc;
@@ -1362,9 +1376,11 @@ struct PeelWalk {
     on_wall = (flags >> 8) & 127;
     bool go = true;
     if (on_wall) {  // peeloff_3d.f90:60-87: leave the radial wall the event sits on
-      ray_f64(ray);
-      const bool inner_wall = fabs(ray.rr0 - __ldg(m.r2arr + ir - 1)) < fabs(ray.rr0 - __ldg(m.r2arr + ir));
-      const bool outwards = ray.hb0 > 0.0;
+      const double x = dval(r.x), y = dval(r.y), z = dval(r.z);
+      const double rr0 = x * x + y * y + z * z;
+      const double hb0 = x * (double)dd.ux + y * (double)dd.uy + z * (double)dd.uz;
+      const bool inner_wall = fabs(rr0 - __ldg(m.r2arr + ir - 1)) < fabs(rr0 - __ldg(m.r2arr + ir));
+      const bool outwards = hb0 > 0.0;
       if (inner_wall && !outwards) {
         if (ir == 1) go = false;
         ir = ir - 1;
@@ -1399,7 +1415,7 @@ struct PeelWalk {
     const unsigned mask = __ldg(m.peelmask + c);
     float dt;
     int iface;
-    if (!next_wall_ray(m, ray, S, ir, it, ip, on_wall, dt, iface)) {
+    if (!next_wall_ray<false>(m, ray, S, ir, it, ip, on_wall, dt, iface)) {
       if (nreloc < 4) {
         ++nreloc;
         return relocate_here(m);
