@@ -35,6 +35,7 @@ UNITS = [
     ("hc3d_kernel_fp64.cu", ["--fmad=false"]),
     ("hc3d_capi.cu", []),
     ("hc3d_noalloc.cu", []),
+    ("hc3d_gridbuild.cu", []),
     ("hc3d_model.cpp", []),
     ("hc3d_driver.cpp", []),
 ]

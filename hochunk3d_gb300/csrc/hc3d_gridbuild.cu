@@ -1,0 +1,311 @@
+// hc3d_gridbuild.cu -- the densities of gridset (gridset.f90:954-1098) on
+// the GPU: disk mass normalisation, per-cell species densities, cell volumes
+// and (rho V)^(1/4), for a model whose walls, parameters and fractal field
+// the host set up.  One thread per (r, theta) column of cells walks the
+// azimuthal cells of that column, as the host loop does; the two mass sums
+// are reduced per column and then over columns in a fixed order, so a run
+// repeats bit for bit.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "hc3d_model.h"
+
+namespace hc3d {
+namespace {
+
+// the density parameters of a Model, copied by value into the kernels
+struct DensParams {
+  int nrg, ntg, npg;
+  int idiskcurve, ienvtype, ihole, ipoly, ifractal;
+  int fractmask[4];
+  double rho0[2], z1[2], a[2], b[2], rmaxd[2], rddust[2];
+  double fmass[4];
+  double rc, rhoe0, rmine, rmax, envexp, rhodens1, rhoamb;
+  double c1e, ex1, z01, c2e, ex2, z02, rhoconst1, rhoconst2, exf;
+  double r3;  // rmincgs^3
+};
+
+// zerod: the Ulrich cubic mu0^3 + (r/Rc - 1) mu0 - (r/Rc) mu = 0, closed form
+// then three Newton steps, the root clamped to [0, 1] (as the host restatement)
+__device__ double zerod_dev(double mu, double rx) {
+  const double p = rx - 1.0, q = -rx * mu;
+  double x;
+  const double disc = 0.25 * q * q + p * p * p / 27.0;
+  if (disc > 0.0) {
+    const double sd = sqrt(disc);
+    x = cbrt(-0.5 * q + sd) + cbrt(-0.5 * q - sd);
+  } else if (p < 0.0) {
+    const double r = sqrt(-p / 3.0);
+    const double arg = fmax(-1.0, fmin(1.0, (3.0 * q) / (2.0 * p) * sqrt(-3.0 / p)));
+    x = 2.0 * r * cos(acos(arg) / 3.0);
+  } else {
+    x = 0.0;
+  }
+  for (int k = 0; k < 3; ++k) {
+    const double fx = x * x * x + p * x + q, d = 3.0 * x * x + p;
+    if (d != 0.0) x -= fx / d;
+  }
+  return fmax(0.0, fmin(1.0, x));
+}
+
+// densdiskg.f90:1-155 for an unwarped, ungapped, unspiralled disk (species 0, 1)
+__device__ double densdisk_dev(const DensParams& P, double rad, double sint, double cost, int id) {
+  const double rp = rad * sint, zp = rad * cost;
+  const double rcoord = P.idiskcurve == 1 ? rad : rp;
+  const double zmr = P.z1[id] * pow(rcoord, P.b[id]);
+  if (rcoord > P.rmaxd[id] || P.rho0[id] == 0.0 || rcoord < P.rddust[id] || zmr < 1.e-10) return 0.0;
+  const double gexp = (zp / zmr) * (zp / zmr);
+  if (gexp > 1.e-15) {
+    if (gexp < 120.0) return P.rho0[id] * pow(rcoord, -P.a[id]) * exp(-0.5 * gexp);
+    return 0.0;
+  }
+  return P.rho0[id] * pow(rcoord, -P.a[id]);
+}
+
+// densenv.f90:1-128: Ulrich envelope or power law with a polynomial bipolar
+// cavity; id 2 is the envelope, 3 the cavity
+__device__ double densenv_dev(const DensParams& P, double rad, double costin, double sina, int id) {
+  const double cosa = fabs(costin);
+  const double rp = rad * sina, zp = rad * cosa;
+  const double zup = P.c1e * pow(rp, P.ex1) + P.z01;
+  const double xmu = zp / rad;
+  double dens = 0.0;
+  int inhole = 0;
+  if (rad > P.rmine) {
+    if (P.ienvtype == 1) {
+      const double rx = rad / P.rc;
+      const double xmu0 = zerod_dev(xmu, rx);
+      const double ratio = xmu0 > 0.0 ? xmu / xmu0 : 1.0;
+      const double factor = 1.0 / (ratio + 2.0 * (xmu0 * xmu0) / rx);
+      dens = P.rhoe0 * pow(rx, -1.5) * factor / sqrt(1.0 + ratio);
+    } else {
+      dens = P.rhodens1 * pow(rad, -P.envexp);
+    }
+  }
+  if (rad > P.rmine && dens < P.rhoamb) dens = P.rhoamb;
+  if (P.ihole == 1 && P.ipoly == 1) {
+    const double zlo = P.c2e * pow(rp, P.ex2) + P.z02;
+    if (zp > zlo) {
+      inhole = 1;
+      dens = P.rhoconst2 * pow(rad, -P.exf);
+    }
+    if (zp > zup) {
+      inhole = 1;
+      dens = P.rhoconst1 * pow(rad, -P.exf);
+    }
+  }
+  if (rad >= P.rmax) dens = 0.0;
+  if (rad <= P.rmine) dens = 0.0;
+  if (id == 3 && inhole == 0) dens = 0.0;
+  if (id == 2 && inhole == 1) dens = 0.0;
+  return dens;
+}
+
+struct Walls {
+  const double *rarr, *ravearr, *thetarr, *thetavearr, *phiarr, *densvar;
+};
+
+// unnormalised disk mass of each column (both disk species), for diskscl
+__global__ void k_disk_colmass(DensParams P, Walls w, double* colmass) {
+  const int ncol = (P.nrg - 1) * (P.ntg - 1);
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int ir = col % (P.nrg - 1), it = col / (P.nrg - 1);
+  const double rad = w.ravearr[ir];
+  const double dr3 = pow(w.rarr[ir + 1], 3.0) - pow(w.rarr[ir], 3.0);
+  const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
+  const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
+  for (int id = 0; id < 2; ++id) {
+    double m = 0.0;
+    if (P.rho0[id] != 0.0) {
+      const double dd = densdisk_dev(P, rad, sint, cost, id);
+      if (dd != 0.0)
+        for (int ip = 0; ip < P.npg - 1; ++ip) m += dd * (-dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3);
+    }
+    colmass[(size_t)id * ncol + col] = m;
+  }
+}
+
+// sums[k] = sum over columns of v[k * n + col], one block, fixed order
+__global__ void k_sum_columns(const double* v, int n, int nsum, double* sums) {
+  __shared__ double part[256];
+  for (int k = 0; k < nsum; ++k) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += v[(size_t)k * n + i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) part[threadIdx.x] += part[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[k] = part[0];
+    __syncthreads();
+  }
+}
+
+// densities, volumes and (rho V)^(1/4) of every cell of a column; per-column
+// disk and envelope masses into colmass[0..1][col]
+__global__ void k_density(DensParams P, Walls w, const double* diskscl, double* densarr, double* massarr,
+                          double* vcell, double* colmass) {
+  const int ncol = (P.nrg - 1) * (P.ntg - 1);
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const int ir = col % (P.nrg - 1), it = col / (P.nrg - 1);
+  const int64_t n4 = (int64_t)P.nrg * P.ntg * P.npg;
+  const double rad = w.ravearr[ir];
+  const double dr3 = pow(w.rarr[ir + 1], 3.0) - pow(w.rarr[ir], 3.0);
+  const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
+  const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
+  double dens_r[4];
+  for (int id = 0; id < 2; ++id) dens_r[id] = densdisk_dev(P, rad, sint, cost, id) * diskscl[id];
+  for (int id = 2; id < 4; ++id) dens_r[id] = densenv_dev(P, rad, cost, sint, id) * P.fmass[id];
+  double mdisk = 0.0, menv = 0.0;
+  for (int ip = 0; ip < P.npg - 1; ++ip) {
+    const double vol = -dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3;
+    const int64_t c = (int64_t)ir + (int64_t)P.nrg * (it + (int64_t)P.ntg * ip);
+    vcell[c] = vol;
+    for (int id = 0; id < 4; ++id) {
+      double d = dens_r[id];
+      if (P.ifractal && P.fractmask[id] == 1)
+        d *= w.densvar[ir + (int64_t)(P.nrg - 1) * (it + (int64_t)(P.ntg - 1) * ip)];
+      densarr[c + n4 * id] = d;
+      massarr[c + n4 * id] = pow(d * vol, 0.25);
+      if (id < 2) mdisk += d * vol;
+      else menv += d * vol;
+    }
+  }
+  colmass[col] = mdisk;
+  colmass[(size_t)ncol + col] = menv;
+}
+
+struct DevBufs {
+  std::vector<void*> p;
+  ~DevBufs() {
+    for (void* q : p) cudaFree(q);
+  }
+  template <class T>
+  T* alloc(size_t n) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, n * sizeof(T) + 16) != cudaSuccess) return nullptr;
+    p.push_back(q);
+    return static_cast<T*>(q);
+  }
+};
+
+}  // namespace
+
+// The densities of gridset on device `device`; replaces m.densarr, massarr,
+// vcell, massdisk, massenv and ndg_active.  ms receives the device time.
+int densities_gpu(Model& m, int device, double* ms, std::string* err) {
+  if (cudaSetDevice(device) != cudaSuccess) { *err = "no CUDA device"; return HC3D_ERR_CUDA; }
+  const int nrg = m.nrg, ntg = m.ntg, npg = m.npg;
+  const int ncol = (nrg - 1) * (ntg - 1);
+  const int64_t n4 = m.n4();
+  if (m.ndg != 4 || ncol <= 0) { *err = "model grid not built"; return HC3D_ERR_STATE; }
+  DensParams P;
+  std::memset(&P, 0, sizeof P);
+  P.nrg = nrg; P.ntg = ntg; P.npg = npg;
+  P.idiskcurve = m.idiskcurve; P.ienvtype = m.ienvtype; P.ihole = m.ihole; P.ipoly = m.ipoly;
+  P.ifractal = m.ifractal;
+  for (int id = 0; id < 4; ++id) { P.fractmask[id] = m.fractmask[id]; P.fmass[id] = m.fmass[id]; }
+  for (int id = 0; id < 2; ++id) {
+    P.rho0[id] = m.rho0[id]; P.z1[id] = m.z1[id]; P.a[id] = m.a[id]; P.b[id] = m.b[id];
+    P.rmaxd[id] = m.rmaxd[id]; P.rddust[id] = m.rddust[id];
+  }
+  P.rc = m.rc; P.rhoe0 = m.rhoe0; P.rmine = m.rmine; P.rmax = m.rmax; P.envexp = m.envexp;
+  P.rhodens1 = m.rhodens1; P.rhoamb = m.rhoamb;
+  P.c1e = m.c1e; P.ex1 = m.ex1; P.z01 = m.z01; P.c2e = m.c2e; P.ex2 = m.ex2; P.z02 = m.z02;
+  P.rhoconst1 = m.rhoconst1; P.rhoconst2 = m.rhoconst2; P.exf = m.exf;
+  const double rmincgs = m.rstar * kRsun;
+  P.r3 = std::pow(rmincgs, 3.0);
+  DevBufs B;
+  double *d_r = B.alloc<double>(nrg), *d_ra = B.alloc<double>(nrg), *d_t = B.alloc<double>(ntg),
+         *d_ta = B.alloc<double>(ntg), *d_p = B.alloc<double>(npg);
+  const size_t nvar = m.ifractal ? m.densvar.size() : 1;
+  double* d_var = B.alloc<double>(nvar);
+  double *d_dens = B.alloc<double>((size_t)n4 * 4), *d_mass = B.alloc<double>((size_t)n4 * 4),
+         *d_vol = B.alloc<double>((size_t)n4), *d_col = B.alloc<double>((size_t)2 * ncol), *d_s = B.alloc<double>(4);
+  if (!d_r || !d_ra || !d_t || !d_ta || !d_p || !d_var || !d_dens || !d_mass || !d_vol || !d_col || !d_s) {
+    *err = "device allocation failed";
+    return HC3D_ERR_NOMEM;
+  }
+  auto up = [](double* d, const std::vector<double>& h, size_t n) {
+    return cudaMemcpy(d, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  if (!up(d_r, m.rarr, nrg) || !up(d_ra, m.ravearr, nrg - 1) || !up(d_t, m.thetarr, ntg) ||
+      !up(d_ta, m.thetavearr, ntg - 1) || !up(d_p, m.phiarr, npg) || (m.ifractal && !up(d_var, m.densvar, nvar))) {
+    *err = "upload failed";
+    return HC3D_ERR_CUDA;
+  }
+  // zero the wall-index entries (ir = nrg, it = ntg, ip = npg) as the host arrays have them
+  cudaMemset(d_dens, 0, sizeof(double) * n4 * 4);
+  cudaMemset(d_mass, 0, sizeof(double) * n4 * 4);
+  cudaMemset(d_vol, 0, sizeof(double) * n4);
+  Walls w{d_r, d_ra, d_t, d_ta, d_p, d_var};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int threads = 128, blocks = (ncol + threads - 1) / threads;
+  cudaEventRecord(e0);
+  // disk mass normalisation: diskscl = massd * fmass / mass on the grid
+  double diskscl[2] = {1.0, 1.0};
+  if (m.massd > 0.0) {
+    k_disk_colmass<<<blocks, threads>>>(P, w, d_col);
+    k_sum_columns<<<1, 256>>>(d_col, ncol, 2, d_s);
+    double tm[2];
+    if (cudaMemcpy(tm, d_s, sizeof(tm), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      *err = "disk mass reduction failed";
+      return HC3D_ERR_CUDA;
+    }
+    for (int id = 0; id < 2; ++id) {
+      if (m.rho0[id] == 0.0) continue;
+      const double tmp = tm[id] / kMsun;
+      if (tmp > 0.0) diskscl[id] = m.massd * m.fmass[id] / tmp;
+    }
+  }
+  cudaMemcpy(d_s + 2, diskscl, sizeof(diskscl), cudaMemcpyHostToDevice);
+  k_density<<<blocks, threads>>>(P, w, d_s + 2, d_dens, d_mass, d_vol, d_col);
+  k_sum_columns<<<1, 256>>>(d_col, ncol, 2, d_s);
+  cudaEventRecord(e1);
+  if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    *err = "density kernels failed";
+    return HC3D_ERR_CUDA;
+  }
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = t;
+  double sums[2];
+  m.densarr.resize((size_t)n4 * 4);
+  m.massarr.resize((size_t)n4 * 4);
+  m.vcell.resize((size_t)n4);
+  if (cudaMemcpy(m.densarr.data(), d_dens, sizeof(double) * n4 * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(m.massarr.data(), d_mass, sizeof(double) * n4 * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(m.vcell.data(), d_vol, sizeof(double) * n4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(sums, d_s, sizeof(sums), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    *err = "download failed";
+    return HC3D_ERR_CUDA;
+  }
+  m.massdisk = sums[0] / kMsun;
+  m.massenv = sums[1] / kMsun;
+  m.ndg_active = 0;
+  for (int id = 0; id < m.ndg; ++id) {
+    bool any = false;
+    for (int64_t k = 0; k < n4 && !any; ++k) any = m.densarr[k + n4 * id] > 0.0;
+    if (any) m.ndg_active++;
+  }
+  return HC3D_OK;
+}
+
+}  // namespace hc3d
+
+extern "C" int hc3d_model_densities_gpu(hc3d_model* mdl, int device, double* ms, char* err, size_t errlen) {
+  if (!mdl) return HC3D_ERR_INVALID;
+  std::string e;
+  const int r = hc3d::densities_gpu(mdl->m, device, ms, &e);
+  if (r && err && errlen) std::snprintf(err, errlen, "%s", e.c_str());
+  return r;
+}

@@ -6,6 +6,7 @@
 #include "hc3d_model.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -813,6 +814,7 @@ static bool gridset(Model* m, std::string* err) {
   if (m->ifractal) fractal_field(m);
 
   // ---- densities (gridset.f90:954-1098) ----
+  const auto t_dens = std::chrono::steady_clock::now();
   m->ndg = 4;  // disk1, disk2, envelope, cavity slots; small-grain slots 5-8 are empty
   const int64_t n4 = m->n4();
   m->densarr.assign(n4 * m->ndg, 0.0);
@@ -880,6 +882,7 @@ static bool gridset(Model* m, std::string* err) {
     for (int64_t k = 0; k < n4 && !any; ++k) any = m->densarr[k + n4 * id] > 0.0;
     if (any) m->ndg_active++;
   }
+  m->density_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_dens).count();
   // initarr(.true.): tdust2 = 0.1 K, tdust = tdust2 (initarr.f90:50,78-84)
   m->tdust.assign(n4 * m->ndg, 0.1 / 11605.0);
   // ltot without accretion or ISRF (gridset.f90:165-180)
@@ -975,6 +978,7 @@ hc3d_model_info Model::info() const {
   i.np = np; i.npmin = npmin; i.np_lucy = np_lucy; i.nimin = nimin; i.nimax = nimax; i.ipeel = ipeel;
   i.ilucy = ilucy; i.ndg_active = ndg_active; i.ltot = ltot; i.tstar_k = tstar_k; i.rstar_rsun = rstar;
   i.autors = autors; i.rminsub = rminsub; i.massdisk = massdisk; i.massenv = massenv; i.ncells = ncells();
+  i.density_host_ms = density_host_ms;
   return i;
 }
 

@@ -63,6 +63,7 @@ struct Model {
   double numin = 0, numax = 0;
   double ltot = 0;
   double massdisk = 0, massenv = 0;
+  double density_host_ms = 0;  // wall time of the host density build
   int image = 1;
   int64_t maxint = 1000000;
   uint64_t seed = 0;

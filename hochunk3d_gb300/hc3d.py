@@ -125,6 +125,7 @@ class ModelInfo(C.Structure):
         ("ipeel", C.c_int), ("ilucy", C.c_int), ("ndg_active", C.c_int), ("ltot", C.c_double),
         ("tstar_k", C.c_double), ("rstar_rsun", C.c_double), ("autors", C.c_double), ("rminsub", C.c_double),
         ("massdisk", C.c_double), ("massenv", C.c_double), ("ncells", C.c_int64),
+        ("density_host_ms", C.c_double),
     ]
 
 
@@ -157,6 +158,7 @@ SIGNATURES = {
     "hc3d_model_destroy": (None, [C.c_void_p]),
     "hc3d_model_views": (C.c_int, [C.c_void_p, P(DustTables), P(Grid), P(RunParams), P(ModelInfo)]),
     "hc3d_model_set_tdust": (C.c_int, [C.c_void_p, dp]),
+    "hc3d_model_densities_gpu": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_char_p, C.c_size_t]),
     "hc3d_tts": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P(DeviceOpts), P(TtsStats), C.c_char_p, C.c_size_t]),
     "hc3d_write_synthetic_dust": (C.c_int, [C.c_char_p]),
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
@@ -288,6 +290,24 @@ class Model:
 
     def set_tdust(self, tdust: np.ndarray) -> None:
         self.tdust = np.asfortranarray(tdust, dtype=np.float64).copy(order="F")
+
+    def densities_gpu(self, device: int = 0) -> float:
+        """Recompute the densities of gridset on the GPU (hc3d_model_densities_gpu)
+        and refresh densarr, massarr, vcell and info; returns the device time in ms."""
+        L = lib()
+        ms = C.c_double(0.0)
+        err = C.create_string_buffer(1024)
+        rc = L.hc3d_model_densities_gpu(self._h, device, C.byref(ms), err, 1024)
+        if rc != 0:
+            raise Hc3dError(rc, err.value.decode())
+        t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
+        L.hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
+        n4 = g.nrg * g.ntg * g.npg
+        self.densarr = _arr(g.densarr, n4 * g.ndg).reshape(self.shape4, order="F")
+        self.massarr = _arr(g.massarr, n4 * g.ndg).reshape(self.shape4, order="F")
+        self.vcell = _arr(g.vcell, n4).reshape(self.shape3, order="F")
+        self.info = info
+        return ms.value
 
     def close(self) -> None:
         if getattr(self, "_h", None):

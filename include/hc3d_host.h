@@ -49,6 +49,7 @@ typedef struct hc3d_model_info {
   double rminsub;      /* sublimation radius, R* */
   double massdisk, massenv; /* Msun on the grid */
   int64_t ncells;      /* (nrg-1)(ntg-1)(npg-1) */
+  double density_host_ms; /* wall time of the host density build in gridset */
 } hc3d_model_info;
 
 /* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
@@ -62,6 +63,13 @@ int hc3d_model_views(hc3d_model *m, hc3d_dust_tables *tables, hc3d_grid *grid, h
 
 /* Replace the model's tdust (nrg,ntg,npg,ndg), e.g. after hc3d_lucy_update. */
 int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
+
+/* The densities of gridset (gridset.f90:954-1098: disk mass normalisation,
+ * densdisk, densenv, the fractal factor, cell volumes and (rho V)^(1/4)) on
+ * CUDA device `device`, replacing the host-built densarr, massarr, vcell and
+ * the grid masses of the model.  *ms receives the device time of the
+ * kernels. */
+int hc3d_model_densities_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
 
 typedef struct hc3d_tts_stats {
   int iterations;            /* Lucy iterations + the final one */
