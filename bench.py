@@ -371,6 +371,14 @@ def main():
         call_ms = (time.perf_counter() - t0) * 1000.0
         grid_build = {"cells": int(model.info.ncells), "host_ms": host_dens_ms, "device_kernel_ms": dev_ms,
                       "device_call_ms": call_ms, "cells_per_s": model.info.ncells / (dev_ms / 1000.0)}
+        host_tab_ms = model.info.tables_host_ms
+        model.tables_gpu(local)
+        t0 = time.perf_counter()
+        tab_ms = model.tables_gpu(local)
+        tab_call_ms = (time.perf_counter() - t0) * 1000.0
+        table_build = {"rows": int(model.nT), "intervals": int(model.nnu), "host_ms": host_tab_ms,
+                       "host_threads": min(16, os.cpu_count() or 1), "device_kernel_ms": tab_ms,
+                       "device_call_ms": tab_call_ms}
         if rank == 0:
             line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -383,7 +391,7 @@ def main():
                                "lucy_setup": f"2 iterations x {args.lucy_packets} packets"},
                     "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),
                             "d2h_bytes_per_step": int(d2h)},
-                    "fp64": fp64, "grid_build": grid_build,
+                    "fp64": fp64, "grid_build": grid_build, "table_build": table_build,
                     "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
                     "gpu_launches": launches + args.steps}
             print(json.dumps(line))

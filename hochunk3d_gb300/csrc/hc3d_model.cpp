@@ -917,6 +917,7 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
   const double numax = 32.0, numin = numax / 1024.0;
   m->nuint.resize(m->nnu);
   for (int i = 0; i < m->nnu; ++i) m->nuint[i] = numin + (double)i * (numax - numin) / (double)(m->nnu - 1);
+  const auto t_tab = std::chrono::steady_clock::now();
   m->kapBint.assign((size_t)m->nT * m->nnu * m->ndg, 0.0);
   m->kappap.assign((size_t)m->nT * m->ndg, 0.0);
   for (int id = 0; id < m->ndg; ++id) {
@@ -932,6 +933,7 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
       setemiss_species(*m, id, kb, kp);
     }
   }
+  m->tables_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tab).count();
   if (!atmosinit(m, m->atname, err)) return false;
   setup_rho0(m);
   if (!gridset(m, err)) return false;
@@ -979,6 +981,7 @@ hc3d_model_info Model::info() const {
   i.ilucy = ilucy; i.ndg_active = ndg_active; i.ltot = ltot; i.tstar_k = tstar_k; i.rstar_rsun = rstar;
   i.autors = autors; i.rminsub = rminsub; i.massdisk = massdisk; i.massenv = massenv; i.ncells = ncells();
   i.density_host_ms = density_host_ms;
+  i.tables_host_ms = tables_host_ms;
   return i;
 }
 

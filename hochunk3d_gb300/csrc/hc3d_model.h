@@ -64,6 +64,7 @@ struct Model {
   double ltot = 0;
   double massdisk = 0, massenv = 0;
   double density_host_ms = 0;  // wall time of the host density build
+  double tables_host_ms = 0;   // wall time of the host setemiss tables
   int image = 1;
   int64_t maxint = 1000000;
   uint64_t seed = 0;

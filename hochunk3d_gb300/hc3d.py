@@ -125,7 +125,7 @@ class ModelInfo(C.Structure):
         ("ipeel", C.c_int), ("ilucy", C.c_int), ("ndg_active", C.c_int), ("ltot", C.c_double),
         ("tstar_k", C.c_double), ("rstar_rsun", C.c_double), ("autors", C.c_double), ("rminsub", C.c_double),
         ("massdisk", C.c_double), ("massenv", C.c_double), ("ncells", C.c_int64),
-        ("density_host_ms", C.c_double),
+        ("density_host_ms", C.c_double), ("tables_host_ms", C.c_double),
     ]
 
 
@@ -159,6 +159,7 @@ SIGNATURES = {
     "hc3d_model_views": (C.c_int, [C.c_void_p, P(DustTables), P(Grid), P(RunParams), P(ModelInfo)]),
     "hc3d_model_set_tdust": (C.c_int, [C.c_void_p, dp]),
     "hc3d_model_densities_gpu": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_char_p, C.c_size_t]),
+    "hc3d_model_tables_gpu": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_char_p, C.c_size_t]),
     "hc3d_tts": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P(DeviceOpts), P(TtsStats), C.c_char_p, C.c_size_t]),
     "hc3d_write_synthetic_dust": (C.c_int, [C.c_char_p]),
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
@@ -307,6 +308,21 @@ class Model:
         self.massarr = _arr(g.massarr, n4 * g.ndg).reshape(self.shape4, order="F")
         self.vcell = _arr(g.vcell, n4).reshape(self.shape3, order="F")
         self.info = info
+        return ms.value
+
+    def tables_gpu(self, device: int = 0) -> float:
+        """Recompute the setemiss tables kapBint and kappap on the GPU
+        (hc3d_model_tables_gpu) and refresh them; returns the device time in ms."""
+        L = lib()
+        ms = C.c_double(0.0)
+        err = C.create_string_buffer(1024)
+        rc = L.hc3d_model_tables_gpu(self._h, device, C.byref(ms), err, 1024)
+        if rc != 0:
+            raise Hc3dError(rc, err.value.decode())
+        t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
+        L.hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
+        self.kapBint = _arr(t.kapBint, t.nT * t.nnu * t.ndg)
+        self.kappap = _arr(t.kappap, t.nT * t.ndg)
         return ms.value
 
     def close(self) -> None:

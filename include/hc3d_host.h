@@ -50,6 +50,7 @@ typedef struct hc3d_model_info {
   double massdisk, massenv; /* Msun on the grid */
   int64_t ncells;      /* (nrg-1)(ntg-1)(npg-1) */
   double density_host_ms; /* wall time of the host density build in gridset */
+  double tables_host_ms;  /* wall time of the host setemiss tables */
 } hc3d_model_info;
 
 /* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
@@ -70,6 +71,12 @@ int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
  * the grid masses of the model.  *ms receives the device time of the
  * kernels. */
 int hc3d_model_densities_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
+
+/* setemiss (dust.f90:394-474: the cumulative emissivity tables kapBint and
+ * the Planck-mean factors kappap of every distinct dust table) on CUDA device
+ * `device`, replacing the host-built kapBint and kappap of the model.  *ms
+ * receives the device time of the kernels. */
+int hc3d_model_tables_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
 
 typedef struct hc3d_tts_stats {
   int iterations;            /* Lucy iterations + the final one */

@@ -1,7 +1,8 @@
-"""The densities of gridset built on the GPU (hc3d_model_densities_gpu)
-against the host build of the same model: densities, (rho V)^(1/4), cell
-volumes and grid masses agree to rounding, and the cells without dust are
-the same cells."""
+"""The model set-up built on the GPU against the host build of the same
+model: the densities of gridset (hc3d_model_densities_gpu) -- densities,
+(rho V)^(1/4), cell volumes and grid masses agree to rounding and the cells
+without dust are the same cells -- and the setemiss tables
+(hc3d_model_tables_gpu)."""
 from __future__ import annotations
 
 import numpy as np
@@ -29,3 +30,20 @@ def test_device_densities_match_host(tmp_path, built, name):
     d1 = m.densarr.copy()
     m.densities_gpu(0)
     np.testing.assert_array_equal(m.densarr, d1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tiny", "plain"])
+def test_device_tables_match_host(tmp_path, built, name):
+    """setemiss on the GPU (hc3d_model_tables_gpu): the cumulative emissivity
+    rows and the Planck-mean factors of the host build, to rounding."""
+    m = make_model(tmp_path / name, name, warm=False)
+    kb, kp = m.kapBint.copy(), m.kappap.copy()
+    ms = m.tables_gpu(0)
+    assert ms > 0.0
+    assert np.all(np.isfinite(m.kapBint)) and np.all(m.kappap > 0.0)
+    np.testing.assert_allclose(m.kappap, kp, rtol=1e-11, atol=0.0)
+    np.testing.assert_allclose(m.kapBint, kb, rtol=1e-11, atol=1e-300)
+    rows = m.kapBint.reshape(m.nT, m.nnu, -1, order="F")
+    assert np.all(rows[:, -1, :] == 1.0)
+    assert np.all(np.diff(rows, axis=1) >= 0.0)
