@@ -3,9 +3,9 @@
 The reference's shipped ``mctherm.par`` lacks keys that ``reapar`` requires
 (NXIMG, RMAXD(1..2), RMIND(1..2), CDISKCURV, ...), so the models here are
 written out in full.  Dust and stellar-spectrum inputs are synthetic fixtures
-written by the library (``hc3d_write_synthetic_dust`` and
-``hc3d_write_wavelength_grid``): the dust files the reference names are not
-shipped.
+written by the library (``hc3d_write_synthetic_dust``,
+``hc3d_write_wavelength_grid`` and ``hc3d_write_synthetic_isrf``): the dust
+files the reference names are not shipped.
 
 Models:
   plain   -- the plain small model: star 4000 K, 2 Rsun; flared disk
@@ -21,6 +21,8 @@ Models:
              1e8 packets.
   tiny    -- a small grid of the plain model for CPU parity tests.
   tiny3d  -- a small 3-D grid (with azimuthal walls) for CPU parity tests.
+  tiny_isrf -- tiny with external illumination (COUTILLUM=YES, a synthetic
+             field of three diluted blackbodies, ISRF_SCL 10).
 """
 from __future__ import annotations
 
@@ -29,6 +31,7 @@ from pathlib import Path
 
 DUST_FILE = "synth_dust.par"
 WAVE_FILE = "synth_wavegrid.ascii"
+ISRF_FILE = "synth_isrf.dat"
 
 
 def _inclinations(n: int) -> list[float]:
@@ -101,6 +104,10 @@ CONFIGS = {
              "CPEEL": "NO", "NPMIN": 100000000},
     "tiny": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 2, "NXIMG": 31,
              "MASSD": 0.0001, "RATE": 5e-7},
+    # tiny with external illumination: ISRF_SCL 10 gives the outside field
+    # about 40 % of the luminosity
+    "tiny_isrf": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 2, "NXIMG": 31,
+                  "MASSD": 0.0001, "RATE": 5e-7, "COUTILLUM": "YES", "ISRF_SCL": 10.0, "ISRF_FILE": ISRF_FILE},
     "tiny3d": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 9, "NXIMG": 31,
                "MASSD": 0.0001, "RATE": 5e-7, "NPEEL": 4, "THETE": "30.013,60.013,80.013,120.013",
                "PHIE": "0.0,90.0,180.0,270.0", "CFRACTAL": "YES", "FRACTLEV": 2, "FRACTN": 8},
@@ -127,6 +134,9 @@ def write_fixtures(directory: str | Path) -> Path:
     rc = L.hc3d_write_wavelength_grid(str(d / WAVE_FILE).encode(), 4000.0)
     if rc != 0:
         raise hc3d.Hc3dError(rc, "cannot write wavelength fixture")
+    rc = L.hc3d_write_synthetic_isrf(str(d / ISRF_FILE).encode())
+    if rc != 0:
+        raise hc3d.Hc3dError(rc, "cannot write external-field fixture")
     return d
 
 

@@ -260,6 +260,15 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   for (int s = 0; s < kSlots; ++s) a->kapfac[s] = (float)(p->rstar_cm * c->kappav[s]);
   a->iintmax = p->iintmax > 0 ? p->iintmax : 10000;
   a->max_interactions = p->max_interactions;
+  if (p->ext_illum) {
+    if (c->dm.nisrf < 2)
+      return fail(c, HC3D_ERR_INVALID, "ext_illum needs the external-illumination tables (nisrf) of hc3d_load_tables");
+    if (!(p->rmax > 1.0)) return fail(c, HC3D_ERR_INVALID, "ext_illum needs rmax > 1 (stellar radii)");
+    if (p->n_star < 0) return fail(c, HC3D_ERR_INVALID, "n_star < 0");
+  }
+  a->ext_illum = p->ext_illum ? 1 : 0;
+  a->n_star = p->n_star;
+  a->rmax = p->rmax;
   a->peeldir = c->d_peeldir;
   a->aperture2 = c->d_ap2;
   a->work = c->d_work;
@@ -521,6 +530,18 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
   c->dm.nudust = d_nud; c->dm.kappad = d_kap; c->dm.adust = d_alb; c->dm.gdust = d_g; c->dm.pldust = d_pl;
   c->dm.nT = t->nT; c->dm.nnu = t->nnu; c->dm.lTint = d_lT; c->dm.nuint = d_nuint; c->dm.kapBint = d_kB;
   c->dm.nhnu = t->nhnu; c->dm.hnuint = d_hn; c->dm.atmosnu = d_an; c->dm.lognu = d_ln; c->dm.loghnu = d_lh;
+  // external radiation field (isrf_mod), FP64 in both forms: one draw per external packet
+  c->dm.nisrf = 0;
+  if (t->nisrf > 0) {
+    if (t->nisrf < 2 || !t->isrf_cdf || !t->isrf_logcdf || !t->isrf_logfreq)
+      return fail(c, HC3D_ERR_INVALID, "external-illumination tables: nisrf < 2 or a NULL pointer");
+    double *d_ic, *d_il, *d_if;
+    if ((r = dupload(c, own, &d_ic, t->isrf_cdf, (size_t)t->nisrf)) ||
+        (r = dupload(c, own, &d_il, t->isrf_logcdf, (size_t)t->nisrf)) ||
+        (r = dupload(c, own, &d_if, t->isrf_logfreq, (size_t)t->nisrf)))
+      return r;
+    c->dm.nisrf = t->nisrf; c->dm.isrf_cdf = d_ic; c->dm.isrf_logcdf = d_il; c->dm.isrf_logfreq = d_if;
+  }
   // FP32 copies for the mixed form
   {
     auto f32 = [](const double* p, size_t n) { return std::vector<float>(p, p + n); };

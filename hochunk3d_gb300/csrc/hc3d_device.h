@@ -80,6 +80,8 @@ struct DevModel {
   const double* lTint; const double* nuint; const double* kapBint;  // kapBint (nT,nnu,kSlots)
   int nhnu;
   const double* hnuint; const double* atmosnu; const double* lognu; const double* loghnu;
+  int nisrf;  // external radiation field (isrf_mod): cdf_i, logcdf_i, logfreq_i; 0 = none
+  const double* isrf_cdf; const double* isrf_logcdf; const double* isrf_logfreq;
   // FP32 copies of the per-event tables, read by the mixed form
   const float* nudustf; const float* kappadf; const float* adustf; const float* gdustf; const float* pldustf;
   const float* lTintf; const float* nuintf; const float* kapBintf;
@@ -107,6 +109,9 @@ struct RunArgs {
   float kapfac[kSlots];      // rstar_cm * kappa_V of each slot, FP32 (mixed-form opacities)
   int iintmax;
   int64_t max_interactions;
+  int ext_illum;             // packets with global id >= n_star enter from the outer sphere
+  int64_t n_star;
+  double rmax;               // outer radius, R*
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
   const double* aperture2;   // [nap]
   unsigned long long* work;  // packet counter

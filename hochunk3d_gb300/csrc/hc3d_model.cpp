@@ -506,6 +506,118 @@ static void fractal_field(Model* m) {
     if (!(call)) return false; \
   } while (0)
 
+// isrf_cdf (isrf_cdf.f90:1-243): the external radiation field on 200
+// log-spaced wavelengths inside the table's range (clamped to 0.05-5000 um),
+// log-log interpolated, reddened by ISRF_AV magnitudes of the extinction law
+// r400_ice095.par (read only when ISRF_AV is not zero), integrated by the
+// trapezoid rule in frequency, normalised, and the frequencies converted to
+// units of 1.2398/lambda[um].  Row 1 keeps its frequency in Hz with
+// logcdf = -99 and logfreq = 0, as the Fortran leaves them.
+static bool isrf_cdf(Model* m, std::string* err) {
+  const double c = 2.99792458e14;  // um Hz
+  std::vector<double> lnu, nufnu;
+  {
+    FILE* f = std::fopen(m->isrf_file.c_str(), "r");
+    if (!f) { *err = "cannot open ISRF_FILE " + m->isrf_file; return false; }
+    char line[512];
+    while (std::fgets(line, sizeof line, f)) {
+      double a, b;
+      if (line[0] == '#') continue;
+      if (std::sscanf(line, "%lf %lf", &a, &b) == 2) { lnu.push_back(a); nufnu.push_back(b); }
+    }
+    std::fclose(f);
+  }
+  const int nin = (int)lnu.size();
+  if (nin < 2) { *err = "ISRF_FILE " + m->isrf_file + " has fewer than two rows"; return false; }
+  for (int i = 1; i < nin; ++i)
+    if (!(lnu[i] > lnu[i - 1])) { *err = "ISRF_FILE frequencies must increase"; return false; }
+  std::vector<double> freqin(nin), logfreqin(nin), logpdfin(nin);
+  for (int i = 0; i < nin; ++i) {
+    freqin[i] = std::pow(10.0, lnu[i]);
+    const double pdf = std::pow(10.0, nufnu[i]) / freqin[i];
+    logfreqin[i] = std::log10(freqin[i]);
+    logpdfin[i] = std::log10(pdf);
+  }
+  double lmin = c / (freqin[nin - 1] * 0.99999999), lmax = c / (freqin[0] * 1.0000001);
+  if (lmin < 0.05) lmin = 0.05;
+  if (lmax > 5000.0) lmax = 5000.0;
+  const int n = kNisrf;
+  std::vector<double> freq(n), pdf(n), cdf(n), logcdf(n), logfreq(n);
+  for (int i = 1; i <= n; ++i) {
+    const double lam = lmin * std::pow(lmax / lmin, (double)i / (double)n);
+    freq[n - i] = c / lam;
+  }
+  // extinction law: columns lam, -, -, kappa (isrf_cdf.f90:120-134)
+  std::vector<double> fext, kext;
+  double kapvext = 1.0;
+  if (m->isrf_av != 0.0) {
+    const std::string path = m->pardir + "/r400_ice095.par";
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) { *err = "ISRF_AV is not zero and the extinction law " + path + " cannot be opened"; return false; }
+    char line[512];
+    while (std::fgets(line, sizeof line, f)) {
+      double lam, j1, j2, kap;
+      if (std::sscanf(line, "%lf %lf %lf %lf", &lam, &j1, &j2, &kap) == 4) { fext.push_back(c / lam); kext.push_back(kap); }
+    }
+    std::fclose(f);
+    if (fext.size() < 2) { *err = "extinction law " + path + " has fewer than two rows"; return false; }
+    std::reverse(fext.begin(), fext.end());
+    std::reverse(kext.begin(), kext.end());
+  }
+  auto locate = [](const std::vector<double>& xx, int nn, double x) {  // nr.f locate2 on xx[0..nn)
+    int jl = 0, ju = nn + 1;
+    const bool asc = xx[nn - 1] > xx[0];
+    while (ju - jl > 1) {
+      const int jm = (ju + jl) / 2;
+      if (asc == (x > xx[jm - 1])) jl = jm; else ju = jm;
+    }
+    return jl;
+  };
+  const int next = (int)fext.size();
+  if (next >= 2) {
+    const double fv = c / 0.55;
+    const int j = locate(fext, next, fv);
+    if (j < 1 || j >= next) { *err = "extinction law does not cover 0.55 um"; return false; }
+    kapvext = kext[j - 1] + (fv - fext[j - 1]) / (fext[j] - fext[j - 1]) * (kext[j] - kext[j - 1]);
+  }
+  for (int i = 0; i < n; ++i) {
+    const double fq = freq[i];
+    double ext = 1.0;
+    if (next >= 2) {
+      int j = locate(fext, next, fq);
+      if (j == 0 && fq == fext[0]) j = 1;
+      double kt;
+      if (j == next) kt = kext[next - 1];
+      else if (j == 0) kt = kext[0];
+      else kt = kext[j - 1] + (fq - fext[j - 1]) / (fext[j] - fext[j - 1]) * (kext[j] - kext[j - 1]);
+      ext = std::exp(-kt / kapvext / 1.086 * m->isrf_av);
+    }
+    int j = locate(freqin, nin, fq);
+    if (j < 1) j = 1;
+    if (j > nin - 1) j = nin - 1;
+    const double lp = logpdfin[j - 1] + (std::log10(fq) - logfreqin[j - 1]) / (logfreqin[j] - logfreqin[j - 1]) *
+                                            (logpdfin[j] - logpdfin[j - 1]);
+    pdf[i] = std::pow(10.0, lp) * ext;
+  }
+  cdf[0] = 0.0;
+  for (int i = 1; i < n; ++i) cdf[i] = cdf[i - 1] + 0.5 * (pdf[i] + pdf[i - 1]) * (freq[i] - freq[i - 1]);
+  m->isrf_int = cdf[n - 1];
+  if (!(m->isrf_int > 0.0)) { *err = "ISRF_FILE integrates to zero"; return false; }
+  cdf[0] = 0.0;
+  logcdf[0] = -99.0;
+  logfreq[0] = 0.0;
+  for (int i = 1; i < n; ++i) {
+    cdf[i] = cdf[i] / cdf[n - 1];
+    logcdf[i] = std::log10(cdf[i]);
+    freq[i] = freq[i] * 1.2398 / c;
+    logfreq[i] = std::log10(freq[i]);
+  }
+  m->isrf_cdfv = cdf;
+  m->isrf_logcdf = logcdf;
+  m->isrf_logfreq = logfreq;
+  return true;
+}
+
 static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std::string* err) {
   int64_t iv;
   double dv;
@@ -521,8 +633,16 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   else { REQ(P.integer("I1", &iv, err)); m->seed = (uint64_t)(iv < 0 ? -iv : iv); }
   REQ(P.str("PARDIR", &m->pardir, err));
   if (par_dir) m->pardir = *par_dir;
-  REQ(P.integer("COUTILLUM", &iv, err));
-  if (iv != 0) { *err = "COUTILLUM=YES (external illumination) is not supported"; return false; }
+  REQ(P.integer("COUTILLUM", &iv, err)); m->iout = (int)iv;
+  if (m->iout) {
+    REQ(P.real("ISRF_SCL", &m->isrf_scl, err));
+    REQ(P.real("ISRF_AV", &m->isrf_av, err));
+    if (!P.has("ISRF_FILE")) {
+      *err = "COUTILLUM=YES needs ISRF_FILE (the external radiation field, log10 nu and log10 nu*F_nu per line)";
+      return false;
+    }
+    REQ(P.str("ISRF_FILE", &sv, err)); m->isrf_file = m->pardir + "/" + sv;
+  }
   REQ(P.integer("CLIMB", &iv, err)); m->limb = (int)iv;
   if (m->limb != 0) { *err = "CLIMB=YES (limb-darkening table) is not supported"; return false; }
   REQ(P.integer("CPLANCKST", &iv, err)); m->iplanckst = (int)iv;
@@ -885,8 +1005,12 @@ static bool gridset(Model* m, std::string* err) {
   m->density_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_dens).count();
   // initarr(.true.): tdust2 = 0.1 K, tdust = tdust2 (initarr.f90:50,78-84)
   m->tdust.assign(n4 * m->ndg, 0.1 / 11605.0);
-  // ltot without accretion or ISRF (gridset.f90:165-180)
-  m->ltot = 4.0 * kPi * kSigt * std::pow(m->tstar_k, 4.0) * rmincgs * rmincgs;
+  // luminosities without accretion (gridset.f90:206-209); l_isrf of
+  // newtts.F90:207 with rmax in stellar radii
+  m->lstar = 4.0 * kPi * kSigt * std::pow(m->tstar_k, 4.0) * rmincgs * rmincgs;
+  m->l_isrf = m->iout ? m->isrf_int * 4.0 * kPi * std::pow(m->rmax * kRsun * m->rstar, 2.0) / 4.0 * m->isrf_scl : 0.0;
+  m->ltot = m->lstar + m->l_isrf;
+  m->isrf_frac = m->l_isrf / m->ltot;
   // Lucy packets per iteration (newtts.F90:159-182)
   const int64_t ncells = m->ncells();
   int64_t npl = (ntg < 10 && npg < 10) ? 100 * ncells : (int64_t)(3.0 * (double)ncells);
@@ -935,6 +1059,7 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
   }
   m->tables_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tab).count();
   if (!atmosinit(m, m->atname, err)) return false;
+  if (m->iout && !isrf_cdf(m, err)) return false;
   setup_rho0(m);
   if (!gridset(m, err)) return false;
   return true;
@@ -950,6 +1075,10 @@ hc3d_dust_tables Model::tables_view() const {
   t.kapBint = kapBint.data(); t.kappap = kappap.data(); t.tsub = tsub_k;
   t.nhnu = (int)hnuint.size(); t.hnuint = hnuint.data(); t.atmosnu = atmosnu.data();
   t.lognu = lognu.data(); t.loghnu = loghnu.data();
+  if (iout) {
+    t.nisrf = (int)isrf_cdfv.size(); t.isrf_cdf = isrf_cdfv.data(); t.isrf_logcdf = isrf_logcdf.data();
+    t.isrf_logfreq = isrf_logfreq.data();
+  }
   return t;
 }
 
@@ -971,6 +1100,7 @@ hc3d_run_params Model::params_view() const {
   p.nxhst = nxhst; p.rmaxi = rmaxi; p.aperture2 = aperture2.data(); p.numin = numin; p.numax = numax;
   p.rstar_cm = rstar * kRsun; p.tstar = tstar_k / 11605.0; p.limb = limb; p.iintmax = 10000;
   p.max_interactions = maxint; p.image = image;
+  p.ext_illum = iout; p.n_star = hc3d_star_packets(isrf_frac, np); p.rmax = rmax;
   return p;
 }
 
@@ -982,6 +1112,7 @@ hc3d_model_info Model::info() const {
   i.autors = autors; i.rminsub = rminsub; i.massdisk = massdisk; i.massenv = massenv; i.ncells = ncells();
   i.density_host_ms = density_host_ms;
   i.tables_host_ms = tables_host_ms;
+  i.lstar = lstar; i.l_isrf = l_isrf; i.isrf_frac = isrf_frac;
   return i;
 }
 
@@ -1040,6 +1171,21 @@ extern "C" int hc3d_model_set_tdust(hc3d_model* m, const double* tdust) {
   return HC3D_OK;
 }
 
+extern "C" int64_t hc3d_star_packets(double isrf_frac, int64_t np) {
+  // newdisktherm.F90:143-175 with accfrac = 0: npout and ns rounded to the
+  // nearest packet (ns from the single-precision real(np)), then ns takes up
+  // the difference
+  int64_t npout = (int64_t)(isrf_frac * (double)np);
+  double rn = isrf_frac * (double)np;
+  if (rn - (double)npout > 0.5) npout += 1;
+  int64_t ns = (int64_t)((double)np * (1.0 - isrf_frac));
+  rn = (double)(float)np * (1.0 - isrf_frac);
+  if (rn - (double)ns > 0.5) ns += 1;
+  const int64_t nsum = ns + npout;
+  if (nsum != np) ns = ns + np - nsum;
+  return ns;
+}
+
 // Fixture writers ------------------------------------------------------------
 extern "C" int hc3d_write_synthetic_dust(const char* path) {
   // kappa: kV*(0.55/lam) below 100 um, continued as lam^-1.7 beyond, flat
@@ -1058,6 +1204,30 @@ extern "C" int hc3d_write_synthetic_dust(const char* path) {
     double alb = 0.5 * (1.0 - x), g = 0.6 * (1.0 - x);
     double cext = kap * 1.0e-22;
     std::fprintf(f, " %.6e %.6e %.6e %.6e %.6e %.6e %.6e\n", lam, cext, alb * cext, kap, g, 0.5, 0.0);
+  }
+  std::fclose(f);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_write_synthetic_isrf(const char* path) {
+  // three diluted blackbodies of the Mathis, Mezger & Panagia (1983) form,
+  // nu F_nu = sum W_i 4 pi nu B_nu(T_i), (T_i, W_i) = (7500 K, 1e-14),
+  // (4000 K, 1.65e-13), (3000 K, 4e-13); 44 frequencies, log-spaced over
+  // 10^11.45 .. 10^15.55 Hz
+  FILE* f = std::fopen(path, "w");
+  if (!f) return HC3D_ERR_IO;
+  const double h = 6.62607015e-27, k = 1.380649e-16, c = 2.99792458e10;
+  const double T[3] = {7500.0, 4000.0, 3000.0}, W[3] = {1.0e-14, 1.65e-13, 4.0e-13};
+  std::fprintf(f, "# synthetic external radiation field: log10 nu[Hz]  log10 nu*F_nu[erg/s/cm^2]\n");
+  const int n = 44;
+  for (int i = 0; i < n; ++i) {
+    const double lnu = 11.45 + (15.55 - 11.45) * i / (double)(n - 1), nu = std::pow(10.0, lnu);
+    double s = 0.0;
+    for (int q = 0; q < 3; ++q) {
+      const double x = h * nu / (k * T[q]);
+      if (x < 700.0) s += W[q] * 4.0 * hc3d::kPi * nu * (2.0 * h * nu * nu * nu / (c * c)) / std::expm1(x);
+    }
+    std::fprintf(f, " %.4f  %.4f\n", lnu, std::log10(std::max(s, 1.0e-300)));
   }
   std::fclose(f);
   return HC3D_OK;

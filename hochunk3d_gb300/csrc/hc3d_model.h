@@ -41,6 +41,8 @@ class ParFile {
   std::map<std::string, std::string> kv_;
 };
 
+constexpr int kNisrf = 200;  // isrf_mod nisrf
+
 struct Model {
   // ---- reapar/setup scalars (units after setup.f90) ----
   int64_t np = 0, npmin = 0, np_lucy = 0;
@@ -65,6 +67,12 @@ struct Model {
   double massdisk = 0, massenv = 0;
   double density_host_ms = 0;  // wall time of the host density build
   double tables_host_ms = 0;   // wall time of the host setemiss tables
+  // external illumination (COUTILLUM, ISRF_SCL, ISRF_AV; isrf_mod)
+  int iout = 0;
+  double isrf_scl = 1.0, isrf_av = 0.0, isrf_int = 0.0;
+  double lstar = 0, l_isrf = 0, isrf_frac = 0;
+  std::string isrf_file;
+  std::vector<double> isrf_cdfv, isrf_logcdf, isrf_logfreq;
   int image = 1;
   int64_t maxint = 1000000;
   uint64_t seed = 0;

@@ -1127,12 +1127,14 @@ __device__ __forceinline__ void stokespeel(R g, R pl, R& sip, R& sqp, R& sup, R&
 // state at a scattering (before stokes), at a re-emission (after reemit) or at
 // its emission from the stellar surface.  Peel-off rays draw no random numbers,
 // so they can run after the event, in any order and on any thread.
+constexpr int kRecNoPeel = 1 << 15;  // PeelRec flag: the event has no peel-off rays
+
 template <class R>
 struct PeelRec {
   typename PosOf<R>::T x, y, z;
   int ir, it, ip;
   int flags;  // bit0 on_wall, bit1 scattered, bits2-4 i_orig, bits5-6 idust2, bit7 stellar-surface emission,
-              // bits8-10 id of the wall the event sits on
+              // bits8-14 walls the event sits on, bit15 no peel-off (kRecNoPeel)
   int inub;
   R sip, sqp, sup, svp;
   R d0, d1, d2, d3, d4;  // scattered: cost, sint, phi, cosp, sinp of the incident packet; stellar: cosb, sinb, coslp, sinlp
@@ -1189,6 +1191,7 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   const int flags = e.flags;
   const int iflag = (flags >> 1) & 1;
   const int i_orig = (flags >> 2) & 7;
+  if (flags & kRecNoPeel) return;
   R sip = e.sip, sqp = e.sqp, sup = e.sup, svp = e.svp;
   if (flags & 128) {
     // newdisktherm.F90:342-360: limb = 0 weight of a stellar-surface packet
@@ -1367,6 +1370,7 @@ struct PeelWalk {
   // false when the ray is not walked (the star's far side, or it enters the star)
   __device__ __forceinline__ bool start(const DevModel& m, const PeelRec<float>& r, const PeelDir& dd) {
     const int flags = r.flags;
+    if (flags & kRecNoPeel) return false;
     if (flags & 128) {  // newdisktherm.F90:342-360: the star's surface faces the observer
       const float cosnorm = r.d0 * dd.coste + (r.d1 * dd.sinte * (dd.cospe * r.d2 + dd.sinpe * r.d3));
       if (!(cosnorm > 0.f)) return false;
@@ -1717,27 +1721,10 @@ struct Flow {
 
 enum { ST_DONE = 0, ST_INTERACT = 1 };
 
-// Stellar packet emission, newdisktherm.F90:256-337 with initpspot (spot-free),
-// initp_sample (limb = 0) and initp_transform (initp_common.f90:1-94).  rec
-// receives the stellar-surface peel-off event.
+// initp_transform (initp_common.f90:31-94): the direction (cost, phi) drawn
+// in the frame of the surface point (cosb, lp), rotated into the grid frame
 template <class R>
-__device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
-  p.on_wall = 0;
-  p.safe = 0.f;
-  p.lrow.key = -1;
-  p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
-  for (;;) {
-    const R xran = ran<R>(rng);
-    p.cosb = R(1) - R(2) * xran;
-    p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
-    if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
-  }
-  p.lp = (R)kR2p * ran<R>(rng);
-  p.cost = xsqrt(ran<R>(rng));
-  p.sint = xsqrt(R(1) - p.cost * p.cost);
-  p.phi = (R)kR2p * ran<R>(rng);
-  p.cosp = xcos(p.phi);
-  p.sinp = xsin(p.phi);
+__device__ __forceinline__ void initp_transform(Pkt<R>& p) {
   if (xabs(p.cosb) < R(0.9999999)) {
     R costi = p.cost * p.cosb - p.sint * p.sinb * p.cosp;
     if (xabs(costi) > R(1)) {
@@ -1768,6 +1755,31 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   if (p.phi < R(0)) p.phi += (R)kR2p;
   p.sinp = xsin(p.phi);
   p.cosp = xcos(p.phi);
+}
+
+// Stellar packet emission, newdisktherm.F90:256-337 with initpspot (spot-free),
+// initp_sample (limb = 0) and initp_transform.  rec receives the
+// stellar-surface peel-off event.
+template <class R>
+__device__ void emit_star(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                          PeelRec<R>& rec, Tracer& tr) {
+  p.on_wall = 0;
+  p.safe = 0.f;
+  p.lrow.key = -1;
+  p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+  for (;;) {
+    const R xran = ran<R>(rng);
+    p.cosb = R(1) - R(2) * xran;
+    p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
+    if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
+  }
+  p.lp = (R)kR2p * ran<R>(rng);
+  p.cost = xsqrt(ran<R>(rng));
+  p.sint = xsqrt(R(1) - p.cost * p.cost);
+  p.phi = (R)kR2p * ran<R>(rng);
+  p.cosp = xcos(p.phi);
+  p.sinp = xsin(p.phi);
+  initp_transform<R>(p);
   p.nub = atmosfreq<R>(m, rng);
   p.i_orig = 1;
   opacset<R>(m, dv, p, p.nub, a);
@@ -1786,6 +1798,72 @@ __device__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a,
   tr.add(0, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   make_rec<R>(rec, p, a, 0, 0, 128);
   rec.d0 = p.cosb; rec.d1 = p.sinb; rec.d2 = coslp; rec.d3 = sinlp;
+}
+
+// rep_isrf (rep_isrf.f90:1-41): the frequency of an external packet, by
+// log-log interpolation in the cumulative distribution of the external field
+// (FP64 in both forms: one draw per external packet)
+template <class R>
+__device__ __forceinline__ R rep_isrf(const DevModel& m, Rng& rng) {
+  const double xran = (double)ran<R>(rng);
+  const int n = m.nisrf;
+  int i = locate_dev(m.isrf_cdf, n, xran);
+  if (i == n) i = n - 1;
+  if (i == 0) i = 1;
+  const double lc0 = __ldg(m.isrf_logcdf + i - 1), lc1 = __ldg(m.isrf_logcdf + i);
+  const double lf0 = __ldg(m.isrf_logfreq + i - 1), lf1 = __ldg(m.isrf_logfreq + i);
+  return (R)pow(10.0, lf0 + (log10(xran) - lc0) / (lc1 - lc0) * (lf1 - lf0));
+}
+
+// External packet, newdisktherm.F90:378-440 with initpout (initpout.f90:3-66):
+// a point on the sphere of 0.999999 rmax, a direction drawn inwards with
+// cost = -sqrt(xi) in the frame of that point, the frequency from the
+// external field.  The packet starts inside the outermost shell (not on a
+// wall).  It has no direct peel-off (the Fortran leaves it commented out, so
+// that the unprocessed background is not imaged): rec is marked empty.
+template <class R>
+__device__ void emit_external(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                              PeelRec<R>& rec, Tracer& tr) {
+  p.on_wall = 0;
+  p.safe = 0.f;
+  p.lrow.key = -1;
+  p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+  p.cosb = R(1) - R(2) * ran<R>(rng);
+  p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
+  p.cost = -xsqrt(ran<R>(rng));
+  p.sint = xsqrt(R(1) - p.cost * p.cost);
+  p.phi = (R)kR2p * ran<R>(rng);
+  p.cosp = xcos(p.phi);
+  p.sinp = xsin(p.phi);
+  p.lp = (R)kR2p * ran<R>(rng);
+  initp_transform<R>(p);
+  p.nub = rep_isrf<R>(m, rng);
+  p.i_orig = 4;
+  opacset<R>(m, dv, p, p.nub, a);
+  const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
+  const double zp = (double)p.cosb * a.rmax * 0.999999, rp_ = (double)p.sinb * a.rmax * 0.999999;
+  set_pos(p.z, zp);
+  set_pos(p.x, rp_ * (double)coslp);
+  set_pos(p.y, rp_ * (double)sinlp);
+  p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
+  p.ir = m.nrg - 1;
+  p.it = locate_dev(m.thetarr, m.ntg, acos((double)p.cosb));
+  p.ip = locate_dev(m.phiarr, m.npg, (double)p.lp);
+  p.it = p.it < 1 ? 1 : (p.it > m.ntg - 1 ? m.ntg - 1 : p.it);
+  p.ip = p.ip < 1 ? 1 : (p.ip > m.npg - 1 ? m.npg - 1 : p.ip);
+  tr.add(0, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
+  make_rec<R>(rec, p, a, 0, 0, kRecNoPeel);
+}
+
+// A new packet: stellar, or from outside when external illumination is on and
+// its global id is past the stellar share (newdisktherm.F90:207-260: the
+// Fortran numbers the stellar packets first)
+template <class R>
+__device__ __forceinline__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                                     PeelRec<R>& rec, Tracer& tr) {
+  const int64_t pid = (int64_t)((uint64_t)rng.c2 | ((uint64_t)rng.c3 << 32));
+  if (a.ext_illum && pid >= a.n_star) emit_external<R>(m, dv, a, p, rng, rec, tr);
+  else emit_star<R>(m, dv, a, p, rng, rec, tr);
 }
 
 __device__ __forceinline__ void set_status(const RunArgs& a, int code) {

@@ -64,6 +64,7 @@ class DustTables(C.Structure):
         ("nudust", dp), ("kappad", dp), ("adust", dp), ("gdust", dp), ("pldust", dp), ("kappav", dp),
         ("nT", C.c_int), ("nnu", C.c_int), ("lTint", dp), ("nuint", dp), ("kapBint", dp), ("kappap", dp),
         ("tsub", C.c_double), ("nhnu", C.c_int), ("hnuint", dp), ("atmosnu", dp), ("lognu", dp), ("loghnu", dp),
+        ("nisrf", C.c_int), ("isrf_cdf", dp), ("isrf_logcdf", dp), ("isrf_logfreq", dp),
     ]
 
 
@@ -84,6 +85,7 @@ class RunParams(C.Structure):
         ("rmaxi", C.c_double), ("aperture2", dp), ("numin", C.c_double), ("numax", C.c_double),
         ("rstar_cm", C.c_double), ("tstar", C.c_double), ("limb", C.c_int), ("iintmax", C.c_int),
         ("max_interactions", C.c_int64), ("image", C.c_int),
+        ("ext_illum", C.c_int), ("n_star", C.c_int64), ("rmax", C.c_double),
     ]
 
 
@@ -126,6 +128,7 @@ class ModelInfo(C.Structure):
         ("tstar_k", C.c_double), ("rstar_rsun", C.c_double), ("autors", C.c_double), ("rminsub", C.c_double),
         ("massdisk", C.c_double), ("massenv", C.c_double), ("ncells", C.c_int64),
         ("density_host_ms", C.c_double), ("tables_host_ms", C.c_double),
+        ("lstar", C.c_double), ("l_isrf", C.c_double), ("isrf_frac", C.c_double),
     ]
 
 
@@ -163,6 +166,8 @@ SIGNATURES = {
     "hc3d_tts": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P(DeviceOpts), P(TtsStats), C.c_char_p, C.c_size_t]),
     "hc3d_write_synthetic_dust": (C.c_int, [C.c_char_p]),
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
+    "hc3d_write_synthetic_isrf": (C.c_int, [C.c_char_p]),
+    "hc3d_star_packets": (C.c_int64, [C.c_double, C.c_int64]),
 }
 
 _LIB = None
@@ -202,6 +207,11 @@ def tally_scales(np_: int) -> tuple[float, float, float]:
     sb = max(16, min(40, 58 - L))
     pb = max(12, min(32, 52 - L))
     return math.ldexp(1.0, sb), math.ldexp(1.0, sb - 8), math.ldexp(1.0, pb)
+
+
+def star_packets(isrf_frac: float, np_: int) -> int:
+    """Stellar packets of an iteration of np_ packets (hc3d_star_packets)."""
+    return int(lib().hc3d_star_packets(float(isrf_frac), int(np_)))
 
 
 # ---------------------------------------------------------------------------
@@ -248,6 +258,9 @@ class Model:
         self.tsub = t.tsub
         self.hnuint = _arr(t.hnuint, t.nhnu); self.atmosnu = _arr(t.atmosnu, t.nhnu)
         self.lognu = _arr(t.lognu, t.nhnu); self.loghnu = _arr(t.loghnu, t.nhnu)
+        self.nisrf = t.nisrf
+        self.isrf_cdf = _arr(t.isrf_cdf, t.nisrf); self.isrf_logcdf = _arr(t.isrf_logcdf, t.nisrf)
+        self.isrf_logfreq = _arr(t.isrf_logfreq, t.nisrf)
         # run parameters
         self.npeel = p.npeel
         self.thete = _arr(p.thete, p.npeel); self.phie = _arr(p.phie, p.npeel)
@@ -264,6 +277,10 @@ class Model:
         for n in ("nudust", "kappad", "adust", "gdust", "pldust", "kappav", "lTint", "nuint", "kapBint", "kappap",
                   "hnuint", "atmosnu", "lognu", "loghnu"):
             setattr(t, n, _ptr(getattr(self, n)))
+        t.nisrf = self.nisrf
+        if self.nisrf:
+            for n in ("isrf_cdf", "isrf_logcdf", "isrf_logfreq"):
+                setattr(t, n, _ptr(getattr(self, n)))
         return t
 
     @property
@@ -287,6 +304,9 @@ class Model:
         q.aperture2 = _ptr(self.aperture2)
         for k, v in over.items():
             setattr(q, k, v)
+        if "np" in over and "n_star" not in over:
+            # the stellar share of this call's packets (newdisktherm.F90:143-175)
+            q.n_star = star_packets(self.info.isrf_frac, q.np)
         return q
 
     def set_tdust(self, tdust: np.ndarray) -> None:

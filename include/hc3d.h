@@ -95,6 +95,10 @@ typedef struct hc3d_dust_tables {
   const double *atmosnu;  /* (nhnu) frequency */
   const double *lognu;    /* (nhnu) log10 frequency */
   const double *loghnu;   /* (nhnu) log10 cumulative distribution */
+  int nisrf;              /* rows of the external-illumination spectrum (isrf_mod, 200); 0 = none */
+  const double *isrf_cdf;     /* (nisrf) cdf_i of isrf_cdf.f90: cumulative, 0 .. 1 */
+  const double *isrf_logcdf;  /* (nisrf) logcdf_i: log10 cdf_i, -99 at row 1 */
+  const double *isrf_logfreq; /* (nisrf) logfreq_i: log10 frequency (1.2398/lambda[um]), 0 at row 1 */
 } hc3d_dust_tables;
 
 /* grid_mod (grid_mod.f90:20-50) as gridset leaves it. */
@@ -137,6 +141,11 @@ typedef struct hc3d_run_params {
   int iintmax;            /* interactions in one cell before a packet is killed (10000) */
   int64_t max_interactions; /* per-packet cap on interactions; 0 = no cap */
   int image;              /* 1 = accumulate broadband I,Q,U,V images of the peeled packets */
+  int ext_illum;          /* 1 = external illumination (COUTILLUM): packets with global id >= n_star
+                             enter from the outer sphere (newdisktherm.F90:378-440); needs nisrf > 0 */
+  int64_t n_star;         /* stellar packets of the whole iteration (ns, newdisktherm.F90:143-175),
+                             from hc3d_star_packets */
+  double rmax;            /* outer radius of the grid, R* (the external packets start at 0.999999 rmax) */
 } hc3d_run_params;
 
 /* Host copies of the device tallies.  Any pointer may be NULL.  Shapes are

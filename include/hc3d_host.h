@@ -22,6 +22,9 @@
  *   SEED              64-bit run seed of the counter-based packet streams
  *   FRACTLEV, FRACTN, FRACTCONTRAST  levels, clumps per level and density
  *                     contrast of the project fractal generator (CFRACTAL=YES)
+ *   ISRF_FILE         with COUTILLUM=YES: the external radiation field, one
+ *                     "log10 nu[Hz]  log10 nu*F_nu" pair per line, increasing
+ *                     in nu (isrf_cdf.f90 carries its table in the source)
  */
 #ifndef HC3D_HOST_H
 #define HC3D_HOST_H
@@ -51,6 +54,9 @@ typedef struct hc3d_model_info {
   int64_t ncells;      /* (nrg-1)(ntg-1)(npg-1) */
   double density_host_ms; /* wall time of the host density build in gridset */
   double tables_host_ms;  /* wall time of the host setemiss tables */
+  double lstar;           /* stellar luminosity, erg/s */
+  double l_isrf;          /* external-illumination luminosity, erg/s (newtts.F90:204-228) */
+  double isrf_frac;       /* l_isrf / ltot (gridset.f90:208-209) */
 } hc3d_model_info;
 
 /* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
@@ -78,6 +84,12 @@ int hc3d_model_densities_gpu(hc3d_model *m, int device, double *ms, char *err, s
  * receives the device time of the kernels. */
 int hc3d_model_tables_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
 
+/* The stellar packets ns of an iteration of np packets when a fraction
+ * isrf_frac of the luminosity enters from outside (newdisktherm.F90:143-175,
+ * without accretion): both shares rounded to the nearest integer, then ns
+ * adjusted so that the shares add up to np.  isrf_frac = 0 gives np. */
+int64_t hc3d_star_packets(double isrf_frac, int64_t np);
+
 typedef struct hc3d_tts_stats {
   int iterations;            /* Lucy iterations + the final one */
   int converged;
@@ -99,6 +111,9 @@ int hc3d_tts(const char *par_path, const char *par_dir, const char *out_dir, con
  * starbarb.f90:24-36): the fixtures of the benchmark models. */
 int hc3d_write_synthetic_dust(const char *path);
 int hc3d_write_wavelength_grid(const char *path, double tstar_k);
+/* Write a synthetic external radiation field in the ISRF_FILE format:
+ * three diluted blackbodies (Mathis, Mezger & Panagia 1983 form). */
+int hc3d_write_synthetic_isrf(const char *path);
 
 #ifdef __cplusplus
 }

@@ -726,23 +726,8 @@ static double orc_atmosfreq(const orc_ctx *c, orc_rng *rng) {
                                  (d->hnuint[i] - d->hnuint[i - 1]);
 }
 
-/* ---- initpspot (ispot=0), initp_common.f90:1-94 --------------------------- */
-static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
-  p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
-  for (;;) {
-    double xran = orc_ran(rng);
-    p->cosb = 1.0 - 2.0 * xran;
-    p->sinb = sqrt(1.0 - p->cosb * p->cosb);
-    if (p->cosb != 0.0 && fabs(p->cosb) < 1.0) break;
-  }
-  p->lp = ORC_R2P * orc_ran(rng);
-  /* initp_sample, limb = 0 */
-  p->cost = sqrt(orc_ran(rng));
-  p->sint = sqrt(1.0 - p->cost * p->cost);
-  p->phi = ORC_R2P * orc_ran(rng);
-  p->cosp = cos(p->phi);
-  p->sinp = sin(p->phi);
-  /* initp_transform */
+/* ---- initp_transform, initp_common.f90:31-94 ----------------------------- */
+static void orc_initp_transform(pkt *p) {
   if (fabs(p->cosb) < 0.9999999) {
     double costi = p->cost * p->cosb - p->sint * p->sinb * p->cosp;
     if (fabs(costi) > 1.0) {
@@ -773,8 +758,56 @@ static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
   if (p->phi < 0.0) p->phi += ORC_R2P;
   p->sinp = sin(p->phi);
   p->cosp = cos(p->phi);
+}
+
+/* ---- initpspot (ispot=0) with initp_sample, initp_common.f90:1-29 -------- */
+static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
+  p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
+  for (;;) {
+    double xran = orc_ran(rng);
+    p->cosb = 1.0 - 2.0 * xran;
+    p->sinb = sqrt(1.0 - p->cosb * p->cosb);
+    if (p->cosb != 0.0 && fabs(p->cosb) < 1.0) break;
+  }
+  p->lp = ORC_R2P * orc_ran(rng);
+  /* initp_sample, limb = 0 */
+  p->cost = sqrt(orc_ran(rng));
+  p->sint = sqrt(1.0 - p->cost * p->cost);
+  p->phi = ORC_R2P * orc_ran(rng);
+  p->cosp = cos(p->phi);
+  p->sinp = sin(p->phi);
+  orc_initp_transform(p);
   /* fspot = 1 without spots: nub = atmosfreq() (initpspot.f90:150-156) */
   p->nub = orc_atmosfreq(c, rng);
+}
+
+/* ---- rep_isrf, rep_isrf.f90:1-41 ------------------------------------------ */
+static double orc_rep_isrf(const orc_ctx *c, orc_rng *rng) {
+  const hc3d_dust_tables *d = &c->dt;
+  const double xran = orc_ran(rng);
+  const int n = d->nisrf;
+  int i = orc_locate(d->isrf_cdf, n, xran);
+  if (i == n) i = n - 1;
+  if (i == 0) i = 1;
+  const double logfreq = d->isrf_logfreq[i - 1] + (log10(xran) - d->isrf_logcdf[i - 1]) /
+                                                      (d->isrf_logcdf[i] - d->isrf_logcdf[i - 1]) *
+                                                      (d->isrf_logfreq[i] - d->isrf_logfreq[i - 1]);
+  return pow(10.0, logfreq);
+}
+
+/* ---- initpout, initpout.f90:3-66 ----------------------------------------- */
+static void orc_initpout(const orc_ctx *c, pkt *p, orc_rng *rng) {
+  p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
+  p->cosb = 1.0 - 2.0 * orc_ran(rng);
+  p->sinb = sqrt(1.0 - p->cosb * p->cosb);
+  p->cost = -sqrt(orc_ran(rng));
+  p->sint = sqrt(1.0 - p->cost * p->cost);
+  p->phi = ORC_R2P * orc_ran(rng);
+  p->cosp = cos(p->phi);
+  p->sinp = sin(p->phi);
+  p->lp = ORC_R2P * orc_ran(rng);
+  orc_initp_transform(p);
+  p->nub = orc_rep_isrf(c, rng);
 }
 
 /* ---- propagate.f90:27-319 ------------------------------------------------- */
@@ -894,12 +927,43 @@ bin:
   orc_bin_escape(c, rp, p, xpold, ypold, zpold, iflag, iscat, t);
 }
 
+/* ---- one external packet: newdisktherm.F90:378-440 ----------------------- */
+/* The packet starts inside the outermost shell at 0.999999 rmax; the walk
+ * (tauint, restated) treats it as not on a wall.  No direct peel-off. */
+static void orc_external_packet(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, orc_rng *rng, orc_tallies *t,
+                                orc_trace *tr) {
+  orc_initpout(c, p, rng);
+  p->i_orig = 4;
+  orc_opacset(c, p, p->nub, rp->rstar_cm);
+  const double coslp = cos(p->lp), sinlp = sin(p->lp);
+  p->zp = p->cosb * rp->rmax * 0.999999;
+  const double rp_ = p->sinb * rp->rmax * 0.999999;
+  p->xp = rp_ * coslp;
+  p->yp = rp_ * sinlp;
+  p->ux = p->sint * p->cosp; p->uy = p->sint * p->sinp; p->uz = p->cost;
+  p->ir = c->g.nrg - 1;
+  p->on_wall = 0;
+  const double thetb = acos(p->cosb);
+  p->it = orc_locate(c->g.thetarr, c->g.ntg, thetb);
+  p->ip = orc_locate(c->g.phiarr, c->g.npg, p->lp);
+  if (p->it < 1) p->it = 1;
+  if (p->it > c->g.ntg - 1) p->it = c->g.ntg - 1;
+  if (p->ip < 1) p->ip = 1;
+  if (p->ip > c->g.npg - 1) p->ip = c->g.npg - 1;
+  trace_add(tr, 0, p->ir, p->it, p->ip, 0, 0, p->xp, p->yp, p->zp);
+  orc_propagate(c, rp, p, rng, t, tr);
+}
+
 /* ---- one stellar packet: newdisktherm.F90:256-377 with ips = 0 ------------ */
 static void orc_packet(const orc_ctx *c, const hc3d_run_params *rp, int64_t pid, orc_rng *rng, orc_tallies *t,
                        orc_trace *tr) {
   pkt p;
   memset(&p, 0, sizeof(p));
   p.on_wall = 0;
+  if (rp->ext_illum && pid >= rp->n_star) {
+    orc_external_packet(c, rp, &p, rng, t, tr);
+    return;
+  }
   orc_initpspot(c, &p, rng);
   p.i_orig = 1;
   orc_opacset(c, &p, p.nub, rp->rstar_cm);
@@ -1035,6 +1099,16 @@ double orc_lucydustfreq_c(const hc3d_dust_tables *dt, const hc3d_grid *g, double
   orc_rng_init(&r, 0, 0, 0);
   r.inj = &xi; r.ninj = 1; r.pos = 0;
   return orc_lucydustfreq(&c, T0, id, &r);
+}
+
+/* rep_isrf for one injected uniform xi (tests) */
+double orc_rep_isrf_c(const hc3d_dust_tables *dt, const hc3d_grid *g, double xi) {
+  orc_ctx c;
+  orc_ctx_init(&c, dt, g);
+  orc_rng r;
+  orc_rng_init(&r, 0, 0, 0);
+  r.inj = &xi; r.ninj = 1; r.pos = 0;
+  return orc_rep_isrf(&c, &r);
 }
 
 /* ---- tfinal (restated): Lucy temperature, dusttemp.f90:30-50 form --------- */

@@ -51,6 +51,8 @@ def lib() -> C.CDLL:
         L.orc_sample_stokes.argtypes = [P(DustTables), P(Grid), C.c_double, C.c_uint64, C.c_int, dp, dp]
         L.orc_lucydustfreq_c.argtypes = [P(DustTables), P(Grid), C.c_double, C.c_int, C.c_double]
         L.orc_lucydustfreq_c.restype = C.c_double
+        L.orc_rep_isrf_c.argtypes = [P(DustTables), P(Grid), C.c_double]
+        L.orc_rep_isrf_c.restype = C.c_double
         L.orc_dusttemp.argtypes = [P(DustTables)] + [C.c_double] * 4 + [C.c_int, C.c_double]
         L.orc_dusttemp.restype = C.c_double
         L.orc_tfinal.argtypes = [P(DustTables), P(Grid), dp, C.c_double, C.c_double, dp]
@@ -147,6 +149,13 @@ def trace(model: hc3d.Model, params: RunParams, pid: int, uniforms=None, max_rec
                                u.ctypes.data_as(P(C.c_double)), len(u), recs.ctypes.data_as(P(TraceRec)), max_rec,
                                C.byref(ex))
     return recs[:n], bool(ex.value), ot.result()
+
+
+def rep_isrf(model: hc3d.Model, xi) -> np.ndarray:
+    """Frequencies of external packets for the uniforms xi (rep_isrf)."""
+    L = lib()
+    t, g = model.tables, model.grid
+    return np.array([L.orc_rep_isrf_c(C.byref(t), C.byref(g), float(x)) for x in np.atleast_1d(xi)])
 
 
 def stream(seed: int, it: int, pid: int, n: int) -> np.ndarray:

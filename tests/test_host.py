@@ -40,12 +40,19 @@ def test_missing_key_is_an_error(tmp_path, built):
     assert "NRG" in str(e.value)
 
 
-@pytest.mark.parametrize("key", ["CSPOT", "CDISKACC", "DIFFUSION", "CLIMB", "COUTILLUM"])
+@pytest.mark.parametrize("key", ["CSPOT", "CDISKACC", "DIFFUSION", "CLIMB"])
 def test_unsupported_options_are_rejected(tmp_path, built, key):
     par = configs.write_par(tmp_path, "tiny", **{key: "YES"})
     with pytest.raises(hc3d.Hc3dError) as e:
         hc3d.Model(par)
     assert e.value.code == -7
+
+
+def test_external_illumination_needs_its_field(tmp_path, built):
+    par = configs.write_par(tmp_path, "tiny", COUTILLUM="YES")
+    with pytest.raises(hc3d.Hc3dError) as e:
+        hc3d.Model(par)
+    assert e.value.code == -1 and "ISRF_FILE" in str(e.value)
 
 
 def test_grid_walls(model_factory):
