@@ -19,6 +19,12 @@ packets: zero the tallies, run the packet loop, solve the Lucy temperatures.
          scaled by crossings
   cpu_baseline  the CPU oracle (C restatement, FP64) on the host cores, on
          a bounded sample of the same workload
+  model_grid  models/hr of 12 seeded models of the model-grid distribution
+         (photon counts scaled down to 5e4..5e5 per iteration) on the
+         model-run server, four concurrent runs against one at a time
+  serving  Poisson arrivals at 20 requests/s (SED + 3 inclinations each):
+         p50/p99 latency and packets/s against the same requests as an
+         offline batch, with the results of both compared
 
 ``--impl reference`` times the CPU oracle alone (the reference cannot be
 built here: no Fortran compiler and 14 modules missing).
@@ -165,6 +171,95 @@ def cpu_baseline(model, workload, budget_s: float = 15.0):
                       f"{threads} threads, {dt:.1f} s)"}
 
 
+GRID_SHAPES = [(100, 99, 2), (200, 199, 2), (200, 199, 33)]  # NRG, NTG, NPG (NPG = azimuthal cells + 1)
+
+
+def model_grid_pars(tmp: Path, n: int, np_lo: float, np_hi: float, seed: int):
+    """Seeded models of the model-grid distribution: log-uniform disk mass
+    1e-4..0.1 Msun and infall rate 1e-7..1e-4 Msun/yr, cavity angle 5..45 deg,
+    stellar temperature 3000..10000 K, a grid of GRID_SHAPES, photon counts
+    log-uniform in [np_lo, np_hi]; two Lucy iterations and the peeled one."""
+    from hochunk3d_gb300 import configs
+
+    rng = np.random.default_rng(seed)
+    pars = []
+    for k in range(n):
+        g = GRID_SHAPES[int(rng.integers(len(GRID_SHAPES)))]
+        npk = int(10 ** rng.uniform(math.log10(np_lo), math.log10(np_hi)))
+        cav = float(rng.uniform(5.0, 45.0))
+        over = {"NRG": g[0], "NTG": g[1], "NPG": g[2], "MASSD": float(10 ** rng.uniform(-4, -1)),
+                "RATE": float(10 ** rng.uniform(-7, -4)), "THET1": cav, "THET2": cav,
+                "TSTAR": float(rng.uniform(3000.0, 10000.0)), "NP": npk, "NPMIN": min(npk, 10000),
+                "NIMIN": 2, "NIMAX": 2, "I1": -(1000 + k)}
+        pars.append(configs.write_par(tmp / f"model{k:03d}", "plain", **over))
+    return pars
+
+
+def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
+    """Models per hour of a seeded model grid on the server, with `slots`
+    concurrent runs and with one run at a time."""
+    from hochunk3d_gb300 import hc3d
+
+    pars = model_grid_pars(tmp / "grid", n, 5e4, 5e5, seed=4)
+    out = {"models": n, "packets_per_model": "log-uniform 5e4..5e5 per iteration",
+           "iterations": "2 Lucy + 1 peeled", "grids": [list(g) for g in GRID_SHAPES]}
+    for k in (slots, 1):
+        srv = hc3d.Server(slots=k, device=device)
+        t0 = time.perf_counter()
+        res = [srv.wait(t) for t in [srv.submit(p) for p in pars]]
+        dt = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        pk = sum(r["packets"] for r in res)
+        key = "concurrent" if k > 1 else "one_at_a_time"
+        out[key] = {"slots": k, "seconds": dt, "models_per_hr": n / dt * 3600.0, "packets_per_s": pk / dt,
+                    "peak_running": st["peak_running"]}
+    return out
+
+
+def serving_latency(tmp: Path, device: int, n: int = 60, rate: float = 20.0, slots: int = 8, np_req: int = 20000):
+    """Poisson arrivals at `rate` requests/s of models of the model-grid
+    distribution, each asking for its SED and three peel-off inclinations
+    (one Lucy iteration of 2e4 packets, a peeled iteration of 2e4 packets):
+    p50/p99 latency from submission to result, against the same requests
+    submitted as one offline batch."""
+    from hochunk3d_gb300 import hc3d
+
+    pars = model_grid_pars(tmp / "serve", n, np_req, np_req, seed=5)
+    th = np.radians([30.0, 60.0, 85.0])
+    req = {"n_lucy": 1, "np_lucy": np_req, "np_": np_req, "thete": th, "phie": np.zeros(3)}
+    rng = np.random.default_rng(6)
+    gaps = rng.exponential(1.0 / rate, n)
+    srv = hc3d.Server(slots=slots, device=device)
+    srv.wait(srv.submit(pars[0], **req))  # slot warm-up: pools, queues, kernels
+    t0 = time.perf_counter()
+    tickets = []
+    due = 0.0
+    for k in range(n):
+        due += gaps[k]
+        wait = t0 + due - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        tickets.append(srv.submit(pars[k], **req))
+    res = [srv.wait(t) for t in tickets]
+    span = time.perf_counter() - t0
+    lat = np.array([r["t_done"] - r["t_submit"] for r in res]) * 1000.0
+    svc = np.array([r["t_done"] - r["t_admit"] for r in res]) * 1000.0
+    pk = sum(r["packets"] for r in res)
+    t1 = time.perf_counter()
+    off = [srv.wait(t) for t in [srv.submit(p, **req) for p in pars]]
+    off_dt = time.perf_counter() - t1
+    srv.close()
+    same = all(np.array_equal(a["si"], b["si"]) and np.array_equal(a["ti"], b["ti"]) for a, b in zip(res, off))
+    return {"requests": n, "rate_per_s": rate, "slots": slots, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+            "run_p50_ms": float(np.percentile(svc, 50)), "run_p99_ms": float(np.percentile(svc, 99)),
+            "packets_per_s": pk / span,
+            "offline_batch_packets_per_s": sum(r["packets"] for r in off) / off_dt,
+            "request": f"1 Lucy x {np_req:.0e} + peeled {np_req:.0e} packets, SED + 3 inclinations",
+            "results_equal_to_offline_batch": bool(same)}
+
+
 def reference_arm(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -211,6 +306,7 @@ def main():
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
     ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison run")
+    ap.add_argument("--no-serving", action="store_true", help="skip the model-grid and serving measurements")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one untimed peeled step after the Lucy set-up and print its crossing and launch "
                          "counts (the command a DRAM-traffic capture of k_wave / k_peel_mixed runs)")
@@ -379,6 +475,10 @@ def main():
         table_build = {"rows": int(model.nT), "intervals": int(model.nnu), "host_ms": host_tab_ms,
                        "host_threads": min(16, os.cpu_count() or 1), "device_kernel_ms": tab_ms,
                        "device_call_ms": tab_call_ms}
+        grid_runs = serving = None
+        if rank == 0 and not args.no_serving:
+            grid_runs = model_grid_throughput(Path(td), local)
+            serving = serving_latency(Path(td), local)
         if rank == 0:
             line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -392,6 +492,7 @@ def main():
                     "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),
                             "d2h_bytes_per_step": int(d2h)},
                     "fp64": fp64, "grid_build": grid_build, "table_build": table_build,
+                    "model_grid": grid_runs, "serving": serving,
                     "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(),
                     "gpu_launches": launches + args.steps}
             print(json.dumps(line))

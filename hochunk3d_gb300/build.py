@@ -40,6 +40,7 @@ UNITS = [
     ("hc3d_tablebuild.cu", ["--fmad=false"]),
     ("hc3d_model.cpp", []),
     ("hc3d_driver.cpp", []),
+    ("hc3d_serve.cpp", []),
 ]
 
 

@@ -22,7 +22,8 @@ struct hc3d_ctx {
   bool tables = false, grid = false;
   // model
   DevModel dm{};
-  std::vector<void*> model_allocs;
+  std::vector<void*> core_allocs;   // counters, fault log, run arguments: the context's lifetime
+  std::vector<void*> model_allocs;  // dust tables: until hc3d_reset
   std::vector<void*> grid_allocs;
   double tsub = 1600.0;
   double kappav[kSlots] = {0, 0, 0, 0};
@@ -73,11 +74,14 @@ int fail(hc3d_ctx* c, int code, const std::string& msg) {
       return fail(c, HC3D_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// Device memory of a context is stream-ordered on the context's stream
+// (cudaMallocAsync / cudaFreeAsync): loading, resetting or destroying one
+// context never waits for the kernels of another context on the device.
 template <class T>
 int dalloc(hc3d_ctx* c, std::vector<void*>& owner, T** p, size_t n) {
   void* q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
-  if (e != cudaSuccess) return fail(c, HC3D_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(n, 1) * sizeof(T), c->stream);
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_NOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
   owner.push_back(q);
   *p = (T*)q;
   return HC3D_OK;
@@ -88,14 +92,23 @@ int dupload(hc3d_ctx* c, std::vector<void*>& owner, T** p, const T* src, size_t 
   int r = dalloc(c, owner, p, n);
   if (r) return r;
   if (n) {
-    cudaError_t e = cudaMemcpy(*p, src, n * sizeof(T), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+    // from pageable memory the call returns once src has been staged
+    cudaError_t e = cudaMemcpyAsync(*p, src, n * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e));
   }
   return HC3D_OK;
 }
 
-void free_all(std::vector<void*>& v) {
-  for (void* p : v) cudaFree(p);
+// device -> host on the context's stream, complete on return
+int d2h(hc3d_ctx* c, void* dst, const void* src, size_t bytes) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("device to host copy: ") + cudaGetErrorString(e));
+  return HC3D_OK;
+}
+
+void free_all(hc3d_ctx* c, std::vector<void*>& v) {
+  for (void* p : v) cudaFreeAsync(p, c->stream);
   v.clear();
 }
 
@@ -159,15 +172,15 @@ int grid_blocks_for(hc3d_ctx* c, int64_t n) {
 }
 
 int alloc_run_tallies(hc3d_ctx* c, const TallyDims& d) {
-  free_all(c->run_allocs);
+  free_all(c, c->run_allocs);
   c->run_tallies = false;
   int r;
   if ((r = dalloc(c, c->run_allocs, &c->dt.sed, (size_t)9 * d.nsed))) return r;
   if ((r = dalloc(c, c->run_allocs, &c->dt.psed, (size_t)9 * std::max<int64_t>(d.npsed, 1)))) return r;
   if ((r = dalloc(c, c->run_allocs, &c->dt.img, (size_t)4 * std::max<int64_t>(d.nimg, 1)))) return r;
-  CK(cudaMemset(c->dt.sed, 0, sizeof(unsigned long long) * 9 * d.nsed));
-  CK(cudaMemset(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(d.npsed, 1)));
-  CK(cudaMemset(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(d.nimg, 1)));
+  CK(cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * d.nsed, c->stream));
+  CK(cudaMemsetAsync(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(d.npsed, 1), c->stream));
+  CK(cudaMemsetAsync(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(d.nimg, 1), c->stream));
   c->dims = d;
   c->run_tallies = true;
   return HC3D_OK;
@@ -278,11 +291,22 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
 
 // Allocate the packet pool and event queue of the wavefront form once per context.
 int ensure_wave(hc3d_ctx* c) {
-  if (c->wave.pool) return HC3D_OK;
   const bool f64 = c->precision == HC3D_PREC_FP64;
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f64 ? wave_fn_fp64() : wave_fn_mixed(), 128, c->dm.dust_smem));
   if (per_sm < 1) per_sm = 1;
+  if (c->wave.pool) {
+    // kept across hc3d_reset while the dust tables of the new model allow the same residency
+    if (c->sm_count * per_sm == c->wave_blocks) return HC3D_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    free_all(c, c->wave_allocs);
+    c->wave = WaveBufs{};
+    for (int i = 0; i < 3; ++i)
+      if (c->wev[i]) {
+        cudaEventDestroy(c->wev[i]);
+        c->wev[i] = nullptr;
+      }
+  }
   c->wave_blocks = c->sm_count * per_sm;
   c->pool_threads = (int64_t)c->wave_blocks * 128;
   int per_sm_p = 0;
@@ -359,7 +383,7 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
 int finish_run(hc3d_ctx* c) {
   CK(cudaStreamSynchronize(c->stream));
   int st = 0;
-  CK(cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (int r_ = d2h(c, &st, c->d_status, sizeof(int))) return r_;
   if (st && !c->status_seen) c->status_seen = st;
   return HC3D_OK;
 }
@@ -398,20 +422,30 @@ extern "C" int hc3d_create(hc3d_ctx** out, const hc3d_device_opts* opts) {
     delete c;
     return HC3D_ERR_CUDA;
   }
-  std::vector<void*>& own = c->model_allocs;
+  {
+    // keep freed stream-ordered memory in this process's pool for the next
+    // model instead of returning it to the driver at every synchronisation
+    cudaMemPool_t mp;
+    if (cudaDeviceGetDefaultMemPool(&mp, c->device) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
+  std::vector<void*>& own = c->core_allocs;
   if (dalloc(c, own, &c->d_work, 1) || dalloc(c, own, &c->d_status, 1) ||
       dalloc(c, own, &c->d_peeldir, 4 * kMaxPeel) || dalloc(c, own, &c->d_ap2, 64) ||
       dalloc(c, own, &c->d_maxrel, 1) || dalloc(c, own, &c->dt.counters, 16) ||
       dalloc(c, own, &c->dt.fault_log, kFaultLog) || dalloc(c, own, &c->dt.fault_count, 1)) {
-    free_all(own);
+    free_all(c, own);
     cudaStreamDestroy(c->stream);
     delete c;
     return HC3D_ERR_NOMEM;
   }
-  cudaMemset(c->dt.counters, 0, 16 * sizeof(unsigned long long));
-  cudaMemset(c->d_status, 0, sizeof(int));
+  cudaMemsetAsync(c->dt.counters, 0, 16 * sizeof(unsigned long long), c->stream);
+  cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+  cudaStreamSynchronize(c->stream);
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
-    free_all(own);
+    free_all(c, own);
     cudaStreamDestroy(c->stream);
     delete c;
     return HC3D_ERR_CUDA;
@@ -424,16 +458,51 @@ extern "C" void hc3d_destroy(hc3d_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  free_all(c->run_allocs);
-  free_all(c->grid_allocs);
-  free_all(c->model_allocs);
+  free_all(c, c->run_allocs);
+  free_all(c, c->grid_allocs);
+  free_all(c, c->model_allocs);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   for (int i = 0; i < 3; ++i)
     if (c->wev[i]) cudaEventDestroy(c->wev[i]);
-  free_all(c->wave_allocs);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  free_all(c, c->wave_allocs);
+  free_all(c, c->core_allocs);
+  if (c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
   delete c;
+}
+
+extern "C" int hc3d_reset(hc3d_ctx* c) {
+  if (!c) return HC3D_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  free_all(c, c->run_allocs);
+  free_all(c, c->grid_allocs);
+  free_all(c, c->model_allocs);
+  c->tables = c->grid = c->run_tallies = false;
+  c->scales_set = false;
+  c->epoch_np = c->epoch_budget = 0;
+  c->dm = DevModel{};
+  c->dims = TallyDims{};
+  c->d_kappap = c->d_massarr = c->d_tdust = nullptr;
+  c->d_tdustf = nullptr;
+  c->d_peelmask = nullptr;
+  c->ndg_in = 0;
+  // the run tallies go; the counters and the fault log stay with the context
+  DevTallies keep{};
+  keep.counters = c->dt.counters;
+  keep.fault_log = c->dt.fault_log;
+  keep.fault_count = c->dt.fault_count;
+  c->dt = keep;
+  CK(cudaMemsetAsync(c->dt.counters, 0, 16 * sizeof(unsigned long long), c->stream));
+  CK(cudaMemsetAsync(c->dt.fault_count, 0, sizeof(unsigned long long), c->stream));
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+  c->status_seen = 0;
+  c->wave_log.clear();
+  CK(cudaStreamSynchronize(c->stream));
+  return HC3D_OK;
 }
 
 extern "C" void* hc3d_get_stream(hc3d_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -662,7 +731,7 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       return fail(c, HC3D_ERR_INVALID, "densarr holds a negative, NaN or infinite value");
   for (int i = 1; i < nrg; ++i)
     if (!(g->rarr[i] > g->rarr[i - 1])) return fail(c, HC3D_ERR_INVALID, "rarr must increase");
-  free_all(c->grid_allocs);
+  free_all(c, c->grid_allocs);
   c->grid = false;
   std::vector<float> tan2f(ntg), hemi(ntg), af(npg), bf(npg);
   for (int i = 0; i < ntg; ++i) {
@@ -829,11 +898,11 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
 extern "C" int hc3d_get_fault_log(hc3d_ctx* c, uint64_t* entries, int max, int* n) {
   if (!c || !n) return HC3D_ERR_INVALID;
   unsigned long long cnt = 0;
-  CK(cudaMemcpy(&cnt, c->dt.fault_count, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (int r_ = d2h(c, &cnt, c->dt.fault_count, sizeof(cnt))) return r_;
   *n = (int)std::min<unsigned long long>(cnt, (unsigned long long)kFaultLog);
   if (entries && max > 0) {
     const int k = std::min(*n, max);
-    if (k) CK(cudaMemcpy(entries, c->dt.fault_log, sizeof(uint64_t) * k, cudaMemcpyDeviceToHost));
+    if (k) if (int r_ = d2h(c, entries, c->dt.fault_log, sizeof(uint64_t) * k)) return r_;
   }
   *n = (int)std::min<unsigned long long>(cnt, (unsigned long long)0x7fffffff);
   return HC3D_OK;
@@ -868,15 +937,15 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   if (c->run_tallies) {
     int64_t* sed[9] = {out->si, out->sq, out->su, out->sv, out->si2, out->sq2, out->su2, out->sv2, out->nums};
     for (int k = 0; k < 9; ++k)
-      if (sed[k]) CK(cudaMemcpy(sed[k], c->dt.sed + k * c->dims.nsed, sizeof(int64_t) * c->dims.nsed, cudaMemcpyDeviceToHost));
+      if (sed[k]) if (int r_ = d2h(c, sed[k], c->dt.sed + k * c->dims.nsed, sizeof(int64_t) * c->dims.nsed)) return r_;
     int64_t* ps[9] = {out->ti, out->tq, out->tu, out->tv, out->ti2, out->tq2, out->tu2, out->tv2, out->numt};
     if (c->dims.npsed > 0)
       for (int k = 0; k < 9; ++k)
-        if (ps[k]) CK(cudaMemcpy(ps[k], c->dt.psed + k * c->dims.npsed, sizeof(int64_t) * c->dims.npsed, cudaMemcpyDeviceToHost));
+        if (ps[k]) if (int r_ = d2h(c, ps[k], c->dt.psed + k * c->dims.npsed, sizeof(int64_t) * c->dims.npsed)) return r_;
     int64_t* im[4] = {out->image_i, out->image_q, out->image_u, out->image_v};
     if (c->dims.nimg > 0)
       for (int k = 0; k < 4; ++k)
-        if (im[k]) CK(cudaMemcpy(im[k], c->dt.img + k * c->dims.nimg, sizeof(int64_t) * c->dims.nimg, cudaMemcpyDeviceToHost));
+        if (im[k]) if (int r_ = d2h(c, im[k], c->dt.img + k * c->dims.nimg, sizeof(int64_t) * c->dims.nimg)) return r_;
   }
   const DevModel& m = c->dm;
   const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
@@ -895,22 +964,22 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   std::vector<unsigned long long> buf;
   if (out->nabs) {
     buf.resize((size_t)kSlots * n);
-    CK(cudaMemcpy(buf.data(), c->dt.nabs, sizeof(unsigned long long) * buf.size(), cudaMemcpyDeviceToHost));
+    if (int r_ = d2h(c, buf.data(), c->dt.nabs, sizeof(unsigned long long) * buf.size())) return r_;
     scatter(buf, ndg, out->nabs);
   }
   if (out->dtauabs) {
     buf.resize((size_t)kSlots * n);
-    CK(cudaMemcpy(buf.data(), c->dt.dtauabs, sizeof(unsigned long long) * buf.size(), cudaMemcpyDeviceToHost));
+    if (int r_ = d2h(c, buf.data(), c->dt.dtauabs, sizeof(unsigned long long) * buf.size())) return r_;
     scatter(buf, ndg, out->dtauabs);
   }
   if (out->jmean) {
     buf.resize((size_t)n);
-    CK(cudaMemcpy(buf.data(), c->dt.jmean, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    if (int r_ = d2h(c, buf.data(), c->dt.jmean, sizeof(unsigned long long) * n)) return r_;
     scatter(buf, 1, out->jmean);
   }
   auto scatter32 = [&](const unsigned int* dsrc, int32_t* dst) -> int {
     std::vector<unsigned int> b32((size_t)n);
-    CK(cudaMemcpy(b32.data(), dsrc, sizeof(unsigned int) * n, cudaMemcpyDeviceToHost));
+    if (int r_ = d2h(c, b32.data(), dsrc, sizeof(unsigned int) * n)) return r_;
     std::fill(dst, dst + n4, 0);
     for (int ip = 1; ip < m.npg; ++ip)
       for (int it = 1; it < m.ntg; ++it)
@@ -925,7 +994,7 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   if (out->killed && (r = scatter32(c->dt.killed, out->killed))) return r;
   if (out->dbig && (r = scatter32(c->dt.dbig, out->dbig))) return r;
   unsigned long long cnt[16];
-  CK(cudaMemcpy(cnt, c->dt.counters, sizeof(cnt), cudaMemcpyDeviceToHost));
+  if (int r_ = d2h(c, cnt, c->dt.counters, sizeof(cnt))) return r_;
   for (int k = 0; k < 16; ++k) out->counters[k] = (int64_t)cnt[k];
   return HC3D_OK;
 }
@@ -964,7 +1033,7 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
     const DevModel& m = c->dm;
     const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
     std::vector<double> td((size_t)4 * n);
-    CK(cudaMemcpy(td.data(), c->d_tdust, sizeof(double) * td.size(), cudaMemcpyDeviceToHost));
+    if (int r_ = d2h(c, td.data(), c->d_tdust, sizeof(double) * td.size())) return r_;
     for (int s = 0; s < std::min(c->ndg_in, kSlots); ++s)
       for (int ip = 1; ip < m.npg; ++ip)
         for (int it = 1; it < m.ntg; ++it)
@@ -994,7 +1063,7 @@ extern "C" int hc3d_trace_packets(hc3d_ctx* c, const hc3d_run_params* p, int npk
   int* d_n;
   if ((r = dupload(c, tmp, &d_u, uniforms, (size_t)npkt * nu)) || (r = dalloc(c, tmp, &d_rec, (size_t)npkt * max_rec)) ||
       (r = dalloc(c, tmp, &d_n, (size_t)npkt))) {
-    free_all(tmp);
+    free_all(c, tmp);
     return r;
   }
   a.inj = d_u;
@@ -1009,9 +1078,11 @@ extern "C" int hc3d_trace_packets(hc3d_ctx* c, const hc3d_run_params* p, int npk
   cudaError_t e = c->precision == HC3D_PREC_FP64 ? launch_transport_fp64(c->dm, c->dt, c->dims, a, cfg)
                                                  : launch_transport_mixed(c->dm, c->dt, c->dims, a, cfg);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e == cudaSuccess) e = cudaMemcpy(recs, d_rec, sizeof(hc3d_trace_rec) * (size_t)npkt * max_rec, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(nrec, d_n, sizeof(int32_t) * npkt, cudaMemcpyDeviceToHost);
-  free_all(tmp);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(recs, d_rec, sizeof(hc3d_trace_rec) * (size_t)npkt * max_rec, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(nrec, d_n, sizeof(int32_t) * npkt, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  free_all(c, tmp);
   if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("trace: ") + cudaGetErrorString(e));
   c->epoch_np += npkt;
   return HC3D_OK;

@@ -138,10 +138,33 @@ class TtsStats(C.Structure):
                 ("counters", C.c_int64 * 16)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("slots", C.c_int), ("hbm_budget", C.c_int64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("par_path", C.c_char_p), ("par_dir", C.c_char_p), ("n_lucy", C.c_int), ("np_lucy", C.c_int64),
+                ("np", C.c_int64), ("npeel", C.c_int), ("thete", dp), ("phie", dp)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("err", C.c_char * 256), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("footprint_bytes", C.c_int64), ("packets", C.c_int64),
+                ("iterations", C.c_int), ("max_rel_change", C.c_double), ("nfreq", C.c_int), ("nmu", C.c_int),
+                ("nph", C.c_int), ("nap", C.c_int), ("npeel", C.c_int), ("si", i64p), ("nums", i64p),
+                ("ti", i64p), ("numt", i64p), ("stokes_scale", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("in_use_bytes", C.c_int64), ("peak_in_use_bytes", C.c_int64),
+                ("running", C.c_int), ("peak_running", C.c_int), ("queued", C.c_int64), ("completed", C.c_int64)]
+
+
 # every symbol the public headers declare, with its ctypes signature
 SIGNATURES = {
     "hc3d_create": (C.c_int, [P(C.c_void_p), P(DeviceOpts)]),
     "hc3d_destroy": (None, [C.c_void_p]),
+    "hc3d_reset": (C.c_int, [C.c_void_p]),
     "hc3d_get_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "hc3d_version": (C.c_char_p, []),
     "hc3d_load_tables": (C.c_int, [C.c_void_p, P(DustTables)]),
@@ -168,6 +191,13 @@ SIGNATURES = {
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
     "hc3d_write_synthetic_isrf": (C.c_int, [C.c_char_p]),
     "hc3d_star_packets": (C.c_int64, [C.c_double, C.c_int64]),
+    "hc3d_server_create": (C.c_int, [P(C.c_void_p), P(ServerOpts)]),
+    "hc3d_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_int64)]),
+    "hc3d_server_wait": (C.c_int, [C.c_void_p, C.c_int64, P(Result)]),
+    "hc3d_result_free": (None, [P(Result)]),
+    "hc3d_server_get_stats": (C.c_int, [C.c_void_p, P(ServerStats)]),
+    "hc3d_server_destroy": (None, [C.c_void_p]),
+    "hc3d_model_footprint": (C.c_int64, [C.c_void_p]),
 }
 
 _LIB = None
@@ -385,6 +415,12 @@ class Context:
         self.model = model
         return self
 
+    def reset(self) -> "Context":
+        """Drop the loaded model, keeping the stream, packet pool and queue (hc3d_reset)."""
+        self._check(lib().hc3d_reset(self._h))
+        self.model = None
+        return self
+
     def zero(self) -> None:
         self._check(lib().hc3d_zero_tallies(self._h))
 
@@ -521,6 +557,75 @@ def tts(par_path, out_dir, par_dir=None, precision: int = PREC_MIXED, device: in
     if rc != 0:
         raise Hc3dError(rc, err.value.decode())
     return st
+
+
+class Server:
+    """A model-run server on one GPU (hc3d_server_*): requests are queued,
+    admitted by device footprint against an HBM budget and run on `slots`
+    concurrent contexts."""
+
+    def __init__(self, slots: int = 4, precision: int = PREC_MIXED, device: int = 0, hbm_budget: int = 0):
+        h = C.c_void_p()
+        rc = lib().hc3d_server_create(C.byref(h), C.byref(ServerOpts(device, precision, slots, hbm_budget)))
+        if rc != 0:
+            raise Hc3dError(rc, "hc3d_server_create failed")
+        self._h = h
+
+    def submit(self, par_path, par_dir=None, n_lucy: int = -1, np_lucy: int = 0, np_: int = 0,
+               thete=None, phie=None) -> int:
+        """Queue a model run; thete/phie (radians) override the model's peel-off directions."""
+        q = Request(str(par_path).encode(), None if par_dir is None else str(par_dir).encode(), n_lucy, np_lucy,
+                    np_, 0, None, None)
+        keep = []
+        if thete is not None:
+            th = np.ascontiguousarray(thete, dtype=np.float64)
+            ph = np.ascontiguousarray(phie if phie is not None else np.zeros_like(th), dtype=np.float64)
+            keep = [th, ph]
+            q.npeel, q.thete, q.phie = len(th), _ptr(th), _ptr(ph)
+        t = C.c_int64(0)
+        rc = lib().hc3d_server_submit(self._h, C.byref(q), C.byref(t))
+        del keep
+        if rc != 0:
+            raise Hc3dError(rc, "hc3d_server_submit failed")
+        return t.value
+
+    def wait(self, ticket: int) -> dict:
+        """Block until the request is done; its SEDs and timings as a dict."""
+        r = Result()
+        rc = lib().hc3d_server_wait(self._h, ticket, C.byref(r))
+        if rc != 0:
+            raise Hc3dError(rc, r.err.decode())
+        sed = (r.nfreq, r.nmu, r.nph, r.nap, NO)
+        psed = (r.nfreq, r.npeel, r.nap, NO)
+        nsed, npsed = int(np.prod(sed)), int(np.prod(psed))
+        out = {k: getattr(r, k) for k in ("t_submit", "t_admit", "t_done", "footprint_bytes", "packets",
+                                          "iterations", "max_rel_change", "stokes_scale")}
+        out["si"] = np.ctypeslib.as_array(r.si, shape=(nsed,)).copy().reshape(sed, order="F")
+        out["nums"] = np.ctypeslib.as_array(r.nums, shape=(nsed,)).copy().reshape(sed, order="F")
+        if npsed:
+            out["ti"] = np.ctypeslib.as_array(r.ti, shape=(npsed,)).copy().reshape(psed, order="F")
+            out["numt"] = np.ctypeslib.as_array(r.numt, shape=(npsed,)).copy().reshape(psed, order="F")
+        else:
+            out["ti"] = np.zeros(psed, dtype=np.int64)
+            out["numt"] = np.zeros(psed, dtype=np.int64)
+        lib().hc3d_result_free(C.byref(r))
+        return out
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        lib().hc3d_server_get_stats(self._h, C.byref(st))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().hc3d_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def version() -> str:

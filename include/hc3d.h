@@ -190,6 +190,11 @@ typedef struct hc3d_tallies {
 /* ---- context ----------------------------------------------------------- */
 int hc3d_create(hc3d_ctx **ctx, const hc3d_device_opts *opts);
 void hc3d_destroy(hc3d_ctx *ctx);
+/* Drop the loaded model (tables, grid, tallies) and keep the stream, the
+ * packet pool and the peel-off queue, so that the next model loads without
+ * reallocating them (a serving slot runs model after model this way).  No
+ * counterpart in the reference, which runs one model per process. */
+int hc3d_reset(hc3d_ctx *ctx);
 int hc3d_get_error(const hc3d_ctx *ctx, char *buf, size_t len);
 /* Library version string and build architecture, e.g. "hc3d 0.1 sm_103a". */
 const char *hc3d_version(void);

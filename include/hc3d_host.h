@@ -106,6 +106,66 @@ typedef struct hc3d_tts_stats {
 int hc3d_tts(const char *par_path, const char *par_dir, const char *out_dir, const hc3d_device_opts *opts,
              hc3d_tts_stats *stats, char *err, size_t errlen);
 
+/* ---- model-run server -----------------------------------------------------
+ * No counterpart in the reference, which runs one model per process.  A
+ * server owns `slots` contexts on one device, each driven by a worker thread
+ * with its own stream.  Submitted requests are queued; a worker builds the
+ * model on the host, waits until the model's device footprint fits the HBM
+ * budget, then runs the Lucy iterations and the peeled iteration of
+ * newtts.F90:294-368 (no output files).  Runs of different slots overlap on
+ * the device.  A request's result does not depend on what else runs. */
+typedef struct hc3d_server hc3d_server;
+
+typedef struct hc3d_server_opts {
+  int device;          /* CUDA device ordinal */
+  int precision;       /* HC3D_PREC_MIXED or HC3D_PREC_FP64 */
+  int slots;           /* concurrent model runs, 1..64 */
+  int64_t hbm_budget;  /* bytes of model footprints admitted at once; 0 = 80 % of free device memory */
+} hc3d_server_opts;
+
+typedef struct hc3d_request {
+  const char *par_path;  /* the model's .par file */
+  const char *par_dir;   /* overrides PARDIR when non-NULL */
+  int n_lucy;            /* Lucy iterations; -1 = the model's NIMIN/NIMAX rule */
+  int64_t np_lucy;       /* packets per Lucy iteration; 0 = the model's */
+  int64_t np;            /* packets of the peeled iteration; 0 = NP */
+  int npeel;             /* peel-off directions of the request; 0 = the model's */
+  const double *thete, *phie; /* (npeel) radians */
+} hc3d_request;
+
+typedef struct hc3d_result {
+  int status;            /* HC3D_OK or the first error */
+  char err[256];
+  double t_submit, t_admit, t_done; /* seconds since the server started */
+  int64_t footprint_bytes;
+  int64_t packets;       /* all iterations */
+  int iterations;        /* Lucy iterations + 1 */
+  double max_rel_change; /* of the last Lucy iteration */
+  int nfreq, nmu, nph, nap, npeel;
+  int64_t *si, *nums;    /* (nfreq,nmu,nph,nap,8) SED of the peeled iteration, si x stokes_scale */
+  int64_t *ti, *numt;    /* (nfreq,npeel,nap,8) peeled SED, ti x stokes_scale */
+  double stokes_scale;
+} hc3d_result;
+
+typedef struct hc3d_server_stats {
+  int64_t budget_bytes, in_use_bytes, peak_in_use_bytes;
+  int running, peak_running;
+  int64_t queued, completed;
+} hc3d_server_stats;
+
+int hc3d_server_create(hc3d_server **s, const hc3d_server_opts *opts);
+/* Queue a request (the strings and arrays are copied); *ticket identifies it. */
+int hc3d_server_submit(hc3d_server *s, const hc3d_request *req, int64_t *ticket);
+/* Block until the request is done; the result's arrays are allocated for the
+ * caller and freed by hc3d_result_free.  Returns the request's status. */
+int hc3d_server_wait(hc3d_server *s, int64_t ticket, hc3d_result *out);
+void hc3d_result_free(hc3d_result *r);
+int hc3d_server_get_stats(hc3d_server *s, hc3d_server_stats *st);
+/* Finish the queued requests, then release the slots. */
+void hc3d_server_destroy(hc3d_server *s);
+/* Device bytes a run of the model holds, as the server's admission counts them. */
+int64_t hc3d_model_footprint(const hc3d_model *m);
+
 /* Write a synthetic 7-column dust file (dustinit's format, dust.f90:336)
  * and a 2-column stellar wavelength grid (atmosinit's format,
  * starbarb.f90:24-36): the fixtures of the benchmark models. */

@@ -109,3 +109,13 @@ def test_tally_scales_formula():
     assert (ss, sq, ps) == (2.0**34, 2.0**26, 2.0**28)
     ss, sq, ps = hc3d.tally_scales(10**8)
     assert ss == 2.0**27 and ps == 2.0**21
+
+
+def test_model_footprint_counts_grid_and_images(tmp_path, built):
+    """The server's admission size grows with the cells and the peel-off images."""
+    a = hc3d.Model(configs.write_par(tmp_path / "a", "tiny"))
+    b = hc3d.Model(configs.write_par(tmp_path / "b", "tiny", NPG=9))
+    c = hc3d.Model(configs.write_par(tmp_path / "c", "tiny", NPEEL=1, THETE="45.0", PHIE="0.0"))
+    fa, fb, fc = (int(hc3d.lib().hc3d_model_footprint(m._h)) for m in (a, b, c))
+    assert 0 < fc < fa < fb
+    assert fb - fa >= (b.info.ncells - a.info.ncells) * 200
