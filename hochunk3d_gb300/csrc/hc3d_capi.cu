@@ -847,6 +847,30 @@ extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
   return HC3D_OK;
 }
 
+// Launch shape of the per-thread transport kernel: a persistent grid of the
+// resident blocks, or fewer blocks when the batch is small.
+LaunchCfg transport_cfg(hc3d_ctx* c, int64_t np) {
+  LaunchCfg cfg;
+  cfg.threads = c->block_size;
+  cfg.stream = c->stream;
+  if (c->grid_blocks > 0) {
+    cfg.blocks = c->grid_blocks;
+    return cfg;
+  }
+  int per_sm = 0;
+  cudaError_t e;
+  if (c->precision == HC3D_PREC_FP64) {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_fp64(), cfg.threads, c->dm.dust_smem);
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_mixed(), cfg.threads, c->dm.dust_smem);
+  }
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  cfg.blocks = c->sm_count * per_sm;
+  const int64_t need = (np + cfg.threads - 1) / cfg.threads;
+  if (need < cfg.blocks) cfg.blocks = (int)std::max<int64_t>(1, need);
+  return cfg;
+}
+
 extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   if (!c) return HC3D_ERR_INVALID;
   CK(cudaSetDevice(c->device));
@@ -861,24 +885,7 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
     c->epoch_np += p->np;
     return HC3D_OK;
   }
-  LaunchCfg cfg;
-  cfg.threads = c->block_size;
-  cfg.stream = c->stream;
-  if (c->grid_blocks > 0) {
-    cfg.blocks = c->grid_blocks;
-  } else {
-    int per_sm = 0;
-    cudaError_t e;
-    if (c->precision == HC3D_PREC_FP64) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_fp64(), cfg.threads, c->dm.dust_smem);
-    } else {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_fn_mixed(), cfg.threads, c->dm.dust_smem);
-    }
-    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-    cfg.blocks = c->sm_count * per_sm;
-    const int64_t need = (p->np + cfg.threads - 1) / cfg.threads;
-    if (need < cfg.blocks) cfg.blocks = (int)std::max<int64_t>(1, need);
-  }
+  const LaunchCfg cfg = transport_cfg(c, p->np);
   CK(cudaEventRecord(c->ev0, c->stream));
   cudaError_t e = c->precision == HC3D_PREC_FP64 ? launch_transport_fp64(c->dm, c->dt, c->dims, a, cfg)
                                                  : launch_transport_mixed(c->dm, c->dt, c->dims, a, cfg);
@@ -999,13 +1006,7 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   return HC3D_OK;
 }
 
-extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* tdust_out, double* max_rel_change,
-                                int* converged) {
-  if (!c) return HC3D_ERR_INVALID;
-  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
-  if (!(ltot > 0.0) || np <= 0) return fail(c, HC3D_ERR_INVALID, "need ltot > 0 and np > 0");
-  if (!c->scales_set) return fail(c, HC3D_ERR_STATE, "no packets were run since the last hc3d_zero_tallies()");
-  CK(cudaSetDevice(c->device));
+LucyArgs lucy_args(hc3d_ctx* c, double ltot, int64_t np) {
   LucyArgs a;
   a.ncell = c->dm.ncell;
   a.nT = c->dm.nT;
@@ -1018,6 +1019,34 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
   a.tsub = c->tsub;
   a.na_min = 1.0e4;
   a.nslots = std::min(c->ndg_in, kSlots);
+  return a;
+}
+
+// the device temperatures into the reference's (nrg,ntg,npg,ndg) layout
+int tdust_to_host(hc3d_ctx* c, double* tdust_out) {
+  const DevModel& m = c->dm;
+  const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
+  std::vector<double> td((size_t)4 * n);
+  if (int r_ = d2h(c, td.data(), c->d_tdust, sizeof(double) * td.size())) return r_;
+  for (int s = 0; s < std::min(c->ndg_in, kSlots); ++s)
+    for (int ip = 1; ip < m.npg; ++ip)
+      for (int it = 1; it < m.ntg; ++it)
+        for (int ir = 1; ir < m.nrg; ++ir) {
+          const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+          const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+          tdust_out[c4 + n4 * s] = td[4 * cc + s];
+        }
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* tdust_out, double* max_rel_change,
+                                int* converged) {
+  if (!c) return HC3D_ERR_INVALID;
+  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
+  if (!(ltot > 0.0) || np <= 0) return fail(c, HC3D_ERR_INVALID, "need ltot > 0 and np > 0");
+  if (!c->scales_set) return fail(c, HC3D_ERR_STATE, "no packets were run since the last hc3d_zero_tallies()");
+  CK(cudaSetDevice(c->device));
+  const LucyArgs a = lucy_args(c, ltot, np);
   CK(cudaMemsetAsync(c->d_maxrel, 0, sizeof(unsigned long long), c->stream));
   k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust, c->d_tdustf,
                                                            c->d_peelmask, c->d_maxrel);
@@ -1029,20 +1058,95 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
   std::memcpy(&rel, &bits, sizeof(rel));
   if (max_rel_change) *max_rel_change = rel;
   if (converged) *converged = rel < 0.01 ? 1 : 0;
-  if (tdust_out) {
-    const DevModel& m = c->dm;
-    const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
-    std::vector<double> td((size_t)4 * n);
-    if (int r_ = d2h(c, td.data(), c->d_tdust, sizeof(double) * td.size())) return r_;
-    for (int s = 0; s < std::min(c->ndg_in, kSlots); ++s)
-      for (int ip = 1; ip < m.npg; ++ip)
-        for (int it = 1; it < m.ntg; ++it)
-          for (int ir = 1; ir < m.nrg; ++ir) {
-            const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
-            const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
-            tdust_out[c4 + n4 * s] = td[4 * cc + s];
-          }
+  if (tdust_out) return tdust_to_host(c, tdust_out);
+  return HC3D_OK;
+}
+
+// The Lucy iterations of newtts.F90:294-330 with a fixed count, captured as
+// one CUDA graph: per iteration, the tally reset of initarr(.false.), the
+// packet loop without peel-off and the temperature update (tfinal).  The
+// graph's kernels read their arguments from the capture, so iteration k runs
+// with iter = p->iter + k exactly as hc3d_zero_tallies + hc3d_run_iteration
+// + hc3d_lucy_update would; no host step sits between the iterations.
+extern "C" int hc3d_lucy_iterations(hc3d_ctx* c, const hc3d_run_params* p, int n_iter, double ltot,
+                                    double* max_rel_change, double* tdust_out) {
+  if (!c || !p || !max_rel_change || n_iter < 1 || n_iter > 1000) return HC3D_ERR_INVALID;
+  if (p->ipeel) return fail(c, HC3D_ERR_INVALID, "the Lucy iterations run without peel-off (ipeel = 0)");
+  if (!(ltot > 0.0) || p->np <= 0) return fail(c, HC3D_ERR_INVALID, "need ltot > 0 and np > 0");
+  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
+  CK(cudaSetDevice(c->device));
+  std::vector<RunArgs> args((size_t)n_iter);
+  for (int k = 0; k < n_iter; ++k) {
+    hc3d_run_params q = *p;
+    q.iter = p->iter + k;
+    c->scales_set = false;  // each iteration starts from zeroed tallies
+    c->epoch_np = 0;
+    const int r = prepare_run(c, &q, &args[(size_t)k]);
+    if (r) return r;
   }
+  std::vector<void*> tmp;
+  unsigned long long* d_rel = nullptr;
+  int r = dalloc(c, tmp, &d_rel, (size_t)n_iter);
+  if (r) return r;
+  const LaunchCfg cfg = transport_cfg(c, p->np);
+  const LucyArgs la = lucy_args(c, ltot, p->np);
+  const int64_t n = c->dm.ncell;
+  CK(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->dt.fault_count, 0, sizeof(unsigned long long), c->stream));
+  CK(cudaMemsetAsync(d_rel, 0, sizeof(unsigned long long) * n_iter, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < n_iter && e == cudaSuccess; ++k) {
+    const cudaStream_t st = c->stream;
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.nabs, 0, sizeof(unsigned long long) * kSlots * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.dtauabs, 0, sizeof(unsigned long long) * kSlots * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.jmean, 0, sizeof(unsigned long long) * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.killed, 0, sizeof(unsigned int) * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.dbig, 0, sizeof(unsigned int) * n, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * c->dims.nsed, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.counters, 0, sizeof(unsigned long long) * 16, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess)
+      e = c->precision == HC3D_PREC_FP64 ? launch_transport_fp64(c->dm, c->dt, c->dims, args[(size_t)k], cfg)
+                                         : launch_transport_mixed(c->dm, c->dt, c->dims, args[(size_t)k], cfg);
+    if (e == cudaSuccess) {
+      k_lucy<<<grid_blocks_for(c, la.ncell), 256, 0, st>>>(la, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust,
+                                                           c->d_tdustf, c->d_peelmask, d_rel + k);
+      e = cudaGetLastError();
+    }
+  }
+  const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+  if (e == cudaSuccess) e = ec;
+  cudaGraphExec_t exec = nullptr;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->stream);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    free_all(c, tmp);
+    return fail(c, HC3D_ERR_CUDA, std::string("Lucy graph: ") + cudaGetErrorString(e));
+  }
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->last_ms = ms;
+  c->last_transport_ms = ms;
+  c->last_peel_ms = 0.0;
+  c->last_launches = 2 * n_iter;
+  std::vector<unsigned long long> bits((size_t)n_iter);
+  r = d2h(c, bits.data(), d_rel, sizeof(unsigned long long) * n_iter);
+  free_all(c, tmp);
+  if (r) return r;
+  for (int k = 0; k < n_iter; ++k) std::memcpy(&max_rel_change[k], &bits[(size_t)k], sizeof(double));
+  if ((r = finish_run(c))) return r;
+  // the tallies now hold the last iteration, as after the step-by-step loop
+  c->scales_set = true;
+  c->epoch_np = p->np;
+  if (tdust_out) return tdust_to_host(c, tdust_out);
   return HC3D_OK;
 }
 

@@ -174,6 +174,7 @@ SIGNATURES = {
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
     "hc3d_lucy_update_noalloc": (C.c_int, [P(LucyBuffers), dp, ip_]),
+    "hc3d_lucy_iterations": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, C.c_double, dp, dp]),
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),
@@ -504,6 +505,16 @@ class Context:
         self._check(lib().hc3d_lucy_update(self._h, ltot, int(np_), None if td is None else td.ctypes.data_as(dp),
                                            C.byref(rel), C.byref(conv)))
         return td, rel.value, bool(conv.value)
+
+    def lucy_iterations(self, params: RunParams, n_iter: int, ltot: float, want_tdust: bool = True):
+        """n_iter Lucy iterations as one CUDA graph (hc3d_lucy_iterations):
+        returns (tdust, max_rel_change per iteration)."""
+        m = self.model
+        td = np.zeros(m.shape4, dtype=np.float64, order="F") if want_tdust else None
+        rel = np.zeros(n_iter, dtype=np.float64)
+        self._check(lib().hc3d_lucy_iterations(self._h, C.byref(params), int(n_iter), float(ltot), _ptr(rel),
+                                               None if td is None else td.ctypes.data_as(dp)))
+        return td, rel
 
     def trace(self, params: RunParams, uniforms: np.ndarray, max_rec: int = 4096):
         u = np.ascontiguousarray(uniforms, dtype=np.float64)

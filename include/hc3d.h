@@ -227,6 +227,16 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
+/* n_iter Lucy iterations of params->np packets without peel-off
+ * (newtts.F90:294-330 with a fixed count), captured as one CUDA graph and
+ * launched once: each iteration zeroes the tallies, runs the packet loop
+ * with iter = params->iter + k and updates the temperatures, as
+ * hc3d_zero_tallies + hc3d_run_iteration + hc3d_lucy_update would, with the
+ * same results.  max_rel_change receives n_iter values; tdust_out the last
+ * temperatures when non-NULL.  params->ipeel must be 0. */
+int hc3d_lucy_iterations(hc3d_ctx *ctx, const hc3d_run_params *params, int n_iter, double ltot,
+                         double *max_rel_change, double *tdust_out);
+
 /* ---- Lucy update that allocates nothing (no counterpart in the reference) --
  * hc3d_lucy_update() needs a context, and a context obtains its device
  * buffers with cudaMalloc.  Callers that cannot allocate device memory when

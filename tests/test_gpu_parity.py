@@ -238,3 +238,32 @@ def test_tts_writes_reference_outputs(fixtures_dir, built):
     assert len(list(out.glob("e_ALL_*_I_img.dat"))) == 10
     tm = (out / "tmidplane1.dat").read_text().splitlines()
     assert len(tm) == 2 + 39
+
+
+@pytest.mark.parametrize("prec", [hc3d.PREC_MIXED, hc3d.PREC_FP64])
+def test_lucy_graph_equals_the_step_by_step_loop(model_factory, prec):
+    """Three Lucy iterations as one CUDA graph give the temperatures, the
+    convergence maxima and the last iteration's tallies of three rounds of
+    zero + run + update, bit for bit."""
+    m = model_factory("tiny3d", warm=False)
+    n = 20000
+    td0 = m.tdust.copy(order="F")
+    ctx = _ctx(m, prec)
+    rels = []
+    for it in (1, 2, 3):
+        p = m.run_params(np=n, iter=it, ipeel=0)
+        ctx.zero()
+        ctx.run(p)
+        td_a, rel, _ = ctx.lucy_update(m.info.ltot, n)
+        rels.append(rel)
+    ta = ctx.tallies(m.run_params(np=n, iter=3, ipeel=0))
+    ctx.close()
+    m.set_tdust(td0)
+    ctx = _ctx(m, prec)
+    td_b, rel_b = ctx.lucy_iterations(m.run_params(np=n, iter=1, ipeel=0), 3, m.info.ltot)
+    tb = ctx.tallies(m.run_params(np=n, iter=3, ipeel=0))
+    ctx.close()
+    np.testing.assert_array_equal(td_a, td_b)
+    np.testing.assert_array_equal(np.array(rels), rel_b)
+    for k in ("nabs", "dtauabs", "jmean", "si", "nums", "counters"):
+        np.testing.assert_array_equal(ta[k], tb[k], err_msg=k)
