@@ -307,6 +307,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison run")
     ap.add_argument("--no-serving", action="store_true", help="skip the model-grid and serving measurements")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default peel-off queue depth")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one untimed peeled step after the Lucy set-up and print its crossing and launch "
                          "counts (the command a DRAM-traffic capture of k_wave / k_peel_mixed runs)")
@@ -338,6 +339,8 @@ def main():
         model = build_model(Path(td), args.workload)
         ctx = hc3d.Context(hc3d.PREC_MIXED, device=local).load(model)
         warm_up_temperatures(model, ctx, args.lucy_packets)
+        # the peel-off queue depth, chosen by timing a sample batch (untimed set-up)
+        tune = ctx.autotune(model.run_params(np=200000, iter=900, ipeel=1)) if not args.no_autotune else None
         stream = torch.cuda.ExternalStream(ctx.stream)
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -488,7 +491,8 @@ def main():
                                "peel_directions": int(model.npeel), "image": [int(model._p.nxhst)] * 2 + [4],
                                "nfreq": int(model._p.nfreq), "packets_per_step": n,
                                "l2": "256 MiB buffer written between timed steps",
-                               "lucy_setup": f"2 iterations x {args.lucy_packets} packets"},
+                               "lucy_setup": f"2 iterations x {args.lucy_packets} packets",
+                               "autotune": tune},
                     "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),
                             "d2h_bytes_per_step": int(d2h)},
                     "fp64": fp64, "grid_build": grid_build, "table_build": table_build,

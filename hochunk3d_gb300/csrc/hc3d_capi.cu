@@ -1,6 +1,7 @@
 // hc3d_capi.cu -- the C-ABI of include/hc3d.h: context, device layouts,
 // the Lucy temperature solve and tally read-back.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -900,6 +901,76 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   c->last_launches = 1;
   c->epoch_np += p->np;
   return HC3D_OK;
+}
+
+// The autotuner: times one sample batch under each candidate launch setting
+// and keeps the fastest.  Peeled runs (the wavefront form) tune the depth of
+// the peel-off queue, which sets the events per packet in a wave and so the
+// number of waves; runs without peel-off tune the block size of the
+// per-thread transport kernel.  Every candidate runs the same packets (the
+// streams are keyed by packet id), so the timings differ by the setting
+// alone.  The tallies are zeroed afterwards.
+extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tune_result* out) {
+  if (!c || !sample || !out || sample->np <= 0) return HC3D_ERR_INVALID;
+  if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
+  std::memset(out, 0, sizeof *out);
+  const bool waves = sample->ipeel && c->use_waves;
+  const int64_t queues[4] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+  const int blocks[3] = {64, 96, 128};
+  const int n = waves ? 4 : 3;
+  const int64_t q0 = c->queue_records;
+  const int b0 = c->block_size;
+  double best = 1e300;
+  for (int k = 0; k < n; ++k) {
+    if (waves) {
+      if (c->wave.pool) {  // reallocated by the next run at the new depth
+        CK(cudaStreamSynchronize(c->stream));
+        free_all(c, c->wave_allocs);
+        c->wave = WaveBufs{};
+        for (int i = 0; i < 3; ++i)
+          if (c->wev[i]) {
+            cudaEventDestroy(c->wev[i]);
+            c->wev[i] = nullptr;
+          }
+      }
+      c->queue_records = queues[k];
+    } else {
+      c->block_size = blocks[k];
+    }
+    int r = hc3d_zero_tallies(c);
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!r) r = hc3d_run_iteration(c, sample);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (r) {
+      c->queue_records = q0;
+      c->block_size = b0;
+      return r;
+    }
+    out->queue_records[k] = c->queue_records;
+    out->block_size[k] = c->block_size;
+    out->ms[k] = ms;
+    if (ms < best) {
+      best = ms;
+      out->best = k;
+    }
+  }
+  out->n = n;
+  if (waves) {
+    if (c->queue_records != out->queue_records[out->best]) {
+      CK(cudaStreamSynchronize(c->stream));
+      free_all(c, c->wave_allocs);
+      c->wave = WaveBufs{};
+      for (int i = 0; i < 3; ++i)
+        if (c->wev[i]) {
+          cudaEventDestroy(c->wev[i]);
+          c->wev[i] = nullptr;
+        }
+    }
+    c->queue_records = out->queue_records[out->best];
+  } else {
+    c->block_size = out->block_size[out->best];
+  }
+  return hc3d_zero_tallies(c);
 }
 
 extern "C" int hc3d_get_fault_log(hc3d_ctx* c, uint64_t* entries, int max, int* n) {

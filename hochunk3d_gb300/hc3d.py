@@ -138,6 +138,11 @@ class TtsStats(C.Structure):
                 ("counters", C.c_int64 * 16)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("queue_records", C.c_int64 * 4), ("block_size", C.c_int * 4),
+                ("ms", C.c_double * 4)]
+
+
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("slots", C.c_int), ("hbm_budget", C.c_int64)]
 
@@ -175,6 +180,7 @@ SIGNATURES = {
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
     "hc3d_lucy_update_noalloc": (C.c_int, [P(LucyBuffers), dp, ip_]),
     "hc3d_lucy_iterations": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, C.c_double, dp, dp]),
+    "hc3d_autotune": (C.c_int, [C.c_void_p, P(RunParams), P(TuneResult)]),
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),
@@ -505,6 +511,13 @@ class Context:
         self._check(lib().hc3d_lucy_update(self._h, ltot, int(np_), None if td is None else td.ctypes.data_as(dp),
                                            C.byref(rel), C.byref(conv)))
         return td, rel.value, bool(conv.value)
+
+    def autotune(self, sample: RunParams) -> dict:
+        """Time the sample batch under each candidate setting and keep the fastest (hc3d_autotune)."""
+        r = TuneResult()
+        self._check(lib().hc3d_autotune(self._h, C.byref(sample), C.byref(r)))
+        return {"candidates": [{"queue_records": int(r.queue_records[k]), "block_size": int(r.block_size[k]),
+                                "ms": float(r.ms[k])} for k in range(r.n)], "best": int(r.best)}
 
     def lucy_iterations(self, params: RunParams, n_iter: int, ltot: float, want_tdust: bool = True):
         """n_iter Lucy iterations as one CUDA graph (hc3d_lucy_iterations):

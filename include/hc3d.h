@@ -227,6 +227,20 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
+/* ---- autotuner (no counterpart in the reference) ---------------------------
+ * Times the sample batch under each candidate setting and keeps the fastest
+ * in the context: the peel-off queue depth (2^20 .. 2^23 records) for peeled
+ * runs, the transport block size (64, 96, 128) otherwise.  The tallies are
+ * zeroed afterwards. */
+typedef struct hc3d_tune_result {
+  int n;                     /* candidates timed */
+  int best;                  /* index of the setting the context now uses */
+  int64_t queue_records[4];  /* per candidate */
+  int block_size[4];
+  double ms[4];              /* wall time of the sample batch */
+} hc3d_tune_result;
+int hc3d_autotune(hc3d_ctx *ctx, const hc3d_run_params *sample, hc3d_tune_result *out);
+
 /* n_iter Lucy iterations of params->np packets without peel-off
  * (newtts.F90:294-330 with a fixed count), captured as one CUDA graph and
  * launched once: each iteration zeroes the tallies, runs the packet loop
