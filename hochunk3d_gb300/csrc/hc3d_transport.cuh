@@ -1306,6 +1306,7 @@ constexpr int kPeelThreads = 256;
 constexpr int kPeelBuf = 64;
 constexpr int kPeelChunk = 256;  // rays a warp reserves per atomic, at most
 constexpr int kPeelStage = 4;    // records a warp stages in shared memory
+constexpr int kPeelSub = 8;      // crossings per lane between refills of the ray pool
 
 // peeloff_3d.f90:155-282 for one ray of the mixed form that reached the grid
 // edge: attenuation, the Stokes rotation of a scattered packet, image pixel
@@ -2181,9 +2182,18 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
     const bool idle = !__any_sync(0xffffffffu, have) && !more && rbase >= rend;
     bool out = false;
     if (have) {
-      const int st = w.step(m, cap, pc);
-      out = st == PeelWalk::OUT;
-      if (st != PeelWalk::GOING) have = false;
+      // up to kPeelSub crossings between refills: the warp-wide refill and
+      // parking steps run once per kPeelSub crossings, at the cost of a lane
+      // whose ray ends idling for the rest of the round
+#pragma unroll 1
+      for (int sub = 0; sub < kPeelSub; ++sub) {
+        const int st = w.step(m, cap, pc);
+        if (st != PeelWalk::GOING) {
+          out = st == PeelWalk::OUT;
+          have = false;
+          break;
+        }
+      }
     }
     // park the rays that left the grid; tally them 32 at a time
     const unsigned outm = __ballot_sync(0xffffffffu, out);
