@@ -22,6 +22,7 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <vector>
@@ -69,6 +70,7 @@ struct hc3d_server {
   clk::time_point t0;
   std::deque<Request> queue;
   std::map<int64_t, Result> done;
+  std::set<int64_t> claimed;  // tickets whose result was handed out
   std::mutex mu;
   std::condition_variable cv_queue, cv_mem, cv_done;
   std::vector<std::thread> workers;
@@ -296,7 +298,9 @@ extern "C" int hc3d_server_wait(hc3d_server* s, int64_t ticket, hc3d_result* out
   Result res;
   {
     std::unique_lock<std::mutex> lk(s->mu);
-    if (ticket >= s->next_ticket) return HC3D_ERR_INVALID;
+    // an unknown ticket, or one whose result was already handed out, would wait forever
+    if (ticket >= s->next_ticket || s->claimed.count(ticket)) return HC3D_ERR_INVALID;
+    s->claimed.insert(ticket);
     s->cv_done.wait(lk, [&] { return s->done.count(ticket) != 0; });
     res = std::move(s->done[ticket]);
     s->done.erase(ticket);

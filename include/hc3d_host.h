@@ -157,7 +157,9 @@ int hc3d_server_create(hc3d_server **s, const hc3d_server_opts *opts);
 /* Queue a request (the strings and arrays are copied); *ticket identifies it. */
 int hc3d_server_submit(hc3d_server *s, const hc3d_request *req, int64_t *ticket);
 /* Block until the request is done; the result's arrays are allocated for the
- * caller and freed by hc3d_result_free.  Returns the request's status. */
+ * caller and freed by hc3d_result_free.  Returns the request's status, or
+ * HC3D_ERR_INVALID for a ticket that was not issued or was already waited
+ * for (one wait per ticket). */
 int hc3d_server_wait(hc3d_server *s, int64_t ticket, hc3d_result *out);
 void hc3d_result_free(hc3d_result *r);
 int hc3d_server_get_stats(hc3d_server *s, hc3d_server_stats *st);

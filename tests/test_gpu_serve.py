@@ -53,7 +53,10 @@ def test_results_same_alone_and_in_the_mix(pars):
 def test_requested_peel_directions_and_packets(pars):
     s = hc3d.Server(slots=2)
     th = np.radians([30.0, 60.0, 85.0])
-    r = s.wait(s.submit(pars[0], n_lucy=1, np_lucy=4000, np_=5000, thete=th))
+    t = s.submit(pars[0], n_lucy=1, np_lucy=4000, np_=5000, thete=th)
+    r = s.wait(t)
+    with pytest.raises(hc3d.Hc3dError):
+        s.wait(t)  # a ticket is waited for once
     s.close()
     assert r["ti"].shape[1] == 3 and r["numt"].sum() > 0
     assert r["packets"] == 4000 + 5000 and r["iterations"] == 2
