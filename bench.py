@@ -203,6 +203,66 @@ def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
     pars = model_grid_pars(tmp / "grid", n, 5e4, 5e5, seed=4)
     out = {"models": n, "packets_per_model": "log-uniform 5e4..5e5 per iteration",
            "iterations": "2 Lucy + 1 peeled", "grids": [list(g) for g in GRID_SHAPES]}
+    # the Lucy iterations of the grid: one batched launch per iteration for all
+    # models (hc3d_run_batch) against one launch per model
+    models = [hc3d.Model(p) for p in pars]
+    ctxs = [hc3d.Context(hc3d.PREC_MIXED, device=device).load(m) for m in models]
+    lucy = {}
+    for mode in ("batched", "one_by_one"):
+        for c, m in zip(ctxs, models):
+            c.reset().load(m)
+        t0 = time.perf_counter()
+        pk = 0
+        for it in (1, 2):
+            ps = [m.run_params(np=int(m.info.np_lucy), iter=it, ipeel=0) for m in models]
+            for c in ctxs:
+                c.zero()
+            if mode == "batched":
+                hc3d.run_batch(ctxs, ps)
+            else:
+                for c, p in zip(ctxs, ps):
+                    c.run(p)
+            for c, m, p in zip(ctxs, models, ps):
+                c.lucy_update(m.info.ltot, p.np, want_tdust=False)
+            pk += sum(p.np for p in ps)
+        dt = time.perf_counter() - t0
+        lucy[mode] = {"seconds": dt, "packets_per_s": pk / dt}
+    for c in ctxs:
+        c.close()
+    out["lucy_iterations"] = lucy
+    # the whole grid with its Lucy iterations batched: the models built on the
+    # host, both Lucy iterations of all models as one launch each, then the
+    # peeled iterations of the models on `slots` host threads, one context each
+    from concurrent.futures import ThreadPoolExecutor
+
+    t0 = time.perf_counter()
+    models = [hc3d.Model(p) for p in pars]
+    ctxs = [hc3d.Context(hc3d.PREC_MIXED, device=device).load(m) for m in models]
+    pk = 0
+    for it in (1, 2):
+        ps = [m.run_params(np=int(m.info.np_lucy), iter=it, ipeel=0) for m in models]
+        for c in ctxs:
+            c.zero()
+        hc3d.run_batch(ctxs, ps)
+        for c, m, p in zip(ctxs, models, ps):
+            c.lucy_update(m.info.ltot, p.np, want_tdust=False)
+        pk += sum(p.np for p in ps)
+
+    def peeled(cm):
+        c, m = cm
+        p = m.run_params(np=int(m.info.np), iter=3, ipeel=1)
+        c.zero()
+        c.run(p)
+        c.tallies(p, grid=False)
+        return p.np
+
+    with ThreadPoolExecutor(slots) as ex:
+        pk += sum(ex.map(peeled, zip(ctxs, models)))
+    dt = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    out["batched_lucy_pipeline"] = {"seconds": dt, "models_per_hr": n / dt * 3600.0, "packets_per_s": pk / dt,
+                                    "peel_threads": slots}
     for k in (slots, 1):
         srv = hc3d.Server(slots=k, device=device)
         t0 = time.perf_counter()

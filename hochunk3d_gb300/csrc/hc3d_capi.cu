@@ -903,6 +903,81 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   return HC3D_OK;
 }
 
+// Several models' packets in one persistent launch (k_transport_batch): the
+// Lucy iterations of a model grid run as one launch per iteration, the
+// small models' long-history tails beside the bulk of the others.  Each
+// context keeps its own tallies, which equal those of hc3d_run_iteration.
+extern "C" int hc3d_run_batch(hc3d_ctx* const* ctxs, const hc3d_run_params* params, int n) {
+  if (!ctxs || !params || n < 1 || n > kMaxBatch) return HC3D_ERR_INVALID;
+  hc3d_ctx* c = ctxs[0];
+  if (!c) return HC3D_ERR_INVALID;
+  for (int j = 0; j < n; ++j) {
+    if (!ctxs[j]) return HC3D_ERR_INVALID;
+    if (ctxs[j]->device != c->device || ctxs[j]->precision != c->precision)
+      return fail(c, HC3D_ERR_INVALID, "batched contexts must share the device and the precision");
+    for (int i = 0; i < j; ++i)
+      if (ctxs[i] == ctxs[j]) return fail(c, HC3D_ERR_INVALID, "a context appears twice in the batch");
+    if (params[j].ipeel) return fail(c, HC3D_ERR_INVALID, "batched runs are unpeeled (ipeel = 0)");
+  }
+  CK(cudaSetDevice(c->device));
+  std::vector<BatchItem> items((size_t)n);
+  std::vector<int64_t> first((size_t)n + 1, 0);
+  for (int j = 0; j < n; ++j) {
+    hc3d_ctx* cj = ctxs[j];
+    const int r = prepare_run(cj, &params[j], &items[(size_t)j].a);
+    if (r) {
+      if (cj != c) c->err = "model " + std::to_string(j) + ": " + cj->err;
+      return r;
+    }
+    if (cudaStreamSynchronize(cj->stream) != cudaSuccess) return fail(c, HC3D_ERR_CUDA, "batch: stream sync");
+    items[(size_t)j].m = cj->dm;
+    items[(size_t)j].m.dust_smem = 0;
+    items[(size_t)j].t = cj->dt;
+    items[(size_t)j].d = cj->dims;
+    first[(size_t)j + 1] = first[(size_t)j] + params[j].np;
+  }
+  const int64_t total = first[(size_t)n];
+  if (total == 0) return HC3D_OK;
+  std::vector<void*> tmp;
+  BatchItem* d_items = nullptr;
+  int64_t* d_first = nullptr;
+  unsigned long long* d_work = nullptr;
+  int r;
+  if ((r = dupload(c, tmp, &d_items, items.data(), items.size())) ||
+      (r = dupload(c, tmp, &d_first, first.data(), first.size())) || (r = dalloc(c, tmp, &d_work, 1))) {
+    free_all(c, tmp);
+    return r;
+  }
+  CK(cudaMemsetAsync(d_work, 0, sizeof(unsigned long long), c->stream));
+  int per_sm = 0;
+  const bool f64 = c->precision == HC3D_PREC_FP64;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f64 ? transport_batch_fn_fp64() : transport_batch_fn_mixed(),
+                                                    128, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  LaunchCfg cfg;
+  cfg.threads = 128;
+  cfg.blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)c->sm_count * per_sm, (total + 127) / 128));
+  cfg.stream = c->stream;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  cudaError_t e = f64 ? launch_transport_batch_fp64(d_items, d_first, n, d_work, total, cfg)
+                      : launch_transport_batch_mixed(d_items, d_first, n, d_work, total, cfg);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  free_all(c, tmp);
+  if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("batched transport: ") + cudaGetErrorString(e));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  for (int j = 0; j < n; ++j) {
+    hc3d_ctx* cj = ctxs[j];
+    if ((r = finish_run(cj))) return r;
+    cj->epoch_np += params[j].np;
+    cj->last_ms = cj->last_transport_ms = ms;
+    cj->last_peel_ms = 0.0;
+    cj->last_launches = 1;
+  }
+  return HC3D_OK;
+}
+
 // The autotuner: times one sample batch under each candidate launch setting
 // and keeps the fastest.  Peeled runs (the wavefront form) tune the depth of
 // the peel-off queue, which sets the events per packet in a wave and so the

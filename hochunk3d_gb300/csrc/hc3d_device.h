@@ -158,6 +158,24 @@ const void* wave_fn_fp64();
 const void* peel_fn_mixed();
 const void* peel_fn_fp64();
 
+// One model of a batched launch: its device model (dust tables read from
+// global memory), tallies, tally shape and run arguments.
+struct BatchItem {
+  DevModel m;
+  DevTallies t;
+  TallyDims d;
+  RunArgs a;
+};
+constexpr int kMaxBatch = 256;
+// k_transport over the packets of several models at once: packet g of the
+// launch belongs to model j with first[j] <= g < first[j+1]
+cudaError_t launch_transport_batch_mixed(const BatchItem* items, const int64_t* first, int n, unsigned long long* work,
+                                         int64_t total, const LaunchCfg& cfg);
+cudaError_t launch_transport_batch_fp64(const BatchItem* items, const int64_t* first, int n, unsigned long long* work,
+                                        int64_t total, const LaunchCfg& cfg);
+const void* transport_batch_fn_mixed();
+const void* transport_batch_fn_fp64();
+
 int transport_regs_mixed();
 int transport_regs_fp64();
 const void* transport_fn_mixed();

@@ -19,6 +19,14 @@ int transport_regs_mixed() {
 
 const void* transport_fn_mixed() { return (const void*)dev::k_transport<float>; }
 
+cudaError_t launch_transport_batch_mixed(const BatchItem* items, const int64_t* first, int n, unsigned long long* work,
+                                         int64_t total, const LaunchCfg& cfg) {
+  dev::k_transport_batch<float><<<cfg.blocks, cfg.threads, 0, cfg.stream>>>(items, first, n, work, total);
+  return cudaGetLastError();
+}
+
+const void* transport_batch_fn_mixed() { return (const void*)dev::k_transport_batch<float>; }
+
 }  // namespace hc3d
 
 namespace hc3d {

@@ -2023,6 +2023,41 @@ __global__ void __launch_bounds__(128) k_transport(DevModel m, DevTallies t, Tal
   flush(t, L);
 }
 
+// ---- batched form: the packets of several models in one persistent launch ------------
+// Every thread takes the next packet of the whole batch from one counter,
+// finds its model by bisection in the packet ranges, and runs it with that
+// model's tables, grid, tallies and run arguments.  Dust tables are read
+// from global memory (each model has its own), and the event counters go
+// straight to the model's global counters.  A model's packets keep their
+// global ids and streams, so a batched run gives the tallies of the model
+// run alone.
+template <class R>
+__global__ void __launch_bounds__(128) k_transport_batch(const BatchItem* items, const int64_t* first, int n,
+                                                         unsigned long long* work, int64_t total) {
+  __shared__ int64_t sfirst[kMaxBatch + 1];
+  for (int i = threadIdx.x; i <= n; i += blockDim.x) sfirst[i] = first[i];
+  __syncthreads();
+  Tracer tr{nullptr, 0, 0};
+  for (;;) {
+    const unsigned long long g = atomicAdd(work, 1ull);
+    if (g >= (unsigned long long)total) break;
+    int lo = 0, hi = n;  // sfirst[lo] <= g < sfirst[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if ((int64_t)g >= sfirst[mid]) lo = mid; else hi = mid;
+    }
+    const BatchItem& b = items[lo];
+    DustView<R> dv;
+    dust_view<R>(b.m, nullptr, dv);  // the host set dust_smem = 0: global tables, no barrier
+    Local L;
+    L.sc = b.t.counters;
+    L.fault = 0;
+    Rng rng;
+    rng_init(rng, b.a.key0, b.a.key1, (uint64_t)(b.a.packet_offset + ((int64_t)g - sfirst[lo])));
+    run_packet<R>(b.m, dv, b.t, b.d, b.a, rng, L, tr);
+  }
+}
+
 // ---- wavefront form: packet pool + peel-off event queue ----------------------------
 // Each thread owns one pool slot.  A wave advances every live packet by up
 // to E events (taking new packets from the batch as slots free up) and

@@ -181,6 +181,7 @@ SIGNATURES = {
     "hc3d_lucy_update_noalloc": (C.c_int, [P(LucyBuffers), dp, ip_]),
     "hc3d_lucy_iterations": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, C.c_double, dp, dp]),
     "hc3d_autotune": (C.c_int, [C.c_void_p, P(RunParams), P(TuneResult)]),
+    "hc3d_run_batch": (C.c_int, [P(C.c_void_p), P(RunParams), C.c_int]),
     "hc3d_get_stream": (C.c_void_p, [C.c_void_p]),
     "hc3d_last_kernel_ms": (C.c_int, [C.c_void_p, P(C.c_double)]),
     "hc3d_last_launch_stats": (C.c_int, [C.c_void_p, ip_, P(C.c_double), P(C.c_double)]),
@@ -581,6 +582,19 @@ def tts(par_path, out_dir, par_dir=None, precision: int = PREC_MIXED, device: in
     if rc != 0:
         raise Hc3dError(rc, err.value.decode())
     return st
+
+
+def run_batch(contexts, params) -> None:
+    """The unpeeled packet loops of several loaded contexts in one persistent
+    launch (hc3d_run_batch); each context's tallies equal a run of its own."""
+    n = len(contexts)
+    hs = (C.c_void_p * n)(*[c._h.value for c in contexts])
+    ps = (RunParams * n)(*params)
+    rc = lib().hc3d_run_batch(hs, ps, n)
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        lib().hc3d_get_error(contexts[0]._h, buf, 1024)
+        raise Hc3dError(rc, buf.value.decode())
 
 
 class Server:

@@ -227,6 +227,13 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
+/* The unpeeled packet loops of n models (1..256) in one persistent launch:
+ * ctxs[j] runs params[j] (ipeel = 0) with its own tables, grid and tallies,
+ * and its tallies equal those of hc3d_run_iteration(ctxs[j], &params[j]).
+ * All contexts share one device and precision; the launch runs on the
+ * stream of ctxs[0].  No counterpart in the reference (one model per run). */
+int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
+
 /* ---- autotuner (no counterpart in the reference) ---------------------------
  * Times the sample batch under each candidate setting and keeps the fastest
  * in the context: the peel-off queue depth (2^20 .. 2^23 records) for peeled

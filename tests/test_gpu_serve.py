@@ -87,3 +87,26 @@ def test_admission_by_device_footprint(pars):
         s.wait(big)
     assert e.value.code == -3
     s.close()
+
+
+@pytest.mark.parametrize("prec", [hc3d.PREC_MIXED, hc3d.PREC_FP64])
+def test_batched_launch_equals_separate_runs(pars, prec):
+    """The unpeeled packet loops of four models in one persistent launch
+    (hc3d_run_batch) give each model the tallies of its own run."""
+    models = [hc3d.Model(p) for p in pars]
+    params = [m.run_params(np=6000 + 1000 * k, iter=2, ipeel=0) for k, m in enumerate(models)]
+    want = []
+    for m, p in zip(models, params):
+        ctx = hc3d.Context(prec).load(m)
+        ctx.zero(); ctx.run(p)
+        want.append(ctx.tallies(p))
+        ctx.close()
+    ctxs = [hc3d.Context(prec).load(m) for m in models]
+    for c in ctxs:
+        c.zero()
+    hc3d.run_batch(ctxs, params)
+    for k, (c, p) in enumerate(zip(ctxs, params)):
+        got = c.tallies(p)
+        for key in ("si", "nums", "nabs", "dtauabs", "jmean", "killed", "counters"):
+            np.testing.assert_array_equal(got[key], want[k][key], err_msg=f"model {k} {key}")
+        c.close()
