@@ -1,6 +1,7 @@
 """CPU tests of the boundary and the host-side model set-up (no GPU calls)."""
 from __future__ import annotations
 
+import ctypes as C
 import re
 from pathlib import Path
 
@@ -119,3 +120,22 @@ def test_model_footprint_counts_grid_and_images(tmp_path, built):
     fa, fb, fc = (int(hc3d.lib().hc3d_model_footprint(m._h)) for m in (a, b, c))
     assert 0 < fc < fa < fb
     assert fb - fa >= (b.info.ncells - a.info.ncells) * 200
+
+
+def test_new_entry_points_reject_bad_arguments(built):
+    """The batch, graph, autotune, reset and server entry points check their
+    arguments before they touch a device (no GPU needed)."""
+    L = hc3d.lib()
+    assert L.hc3d_reset(None) == -1
+    assert L.hc3d_run_batch(None, None, 1) == -1
+    assert L.hc3d_lucy_iterations(None, None, 3, 1.0, None, None) == -1
+    assert L.hc3d_autotune(None, None, None) == -1
+    h = C.c_void_p()
+    assert L.hc3d_server_create(C.byref(h), C.byref(hc3d.ServerOpts(0, 0, 0, 0))) == -1  # no slots
+    assert L.hc3d_server_create(C.byref(h), C.byref(hc3d.ServerOpts(0, 0, 65, 0))) == -1  # too many
+    assert L.hc3d_server_submit(None, None, None) == -1
+    r = hc3d.Result()
+    assert L.hc3d_server_wait(None, 1, C.byref(r)) == -1
+    assert L.hc3d_model_footprint(None) == -1
+    L.hc3d_result_free(None)
+    L.hc3d_server_destroy(None)

@@ -146,3 +146,22 @@ def test_thin_model_external_packets_cross_unscattered(O, model_factory):
     unscat = (c[hc3d.CNT["sumall"]] - c[hc3d.CNT["sumsub"]]) / r["stokes_scale"]
     assert unscat >= 0.99 * (n - p.n_star)
     assert c[hc3d.CNT["escaped"]] + c[hc3d.CNT["aflux"]] == n
+
+
+def test_sharded_external_runs_sum_to_one_run(O, model_factory):
+    """Two packet ranges of one iteration (packet_offset) split the stellar
+    and external packets by the iteration's global n_star, so their tallies
+    add up exactly to the single run's."""
+    m = model_factory("tiny_isrf")
+    n = 2400
+    whole = m.run_params(np=n, iter=2, ipeel=1)
+    a = O.run(m, whole)
+    k = 1100
+    first = m.run_params(np=k, iter=2, ipeel=1, n_star=whole.n_star)
+    second = m.run_params(np=n - k, iter=2, ipeel=1, packet_offset=k, n_star=whole.n_star)
+    sc = hc3d.tally_scales(n)  # the fixed-point scales of the whole iteration on both ranges
+    a = O.run(m, whole, scales=sc)
+    b, c = O.run(m, first, scales=sc), O.run(m, second, scales=sc)
+    assert 0 < whole.n_star < n
+    for key in ("si", "nums", "ti", "numt", "nabs", "dtauabs", "jmean"):
+        np.testing.assert_array_equal(a[key], b[key] + c[key], err_msg=key)
