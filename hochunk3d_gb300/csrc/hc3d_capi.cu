@@ -214,7 +214,9 @@ int check_params(hc3d_ctx* c, const hc3d_run_params* p) {
     if (!p->thete || !p->phie) return fail(c, HC3D_ERR_INVALID, "thete/phie are NULL");
     if (p->nxhst < 1) return fail(c, HC3D_ERR_INVALID, "nxhst must be >= 1");
   }
-  if (p->limb != 0) return fail(c, HC3D_ERR_UNSUPPORTED, "limb-darkening table (CLIMB=YES) is not supported");
+  if (p->limb != 0 && p->limb != 1) return fail(c, HC3D_ERR_INVALID, "limb must be 0 or 1");
+  if (p->limb == 1 && c->tables && c->dm.nlimb < 2)
+    return fail(c, HC3D_ERR_INVALID, "limb = 1 needs the limb-darkening table (ntab) of hc3d_load_tables");
   if (!(p->numin > 0.0) || !(p->numax > p->numin)) return fail(c, HC3D_ERR_INVALID, "need 0 < numin < numax");
   if (!(p->rstar_cm > 0.0) || !(p->rmaxi > 0.0 || !p->ipeel)) return fail(c, HC3D_ERR_INVALID, "bad rstar_cm/rmaxi");
   return HC3D_OK;
@@ -280,6 +282,7 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
     if (!(p->rmax > 1.0)) return fail(c, HC3D_ERR_INVALID, "ext_illum needs rmax > 1 (stellar radii)");
     if (p->n_star < 0) return fail(c, HC3D_ERR_INVALID, "n_star < 0");
   }
+  a->limb = p->limb;
   a->ext_illum = p->ext_illum ? 1 : 0;
   a->n_star = p->n_star;
   a->rmax = p->rmax;
@@ -611,6 +614,17 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
         (r = dupload(c, own, &d_if, t->isrf_logfreq, (size_t)t->nisrf)))
       return r;
     c->dm.nisrf = t->nisrf; c->dm.isrf_cdf = d_ic; c->dm.isrf_logcdf = d_il; c->dm.isrf_logfreq = d_if;
+  }
+  // limb-darkening table (tabl_mod)
+  c->dm.nlimb = 0;
+  if (t->ntab > 0) {
+    if (t->ntab < 2 || !t->limb_xmu || !t->limb_prob)
+      return fail(c, HC3D_ERR_INVALID, "limb-darkening table: ntab < 2 or a NULL pointer");
+    double *d_x, *d_p;
+    if ((r = dupload(c, own, &d_x, t->limb_xmu, (size_t)t->ntab)) ||
+        (r = dupload(c, own, &d_p, t->limb_prob, (size_t)t->ntab)))
+      return r;
+    c->dm.nlimb = t->ntab; c->dm.limb_xmu = d_x; c->dm.limb_prob = d_p;
   }
   // FP32 copies for the mixed form
   {

@@ -82,6 +82,8 @@ struct DevModel {
   const double* hnuint; const double* atmosnu; const double* lognu; const double* loghnu;
   int nisrf;  // external radiation field (isrf_mod): cdf_i, logcdf_i, logfreq_i; 0 = none
   const double* isrf_cdf; const double* isrf_logcdf; const double* isrf_logfreq;
+  int nlimb;  // rows of the limb-darkening table (tabl_mod ntab), CLIMB=YES; 0 = none
+  const double* limb_xmu; const double* limb_prob;
   // FP32 copies of the per-event tables, read by the mixed form
   const float* nudustf; const float* kappadf; const float* adustf; const float* gdustf; const float* pldustf;
   const float* lTintf; const float* nuintf; const float* kapBintf;
@@ -109,6 +111,7 @@ struct RunArgs {
   float kapfac[kSlots];      // rstar_cm * kappa_V of each slot, FP32 (mixed-form opacities)
   int iintmax;
   int64_t max_interactions;
+  int limb;                  // 1: Eddington limb darkening of the stellar emission
   int ext_illum;             // packets with global id >= n_star enter from the outer sphere
   int64_t n_star;
   double rmax;               // outer radius, R*

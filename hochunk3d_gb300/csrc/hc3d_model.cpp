@@ -644,7 +644,17 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
     REQ(P.str("ISRF_FILE", &sv, err)); m->isrf_file = m->pardir + "/" + sv;
   }
   REQ(P.integer("CLIMB", &iv, err)); m->limb = (int)iv;
-  if (m->limb != 0) { *err = "CLIMB=YES (limb-darkening table) is not supported"; return false; }
+  if (m->limb) {
+    // table (samptabl.f90:1-23): xmu(1) = 0, xmu(i) = i/ntab, prob(i) = 0.5 (mu^3 + mu^2), prob(1) = 0
+    const double delmu = 1.0 / (double)kNtab;
+    m->limb_xmu.assign(kNtab, 0.0);
+    m->limb_prob.assign(kNtab, 0.0);
+    for (int i = 2; i <= kNtab; ++i) {
+      const double x = delmu * (double)i;
+      m->limb_xmu[i - 1] = x;
+      m->limb_prob[i - 1] = 0.5 * (std::pow(x, 3.0) + std::pow(x, 2.0));
+    }
+  }
   REQ(P.integer("CPLANCKST", &iv, err)); m->iplanckst = (int)iv;
   REQ(P.str("ATNAME", &sv, err)); m->atname = m->pardir + "/" + sv;
   REQ(P.real("RSTAR", &m->rstar, err));
@@ -1078,6 +1088,9 @@ hc3d_dust_tables Model::tables_view() const {
   if (iout) {
     t.nisrf = (int)isrf_cdfv.size(); t.isrf_cdf = isrf_cdfv.data(); t.isrf_logcdf = isrf_logcdf.data();
     t.isrf_logfreq = isrf_logfreq.data();
+  }
+  if (limb) {
+    t.ntab = (int)limb_xmu.size(); t.limb_xmu = limb_xmu.data(); t.limb_prob = limb_prob.data();
   }
   return t;
 }

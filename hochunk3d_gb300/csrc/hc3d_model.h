@@ -42,6 +42,7 @@ class ParFile {
 };
 
 constexpr int kNisrf = 200;  // isrf_mod nisrf
+constexpr int kNtab = 100;   // tabl_mod ntab (module not shipped; restated)
 
 struct Model {
   // ---- reapar/setup scalars (units after setup.f90) ----
@@ -73,6 +74,8 @@ struct Model {
   double lstar = 0, l_isrf = 0, isrf_frac = 0;
   std::string isrf_file;
   std::vector<double> isrf_cdfv, isrf_logcdf, isrf_logfreq;
+  // limb-darkening table (tabl_mod) for CLIMB=YES
+  std::vector<double> limb_xmu, limb_prob;
   int image = 1;
   int64_t maxint = 1000000;
   uint64_t seed = 0;

@@ -1194,10 +1194,11 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
   if (flags & kRecNoPeel) return;
   R sip = e.sip, sqp = e.sqp, sup = e.sup, svp = e.svp;
   if (flags & 128) {
-    // newdisktherm.F90:342-360: limb = 0 weight of a stellar-surface packet
+    // newdisktherm.F90:342-360: weight of a stellar-surface packet, uniform
+    // disk (limb = 0) or Eddington limb darkening (limb = 1)
     const R cosnorm = e.d0 * coste + (e.d1 * sinte * (cospe * e.d2 + sinpe * e.d3));
     if (!(cosnorm > R(0))) return;
-    sip = R(4) * e.sip * cosnorm;
+    sip = a.limb ? R(12.0 / 5.0) * e.sip * (cosnorm + cosnorm * cosnorm) : R(4) * e.sip * cosnorm;
   }
   double xp1 = e.x, yp1 = e.y, zp1 = e.z;
   int ir = e.ir, it = e.it, ip = e.ip;
@@ -1319,7 +1320,10 @@ __device__ __forceinline__ void peel_tally_mixed(const DevTallies& t, const Tall
   const int i_orig = (flags >> 2) & 7;
   const float coste = dd.coste, sinte = dd.sinte, cospe = dd.cospe, sinpe = dd.sinpe;
   float sip = e.sip, sqp = e.sqp, sup = e.sup, svp = e.svp;
-  if (flags & 128) sip = 4.f * e.sip * (e.d0 * coste + (e.d1 * sinte * (cospe * e.d2 + sinpe * e.d3)));
+  if (flags & 128) {  // newdisktherm.F90:342-360, limb = 0 or 1
+    const float cosnorm = e.d0 * coste + (e.d1 * sinte * (cospe * e.d2 + sinpe * e.d3));
+    sip = a.limb ? (float)(12.0 / 5.0) * e.sip * (cosnorm + cosnorm * cosnorm) : 4.f * e.sip * cosnorm;
+  }
   const float factor = expf(-tsum);
   sip *= factor; sqp *= factor; sup *= factor; svp *= factor;
   if (iflag == 1) {
@@ -1758,6 +1762,19 @@ __device__ __forceinline__ void initp_transform(Pkt<R>& p) {
   p.cosp = xcos(p.phi);
 }
 
+// darkening (samptabl.f90:29-65): mu from the table of prob(mu) = (mu^3 + mu^2)/2
+// (Eddington limb darkening, intensity ~ 1 + mu), interpolated as the Fortran
+// does, with the table step delmu = 1/ntab
+template <class R>
+__device__ __forceinline__ R darkening(const DevModel& m, Rng& rng) {
+  const double xi = (double)ran<R>(rng);
+  int n = locate_dev(m.limb_prob, m.nlimb, xi);  // 1 <= n <= ntab-1 for 0 < xi < 1
+  n = n < 1 ? 1 : (n > m.nlimb - 1 ? m.nlimb - 1 : n);
+  const double delmu = 1.0 / (double)m.nlimb;
+  const double p1 = __ldg(m.limb_prob + n), p0 = __ldg(m.limb_prob + n - 1);
+  return (R)(__ldg(m.limb_xmu + n) - (p1 - xi) / (p1 - p0) * delmu);
+}
+
 // Stellar packet emission, newdisktherm.F90:256-337 with initpspot (spot-free),
 // initp_sample (limb = 0) and initp_transform.  rec receives the
 // stellar-surface peel-off event.
@@ -1775,7 +1792,8 @@ __device__ void emit_star(const DevModel& m, const DustView<R>& dv, const RunArg
     if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
   }
   p.lp = (R)kR2p * ran<R>(rng);
-  p.cost = xsqrt(ran<R>(rng));
+  // initp_sample (initp_common.f90:1-29): cost = sqrt(xi), or the Eddington table
+  p.cost = a.limb ? darkening<R>(m, rng) : xsqrt(ran<R>(rng));
   p.sint = xsqrt(R(1) - p.cost * p.cost);
   p.phi = (R)kR2p * ran<R>(rng);
   p.cosp = xcos(p.phi);

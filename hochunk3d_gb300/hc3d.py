@@ -65,6 +65,7 @@ class DustTables(C.Structure):
         ("nT", C.c_int), ("nnu", C.c_int), ("lTint", dp), ("nuint", dp), ("kapBint", dp), ("kappap", dp),
         ("tsub", C.c_double), ("nhnu", C.c_int), ("hnuint", dp), ("atmosnu", dp), ("lognu", dp), ("loghnu", dp),
         ("nisrf", C.c_int), ("isrf_cdf", dp), ("isrf_logcdf", dp), ("isrf_logfreq", dp),
+        ("ntab", C.c_int), ("limb_xmu", dp), ("limb_prob", dp),
     ]
 
 
@@ -299,6 +300,8 @@ class Model:
         self.nisrf = t.nisrf
         self.isrf_cdf = _arr(t.isrf_cdf, t.nisrf); self.isrf_logcdf = _arr(t.isrf_logcdf, t.nisrf)
         self.isrf_logfreq = _arr(t.isrf_logfreq, t.nisrf)
+        self.ntab = t.ntab
+        self.limb_xmu = _arr(t.limb_xmu, t.ntab); self.limb_prob = _arr(t.limb_prob, t.ntab)
         # run parameters
         self.npeel = p.npeel
         self.thete = _arr(p.thete, p.npeel); self.phie = _arr(p.phie, p.npeel)
@@ -319,6 +322,9 @@ class Model:
         if self.nisrf:
             for n in ("isrf_cdf", "isrf_logcdf", "isrf_logfreq"):
                 setattr(t, n, _ptr(getattr(self, n)))
+        t.ntab = self.ntab
+        if self.ntab:
+            t.limb_xmu, t.limb_prob = _ptr(self.limb_xmu), _ptr(self.limb_prob)
         return t
 
     @property

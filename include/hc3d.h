@@ -99,6 +99,9 @@ typedef struct hc3d_dust_tables {
   const double *isrf_cdf;     /* (nisrf) cdf_i of isrf_cdf.f90: cumulative, 0 .. 1 */
   const double *isrf_logcdf;  /* (nisrf) logcdf_i: log10 cdf_i, -99 at row 1 */
   const double *isrf_logfreq; /* (nisrf) logfreq_i: log10 frequency (1.2398/lambda[um]), 0 at row 1 */
+  int ntab;               /* rows of the limb-darkening table (tabl_mod) for limb = 1; 0 = none */
+  const double *limb_xmu;     /* (ntab) xmu of samptabl.f90 table: 0, 2d, 3d, .., 1 with d = 1/ntab */
+  const double *limb_prob;    /* (ntab) prob: 0.5 (mu^3 + mu^2), 0 at row 1 */
 } hc3d_dust_tables;
 
 /* grid_mod (grid_mod.f90:20-50) as gridset leaves it. */
@@ -137,7 +140,7 @@ typedef struct hc3d_run_params {
   double numin, numax;    /* SED frequency range, units of 1.2398/lambda[um] */
   double rstar_cm;        /* stellar radius in cm (rmincgs) */
   double tstar;           /* stellar temperature, K/11605 */
-  int limb;               /* 0 = uniform disk; 1 (limb-darkening table) is not supported */
+  int limb;               /* 0 = uniform disk; 1 = Eddington limb darkening (the table of hc3d_dust_tables) */
   int iintmax;            /* interactions in one cell before a packet is killed (10000) */
   int64_t max_interactions; /* per-packet cap on interactions; 0 = no cap */
   int image;              /* 1 = accumulate broadband I,Q,U,V images of the peeled packets */

@@ -52,6 +52,7 @@ typedef struct orc_ctx {
   hc3d_grid g;
   int ndg;
   int64_t ncell4; /* nrg*ntg*npg */
+  int limb;       /* run parameter limb (0 or 1) */
 } orc_ctx;
 
 /* Tallies: the fixed-point arrays of hc3d_tallies plus FP64 sums of the
@@ -760,6 +761,16 @@ static void orc_initp_transform(pkt *p) {
   p->cosp = cos(p->phi);
 }
 
+/* ---- darkening, samptabl.f90:29-65 (delmu = 1/ntab of tabl_mod) --------- */
+static double orc_darkening(const orc_ctx *c, double xi) {
+  const hc3d_dust_tables *d = &c->dt;
+  int n = orc_locate(d->limb_prob, d->ntab, xi);
+  if (n < 1) n = 1;
+  if (n > d->ntab - 1) n = d->ntab - 1;
+  const double delmu = 1.0 / (double)d->ntab;
+  return d->limb_xmu[n] - (d->limb_prob[n] - xi) / (d->limb_prob[n] - d->limb_prob[n - 1]) * delmu;
+}
+
 /* ---- initpspot (ispot=0) with initp_sample, initp_common.f90:1-29 -------- */
 static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
   p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
@@ -770,8 +781,8 @@ static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
     if (p->cosb != 0.0 && fabs(p->cosb) < 1.0) break;
   }
   p->lp = ORC_R2P * orc_ran(rng);
-  /* initp_sample, limb = 0 */
-  p->cost = sqrt(orc_ran(rng));
+  /* initp_sample: uniform disk (limb = 0) or the Eddington table (darkening) */
+  p->cost = c->limb ? orc_darkening(c, orc_ran(rng)) : sqrt(orc_ran(rng));
   p->sint = sqrt(1.0 - p->cost * p->cost);
   p->phi = ORC_R2P * orc_ran(rng);
   p->cosp = cos(p->phi);
@@ -989,7 +1000,8 @@ static void orc_packet(const orc_ctx *c, const hc3d_run_params *rp, int64_t pid,
       const double coste = cos(rp->thete[k]), sinte = sin(rp->thete[k]);
       const double cospe = cos(rp->phie[k]), sinpe = sin(rp->phie[k]);
       const double cosnorm = p.cosb * coste + (p.sinb * sinte * (cospe * coslp + sinpe * sinlp));
-      const double sipnew = 4.0 * p.sip * cosnorm; /* limb = 0 */
+      /* limb = 0: I constant, energy/sr ~ mu; limb = 1: I ~ 1 + mu (newdisktherm.F90:349-355) */
+      const double sipnew = rp->limb ? 12.0 / 5.0 * p.sip * (cosnorm + cosnorm * cosnorm) : 4.0 * p.sip * cosnorm;
       if (cosnorm > 0.0) orc_peeloff(c, rp, &p, sipnew, 0, 0, k, t);
     }
   }
@@ -1005,6 +1017,7 @@ int orc_version(void) { return 1; }
 static void orc_ctx_init(orc_ctx *c, const hc3d_dust_tables *dt, const hc3d_grid *g) {
   c->dt = *dt;
   c->g = *g;
+  c->limb = 0;
   c->ndg = g->ndg;
   c->ncell4 = (int64_t)g->nrg * g->ntg * g->npg;
 }
@@ -1014,6 +1027,7 @@ int orc_run_range(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run
                   int64_t pid_begin, int64_t pid_end) {
   orc_ctx c;
   orc_ctx_init(&c, dt, g);
+  c.limb = rp->limb;
   for (int64_t pid = pid_begin; pid < pid_end; ++pid) {
     orc_rng rng;
     orc_rng_init(&rng, rp->seed, rp->iter, rp->packet_offset + pid);
@@ -1029,6 +1043,7 @@ int orc_trace_packet(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_
                      int *exhausted) {
   orc_ctx c;
   orc_ctx_init(&c, dt, g);
+  c.limb = rp->limb;
   orc_rng rng;
   orc_rng_init(&rng, rp->seed, rp->iter, rp->packet_offset + pid);
   if (uniforms) { rng.inj = uniforms; rng.ninj = nu; rng.pos = 0; }
@@ -1099,6 +1114,13 @@ double orc_lucydustfreq_c(const hc3d_dust_tables *dt, const hc3d_grid *g, double
   orc_rng_init(&r, 0, 0, 0);
   r.inj = &xi; r.ninj = 1; r.pos = 0;
   return orc_lucydustfreq(&c, T0, id, &r);
+}
+
+/* darkening for one uniform xi (tests) */
+double orc_darkening_c(const hc3d_dust_tables *dt, const hc3d_grid *g, double xi) {
+  orc_ctx c;
+  orc_ctx_init(&c, dt, g);
+  return orc_darkening(&c, xi);
 }
 
 /* rep_isrf for one injected uniform xi (tests) */

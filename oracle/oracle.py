@@ -53,6 +53,8 @@ def lib() -> C.CDLL:
         L.orc_lucydustfreq_c.restype = C.c_double
         L.orc_rep_isrf_c.argtypes = [P(DustTables), P(Grid), C.c_double]
         L.orc_rep_isrf_c.restype = C.c_double
+        L.orc_darkening_c.argtypes = [P(DustTables), P(Grid), C.c_double]
+        L.orc_darkening_c.restype = C.c_double
         L.orc_dusttemp.argtypes = [P(DustTables)] + [C.c_double] * 4 + [C.c_int, C.c_double]
         L.orc_dusttemp.restype = C.c_double
         L.orc_tfinal.argtypes = [P(DustTables), P(Grid), dp, C.c_double, C.c_double, dp]
@@ -156,6 +158,13 @@ def rep_isrf(model: hc3d.Model, xi) -> np.ndarray:
     L = lib()
     t, g = model.tables, model.grid
     return np.array([L.orc_rep_isrf_c(C.byref(t), C.byref(g), float(x)) for x in np.atleast_1d(xi)])
+
+
+def darkening(model: hc3d.Model, xi) -> np.ndarray:
+    """Emission cosines of the limb-darkening table for the uniforms xi (darkening)."""
+    L = lib()
+    t, g = model.tables, model.grid
+    return np.array([L.orc_darkening_c(C.byref(t), C.byref(g), float(x)) for x in np.atleast_1d(xi)])
 
 
 def stream(seed: int, it: int, pid: int, n: int) -> np.ndarray:

@@ -216,9 +216,13 @@ def test_invalid_arguments_are_rejected(model_factory):
     with pytest.raises(hc3d.Hc3dError) as e:
         ctx.run(m.run_params(np=10, ipeel=1, npeel=1000))
     assert e.value.code == -1
+    # limb darkening needs the table that a CLIMB=YES model loads
     with pytest.raises(hc3d.Hc3dError) as e:
         ctx.run(m.run_params(np=10, limb=1))
-    assert e.value.code == -7
+    assert e.value.code == -1 and "limb" in str(e.value)
+    with pytest.raises(hc3d.Hc3dError) as e:
+        ctx.run(m.run_params(np=10, limb=2))
+    assert e.value.code == -1
 
 
 def test_tts_writes_reference_outputs(fixtures_dir, built):

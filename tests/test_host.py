@@ -41,7 +41,7 @@ def test_missing_key_is_an_error(tmp_path, built):
     assert "NRG" in str(e.value)
 
 
-@pytest.mark.parametrize("key", ["CSPOT", "CDISKACC", "DIFFUSION", "CLIMB"])
+@pytest.mark.parametrize("key", ["CSPOT", "CDISKACC", "DIFFUSION"])
 def test_unsupported_options_are_rejected(tmp_path, built, key):
     par = configs.write_par(tmp_path, "tiny", **{key: "YES"})
     with pytest.raises(hc3d.Hc3dError) as e:
