@@ -339,7 +339,13 @@ class Model:
             setattr(g, n, a.ctypes.data_as(dp))
         return g
 
-    def run_params(self, **over) -> RunParams:
+    def run_params(self, np_total: int | None = None, **over) -> RunParams:
+        """The model's run parameters with fields of RunParams overridden.
+
+        n_star, the stellar share of the iteration, follows np unless given.
+        A shard of an iteration (packet_offset > 0, or np below the whole)
+        passes np_total, the packets of the whole iteration, so that every
+        shard splits stellar and external packets as one run would."""
         q = RunParams()
         for f, _ in RunParams._fields_:
             setattr(q, f, getattr(self._p, f))
@@ -347,10 +353,12 @@ class Model:
         q.phie = _ptr(self.phie)
         q.aperture2 = _ptr(self.aperture2)
         for k, v in over.items():
+            if not hasattr(q, k):
+                raise AttributeError(f"RunParams has no field {k}")
             setattr(q, k, v)
-        if "np" in over and "n_star" not in over:
-            # the stellar share of this call's packets (newdisktherm.F90:143-175)
-            q.n_star = star_packets(self.info.isrf_frac, q.np)
+        if "n_star" not in over and (np_total is not None or "np" in over):
+            # the stellar share of the iteration's packets (newdisktherm.F90:143-175)
+            q.n_star = star_packets(self.info.isrf_frac, q.np if np_total is None else np_total)
         return q
 
     def set_tdust(self, tdust: np.ndarray) -> None:

@@ -28,7 +28,7 @@ def _free_port() -> int:
     return p
 
 
-def _rank(rank, world, port, directory, n, q):
+def _rank(rank, world, port, directory, n, q, name):
     import torch
     import torch.distributed as dist
 
@@ -40,13 +40,13 @@ def _rank(rank, world, port, directory, n, q):
     try:
         # each rank writes its own copy of the model files: two ranks writing
         # one directory at once could read each other's half-written files
-        m = make_model(directory / f"rank{rank}", "tiny3d")
+        m = make_model(directory / f"rank{rank}", name)
     except Exception as e:  # report instead of leaving the parent waiting
         q.put(e)
         raise
     dist.init_process_group("gloo", rank=rank, world_size=world)
     lo, hi = n * rank // world, n * (rank + 1) // world
-    p = m.run_params(np=hi - lo, packet_offset=lo, iter=2, ipeel=1)
+    p = m.run_params(np=hi - lo, packet_offset=lo, iter=2, ipeel=1, np_total=n)
     r = O.run(m, p, scales=hc3d.tally_scales(n))
     out = {}
     for k in KEYS + ("counters",):
@@ -59,7 +59,10 @@ def _rank(rank, world, port, directory, n, q):
     dist.destroy_process_group()
 
 
-def test_two_rank_shards_sum_to_the_single_run(tmp_path, built):
+@pytest.mark.parametrize("name", ["tiny3d", "tiny_isrf"])
+def test_two_rank_shards_sum_to_the_single_run(tmp_path, built, name):
+    """With external illumination the shards split stellar and external
+    packets by the iteration's global stellar share (np_total)."""
     import oracle.oracle as O
     from hochunk3d_gb300 import hc3d
 
@@ -67,7 +70,7 @@ def test_two_rank_shards_sum_to_the_single_run(tmp_path, built):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, tmp_path / "m", n, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, tmp_path / "m", n, q, name)) for r in range(2)]
     for p in procs:
         p.start()
     got = q.get(timeout=300)
@@ -76,7 +79,7 @@ def test_two_rank_shards_sum_to_the_single_run(tmp_path, built):
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
-    m = make_model(tmp_path / "single", "tiny3d")
+    m = make_model(tmp_path / "single", name)
     ref = O.run(m, m.run_params(np=n, iter=2, ipeel=1), scales=hc3d.tally_scales(n))
     for k in KEYS + ("counters",):
         np.testing.assert_array_equal(got[k], np.ascontiguousarray(ref[k]).astype(np.int64), err_msg=k)
