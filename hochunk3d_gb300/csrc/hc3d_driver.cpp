@@ -74,15 +74,24 @@ const char* kSedHeader =
     "# Lambda         I          I_err         Q/I       (Q/I)_err       U/I       (U/I)_err       V/I       (V/I)_err\n";
 
 // diskflux (flux.f90:23-121) + output (output.F90:166-503), ASCII part
-int write_outputs(const Model& m, const hc3d_run_params& p, const Tallies& T, const std::vector<double>& tdust_used,
-                  const std::vector<double>& tdust2, const std::string& dir) {
+int write_outputs(const Model& m, const hc3d_run_params& p, const hc3d_tallies& t, const double* tdust_used,
+                  const double* tdust2, const std::string& dir) {
+  // the nine SED and peeled-SED arrays and the four images, in hc3d_tallies order
+  const int64_t* sed[9] = {t.si, t.sq, t.su, t.sv, t.si2, t.sq2, t.su2, t.sv2, t.nums};
+  const int64_t* psed[9] = {t.ti, t.tq, t.tu, t.tv, t.ti2, t.tq2, t.tu2, t.tv2, t.numt};
+  const int64_t* img[4] = {t.image_i, t.image_q, t.image_u, t.image_v};
+  for (int k = 0; k < 9; ++k)
+    if (!sed[k] || (p.ipeel && !psed[k])) return HC3D_ERR_INVALID;
+  for (int k = 0; k < 4; ++k)
+    if (p.ipeel && p.image && !img[k]) return HC3D_ERR_INVALID;
+  if (!tdust_used || !tdust2) return HC3D_ERR_INVALID;
   const double lsol = hc3d::kLsun;
   const double rnp = (double)p.np;
   const double rnorm = rnp / (double)p.nmu / (double)p.nph / (m.ltot / lsol);
   const double image_norm = rnp / (m.ltot / lsol);
   const double nurat = m.numax / m.numin;
   const double nunorm = std::pow(nurat, 0.5 / p.nfreq) - std::pow(nurat, -0.5 / p.nfreq);
-  const double ss = T.t.stokes_scale, sq = T.t.square_scale;
+  const double ss = t.stokes_scale, sq = t.square_scale;
   std::vector<double> wav(p.nfreq);
   for (int i = 0; i < p.nfreq; ++i) wav[i] = 1.2398 / (m.numin * std::pow(nurat, ((double)(i + 1) - 0.5) / p.nfreq));
   // ---- flux*.dat ----
@@ -98,11 +107,11 @@ int write_outputs(const Model& m, const hc3d_run_params& p, const Tallies& T, co
         for (int ip = 0; ip < p.nph; ++ip)
           for (int inub = 0; inub < p.nfreq; ++inub) {
             const int64_t b = inub + (int64_t)p.nfreq * (i + (int64_t)p.nmu * (ip + (int64_t)p.nph * ia)) + nsed * io;
-            const double n = (double)T.sed[8][b];
-            double si = T.sed[0][b] / ss, sQ = T.sed[1][b] / ss, sU = T.sed[2][b] / ss, sV = T.sed[3][b] / ss;
+            const double n = (double)sed[8][b];
+            double si = sed[0][b] / ss, sQ = sed[1][b] / ss, sU = sed[2][b] / ss, sV = sed[3][b] / ss;
             double e[4] = {0, 0, 0, 0};
             if (n > 1.0) {
-              const double s2[4] = {T.sed[4][b] / sq, T.sed[5][b] / sq, T.sed[6][b] / sq, T.sed[7][b] / sq};
+              const double s2[4] = {sed[4][b] / sq, sed[5][b] / sq, sed[6][b] / sq, sed[7][b] / sq};
               const double s1[4] = {si, sQ, sU, sV};
               for (int k = 0; k < 4; ++k) {
                 double var = (s2[k] - s1[k] * s1[k] / n) / (n - 1.0) * n;
@@ -131,12 +140,12 @@ int write_outputs(const Model& m, const hc3d_run_params& p, const Tallies& T, co
         for (int ia = 0; ia < p.nap; ++ia)
           for (int inub = 0; inub < p.nfreq; ++inub) {
             const int64_t b = inub + (int64_t)p.nfreq * (k + (int64_t)p.npeel * ia) + npsed * io;
-            const double n = (double)T.psed[8][b];
-            double t1[4] = {T.psed[0][b] / ss, T.psed[1][b] / ss, T.psed[2][b] / ss, T.psed[3][b] / ss};
+            const double n = (double)psed[8][b];
+            double t1[4] = {psed[0][b] / ss, psed[1][b] / ss, psed[2][b] / ss, psed[3][b] / ss};
             double e[4] = {0, 0, 0, 0};
             if (n > 1.0)
               for (int q = 0; q < 4; ++q) {
-                const double t2 = T.psed[4 + q][b] / sq;
+                const double t2 = psed[4 + q][b] / sq;
                 const double var = t1[q] != 0.0 ? (t2 * n / (t1[q] * t1[q]) - 1.0) / (n - 1.0) : 0.0;
                 e[q] = std::sqrt(std::max(var, 0.0));
               }
@@ -164,10 +173,10 @@ int write_outputs(const Model& m, const hc3d_run_params& p, const Tallies& T, co
           for (int iy = 0; iy < nx; ++iy) {
             for (int ix = 0; ix < nx; ++ix) {
               const int64_t b = k + (int64_t)p.npeel * (ix + (int64_t)nx * iy);
-              const double I = T.img[0][b] / ss;
+              const double I = img[0][b] / ss;
               double v;
               if (q == 0) v = I / image_norm_intensity;
-              else v = I > 0.0 ? (T.img[q][b] / ss) / I : 0.0;
+              else v = I > 0.0 ? (img[q][b] / ss) / I : 0.0;
               std::fprintf(f, "%s ", es11(v).c_str());
             }
             std::fputc('\n', f);
@@ -309,7 +318,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   st.seconds_lucy = std::chrono::duration<double>(t1 - t0).count();
   st.seconds_final = std::chrono::duration<double>(t2 - t1).count();
   for (int k = 0; k < 16; ++k) st.counters[k] = T.t.counters[k];
-  r = write_outputs(m, p, T, tdust_used, tdust2, out_dir);
+  r = write_outputs(m, p, T.t, tdust_used.data(), tdust2.data(), out_dir);
   if (r) {
     put_err(err, errlen, std::string("cannot write outputs into ") + out_dir);
     hc3d_destroy(ctx);
@@ -320,4 +329,13 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   hc3d_destroy(ctx);
   hc3d_model_destroy(hm);
   return HC3D_OK;
+}
+
+extern "C" int hc3d_write_outputs(const hc3d_model* hm, const hc3d_run_params* p, const hc3d_tallies* t,
+                                  const double* tdust_used, const double* tdust, const char* out_dir) {
+  if (!hm || !p || !t || !tdust_used || !tdust || !out_dir) return HC3D_ERR_INVALID;
+  if (!(t->stokes_scale > 0.0) || !(t->square_scale > 0.0)) return HC3D_ERR_INVALID;
+  if (p->nfreq < 1 || p->nmu < 1 || p->nph < 1 || p->nap < 1 || (p->ipeel && (p->npeel < 1 || !p->thete)))
+    return HC3D_ERR_INVALID;
+  return write_outputs(hm->m, *p, *t, tdust_used, tdust, out_dir);
 }

@@ -168,6 +168,16 @@ void hc3d_server_destroy(hc3d_server *s);
 /* Device bytes a run of the model holds, as the server's admission counts them. */
 int64_t hc3d_model_footprint(const hc3d_model *m);
 
+/* diskflux (flux.f90:23-121) and the ASCII writers of output
+ * (output.F90:166-503) for tallies the host holds, e.g. after summing the
+ * tallies of several ranks: flux*.dat, peel_flux*.dat, e_ALL_*_img.dat
+ * (when params->image), tmidplane*.dat and tave*.dat into out_dir.  The
+ * tally pointers follow hc3d_tallies (nabs .. dbig are not read); tdust_used
+ * and tdust are the (nrg,ntg,npg,ndg) temperatures before and after the
+ * last Lucy update.  hc3d_tts calls the same writer. */
+int hc3d_write_outputs(const hc3d_model *m, const hc3d_run_params *params, const hc3d_tallies *tallies,
+                       const double *tdust_used, const double *tdust, const char *out_dir);
+
 /* Write a synthetic 7-column dust file (dustinit's format, dust.f90:336)
  * and a 2-column stellar wavelength grid (atmosinit's format,
  * starbarb.f90:24-36): the fixtures of the benchmark models. */
