@@ -1,8 +1,10 @@
 // hc3d_driver.cpp -- program tts (newtts.F90:141-368) over the C-ABI:
 // Lucy iterations, the final peeled iteration, diskflux (flux.f90:23-121)
 // and the ASCII writers of output (output.F90:166-503).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -234,6 +236,90 @@ int write_outputs(const Model& m, const hc3d_run_params& p, const hc3d_tallies& 
   return HC3D_OK;
 }
 
+// output_grid (output.F90:38-150): a Fortran unformatted sequential file,
+// each record framed by its length in a 4-byte integer before and after it:
+// the cell counts and lastdim, the cell-centre radii in AU, the polar and
+// azimuthal cell centres, then the array over the cells (ir fastest) for
+// id = 1..lastdim.  real8 (8-byte) or integer (4-byte) arrays, (nrg, ntg, npg,
+// lastdim) in Fortran order; the wall entries (ir = nrg, ...) are skipped.
+int write_grid_unf(const Model& m, const std::string& path, int lastdim, const double* r8, const int32_t* i4) {
+  if (lastdim < 1 || (!r8 && !i4) || (r8 && i4)) return HC3D_ERR_INVALID;
+  const int64_t nc = m.ncells(), n4 = m.n4();
+  const int64_t body = nc * lastdim * (r8 ? 8 : 4);
+  if (body > 0x7fffffffLL) return HC3D_ERR_UNSUPPORTED;  // would need Fortran subrecords
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return HC3D_ERR_IO;
+  bool ok = true;
+  auto rec = [&](const void* d, int64_t bytes) {
+    const uint32_t nb = (uint32_t)bytes;
+    ok = ok && std::fwrite(&nb, 4, 1, f) == 1 && (bytes == 0 || std::fwrite(d, 1, (size_t)bytes, f) == (size_t)bytes) &&
+         std::fwrite(&nb, 4, 1, f) == 1;
+  };
+  const int32_t dims[4] = {m.nrg - 1, m.ntg - 1, m.npg - 1, lastdim};
+  rec(dims, sizeof dims);
+  std::vector<double> v((size_t)std::max(m.nrg, std::max(m.ntg, m.npg)));
+  for (int i = 0; i < m.nrg - 1; ++i) v[i] = m.ravearr[i] / m.autors;
+  rec(v.data(), 8LL * (m.nrg - 1));
+  for (int i = 0; i < m.ntg - 1; ++i) v[i] = m.thetavearr[i];
+  rec(v.data(), 8LL * (m.ntg - 1));
+  for (int i = 0; i < m.npg - 1; ++i) v[i] = 0.5 * (m.phiarr[i] + m.phiarr[i + 1]);  // phiavearr, gridset.f90:654
+  rec(v.data(), 8LL * (m.npg - 1));
+  std::vector<unsigned char> buf((size_t)body);
+  int64_t k = 0;
+  for (int id = 0; id < lastdim; ++id)
+    for (int ip = 0; ip < m.npg - 1; ++ip)
+      for (int it = 0; it < m.ntg - 1; ++it)
+        for (int ir = 0; ir < m.nrg - 1; ++ir, ++k) {
+          const int64_t c4 = ir + (int64_t)m.nrg * (it + (int64_t)m.ntg * ip) + n4 * id;
+          if (r8) std::memcpy(&buf[(size_t)k * 8], &r8[c4], 8);
+          else std::memcpy(&buf[(size_t)k * 4], &i4[c4], 4);
+        }
+  rec(buf.data(), body);
+  ok = std::fclose(f) == 0 && ok;
+  return ok ? HC3D_OK : HC3D_ERR_IO;
+}
+
+// The grid files of gridset (gridset.f90:1577-1586): marr (rho V), darr,
+// darrtot, tarr, darr_000, diffus and diffdir (all zero: no diffusion here).
+int write_setup_grids(const Model& m, const std::string& dir) {
+  const int64_t n4 = m.n4();
+  std::vector<double> rhov((size_t)n4 * m.ndg), tot((size_t)n4, 0.0);
+  for (size_t k = 0; k < rhov.size(); ++k) rhov[k] = std::pow(m.massarr[k], 4.0);
+  for (int s = 0; s < m.ndg; ++s)
+    for (int64_t k = 0; k < n4; ++k) tot[(size_t)k] += m.densarr[(size_t)(k + n4 * s)];
+  const std::vector<int32_t> zero((size_t)n4, 0);
+  int r;
+  if ((r = write_grid_unf(m, dir + "/marr.unf", m.ndg, rhov.data(), nullptr)) ||
+      (r = write_grid_unf(m, dir + "/darr.unf", m.ndg, m.densarr.data(), nullptr)) ||
+      (r = write_grid_unf(m, dir + "/darrtot.unf", 1, tot.data(), nullptr)) ||
+      (r = write_grid_unf(m, dir + "/tarr.unf", m.ndg, m.tdust.data(), nullptr)) ||
+      (r = write_grid_unf(m, dir + "/darr_000.unf", m.ndg, m.densarr.data(), nullptr)) ||
+      (r = write_grid_unf(m, dir + "/diffus.unf", 1, nullptr, zero.data())) ||
+      (r = write_grid_unf(m, dir + "/diffdir.unf", 1, nullptr, zero.data())))
+    return r;
+  return HC3D_OK;
+}
+
+// The grid files that disk() writes after each iteration
+// (newdisktherm.F90:605-610): diffus_NNN, diffdir_NNN (zero) and killed_NNN.
+int write_iteration_grids(const Model& m, hc3d_ctx* ctx, int iter, const std::string& dir) {
+  const int64_t n4 = m.n4();
+  std::vector<int32_t> killed((size_t)n4, 0);
+  hc3d_tallies k;
+  std::memset(&k, 0, sizeof k);
+  k.killed = killed.data();
+  int r = hc3d_get_tallies(ctx, nullptr, &k);
+  if (r) return r;
+  char suffix[16];
+  std::snprintf(suffix, sizeof suffix, "_%03d", iter);
+  const std::vector<int32_t> zero((size_t)n4, 0);
+  if ((r = write_grid_unf(m, dir + "/diffus" + suffix + ".unf", 1, nullptr, zero.data())) ||
+      (r = write_grid_unf(m, dir + "/diffdir" + suffix + ".unf", 1, nullptr, zero.data())) ||
+      (r = write_grid_unf(m, dir + "/killed" + suffix + ".unf", 1, nullptr, killed.data())))
+    return r;
+  return HC3D_OK;
+}
+
 void put_err(char* err, size_t len, const std::string& s) {
   if (err && len) std::snprintf(err, len, "%s", s.c_str());
 }
@@ -272,6 +358,13 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   if ((r = hc3d_load_grid(ctx, &gv))) return bail(r);
   hc3d_run_params p = m.params_view();
   const int ipeelorig = p.ipeel;
+  auto io_fail = [&](int code, const char* what) {
+    put_err(err, errlen, std::string("cannot write ") + what + " into " + out_dir);
+    hc3d_destroy(ctx);
+    hc3d_model_destroy(hm);
+    return code;
+  };
+  if ((r = write_setup_grids(m, out_dir))) return io_fail(r, "the gridset .unf files");
   hc3d_tts_stats st;
   std::memset(&st, 0, sizeof st);
   using clk = std::chrono::steady_clock;
@@ -290,6 +383,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
     double rel = 0;
     int conv = 0;
     if ((r = hc3d_lucy_update(ctx, m.ltot, p.np, tdust2.data(), &rel, &conv))) return bail(r);
+    if ((r = write_iteration_grids(m, ctx, iter, out_dir))) return io_fail(r, "the iteration .unf files");
     st.max_rel_change = rel;
     st.packets_total += p.np;
     converge = conv != 0;
@@ -312,6 +406,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   double rel = 0;
   int conv = 0;
   if ((r = hc3d_lucy_update(ctx, m.ltot, p.np, tdust2.data(), &rel, &conv))) return bail(r);
+  if ((r = write_iteration_grids(m, ctx, iter, out_dir))) return io_fail(r, "the iteration .unf files");
   auto t2 = clk::now();
   st.packets_total += p.np;
   st.iterations = iter;
@@ -338,4 +433,10 @@ extern "C" int hc3d_write_outputs(const hc3d_model* hm, const hc3d_run_params* p
   if (p->nfreq < 1 || p->nmu < 1 || p->nph < 1 || p->nap < 1 || (p->ipeel && (p->npeel < 1 || !p->thete)))
     return HC3D_ERR_INVALID;
   return write_outputs(hm->m, *p, *t, tdust_used, tdust, out_dir);
+}
+
+extern "C" int hc3d_write_grid_unf(const hc3d_model* hm, const char* path, int lastdim, const double* real_array,
+                                   const int32_t* int_array) {
+  if (!hm || !path) return HC3D_ERR_INVALID;
+  return write_grid_unf(hm->m, path, lastdim, real_array, int_array);
 }

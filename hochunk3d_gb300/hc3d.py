@@ -200,6 +200,7 @@ SIGNATURES = {
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
     "hc3d_write_synthetic_isrf": (C.c_int, [C.c_char_p]),
     "hc3d_write_outputs": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies), dp, dp, C.c_char_p]),
+    "hc3d_write_grid_unf": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, dp, i32p]),
     "hc3d_star_packets": (C.c_int64, [C.c_double, C.c_int64]),
     "hc3d_server_create": (C.c_int, [P(C.c_void_p), P(ServerOpts)]),
     "hc3d_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_int64)]),

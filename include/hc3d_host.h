@@ -100,9 +100,10 @@ typedef struct hc3d_tts_stats {
   int64_t counters[16];      /* final iteration, see HC3D_CNT_* */
 } hc3d_tts_stats;
 
-/* program tts: run the whole model on the GPU and write the reference's ASCII
- * output files (flux*.dat, peel_flux*.dat, e_ALL_*_img.dat, tmidplane*.dat,
- * tave*.dat) into out_dir. */
+/* program tts: run the whole model on the GPU and write the reference's
+ * output files into out_dir (an existing directory): the ASCII files
+ * (flux*.dat, peel_flux*.dat, e_ALL_*_img.dat, tmidplane*.dat, tave*.dat)
+ * and the .unf grid files of hc3d_write_grid_unf. */
 int hc3d_tts(const char *par_path, const char *par_dir, const char *out_dir, const hc3d_device_opts *opts,
              hc3d_tts_stats *stats, char *err, size_t errlen);
 
@@ -177,6 +178,17 @@ int64_t hc3d_model_footprint(const hc3d_model *m);
  * last Lucy update.  hc3d_tts calls the same writer. */
 int hc3d_write_outputs(const hc3d_model *m, const hc3d_run_params *params, const hc3d_tallies *tallies,
                        const double *tdust_used, const double *tdust, const char *out_dir);
+
+/* output_grid (output.F90:38-150): a Fortran unformatted sequential .unf
+ * file (4-byte record lengths around each record) holding the cell counts
+ * and lastdim, the cell-centre radii (AU), polar and azimuthal angles, and
+ * the array over the cells for id = 1..lastdim.  Exactly one of real_array
+ * (real*8) and int_array (integer) is given, shaped (nrg,ntg,npg,lastdim) in
+ * Fortran order.  hc3d_tts writes the reference's set: marr, darr, darrtot,
+ * tarr, darr_000, diffus, diffdir after the set-up and diffus_NNN,
+ * diffdir_NNN, killed_NNN after each iteration. */
+int hc3d_write_grid_unf(const hc3d_model *m, const char *path, int lastdim, const double *real_array,
+                        const int32_t *int_array);
 
 /* Write a synthetic 7-column dust file (dustinit's format, dust.f90:336)
  * and a 2-column stellar wavelength grid (atmosinit's format,

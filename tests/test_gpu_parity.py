@@ -242,6 +242,12 @@ def test_tts_writes_reference_outputs(fixtures_dir, built):
     assert len(list(out.glob("e_ALL_*_I_img.dat"))) == 10
     tm = (out / "tmidplane1.dat").read_text().splitlines()
     assert len(tm) == 2 + 39
+    # the .unf grid files of gridset and of each iteration (output.F90:38-150)
+    for name in ("marr", "darr", "darrtot", "tarr", "darr_000", "diffus", "diffdir"):
+        assert (out / f"{name}.unf").stat().st_size > 0, name
+    for it in (1, 2, 3):
+        for name in ("diffus", "diffdir", "killed"):
+            assert (out / f"{name}_{it:03d}.unf").exists(), (name, it)
 
 
 @pytest.mark.parametrize("prec", [hc3d.PREC_MIXED, hc3d.PREC_FP64])

@@ -84,3 +84,44 @@ def test_writer_rejects_missing_arrays(model_factory, tmp_path):
     rc = hc3d.lib().hc3d_write_outputs(m._h, C.byref(p), C.byref(T), td.ctypes.data_as(hc3d.dp),
                                        td.ctypes.data_as(hc3d.dp), str(tmp_path).encode())
     assert rc == -1
+
+
+def _read_unf(path):
+    """Fortran unformatted sequential records (4-byte length markers)."""
+    raw = path.read_bytes()
+    recs, i = [], 0
+    while i < len(raw):
+        n = int(np.frombuffer(raw[i:i + 4], dtype="<i4")[0])
+        recs.append(raw[i + 4:i + 4 + n])
+        assert int(np.frombuffer(raw[i + 4 + n:i + 8 + n], dtype="<i4")[0]) == n
+        i += 8 + n
+    return recs
+
+
+def test_grid_unf_files(model_factory, tmp_path):
+    """output_grid (output.F90:38-150): header record, cell-centre radii in AU,
+    polar and azimuthal centres, then the array over the cells."""
+    m = model_factory("tiny3d")
+    nrg, ntg, npg, ndg = m.shape4
+    path = tmp_path / "darr.unf"
+    d = np.asfortranarray(m.densarr)
+    assert hc3d.lib().hc3d_write_grid_unf(m._h, str(path).encode(), ndg, d.ctypes.data_as(hc3d.dp), None) == 0
+    recs = _read_unf(path)
+    assert len(recs) == 5
+    assert list(np.frombuffer(recs[0], dtype="<i4")) == [nrg - 1, ntg - 1, npg - 1, ndg]
+    rave = np.sqrt(m.rarr[:-1] * m.rarr[1:])
+    np.testing.assert_allclose(np.frombuffer(recs[1], dtype="<f8") * m.info.autors, rave, rtol=1e-12)
+    assert len(np.frombuffer(recs[2], dtype="<f8")) == ntg - 1
+    np.testing.assert_allclose(np.frombuffer(recs[3], dtype="<f8"), 0.5 * (m.phiarr[:-1] + m.phiarr[1:]), rtol=1e-15)
+    body = np.frombuffer(recs[4], dtype="<f8").reshape((nrg - 1, ntg - 1, npg - 1, ndg), order="F")
+    np.testing.assert_array_equal(body, m.densarr[:-1, :-1, :-1, :])
+    # an integer grid (lastdim 1)
+    k = np.asfortranarray(np.arange(nrg * ntg * npg, dtype=np.int32).reshape((nrg, ntg, npg), order="F"))
+    path = tmp_path / "killed_001.unf"
+    assert hc3d.lib().hc3d_write_grid_unf(m._h, str(path).encode(), 1, None,
+                                          k.ctypes.data_as(hc3d.i32p)) == 0
+    recs = _read_unf(path)
+    got = np.frombuffer(recs[4], dtype="<i4").reshape((nrg - 1, ntg - 1, npg - 1), order="F")
+    np.testing.assert_array_equal(got, k[:-1, :-1, :-1])
+    # exactly one array
+    assert hc3d.lib().hc3d_write_grid_unf(m._h, str(path).encode(), 1, None, None) == -1
