@@ -199,6 +199,11 @@ struct DevBufs {
 // The densities of gridset on device `device`; replaces m.densarr, massarr,
 // vcell, massdisk, massenv and ndg_active.  ms receives the device time.
 int densities_gpu(Model& m, int device, double* ms, std::string* err) {
+  if (m.disk_structured()) {
+    *err = "the device density build covers the plain flared disk; this model's gap, spiral, warp, rim or "
+           "radial-cutoff options are built on the host";
+    return HC3D_ERR_UNSUPPORTED;
+  }
   if (cudaSetDevice(device) != cudaSuccess) { *err = "no CUDA device"; return HC3D_ERR_CUDA; }
   const int nrg = m.nrg, ntg = m.ntg, npg = m.npg;
   const int ncol = (nrg - 1) * (ntg - 1);

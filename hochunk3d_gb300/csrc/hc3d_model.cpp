@@ -369,19 +369,65 @@ double zerod(double mu, double rx) {
   return std::max(0.0, std::min(1.0, x));
 }
 
-// densdisk, densdiskg.f90:1-155 for an unwarped, ungapped, unspiralled disk.
-double densdisk(const Model& m, double rad, double sint, double cost, int id) {
+// densdisk, densdiskg.f90:1-155: the flared disk with its gap, spiral arms,
+// warp, rim and gap puffs and curves and radial cutoff, at azimuth phi.
+double densdisk(const Model& m, double rad, double sint, double cost, double phi, int id) {
   const double rp = rad * sint, zp = rad * cost;
   const double rcoord = m.idiskcurve == 1 ? rad : rp;
   const double rmin = 1.0;
-  double zmr = m.z1[id] * std::pow(rcoord / rmin, m.b[id]);
-  if (rcoord > m.rmaxd[id] || m.rho0[id] == 0.0 || rcoord < m.rddust[id] || zmr < 1.e-10) return 0.0;
-  double gexp = (zp / zmr) * (zp / zmr);
-  if (gexp > 1.e-15) {
-    if (gexp < 120.0) return m.rho0[id] * std::pow(rcoord / rmin, -m.a[id]) * std::exp(-0.5 * gexp);
-    return 0.0;
+  // inside the gap the gap's density law (densdiskg.f90:34-44)
+  const bool ingap = m.igapd == 1 && rcoord < m.rgapd2 && rcoord > m.rgapd1;
+  const double adens = ingap ? m.agap[id] : m.a[id], bdens = ingap ? m.bgap[id] : m.b[id];
+  const double rhodens = ingap ? m.rhogap0[id] : m.rho0[id], zscale = ingap ? m.z1gap[id] : m.z1[id];
+  // warp of spot longitudes 0 and 180 deg (densdiskg.f90:46-68)
+  double warp = 0.0, warp2 = 0.0;
+  if (m.idiskwarp == 1) {
+    const double fall = std::exp(-std::pow((rcoord - m.rddust[id]) / m.warplength, 2.0));
+    warp = (phi < kPi ? 1.0 : -1.0) * m.warpheight * std::pow(std::cos(phi / 2.0), m.wexp) * fall;
+    if (m.nspot == 2) warp2 = m.warpheight * std::pow(std::cos(phi / 2.0 - kPi / 2.0), m.wexp) * fall;
   }
-  return m.rho0[id] * std::pow(rcoord / rmin, -m.a[id]);
+  double rimcurve = 0.0, rimpuff = 0.0, gappuff = 0.0, gapcurve = 0.0;
+  if (m.irimcurve == 1)
+    rimcurve = m.rimcurveheight * std::exp(-std::pow((rcoord - m.rddust[id]) / m.rimcurvelength, m.rimcurveexp));
+  if (m.irimpuff == 1) rimpuff = m.rimheight * std::exp(-std::pow((rcoord - m.rddust[id]) / m.rimlength, 2.0));
+  if (rcoord < m.rddust[id]) rimpuff = 0.0;
+  if (m.igappuff == 1 && m.igapd == 1) gappuff = m.gapheight * std::exp(-std::pow((rcoord - m.rgapd2) / m.gaplength, 2.0));
+  if (rcoord < m.rgapd2) gappuff = 0.0;
+  if (m.igapcurve == 1 && m.igapd == 1)
+    gapcurve = m.gapcurveheight * std::exp(-std::pow((rcoord - m.rgapd2) / m.gapcurvelength, m.gapcurveexp));
+  if (rcoord < m.rgapd2) gapcurve = 0.0;
+  // spiral arms (densdiskg.f90:101-112): SN-th power of a logarithmic spiral,
+  // normalised by the product of is/(is-1) over even is
+  double spiral = 1.0;
+  if (m.ispiral == 1) {
+    double sfact = 1.0;
+    for (int is = 2; is <= m.sn; is += 2) sfact = sfact * ((double)is / ((double)is - 1.0));
+    spiral = 1.0 - m.sw + sfact * m.sw * std::pow(std::sin(std::log(rcoord) / std::tan(m.pitch) - phi + 0.7854), m.sn);
+    if (rcoord < m.rspiral1 || rcoord > m.rspiral2) spiral = 1.0;
+  }
+  double zmr = zscale * std::pow(rcoord / rmin, bdens);
+  double densfact1 = 1.0;
+  if (phi < kPi / 2.0 || phi > 3.0 * kPi / 2.0) {
+    if (zp > 0.0) zmr = zmr * (1.0 + warp);  // the warp lifts the +z side of spot 1 only
+    densfact1 = 1.0 / (1.0 + warp);
+  } else {
+    if (zp < 0.0) zmr = zmr * (1.0 + warp2);
+    densfact1 = 1.0 / (1.0 + warp2);
+  }
+  const double puff = 1.0 + rimpuff + gappuff - rimcurve - gapcurve;
+  const double densfact = 1.0 / puff * densfact1;
+  zmr = zmr * puff;
+  if (rcoord > m.rmaxd[id] || rhodens == 0.0 || rcoord < m.rddust[id] || zmr < 1.e-10) return 0.0;
+  const double gexp = (zp / zmr) * (zp / zmr);
+  double dens;
+  if (gexp > 1.e-15) {
+    if (gexp < 120.0) dens = densfact * spiral * rhodens * std::pow(rcoord / rmin, -adens) * std::exp(-0.5 * gexp);
+    else dens = 0.0;
+  } else {
+    dens = densfact * spiral * rhodens * std::pow(rcoord / rmin, -adens);
+  }
+  if (m.iradexp == 1) dens = dens * std::exp(-rcoord / m.radexp);
+  return dens;
 }
 
 // densenv, densenv.f90:1-128: Ulrich envelope (or power law) with a
@@ -671,15 +717,67 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   double fmassd1;
   REQ(P.real("FMASSD1", &fmassd1, err));
   if (P.has("CDISKCURV")) { REQ(P.str("CDISKCURV", &sv, err)); m->idiskcurve = sv == "SPH" ? 1 : 0; }
-  const char* off_keys[] = {"CHSEQ", "CGAPD", "CSPIRAL", "CDISKWARP", "CRIMPUFF", "CGAPPUFF",
-                            "CRIMCURVE", "CGAPCURVE", "CMISALIGN", "CRADEXP", "CDISKACC", "DIFFUSION",
-                            "DENSINPUT", "CGAPE"};
+  const char* off_keys[] = {"CHSEQ", "CMISALIGN", "CDISKACC", "DIFFUSION", "DENSINPUT", "CGAPE"};
   for (const char* k : off_keys) {
     if (P.has(k)) {
       REQ(P.integer(k, &iv, err));
       if (iv != 0) { *err = std::string(k) + "=YES is not supported by this build"; return false; }
     }
   }
+  // disk structure (reapar.f90:155-271)
+  auto flag = [&](const char* k, int* out) {
+    *out = 0;
+    if (!P.has(k)) return true;
+    int64_t v;
+    if (!P.integer(k, &v, err)) return false;
+    *out = (int)v;
+    return true;
+  };
+  REQ(flag("CGAPD", &m->igapd));
+  REQ(flag("CSPIRAL", &m->ispiral));
+  REQ(flag("CDISKWARP", &m->idiskwarp));
+  REQ(flag("CRIMPUFF", &m->irimpuff));
+  REQ(flag("CGAPPUFF", &m->igappuff));
+  REQ(flag("CRIMCURVE", &m->irimcurve));
+  REQ(flag("CGAPCURVE", &m->igapcurve));
+  REQ(flag("CRADEXP", &m->iradexp));
+  if (m->igapd) {
+    REQ(P.real("RGAPD1", &m->rgapd1, err));
+    REQ(P.real("RGAPD2", &m->rgapd2, err));
+    for (int d = 1; d <= 2; ++d) {
+      char key[64];
+      snprintf(key, sizeof key, "ZSCALE_GAP(%d)", d); REQ(P.real(key, &m->z1gap[d - 1], err));
+      snprintf(key, sizeof key, "A_GAP(%d)", d); REQ(P.real(key, &m->agap[d - 1], err));
+      snprintf(key, sizeof key, "B_GAP(%d)", d); REQ(P.real(key, &m->bgap[d - 1], err));
+      snprintf(key, sizeof key, "RHOSCALE_GAP(%d)", d); REQ(P.real(key, &m->rhoscale_gap[d - 1], err));
+    }
+  }
+  if (m->ispiral) {
+    REQ(P.real("PITCH", &m->pitch, err));
+    REQ(P.integer("SN", &iv, err)); m->sn = (int)iv;
+    REQ(P.real("SW", &m->sw, err));
+    REQ(P.real("RSPIRAL1", &m->rspiral1, err));
+    REQ(P.real("RSPIRAL2", &m->rspiral2, err));
+  }
+  if (m->idiskwarp) {
+    REQ(P.real("WARPHEIGHT", &m->warpheight, err));
+    REQ(P.real("WEXP", &m->wexp, err));
+    REQ(P.real("WARPLENGTH", &m->warplength, err));
+    if (P.has("NSPOT")) { REQ(P.integer("NSPOT", &iv, err)); m->nspot = (int)iv; }
+  }
+  if (m->irimpuff) { REQ(P.real("RIMHEIGHT", &m->rimheight, err)); REQ(P.real("RIMLENGTH", &m->rimlength, err)); }
+  if (m->igappuff) { REQ(P.real("GAPHEIGHT", &m->gapheight, err)); REQ(P.real("GAPLENGTH", &m->gaplength, err)); }
+  if (m->irimcurve) {
+    REQ(P.real("RIMCURVEHEIGHT", &m->rimcurveheight, err));
+    REQ(P.real("RIMCURVELENGTH", &m->rimcurvelength, err));
+    REQ(P.real("RIMCURVEEXP", &m->rimcurveexp, err));
+  }
+  if (m->igapcurve) {
+    REQ(P.real("GAPCURVEHEIGHT", &m->gapcurveheight, err));
+    REQ(P.real("GAPCURVELENGTH", &m->gapcurvelength, err));
+    REQ(P.real("GAPCURVEEXP", &m->gapcurveexp, err));
+  }
+  if (m->iradexp) REQ(P.real("RADEXP", &m->radexp, err));
   double rmind_in[HC3D_NDG] = {0}, fsg[4] = {0};
   for (int d = 1; d <= 2; ++d) {
     char key[64];
@@ -776,12 +874,33 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   } else {
     m->rmine = rmine_in;
   }
+  m->rspiral1 *= m->autors;
+  m->rspiral2 *= m->autors;
   if (czmin == "RSUB") {
     const double muc = 2.3, rcgs = m->rminsub * m->rstar * kRsun, mcgs = m->massc * kMsun;
     const double honr = std::sqrt(kBoltz * m->tsub_k / kGn / mcgs * rcgs / muc / kMH);
-    for (int d = 0; d < 2; ++d) m->z1[d] = m->z1[d] * honr * m->rminsub / std::pow(m->rminsub, m->b[d]);
+    for (int d = 0; d < 2; ++d) {
+      m->z1[d] = m->z1[d] * honr * m->rminsub / std::pow(m->rminsub, m->b[d]);
+      m->z1gap[d] = m->z1gap[d] * honr * m->rminsub / std::pow(m->rminsub, m->bgap[d]);
+    }
   } else if (czmin == "R100") {
-    for (int d = 0; d < 2; ++d) m->z1[d] = m->z1[d] * m->autors / std::pow(100.0 * m->autors, m->b[d]);
+    for (int d = 0; d < 2; ++d) {
+      m->z1[d] = m->z1[d] * m->autors / std::pow(100.0 * m->autors, m->b[d]);
+      m->z1gap[d] = m->z1gap[d] * m->autors / std::pow(100.0 * m->autors, m->bgap[d]);
+    }
+  }
+  m->rgapd1 *= m->autors;
+  if (m->rgapd1 < 1.0) m->rgapd1 = 1.0;
+  m->rgapd2 *= m->autors;
+  m->warplength *= m->autors;
+  m->gaplength *= m->autors;
+  m->rimlength *= m->autors;
+  m->rimcurvelength *= m->autors;
+  m->gapcurvelength *= m->autors;
+  m->radexp *= m->autors;
+  m->pitch = m->pitch * kPi / 180.0;
+  if (m->massd == 0.0) {  // reapar.f90:315-326
+    m->idiskwarp = 0; m->igapd = 0; m->ispiral = 0; m->igappuff = 0; m->irimpuff = 0;
   }
   m->rmax *= m->autors;
   for (int d = 0; d < 2; ++d) m->rmaxd[d] *= m->autors;
@@ -951,6 +1070,30 @@ static bool gridset(Model* m, std::string* err) {
   m->massarr.assign(n4 * m->ndg, 0.0);
   m->vcell.assign(n4, 0.0);
   auto cell = [&](int ir, int it, int ip) { return (int64_t)ir + (int64_t)nrg * (it + (int64_t)ntg * ip); };
+  const bool phidep = m->disk_depends_on_phi();
+  auto phic = [&](int ip) { return 0.5 * (m->phiarr[ip] + m->phiarr[ip + 1]); };
+  // the gap's density scale: rho0 times RHOSCALE_GAP times the ratio of the
+  // surface densities just outside and just inside the gap's outer wall,
+  // integrated over theta and phi with rhogap0 = rho0 (gridset.f90:906-942)
+  for (int id = 0; id < 2; ++id) m->rhogap0[id] = m->rho0[id];
+  if (m->igapd) {
+    double rhogap[2];
+    for (int id = 0; id < 2; ++id) {
+      double sig[2] = {0.0, 0.0};
+      for (int i = 0; i < 2; ++i) {
+        const double rad = m->rgapd2 * (i == 0 ? 0.9 : 1.1);
+        for (int it = 0; it < ntg - 1; ++it) {
+          const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
+          const double dcost = m->costarr[it] - m->costarr[it + 1];
+          for (int ip = 0; ip < npg - 1; ++ip)
+            sig[i] += std::fabs(densdisk(*m, rad, sint, cost, phic(ip), id) * rad * dcost * rmincgs) / (double)(npg - 1);
+        }
+      }
+      // a gap wall with no disk inside it (sig[0] = 0) keeps the disk's scale
+      rhogap[id] = sig[0] > 0.0 ? m->rho0[id] * m->rhoscale_gap[id] * sig[1] / sig[0] : m->rho0[id] * m->rhoscale_gap[id];
+    }
+    for (int id = 0; id < 2; ++id) m->rhogap0[id] = rhogap[id];
+  }
   // disk mass normalisation: diskscl = massd*fmass / mass on the grid
   double diskscl[2] = {1.0, 1.0};
   if (m->massd > 0.0) {
@@ -963,9 +1106,10 @@ static bool gridset(Model* m, std::string* err) {
         for (int it = 0; it < ntg - 1; ++it) {
           const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
           const double dcost = std::cos(m->thetarr[it + 1]) - std::cos(m->thetarr[it]);
-          const double dd = densdisk(*m, rad, sint, cost, id);
-          if (dd == 0.0) continue;
+          const double dd0 = phidep ? 0.0 : densdisk(*m, rad, sint, cost, 0.0, id);
+          if (!phidep && dd0 == 0.0) continue;
           for (int ip = 0; ip < npg - 1; ++ip) {
+            const double dd = phidep ? densdisk(*m, rad, sint, cost, phic(ip), id) : dd0;
             const double dpp = m->phiarr[ip + 1] - m->phiarr[ip];
             const double vol = -dr3 * dcost * dpp / 3.0 * std::pow(rmincgs, 3.0);
             tmpmass[id] += dd * vol;
@@ -986,9 +1130,11 @@ static bool gridset(Model* m, std::string* err) {
       const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
       const double dcost = std::cos(m->thetarr[it + 1]) - std::cos(m->thetarr[it]);
       double dens_r[4];
-      for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, id) * diskscl[id];
+      for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, 0.0, id) * diskscl[id];
       for (int id = 2; id < 4; ++id) dens_r[id] = densenv(*m, rad, thet, cost, sint, id) * m->fmass[id];
       for (int ip = 0; ip < npg - 1; ++ip) {
+        if (phidep)
+          for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, phic(ip), id) * diskscl[id];
         const double dpp = m->phiarr[ip + 1] - m->phiarr[ip];
         const double vol = -dr3 * dcost * dpp / 3.0 * r3;
         const int64_t c = cell(ir, it, ip);

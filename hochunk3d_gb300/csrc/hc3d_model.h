@@ -74,6 +74,22 @@ struct Model {
   double lstar = 0, l_isrf = 0, isrf_frac = 0;
   std::string isrf_file;
   std::vector<double> isrf_cdfv, isrf_logcdf, isrf_logfreq;
+  // disk structure of densdiskg (densdiskg.f90:25-155): gap, spiral arms,
+  // warp, puffed and curved inner rim and outer gap wall, radial cutoff
+  int igapd = 0, ispiral = 0, idiskwarp = 0, irimpuff = 0, igappuff = 0, irimcurve = 0, igapcurve = 0, iradexp = 0;
+  double rgapd1 = 0, rgapd2 = 0;
+  double z1gap[2] = {0, 0}, agap[2] = {0, 0}, bgap[2] = {0, 0}, rhoscale_gap[2] = {0, 0}, rhogap0[2] = {0, 0};
+  double pitch = 0, sw = 0, rspiral1 = 0, rspiral2 = 0;
+  int sn = 0, nspot = 1;
+  double warpheight = 0, wexp = 0, warplength = 1;
+  double rimheight = 0, rimlength = 1, gapheight = 0, gaplength = 1;
+  double rimcurveheight = 0, rimcurvelength = 1, rimcurveexp = 1;
+  double gapcurveheight = 0, gapcurvelength = 1, gapcurveexp = 1;
+  double radexp = 1;
+  bool disk_depends_on_phi() const { return idiskwarp || ispiral; }
+  bool disk_structured() const {
+    return igapd || ispiral || idiskwarp || irimpuff || igappuff || irimcurve || igapcurve || iradexp;
+  }
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;
   int image = 1;
@@ -115,7 +131,7 @@ void setemiss_species(const Model& m, int id, double* kapB /*(nT,nnu)*/, double*
 
 // densdisk (densdiskg.f90:1-155) and densenv (densenv.f90:1-128) for the
 // options the benchmark models use
-double densdisk(const Model& m, double rad, double sint, double cost, int id);
+double densdisk(const Model& m, double rad, double sint, double cost, double phi, int id);
 double densenv(const Model& m, double rad, double thetin, double costin, double sina, int id);
 // zerod: the Ulrich streamline root mu0 (module not shipped; restated)
 double zerod(double mu, double rx);
