@@ -431,8 +431,8 @@ double densdisk(const Model& m, double rad, double sint, double cost, double phi
 }
 
 // densenv, densenv.f90:1-128: Ulrich envelope (or power law) with a
-// polynomial bipolar cavity; species id is the envelope (slot 3) or cavity
-// (slot 4).
+// polynomial bipolar cavity and an optional gap; species id is the envelope
+// (slot 3) or cavity (slot 4).
 double densenv(const Model& m, double rad, double thetin, double costin, double sina, int id) {
   const bool is_env = (id == 2 || id == 6), is_cav = (id == 3 || id == 7);
   int inhole = 0;
@@ -457,6 +457,9 @@ double densenv(const Model& m, double rad, double thetin, double costin, double 
   } else {
     dens = 0.0;
   }
+  // constant density in the envelope gap, before the ambient floor and the cavity
+  const bool ingape = m.igape == 1 && rad < m.rgape2 && rad > m.rgape1;
+  if (ingape && m.igapedens == 0) dens = m.rhogape;
   if (rad > m.rmine && dens < m.rhoamb) dens = m.rhoamb;
   if (m.ihole == 1 && m.ipoly == 1) {
     double zlo = m.c2e * std::pow(rp, m.ex2) + m.z02;
@@ -469,6 +472,7 @@ double densenv(const Model& m, double rad, double thetin, double costin, double 
       dens = m.rhoconst1 * std::pow(rad, -m.exf);
     }
   }
+  if (ingape && m.igapedens == 1) dens = dens * m.fracte;  // scaled density in the gap
   if (rad >= m.rmax) dens = 0.0;
   if (rad <= m.rmine) dens = 0.0;
   if (is_cav && inhole == 0) dens = 0.0;
@@ -717,7 +721,7 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   double fmassd1;
   REQ(P.real("FMASSD1", &fmassd1, err));
   if (P.has("CDISKCURV")) { REQ(P.str("CDISKCURV", &sv, err)); m->idiskcurve = sv == "SPH" ? 1 : 0; }
-  const char* off_keys[] = {"CHSEQ", "CMISALIGN", "CDISKACC", "DIFFUSION", "DENSINPUT", "CGAPE"};
+  const char* off_keys[] = {"CHSEQ", "CMISALIGN", "CDISKACC", "DIFFUSION", "DENSINPUT"};
   for (const char* k : off_keys) {
     if (P.has(k)) {
       REQ(P.integer(k, &iv, err));
@@ -778,6 +782,18 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
     REQ(P.real("GAPCURVEEXP", &m->gapcurveexp, err));
   }
   if (m->iradexp) REQ(P.real("RADEXP", &m->radexp, err));
+  // envelope gap (reapar.f90:369-391)
+  REQ(flag("CGAPE", &m->igape));
+  if (m->igape) {
+    REQ(P.real("RGAPE1", &m->rgape1, err));
+    REQ(P.real("RGAPE2", &m->rgape2, err));
+    REQ(P.str("CGAPEDENS", &sv, err));
+    if (sv == "SCALE") m->igapedens = 1;
+    else if (sv == "CONST") m->igapedens = 0;
+    else { *err = "CGAPEDENS should be set to SCALE or CONST"; return false; }
+    REQ(P.real("FRACTE", &m->fracte, err));
+    REQ(P.real("RHOGAPE", &m->rhogape, err));
+  }
   double rmind_in[HC3D_NDG] = {0}, fsg[4] = {0};
   for (int d = 1; d <= 2; ++d) {
     char key[64];
@@ -892,6 +908,8 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   m->rgapd1 *= m->autors;
   if (m->rgapd1 < 1.0) m->rgapd1 = 1.0;
   m->rgapd2 *= m->autors;
+  m->rgape1 *= m->autors;
+  m->rgape2 *= m->autors;
   m->warplength *= m->autors;
   m->gaplength *= m->autors;
   m->rimlength *= m->autors;

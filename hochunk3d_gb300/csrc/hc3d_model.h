@@ -86,9 +86,14 @@ struct Model {
   double rimcurveheight = 0, rimcurvelength = 1, rimcurveexp = 1;
   double gapcurveheight = 0, gapcurvelength = 1, gapcurveexp = 1;
   double radexp = 1;
+  // envelope gap (CGAPE, densenv.f90:52-58,114-119): constant density rhogape,
+  // or the envelope density scaled by fracte, between rgape1 and rgape2
+  int igape = 0, igapedens = 0;
+  double rgape1 = 0, rgape2 = 0, fracte = 1, rhogape = 0;
   bool disk_depends_on_phi() const { return idiskwarp || ispiral; }
+  // density options the host build covers and the device build does not
   bool disk_structured() const {
-    return igapd || ispiral || idiskwarp || irimpuff || igappuff || irimcurve || igapcurve || iradexp;
+    return igapd || ispiral || idiskwarp || irimpuff || igappuff || irimcurve || igapcurve || iradexp || igape;
   }
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;

@@ -76,8 +76,8 @@ int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
  * CUDA device `device`, replacing the host-built densarr, massarr, vcell and
  * the grid masses of the model.  *ms receives the device time of the
  * kernels.  Models with disk structure (CGAPD, CSPIRAL, CDISKWARP, CRIMPUFF,
- * CGAPPUFF, CRIMCURVE, CGAPCURVE, CRADEXP), which the host build covers,
- * return HC3D_ERR_UNSUPPORTED. */
+ * CGAPPUFF, CRIMCURVE, CGAPCURVE, CRADEXP) or an envelope gap (CGAPE), which
+ * the host build covers, return HC3D_ERR_UNSUPPORTED. */
 int hc3d_model_densities_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
 
 /* setemiss (dust.f90:394-474: the cumulative emissivity tables kapBint and

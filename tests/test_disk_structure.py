@@ -107,3 +107,25 @@ def test_device_density_build_leaves_structured_disks_to_the_host(tmp_path, buil
     with pytest.raises(hc3d.Hc3dError) as e:
         m.densities_gpu(0)
     assert e.value.code == -7
+
+
+@pytest.mark.parametrize("mode", ["CONST", "SCALE"])
+def test_envelope_gap(tmp_path, built, mode):
+    """CGAPE (densenv.f90:52-58,114-119): the envelope between RGAPE1 and
+    RGAPE2 takes RHOGAPE (CONST) or FRACTE times its density (SCALE)."""
+    over = {"RATE": 5e-6, "MASSD": 0.0001, "CGAPE": "YES", "RGAPE1": 20.0, "RGAPE2": 60.0, "CGAPEDENS": mode,
+            "FRACTE": 0.01, "RHOGAPE": 3e-21}
+    g = _model(tmp_path, "egap" + mode, **over)
+    p = _model(tmp_path, "enogap" + mode, RATE=5e-6, MASSD=0.0001)
+    au = g.info.autors
+    rave = np.sqrt(g.rarr[:-1] * g.rarr[1:])
+    it = 5  # a polar-angle cell off the disk, outside the cavity
+    e_g, e_p = g.densarr[:-1, it, 0, 2], p.densarr[:-1, it, 0, 2]
+    gap = (rave > 21 * au) & (rave < 59 * au) & (e_p > 0)
+    away = ((rave < 19 * au) | (rave > 61 * au)) & (e_p > 0)
+    assert gap.sum() >= 2 and away.sum() >= 2
+    if mode == "CONST":
+        np.testing.assert_allclose(e_g[gap], 3e-21, rtol=1e-12)
+    else:
+        np.testing.assert_allclose(e_g[gap], 0.01 * e_p[gap], rtol=1e-12)
+    np.testing.assert_array_equal(e_g[away], e_p[away])
