@@ -670,7 +670,6 @@ static bool isrf_cdf(Model* m, std::string* err) {
 
 static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std::string* err) {
   int64_t iv;
-  double dv;
   std::string sv;
   REQ(P.integer("NP", &m->np, err));
   REQ(P.integer("NPMIN", &m->npmin, err));
