@@ -320,6 +320,85 @@ def serving_latency(tmp: Path, device: int, n: int = 60, rate: float = 20.0, slo
             "results_equal_to_offline_batch": bool(same)}
 
 
+def fp64_comparison(model, td_init, device: int, n_sed: int, n_lucy: int) -> dict:
+    """The mixed form against the all-FP64 form on the same inputs.
+
+    Lucy: the FP64 form repeats the two set-up iterations (same packets, same
+    streams) from the same starting temperatures; the temperatures are
+    compared in the cells whose last iteration absorbed >= 100 packets.
+    SED: both forms run one peeled batch of n_sed packets on the mixed form's
+    set-up temperatures (same streams), timed alike (packet loop only); the
+    SEDs, peeled SEDs and images are compared per bin (chi^2/dof per Stokes
+    component, the largest relative Stokes-I error over bins with >= 100
+    packets, the relative error of the summed flux)."""
+    import torch
+
+    from hochunk3d_gb300 import compare as K
+    from hochunk3d_gb300 import hc3d
+
+    out = {}
+    td_mixed = model.tdust.copy(order="F")
+    # (1) the Lucy set-up in FP64
+    model.set_tdust(td_init)
+    c64 = hc3d.Context(hc3d.PREC_FP64, device=device).load(model)
+    t0 = time.perf_counter()
+    for it in (1, 2):
+        p = model.run_params(np=n_lucy, iter=it, ipeel=0)
+        c64.zero()
+        c64.run(p)
+        td64, _, _ = c64.lucy_update(model.info.ltot, n_lucy)
+    lucy_s = time.perf_counter() - t0
+    nabs = c64.tallies(p)["nabs"]
+    c64.close()
+    sel = (nabs >= 100) & (td64 > 1.0 / 11605.0) & (model.densarr > 0)
+    rel = np.abs(td_mixed[sel] - td64[sel]) / td64[sel]
+    out["lucy"] = {"iterations": 2, "packets_per_iteration": n_lucy, "cells_compared": int(sel.sum()),
+                   "tdust_max_rel": float(rel.max()) if rel.size else None,
+                   "tdust_p99_rel": float(np.percentile(rel, 99)) if rel.size else None,
+                   "tdust_median_rel": float(np.median(rel)) if rel.size else None,
+                   "fp64_seconds": lucy_s}
+    # (2) one peeled batch in both forms
+    model.set_tdust(td_mixed)
+    c64 = hc3d.Context(hc3d.PREC_FP64, device=device).load(model)
+
+    def timed_run(c, it, np_):
+        c.zero()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.run(model.run_params(np=np_, iter=it, ipeel=1))
+        dt = time.perf_counter() - t0
+        return dt, c.tallies(model.run_params(np=np_, iter=it, ipeel=1), grid=False)
+
+    timed_run(c64, 500, 1000)  # loads the FP64 kernels
+    t64, a = timed_run(c64, 501, n_sed)
+    c64.close()
+    # a fresh mixed context on the same temperatures (the timed steps have
+    # moved the bench context's temperatures on)
+    c32 = hc3d.Context(hc3d.PREC_MIXED, device=device).load(model)
+    timed_run(c32, 500, 1000)
+    t32, b = timed_run(c32, 501, n_sed)
+    c32.close()
+    rep = K.sed_report(b, a, rel_min_count=100)
+    flux = {}
+    for tag, key in (("sed", "si"), ("peeled_sed", "ti"), ("image", "image_i")):
+        sa = float(np.sum(a[key][..., 0] if key != "image_i" else a[key]))
+        sb = float(np.sum(b[key][..., 0] if key != "image_i" else b[key]))
+        flux[tag] = abs(sb - sa) / abs(sa) if sa else None
+    worst = max(v for k, v in rep.items() if k.endswith("max_rel_err_i") and v == v)
+    out.update({"value": n_sed / t64, "unit": "packets/s", "packets_per_step": n_sed,
+                "mixed_same_batch": n_sed / t32, "speedup_mixed_over_fp64": t64 / t32,
+                "sed_chi2": {c: rep[f"sed_chi2_{c}"] for c in "iquv"},
+                "peeled_sed_chi2": {c: rep[f"peeled_sed_chi2_{c}"] for c in "iquv"},
+                "chi2_dof": {t: {c: rep[f"{t}_dof_{c}"] for c in "iquv"} for t in ("sed", "peeled_sed")},
+                "max_rel_err": {"sed": rep["sed_max_rel_err_i"], "peeled_sed": rep["peeled_sed_max_rel_err_i"],
+                                "bins": "Stokes I, bins with >= 100 packets on both sides"},
+                "flux_rel_err": flux,
+                "sed_err_le_1pct": bool(worst <= 0.01),
+                "tdust_max_rel": out["lucy"]["tdust_max_rel"],
+                "same_streams": True})
+    return out
+
+
 def reference_arm(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -366,6 +445,8 @@ def main():
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
     ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison run")
+    ap.add_argument("--fp64-packets", type=int, default=1_000_000,
+                    help="packets of the peeled batch that both forms run for the speed-up and the error")
     ap.add_argument("--no-serving", action="store_true", help="skip the model-grid and serving measurements")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default peel-off queue depth")
     ap.add_argument("--profile-step", action="store_true",
@@ -398,6 +479,7 @@ def main():
     with tempfile.TemporaryDirectory() as td:
         model = build_model(Path(td), args.workload)
         ctx = hc3d.Context(hc3d.PREC_MIXED, device=local).load(model)
+        td_init = model.tdust.copy(order="F")
         warm_up_temperatures(model, ctx, args.lucy_packets)
         # the peel-off queue depth, chosen by timing a sample batch (untimed set-up)
         tune = ctx.autotune(model.run_params(np=200000, iter=900, ipeel=1)) if not args.no_autotune else None
@@ -478,26 +560,11 @@ def main():
             h2d = 8 * 4 * model.npeel + 8 * len(model.aperture2)
         e2e = n * world / (sum(e2e_times) / len(e2e_times))
 
-        # the all-FP64 form on the same model, temperatures and packets, for the
-        # speed-up: both forms time the same batch (packet loop only)
+        # the all-FP64 form on the same model, temperatures and packets: the
+        # speed-up on one batch and the mixed form's error against it
         fp64 = None
         if not args.no_fp64:
-            n64 = min(n, 100000)
-
-            def timed_run(c, it, np_):
-                c.zero()
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                c.run(model.run_params(np=np_, iter=it, ipeel=1))
-                return time.perf_counter() - t0
-
-            ctx64 = hc3d.Context(hc3d.PREC_FP64, device=local).load(model)
-            timed_run(ctx64, 500, 1000)  # loads the FP64 kernels
-            t64 = timed_run(ctx64, 501, n64)
-            ctx64.close()
-            t32 = timed_run(ctx, 501, n64)
-            fp64 = {"value": n64 / t64, "unit": "packets/s", "packets_per_step": n64,
-                    "mixed_same_batch": n64 / t32, "speedup_mixed_over_fp64": t64 / t32}
+            fp64 = fp64_comparison(model, td_init, local, args.fp64_packets, args.lucy_packets)
 
         launches = sum(k[0] for k in kern_ms)
         tms = sum(k[1] for k in kern_ms) / len(kern_ms)

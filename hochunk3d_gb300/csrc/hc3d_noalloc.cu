@@ -35,7 +35,9 @@ constexpr long long kMaxBlocks = HC3D_NOALLOC_MAX_ELEMENTS / (kThreads * kPerThr
 // [kMaxBlocks + 1]: the maximum over all blocks.
 static __device__ __align__(256) unsigned long long g_lucy_scratch[kMaxBlocks + 2];
 
-// Device address of g_lucy_scratch per device ordinal, found once per device.
+// Device address of g_lucy_scratch per device ordinal, found once per device
+// and kept for the life of the process (a device reset would load the module
+// again elsewhere; the header tells callers not to use the call after one).
 std::mutex g_mu;
 void* g_addr[64] = {};
 

@@ -71,6 +71,7 @@ struct hc3d_server {
   std::deque<Request> queue;
   std::map<int64_t, Result> done;
   std::set<int64_t> claimed;  // tickets whose result was handed out
+  std::set<int64_t> cancelled;  // running requests asked to stop at their next iteration
   std::mutex mu;
   std::condition_variable cv_queue, cv_mem, cv_done;
   std::vector<std::thread> workers;
@@ -159,8 +160,17 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
     hc3d_model_destroy(hm);
     return r;
   }
+  // a cancelled request stops between iterations, with no kernel in flight
+  auto stop_asked = [&] {
+    std::lock_guard<std::mutex> lk(s->mu);
+    return s->cancelled.count(q.ticket) != 0;
+  };
   bool converge = q.n_lucy == 0;
   while (!converge) {
+    if (stop_asked()) {
+      r = HC3D_ERR_CANCELLED;
+      break;
+    }
     ++iter;
     p.np = m.np_lucy;
     p.n_star = hc3d_star_packets(m.isrf_frac, p.np);
@@ -181,6 +191,7 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
       if (iter >= m.nimax) converge = true;
     }
   }
+  if (!r && stop_asked()) r = HC3D_ERR_CANCELLED;
   if (!r) {
     ++iter;
     p.np = m.np;
@@ -203,7 +214,12 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
     }
   }
   res->iterations = iter;
-  if (r) ctx_error(c, r, res);
+  if (r == HC3D_ERR_CANCELLED) {
+    res->status = r;
+    res->err = "the request was cancelled";
+  } else if (r) {
+    ctx_error(c, r, res);
+  }
   release();
   hc3d_model_destroy(hm);
   return r;
@@ -225,6 +241,7 @@ void worker(hc3d_server* s, int slot) {
     run_request(s, c, q, &res);
     res.t_done = since(s);
     std::lock_guard<std::mutex> lk(s->mu);
+    s->cancelled.erase(q.ticket);
     s->completed++;
     s->done[q.ticket] = std::move(res);
     s->cv_done.notify_all();
@@ -326,6 +343,28 @@ extern "C" int hc3d_server_wait(hc3d_server* s, int64_t ticket, hc3d_result* out
     }
   }
   return out->status;
+}
+
+extern "C" int hc3d_server_cancel(hc3d_server* s, int64_t ticket) {
+  if (!s || ticket < 1) return HC3D_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (ticket >= s->next_ticket || s->claimed.count(ticket)) return HC3D_ERR_INVALID;
+  if (s->done.count(ticket)) return HC3D_ERR_STATE;  // finished: its result stands
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+    if (it->ticket != ticket) continue;
+    Result res;
+    res.status = HC3D_ERR_CANCELLED;
+    res.err = "the request was cancelled before it was admitted";
+    res.t_submit = it->t_submit;
+    res.t_done = since(s);
+    s->queue.erase(it);
+    s->completed++;
+    s->done[ticket] = std::move(res);
+    s->cv_done.notify_all();
+    return HC3D_OK;
+  }
+  s->cancelled.insert(ticket);  // running: it stops before its next iteration
+  return HC3D_OK;
 }
 
 extern "C" void hc3d_result_free(hc3d_result* r) {

@@ -102,13 +102,23 @@ __device__ __forceinline__ uint32_t next_u32(Rng& r) {
   return u;
 }
 
+// The trace harness draws from an injected list.  Past its end the draws
+// continue as the equidistributed sequence frac(0.5 + k (sqrt(5) - 1) / 2),
+// k = 0, 1, ..., so that a rejection loop (stokes) still ends when a caller
+// passes too few uniforms; the CPU restatement continues the same way.
+__device__ __forceinline__ double inj_next(Rng& r) {
+  if (r.pos < r.ninj) return r.inj[r.pos++];
+  const double v = 0.5 + (double)(r.pos++ - r.ninj) * 0.6180339887498949;
+  return v - floor(v);
+}
+
 template <class R> __device__ __forceinline__ R ran(Rng& r);
 template <> __device__ __forceinline__ double ran<double>(Rng& r) {
-  if (r.inj) return r.pos < r.ninj ? r.inj[r.pos++] : 0.5;
+  if (r.inj) return inj_next(r);
   return ((double)next_u32(r) + 0.5) * (1.0 / 4294967296.0);
 }
 template <> __device__ __forceinline__ float ran<float>(Rng& r) {
-  if (r.inj) return r.pos < r.ninj ? (float)r.inj[r.pos++] : 0.5f;
+  if (r.inj) return (float)inj_next(r);
   return ((float)(next_u32(r) >> 8) + 0.5f) * (1.0f / 16777216.0f);
 }
 

@@ -33,6 +33,7 @@ PREC_FP64 = 1
 ERRORS = {
     -1: "HC3D_ERR_INVALID", -2: "HC3D_ERR_CUDA", -3: "HC3D_ERR_NOMEM", -4: "HC3D_ERR_STATE",
     -5: "HC3D_ERR_DEVICE", -6: "HC3D_ERR_IO", -7: "HC3D_ERR_UNSUPPORTED", -8: "HC3D_ERR_TIMEOUT",
+    -9: "HC3D_ERR_CANCELLED",
 }
 
 CNT = {
@@ -206,6 +207,7 @@ SIGNATURES = {
     "hc3d_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_int64)]),
     "hc3d_server_wait": (C.c_int, [C.c_void_p, C.c_int64, P(Result)]),
     "hc3d_result_free": (None, [P(Result)]),
+    "hc3d_server_cancel": (C.c_int, [C.c_void_p, C.c_int64]),
     "hc3d_server_get_stats": (C.c_int, [C.c_void_p, P(ServerStats)]),
     "hc3d_server_destroy": (None, [C.c_void_p]),
     "hc3d_model_footprint": (C.c_int64, [C.c_void_p]),
@@ -664,6 +666,12 @@ class Server:
             out["numt"] = np.zeros(psed, dtype=np.int64)
         lib().hc3d_result_free(C.byref(r))
         return out
+
+    def cancel(self, ticket: int) -> int:
+        """Cancel a request (hc3d_server_cancel): a queued one is dropped, a
+        running one stops before its next iteration; its wait then raises
+        Hc3dError with code HC3D_ERR_CANCELLED.  Returns the call's code."""
+        return int(lib().hc3d_server_cancel(self._h, ticket))
 
     def stats(self) -> dict:
         st = ServerStats()

@@ -58,6 +58,7 @@ extern "C" {
 #define HC3D_ERR_IO (-6)          /* file could not be read or written */
 #define HC3D_ERR_UNSUPPORTED (-7) /* option of the reference that this build leaves out */
 #define HC3D_ERR_TIMEOUT (-8)     /* a bounded wait ran out */
+#define HC3D_ERR_CANCELLED (-9)   /* a server request was cancelled (hc3d_server_cancel) */
 
 #define HC3D_PREC_MIXED 0 /* FP32 walk/scatter/peel; FP64 radial quadratic, peel tau sum, Lucy root */
 #define HC3D_PREC_FP64 1  /* everything FP64: the all-FP64 GPU form */
@@ -278,7 +279,10 @@ int hc3d_lucy_iterations(hc3d_ctx *ctx, const hc3d_run_params *params, int n_ite
  * HC3D_NOALLOC_MAX_ELEMENTS; a larger one returns HC3D_ERR_INVALID with a
  * message on stderr.  The first call on each device looks the array's device
  * address up (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array, which keeps the
+ * call before any stream capture.  The address is kept for the life of the
+ * process, so the call must not be used on a device after cudaDeviceReset()
+ * (or any other end of the primary context it first ran in): the module is
+ * then loaded again at another address.  All calls share the array, which keeps the
  * last call's contents, so calls that overlap on the GPU (different streams
  * without ordering between them) race and must not be issued.  The call
  * returns after the update on `stream` is complete. */

@@ -165,6 +165,13 @@ int hc3d_server_submit(hc3d_server *s, const hc3d_request *req, int64_t *ticket)
  * for (one wait per ticket). */
 int hc3d_server_wait(hc3d_server *s, int64_t ticket, hc3d_result *out);
 void hc3d_result_free(hc3d_result *r);
+/* Cancel a request (no counterpart in the reference): a queued request is
+ * dropped at once; a running one stops before its next iteration, so no
+ * kernel of it is in flight when it ends.  Its wait then returns
+ * HC3D_ERR_CANCELLED.  Returns HC3D_ERR_STATE when the request has already
+ * finished (its result stands) and HC3D_ERR_INVALID for an unknown or
+ * already-waited ticket. */
+int hc3d_server_cancel(hc3d_server *s, int64_t ticket);
 int hc3d_server_get_stats(hc3d_server *s, hc3d_server_stats *st);
 /* Finish the queued requests, then release the slots. */
 void hc3d_server_destroy(hc3d_server *s);

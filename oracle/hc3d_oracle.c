@@ -64,6 +64,8 @@ typedef struct orc_tallies {
   double *image_i_d;   /* (npeel,nx,nx) FP64, may be NULL */
   double *dtauabs_d;   /* (nrg,ntg,npg,ndg) FP64 absorbed-path estimator, may be NULL */
   int64_t errors;      /* packets stopped by a geometry or table fault */
+  double *image_m2_d;  /* (npeel,nx,nx,4): per pixel the count of peeled rays and the
+                          sums of sip^2, sqp^2, sup^2 (variance of the image sums), may be NULL */
 } orc_tallies;
 
 typedef struct orc_trace {
@@ -658,6 +660,13 @@ static void orc_peeloff(const orc_ctx *c, const hc3d_run_params *rp, const pkt *
     t->fx.image_i[b] += fx_round(sip, ss); t->fx.image_q[b] += fx_round(sqp, ss);
     t->fx.image_u[b] += fx_round(sup, ss); t->fx.image_v[b] += fx_round(svp, ss);
     if (t->image_i_d) t->image_i_d[b] += sip;
+    if (t->image_m2_d) {
+      const int64_t n = (int64_t)rp->npeel * rp->nxhst * rp->nxhst;
+      t->image_m2_d[b] += 1.0;
+      t->image_m2_d[b + n] += sip * sip;
+      t->image_m2_d[b + 2 * n] += sqp * sqp;
+      t->image_m2_d[b + 3 * n] += sup * sup;
+    }
   }
 }
 
@@ -1084,6 +1093,109 @@ int orc_locate_c(const double *xx, int n, double x) { return orc_locate(xx, n, x
 void orc_findangle3_c(double cost1, double sint1, double phi1, double cosp1, double sinp1, double cost2,
                       double sint2, double phi2, double cosp2, double sinp2, double *out3) {
   orc_findangle3(cost1, sint1, phi1, cosp1, sinp1, cost2, sint2, phi2, cosp2, sinp2, &out3[0], &out3[1], &out3[2]);
+}
+
+/* ---- single-routine entry points, checked against an independent NumPy
+ * restatement of the Fortran routines (tests/golden/ref_routines.py) ------- */
+
+/* closest_wall.f90:13-66: insert n roots (t, id), then find_next_wall.
+ * state6 = tn1, tp1, tp2, in1, ip1, ip2; returns 0 when no wall is found. */
+int orc_closest_wall_c(int n, const double *t, const int *ids, int on_wall, double *tout, int *iout,
+                       double *state6) {
+  walls w;
+  reset_t(&w);
+  for (int k = 0; k < n; ++k) insert_t(&w, t[k], ids[k]);
+  state6[0] = w.tn1; state6[1] = w.tp1; state6[2] = w.tp2;
+  state6[3] = w.in1; state6[4] = w.ip1; state6[5] = w.ip2;
+  return find_next_wall(&w, on_wall, tout, iout);
+}
+
+/* phiface.f90:48-56 with C = D = 0 (planes through the z axis) */
+void orc_phiface_roots(double A1, double B1, double A2, double B2, double ux, double uy, double x1, double y1,
+                       double *out3, int *ids3) {
+  walls w;
+  reset_t(&w);
+  phiface(&w, A1, B1, A2, B2, ux, uy, x1, y1);
+  out3[0] = w.tn1; out3[1] = w.tp1; out3[2] = w.tp2;
+  ids3[0] = w.in1; ids3[1] = w.ip1; ids3[2] = w.ip2;
+}
+
+/* the dust_mod phase-function terms of one species with parameters g, pl
+ * (dust.f90:70-74) in slot 0 of a packet */
+static void orc_set_phase(pkt *p, double g, double pl) {
+  memset(p, 0, sizeof(*p));
+  p->g[0] = g; p->pl[0] = pl;
+  p->g2[0] = g * g; p->g2p1[0] = p->g2[0] + 1.0; p->onemg2[0] = 1.0 - p->g2[0]; p->twog[0] = 2.0 * g;
+}
+
+/* dustmat.f90:40-65: out4 = p1, p2, p3, p4 */
+void orc_dustmat_c(double g, double pl, double cost, double cost2, double *out4) {
+  pkt p;
+  orc_set_phase(&p, g, pl);
+  orc_dustmat(&p, 0, cost, cost2, &out4[0], &out4[1], &out4[2], &out4[3]);
+}
+
+/* stokespeel.f90:49-376 on s4 = (sip, sqp, sup, svp), in place */
+void orc_stokespeel_c(double g, double pl, double *s4, double cost, double sint, double ri1, double bmu,
+                      double costp, double sintp) {
+  pkt p;
+  orc_set_phase(&p, g, pl);
+  orc_stokespeel(&p, 0, &s4[0], &s4[1], &s4[2], &s4[3], cost, sint, ri1, bmu, costp, sintp);
+}
+
+/* stokes.f90:46-388 with injected uniforms u[0..nu).  st9 = (sip, sqp, sup,
+ * svp, cost, sint, phi, cosp, sinp), in place.  Returns the number of
+ * uniforms drawn, or -1 when u ran out. */
+int orc_stokes_c(double g, double pl, double *st9, const double *u, int nu) {
+  pkt p;
+  orc_set_phase(&p, g, pl);
+  p.sip = st9[0]; p.sqp = st9[1]; p.sup = st9[2]; p.svp = st9[3];
+  p.cost = st9[4]; p.sint = st9[5]; p.phi = st9[6]; p.cosp = st9[7]; p.sinp = st9[8];
+  orc_rng r;
+  orc_rng_init(&r, 0, 0, 0);
+  r.inj = u; r.ninj = nu; r.pos = 0;
+  orc_stokes(&p, 0, &r);
+  st9[0] = p.sip; st9[1] = p.sqp; st9[2] = p.sup; st9[3] = p.svp;
+  st9[4] = p.cost; st9[5] = p.sint; st9[6] = p.phi; st9[7] = p.cosp; st9[8] = p.sinp;
+  return r.exhausted ? -1 : r.pos;
+}
+
+/* opacset (dust.f90:9-80) at frequency nu: out = g[ndg], pl[ndg],
+ * albedo[ndg], kappa[ndg] (kappa = kappad interpolated, before the
+ * kappav and stellar-radius factors of kapd) */
+void orc_opacset_c(const hc3d_dust_tables *dt, const hc3d_grid *g, double nu, double *out) {
+  orc_ctx c;
+  orc_ctx_init(&c, dt, g);
+  pkt p;
+  memset(&p, 0, sizeof(p));
+  orc_opacset(&c, &p, nu, 1.0);
+  const int n = c.ndg;
+  for (int id = 0; id < n; ++id) {
+    out[id] = p.g[id];
+    out[n + id] = p.pl[id];
+    out[2 * n + id] = p.albedo[id];
+    out[3 * n + id] = p.kapd[id] / dt->kappav[id];
+  }
+}
+
+/* select_dust.f90:16-42 for one cell whose species densities are dens[ndg],
+ * opacities kapd[ndg] and draw xran; returns the 0-based species or -1 */
+int orc_select_dust_c(int ndg, const double *kapd, const double *dens, double xran) {
+  hc3d_grid g1;
+  memset(&g1, 0, sizeof(g1));
+  g1.nrg = 1; g1.ntg = 1; g1.npg = 1; g1.ndg = ndg;
+  g1.densarr = (double *)dens;
+  orc_ctx c;
+  memset(&c, 0, sizeof(c));
+  c.g = g1; c.ndg = ndg; c.ncell4 = 1;
+  pkt p;
+  memset(&p, 0, sizeof(p));
+  p.ir = 1; p.it = 1; p.ip = 1;
+  for (int id = 0; id < ndg; ++id) p.kapd[id] = kapd[id];
+  orc_rng r;
+  orc_rng_init(&r, 0, 0, 0);
+  r.inj = &xran; r.ninj = 1; r.pos = 0;
+  return orc_select_dust(&c, &p, &r);
 }
 
 /* Sample n scattering events of an unpolarised packet travelling along +z

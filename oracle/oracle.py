@@ -23,7 +23,7 @@ LIB_PATH = ROOT / "_build" / "libhc3d_oracle.so"
 
 class OrcTallies(C.Structure):
     _fields_ = [("fx", Tallies), ("si_d", P(C.c_double)), ("ti_d", P(C.c_double)), ("image_i_d", P(C.c_double)),
-                ("dtauabs_d", P(C.c_double)), ("errors", C.c_int64)]
+                ("dtauabs_d", P(C.c_double)), ("errors", C.c_int64), ("image_m2_d", P(C.c_double))]
 
 
 _LIB = None
@@ -58,6 +58,14 @@ def lib() -> C.CDLL:
         L.orc_dusttemp.argtypes = [P(DustTables)] + [C.c_double] * 4 + [C.c_int, C.c_double]
         L.orc_dusttemp.restype = C.c_double
         L.orc_tfinal.argtypes = [P(DustTables), P(Grid), dp, C.c_double, C.c_double, dp]
+        ip = P(C.c_int)
+        L.orc_closest_wall_c.argtypes = [C.c_int, dp, ip, C.c_int, dp, ip, dp]
+        L.orc_phiface_roots.argtypes = [C.c_double] * 8 + [dp, ip]
+        L.orc_dustmat_c.argtypes = [C.c_double] * 4 + [dp]
+        L.orc_stokespeel_c.argtypes = [C.c_double, C.c_double, dp] + [C.c_double] * 6
+        L.orc_stokes_c.argtypes = [C.c_double, C.c_double, dp, dp, C.c_int]
+        L.orc_opacset_c.argtypes = [P(DustTables), P(Grid), C.c_double, dp]
+        L.orc_select_dust_c.argtypes = [C.c_int, dp, dp, C.c_double]
         _LIB = L
     return _LIB
 
@@ -87,7 +95,7 @@ class OracleTallies:
         self._add(T.fx, "killed", self.g3, np.int32, C.c_int32)
         self._add(T.fx, "dbig", self.g3, np.int32, C.c_int32)
         for n, shape in (("si_d", self.sed_shape), ("ti_d", self.psed_shape), ("image_i_d", self.img_shape),
-                         ("dtauabs_d", self.g4)):
+                         ("dtauabs_d", self.g4), ("image_m2_d", self.img_shape + (4,))):
             arr = np.zeros(shape, dtype=np.float64, order="F")
             self.a[n] = arr
             setattr(T, n, arr.ctypes.data_as(P(C.c_double)))

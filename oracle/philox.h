@@ -11,6 +11,7 @@
  */
 #ifndef HC3D_ORACLE_PHILOX_H
 #define HC3D_ORACLE_PHILOX_H
+#include <math.h>
 #include <stdint.h>
 
 #define PHILOX_M0 0xD2511F53u
@@ -58,8 +59,11 @@ static inline void orc_rng_init(orc_rng *r, uint64_t seed, int iter, int64_t pid
 static inline double orc_ran(orc_rng *r) {
   if (r->inj) {
     if (r->pos < r->ninj) return r->inj[r->pos++];
+    /* past the end of the injected list: frac(0.5 + k (sqrt(5) - 1) / 2),
+     * as the device continues, so that rejection loops still end */
     r->exhausted = 1;
-    return 0.5;
+    double v = 0.5 + (double)(r->pos++ - r->ninj) * 0.6180339887498949;
+    return v - floor(v);
   }
   if (r->left == 0) {
     orc_philox4x32_10(r->ctr, r->key, r->buf);
