@@ -1,8 +1,13 @@
 """Build recipe of the GB300 library (sm_103a) and of the CPU oracle.
 
-``build_library()`` compiles the CUDA kernels, the C-ABI and the host driver
-into ``hochunk3d_gb300/libhc3d.so`` with nvcc; ``build_oracle()`` compiles the
-CPU restatement used by the tests into ``oracle/_build/libhc3d_oracle.so``.
+``build_host_library()`` compiles the host-only model set-up (the .par
+reader, gridset, the dust tables; no CUDA) into
+``hochunk3d_gb300/libhc3d_host.so`` with g++; ``build_library()`` compiles
+the CUDA kernels, the C-ABI, the server and the host driver into
+``hochunk3d_gb300/libhc3d.so`` with nvcc, linked against the host library;
+``build_oracle()`` compiles the CPU restatement used by the tests into
+``oracle/_build/libhc3d_oracle.so``.  A process that only sets models up
+(the CPU legs of the benchmark) loads the host library alone.
 Translation units are compiled in parallel; a unit is rebuilt when its source
 or any header is newer than its object file.
 """
@@ -19,6 +24,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhc3d.so"
+HOST_LIB = PKG / "libhc3d_host.so"
+HOST_UNITS = ["hc3d_model.cpp"]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "libhc3d_oracle.so"
 
@@ -38,7 +45,6 @@ UNITS = [
     ("hc3d_noalloc.cu", []),
     ("hc3d_gridbuild.cu", []),
     ("hc3d_tablebuild.cu", ["--fmad=false"]),
-    ("hc3d_model.cpp", []),
     ("hc3d_driver.cpp", []),
     ("hc3d_serve.cpp", []),
 ]
@@ -68,8 +74,24 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("command failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
+def build_host_library(verbose: bool = False, force: bool = False) -> Path:
+    """Compile the host-only model set-up into libhc3d_host.so (g++, no CUDA)."""
+    BUILD.mkdir(exist_ok=True)
+    srcs = [CSRC / u for u in HOST_UNITS]
+    if force or not HOST_LIB.exists() or any(_stale(HOST_LIB, src) for src in srcs):
+        tmp = HOST_LIB.with_suffix(".so.tmp")
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wl,-soname,libhc3d_host.so", "-o", str(tmp),
+              *map(str, srcs), "-lpthread"])
+        os.replace(tmp, HOST_LIB)
+    if verbose:
+        print(f"built {HOST_LIB}")
+    return HOST_LIB
+
+
 def build_library(verbose: bool = False, force: bool = False) -> Path:
-    """Compile every translation unit for sm_103a and link libhc3d.so."""
+    """Compile every translation unit for sm_103a and link libhc3d.so
+    against libhc3d_host.so (found beside it at run time)."""
+    build_host_library(verbose=verbose, force=force)
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     jobs = []
@@ -86,9 +108,11 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for _ in ex.map(_run, jobs):
                 pass
-    if force or jobs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+    if (force or jobs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs)
+            or HOST_LIB.stat().st_mtime > LIB.stat().st_mtime):
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-L" + str(PKG), "-lhc3d_host",
+              "-Xlinker", "-rpath=$ORIGIN", "-lpthread"])
         os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}")

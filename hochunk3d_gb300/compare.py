@@ -10,6 +10,10 @@ all-FP64 form (or the CPU oracle) with these measures:
   either side are left out.
 * ``max_rel_err``: the largest |a - b| / |b| of Stokes I over bins with at
   least ``min_count`` packets on both sides.
+* ``precise_rel_err``: the largest |a - b| / |b| of Stokes I over the bins
+  that b measures to better than a given Monte Carlo error
+  (sqrt(sum w^2) / sum w), so that a 1 % bound is tested only where the
+  bins resolve 1 %.
 * ``binned_image``: images summed over b x b pixel blocks, so that the
   per-pixel counts of a small run reach the chi^2 threshold.
 
@@ -65,6 +69,26 @@ def max_rel_err(a, b, min_count: int = 100) -> float:
     if not ok.any():
         return float("nan")
     return float(np.max(np.abs(sa[ok] - sb[ok]) / np.abs(sb[ok])))
+
+
+def precise_rel_err(a, b, mc_max: float = 0.005):
+    """(largest |a - b| / |b|, bins) of Stokes I over the bins whose Monte Carlo
+    error in b, sqrt(sum w^2) / sum w, is at most mc_max."""
+    sa, _, _ = a
+    sb, vb, nb = b
+    with np.errstate(divide="ignore", invalid="ignore"):
+        mc = np.sqrt(vb) / np.abs(sb)
+    ok = (nb > 1) & (sb != 0) & (mc <= mc_max)
+    if not ok.any():
+        return float("nan"), 0
+    return float(np.max(np.abs(sa[ok] - sb[ok]) / np.abs(sb[ok]))), int(ok.sum())
+
+
+def quantiles(x: np.ndarray, qs=(50, 90, 99, 100)) -> dict:
+    x = np.asarray(x, dtype=np.float64)
+    if x.size == 0:
+        return {("max" if q == 100 else f"p{q}"): None for q in qs}
+    return {("max" if q == 100 else f"p{q}"): float(np.percentile(x, q)) for q in qs}
 
 
 def binned_image(img: np.ndarray, b: int) -> np.ndarray:

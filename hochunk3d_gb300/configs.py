@@ -127,7 +127,7 @@ def write_fixtures(directory: str | Path) -> Path:
 
     d = Path(directory)
     d.mkdir(parents=True, exist_ok=True)
-    L = hc3d.lib()
+    L = hc3d.host_lib()
     rc = L.hc3d_write_synthetic_dust(str(d / DUST_FILE).encode())
     if rc != 0:
         raise hc3d.Hc3dError(rc, "cannot write dust fixture")

@@ -33,6 +33,7 @@ struct hc3d_ctx {
   double* d_tdust = nullptr;   // (ncell*4), also dm.tdust
   float* d_tdustf = nullptr;   // (ncell*4) FP32 copy, also dm.tdustf
   unsigned char* d_peelmask = nullptr;
+  float4* d_rho4p = nullptr;  // (ncell) peel-masked FP32 densities, also dm.rho4p
   int ndg_in = 0;
   // tallies
   DevTallies dt{};
@@ -48,7 +49,9 @@ struct hc3d_ctx {
   double* d_ap2 = nullptr;
   unsigned long long* d_maxrel = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t wev[3] = {nullptr, nullptr, nullptr};
+  cudaStream_t pstream = nullptr;   // the peel-off kernels of the wavefront loop
+  std::vector<cudaEvent_t> wev;     // 4 per wave: k_wave start/end (stream), k_peel start/end (pstream)
+  cudaEvent_t join = nullptr;       // end of the last k_peel of a run, waited for on stream
   double last_ms = 0.0, last_transport_ms = 0.0, last_peel_ms = 0.0;
   int last_launches = 0;
   std::vector<double> wave_log;  // per wave: E, active, alive after, transport ms, peel ms, events
@@ -134,8 +137,17 @@ __device__ double dusttemp_dev(const LucyArgs& a, double na, double T0, int s, d
   return lucy_dusttemp(a.lTint, a.nT, a.kappap + (size_t)s * a.nT, a.kappav[s], a.ltot, a.nphot, na, T0, massarr);
 }
 
+// The peel-off walk of the mixed form reads one row per cell with the peel
+// mask applied (a species hotter than Tsub contributes no opacity,
+// peeloff_3d.f90:105-110): rho4p = rho4f with the masked slots zeroed.
+__device__ __forceinline__ float4 masked_rho(float4 r, unsigned mask) {
+  return make_float4((mask & 1u) ? r.x : 0.f, (mask & 2u) ? r.y : 0.f, (mask & 4u) ? r.z : 0.f,
+                     (mask & 8u) ? r.w : 0.f);
+}
+
 __global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const double* rho4d, const double* massarr,
-                       double* tdust, float* tdustf, unsigned char* peelmask, unsigned long long* maxrel) {
+                       double* tdust, float* tdustf, unsigned char* peelmask, unsigned long long* maxrel,
+                       const float4* rho4f, float4* rho4p) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.ncell; c += (int64_t)gridDim.x * blockDim.x) {
     unsigned mask = 0;
     for (int s = 0; s < kSlots; ++s) {
@@ -154,15 +166,18 @@ __global__ void k_lucy(LucyArgs a, const unsigned long long* dtauabs, const doub
       if (T < a.tsub / 11605.0) mask |= 1u << s;
     }
     peelmask[c] = (unsigned char)mask;
+    rho4p[c] = masked_rho(rho4f[c], mask);
   }
 }
 
-__global__ void k_peelmask(int64_t ncell, const double* tdust, double tsub, unsigned char* peelmask) {
+__global__ void k_peelmask(int64_t ncell, const double* tdust, double tsub, unsigned char* peelmask,
+                           const float4* rho4f, float4* rho4p) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
     unsigned mask = 0;
     for (int s = 0; s < kSlots; ++s)
       if (tdust[4 * c + s] < tsub / 11605.0) mask |= 1u << s;
     peelmask[c] = (unsigned char)mask;
+    rho4p[c] = masked_rho(rho4f[c], mask);
   }
 }
 
@@ -293,7 +308,16 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   return HC3D_OK;
 }
 
-// Allocate the packet pool and event queue of the wavefront form once per context.
+// Release the wavefront buffers (after both streams are idle).
+void drop_wave(hc3d_ctx* c) {
+  if (!c->wave.pool) return;
+  cudaStreamSynchronize(c->pstream);
+  cudaStreamSynchronize(c->stream);
+  free_all(c, c->wave_allocs);
+  c->wave = WaveBufs{};
+}
+
+// Allocate the packet pool and the two event queues of the wavefront form once per context.
 int ensure_wave(hc3d_ctx* c) {
   const bool f64 = c->precision == HC3D_PREC_FP64;
   int per_sm = 0;
@@ -302,14 +326,7 @@ int ensure_wave(hc3d_ctx* c) {
   if (c->wave.pool) {
     // kept across hc3d_reset while the dust tables of the new model allow the same residency
     if (c->sm_count * per_sm == c->wave_blocks) return HC3D_OK;
-    CK(cudaStreamSynchronize(c->stream));
-    free_all(c, c->wave_allocs);
-    c->wave = WaveBufs{};
-    for (int i = 0; i < 3; ++i)
-      if (c->wev[i]) {
-        cudaEventDestroy(c->wev[i]);
-        c->wev[i] = nullptr;
-      }
+    drop_wave(c);
   }
   c->wave_blocks = c->sm_count * per_sm;
   c->pool_threads = (int64_t)c->wave_blocks * 128;
@@ -320,29 +337,46 @@ int ensure_wave(hc3d_ctx* c) {
   const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
   const size_t rec = f64 ? rec_bytes_fp64() : rec_bytes_mixed();
   int r;
-  unsigned char *pool, *queue;
+  unsigned char *pool, *q0, *q1;
   if ((r = dalloc(c, c->wave_allocs, &pool, slot * (size_t)c->pool_threads)) ||
-      (r = dalloc(c, c->wave_allocs, &queue, rec * (size_t)c->qcap)) ||
-      (r = dalloc(c, c->wave_allocs, &c->wave.qcount, 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.alive, 1)) ||
-      (r = dalloc(c, c->wave_allocs, &c->wave.next_ray, 1)))
+      (r = dalloc(c, c->wave_allocs, &q0, rec * (size_t)c->qcap)) ||
+      (r = dalloc(c, c->wave_allocs, &q1, rec * (size_t)c->qcap)) ||
+      (r = dalloc(c, c->wave_allocs, &c->wave.qcount[0], 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.qcount[1], 1)) ||
+      (r = dalloc(c, c->wave_allocs, &c->wave.alive, 1)) ||
+      (r = dalloc(c, c->wave_allocs, &c->wave.next_ray[0], 1)) || (r = dalloc(c, c->wave_allocs, &c->wave.next_ray[1], 1)))
     return r;
   c->wave.pool = pool;
-  c->wave.queue = queue;
-  for (int i = 0; i < 3; ++i) CK(cudaEventCreate(&c->wev[i]));
+  c->wave.queue[0] = q0;
+  c->wave.queue[1] = q1;
+  return HC3D_OK;
+}
+
+// the events of wave w (created on first use, kept with the context)
+int wave_events(hc3d_ctx* c, int w) {
+  while ((int)c->wev.size() < 4 * (w + 1)) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->wev.push_back(e);
+  }
   return HC3D_OK;
 }
 
 // The wavefront loop of one peeled run: waves until the batch is exhausted
-// and no packet is alive.  The per-wave event budget E keeps the queue within
+// and no packet is alive.  The per-wave event budget E keeps a queue within
 // its capacity: at most min(pool, alive + unstarted) threads append, each at
-// most E records.
+// most E records.  Wave w's k_wave fills queue w % 2 on the context's stream;
+// its k_peel walks that queue on the second stream, while k_wave of wave w + 1
+// fills the other queue on the first.  So the peel-off work of one wave runs
+// beside the transport of the next -- in particular beside the long packet
+// histories that leave most of the device idle at the end of a batch.  Before
+// k_wave reuses a queue it waits for the k_peel that read it.
 int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
   int r;
   if ((r = ensure_wave(c))) return r;
   const bool f64 = c->precision == HC3D_PREC_FP64;
   const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
   CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
-  LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->stream};
+  LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->pstream};
   int64_t alive_prev = 0;
   unsigned long long work = 0, events_prev = 0;
   CK(cudaMemcpyAsync(&events_prev, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events_prev), cudaMemcpyDeviceToHost,
@@ -350,17 +384,35 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
   c->last_transport_ms = c->last_peel_ms = 0.0;
   c->last_launches = 0;
   c->wave_log.clear();
+  int nwave = 0;
+  int prev_peel_end[2] = {-1, -1};  // index in wev of the k_peel end that last read each queue
   for (int wave = 0;; ++wave) {
     const int64_t remaining = p->np - (int64_t)std::min<unsigned long long>(work, (unsigned long long)p->np);
     const int64_t active = std::min<int64_t>(c->pool_threads, alive_prev + remaining);
     if (active <= 0) break;
     const int E = (int)std::max<int64_t>(1, std::min<int64_t>(c->qcap / active, 1 << 20));
-    CK(cudaMemsetAsync(c->wave.qcount, 0, sizeof(unsigned long long), c->stream));
+    const int q = wave & 1;
+    if ((r = wave_events(c, wave))) return r;
+    const int ev = 4 * wave;
+    if (prev_peel_end[q] >= 0) CK(cudaStreamWaitEvent(c->stream, c->wev[prev_peel_end[q]], 0));  // queue q read
+    CK(cudaMemsetAsync(c->wave.qcount[q], 0, sizeof(unsigned long long), c->stream));
     CK(cudaMemsetAsync(c->wave.alive, 0, sizeof(unsigned int), c->stream));
-    CK(cudaMemsetAsync(c->wave.next_ray, 0, sizeof(unsigned long long), c->stream));
-    cudaError_t e = f64 ? launch_wave_fp64(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev)
-                        : launch_wave_mixed(c->dm, c->dt, c->dims, a, c->wave, E, wc, pc, c->wev);
+    CK(cudaEventRecord(c->wev[ev], c->stream));
+    cudaError_t e = f64 ? launch_wave_transport_fp64(c->dm, c->dt, c->dims, a, c->wave, q, E, wc)
+                        : launch_wave_transport_mixed(c->dm, c->dt, c->dims, a, c->wave, q, E, wc);
     if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("wave launch: ") + cudaGetErrorString(e));
+    CK(cudaEventRecord(c->wev[ev + 1], c->stream));
+    // the peel-off rays of this wave, on the second stream
+    CK(cudaStreamWaitEvent(c->pstream, c->wev[ev + 1], 0));
+    CK(cudaMemsetAsync(c->wave.next_ray[q], 0, sizeof(unsigned long long), c->pstream));
+    CK(cudaEventRecord(c->wev[ev + 2], c->pstream));
+    e = f64 ? launch_wave_peel_fp64(c->dm, c->dt, c->dims, a, c->wave, q, pc)
+            : launch_wave_peel_mixed(c->dm, c->dt, c->dims, a, c->wave, q, pc);
+    if (e != cudaSuccess) return fail(c, HC3D_ERR_CUDA, std::string("peel-off launch: ") + cudaGetErrorString(e));
+    CK(cudaEventRecord(c->wev[ev + 3], c->pstream));
+    prev_peel_end[q] = ev + 3;
+    // whether another wave is needed: the counters after this k_wave (the
+    // copies wait for it on the first stream, not for the k_peel)
     unsigned int alive = 0;
     unsigned long long events = 0;
     CK(cudaMemcpyAsync(&alive, c->wave.alive, sizeof(alive), cudaMemcpyDeviceToHost, c->stream));
@@ -368,19 +420,32 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     CK(cudaMemcpyAsync(&events, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events), cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    float t0 = 0.f, t1 = 0.f;
-    CK(cudaEventElapsedTime(&t0, c->wev[0], c->wev[1]));
-    CK(cudaEventElapsedTime(&t1, c->wev[1], c->wev[2]));
-    c->last_transport_ms += t0;
-    c->last_peel_ms += t1;
-    c->last_launches += 2;
     c->wave_log.insert(c->wave_log.end(),
-                       {(double)E, (double)active, (double)alive, (double)t0, (double)t1, (double)(events - events_prev)});
+                       {(double)E, (double)active, (double)alive, 0.0, 0.0, (double)(events - events_prev)});
     events_prev = events;
     alive_prev = alive;
+    ++nwave;
     if (alive == 0 && work >= (unsigned long long)p->np) break;
   }
-  c->last_ms = c->last_transport_ms + c->last_peel_ms;
+  // the first stream waits for the last k_peel, so that what follows on it
+  // (tallies, temperatures) sees every ray
+  CK(cudaEventRecord(c->join, c->pstream));
+  CK(cudaStreamWaitEvent(c->stream, c->join, 0));
+  CK(cudaEventSynchronize(c->join));
+  for (int w = 0; w < nwave; ++w) {
+    float t0 = 0.f, t1 = 0.f;
+    CK(cudaEventElapsedTime(&t0, c->wev[4 * w], c->wev[4 * w + 1]));
+    CK(cudaEventElapsedTime(&t1, c->wev[4 * w + 2], c->wev[4 * w + 3]));
+    c->last_transport_ms += t0;
+    c->last_peel_ms += t1;
+    c->wave_log[6 * w + 3] = t0;
+    c->wave_log[6 * w + 4] = t1;
+  }
+  c->last_launches = 2 * nwave;
+  // the span of the loop: first k_wave start to last k_peel end (the kernels overlap)
+  float span = 0.f;
+  if (nwave) CK(cudaEventElapsedTime(&span, c->wev[0], c->join));
+  c->last_ms = span;
   return HC3D_OK;
 }
 
@@ -426,6 +491,13 @@ extern "C" int hc3d_create(hc3d_ctx** out, const hc3d_device_opts* opts) {
     delete c;
     return HC3D_ERR_CUDA;
   }
+  if (cudaStreamCreateWithFlags(&c->pstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->join) != cudaSuccess) {
+    if (c->pstream) cudaStreamDestroy(c->pstream);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return HC3D_ERR_CUDA;
+  }
   {
     // keep freed stream-ordered memory in this process's pool for the next
     // model instead of returning it to the driver at every synchronisation
@@ -467,10 +539,13 @@ extern "C" void hc3d_destroy(hc3d_ctx* c) {
   free_all(c, c->model_allocs);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
-  for (int i = 0; i < 3; ++i)
-    if (c->wev[i]) cudaEventDestroy(c->wev[i]);
+  if (c->pstream) cudaStreamSynchronize(c->pstream);
+  for (cudaEvent_t e : c->wev) cudaEventDestroy(e);
+  c->wev.clear();
+  if (c->join) cudaEventDestroy(c->join);
   free_all(c, c->wave_allocs);
   free_all(c, c->core_allocs);
+  if (c->pstream) cudaStreamDestroy(c->pstream);
   if (c->stream) {
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
@@ -493,6 +568,7 @@ extern "C" int hc3d_reset(hc3d_ctx* c) {
   c->d_kappap = c->d_massarr = c->d_tdust = nullptr;
   c->d_tdustf = nullptr;
   c->d_peelmask = nullptr;
+  c->d_rho4p = nullptr;
   c->ndg_in = 0;
   // the run tallies go; the counters and the fault log stay with the context
   DevTallies keep{};
@@ -715,7 +791,8 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
   c->tsub = t->tsub > 0.0 ? t->tsub : 1600.0;
   c->tables = true;
   if (c->grid) {
-    k_peelmask<<<grid_blocks_for(c, c->dm.ncell), 256, 0, c->stream>>>(c->dm.ncell, c->d_tdust, c->tsub, c->d_peelmask);
+    k_peelmask<<<grid_blocks_for(c, c->dm.ncell), 256, 0, c->stream>>>(c->dm.ncell, c->d_tdust, c->tsub, c->d_peelmask,
+                                                                       c->dm.rho4f, c->d_rho4p);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
   }
@@ -787,7 +864,8 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       (r = dupload(c, own, &d_hemi, hemi.data(), hemi.size())) || (r = dupload(c, own, &d_af, af.data(), af.size())) ||
       (r = dupload(c, own, &d_bf, bf.data(), bf.size())) || (r = dupload(c, own, &d_rf, rf.data(), rf.size())) ||
       (r = dupload(c, own, &d_rd, rd.data(), rd.size())) || (r = dupload(c, own, &c->d_tdust, td.data(), td.size())) ||
-      (r = dupload(c, own, &c->d_massarr, ma.data(), ma.size())) || (r = dalloc(c, own, &c->d_peelmask, (size_t)ncell)))
+      (r = dupload(c, own, &c->d_massarr, ma.data(), ma.size())) || (r = dalloc(c, own, &c->d_peelmask, (size_t)ncell)) ||
+      (r = dalloc(c, own, &c->d_rho4p, (size_t)ncell)))
     return r;
   {
     const std::vector<float> tdf(td.begin(), td.end());
@@ -814,26 +892,65 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
     float2* d_cs = nullptr;
     if ((r = dupload(c, own, &d_cs, cs.data(), cs.size()))) return r;
     m.thcs = d_cs;
-    std::vector<float2> r2p(nrg - 1), cf(ntg), pf(npg);
+    std::vector<float2> r2p(nrg - 1), cf(ntg), pf(npg), cc(ntg);
     for (int i = 0; i < nrg - 1; ++i) r2p[i] = make_float2(r2f32[i], r2f32[i + 1]);
     for (int i = 0; i < ntg; ++i) cf[i] = make_float2(tan2f[i], hemi[i]);
+    for (int i = 0; i < ntg; ++i) {
+      // cos^2 theta of the wall; the midplane (tan2arr = -1) and the poles (tan2arr = 0) are marked
+      const double cth = std::cos(g->thetarr[i]);
+      if (g->tan2arr[i] < 0.0) cc[i] = make_float2(-1.f, 0.f);
+      else if (g->tan2arr[i] == 0.0) cc[i] = make_float2(1.f, 0.f);
+      else cc[i] = make_float2((float)(cth * cth), hemi[i]);
+    }
     for (int i = 0; i < npg; ++i) pf[i] = make_float2(af[i], bf[i]);
-    float2 *d_r2p = nullptr, *d_cf = nullptr, *d_pf = nullptr;
+    float2 *d_r2p = nullptr, *d_cf = nullptr, *d_pf = nullptr, *d_cc = nullptr;
     if ((r = dupload(c, own, &d_r2p, r2p.data(), r2p.size())) || (r = dupload(c, own, &d_cf, cf.data(), cf.size())) ||
-        (r = dupload(c, own, &d_pf, pf.data(), pf.size())))
+        (r = dupload(c, own, &d_pf, pf.data(), pf.size())) || (r = dupload(c, own, &d_cc, cc.data(), cc.size())))
       return r;
     m.r2pair = d_r2p;
     m.conef = d_cf;
+    m.conec = d_cc;
     m.planef = d_pf;
   }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
-  m.peelmask = c->d_peelmask; m.tdust = c->d_tdust; m.tdustf = c->d_tdustf;
+  m.peelmask = c->d_peelmask; m.rho4p = c->d_rho4p; m.tdust = c->d_tdust; m.tdustf = c->d_tdustf;
   c->ndg_in = g->ndg;
-  k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask);
+  k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask, d_rf,
+                                                                c->d_rho4p);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
   c->grid = true;
   return hc3d_zero_tallies(c);
+}
+
+extern "C" int hc3d_set_tdust(hc3d_ctx* c, const double* tdust) {
+  if (!c || !tdust) return HC3D_ERR_INVALID;
+  if (!c->grid) return fail(c, HC3D_ERR_STATE, "load the grid first");
+  CK(cudaSetDevice(c->device));
+  const int nrg = c->dm.nrg, ntg = c->dm.ntg, npg = c->dm.npg;
+  const int64_t n4 = (int64_t)nrg * ntg * npg, ncell = c->dm.ncell;
+  const int ns = std::min(c->ndg_in, kSlots);
+  // the device layout of hc3d_load_grid: 4 slots per compact cell; empty slots keep the floor value
+  std::vector<double> td(4 * ncell, 0.1 / 11605.0);
+  for (int ip = 1; ip < npg; ++ip)
+    for (int it = 1; it < ntg; ++it)
+      for (int ir = 1; ir < nrg; ++ir) {
+        const int64_t c4 = (int64_t)(ir - 1) + (int64_t)nrg * ((it - 1) + (int64_t)ntg * (ip - 1));
+        const int64_t cc = (int64_t)(ir - 1) + (int64_t)(nrg - 1) * ((it - 1) + (int64_t)(ntg - 1) * (ip - 1));
+        for (int s = 0; s < ns; ++s) {
+          const double v = tdust[c4 + n4 * s];
+          if (!(v >= 0.0) || std::isinf(v)) return fail(c, HC3D_ERR_INVALID, "tdust holds a negative, NaN or infinite value");
+          td[4 * cc + s] = v > 0.0 ? v : 0.1 / 11605.0;  // 0: the 0.1 K floor of the starting field
+        }
+      }
+  const std::vector<float> tdf(td.begin(), td.end());
+  CK(cudaMemcpyAsync(c->d_tdust, td.data(), td.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_tdustf, tdf.data(), tdf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask, c->dm.rho4f,
+                                                                c->d_rho4p);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return HC3D_OK;
 }
 
 extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
@@ -1012,16 +1129,7 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
   double best = 1e300;
   for (int k = 0; k < n; ++k) {
     if (waves) {
-      if (c->wave.pool) {  // reallocated by the next run at the new depth
-        CK(cudaStreamSynchronize(c->stream));
-        free_all(c, c->wave_allocs);
-        c->wave = WaveBufs{};
-        for (int i = 0; i < 3; ++i)
-          if (c->wev[i]) {
-            cudaEventDestroy(c->wev[i]);
-            c->wev[i] = nullptr;
-          }
-      }
+      drop_wave(c);  // reallocated by the next run at the new depth
       c->queue_records = queues[k];
     } else {
       c->block_size = blocks[k];
@@ -1045,16 +1153,7 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
   }
   out->n = n;
   if (waves) {
-    if (c->queue_records != out->queue_records[out->best]) {
-      CK(cudaStreamSynchronize(c->stream));
-      free_all(c, c->wave_allocs);
-      c->wave = WaveBufs{};
-      for (int i = 0; i < 3; ++i)
-        if (c->wev[i]) {
-          cudaEventDestroy(c->wev[i]);
-          c->wev[i] = nullptr;
-        }
-    }
+    if (c->queue_records != out->queue_records[out->best]) drop_wave(c);
     c->queue_records = out->queue_records[out->best];
   } else {
     c->block_size = out->block_size[out->best];
@@ -1209,7 +1308,7 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
   const LucyArgs a = lucy_args(c, ltot, np);
   CK(cudaMemsetAsync(c->d_maxrel, 0, sizeof(unsigned long long), c->stream));
   k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust, c->d_tdustf,
-                                                           c->d_peelmask, c->d_maxrel);
+                                                           c->d_peelmask, c->d_maxrel, c->dm.rho4f, c->d_rho4p);
   CK(cudaGetLastError());
   unsigned long long bits = 0;
   CK(cudaMemcpyAsync(&bits, c->d_maxrel, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
@@ -1273,7 +1372,8 @@ extern "C" int hc3d_lucy_iterations(hc3d_ctx* c, const hc3d_run_params* p, int n
                                          : launch_transport_mixed(c->dm, c->dt, c->dims, args[(size_t)k], cfg);
     if (e == cudaSuccess) {
       k_lucy<<<grid_blocks_for(c, la.ncell), 256, 0, st>>>(la, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust,
-                                                           c->d_tdustf, c->d_peelmask, d_rel + k);
+                                                           c->d_tdustf, c->d_peelmask, d_rel + k, c->dm.rho4f,
+                                                           c->d_rho4p);
       e = cudaGetLastError();
     }
   }

@@ -59,12 +59,15 @@ struct DevModel {
   // interleaved FP32 wall data of the mixed-form wall search (one load per family)
   const float2* r2pair;   // (nrg-1) squared inner and outer radius of radial cell ir (index ir-1)
   const float2* conef;    // (ntg) tan^2 and hemisphere sign of polar wall it (index it-1)
+  const float2* conec;    // (ntg) cos^2 theta and hemisphere sign of polar wall it: C < 0 marks the
+                          // midplane, a hemisphere sign of 0 a pole (mixed-form peel-off walk)
   const float2* planef;   // (npg) A = sin(phi), B = -cos(phi) of azimuthal wall ip (index ip-1)
   const double* aarrd; const double* barrd;  // (npg)
   const float* aarrf; const float* barrf;    // (npg)
   const float4* rho4f;    // (ncell) species slots x,y,z,w  (mixed form)
   const double* rho4d;    // (ncell*4)                     (FP64 form)
   const unsigned char* peelmask;  // (ncell) bit s: tdust(s) < Tsub
+  const float4* rho4p;    // (ncell) rho4f with the slots outside the peel mask zeroed (mixed-form peel-off)
   const double* tdust;    // (ncell*4) K/11605
   const float* tdustf;    // (ncell*4) FP32 copy (mixed form)
   // dust tables
@@ -135,23 +138,26 @@ cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const
 cudaError_t launch_transport_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                   const LaunchCfg& cfg);
 // Buffers of the wavefront form: the packet pool (one slot per thread of
-// k_wave) and the peel-off event queue.
+// k_wave) and two peel-off event queues, so that the peel-off rays of one
+// wave are walked while k_wave fills the other queue with the next wave.
 struct WaveBufs {
   void* pool;
-  void* queue;
-  unsigned long long* qcount;
+  void* queue[2];
+  unsigned long long* qcount[2];
   unsigned int* alive;
-  unsigned long long* next_ray;  // ray counter of k_peel
+  unsigned long long* next_ray[2];  // ray counters of k_peel
 };
 
-// One wave: k_wave (advance every live packet by up to E events) then k_peel
-// (walk the queued peel-off rays); ev[0..2] bracket the two kernels.
-cudaError_t launch_wave_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
-                              const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
-                              cudaEvent_t ev[3]);
-cudaError_t launch_wave_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
-                             const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
-                             cudaEvent_t ev[3]);
+// k_wave: advance every live packet by up to E events, appending peel-off
+// records to queue q; k_peel: walk the peel-off rays of queue q.
+cudaError_t launch_wave_transport_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                        const WaveBufs& w, int q, int E, const LaunchCfg& cfg);
+cudaError_t launch_wave_peel_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                   const WaveBufs& w, int q, const LaunchCfg& cfg);
+cudaError_t launch_wave_transport_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                       const WaveBufs& w, int q, int E, const LaunchCfg& cfg);
+cudaError_t launch_wave_peel_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                  const WaveBufs& w, int q, const LaunchCfg& cfg);
 size_t slot_bytes_mixed();
 size_t slot_bytes_fp64();
 size_t rec_bytes_mixed();

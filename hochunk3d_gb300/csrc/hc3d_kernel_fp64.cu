@@ -31,20 +31,19 @@ const void* transport_batch_fn_fp64() { return (const void*)dev::k_transport_bat
 
 namespace hc3d {
 
-cudaError_t launch_wave_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
-                              const WaveBufs& w, int E, const LaunchCfg& wave, const LaunchCfg& peel,
-                              cudaEvent_t ev[3]) {
-  cudaError_t e;
-  if (ev && (e = cudaEventRecord(ev[0], wave.stream)) != cudaSuccess) return e;
-  dev::k_wave<double><<<wave.blocks, wave.threads, m.dust_smem, wave.stream>>>(
-      m, t, d, a, static_cast<dev::Slot<double>*>(w.pool), static_cast<dev::PeelRec<double>*>(w.queue), w.qcount, E, w.alive);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (ev && (e = cudaEventRecord(ev[1], wave.stream)) != cudaSuccess) return e;
-  dev::k_peel<double><<<peel.blocks, peel.threads, 0, peel.stream>>>(
-      m, t, d, a, static_cast<const dev::PeelRec<double>*>(w.queue), w.qcount, w.next_ray);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (ev && (e = cudaEventRecord(ev[2], wave.stream)) != cudaSuccess) return e;
-  return cudaSuccess;
+cudaError_t launch_wave_transport_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                        const WaveBufs& w, int q, int E, const LaunchCfg& cfg) {
+  dev::k_wave<double><<<cfg.blocks, cfg.threads, m.dust_smem, cfg.stream>>>(
+      m, t, d, a, static_cast<dev::Slot<double>*>(w.pool), static_cast<dev::PeelRec<double>*>(w.queue[q]), w.qcount[q], E,
+      w.alive);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wave_peel_fp64(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
+                                   const WaveBufs& w, int q, const LaunchCfg& cfg) {
+  dev::k_peel<double><<<cfg.blocks, cfg.threads, 0, cfg.stream>>>(
+      m, t, d, a, static_cast<const dev::PeelRec<double>*>(w.queue[q]), w.qcount[q], w.next_ray[q]);
+  return cudaGetLastError();
 }
 
 size_t slot_bytes_fp64() { return sizeof(dev::Slot<double>); }

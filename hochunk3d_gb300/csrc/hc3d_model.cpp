@@ -1106,8 +1106,19 @@ static bool gridset(Model* m, std::string* err) {
             sig[i] += std::fabs(densdisk(*m, rad, sint, cost, phic(ip), id) * rad * dcost * rmincgs) / (double)(npg - 1);
         }
       }
-      // a gap wall with no disk inside it (sig[0] = 0) keeps the disk's scale
-      rhogap[id] = sig[0] > 0.0 ? m->rho0[id] * m->rhoscale_gap[id] * sig[1] / sig[0] : m->rho0[id] * m->rhoscale_gap[id];
+      // The reference divides by the surface density just inside the gap's
+      // outer wall; a disk with none there (sig[0] = 0 while the slot holds
+      // a disk) leaves the gap's density scale undefined: reject the model.
+      if (!(sig[0] > 0.0)) {
+        if (m->rho0[id] != 0.0 && m->rhoscale_gap[id] != 0.0) {
+          *err = "CGAPD=YES: the disk has no density just inside the gap's outer wall (0.9 RGAPD2), so the "
+                 "gap's density scale rho0 RHOSCALE_GAP sigma(1.1 RGAPD2) / sigma(0.9 RGAPD2) is undefined";
+          return false;
+        }
+        rhogap[id] = 0.0;
+        continue;
+      }
+      rhogap[id] = m->rho0[id] * m->rhoscale_gap[id] * sig[1] / sig[0];
     }
     for (int id = 0; id < 2; ++id) m->rhogap0[id] = rhogap[id];
   }

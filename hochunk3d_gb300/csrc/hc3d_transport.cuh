@@ -1371,16 +1371,128 @@ __device__ __forceinline__ void peel_tally_mixed(const DevTallies& t, const Tall
   }
 }
 
-// The walk of one peel-off ray of the mixed form (peeloff_3d.f90:52-154):
-// start() sets it up from an event record and a direction, step() crosses
-// one cell wall.
-struct PeelWalk {
-  Ray ray;
-  PathLen S;
-  double tsum;  // FP64 escape tau
-  float tf;     // FP32 copy of the sum for the taumax test only
-  int ir, it, ip, on_wall, nstep, nreloc, ntiny;
+// The walk of one peel-off ray of the mixed form (peeloff_3d.f90:52-154).
+//
+// A peel-off ray is a straight line x(t) = c + t u, with t measured from the
+// point c of closest approach to the origin (c.u = 0, |c| = p).  Each wall
+// family's crossings along the line follow from invariants of the ray:
+//   spheres  |x|^2 = p^2 + t^2 = R^2        t = -+sqrt((R - p)(R + p))
+//   cones    C rho^2 = (1 - C) z^2,          a t^2 + 2 h t + q = 0 with
+//            C = cos^2 theta                 a = C - uz^2, h = -cz uz, q = C p^2 - cz^2
+//   planes   A x + B y = 0                   t = -(A cx + B cy) / (A ux + B uy)
+// The walk keeps the next crossing of each family: the sphere bounding the
+// cell in the direction of travel, the two roots ahead on each polar wall of
+// the cell, and the azimuthal wall the ray turns towards (its azimuth
+// changes monotonically).  A step crosses the nearest of them and recomputes
+// only that family's next crossing -- one square root or one division --
+// instead of the roots of every wall of the cell; the cell index changes
+// only at those crossings, so the walk needs no re-location.  Measuring t
+// from the point of closest approach keeps the FP32 resolution of t
+// proportional to the distance from the origin, where the cells are
+// proportionally small.  FP64 enters once per ray (the start point and c)
+// and once per round of crossings (the escape tau sum, flush_tau).
+//
+// Walls the event sits on (PeelRec bits 8-14): a radial wall moves the ray
+// into the cell on its side of travel (peeloff_3d.f90:60-87, tested on any
+// wall as there); the root of a polar or azimuthal wall at the start point
+// is not taken (the on_wall rule of closest_wall.f90:49-58).
+constexpr float kInf = 3.402823466e38f;
+
+// A ray set up by PeelWalk::start() (k_peel_mixed keeps these in shared
+// memory until a lane takes one): the walk state at its first crossing
+// search, its event record e and direction k.
+struct PeelStart {
+  float cx, cy, cz, p, p2, t, tr, lo1, lo2, hi1, hi2, tp;
   float kap[kSlots];
+  int irit;  // ir | it << 16
+  int ipup;  // ip | up << 16
+  unsigned e;
+  int k;
+};
+
+struct PeelWalk {
+  float cx, cy, cz, ux, uy, uz;  // point of closest approach, direction
+  float p, p2;                   // |c| and |c|^2
+  float t;                       // parameter of the current point
+  float tr;                      // next sphere crossing: the inner sphere when tr < 0, else the outer
+  float lo1, lo2, hi1, hi2;      // roots ahead on the lower and upper polar wall of the cell
+  float tp;                      // next azimuthal crossing
+  int ir, it, ip, nstep;
+  bool up;                       // azimuth increases along the ray
+  float kap[kSlots];
+  double tsum;  // FP64 escape tau: the FP32 partial sum tpart is added once per round
+  float tpart;
+  float tf;     // FP32 running tau, for the taumax test only
+
+  enum { GOING = 0, OUT = 1, ENDED = 2 };  // OUT: left the grid, to be tallied
+
+  // the sphere bounding cell ir in the direction of travel at parameter t
+  __device__ __forceinline__ void next_sphere(const DevModel& m) {
+    const float rin = __ldg(m.rarrf + ir - 1);
+    if (t < 0.f && rin > p) {
+      const float ti = -fsqrt_pos((rin - p) * (rin + p));
+      if (ti >= t) {
+        tr = ti;
+        return;
+      }
+    }
+    const float rout = __ldg(m.rarrf + ir);
+    const float q = (rout - p) * (rout + p);
+    tr = fmaxf(fmaxf(q > 0.f ? fsqrt_pos(q) : 0.f, t), 0.f);
+  }
+
+  // The roots r1 <= r2 at or after t of polar wall w (index into conec) on
+  // the nappe of its hemisphere, kInf where there are none; own: the ray
+  // starts on this wall, so the root nearest t is not taken.  The cone is
+  // C rho^2 - (1 - C) z^2 = 0 with C = cos^2 theta, so no coefficient grows
+  // like tan^2 theta near the midplane; with |u| = 1 and c.u = 0 the terms
+  // are a = C - uz^2, h = -cz uz, q = C p^2 - cz^2, and the discriminant
+  // h^2 - a q = C (cz^2 - a p^2) has no cancelling terms.
+  __device__ __forceinline__ void cone_roots(const DevModel& m, int w, bool own, float& r1, float& r2) const {
+    r1 = r2 = kInf;
+    const float2 cw = __ldg(m.conec + w);
+    const float C = cw.x, hemi = cw.y;
+    if (hemi == 0.f) return;  // a pole: no crossing
+    if (C < 0.f) {            // the midplane z = 0
+      if (!own && uz != 0.f) {
+        const float r = __fdividef(-cz, uz);
+        if (r >= t) r1 = r;
+      }
+      return;
+    }
+    const float a = fmaf(-uz, uz, C);
+    const float h = -cz * uz;
+    const float q = fmaf(C, p2, -cz * cz);
+    const float D = C * fmaf(-a, p2, cz * cz);
+    if (!(D > 0.f)) return;
+    const float w_ = -(h + copysignf(fsqrt_pos(D), h));  // |w_| >= sqrt(D) > 0
+    const float ra = a != 0.f ? __fdividef(w_, a) : kInf, rb = __fdividef(q, w_);
+    const float x1 = fminf(ra, rb), x2 = fmaxf(ra, rb);
+    bool v1 = fmaf(x1, uz, cz) * hemi > 0.f;
+    bool v2 = x2 < kInf && fmaf(x2, uz, cz) * hemi > 0.f;
+    if (own) {
+      if (fabsf(x1 - t) <= fabsf(x2 - t)) v1 = false;
+      else v2 = false;
+    }
+    v1 = v1 && x1 >= t;
+    v2 = v2 && x2 >= t;
+    r1 = v1 ? x1 : (v2 ? x2 : kInf);
+    r2 = v1 && v2 ? x2 : kInf;
+  }
+
+  // the crossing at or after t of azimuthal wall w (index into planef) on its
+  // half-plane, kInf where there is none
+  __device__ __forceinline__ float plane_root(const DevModel& m, int w) const {
+    const float2 ab = __ldg(m.planef + w);
+    const float A = ab.x, B = ab.y;
+    const float den = fmaf(A, ux, B * uy);
+    if (den == 0.f) return kInf;
+    const float r = __fdividef(-fmaf(A, cx, B * cy), den);
+    if (!(r >= t)) return kInf;
+    // (x, y) . (cos phi, sin phi) > 0 with cos phi = -B, sin phi = A
+    if (fmaf(A, fmaf(r, uy, cy), -B * fmaf(r, ux, cx)) <= 0.f) return kInf;
+    return r;
+  }
 
   // false when the ray is not walked (the star's far side, or it enters the star)
   __device__ __forceinline__ bool start(const DevModel& m, const PeelRec<float>& r, const PeelDir& dd) {
@@ -1390,36 +1502,49 @@ struct PeelWalk {
       const float cosnorm = r.d0 * dd.coste + (r.d1 * dd.sinte * (dd.cospe * r.d2 + dd.sinpe * r.d3));
       if (!(cosnorm > 0.f)) return false;
     }
-    ray_init(ray, r.x, r.y, r.z, dd.ux, dd.uy, dd.uz);
     ir = r.ir; it = r.it; ip = r.ip;
-    on_wall = (flags >> 8) & 127;
+    const int own = (flags >> 8) & 127;
+    const double x = dval(r.x), y = dval(r.y), z = dval(r.z);
+    const double uxd = dd.ux, uyd = dd.uy, uzd = dd.uz;
+    const double b = x * uxd + y * uyd + z * uzd;  // t of the start point
     bool go = true;
-    if (on_wall) {  // peeloff_3d.f90:60-87: leave the radial wall the event sits on
-      const double x = dval(r.x), y = dval(r.y), z = dval(r.z);
+    if (own) {  // peeloff_3d.f90:60-87: leave the radial wall the event sits on
       const double rr0 = x * x + y * y + z * z;
-      const double hb0 = x * (double)dd.ux + y * (double)dd.uy + z * (double)dd.uz;
       const bool inner_wall = fabs(rr0 - __ldg(m.r2arr + ir - 1)) < fabs(rr0 - __ldg(m.r2arr + ir));
-      const bool outwards = hb0 > 0.0;
+      const bool outwards = b > 0.0;
       if (inner_wall && !outwards) {
         if (ir == 1) go = false;
         ir = ir - 1;
-        on_wall = 1 << 2;
       }
-      if (!inner_wall && outwards) {
-        ir = ir + 1;
-        on_wall = 1 << 1;
-      }
+      if (!inner_wall && outwards) ir = ir + 1;
     }
+    const double cxd = fma(-b, uxd, x), cyd = fma(-b, uyd, y), czd = fma(-b, uzd, z);
+    cx = (float)cxd; cy = (float)cyd; cz = (float)czd;
+    ux = dd.ux; uy = dd.uy; uz = dd.uz;
+    p2 = (float)(cxd * cxd + cyd * cyd + czd * czd);
+    p = sqrtf(p2);
+    t = (float)b;
 #pragma unroll
     for (int s = 0; s < kSlots; ++s) kap[s] = r.kapd[s];
-    S = PathLen{0.f, 0.f};
     tsum = 0.0;
+    tpart = 0.f;
     tf = 0.f;
-    nstep = 0; nreloc = 0; ntiny = 0;
+    nstep = 0;
+    lo1 = lo2 = hi1 = hi2 = tp = kInf;
+    tr = fmaxf(t, 0.f);
+    up = x * uyd - y * uxd > 0.0;  // z component of x cross u, constant along the line
+    if (!go || ir < 1 || ir > m.nrg - 1) return go;
+    next_sphere(m);
+    if (m.ntg > 2) {
+      cone_roots(m, it - 1, (own >> 3) & 1, lo1, lo2);
+      cone_roots(m, it, (own >> 4) & 1, hi1, hi2);
+      if (m.npg > 2) {
+        const bool mine = up ? ((own >> 6) & 1) : ((own >> 5) & 1);
+        tp = mine ? kInf : plane_root(m, up ? ip : ip - 1);
+      }
+    }
     return go;
   }
-
-  enum { GOING = 0, OUT = 1, ENDED = 2 };  // OUT: left the grid, to be tallied
 
   __device__ __forceinline__ int step(const DevModel& m, int cap, PeelCount& pc) {
     if (nstep > cap || it < 1 || it > m.ntg - 1 || ir < 1 || ir > m.nrg - 1) {
@@ -1427,62 +1552,87 @@ struct PeelWalk {
       return ENDED;
     }
     ++nstep;
-    // the cell's density and peel mask, loaded before the wall search so
+    // the cell's peel-masked densities, loaded before the crossing search so
     // that their latency overlaps it
-    const int64_t c = cidx(m, ir, it, ip);
-    const Rho<float> rho = load_rho<float>(m, c);
-    const unsigned mask = __ldg(m.peelmask + c);
-    float dt;
-    int iface;
-    if (!next_wall_ray<false>(m, ray, S, ir, it, ip, on_wall, dt, iface)) {
-      if (nreloc < 4) {
-        ++nreloc;
-        return relocate_here(m);
-      }
-      pc.stuck++;
-      return ENDED;
-    }
-    float opac = 0.f;
-#pragma unroll
-    for (int s = 0; s < kSlots; ++s)
-      if (mask & (1u << s)) opac += kap[s] * rho.v[s];
-    const float dtau = opac * dt;
-    tsum += (double)dtau;
+    const float4 rho = __ldg(m.rho4p + (ir - 1) + (m.nrg - 1) * ((it - 1) + (m.ntg - 1) * (ip - 1)));
+    const float th = fminf(lo1, hi1);
+    const float tn = fminf(tr, fminf(th, tp));
+    const float ds = tn - t;
+    t = tn;
+    const float opac = fmaf(kap[0], rho.x, fmaf(kap[1], rho.y, fmaf(kap[2], rho.z, kap[3] * rho.w)));
+    const float dtau = opac * ds;
+    tpart += dtau;
     tf += dtau;
     pc.cross++;
     if (tf > (float)kTauMax) return ENDED;
-    step_index(m.npg, iface, ir, it, ip);
-    path_add(S, dt);
-    on_wall = 1 << own_after(iface);
-    if (ir == m.nrg) return OUT;
-    if (ir == 0) return ENDED;
-    if (!tiny_step(m, dt, ir)) {
-      ntiny = 0;
-    } else if (++ntiny > 6 && nreloc < 4) {
-      ++nreloc;
-      ntiny = 0;
-      return relocate_here(m);
+    if (tn == tr) {
+      ir += tr < 0.f ? -1 : 1;
+      if (ir == m.nrg) return OUT;
+      if (ir == 0) return ENDED;
+      next_sphere(m);
+    } else if (tn == th) {
+      if (lo1 <= hi1) {  // the lower polar wall: into cell it - 1
+        hi1 = lo2;
+        hi2 = kInf;
+        --it;
+        if (it < 1) return GOING;  // caught by the range check of the next step
+        cone_roots(m, it - 1, false, lo1, lo2);
+      } else {           // the upper polar wall: into cell it + 1
+        lo1 = hi2;
+        lo2 = kInf;
+        ++it;
+        if (it > m.ntg - 1) return GOING;
+        cone_roots(m, it, false, hi1, hi2);
+      }
+    } else {  // the azimuthal wall, with the wrap at 0 / 2 pi
+      if (up) {
+        ip = ip == m.npg - 1 ? 1 : ip + 1;
+        tp = plane_root(m, ip);
+      } else {
+        ip = ip == 1 ? m.npg - 1 : ip - 1;
+        tp = plane_root(m, ip - 1);
+      }
     }
     return GOING;
   }
 
-  __device__ __forceinline__ int relocate_here(const DevModel& m) {
-    double x, y, z;
-    ray_at(ray, S, x, y, z);
-    int jr = ir, jt = it, jp = ip;  // locals: the walk's fields stay in registers
-    const int where = relocate(m, x, y, z, jr, jt, jp);
-    ir = jr; it = jt; ip = jp;
-    if (where == 1) return OUT;
-    if (where == 2) return ENDED;
-    on_wall = 0;
-    return GOING;
+  // the set-up state of a ray that start() accepted, for a lane to take later
+  __device__ __forceinline__ void save(PeelStart& q, unsigned e, int k) const {
+    q.cx = cx; q.cy = cy; q.cz = cz; q.p = p; q.p2 = p2; q.t = t; q.tr = tr;
+    q.lo1 = lo1; q.lo2 = lo2; q.hi1 = hi1; q.hi2 = hi2; q.tp = tp;
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) q.kap[s] = kap[s];
+    q.irit = ir | (it << 16);
+    q.ipup = ip | ((int)up << 16);
+    q.e = e;
+    q.k = k;
+  }
+
+  __device__ __forceinline__ void load(const PeelStart& q, const PeelDir& dd) {
+    cx = q.cx; cy = q.cy; cz = q.cz; p = q.p; p2 = q.p2; t = q.t; tr = q.tr;
+    lo1 = q.lo1; lo2 = q.lo2; hi1 = q.hi1; hi2 = q.hi2; tp = q.tp;
+#pragma unroll
+    for (int s = 0; s < kSlots; ++s) kap[s] = q.kap[s];
+    ir = q.irit & 0xffff; it = q.irit >> 16;
+    ip = q.ipup & 0xffff; up = (q.ipup >> 16) != 0;
+    ux = dd.ux; uy = dd.uy; uz = dd.uz;
+    tsum = 0.0;
+    tpart = 0.f;
+    tf = 0.f;
+    nstep = 0;
+  }
+
+  // add the FP32 partial escape tau of the last round to the FP64 sum
+  __device__ __forceinline__ void flush_tau() {
+    tsum += (double)tpart;
+    tpart = 0.f;
   }
 
   // FP32 point of the ray where it left the grid
   __device__ __forceinline__ void end_point(float& x, float& y, float& z) const {
-    x = fmaf(S.hi, ray.ux, fmaf(S.lo, ray.ux, ray.x0));
-    y = fmaf(S.hi, ray.uy, fmaf(S.lo, ray.uy, ray.y0));
-    z = fmaf(S.hi, ray.uz, fmaf(S.lo, ray.uz, ray.z0));
+    x = fmaf(t, ux, cx);
+    y = fmaf(t, uy, cy);
+    z = fmaf(t, uz, cz);
   }
 };
 
@@ -1506,7 +1656,9 @@ __device__ __forceinline__ void peel_ray_mixed(const DevModel& m, const DevTalli
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int st;
   while ((st = w.step(m, cap, pc)) == PeelWalk::GOING) {
+    if ((w.nstep & 7) == 0) w.flush_tau();  // the rounds of k_peel_mixed
   }
+  w.flush_tau();
   L.add(HC3D_CNT_PEELS);
   L.add(HC3D_CNT_CROSS_PEEL, pc.cross);
   if (pc.stuck) L.add(HC3D_CNT_PEEL_STUCK, pc.stuck);
@@ -2173,6 +2325,33 @@ __global__ void __launch_bounds__(256, 3) k_peel(DevModel m, DevTallies t, Tally
 }
 
 
+// Set up rays i0 .. i0 + n - 1 (n <= 32) of the warp's staged chunk, one per
+// lane, and push those that are walked onto the warp's stack of set-up rays
+// (buf, nbuf entries so far).  Every lane of the warp calls it, so the
+// set-up -- FP64 closest-approach point and the first crossing of each wall
+// family -- runs with the whole warp instead of the few lanes whose ray
+// ended; not inlined, so the live walk state of the other lanes stays out of
+// its registers.  Returns the number of rays pushed.
+static __device__ __noinline__ int prep_rays(const DevModel& m, const PeelRec<float>* st, unsigned e0,
+                                             const PeelDir* dirs, unsigned npeel, unsigned i0, unsigned n,
+                                             PeelStart* buf, int nbuf) {
+  const int lane = threadIdx.x & 31;
+  bool ok = false;
+  unsigned e = 0;
+  int k = 0;
+  PeelWalk w;
+  if ((unsigned)lane < n) {
+    const unsigned i = i0 + (unsigned)lane;
+    e = i / npeel;
+    k = (int)(i - e * npeel);
+    ok = w.start(m, st[e - e0], dirs[k]);
+  }
+  const unsigned okm = __ballot_sync(0xffffffffu, ok);
+  if (ok) w.save(buf[nbuf + __popc(okm & ((1u << lane) - 1u))], e, k);
+  __syncwarp();
+  return __popc(okm);
+}
+
 template <class R>
 __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                                   const PeelRec<R>* queue,
@@ -2182,6 +2361,7 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
   __shared__ PeelDir dirs[kMaxPeel];
   __shared__ PeelEsc esc[kPeelThreads / 32][kPeelBuf];
   __shared__ PeelRec<float> stage[kPeelThreads / 32][kPeelStage];
+  __shared__ PeelStart prep[kPeelThreads / 32][32];
   static_assert(sizeof(PeelRec<float>) % 4 == 0, "records are staged as 32-bit words");
   for (int k = threadIdx.x; k < a.npeel; k += blockDim.x) dirs[k] = peel_dir(a, k);
   __syncthreads();
@@ -2191,6 +2371,7 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   PeelEsc* buf = esc[warp];
+  PeelStart* pbuf = prep[warp];
   // ray indices of one wave fit 32 bits: at most 2^22 records x 256 directions
   const unsigned npeel = (unsigned)a.npeel;
   const unsigned n = (unsigned)(*qcount) * npeel;
@@ -2201,48 +2382,57 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
   PeelRec<float>* st = stage[warp];
   unsigned e0 = 0;  // first record staged
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
-  int nbuf = 0;
+  int nbuf = 0;     // rays parked for the tally
+  int nprep = 0;    // rays set up and not yet taken (warp-uniform)
   bool have = false, more = n > 0;
-  unsigned rbase = 0, rend = 0;  // rays reserved by this warp, not yet started
+  unsigned rbase = 0, rend = 0;  // rays of the staged chunk not yet set up
   unsigned e = 0;                // the ray of this lane: event e, direction k
   int k = 0;
   PeelWalk w;
   PeelCount pc{0u, 0u, 0u};
   for (;;) {
-    if (more || rbase < rend) {
-      const unsigned need = __ballot_sync(0xffffffffu, !have);
-      if (need) {
-        if (rbase >= rend) {  // reserve the next chunk of rays for this warp
-          unsigned long long b = 0;
-          if (lane == 0) b = atomicAdd(next_ray, (unsigned long long)chunk);
-          b = __shfl_sync(0xffffffffu, b, 0);
-          if (b >= n) {
-            more = false;
-          } else {
-            rbase = (unsigned)b;
-            rend = b + chunk < n ? (unsigned)b + chunk : n;
-            if (rend >= n) more = false;
-            // stage the chunk's records (whole records: chunks are multiples of npeel)
-            e0 = rbase / npeel;
-            const int words = (int)((rend - rbase) / npeel) * (int)(sizeof(PeelRec<float>) / 4);
-            const unsigned* src = reinterpret_cast<const unsigned*>(queue + e0);
-            unsigned* dst = reinterpret_cast<unsigned*>(st);
-            for (int j = lane; j < words; j += 32) dst[j] = __ldg(src + j);
-            __syncwarp();
-          }
+    const unsigned need = __ballot_sync(0xffffffffu, !have);
+    const int nneed = __popc(need);
+    // top up the stack of set-up rays, a warp-wide set-up of up to 32 at a time
+    while (nprep < nneed && (more || rbase < rend)) {
+      if (rbase >= rend) {  // reserve the next chunk of rays for this warp
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(next_ray, (unsigned long long)chunk);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= n) {
+          more = false;
+          break;
         }
-        const unsigned avail = rend - rbase;
-        const unsigned i = rbase + (unsigned)__popc(need & lt);
-        rbase += (unsigned)__popc(need) < avail ? (unsigned)__popc(need) : avail;
-        if (!have && i < rend) {
-          e = i / npeel;
-          k = (int)(i - e * npeel);
-          have = w.start(m, st[e - e0], dirs[k]);
-          if (have) pc.peels++;
-        }
+        rbase = (unsigned)b;
+        rend = b + chunk < n ? (unsigned)b + chunk : n;
+        if (rend >= n) more = false;
+        // stage the chunk's records (whole records: chunks are multiples of npeel)
+        e0 = rbase / npeel;
+        const int words = (int)((rend - rbase) / npeel) * (int)(sizeof(PeelRec<float>) / 4);
+        const unsigned* src = reinterpret_cast<const unsigned*>(queue + e0);
+        unsigned* dst = reinterpret_cast<unsigned*>(st);
+        for (int j = lane; j < words; j += 32) dst[j] = __ldg(src + j);
+        __syncwarp();
+      }
+      const unsigned room = 32u - (unsigned)nprep, avail = rend - rbase;
+      const unsigned take = room < avail ? room : avail;
+      nprep += prep_rays(m, st, e0, dirs, npeel, rbase, take, pbuf, nprep);
+      rbase += take;
+    }
+    if (!have) {  // the lanes without a ray take the top of the stack
+      const int idx = __popc(need & lt);
+      if (idx < nprep) {
+        const PeelStart& q = pbuf[nprep - 1 - idx];
+        e = q.e;
+        k = q.k;
+        w.load(q, dirs[k]);
+        have = true;
+        pc.peels++;
       }
     }
-    const bool idle = !__any_sync(0xffffffffu, have) && !more && rbase >= rend;
+    __syncwarp();
+    nprep -= nneed < nprep ? nneed : nprep;
+    const bool idle = !__any_sync(0xffffffffu, have) && nprep == 0 && !more && rbase >= rend;
     bool out = false;
     if (have) {
       // up to kPeelSub crossings between refills: the warp-wide refill and
@@ -2250,13 +2440,14 @@ __global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevT
       // whose ray ends idling for the rest of the round
 #pragma unroll 1
       for (int sub = 0; sub < kPeelSub; ++sub) {
-        const int st = w.step(m, cap, pc);
-        if (st != PeelWalk::GOING) {
-          out = st == PeelWalk::OUT;
+        const int s = w.step(m, cap, pc);
+        if (s != PeelWalk::GOING) {
+          out = s == PeelWalk::OUT;
           have = false;
           break;
         }
       }
+      w.flush_tau();  // one FP64 add per round of up to kPeelSub crossings
     }
     // park the rays that left the grid; tally them 32 at a time
     const unsigned outm = __ballot_sync(0xffffffffu, out);

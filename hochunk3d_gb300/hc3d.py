@@ -11,7 +11,9 @@ The Python host mirrors the Fortran caller of ``disk()``:
 * :func:`tts` -- the whole program ``tts`` (newtts.F90) in the library.
 
 There is no CPU fallback: every function that computes needs ``libhc3d.so``
-and a CUDA device, and raises :class:`Hc3dError` otherwise.
+and a CUDA device, and raises :class:`Hc3dError` otherwise.  Building a
+model from its .par file needs only ``libhc3d_host.so`` (host code, no
+CUDA), which ``libhc3d.so`` links against.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ import numpy as np
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libhc3d.so"
+HOST_LIB_PATH = PKG / "libhc3d_host.so"
 
 NDG = 8
 NO = 8
@@ -177,6 +180,7 @@ SIGNATURES = {
     "hc3d_load_tables": (C.c_int, [C.c_void_p, P(DustTables)]),
     "hc3d_load_grid": (C.c_int, [C.c_void_p, P(Grid)]),
     "hc3d_zero_tallies": (C.c_int, [C.c_void_p]),
+    "hc3d_set_tdust": (C.c_int, [C.c_void_p, dp]),
     "hc3d_run_iteration": (C.c_int, [C.c_void_p, P(RunParams)]),
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
@@ -213,7 +217,32 @@ SIGNATURES = {
     "hc3d_model_footprint": (C.c_int64, [C.c_void_p]),
 }
 
+# entry points of libhc3d_host.so (the model set-up, no CUDA)
+HOST_SYMBOLS = ("hc3d_model_create", "hc3d_model_destroy", "hc3d_model_views", "hc3d_model_set_tdust",
+                "hc3d_star_packets", "hc3d_write_synthetic_dust", "hc3d_write_wavelength_grid",
+                "hc3d_write_synthetic_isrf")
+
 _LIB = None
+_HOST = None
+
+
+def _bind(L: C.CDLL, names) -> C.CDLL:
+    for name in names:
+        res, args = SIGNATURES[name]
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
+def host_lib() -> C.CDLL:
+    """Load libhc3d_host.so, the host-only model set-up; fail loudly if absent."""
+    global _HOST
+    if _HOST is None:
+        if not HOST_LIB_PATH.exists():
+            raise Hc3dError(-4, f"{HOST_LIB_PATH} is not built; run hochunk3d_gb300.build.build_host_library()")
+        _HOST = _bind(C.CDLL(str(HOST_LIB_PATH)), HOST_SYMBOLS)
+    return _HOST
 
 
 def lib() -> C.CDLL:
@@ -222,12 +251,8 @@ def lib() -> C.CDLL:
     if _LIB is None:
         if not LIB_PATH.exists():
             raise Hc3dError(-4, f"{LIB_PATH} is not built; run hochunk3d_gb300.build.build_library()")
-        L = C.CDLL(str(LIB_PATH))
-        for name, (res, args) in SIGNATURES.items():
-            f = getattr(L, name)
-            f.restype = res
-            f.argtypes = args
-        _LIB = L
+        host_lib()  # the same instance serves libhc3d.so's dependency on it
+        _LIB = _bind(C.CDLL(str(LIB_PATH)), SIGNATURES)
     return _LIB
 
 
@@ -254,7 +279,7 @@ def tally_scales(np_: int) -> tuple[float, float, float]:
 
 def star_packets(isrf_frac: float, np_: int) -> int:
     """Stellar packets of an iteration of np_ packets (hc3d_star_packets)."""
-    return int(lib().hc3d_star_packets(float(isrf_frac), int(np_)))
+    return int(host_lib().hc3d_star_packets(float(isrf_frac), int(np_)))
 
 
 # ---------------------------------------------------------------------------
@@ -267,7 +292,7 @@ class Model:
     """
 
     def __init__(self, par_path: str | os.PathLike, par_dir: str | os.PathLike | None = None):
-        L = lib()
+        L = host_lib()
         h = C.c_void_p()
         err = C.create_string_buffer(1024)
         rc = L.hc3d_model_create(C.byref(h), str(par_path).encode(),
@@ -378,7 +403,7 @@ class Model:
         if rc != 0:
             raise Hc3dError(rc, err.value.decode())
         t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
-        L.hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
+        host_lib().hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
         n4 = g.nrg * g.ntg * g.npg
         self.densarr = _arr(g.densarr, n4 * g.ndg).reshape(self.shape4, order="F")
         self.massarr = _arr(g.massarr, n4 * g.ndg).reshape(self.shape4, order="F")
@@ -396,14 +421,14 @@ class Model:
         if rc != 0:
             raise Hc3dError(rc, err.value.decode())
         t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
-        L.hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
+        host_lib().hc3d_model_views(self._h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
         self.kapBint = _arr(t.kapBint, t.nT * t.nnu * t.ndg)
         self.kappap = _arr(t.kappap, t.nT * t.ndg)
         return ms.value
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().hc3d_model_destroy(self._h)
+            host_lib().hc3d_model_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -446,6 +471,13 @@ class Context:
         self._check(lib().hc3d_reset(self._h))
         self.model = None
         return self
+
+    def set_tdust(self, tdust: np.ndarray) -> None:
+        """Replace the device temperature field (hc3d_set_tdust); (nrg,ntg,npg,ndg), K/11605."""
+        td = np.asfortranarray(tdust, dtype=np.float64)
+        if td.shape != self.model.shape4:
+            raise Hc3dError(-1, f"tdust shape {td.shape} != {self.model.shape4}")
+        self._check(lib().hc3d_set_tdust(self._h, td.ctypes.data_as(dp)))
 
     def zero(self) -> None:
         self._check(lib().hc3d_zero_tallies(self._h))

@@ -209,6 +209,14 @@ int hc3d_load_tables(hc3d_ctx *ctx, const hc3d_dust_tables *tables);
 /* gridset/initarr outputs (gridset.f90:411-1098, initarr.f90:11-56) */
 int hc3d_load_grid(hc3d_ctx *ctx, const hc3d_grid *grid);
 
+/* Replace the dust temperatures of the loaded grid with tdust (nrg,ntg,npg,ndg),
+ * K/11605, Fortran order -- the temperature field initarr copies in before
+ * an iteration (initarr.f90:78-84), e.g. a field read back from an earlier
+ * run.  The sublimation (peel-off) mask follows the new field.  A value of 0
+ * stands for the 0.1 K floor of the starting field; a negative, NaN or
+ * infinite value is rejected (HC3D_ERR_INVALID). */
+int hc3d_set_tdust(hc3d_ctx *ctx, const double *tdust);
+
 /* initarr(.false.) tally reset (initarr.f90:58-89): zero every tally. */
 int hc3d_zero_tallies(hc3d_ctx *ctx);
 

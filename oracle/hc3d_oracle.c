@@ -1301,12 +1301,19 @@ typedef struct mt_job {
   const hc3d_grid *g;
   const hc3d_run_params *rp;
   orc_tallies *t;
-  int64_t b, e;
+  int64_t *next; /* shared: the next packet to claim */
 } mt_job;
 
+/* Each thread claims packets one at a time from a shared counter, so a few
+ * long histories do not leave the other threads idle; the int64 tallies of
+ * the threads sum to the same totals whatever the assignment. */
 static void *mt_main(void *arg) {
   mt_job *j = (mt_job *)arg;
-  orc_run_range(j->dt, j->g, j->rp, j->t, j->b, j->e);
+  for (;;) {
+    const int64_t pid = __atomic_fetch_add(j->next, 1, __ATOMIC_RELAXED);
+    if (pid >= j->rp->np) break;
+    orc_run_range(j->dt, j->g, j->rp, j->t, pid, pid + 1);
+  }
   return NULL;
 }
 
@@ -1317,11 +1324,11 @@ int orc_run_mt(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run_pa
   if (nthreads < 1) nthreads = 1;
   pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
   mt_job *jobs = (mt_job *)calloc((size_t)nthreads, sizeof(mt_job));
+  int64_t next = 0;
   if (!th || !jobs) { free(th); free(jobs); return -3; }
   for (int k = 0; k < nthreads; ++k) {
     jobs[k].dt = dt; jobs[k].g = g; jobs[k].rp = rp; jobs[k].t = &tls[k];
-    jobs[k].b = rp->np * k / nthreads;
-    jobs[k].e = rp->np * (k + 1) / nthreads;
+    jobs[k].next = &next;
     pthread_create(&th[k], NULL, mt_main, &jobs[k]);
   }
   for (int k = 0; k < nthreads; ++k) pthread_join(th[k], NULL);

@@ -53,3 +53,31 @@ def splitmix_uniforms(npkt: int, nu: int, seed: int = 20261203) -> np.ndarray:
         z = z ^ (z >> np.uint64(31))
     u = ((z >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
     return u.reshape(npkt, nu)
+
+
+def make_gray_model(directory: Path, rate: float = 1e-11, np_: int = 100000) -> hc3d.Model:
+    """An optically thin Ulrich envelope (no disk, no cavity) of gray,
+    purely absorbing dust around the 4000 K star of the tiny grid: its Lucy
+    temperatures must be those of radiative equilibrium with the diluted
+    stellar field, T = T* W(r)^(1/4)."""
+    d = Path(directory)
+    configs.write_fixtures(d)
+    lam = 10.0 ** np.linspace(-2.0, 4.0, 241)
+    with open(d / "gray_dust.par", "w") as f:
+        for l in lam:  # lambda, C_ext, C_sca, kappa, g, p_max, (unused): kappa = 100 cm^2/g at every lambda
+            f.write(f" {l:.6e} {1e-20:.6e} {0.0:.6e} {100.0:.6e} {0.0:.6e} {0.0:.6e} {0.0:.6e}\n")
+    over = {f"DUSTNAME({k})": "gray_dust.par" for k in range(1, 9)}
+    over.update({"MASSD": 0.0, "RATE": rate, "CHOLE": "NO", "NP": np_, "NPMIN": np_})
+    return hc3d.Model(configs.write_par(d, "tiny", **over))
+
+
+def dilution_temperature(model: hc3d.Model) -> np.ndarray:
+    """T* <W>^(1/4) per radial cell, <W> the volume mean over the shell of the
+    geometric dilution factor W(r) = (1 - sqrt(1 - (R*/r)^2)) / 2 (r in R*)."""
+    out = []
+    for a, b in zip(model.rarr[:-1], model.rarr[1:]):
+        rr = np.linspace(a, b, 2001)
+        w = 0.5 * (1.0 - np.sqrt(np.clip(1.0 - 1.0 / rr ** 2, 0.0, 1.0)))
+        f, g = w * rr ** 2, rr ** 2  # trapezoid rule on a uniform grid
+        out.append((f.sum() - 0.5 * (f[0] + f[-1])) / (g.sum() - 0.5 * (g[0] + g[-1])))
+    return model.info.tstar_k * np.array(out) ** 0.25

@@ -221,3 +221,26 @@ def test_tfinal_energy_balance(O, model_factory):
 
 
 ORC_HUGE = 1.7976931348623157e308
+
+
+def test_optically_thin_lucy_temperature_is_radiative_equilibrium(tmp_path, built):
+    """Known answer: gray, purely absorbing dust in an optically thin envelope
+    reaches T = T* W(r)^(1/4), W the dilution of the stellar field.  The
+    oracle's Lucy estimator (tfinal, dusttemp.f90:30-50) on 1e5 packets gives
+    it to 1 % in the median cell and 3 % in every cell."""
+    import oracle.oracle as O
+    from tests.helpers import dilution_temperature, make_gray_model
+
+    m = make_gray_model(tmp_path)
+    n = 100000
+    p = m.run_params(np=n, iter=1, ipeel=0)
+    r = O.run(m, p, nthreads=4)
+    c = r["counters"]
+    assert c[4] < 1e-3 * n  # optically thin: almost no packet interacts
+    T = O.tfinal(m, r["dtauabs"] / r["path_scale"], m.info.ltot, n)[..., 2] * 11605.0
+    sel = m.densarr[..., 2] > 0
+    want = np.broadcast_to(dilution_temperature(m)[:, None, None], (m.shape4[0] - 1,) + m.shape4[1:3])
+    got = T[:-1][sel[:-1]]
+    rel = np.abs(got - want[sel[:-1]]) / want[sel[:-1]]
+    assert sel.sum() > 500
+    assert np.median(rel) < 0.01 and rel.max() < 0.03, (np.median(rel), rel.max())
