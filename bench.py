@@ -269,6 +269,30 @@ def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
         c.close()
     out["batched_lucy_pipeline"] = {"seconds": dt, "models_per_hr": n / dt * 3600.0, "packets_per_s": pk / dt,
                                     "peel_threads": slots}
+    # the whole grid as one launch per iteration: both Lucy iterations and
+    # the peeled iteration of every model batched (hc3d_run_batch)
+    t0 = time.perf_counter()
+    models = [hc3d.Model(p) for p in pars]
+    ctxs = [hc3d.Context(hc3d.PREC_MIXED, device=device).load(m) for m in models]
+    pk = 0
+    for it in (1, 2, 3):
+        peel = it == 3
+        ps = [m.run_params(np=int(m.info.np if peel else m.info.np_lucy), iter=it, ipeel=1 if peel else 0)
+              for m in models]
+        for c in ctxs:
+            c.zero()
+        hc3d.run_batch(ctxs, ps)
+        for c, m, p in zip(ctxs, models, ps):
+            if peel:
+                c.tallies(p, grid=False)
+            else:
+                c.lucy_update(m.info.ltot, p.np, want_tdust=False)
+        pk += sum(p.np for p in ps)
+    dt = time.perf_counter() - t0
+    for c in ctxs:
+        c.close()
+    out["batched_pipeline"] = {"seconds": dt, "models_per_hr": n / dt * 3600.0, "packets_per_s": pk / dt,
+                               "launches": 3}
     for k in (slots, 1):
         srv = hc3d.Server(slots=k, device=device)
         t0 = time.perf_counter()

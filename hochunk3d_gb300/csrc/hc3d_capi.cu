@@ -1048,7 +1048,6 @@ extern "C" int hc3d_run_batch(hc3d_ctx* const* ctxs, const hc3d_run_params* para
       return fail(c, HC3D_ERR_INVALID, "batched contexts must share the device and the precision");
     for (int i = 0; i < j; ++i)
       if (ctxs[i] == ctxs[j]) return fail(c, HC3D_ERR_INVALID, "a context appears twice in the batch");
-    if (params[j].ipeel) return fail(c, HC3D_ERR_INVALID, "batched runs are unpeeled (ipeel = 0)");
   }
   CK(cudaSetDevice(c->device));
   std::vector<BatchItem> items((size_t)n);

@@ -917,6 +917,11 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   m->radexp *= m->autors;
   m->pitch = m->pitch * kPi / 180.0;
   if (m->massd == 0.0) {  // reapar.f90:315-326
+    // Switches off the disk's structure options.  The reference does this
+    // before its setup; here it follows the unit scaling above, which reads
+    // none of these flags, so the order gives the same model.  (The other
+    // massd == 0 reset of the reference, the inner radius and the radial
+    // grid of a disk-less model, is the radial grid of gridset below.)
     m->idiskwarp = 0; m->igapd = 0; m->ispiral = 0; m->igappuff = 0; m->irimpuff = 0;
   }
   m->rmax *= m->autors;

@@ -635,8 +635,9 @@ def tts(par_path, out_dir, par_dir=None, precision: int = PREC_MIXED, device: in
 
 
 def run_batch(contexts, params) -> None:
-    """The unpeeled packet loops of several loaded contexts in one persistent
-    launch (hc3d_run_batch); each context's tallies equal a run of its own."""
+    """The packet loops of several loaded contexts in one persistent launch
+    (hc3d_run_batch), unpeeled or peeled; each context's tallies equal a run
+    of its own (bit for bit in the FP64 form)."""
     n = len(contexts)
     hs = (C.c_void_p * n)(*[c._h.value for c in contexts])
     ps = (RunParams * n)(*params)

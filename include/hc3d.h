@@ -239,11 +239,14 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
-/* The unpeeled packet loops of n models (1..256) in one persistent launch:
- * ctxs[j] runs params[j] (ipeel = 0) with its own tables, grid and tallies,
- * and its tallies equal those of hc3d_run_iteration(ctxs[j], &params[j]).
- * All contexts share one device and precision; the launch runs on the
- * stream of ctxs[0].  No counterpart in the reference (one model per run). */
+/* The packet loops of n models (1..256) in one persistent launch: ctxs[j]
+ * runs params[j] with its own tables, grid and tallies.  Peeled runs
+ * (ipeel = 1) walk each event's peel-off rays in the thread that made the
+ * event, with the same walk as the wavefront form, so the tallies equal
+ * those of hc3d_run_iteration(ctxs[j], &params[j]) bit for bit in the FP64
+ * form and within FP32 rounding in the mixed form.  All contexts share one
+ * device and precision; the launch runs on the stream of ctxs[0].  No
+ * counterpart in the reference (one model per run). */
 int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
 
 /* ---- autotuner (no counterpart in the reference) ---------------------------

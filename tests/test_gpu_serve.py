@@ -121,3 +121,33 @@ def test_batched_launch_equals_separate_runs(pars, prec):
             assert np.abs(a - b).sum() <= 1e-3 * np.abs(b).sum() + 2, (k, key)
             assert np.mean(got[key] == want[k][key]) >= 0.99 or key == "counters", (k, key)
         c.close()
+
+
+@pytest.mark.parametrize("prec", [hc3d.PREC_MIXED, hc3d.PREC_FP64])
+def test_batched_peeled_launch_equals_separate_runs(pars, prec):
+    """The peeled iterations of four models in one persistent launch
+    (hc3d_run_batch, peel-off rays walked by the thread of each event) give
+    each model the SED, peeled SED and images of its own wavefront run: bit
+    for bit in the FP64 form, and in the mixed form to 1e-3 of each array's
+    total (the two paths are separately compiled FP32 code)."""
+    models = [hc3d.Model(p) for p in pars]
+    params = [m.run_params(np=4000 + 500 * k, iter=3, ipeel=1) for k, m in enumerate(models)]
+    want = []
+    for m, p in zip(models, params):
+        ctx = hc3d.Context(prec).load(m)
+        ctx.zero(); ctx.run(p)
+        want.append(ctx.tallies(p))
+        ctx.close()
+    ctxs = [hc3d.Context(prec).load(m) for m in models]
+    for c in ctxs:
+        c.zero()
+    hc3d.run_batch(ctxs, params)
+    for k, (c, p) in enumerate(zip(ctxs, params)):
+        got = c.tallies(p)
+        for key in ("si", "sq", "nums", "ti", "tq", "tu", "numt", "image_i", "image_q", "nabs", "dtauabs"):
+            if prec == hc3d.PREC_FP64:
+                np.testing.assert_array_equal(got[key], want[k][key], err_msg=f"model {k} {key}")
+                continue
+            a, b = got[key].astype(np.float64), want[k][key].astype(np.float64)
+            assert np.abs(a - b).sum() <= 1e-3 * np.abs(b).sum() + 16, (k, key)
+        c.close()
