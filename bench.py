@@ -201,13 +201,14 @@ def model_grid_pars(tmp: Path, n: int, np_lo: float, np_hi: float, seed: int):
     return pars
 
 
-def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
+def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4, np_lo: float = 5e4,
+                          np_hi: float = 5e5, one_at_a_time: bool = True):
     """Models per hour of a seeded model grid on the server, with `slots`
     concurrent runs and with one run at a time."""
     from hochunk3d_gb300 import hc3d
 
-    pars = model_grid_pars(tmp / "grid", n, 5e4, 5e5, seed=4)
-    out = {"models": n, "packets_per_model": "log-uniform 5e4..5e5 per iteration",
+    pars = model_grid_pars(tmp / "grid", n, np_lo, np_hi, seed=4)
+    out = {"models": n, "packets_per_model": f"log-uniform {np_lo:.0e}..{np_hi:.0e} per iteration",
            "iterations": "2 Lucy + 1 peeled", "grids": [list(g) for g in GRID_SHAPES]}
     # the Lucy iterations of the grid: one batched launch per iteration for all
     # models (hc3d_run_batch) against one launch per model
@@ -293,7 +294,7 @@ def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
         c.close()
     out["batched_pipeline"] = {"seconds": dt, "models_per_hr": n / dt * 3600.0, "packets_per_s": pk / dt,
                                "launches": 3}
-    for k in (slots, 1):
+    for k in ((slots, 1) if one_at_a_time else (slots,)):
         srv = hc3d.Server(slots=k, device=device)
         t0 = time.perf_counter()
         res = [srv.wait(t) for t in [srv.submit(p) for p in pars]]
@@ -308,46 +309,76 @@ def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4):
 
 
 def serving_latency(tmp: Path, device: int, n: int = 60, rate: float = 20.0, slots: int = 8, np_req: int = 20000):
-    """Poisson arrivals at `rate` requests/s of models of the model-grid
-    distribution, each asking for its SED and three peel-off inclinations
-    (one Lucy iteration of 2e4 packets, a peeled iteration of 2e4 packets):
-    p50/p99 latency from submission to result, against the same requests
-    submitted as one offline batch."""
+    """Requests of models of the model-grid distribution, each asking for its
+    SED and three peel-off inclinations (one Lucy iteration of np_req
+    packets, a peeled iteration of np_req packets).  The same requests are
+    first run as one offline batch, which gives the server's capacity in
+    requests/s; then Poisson arrivals at 0.8 of that capacity (a sustainable
+    load) and at `rate` requests/s give p50/p99 latency from submission to
+    result.  Above capacity the queue grows for as long as requests arrive,
+    so the latency there is mostly waiting."""
     from hochunk3d_gb300 import hc3d
 
     pars = model_grid_pars(tmp / "serve", n, np_req, np_req, seed=5)
     th = np.radians([30.0, 60.0, 85.0])
     req = {"n_lucy": 1, "np_lucy": np_req, "np_": np_req, "thete": th, "phie": np.zeros(3)}
-    rng = np.random.default_rng(6)
-    gaps = rng.exponential(1.0 / rate, n)
     srv = hc3d.Server(slots=slots, device=device)
     srv.wait(srv.submit(pars[0], **req))  # slot warm-up: pools, queues, kernels
-    t0 = time.perf_counter()
-    tickets = []
-    due = 0.0
-    for k in range(n):
-        due += gaps[k]
-        wait = t0 + due - time.perf_counter()
-        if wait > 0:
-            time.sleep(wait)
-        tickets.append(srv.submit(pars[k], **req))
-    res = [srv.wait(t) for t in tickets]
-    span = time.perf_counter() - t0
-    lat = np.array([r["t_done"] - r["t_submit"] for r in res]) * 1000.0
-    svc = np.array([r["t_done"] - r["t_admit"] for r in res]) * 1000.0
-    pk = sum(r["packets"] for r in res)
     t1 = time.perf_counter()
     off = [srv.wait(t) for t in [srv.submit(p, **req) for p in pars]]
     off_dt = time.perf_counter() - t1
+    capacity = n / off_dt
+
+    def poisson(r, seed):
+        gaps = np.random.default_rng(seed).exponential(1.0 / r, n)
+        t0 = time.perf_counter()
+        tickets, due = [], 0.0
+        for k in range(n):
+            due += gaps[k]
+            wait = t0 + due - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            tickets.append(srv.submit(pars[k], **req))
+        res = [srv.wait(t) for t in tickets]
+        span = time.perf_counter() - t0
+        lat = np.array([x["t_done"] - x["t_submit"] for x in res]) * 1000.0
+        svc = np.array([x["t_done"] - x["t_admit"] for x in res]) * 1000.0
+        same = all(np.array_equal(a["si"], b["si"]) and np.array_equal(a["ti"], b["ti"]) for a, b in zip(res, off))
+        return {"rate_per_s": r, "utilisation": r / capacity, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+                "run_p50_ms": float(np.percentile(svc, 50)), "run_p99_ms": float(np.percentile(svc, 99)),
+                "packets_per_s": sum(x["packets"] for x in res) / span, "results_equal_to_offline_batch": bool(same)}
+
+    sustainable = poisson(0.8 * capacity, 7)
+    at_rate = poisson(rate, 6)
     srv.close()
-    same = all(np.array_equal(a["si"], b["si"]) and np.array_equal(a["ti"], b["ti"]) for a, b in zip(res, off))
-    return {"requests": n, "rate_per_s": rate, "slots": slots, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
-            "run_p50_ms": float(np.percentile(svc, 50)), "run_p99_ms": float(np.percentile(svc, 99)),
-            "packets_per_s": pk / span,
-            "offline_batch_packets_per_s": sum(r["packets"] for r in off) / off_dt,
+    return {"requests": n, "slots": slots,
             "request": f"1 Lucy x {np_req:.0e} + peeled {np_req:.0e} packets, SED + 3 inclinations",
-            "results_equal_to_offline_batch": bool(same)}
+            "capacity_requests_per_s": capacity,
+            "offline_batch_packets_per_s": sum(r["packets"] for r in off) / off_dt,
+            "sustainable": sustainable, "at_rate": at_rate,
+            # the keys of a single arrival rate, at the stated rate
+            "rate_per_s": rate, "p50_ms": at_rate["p50_ms"], "p99_ms": at_rate["p99_ms"],
+            "results_equal_to_offline_batch": sustainable["results_equal_to_offline_batch"] and
+            at_rate["results_equal_to_offline_batch"]}
+
+
+def shared_field(model, workload: str):
+    """The temperature field both arms run their timed packets on, and its
+    description: for the full-3D workload the committed azimuthal average of
+    the GPU's two Lucy set-up iterations (tests/golden/make_lucy_field.py),
+    otherwise the analytic warm profile of the tests."""
+    from tests.helpers import warm_tdust
+
+    if workload == "full3d":
+        try:
+            from tests.golden.make_lucy_field import LUCY_PACKETS, field
+
+            return field(model), (f"Lucy field of two set-up iterations x {LUCY_PACKETS} packets, azimuthal average "
+                                  "(tests/golden/full3d_tdust_phiavg.npz)")
+        except (OSError, ValueError):
+            pass
+    return warm_tdust(model), "analytic warm profile, T = 1600 K (r/Rsub)^-0.45"
 
 
 def fp64_comparison(model, td_init, td_lucy, td_sed, device: int, n_sed: int, n_lucy: int) -> dict:
@@ -457,8 +488,8 @@ def fp64_comparison(model, td_init, td_lucy, td_sed, device: int, n_sed: int, n_
 def reference_arm(args):
     """The reference's method on the host cores: the oracle (FP64 C
     restatement) with all threads, on the workload and temperature field of
-    the GPU arm's default steps (the analytic warm profile).  Only the host
-    model set-up (libhc3d_host.so) and the oracle are loaded."""
+    the GPU arm's default steps (shared_field).  Only the host model set-up
+    (libhc3d_host.so) and the oracle are loaded."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
@@ -468,9 +499,8 @@ def reference_arm(args):
         build_host_library()
         build_oracle()
         model = build_model(Path(td), args.workload)
-        from tests.helpers import warm_tdust
-
-        model.set_tdust(warm_tdust(model))
+        td_field, field_desc = shared_field(model, args.workload)
+        model.set_tdust(td_field)
         threads = os.cpu_count() or 1
         n = max(threads * 2, 32)
         dt, _ = run_cpu_oracle(model, n, threads)
@@ -490,7 +520,7 @@ def reference_arm(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
                 "config": {"workload": args.workload, "packets_per_step": n,
-                           "temperatures": "analytic warm profile (the GPU arm's default steps)"},
+                           "temperatures": field_desc + " (the GPU arm's timed steps)"},
                 "cpu_baseline": {"value": v, "unit": "packets/s", "cores": threads, "kind": "port",
                                  "crossings_per_s": cross / sum(times),
                                  "sample": f"{n} packets per step, oracle C restatement with {threads} threads"},
@@ -509,9 +539,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lucy-packets", type=int, default=2_000_000)
     ap.add_argument("--workload", default=WORKLOAD, help="model of configs.CONFIGS (full3d, plain, ...)")
-    ap.add_argument("--temps", default="warm", choices=["warm", "lucy"],
-                    help="temperature field of the timed steps: the analytic warm profile (default; the field "
-                         "of the reference arm) or the field of the two Lucy set-up iterations")
+    ap.add_argument("--temps", default="shared", choices=["shared", "warm", "lucy"],
+                    help="temperature field of the timed steps: the field the reference arm also uses (default; "
+                         "see shared_field), the analytic warm profile, or this run's two Lucy set-up iterations")
     ap.add_argument("--full-iteration", type=int, default=100_000_000,
                     help="packets of the one full peeled iteration timed after the steps (the published run's "
                          "batch: its last long histories are charged once per this many packets); 0 = skip")
@@ -519,6 +549,12 @@ def main():
     ap.add_argument("--fp64-packets", type=int, default=1_000_000,
                     help="packets of the peeled batch that both forms run for the speed-up and the error")
     ap.add_argument("--no-serving", action="store_true", help="skip the model-grid and serving measurements")
+    ap.add_argument("--grid-models", type=int, default=12, help="models of the model-grid measurement")
+    ap.add_argument("--grid-packets", default="5e4,5e5",
+                    help="photon-count range per iteration of the model-grid measurement (the model-grid "
+                         "distribution is 1e6,1e8; the default is scaled down to keep the benchmark to minutes)")
+    ap.add_argument("--grid-only", action="store_true",
+                    help="run only the model-grid measurement (one-off runs at the distribution's photon counts)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default peel-off queue depth")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one untimed peeled step after the Lucy set-up and print its crossing and launch "
@@ -547,6 +583,15 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
+    if args.grid_only:
+        with tempfile.TemporaryDirectory() as td:
+            lo, hi = (float(v) for v in args.grid_packets.split(","))
+            res = model_grid_throughput(Path(td), local, n=args.grid_models, np_lo=lo, np_hi=hi,
+                                        one_at_a_time=hi <= 1e6)
+        if rank == 0:
+            print(json.dumps({"model_grid": res}))
+        return
+
     with tempfile.TemporaryDirectory() as td:
         model = build_model(Path(td), args.workload)
         from tests.helpers import warm_tdust
@@ -554,7 +599,11 @@ def main():
         ctx = hc3d.Context(hc3d.PREC_MIXED, device=local).load(model)
         td_init = model.tdust.copy(order="F")
         td_lucy = warm_up_temperatures(model, ctx, args.lucy_packets)
-        td_steps = warm_tdust(model) if args.temps == "warm" else td_lucy
+        td_shared, shared_desc = shared_field(model, args.workload)
+        td_steps = {"shared": td_shared, "warm": warm_tdust(model), "lucy": td_lucy}[args.temps]
+        steps_desc = {"shared": shared_desc + "; the reference arm's field",
+                      "warm": "analytic warm profile, T = 1600 K (r/Rsub)^-0.45",
+                      "lucy": f"this run's two Lucy set-up iterations x {args.lucy_packets} packets"}[args.temps]
         model.set_tdust(td_steps)
         ctx.set_tdust(td_steps)
         # the peel-off queue depth, chosen by timing a sample batch (untimed set-up)
@@ -665,8 +714,10 @@ def main():
                        "transport_ms": fst[1], "peel_ms": fst[2],
                        "note": "one disk() call: zero, packet loop, tfinal; the temperatures of the timed steps"}
 
-        # the other temperature field, for comparison: two steps on it
-        td_other = td_lucy if args.temps == "warm" else warm_tdust(model)
+        # another temperature field, for comparison: two steps on the analytic
+        # warm profile (hot disk interior: long histories), or on the shared
+        # field when the steps ran on another
+        td_other = warm_tdust(model) if args.temps != "warm" else td_shared
         ot = []
         for s_ in range(2):
             ctx.set_tdust(td_other)
@@ -678,7 +729,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             ot.append(e0.elapsed_time(e1))
-        other = {"temperatures": "two Lucy set-up iterations" if args.temps == "warm" else "analytic warm profile",
+        other = {"temperatures": "analytic warm profile" if args.temps != "warm" else shared_desc,
                  "steps": 2, "ms_per_step": sum(ot) / 2, "packets_per_s": n / (sum(ot) / 2 / 1000.0)}
 
         fp64 = None
@@ -726,7 +777,9 @@ def main():
                        "device_call_ms": tab_call_ms}
         grid_runs = serving = None
         if rank == 0 and not args.no_serving:
-            grid_runs = model_grid_throughput(Path(td), local)
+            lo, hi = (float(v) for v in args.grid_packets.split(","))
+            grid_runs = model_grid_throughput(Path(td), local, n=args.grid_models, np_lo=lo, np_hi=hi,
+                                              one_at_a_time=hi <= 1e6)
             serving = serving_latency(Path(td), local)
         if rank == 0:
             line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
@@ -737,10 +790,8 @@ def main():
                                "peel_directions": int(model.npeel), "image": [int(model._p.nxhst)] * 2 + [4],
                                "nfreq": int(model._p.nfreq), "packets_per_step": n,
                                "l2": "256 MiB buffer written between timed steps",
-                               "temperatures": ("analytic warm profile, T = 1600 K (r/Rsub)^-0.45 (the reference "
-                                                "arm's field)" if args.temps == "warm" else
-                                                f"two Lucy set-up iterations x {args.lucy_packets} packets") +
-                                               "; every step starts from it (restored between steps, untimed)",
+                               "temperatures": steps_desc + "; every step starts from it (restored between "
+                                                            "steps, untimed)",
                                "autotune": tune},
                     "other_temperatures": other, "full_iteration": full_it,
                     "e2e": {"value": e2e, "unit": "packets/s", "h2d_bytes_per_step": int(h2d),

@@ -1,7 +1,9 @@
 // hc3d_gridbuild.cu -- the densities of gridset (gridset.f90:954-1098) on
 // the GPU: disk mass normalisation, per-cell species densities, cell volumes
-// and (rho V)^(1/4), for a model whose walls, parameters and fractal field
-// the host set up.  One thread per (r, theta) column of cells walks the
+// and (rho V)^(1/4), for a model whose walls, parameters, gap scale
+// (rhogap0, gridset.f90:906-942) and fractal field the host set up.  Every
+// disk structure option of densdiskg and the envelope gap are evaluated;
+// a warped or spiral disk per azimuthal cell.  One thread per (r, theta) column of cells walks the
 // azimuthal cells of that column, as the host loop does; the two mass sums
 // are reduced per column and then over columns in a fixed order, so a run
 // repeats bit for bit.
@@ -25,6 +27,14 @@ struct DensParams {
   double rc, rhoe0, rmine, rmax, envexp, rhodens1, rhoamb;
   double c1e, ex1, z01, c2e, ex2, z02, rhoconst1, rhoconst2, exf;
   double r3;  // rmincgs^3
+  // disk structure (densdiskg.f90:25-155) and the envelope gap (densenv.f90:52-58,114-119)
+  int igapd, idiskwarp, nspot, irimcurve, irimpuff, igappuff, igapcurve, ispiral, sn, iradexp;
+  double rgapd1, rgapd2, agap[2], bgap[2], rhogap0[2], z1gap[2];
+  double warpheight, wexp, warplength, rimcurveheight, rimcurvelength, rimcurveexp, rimheight, rimlength;
+  double gapheight, gaplength, gapcurveheight, gapcurvelength, gapcurveexp;
+  double sw, pitch, rspiral1, rspiral2, radexp;
+  int igape, igapedens;
+  double rgape1, rgape2, rhogape, fracte;
 };
 
 // zerod: the Ulrich cubic mu0^3 + (r/Rc - 1) mu0 - (r/Rc) mu = 0, closed form
@@ -50,18 +60,63 @@ __device__ double zerod_dev(double mu, double rx) {
   return fmax(0.0, fmin(1.0, x));
 }
 
-// densdiskg.f90:1-155 for an unwarped, ungapped, unspiralled disk (species 0, 1)
-__device__ double densdisk_dev(const DensParams& P, double rad, double sint, double cost, int id) {
+// densdiskg.f90:1-155 at azimuth phi (species 0, 1): the flared disk with
+// its gap and the gap's density law, warp, spiral arms, puffed and curved
+// rim and gap wall, and radial cutoff -- the algebra of the host build
+// (hc3d_model.cpp densdisk) term by term
+__device__ double densdisk_dev(const DensParams& P, double rad, double sint, double cost, double phi, int id) {
+  const double pi = 3.14159265358979323846;
   const double rp = rad * sint, zp = rad * cost;
   const double rcoord = P.idiskcurve == 1 ? rad : rp;
-  const double zmr = P.z1[id] * pow(rcoord, P.b[id]);
-  if (rcoord > P.rmaxd[id] || P.rho0[id] == 0.0 || rcoord < P.rddust[id] || zmr < 1.e-10) return 0.0;
-  const double gexp = (zp / zmr) * (zp / zmr);
-  if (gexp > 1.e-15) {
-    if (gexp < 120.0) return P.rho0[id] * pow(rcoord, -P.a[id]) * exp(-0.5 * gexp);
-    return 0.0;
+  const bool ingap = P.igapd == 1 && rcoord < P.rgapd2 && rcoord > P.rgapd1;
+  const double adens = ingap ? P.agap[id] : P.a[id], bdens = ingap ? P.bgap[id] : P.b[id];
+  const double rhodens = ingap ? P.rhogap0[id] : P.rho0[id], zscale = ingap ? P.z1gap[id] : P.z1[id];
+  double warp = 0.0, warp2 = 0.0;
+  if (P.idiskwarp == 1) {
+    const double fall = exp(-pow((rcoord - P.rddust[id]) / P.warplength, 2.0));
+    warp = (phi < pi ? 1.0 : -1.0) * P.warpheight * pow(cos(phi / 2.0), P.wexp) * fall;
+    if (P.nspot == 2) warp2 = P.warpheight * pow(cos(phi / 2.0 - pi / 2.0), P.wexp) * fall;
   }
-  return P.rho0[id] * pow(rcoord, -P.a[id]);
+  double rimcurve = 0.0, rimpuff = 0.0, gappuff = 0.0, gapcurve = 0.0;
+  if (P.irimcurve == 1)
+    rimcurve = P.rimcurveheight * exp(-pow((rcoord - P.rddust[id]) / P.rimcurvelength, P.rimcurveexp));
+  if (P.irimpuff == 1) rimpuff = P.rimheight * exp(-pow((rcoord - P.rddust[id]) / P.rimlength, 2.0));
+  if (rcoord < P.rddust[id]) rimpuff = 0.0;
+  if (P.igappuff == 1 && P.igapd == 1) gappuff = P.gapheight * exp(-pow((rcoord - P.rgapd2) / P.gaplength, 2.0));
+  if (rcoord < P.rgapd2) gappuff = 0.0;
+  if (P.igapcurve == 1 && P.igapd == 1)
+    gapcurve = P.gapcurveheight * exp(-pow((rcoord - P.rgapd2) / P.gapcurvelength, P.gapcurveexp));
+  if (rcoord < P.rgapd2) gapcurve = 0.0;
+  double spiral = 1.0;
+  if (P.ispiral == 1) {
+    double sfact = 1.0;
+    for (int is = 2; is <= P.sn; is += 2) sfact = sfact * ((double)is / ((double)is - 1.0));
+    spiral = 1.0 - P.sw + sfact * P.sw * pow(sin(log(rcoord) / tan(P.pitch) - phi + 0.7854), (double)P.sn);
+    if (rcoord < P.rspiral1 || rcoord > P.rspiral2) spiral = 1.0;
+  }
+  double zmr = zscale * pow(rcoord, bdens);
+  double densfact1 = 1.0;
+  if (phi < pi / 2.0 || phi > 3.0 * pi / 2.0) {
+    if (zp > 0.0) zmr = zmr * (1.0 + warp);
+    densfact1 = 1.0 / (1.0 + warp);
+  } else {
+    if (zp < 0.0) zmr = zmr * (1.0 + warp2);
+    densfact1 = 1.0 / (1.0 + warp2);
+  }
+  const double puff = 1.0 + rimpuff + gappuff - rimcurve - gapcurve;
+  const double densfact = 1.0 / puff * densfact1;
+  zmr = zmr * puff;
+  if (rcoord > P.rmaxd[id] || rhodens == 0.0 || rcoord < P.rddust[id] || zmr < 1.e-10) return 0.0;
+  const double gexp = (zp / zmr) * (zp / zmr);
+  double dens;
+  if (gexp > 1.e-15) {
+    if (gexp < 120.0) dens = densfact * spiral * rhodens * pow(rcoord, -adens) * exp(-0.5 * gexp);
+    else dens = 0.0;
+  } else {
+    dens = densfact * spiral * rhodens * pow(rcoord, -adens);
+  }
+  if (P.iradexp == 1) dens = dens * exp(-rcoord / P.radexp);
+  return dens;
 }
 
 // densenv.f90:1-128: Ulrich envelope or power law with a polynomial bipolar
@@ -84,6 +139,9 @@ __device__ double densenv_dev(const DensParams& P, double rad, double costin, do
       dens = P.rhodens1 * pow(rad, -P.envexp);
     }
   }
+  // constant density in the envelope gap, before the ambient floor and the cavity
+  const bool ingape = P.igape == 1 && rad < P.rgape2 && rad > P.rgape1;
+  if (ingape && P.igapedens == 0) dens = P.rhogape;
   if (rad > P.rmine && dens < P.rhoamb) dens = P.rhoamb;
   if (P.ihole == 1 && P.ipoly == 1) {
     const double zlo = P.c2e * pow(rp, P.ex2) + P.z02;
@@ -96,6 +154,7 @@ __device__ double densenv_dev(const DensParams& P, double rad, double costin, do
       dens = P.rhoconst1 * pow(rad, -P.exf);
     }
   }
+  if (ingape && P.igapedens == 1) dens = dens * P.fracte;  // scaled density in the gap
   if (rad >= P.rmax) dens = 0.0;
   if (rad <= P.rmine) dens = 0.0;
   if (id == 3 && inhole == 0) dens = 0.0;
@@ -117,12 +176,16 @@ __global__ void k_disk_colmass(DensParams P, Walls w, double* colmass) {
   const double dr3 = pow(w.rarr[ir + 1], 3.0) - pow(w.rarr[ir], 3.0);
   const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
   const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
+  const bool phidep = P.idiskwarp || P.ispiral;
   for (int id = 0; id < 2; ++id) {
     double m = 0.0;
     if (P.rho0[id] != 0.0) {
-      const double dd = densdisk_dev(P, rad, sint, cost, id);
-      if (dd != 0.0)
-        for (int ip = 0; ip < P.npg - 1; ++ip) m += dd * (-dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3);
+      const double dd0 = phidep ? 0.0 : densdisk_dev(P, rad, sint, cost, 0.0, id);
+      if (phidep || dd0 != 0.0)
+        for (int ip = 0; ip < P.npg - 1; ++ip) {
+          const double dd = phidep ? densdisk_dev(P, rad, sint, cost, 0.5 * (w.phiarr[ip] + w.phiarr[ip + 1]), id) : dd0;
+          m += dd * (-dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3);
+        }
     }
     colmass[(size_t)id * ncol + col] = m;
   }
@@ -159,10 +222,14 @@ __global__ void k_density(DensParams P, Walls w, const double* diskscl, double* 
   const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
   const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
   double dens_r[4];
-  for (int id = 0; id < 2; ++id) dens_r[id] = densdisk_dev(P, rad, sint, cost, id) * diskscl[id];
+  const bool phidep = P.idiskwarp || P.ispiral;
+  for (int id = 0; id < 2; ++id) dens_r[id] = densdisk_dev(P, rad, sint, cost, 0.0, id) * diskscl[id];
   for (int id = 2; id < 4; ++id) dens_r[id] = densenv_dev(P, rad, cost, sint, id) * P.fmass[id];
   double mdisk = 0.0, menv = 0.0;
   for (int ip = 0; ip < P.npg - 1; ++ip) {
+    if (phidep)
+      for (int id = 0; id < 2; ++id)
+        dens_r[id] = densdisk_dev(P, rad, sint, cost, 0.5 * (w.phiarr[ip] + w.phiarr[ip + 1]), id) * diskscl[id];
     const double vol = -dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3;
     const int64_t c = (int64_t)ir + (int64_t)P.nrg * (it + (int64_t)P.ntg * ip);
     vcell[c] = vol;
@@ -199,11 +266,6 @@ struct DevBufs {
 // The densities of gridset on device `device`; replaces m.densarr, massarr,
 // vcell, massdisk, massenv and ndg_active.  ms receives the device time.
 int densities_gpu(Model& m, int device, double* ms, std::string* err) {
-  if (m.disk_structured()) {
-    *err = "the device density build covers the plain flared disk; this model's gap, spiral, warp, rim or "
-           "radial-cutoff options are built on the host";
-    return HC3D_ERR_UNSUPPORTED;
-  }
   if (cudaSetDevice(device) != cudaSuccess) { *err = "no CUDA device"; return HC3D_ERR_CUDA; }
   const int nrg = m.nrg, ntg = m.ntg, npg = m.npg;
   const int ncol = (nrg - 1) * (ntg - 1);
@@ -223,6 +285,20 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   P.rhodens1 = m.rhodens1; P.rhoamb = m.rhoamb;
   P.c1e = m.c1e; P.ex1 = m.ex1; P.z01 = m.z01; P.c2e = m.c2e; P.ex2 = m.ex2; P.z02 = m.z02;
   P.rhoconst1 = m.rhoconst1; P.rhoconst2 = m.rhoconst2; P.exf = m.exf;
+  P.igapd = m.igapd; P.idiskwarp = m.idiskwarp; P.nspot = m.nspot; P.irimcurve = m.irimcurve;
+  P.irimpuff = m.irimpuff; P.igappuff = m.igappuff; P.igapcurve = m.igapcurve; P.ispiral = m.ispiral;
+  P.sn = m.sn; P.iradexp = m.iradexp;
+  P.rgapd1 = m.rgapd1; P.rgapd2 = m.rgapd2;
+  for (int id = 0; id < 2; ++id) {
+    P.agap[id] = m.agap[id]; P.bgap[id] = m.bgap[id]; P.rhogap0[id] = m.rhogap0[id]; P.z1gap[id] = m.z1gap[id];
+  }
+  P.warpheight = m.warpheight; P.wexp = m.wexp; P.warplength = m.warplength;
+  P.rimcurveheight = m.rimcurveheight; P.rimcurvelength = m.rimcurvelength; P.rimcurveexp = m.rimcurveexp;
+  P.rimheight = m.rimheight; P.rimlength = m.rimlength; P.gapheight = m.gapheight; P.gaplength = m.gaplength;
+  P.gapcurveheight = m.gapcurveheight; P.gapcurvelength = m.gapcurvelength; P.gapcurveexp = m.gapcurveexp;
+  P.sw = m.sw; P.pitch = m.pitch; P.rspiral1 = m.rspiral1; P.rspiral2 = m.rspiral2; P.radexp = m.radexp;
+  P.igape = m.igape; P.igapedens = m.igapedens; P.rgape1 = m.rgape1; P.rgape2 = m.rgape2;
+  P.rhogape = m.rhogape; P.fracte = m.fracte;
   const double rmincgs = m.rstar * kRsun;
   P.r3 = std::pow(rmincgs, 3.0);
   DevBufs B;

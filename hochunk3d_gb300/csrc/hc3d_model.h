@@ -91,10 +91,6 @@ struct Model {
   int igape = 0, igapedens = 0;
   double rgape1 = 0, rgape2 = 0, fracte = 1, rhogape = 0;
   bool disk_depends_on_phi() const { return idiskwarp || ispiral; }
-  // density options the host build covers and the device build does not
-  bool disk_structured() const {
-    return igapd || ispiral || idiskwarp || irimpuff || igappuff || irimcurve || igapcurve || iradexp || igape;
-  }
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;
   int image = 1;

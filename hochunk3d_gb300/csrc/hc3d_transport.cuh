@@ -1452,14 +1452,14 @@ struct PeelWalk {
     r1 = r2 = kInf;
     const float2 cw = __ldg(m.conec + w);
     const float C = cw.x, hemi = cw.y;
-    if (hemi == 0.f) return;  // a pole: no crossing
-    if (C < 0.f) {            // the midplane z = 0
+    if (C < 0.f) {  // the midplane z = 0
       if (!own && uz != 0.f) {
         const float r = __fdividef(-cz, uz);
         if (r >= t) r1 = r;
       }
       return;
     }
+    if (hemi == 0.f) return;  // a pole: no crossing
     const float a = fmaf(-uz, uz, C);
     const float h = -cz * uz;
     const float q = fmaf(C, p2, -cz * cz);
@@ -2352,8 +2352,11 @@ static __device__ __noinline__ int prep_rays(const DevModel& m, const PeelRec<fl
   return __popc(okm);
 }
 
+// Two blocks per SM: the walk state of a lane, the set-up stack and the
+// 32-ray tally need about 114 registers; at three blocks (80 registers) the
+// compiler kept part of the walk state in local memory inside the loop.
 template <class R>
-__global__ void __launch_bounds__(kPeelThreads, 3) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+__global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                                   const PeelRec<R>* queue,
                                                                   const unsigned long long* qcount,
                                                                   unsigned long long* next_ray) {

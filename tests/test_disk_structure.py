@@ -102,13 +102,6 @@ def test_puffed_rim_thickens_the_inner_disk(tmp_path, built):
     assert (col_q * w).sum() / col_q.sum() > (col_p * w).sum() / col_p.sum()
 
 
-def test_device_density_build_leaves_structured_disks_to_the_host(tmp_path, built):
-    m = _model(tmp_path, "gapdev", CGAPD="YES", RGAPD1=3.0, RGAPD2=5.0)
-    with pytest.raises(hc3d.Hc3dError) as e:
-        m.densities_gpu(0)
-    assert e.value.code == -7
-
-
 @pytest.mark.parametrize("mode", ["CONST", "SCALE"])
 def test_envelope_gap(tmp_path, built, mode):
     """CGAPE (densenv.f90:52-58,114-119): the envelope between RGAPE1 and

@@ -32,6 +32,40 @@ def test_device_densities_match_host(tmp_path, built, name):
     np.testing.assert_array_equal(m.densarr, d1)
 
 
+STRUCTURED = {
+    "gap": {"CGAPD": "YES", "RGAPD1": 3.0, "RGAPD2": 5.0, "RHOSCALE_GAP(1)": 0.1, "RHOSCALE_GAP(2)": 0.1},
+    "gap_puff_curve": {"CGAPD": "YES", "RGAPD1": 3.0, "RGAPD2": 5.0, "CGAPPUFF": "YES", "GAPHEIGHT": 0.5,
+                       "GAPLENGTH": 2.0, "CGAPCURVE": "YES", "GAPCURVEHEIGHT": 0.3, "GAPCURVELENGTH": 3.0,
+                       "GAPCURVEEXP": 1.2},
+    "rim": {"CRIMPUFF": "YES", "RIMHEIGHT": 1.0, "RIMLENGTH": 0.5, "CRIMCURVE": "YES", "RIMCURVEHEIGHT": 0.3,
+            "RIMCURVELENGTH": 0.8, "RIMCURVEEXP": 1.0},
+    "cutoff": {"CRADEXP": "YES", "RADEXP": 20.0},
+    "spiral": {"NPG": 17, "CSPIRAL": "YES", "PITCH": 15.0, "SN": 4, "SW": 0.5, "RSPIRAL1": 2.0, "RSPIRAL2": 50.0},
+    "warp": {"NPG": 9, "CDISKWARP": "YES", "WARPHEIGHT": 1.0, "WEXP": 41.0, "WARPLENGTH": 5.0},
+    "envelope_gap": {"RATE": 5e-6, "CGAPE": "YES", "RGAPE1": 20.0, "RGAPE2": 60.0, "CGAPEDENS": "SCALE",
+                     "FRACTE": 0.01},
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("option", sorted(STRUCTURED))
+def test_device_densities_of_structured_disks_match_host(tmp_path, built, option):
+    """The disk structure of densdiskg (gap with its own density law, puffed
+    and curved rim and gap wall, radial cutoff, spiral arms, warp) and the
+    envelope gap on the GPU: the host build of the same model to 1e-12."""
+    over = {"NRG": 60, "NTG": 41, "NPG": 2, "MASSD": 0.01, "RATE": 1e-9}
+    over.update(STRUCTURED[option])
+    m = make_model(tmp_path / option, "tiny", warm=False, **over)
+    dens, mass = m.densarr.copy(), m.massarr.copy()
+    mdisk, menv = m.info.massdisk, m.info.massenv
+    m.densities_gpu(0)
+    np.testing.assert_array_equal(m.densarr == 0.0, dens == 0.0)
+    np.testing.assert_allclose(m.densarr, dens, rtol=1e-12, atol=0.0)
+    np.testing.assert_allclose(m.massarr, mass, rtol=1e-12, atol=0.0)
+    assert m.info.massdisk == pytest.approx(mdisk, rel=1e-12)
+    assert m.info.massenv == pytest.approx(menv, rel=1e-12)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["tiny", "plain"])
 def test_device_tables_match_host(tmp_path, built, name):
