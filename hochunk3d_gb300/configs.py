@@ -23,6 +23,10 @@ Models:
   tiny3d  -- a small 3-D grid (with azimuthal walls) for CPU parity tests.
   tiny_isrf -- tiny with external illumination (COUTILLUM=YES, a synthetic
              field of three diluted blackbodies, ISRF_SCL 10).
+  tiny_acc -- tiny with disk accretion (CDISKACC=YES, Mdot 3e-7 Msun/yr,
+             magnetospheric truncation at 5 R*), two hot spots at latitude
+             60 deg covering 5 % of the star, and a gap between 0.1 and
+             0.2 AU where the accretion packets are emitted by the gas.
 """
 from __future__ import annotations
 
@@ -108,6 +112,10 @@ CONFIGS = {
     # about 40 % of the luminosity
     "tiny_isrf": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 2, "NXIMG": 31,
                   "MASSD": 0.0001, "RATE": 5e-7, "COUTILLUM": "YES", "ISRF_SCL": 10.0, "ISRF_FILE": ISRF_FILE},
+    "tiny_acc": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 2, "NXIMG": 31,
+                 "MASSD": 0.001, "RATE": 5e-7, "CDISKACC": "YES", "CALPHA": "NO", "ALPHA/MDOT": 3e-7, "RTRUNC": 5.0,
+                 "CSPOT": "YES", "SPOTLAT": 60.0, "NSPOT": 2, "CTEMP": "NO", "TSPOT/FSPOT": 0.05,
+                 "CGAPD": "YES", "RGAPD1": 0.1, "RGAPD2": 0.2, "RHOSCALE_GAP(1)": 0.0, "RHOSCALE_GAP(2)": 0.0},
     "tiny3d": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 9, "NXIMG": 31,
                "MASSD": 0.0001, "RATE": 5e-7, "NPEEL": 4, "THETE": "30.013,60.013,80.013,120.013",
                "PHIE": "0.0,90.0,180.0,270.0", "CFRACTAL": "YES", "FRACTLEV": 2, "FRACTN": 8},

@@ -61,6 +61,7 @@ struct hc3d_ctx {
   int64_t pool_threads = 0, qcap = 0;
   int wave_blocks = 0, peel_blocks = 0;
   int64_t queue_records = 1 << 22;  // peel-off events held per wave
+  int regen = 1;                    // k_wave regeneration threshold (lanes of a warp)
   bool use_waves = true;            // peeled runs use the wavefront form
 };
 
@@ -298,6 +299,30 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
     if (p->n_star < 0) return fail(c, HC3D_ERR_INVALID, "n_star < 0");
   }
   a->limb = p->limb;
+  a->regen = c->regen;
+  // disk accretion and hot-spot packets
+  a->n_acc = 0;
+  a->n_spot = 0;
+  a->src_on = 0;
+  if (p->sources) {
+    const hc3d_sources& S = *p->sources;
+    if (p->n_acc < 0 || p->n_spot < p->n_acc) return fail(c, HC3D_ERR_INVALID, "need 0 <= n_acc <= n_spot");
+    if (p->n_acc > 0 && !(S.rddustmin > 0.0 && S.rddustmin < S.rmaxdmax && S.rmax > 0.0 && S.gas_den > 0.0 &&
+                          S.rstar > 0.0 && S.rsun > 0.0))
+      return fail(c, HC3D_ERR_INVALID, "accretion packets need 0 < rddustmin < rmaxdmax, rmax, gas_den, rstar, rsun > 0");
+    if (p->n_spot > p->n_acc && !(S.tshock > 0.0))
+      return fail(c, HC3D_ERR_INVALID, "hot-spot packets need tshock > 0");
+    if (S.ispot && ((S.nspot != 1 && S.nspot != 2) || !(S.csprad >= -1.0 && S.csprad <= 1.0)))
+      return fail(c, HC3D_ERR_INVALID, "spots need nspot 1 or 2 and -1 <= csprad <= 1");
+    if (S.ispot && S.fspot < 1.0 && S.csprad < 1.0 && !(S.tshock > 0.0))
+      return fail(c, HC3D_ERR_INVALID, "stellar packets that fall in a spot need tshock > 0");
+    a->src = S;
+    a->src_on = 1;
+    a->n_acc = p->n_acc;
+    a->n_spot = p->n_spot;
+  } else if (p->n_acc || p->n_spot) {
+    return fail(c, HC3D_ERR_INVALID, "n_acc and n_spot need sources");
+  }
   a->ext_illum = p->ext_illum ? 1 : 0;
   a->n_star = p->n_star;
   a->rmax = p->rmax;
@@ -691,6 +716,18 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
       return r;
     c->dm.nisrf = t->nisrf; c->dm.isrf_cdf = d_ic; c->dm.isrf_logcdf = d_il; c->dm.isrf_logfreq = d_if;
   }
+  // partial sums of the blackbody sampler (zetainit, random.f90:79-97): inczeta(i) = sum_{j<=i} 1/j^4,
+  // accumulated from j = izmax down to 1 as the reference does
+  {
+    std::vector<double> z(kIzmax, 0.0);
+    for (int j = kIzmax; j >= 1; --j) {
+      const double term = 1.0 / (double)(j * j * j * j);
+      for (int i = kIzmax; i >= j; --i) z[i - 1] = z[i - 1] + term;
+    }
+    double* d_z;
+    if ((r = dupload(c, own, &d_z, z.data(), z.size()))) return r;
+    c->dm.inczeta = d_z;
+  }
   // limb-darkening table (tabl_mod)
   c->dm.nlimb = 0;
   if (t->ntab > 0) {
@@ -854,11 +891,12 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       }
   std::vector<void*>& own = c->grid_allocs;
   int r;
-  double *d_r, *d_r2, *d_th, *d_ph, *d_t2, *d_a, *d_b, *d_rd;
+  double *d_r, *d_r2, *d_th, *d_ct, *d_ph, *d_t2, *d_a, *d_b, *d_rd;
   float *d_t2f, *d_hemi, *d_af, *d_bf;
   float4* d_rf;
   if ((r = dupload(c, own, &d_r, g->rarr, (size_t)nrg)) || (r = dupload(c, own, &d_r2, g->r2arr, (size_t)nrg)) ||
-      (r = dupload(c, own, &d_th, g->thetarr, (size_t)ntg)) || (r = dupload(c, own, &d_ph, g->phiarr, (size_t)npg)) ||
+      (r = dupload(c, own, &d_th, g->thetarr, (size_t)ntg)) || (r = dupload(c, own, &d_ct, g->costarr, (size_t)ntg)) ||
+      (r = dupload(c, own, &d_ph, g->phiarr, (size_t)npg)) ||
       (r = dupload(c, own, &d_t2, g->tan2arr, (size_t)ntg)) || (r = dupload(c, own, &d_a, g->aarr, (size_t)npg)) ||
       (r = dupload(c, own, &d_b, g->barr, (size_t)npg)) || (r = dupload(c, own, &d_t2f, tan2f.data(), tan2f.size())) ||
       (r = dupload(c, own, &d_hemi, hemi.data(), hemi.size())) || (r = dupload(c, own, &d_af, af.data(), af.size())) ||
@@ -878,7 +916,7 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
     return r;
   DevModel& m = c->dm;
   m.nrg = nrg; m.ntg = ntg; m.npg = npg; m.ncell = ncell;
-  m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
+  m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.costarr = d_ct; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
   {
     std::vector<float> rf32(g->rarr, g->rarr + nrg), r2f32(g->r2arr, g->r2arr + nrg);
     float *d_rarrf = nullptr, *d_r2arrf = nullptr;
@@ -1120,43 +1158,58 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
   if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
   std::memset(out, 0, sizeof *out);
   const bool waves = sample->ipeel && c->use_waves;
-  const int64_t queues[4] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
-  const int blocks[3] = {64, 96, 128};
-  const int n = waves ? 4 : 3;
   const int64_t q0 = c->queue_records;
-  const int b0 = c->block_size;
-  double best = 1e300;
-  for (int k = 0; k < n; ++k) {
-    if (waves) {
-      drop_wave(c);  // reallocated by the next run at the new depth
-      c->queue_records = queues[k];
-    } else {
-      c->block_size = blocks[k];
-    }
+  const int b0 = c->block_size, g0 = c->regen;
+  // time the sample under the context's current settings as candidate k
+  auto time_one = [&](int k) -> int {
     int r = hc3d_zero_tallies(c);
     const auto t0 = std::chrono::steady_clock::now();
     if (!r) r = hc3d_run_iteration(c, sample);
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (r) {
+      if (c->queue_records != q0) drop_wave(c);
       c->queue_records = q0;
       c->block_size = b0;
+      c->regen = g0;
       return r;
     }
     out->queue_records[k] = c->queue_records;
     out->block_size[k] = c->block_size;
+    out->regen[k] = c->regen;
     out->ms[k] = ms;
-    if (ms < best) {
-      best = ms;
-      out->best = k;
-    }
-  }
-  out->n = n;
+    if (k == 0 || ms < out->ms[out->best]) out->best = k;
+    return HC3D_OK;
+  };
+  int n = 0, r;
   if (waves) {
-    if (c->queue_records != out->queue_records[out->best]) drop_wave(c);
-    c->queue_records = out->queue_records[out->best];
+    // the queue depth at the current threshold, then the threshold at the best depth
+    const int64_t queues[4] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+    for (int k = 0; k < 4; ++k, ++n) {
+      if (c->queue_records != queues[k]) {
+        drop_wave(c);  // reallocated by the next run at the new depth
+        c->queue_records = queues[k];
+      }
+      if ((r = time_one(n))) return r;
+    }
+    const int64_t qbest = out->queue_records[out->best];
+    if (c->queue_records != qbest) drop_wave(c);
+    c->queue_records = qbest;
+    const int regens[4] = {1, 4, 8, 16};
+    for (int k = 0; k < 4; ++k) {
+      if (regens[k] == out->regen[out->best]) continue;  // timed above
+      c->regen = regens[k];
+      if ((r = time_one(n++))) return r;
+    }
+    c->regen = out->regen[out->best];
   } else {
+    const int blocks[3] = {64, 96, 128};
+    for (int k = 0; k < 3; ++k, ++n) {
+      c->block_size = blocks[k];
+      if ((r = time_one(n))) return r;
+    }
     c->block_size = out->block_size[out->best];
   }
+  out->n = n;
   return hc3d_zero_tallies(c);
 }
 

@@ -15,6 +15,7 @@ constexpr int kMaxPeel = 256;
 constexpr int kFaultLog = 256;
 constexpr int kGuide = 64;      // probability levels of the Lucy-CDF guide table
 constexpr int kDustGuide = 64;  // ln(nu) buckets of the dust-table guide
+constexpr int kIzmax = 145;     // terms of the blackbody sampler's mixture (random.f90:17)
 
 // Fortran-layout sizes of the tally arrays of one run configuration.
 struct TallyDims {
@@ -51,6 +52,7 @@ struct DevModel {
   const float* r2arrf;    // (nrg) squares of rarr rounded to FP32
   const double* r2arr;    // (nrg)
   const double* thetarr;  // (ntg)
+  const double* costarr;  // (ntg) cos of the polar walls (accretion packets locate their cell by it)
   const double* phiarr;   // (npg)
   const double* tan2d;    // (ntg)
   const float* tan2f;     // (ntg)
@@ -85,6 +87,7 @@ struct DevModel {
   const double* hnuint; const double* atmosnu; const double* lognu; const double* loghnu;
   int nisrf;  // external radiation field (isrf_mod): cdf_i, logcdf_i, logfreq_i; 0 = none
   const double* isrf_cdf; const double* isrf_logcdf; const double* isrf_logfreq;
+  const double* inczeta;   // (kIzmax) partial sums of 1/i^4 of bbfreq (random.f90:79-97)
   int nlimb;  // rows of the limb-darkening table (tabl_mod ntab), CLIMB=YES; 0 = none
   const double* limb_xmu; const double* limb_prob;
   // FP32 copies of the per-event tables, read by the mixed form
@@ -118,6 +121,10 @@ struct RunArgs {
   int ext_illum;             // packets with global id >= n_star enter from the outer sphere
   int64_t n_star;
   double rmax;               // outer radius, R*
+  int64_t n_acc, n_spot;     // ids < n_acc: disk accretion; [n_acc, n_spot): hot spot
+  int src_on;                // 1: src holds the accretion and spot constants
+  int regen;                 // k_wave regeneration threshold: waiting lanes of a warp before they take new packets
+  hc3d_sources src;
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
   const double* aperture2;   // [nap]
   unsigned long long* work;  // packet counter

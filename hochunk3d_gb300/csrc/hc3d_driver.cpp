@@ -376,7 +376,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   while (!converge) {
     ++iter;
     p.np = m.np_lucy;
-    p.n_star = hc3d_star_packets(m.isrf_frac, p.np);
+    m.set_shares(&p, p.np);
     p.ipeel = 0;
     p.iter = iter;
     if ((r = hc3d_zero_tallies(ctx)) || (r = hc3d_run_iteration(ctx, &p))) return bail(r);
@@ -396,7 +396,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
   // final iteration (newtts.F90:333-368)
   ++iter;
   p.np = m.np;
-  p.n_star = hc3d_star_packets(m.isrf_frac, p.np);
+  m.set_shares(&p, p.np);
   p.ipeel = ipeelorig;
   p.iter = iter;
   Tallies T;

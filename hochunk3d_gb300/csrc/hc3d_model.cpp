@@ -709,18 +709,44 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   REQ(P.real("RSTAR", &m->rstar, err));
   REQ(P.real("TSTAR", &m->tstar_k, err));
   REQ(P.real("MASSC", &m->massc, err));
-  REQ(P.integer("CSPOT", &iv, err));
-  if (iv != 0) { *err = "CSPOT=YES (stellar hotspots) is not supported"; return false; }
+  // hot spots (reapar.f90:288-305); the spot radius and temperature follow from the accretion shock in gridset
+  // (reapar reads these keys whether or not CSPOT is set; the shock of CDISKACC uses NSPOT, CTEMP and
+  // TSPOT/FSPOT without spots too)
+  REQ(P.integer("CSPOT", &iv, err)); m->ispot = (int)iv;
+  if (P.has("SPOTLAT")) REQ(P.real("SPOTLAT", &m->spotlat, err));
+  if (P.has("NSPOT")) { REQ(P.integer("NSPOT", &iv, err)); m->nspot = (int)iv; }
+  if (P.has("CTEMP")) { REQ(P.integer("CTEMP", &iv, err)); m->itemp = (int)iv; }
+  if (P.has("TSPOT/FSPOT")) REQ(P.real("TSPOT/FSPOT", m->itemp ? &m->tspot : &m->fspot, err));
+  if (!m->ispot) m->fspot = 1.0;  // reapar.f90:302-305
   REQ(P.real("MASSD", &m->massd, err));
   REQ(P.str("CRMIN", &sv, err));
-  int irminsub = sv == "RSTAR" ? 0 : sv == "RSUB" ? 1 : sv == "AU" ? 2 : -1;
+  const int irminsub = sv == "RSTAR" ? 0 : sv == "RSUB" ? 1 : sv == "AU" ? 2 : -1;
   if (irminsub < 0) { *err = "CRMIN should be one of RSTAR/RSUB/AU"; return false; }
+  m->irminsub = irminsub;
   std::string czmin;
   REQ(P.str("CZMIN", &czmin, err));
   double fmassd1;
   REQ(P.real("FMASSD1", &fmassd1, err));
   if (P.has("CDISKCURV")) { REQ(P.str("CDISKCURV", &sv, err)); m->idiskcurve = sv == "SPH" ? 1 : 0; }
-  const char* off_keys[] = {"CHSEQ", "CMISALIGN", "CDISKACC", "DIFFUSION", "DENSINPUT"};
+  // disk accretion (reapar.f90:275-284); RTRUNC is read whether or not it is used
+  if (P.has("CDISKACC")) { REQ(P.integer("CDISKACC", &iv, err)); m->idiskacc = (int)iv; }
+  if (m->idiskacc) {
+    REQ(P.integer("CALPHA", &iv, err)); m->ialpha = (int)iv;
+    REQ(P.real("ALPHA/MDOT", m->ialpha ? &m->alphad : &m->mdotdisk, err));
+  }
+  if (P.has("RTRUNC")) REQ(P.real("RTRUNC", &m->rtrunc, err));
+  if (m->ispot && !m->idiskacc) {
+    // the spot temperature exists only through the accretion shock luminosity (gridset.f90:169-178):
+    // the reference would emit the spot's packets at T = 0
+    *err = "CSPOT=YES needs CDISKACC=YES: the hot-spot temperature comes from the accretion shock";
+    return false;
+  }
+  if (m->idiskacc && m->nspot != 1 && m->nspot != 2) { *err = "NSPOT must be 1 or 2"; return false; }
+  if (m->idiskacc && m->itemp == 0 && m->fspot == 0.0) {
+    *err = "ERROR: fspot=0 and CDISKACC=yes - 0 area hotspot is a singularity";  // reapar.f90:307-311
+    return false;
+  }
+  const char* off_keys[] = {"CHSEQ", "CMISALIGN", "DIFFUSION", "DENSINPUT"};
   for (const char* k : off_keys) {
     if (P.has(k)) {
       REQ(P.integer(k, &iv, err));
@@ -766,7 +792,6 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
     REQ(P.real("WARPHEIGHT", &m->warpheight, err));
     REQ(P.real("WEXP", &m->wexp, err));
     REQ(P.real("WARPLENGTH", &m->warplength, err));
-    if (P.has("NSPOT")) { REQ(P.integer("NSPOT", &iv, err)); m->nspot = (int)iv; }
   }
   if (m->irimpuff) { REQ(P.real("RIMHEIGHT", &m->rimheight, err)); REQ(P.real("RIMLENGTH", &m->rimlength, err)); }
   if (m->igappuff) { REQ(P.real("GAPHEIGHT", &m->gapheight, err)); REQ(P.real("GAPLENGTH", &m->gaplength, err)); }
@@ -812,10 +837,11 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   for (int k = 0; k < 4; ++k)
     if (fsg[k] != 0.0) { *err = "FSG > 0 (small-grain emission) is not supported"; return false; }
   m->fmass[0] = fmassd1; m->fmass[1] = 1.0 - fmassd1; m->fmass[2] = 1.0; m->fmass[3] = 1.0;
-  for (int d = 0; d < 2; ++d) m->rddust[d] = rmind_in[d];
+  for (int d = 0; d < 2; ++d) m->rddust[d] = m->rmind_in[d] = rmind_in[d];
   REQ(P.real("RMAX", &m->rmax, err));
   double rmine_in;
   REQ(P.real("RMINE", &rmine_in, err));
+  m->rmine_in = rmine_in;
   REQ(P.str("ENVTYPE", &sv, err));
   m->ienvtype = sv == "ULRICH" ? 1 : sv == "POWLAW" ? 0 : -1;
   if (m->ienvtype < 0) { *err = "ERROR: ENVTYPE should be set to ULRICH or POWLAW"; return false; }
@@ -923,6 +949,12 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
     // massd == 0 reset of the reference, the inner radius and the radial
     // grid of a disk-less model, is the radial grid of gridset below.)
     m->idiskwarp = 0; m->igapd = 0; m->ispiral = 0; m->igappuff = 0; m->irimpuff = 0;
+    m->idiskacc = 0;
+    if (m->ispot) {
+      *err = "CSPOT=YES needs a disk (MASSD > 0) with CDISKACC=YES: the hot-spot temperature comes from the "
+             "accretion shock";
+      return false;
+    }
   }
   m->rmax *= m->autors;
   for (int d = 0; d < 2; ++d) m->rmaxd[d] *= m->autors;
@@ -991,6 +1023,126 @@ static void setup_rho0(Model* m) {
       m->rho0[id] = 0.0;
     }
   }
+}
+
+// The luminosities of gridset.f90:72-290: the star, the external field
+// (newtts.F90:207, rmax in stellar radii) and, with CDISKACC, the accretion
+// luminosity of the disk (lacc) and of the shock on the star (lacc2), the
+// hot-spot size and temperature, the mean stellar temperature tave and the
+// sublimation radius it sets, and the constants of the accretion and spot
+// sources (spotset.f90:179-206).  Runs after setup_rho0 (the accretion rate
+// of CALPHA=YES scales with the disk's rho0) and before the grid walls, which
+// the new sublimation radius moves.
+static bool luminosities(Model* m, std::string* err) {
+  const double rmincgs = m->rstar * kRsun;
+  const double yr = 3600.0 * 24.0 * 365.25;
+  const double deg2rad = kPi / 180.0, rad2deg = 180.0 / kPi;
+  m->lstar = 4.0 * kPi * kSigt * std::pow(m->tstar_k, 4.0) * rmincgs * rmincgs;
+  m->l_isrf = m->iout ? m->isrf_int * 4.0 * kPi * std::pow(m->rmax * kRsun * m->rstar, 2.0) / 4.0 * m->isrf_scl : 0.0;
+  m->mdotcgs[0] = m->mdotcgs[1] = 0.0;
+  m->lacc = m->lacc2 = 0.0;
+  m->tshock_k = 0.0;
+  m->thspot_deg = 0.0;
+  if (m->idiskacc) {
+    const double vc = std::sqrt(kGn * kMsun * m->massc / rmincgs);
+    if (m->ialpha) {
+      // eqs. 5 and 6 of Whitney et al. 2003 (ApJ 591, 1049) for each disk slot
+      double mdot = 0.0;
+      for (int id = 0; id < 2; ++id) {
+        m->mdotcgs[id] = std::sqrt(18.0 * std::pow(kPi, 3.0)) * m->alphad * vc * m->rho0[id] *
+                         std::pow(m->z1[id] * rmincgs, 3.0) / rmincgs;
+        mdot += m->mdotcgs[id];
+      }
+      m->mdotdisk = mdot * yr / kMsun;
+    } else {
+      // the total rate split between the slots as rho0 z1^3 (IEEE: all to slot 1 when slot 2 is empty)
+      const double mdottot = m->mdotdisk / (yr / kMsun);
+      const double z1a = m->z1[0] * m->z1[0] * m->z1[0], z1b = m->z1[1] * m->z1[1] * m->z1[1];
+      const double ratio = m->rho0[0] * z1a / m->rho0[1] / z1b;
+      m->mdotcgs[1] = mdottot / (1.0 + ratio);
+      m->mdotcgs[0] = mdottot - m->mdotcgs[1];
+    }
+    m->mdot_cgs = m->mdotcgs[0] + m->mdotcgs[1];
+    m->mdotdisk = m->mdot_cgs * yr / kMsun;
+    m->lacc = kGn * (kMsun * m->massc) * m->mdot_cgs / 2.0 / (m->rddustmin * rmincgs);
+    if (m->massd > 0.0) m->lacc2 = kGn * (kMsun * m->massc) * m->mdot_cgs * (1.0 / rmincgs - 1.0 / (rmincgs * m->rtrunc));
+    else m->lacc = 0.0;
+  }
+  m->ltot = m->lacc + m->lacc2 + m->lstar + m->l_isrf;
+  m->accfrac = m->lacc / m->ltot;
+  m->accfrac2 = m->lacc2 / m->ltot;
+  m->isrf_frac = m->l_isrf / m->ltot;
+  if (m->idiskacc && m->lacc2 > 0.0) {
+    double fluxratio;
+    if (m->itemp == 0) {
+      fluxratio = 0.5 * m->lacc2 / m->lstar / m->fspot;
+      m->tshock_k = m->tstar_k * std::pow(1.0 + fluxratio, 0.25);
+      m->tspot = m->tshock_k;
+    } else {
+      m->tshock_k = m->tspot;
+      fluxratio = std::pow(m->tshock_k / m->tstar_k, 4.0) - 1.0;
+      m->fspot = 0.5 * m->lacc2 / m->lstar / fluxratio;
+    }
+    if (m->nspot == 1) m->thspot_deg = std::acos(1.0 - 2.0 * m->fspot) * rad2deg;
+    else if (m->nspot == 2) m->thspot_deg = std::acos(1.0 - m->fspot) * rad2deg;
+    else { *err = "error!  nspot not set (NSPOT must be 1 or 2)"; return false; }
+    if (!(m->tshock_k > 0.0) || !std::isfinite(m->tshock_k) || !(m->fspot > 0.0) || !std::isfinite(m->thspot_deg)) {
+      *err = "the hot spots have no valid temperature or size (CTEMP=YES needs TSPOT > TSTAR; the spots "
+             "cannot cover more than the star)";
+      return false;
+    }
+  }
+  // mean stellar temperature including the shock, and the sublimation radius it sets
+  m->tave_k = m->tstar_k * std::pow(1.0 + 0.5 * m->lacc2 / m->lstar, 0.25);
+  m->rminsub = std::pow(m->tsub_k / m->tave_k, -2.1);
+  if ((m->rminsub > m->rmaxd[0] || m->rminsub > m->rmaxd[1]) && m->massd > 0.0) {
+    *err = "ERROR.  dust sublimation radius larger than RMAXD; increase RMAXD";
+    return false;
+  }
+  if (m->irminsub == 1) {
+    m->rmine = m->rminsub * m->rmine_in;
+    for (int d = 0; d < 2; ++d) m->rddust[d] = m->rminsub * m->rmind_in[d];
+  }
+  for (int d = 0; d < 2; ++d)
+    if (m->rddust[d] > m->rmaxd[d] && m->fmass[d] > 0.0) { *err = "ERROR, rddust > rmaxd"; return false; }
+  m->rddustmin = std::min(m->rddust[0], m->rddust[1]);
+  m->rmaxdmax = std::max(m->rmaxd[0], m->rmaxd[1]);
+  // the source constants
+  hc3d_sources& s = m->src;
+  s = hc3d_sources{};
+  s.rddustmin = m->rddustmin;
+  s.rmaxdmax = m->rmaxdmax;
+  s.rmax = m->rmax;
+  for (int d = 0; d < 2; ++d) {
+    s.zfac[d] = m->fmass[d] * m->z1[d];
+    s.zexp[d] = m->b[d];
+    s.kapv[d] = 0.0;  // set with the dust tables (build_model)
+  }
+  // The reference sets the gas temperature's accretion rate only for CALPHA=YES; for CALPHA=NO it
+  // leaves it unset.  Both use the total rate here (what its FITS writer uses for the same formula).
+  s.gas_num = 3.0 * kGn * (kMsun * m->massc) * m->mdot_cgs;
+  s.gas_den = 8.0 * kPi * kSigt;
+  s.rstar = m->rstar;
+  s.rsun = kRsun;
+  s.ispot = m->ispot;
+  s.nspot = m->nspot;
+  if (m->ispot) {
+    const double thspot = m->thspot_deg * deg2rad;
+    const double th1 = (90.0 - m->spotlat) * deg2rad, ph1 = 0.0 * deg2rad;  // spotlon = 0 (reapar.f90:291)
+    const double th2 = kPi - th1, ph2 = ph1 + kPi;
+    s.spot1[0] = std::sin(th1) * std::cos(ph1); s.spot1[1] = std::sin(th1) * std::sin(ph1);
+    s.spot1[2] = std::cos(th1); s.spot1[3] = std::sin(th1);
+    s.spot2[0] = std::sin(th2) * std::cos(ph2); s.spot2[1] = std::sin(th2) * std::sin(ph2);
+    s.spot2[2] = std::cos(th2); s.spot2[3] = std::sin(th2);
+    s.csprad = std::cos(thspot);
+  }
+  s.fspot = m->fspot;
+  s.tshock = m->tshock_k / 11605.0;
+  if (m->idiskacc && !(m->rddustmin < m->rmaxdmax)) {
+    *err = "CDISKACC=YES needs the disk's inner radius below its outer radius (no radius to emit from)";
+    return false;
+  }
+  return true;
 }
 
 // gridset walls and densities, gridset.f90:411-664 and 954-1098
@@ -1194,12 +1346,6 @@ static bool gridset(Model* m, std::string* err) {
   m->density_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_dens).count();
   // initarr(.true.): tdust2 = 0.1 K, tdust = tdust2 (initarr.f90:50,78-84)
   m->tdust.assign(n4 * m->ndg, 0.1 / 11605.0);
-  // luminosities without accretion (gridset.f90:206-209); l_isrf of
-  // newtts.F90:207 with rmax in stellar radii
-  m->lstar = 4.0 * kPi * kSigt * std::pow(m->tstar_k, 4.0) * rmincgs * rmincgs;
-  m->l_isrf = m->iout ? m->isrf_int * 4.0 * kPi * std::pow(m->rmax * kRsun * m->rstar, 2.0) / 4.0 * m->isrf_scl : 0.0;
-  m->ltot = m->lstar + m->l_isrf;
-  m->isrf_frac = m->l_isrf / m->ltot;
   // Lucy packets per iteration (newtts.F90:159-182)
   const int64_t ncells = m->ncells();
   int64_t npl = (ntg < 10 && npg < 10) ? 100 * ncells : (int64_t)(3.0 * (double)ncells);
@@ -1250,6 +1396,9 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
   if (!atmosinit(m, m->atname, err)) return false;
   if (m->iout && !isrf_cdf(m, err)) return false;
   setup_rho0(m);
+  for (int d = 0; d < 2; ++d) m->src.kapv[d] = 0.0;
+  if (!luminosities(m, err)) return false;
+  for (int d = 0; d < 2; ++d) m->src.kapv[d] = m->kappav[d] * (m->rstar * kRsun);
   if (!gridset(m, err)) return false;
   return true;
 }
@@ -1292,7 +1441,8 @@ hc3d_run_params Model::params_view() const {
   p.nxhst = nxhst; p.rmaxi = rmaxi; p.aperture2 = aperture2.data(); p.numin = numin; p.numax = numax;
   p.rstar_cm = rstar * kRsun; p.tstar = tstar_k / 11605.0; p.limb = limb; p.iintmax = 10000;
   p.max_interactions = maxint; p.image = image;
-  p.ext_illum = iout; p.n_star = hc3d_star_packets(isrf_frac, np); p.rmax = rmax;
+  p.ext_illum = iout; p.rmax = rmax;
+  set_shares(&p, np);
   return p;
 }
 
@@ -1305,6 +1455,8 @@ hc3d_model_info Model::info() const {
   i.density_host_ms = density_host_ms;
   i.tables_host_ms = tables_host_ms;
   i.lstar = lstar; i.l_isrf = l_isrf; i.isrf_frac = isrf_frac;
+  i.lacc = lacc; i.lacc2 = lacc2; i.accfrac = accfrac; i.accfrac2 = accfrac2; i.mdot_msun_yr = mdotdisk;
+  i.tshock_k = tshock_k; i.fspot = fspot; i.thspot_deg = thspot_deg; i.tave_k = tave_k;
   return i;
 }
 
@@ -1376,6 +1528,37 @@ extern "C" int64_t hc3d_star_packets(double isrf_frac, int64_t np) {
   const int64_t nsum = ns + npout;
   if (nsum != np) ns = ns + np - nsum;
   return ns;
+}
+
+extern "C" int hc3d_packet_split(double accfrac, double accfrac2, double isrf_frac, int64_t np, int64_t* n_acc,
+                                 int64_t* n_spot, int64_t* n_star) {
+  if (np < 0 || !n_acc || !n_spot || !n_star) return HC3D_ERR_INVALID;
+  // newdisktherm.F90:143-175: shares rounded as the reference rounds them (the
+  // accretion and hot-spot shares are truncated), ns takes up the difference
+  int64_t npout = (int64_t)(isrf_frac * (double)np);
+  double rn = isrf_frac * (double)np;
+  if (rn - (double)npout > 0.5) npout += 1;
+  int64_t ns = (int64_t)((double)np * (1.0 - accfrac - isrf_frac));
+  rn = (double)(float)np * (1.0 - accfrac - isrf_frac);
+  if (rn - (double)ns > 0.5) ns += 1;
+  const int64_t npacc = (int64_t)((double)np * accfrac);
+  int64_t npaccstar = (int64_t)(accfrac2 * (double)np);
+  rn = (double)(int64_t)((double)ns * accfrac2);
+  if (rn - (double)npaccstar > 0.5) npaccstar += 1;
+  const int64_t nsum = ns + npacc + npout;
+  if (nsum != np) ns = ns + np - nsum;
+  // the packet loop runs iphot = 1..np: iphot < npacc accretion, iphot <
+  // npacc + npaccstar hot spot, iphot <= npacc + ns star, the rest external
+  // (newdisktherm.F90:209,256,258); global ids here are iphot - 1
+  *n_star = std::max<int64_t>(0, std::min<int64_t>(np, npacc + ns));
+  *n_acc = std::max<int64_t>(0, std::min<int64_t>(*n_star, npacc - 1));
+  *n_spot = std::max<int64_t>(*n_acc, std::min<int64_t>(*n_star, npacc + npaccstar - 1));
+  return HC3D_OK;
+}
+
+void hc3d::Model::set_shares(hc3d_run_params* p, int64_t np_total) const {
+  p->sources = has_sources() ? &src : nullptr;
+  hc3d_packet_split(accfrac, accfrac2, isrf_frac, np_total, &p->n_acc, &p->n_spot, &p->n_star);
 }
 
 // Fixture writers ------------------------------------------------------------

@@ -91,6 +91,14 @@ struct Model {
   int igape = 0, igapedens = 0;
   double rgape1 = 0, rgape2 = 0, fracte = 1, rhogape = 0;
   bool disk_depends_on_phi() const { return idiskwarp || ispiral; }
+  // disk accretion and stellar hot spots (reapar.f90:275-312, gridset.f90:72-270, spotset.f90:179-206)
+  int idiskacc = 0, ialpha = 0, ispot = 0, itemp = 0, irminsub = 0;
+  double alphad = 0, mdotdisk = 0, rtrunc = 5, spotlat = 0, tspot = 0, fspot = 1;
+  double rmine_in = 0, rmind_in[2] = {0, 0};
+  double mdotcgs[2] = {0, 0}, mdot_cgs = 0, lacc = 0, lacc2 = 0, accfrac = 0, accfrac2 = 0;
+  double tshock_k = 0, thspot_deg = 0, tave_k = 0, rmaxdmax = 0;
+  hc3d_sources src{};
+  bool has_sources() const { return idiskacc || ispot; }
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;
   int image = 1;
@@ -119,6 +127,8 @@ struct Model {
   hc3d_dust_tables tables_view() const;
   hc3d_grid grid_view() const;
   hc3d_run_params params_view() const;  // pointers into this model
+  // n_acc, n_spot, n_star and sources of p for an iteration of np_total packets
+  void set_shares(hc3d_run_params* p, int64_t np_total) const;
   hc3d_model_info info() const;
   int64_t ncells() const { return (int64_t)(nrg - 1) * (ntg - 1) * (npg - 1); }
   int64_t n4() const { return (int64_t)nrg * ntg * npg; }

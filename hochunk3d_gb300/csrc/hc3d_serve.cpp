@@ -173,7 +173,7 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
     }
     ++iter;
     p.np = m.np_lucy;
-    p.n_star = hc3d_star_packets(m.isrf_frac, p.np);
+    m.set_shares(&p, p.np);
     p.ipeel = 0;
     p.iter = iter;
     double rel = 0;
@@ -195,7 +195,7 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
   if (!r) {
     ++iter;
     p.np = m.np;
-    p.n_star = hc3d_star_packets(m.isrf_frac, p.np);
+    m.set_shares(&p, p.np);
     p.ipeel = m.ipeel;
     p.iter = iter;
     res->nfreq = p.nfreq; res->nmu = p.nmu; res->nph = p.nph; res->nap = p.nap;

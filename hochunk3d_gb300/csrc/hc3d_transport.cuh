@@ -1937,23 +1937,81 @@ __device__ __forceinline__ R darkening(const DevModel& m, Rng& rng) {
   return (R)(__ldg(m.limb_xmu + n) - (p1 - xi) / (p1 - p0) * delmu);
 }
 
-// Stellar packet emission, newdisktherm.F90:256-337 with initpspot (spot-free),
-// initp_sample (limb = 0) and initp_transform.  rec receives the
-// stellar-surface peel-off event.
+__device__ __forceinline__ void set_status(const RunArgs& a, int code) {
+  if (a.status) atomicCAS(a.status, 0, code);
+}
+
+// Record a faulted packet (global id and fault code) in the fault log.
+__device__ __forceinline__ void log_fault(const DevTallies& t, const Rng& rng, int code) {
+  if (!t.fault_log) return;
+  const unsigned long long k = atomicAdd(t.fault_count, 1ull);
+  if (k < (unsigned long long)kFaultLog)
+    t.fault_log[k] = ((unsigned long long)rng.c2 | ((unsigned long long)rng.c3 << 32)) | ((unsigned long long)code << 56);
+}
+
+// bbfreq (random.f90:49-77): a frequency from the Planck function of
+// temperature teff (K/11605), drawn as -ln(z1 z2 z3 z4) teff / i, a Gamma(4)
+// variate of rate i, with i picked with weight 1/i^4 from the partial sums
+// inczeta.  FP64 in both forms (one draw per hot-spot or gas packet).
 template <class R>
-__device__ void emit_star(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
-                          PeelRec<R>& rec, Tracer& tr) {
+__device__ double bbfreq(const DevModel& m, double teff, Rng& rng) {
+  const double z0 = __ldg(m.inczeta + kIzmax - 1) * (double)ran<R>(rng);
+  const double z1 = (double)ran<R>(rng), z2 = (double)ran<R>(rng), z3 = (double)ran<R>(rng),
+               z4 = (double)ran<R>(rng);
+  int i = 1;
+  while (i < kIzmax && z0 > __ldg(m.inczeta + i - 1)) ++i;
+  return -log(z1 * z2 * z3 * z4) * teff / (double)i;
+}
+
+constexpr int kEmitTries = 1 << 24;  // cap of the rejection loops of an emission point
+enum { F_EMIT = 5 };                 // fault code: no emission point within the cap
+
+// Stellar and hot-spot packet emission, newdisktherm.F90:256-337 with
+// initpspot (initpspot.f90:33-160), initp_sample (limb = 0, or the Eddington
+// table) and initp_transform.  spotph = 1 for a hot-spot packet: with spots
+// (ispot) its point is redrawn until it lies in a spot; it radiates at the
+// shock temperature, half of the hot-spot packets as X-rays
+// (newdisktherm.F90:270-273).  A stellar packet whose point falls in a spot
+// also takes the shock temperature when the spots cover less than the star
+// (fspot < 1).  The spot geometry is FP64 in both forms (one test per packet).
+// rec receives the stellar-surface peel-off event.  Returns false when no
+// point was found within the cap (the packet is dropped and logged).
+template <class R>
+__device__ bool emit_star(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
+                          PeelRec<R>& rec, Tracer& tr, int spotph) {
   p.on_wall = 0;
   p.safe = 0.f;
   p.lrow.key = -1;
   p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
-  for (;;) {
-    const R xran = ran<R>(rng);
-    p.cosb = R(1) - R(2) * xran;
-    p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
-    if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
+  const bool spots = a.src_on && a.src.ispot;
+  for (int tries = 0;; ++tries) {
+    for (;;) {
+      const R xran = ran<R>(rng);
+      p.cosb = R(1) - R(2) * xran;
+      p.sinb = xsqrt(R(1) - p.cosb * p.cosb);
+      if (p.cosb != R(0) && xabs(p.cosb) < R(1)) break;
+    }
+    p.lp = (R)kR2p * ran<R>(rng);
+    if (!spots) break;
+    const hc3d_sources& S = a.src;
+    const double cb = (double)p.cosb, sb = (double)p.sinb, lp = (double)p.lp;
+    const double cphi = cos(lp), sphi = sin(lp);
+    const double d1 = S.spot1[0] * sb * cphi + S.spot1[1] * sb * sphi + S.spot1[2] * cb;
+    const double d2 = S.spot2[0] * sb * cphi + S.spot2[1] * sb * sphi + S.spot2[2] * cb;
+    if (spotph == 1 && (S.nspot == 1 ? d1 < S.csprad : (d1 < S.csprad && d2 < S.csprad))) {
+      if (tries >= kEmitTries) return false;
+      continue;
+    }
+    if (S.fspot < 1.0) {
+      double dellon = lp < kPi ? lp : kR2p - lp;
+      if (S.spot1[2] * cb + S.spot1[3] * sb * cos(dellon) > S.csprad) spotph = 1;
+      if (S.nspot == 2) {
+        dellon = lp < kPi ? kPi - lp : lp - kPi;
+        if (S.spot2[2] * cb + S.spot2[3] * sb * cos(dellon) > S.csprad) spotph = 1;
+      }
+    }
+    break;
   }
-  p.lp = (R)kR2p * ran<R>(rng);
   // initp_sample (initp_common.f90:1-29): cost = sqrt(xi), or the Eddington table
   p.cost = a.limb ? darkening<R>(m, rng) : xsqrt(ran<R>(rng));
   p.sint = xsqrt(R(1) - p.cost * p.cost);
@@ -1961,7 +2019,13 @@ __device__ void emit_star(const DevModel& m, const DustView<R>& dv, const RunArg
   p.cosp = xcos(p.phi);
   p.sinp = xsin(p.phi);
   initp_transform<R>(p);
-  p.nub = atmosfreq<R>(m, rng);
+  if (spotph) {
+    double nu = bbfreq<R>(m, a.src.tshock, rng);
+    if (ran<R>(rng) < R(0.5)) nu = 1.2398 / 0.06 + (double)ran<R>(rng) * (1.2398 / 0.015 - 1.2398 / 0.06);
+    p.nub = (R)nu;
+  } else {
+    p.nub = atmosfreq<R>(m, rng);
+  }
   p.i_orig = 1;
   opacset<R>(m, dv, p, p.nub, a);
   const R coslp = xcos(p.lp), sinlp = xsin(p.lp);
@@ -1979,6 +2043,7 @@ __device__ void emit_star(const DevModel& m, const DustView<R>& dv, const RunArg
   tr.add(0, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   make_rec<R>(rec, p, a, 0, 0, 128);
   rec.d0 = p.cosb; rec.d1 = p.sinb; rec.d2 = coslp; rec.d3 = sinlp;
+  return true;
 }
 
 // rep_isrf (rep_isrf.f90:1-41): the frequency of an external packet, by
@@ -2036,28 +2101,172 @@ __device__ void emit_external(const DevModel& m, const DustView<R>& dv, const Ru
   make_rec<R>(rec, p, a, 0, 0, kRecNoPeel);
 }
 
-// A new packet: stellar, or from outside when external illumination is on and
-// its global id is past the stellar share (newdisktherm.F90:207-260: the
-// Fortran numbers the stellar packets first)
+// gasdev (random.f90:140-159): polar Box-Muller pairs, the second deviate of a
+// pair returned by the next call.  The reference keeps that deviate in the
+// process, so one packet's height uses the deviate its predecessor drew; here
+// it is kept in the packet (each packet starts a new pair), which the
+// counter-based per-packet streams require.  The deviates are N(0,1) either way.
+struct Gauss {
+  int have;
+  double next;
+};
 template <class R>
-__device__ __forceinline__ void emit(const DevModel& m, const DustView<R>& dv, const RunArgs& a, Pkt<R>& p, Rng& rng,
-                                     PeelRec<R>& rec, Tracer& tr) {
+__device__ double gasdev(Gauss& g, Rng& rng) {
+  if (g.have) {
+    g.have = 0;
+    return g.next;
+  }
+  double v1, v2, rsq;
+  do {
+    v1 = 2.0 * (double)ran<R>(rng) - 1.0;
+    v2 = 2.0 * (double)ran<R>(rng) - 1.0;
+    rsq = v1 * v1 + v2 * v2;
+  } while (!(rsq < 1.0 && rsq > 0.0));
+  const double fac = sqrt(-2.0 * log(rsq) / rsq);
+  g.next = v1 * fac;
+  g.have = 1;
+  return v2 * fac;
+}
+
+// Disk accretion packet, newdisktherm.F90:209-251 with initpacc
+// (initpacc.f90:24-119), emit_common (emit_common.f90:25-79), emit_gasacc
+// (emit_gasacc.f90:26-42) and reemit (reemit.f90:17-34).  The radius is drawn
+// from the accretion luminosity profile (w = 1/r with density 1 - sqrt(w),
+// in (rddustmin, rmaxdmax)), the azimuth by rantheta, the height as a
+// Gaussian of the mass-weighted disk scale height; the point must lie inside
+// rmax.  In a cell with thermal disk dust the packet is emitted by a disk
+// grain species picked by its V-band opacity (the reference picks with the
+// opacities at the previous packet's frequency, a dependence between packets
+// that per-packet streams cannot have; with one disk species or one dust file
+// the choice is the same) at that species' temperature, and counted as an
+// absorption there; otherwise by the gas at the Pringle (1981) accretion
+// disk temperature.  The packet starts inside its cell (not on a wall) with
+// origin 2 (disk) and an unscattered peel-off.  FP64 set-up in both forms
+// (one per accretion packet).  Returns false when no point was found within
+// the cap or no species can be picked (the packet is dropped and logged).
+template <class R>
+__device__ __forceinline__ bool emit_acc(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a,
+                                      Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr) {
+  const hc3d_sources& S = a.src;
+  p.on_wall = 0;
+  p.safe = 0.f;
+  p.lrow.key = -1;
+  Gauss g{0, 0.0};
+  double rp, xp, yp, zp;
+  int tries = 0;
+  for (;;) {
+    rp = 0.0;
+    while (rp >= S.rmaxdmax || rp <= S.rddustmin) {
+      double winv = (double)ran<R>(rng);
+      while ((double)ran<R>(rng) > 1.0 - sqrt(winv)) {
+        winv = (double)ran<R>(rng);
+        if (++tries > kEmitTries) return false;
+      }
+      rp = 1.0 / winv;
+      if (++tries > kEmitTries) return false;
+    }
+    // rantheta (random.f90:28-47): a uniform azimuth from a point in the unit disk
+    double x, y, r2;
+    do {
+      x = (double)ran<R>(rng);
+      x = x + x - 1.0;
+      y = (double)ran<R>(rng);
+      y = y + y - 1.0;
+      r2 = x * x + y * y;
+    } while (r2 > 1.0 || r2 == 0.0);
+    const double r = sqrt(r2);
+    xp = rp * (x / r);
+    yp = rp * (y / r);
+    const double h = (0.0 + S.zfac[0] * pow(rp, S.zexp[0])) + S.zfac[1] * pow(rp, S.zexp[1]);
+    zp = h * gasdev<R>(g, rng);
+    if (zp * zp + rp * rp < S.rmax * S.rmax) break;
+    if (++tries > kEmitTries) return false;
+  }
+  p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+  const double rsq = xp * xp + yp * yp + zp * zp;
+  const double rtot = sqrt(rsq);
+  int ir = locate_dev(m.r2arr, m.nrg, rsq);
+  const double cosb = zp / rtot;
+  int it = locate_dev(m.costarr, m.ntg, cosb);
+  double lp = atan2(yp, xp);
+  if (lp < 0.0) lp = lp + kR2p;
+  int ip = locate_dev(m.phiarr, m.npg, lp);
+  p.ir = ir < 1 ? 1 : (ir > m.nrg - 1 ? m.nrg - 1 : ir);
+  p.it = it < 1 ? 1 : (it > m.ntg - 1 ? m.ntg - 1 : it);
+  p.ip = ip < 1 ? 1 : (ip > m.npg - 1 ? m.npg - 1 : ip);
+  set_pos(p.x, xp);
+  set_pos(p.y, yp);
+  set_pos(p.z, zp);
+  p.cosb = (R)cosb;
+  p.lp = (R)lp;
+  const int64_t c = cidx(m, p.ir, p.it, p.ip);
+  // select_dust over the thermal disk slots (select_dust.f90:16-42)
+  const double d0 = __ldg(m.rho4d + 4 * c), d1 = __ldg(m.rho4d + 4 * c + 1);
+  int idust2 = -1;
+  if (0.0 + d0 + d1 > 0.0) {
+    const double xran = (double)ran<R>(rng);
+    const double opac = (0.0 + S.kapv[0] * d0) + S.kapv[1] * d1;
+    if (opac == 0.0) return false;
+    const double eps = (double)1.e-10f;
+    double frac = 0.0 + S.kapv[0] * d0 / opac;
+    if (xran <= frac + eps) {
+      idust2 = 0;
+    } else {
+      frac = frac + S.kapv[1] * d1 / opac;
+      if (xran <= frac + eps) idust2 = 1;
+      else return false;
+    }
+    atomicAdd(t.dbig + c, 1u);
+    atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
+    // reemit at the species' temperature
+    p.cost = R(1) - R(2) * ran<R>(rng);
+    p.sint = xsqrt(R(1) - p.cost * p.cost);
+    p.phi = (R)kR2p * ran<R>(rng);
+    p.cosp = xcos(p.phi);
+    p.sinp = xsin(p.phi);
+    if constexpr (sizeof(R) == 4) p.nub = lucy_freq_mixed(m, p.lrow, c, idust2, rng);
+    else p.nub = lucydustfreq<R>(m, __ldg(m.tdust + 4 * c + idust2), idust2, rng);
+  } else {
+    // gas at the accretion disk temperature (Pringle 1981, eq. 3.23)
+    const double t0 = S.gas_num / (S.gas_den * pow(rtot * S.rstar * S.rsun, 3.0));
+    const double tgas = pow(t0 * (1.0 - sqrt(1.0 / rtot)), 0.25) / 11605.0;
+    p.nub = (R)bbfreq<R>(m, tgas, rng);
+    p.cost = R(1) - R(2) * ran<R>(rng);
+    p.sint = xsqrt(R(1) - p.cost * p.cost);
+    p.phi = (R)kR2p * ran<R>(rng);
+    p.cosp = xcos(p.phi);
+    p.sinp = xsin(p.phi);
+  }
+  p.ux = p.sint * p.cosp; p.uy = p.sint * p.sinp; p.uz = p.cost;
+  p.i_orig = 2;
+  opacset<R>(m, dv, p, p.nub, a);
+  tr.add(0, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
+  make_rec<R>(rec, p, a, 0, idust2 < 0 ? 0 : idust2);
+  return true;
+}
+
+// A new packet, by its global id (newdisktherm.F90:207-449: the Fortran
+// numbers the accretion packets first, then the hot-spot, stellar and
+// external ones).  Returns false when the packet could not be emitted (a
+// rejection loop ran out; counted and logged): it is dropped and its peel-off
+// record is marked empty.
+template <class R>
+__device__ __forceinline__ bool emit(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a,
+                                     Pkt<R>& p, Rng& rng, PeelRec<R>& rec, Tracer& tr, Local& L) {
   const int64_t pid = (int64_t)((uint64_t)rng.c2 | ((uint64_t)rng.c3 << 32));
+  bool ok = true;
   if (a.ext_illum && pid >= a.n_star) emit_external<R>(m, dv, a, p, rng, rec, tr);
-  else emit_star<R>(m, dv, a, p, rng, rec, tr);
+  else if (pid < a.n_acc) ok = emit_acc<R>(m, dv, t, a, p, rng, rec, tr);
+  else ok = emit_star<R>(m, dv, a, p, rng, rec, tr, pid < a.n_spot ? 1 : 0);
+  if (!ok) {
+    L.add(HC3D_CNT_STUCK);
+    set_status(a, 2);
+    log_fault(t, rng, F_EMIT);
+    rec.flags = kRecNoPeel;
+  }
+  return ok;
 }
 
-__device__ __forceinline__ void set_status(const RunArgs& a, int code) {
-  if (a.status) atomicCAS(a.status, 0, code);
-}
-
-// Record a faulted packet (global id and fault code) in the fault log.
-__device__ __forceinline__ void log_fault(const DevTallies& t, const Rng& rng, int code) {
-  if (!t.fault_log) return;
-  const unsigned long long k = atomicAdd(t.fault_count, 1ull);
-  if (k < (unsigned long long)kFaultLog)
-    t.fault_log[k] = ((unsigned long long)rng.c2 | ((unsigned long long)rng.c3 << 32)) | ((unsigned long long)code << 56);
-}
 
 // tau sample + tauint + outcome, propagate.f90:46-62 (first) and 169-202.
 template <class R>
@@ -2157,7 +2366,7 @@ __device__ void run_packet(const DevModel& m, const DustView<R>& dv, const DevTa
                            Local& L, Tracer& tr) {
   Pkt<R> p;
   PeelRec<R> rec;
-  emit<R>(m, dv, a, p, rng, rec, tr);
+  if (!emit<R>(m, dv, t, a, p, rng, rec, tr, L)) return;
   if (a.ipeel == 1) peel_all<R>(m, t, d, a, rec, L);
   Flow<R> f;
   f.xpold = p.x; f.ypold = p.y; f.zpold = p.z;
@@ -2275,10 +2484,24 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     if (rng.left > 0) philox(rng.c0 - 1, 0u, rng.c2, rng.c3, rng.k0, rng.k1, rng.b);
   }
   Tracer tr{nullptr, 0, 0};
+  // The warp runs its rounds in step (every lane takes part in the ballots).
+  // Regeneration threshold: a lane whose packet has ended takes the next one
+  // only when at least a.regen lanes of its warp are waiting, or no lane is
+  // busy, so that emissions run together instead of beside the other lanes'
+  // interactions.  The tallies do not depend on it (each packet's stream is
+  // keyed by its id).
+  bool done = false;  // the batch has no packet left for this lane
   for (int nrec = 0; nrec < E; ++nrec) {
+    const unsigned waiting = __ballot_sync(0xffffffffu, s.stage == 0 && !done);
+    const unsigned busy = __ballot_sync(0xffffffffu, s.stage != 0);
+    if (waiting == 0u && busy == 0u) break;  // warp-uniform
     if (s.stage == 0) {
+      if (done || (busy != 0u && __popc(waiting) < a.regen)) continue;
       const unsigned long long pid = atomicAdd(a.work, 1ull);
-      if (pid >= (unsigned long long)a.np) break;
+      if (pid >= (unsigned long long)a.np) {
+        done = true;
+        continue;
+      }
       s.pid = (uint64_t)(a.packet_offset + (int64_t)pid);
       rng_init(rng, a.key0, a.key1, s.pid);
     }
@@ -2287,7 +2510,7 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     // that work, and the record occupies no registers across the walk.
     PeelRec<R>& rec = queue[atomicAdd(qcount, 1ull)];
     if (s.stage == 0) {
-      emit<R>(m, dv, a, s.p, rng, rec, tr);
+      if (!emit<R>(m, dv, t, a, s.p, rng, rec, tr, L)) continue;  // dropped: the lane takes the next packet
       s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
       s.f.iflag = 0; s.f.iscat = 0; s.f.iint = 0; s.f.idust2 = 0; s.f.ntot = 0;
       s.stage = 2;  // emitted: walk to the first interaction after the record

@@ -82,6 +82,17 @@ class Grid(C.Structure):
     ]
 
 
+class Sources(C.Structure):
+    """hc3d_sources: constants of the disk-accretion and hot-spot packets."""
+    _fields_ = [
+        ("rddustmin", C.c_double), ("rmaxdmax", C.c_double), ("rmax", C.c_double),
+        ("zfac", C.c_double * 2), ("zexp", C.c_double * 2), ("kapv", C.c_double * 2),
+        ("gas_num", C.c_double), ("gas_den", C.c_double), ("rstar", C.c_double), ("rsun", C.c_double),
+        ("ispot", C.c_int), ("nspot", C.c_int), ("spot1", C.c_double * 4), ("spot2", C.c_double * 4),
+        ("csprad", C.c_double), ("fspot", C.c_double), ("tshock", C.c_double),
+    ]
+
+
 class RunParams(C.Structure):
     _fields_ = [
         ("np", C.c_int64), ("packet_offset", C.c_int64), ("seed", C.c_uint64), ("iter", C.c_int),
@@ -91,6 +102,7 @@ class RunParams(C.Structure):
         ("rstar_cm", C.c_double), ("tstar", C.c_double), ("limb", C.c_int), ("iintmax", C.c_int),
         ("max_interactions", C.c_int64), ("image", C.c_int),
         ("ext_illum", C.c_int), ("n_star", C.c_int64), ("rmax", C.c_double),
+        ("n_acc", C.c_int64), ("n_spot", C.c_int64), ("sources", C.POINTER(Sources)),
     ]
 
 
@@ -134,6 +146,9 @@ class ModelInfo(C.Structure):
         ("massdisk", C.c_double), ("massenv", C.c_double), ("ncells", C.c_int64),
         ("density_host_ms", C.c_double), ("tables_host_ms", C.c_double),
         ("lstar", C.c_double), ("l_isrf", C.c_double), ("isrf_frac", C.c_double),
+        ("lacc", C.c_double), ("lacc2", C.c_double), ("accfrac", C.c_double), ("accfrac2", C.c_double),
+        ("mdot_msun_yr", C.c_double), ("tshock_k", C.c_double), ("fspot", C.c_double),
+        ("thspot_deg", C.c_double), ("tave_k", C.c_double),
     ]
 
 
@@ -144,8 +159,8 @@ class TtsStats(C.Structure):
 
 
 class TuneResult(C.Structure):
-    _fields_ = [("n", C.c_int), ("best", C.c_int), ("queue_records", C.c_int64 * 4), ("block_size", C.c_int * 4),
-                ("ms", C.c_double * 4)]
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("queue_records", C.c_int64 * 8), ("block_size", C.c_int * 8),
+                ("regen", C.c_int * 8), ("ms", C.c_double * 8)]
 
 
 class ServerOpts(C.Structure):
@@ -207,6 +222,8 @@ SIGNATURES = {
     "hc3d_write_outputs": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies), dp, dp, C.c_char_p]),
     "hc3d_write_grid_unf": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, dp, i32p]),
     "hc3d_star_packets": (C.c_int64, [C.c_double, C.c_int64]),
+    "hc3d_packet_split": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_int64, P(C.c_int64), P(C.c_int64),
+                                    P(C.c_int64)]),
     "hc3d_server_create": (C.c_int, [P(C.c_void_p), P(ServerOpts)]),
     "hc3d_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_int64)]),
     "hc3d_server_wait": (C.c_int, [C.c_void_p, C.c_int64, P(Result)]),
@@ -219,7 +236,7 @@ SIGNATURES = {
 
 # entry points of libhc3d_host.so (the model set-up, no CUDA)
 HOST_SYMBOLS = ("hc3d_model_create", "hc3d_model_destroy", "hc3d_model_views", "hc3d_model_set_tdust",
-                "hc3d_star_packets", "hc3d_write_synthetic_dust", "hc3d_write_wavelength_grid",
+                "hc3d_star_packets", "hc3d_packet_split", "hc3d_write_synthetic_dust", "hc3d_write_wavelength_grid",
                 "hc3d_write_synthetic_isrf")
 
 _LIB = None
@@ -280,6 +297,16 @@ def tally_scales(np_: int) -> tuple[float, float, float]:
 def star_packets(isrf_frac: float, np_: int) -> int:
     """Stellar packets of an iteration of np_ packets (hc3d_star_packets)."""
     return int(host_lib().hc3d_star_packets(float(isrf_frac), int(np_)))
+
+
+def packet_split(accfrac: float, accfrac2: float, isrf_frac: float, np_: int) -> tuple[int, int, int]:
+    """(n_acc, n_spot, n_star) of an iteration of np_ packets (hc3d_packet_split)."""
+    a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+    rc = host_lib().hc3d_packet_split(float(accfrac), float(accfrac2), float(isrf_frac), int(np_), C.byref(a),
+                                      C.byref(b), C.byref(c))
+    if rc != 0:
+        raise Hc3dError(rc, "hc3d_packet_split")
+    return a.value, b.value, c.value
 
 
 # ---------------------------------------------------------------------------
@@ -371,10 +398,11 @@ class Model:
     def run_params(self, np_total: int | None = None, **over) -> RunParams:
         """The model's run parameters with fields of RunParams overridden.
 
-        n_star, the stellar share of the iteration, follows np unless given.
-        A shard of an iteration (packet_offset > 0, or np below the whole)
-        passes np_total, the packets of the whole iteration, so that every
-        shard splits stellar and external packets as one run would."""
+        The shares of the iteration (n_acc, n_spot, n_star: accretion,
+        hot-spot, stellar and external packets) follow np unless n_star is
+        given.  A shard of an iteration (packet_offset > 0, or np below the
+        whole) passes np_total, the packets of the whole iteration, so that
+        every shard splits the sources as one run would."""
         q = RunParams()
         for f, _ in RunParams._fields_:
             setattr(q, f, getattr(self._p, f))
@@ -386,9 +414,21 @@ class Model:
                 raise AttributeError(f"RunParams has no field {k}")
             setattr(q, k, v)
         if "n_star" not in over and (np_total is not None or "np" in over):
-            # the stellar share of the iteration's packets (newdisktherm.F90:143-175)
-            q.n_star = star_packets(self.info.isrf_frac, q.np if np_total is None else np_total)
+            # the shares of the iteration's packets (newdisktherm.F90:143-175)
+            i = self.info
+            n_acc, n_spot, n_star = packet_split(i.accfrac, i.accfrac2, i.isrf_frac,
+                                                 q.np if np_total is None else np_total)
+            q.n_star = n_star
+            if "n_acc" not in over:
+                q.n_acc = n_acc
+            if "n_spot" not in over:
+                q.n_spot = n_spot
         return q
+
+    @property
+    def sources(self) -> Sources | None:
+        """The accretion and hot-spot constants of the model (None without either)."""
+        return self._p.sources.contents if self._p.sources else None
 
     def set_tdust(self, tdust: np.ndarray) -> None:
         self.tdust = np.asfortranarray(tdust, dtype=np.float64).copy(order="F")
@@ -568,7 +608,8 @@ class Context:
         r = TuneResult()
         self._check(lib().hc3d_autotune(self._h, C.byref(sample), C.byref(r)))
         return {"candidates": [{"queue_records": int(r.queue_records[k]), "block_size": int(r.block_size[k]),
-                                "ms": float(r.ms[k])} for k in range(r.n)], "best": int(r.best)}
+                                "regen": int(r.regen[k]), "ms": float(r.ms[k])} for k in range(r.n)],
+                "best": int(r.best)}
 
     def lucy_iterations(self, params: RunParams, n_iter: int, ltot: float, want_tdust: bool = True):
         """n_iter Lucy iterations as one CUDA graph (hc3d_lucy_iterations):

@@ -123,6 +123,30 @@ typedef struct hc3d_grid {
   const double *tdust;    /* (nrg,ntg,npg,ndg) temperature used by re-emission, K/11605 */
 } hc3d_grid;
 
+/* Constants of the disk-accretion and stellar hot-spot sources (CDISKACC,
+ * CSPOT), as gridset (gridset.f90:72-203) and spotset (spotset.f90:179-206)
+ * leave them.  Lengths in stellar radii, temperatures in K/11605. */
+typedef struct hc3d_sources {
+  /* disk accretion packets (initpacc.f90:24-49, emit_gasacc.f90:26-29) */
+  double rddustmin;       /* emission radii lie in (rddustmin, rmaxdmax) */
+  double rmaxdmax;        /* max(rmaxd(1), rmaxd(2)), setup.f90:181 */
+  double rmax;            /* the emission point lies inside the sphere of radius rmax */
+  double zfac[2];         /* fmass*z1 of the two disk slots: height = sum(zfac r^zexp) * gasdev() */
+  double zexp[2];         /* b of the two disk slots */
+  double kapv[2];         /* kappa_V * rmincgs of the two disk slots: the weights that pick the emitting dust */
+  double gas_num;         /* 3 G (Msun Mc) Mdot, cgs */
+  double gas_den;         /* 8 pi sigma_SB: T_gas^4 = gas_num / (gas_den (r rstar rsun)^3) (1 - r^-1/2) K^4 */
+  double rstar, rsun;     /* stellar radius in Rsun, and Rsun in cm */
+  /* hot spots (initpspot.f90:33-160) */
+  int ispot;              /* CSPOT: 1 = spots on the stellar surface */
+  int nspot;              /* 1 or 2 (the second opposite the first) */
+  double spot1[4];        /* sin th0 cos phi0, sin th0 sin phi0, cos th0, sin th0 of spot 1 (scspot1 ..) */
+  double spot2[4];        /* the same for spot 2 */
+  double csprad;          /* cos of the spot radius: points with dot > csprad lie in a spot */
+  double fspot;           /* filling factor of the spots; 1 = stellar packets keep the stellar spectrum */
+  double tshock;          /* spot (shock) temperature */
+} hc3d_sources;
+
 /* The scalars and small arrays of tts_mod/out_mod that one call of disk()
  * reads (setup.f90:37-43,118-130,196-202; initarr.f90:17-21). */
 typedef struct hc3d_run_params {
@@ -147,9 +171,15 @@ typedef struct hc3d_run_params {
   int image;              /* 1 = accumulate broadband I,Q,U,V images of the peeled packets */
   int ext_illum;          /* 1 = external illumination (COUTILLUM): packets with global id >= n_star
                              enter from the outer sphere (newdisktherm.F90:378-440); needs nisrf > 0 */
-  int64_t n_star;         /* stellar packets of the whole iteration (ns, newdisktherm.F90:143-175),
-                             from hc3d_star_packets */
+  int64_t n_star;         /* packets of the whole iteration with a source inside the grid: global ids
+                             >= n_star are external (npacc + ns of newdisktherm.F90:143-175, from
+                             hc3d_packet_split; hc3d_star_packets without accretion) */
   double rmax;            /* outer radius of the grid, R* (the external packets start at 0.999999 rmax) */
+  int64_t n_acc;          /* global ids < n_acc are disk accretion packets (iphot < npacc,
+                             newdisktherm.F90:209); needs sources */
+  int64_t n_spot;         /* global ids in [n_acc, n_spot) are hot-spot packets (iphot < npacc + npaccstar,
+                             newdisktherm.F90:258); needs sources */
+  const hc3d_sources *sources; /* accretion and spot constants; NULL = neither (n_acc = n_spot = 0) */
 } hc3d_run_params;
 
 /* Host copies of the device tallies.  Any pointer may be NULL.  Shapes are
@@ -251,15 +281,19 @@ int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
 
 /* ---- autotuner (no counterpart in the reference) ---------------------------
  * Times the sample batch under each candidate setting and keeps the fastest
- * in the context: the peel-off queue depth (2^20 .. 2^23 records) for peeled
- * runs, the transport block size (64, 96, 128) otherwise.  The tallies are
- * zeroed afterwards. */
+ * in the context.  Peeled runs: the peel-off queue depth (2^20 .. 2^23
+ * records), then at the best depth the regeneration threshold of the
+ * wavefront kernel (1, 4, 8, 16: how many lanes of a warp must be waiting
+ * before they take new packets).  Other runs: the transport block size (64,
+ * 96, 128).  The settings do not change the tallies.  The tallies are zeroed
+ * afterwards. */
 typedef struct hc3d_tune_result {
   int n;                     /* candidates timed */
   int best;                  /* index of the setting the context now uses */
-  int64_t queue_records[4];  /* per candidate */
-  int block_size[4];
-  double ms[4];              /* wall time of the sample batch */
+  int64_t queue_records[8];  /* per candidate */
+  int block_size[8];
+  int regen[8];
+  double ms[8];              /* wall time of the sample batch */
 } hc3d_tune_result;
 int hc3d_autotune(hc3d_ctx *ctx, const hc3d_run_params *sample, hc3d_tune_result *out);
 
@@ -332,7 +366,9 @@ int hc3d_last_launch_stats(hc3d_ctx *ctx, int *launches, double *transport_ms, d
 /* Packets stopped by a fault since the last hc3d_zero_tallies(): *n receives
  * the count and entries[0..min(n,max,256)-1] the global packet id in the low
  * 56 bits and the fault code in the high 8 (1 index range, 2 no wall found,
- * 3 crossing cap, 4 no opacity to select a species).  Replaying a logged id
+ * 3 crossing cap, 4 no opacity to select a species, 5 an accretion or
+ * hot-spot packet without an emission point within the sampling cap or
+ * without a species to emit it).  Replaying a logged id
  * through hc3d_trace_packets with its counter-based uniforms reproduces it. */
 int hc3d_get_fault_log(hc3d_ctx *ctx, uint64_t *entries, int max, int *n);
 /* Per wave of the last peeled run: event budget E, threads that could run,

@@ -57,6 +57,16 @@ typedef struct hc3d_model_info {
   double lstar;           /* stellar luminosity, erg/s */
   double l_isrf;          /* external-illumination luminosity, erg/s (newtts.F90:204-228) */
   double isrf_frac;       /* l_isrf / ltot (gridset.f90:208-209) */
+  /* disk accretion and hot spots (gridset.f90:72-270); zero without CDISKACC */
+  double lacc;            /* accretion luminosity of the disk, erg/s */
+  double lacc2;           /* accretion shock luminosity on the star, erg/s */
+  double accfrac;         /* lacc / ltot */
+  double accfrac2;        /* lacc2 / ltot */
+  double mdot_msun_yr;    /* disk accretion rate */
+  double tshock_k;        /* hot-spot temperature, K */
+  double fspot;           /* spot filling factor (1 without spots) */
+  double thspot_deg;      /* spot radius, degrees */
+  double tave_k;          /* mean stellar temperature with the shock, K; sets rminsub */
 } hc3d_model_info;
 
 /* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
@@ -75,9 +85,9 @@ int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
  * densdisk, densenv, the fractal factor, cell volumes and (rho V)^(1/4)) on
  * CUDA device `device`, replacing the host-built densarr, massarr, vcell and
  * the grid masses of the model.  *ms receives the device time of the
- * kernels.  Models with disk structure (CGAPD, CSPIRAL, CDISKWARP, CRIMPUFF,
- * CGAPPUFF, CRIMCURVE, CGAPCURVE, CRADEXP) or an envelope gap (CGAPE), which
- * the host build covers, return HC3D_ERR_UNSUPPORTED. */
+ * kernels.  Every disk structure option (CGAPD, CSPIRAL, CDISKWARP, CRIMPUFF,
+ * CGAPPUFF, CRIMCURVE, CGAPCURVE, CRADEXP) and the envelope gap (CGAPE) are
+ * built on the device. */
 int hc3d_model_densities_gpu(hc3d_model *m, int device, double *ms, char *err, size_t errlen);
 
 /* setemiss (dust.f90:394-474: the cumulative emissivity tables kapBint and
@@ -91,6 +101,16 @@ int hc3d_model_tables_gpu(hc3d_model *m, int device, double *ms, char *err, size
  * without accretion): both shares rounded to the nearest integer, then ns
  * adjusted so that the shares add up to np.  isrf_frac = 0 gives np. */
 int64_t hc3d_star_packets(double isrf_frac, int64_t np);
+
+/* The packet shares of an iteration of np packets (newdisktherm.F90:143-175)
+ * as the boundaries of hc3d_run_params: global ids < n_acc are accretion
+ * packets, [n_acc, n_spot) hot-spot packets, [n_spot, n_star) stellar
+ * packets and the rest external.  accfrac, accfrac2 and isrf_frac are the
+ * luminosity fractions of hc3d_model_info.  The reference's loop tests
+ * iphot < npacc, so its accretion share is npacc - 1 packets and the stellar
+ * share one more than ns - npaccstar; the boundaries keep that. */
+int hc3d_packet_split(double accfrac, double accfrac2, double isrf_frac, int64_t np, int64_t *n_acc,
+                      int64_t *n_spot, int64_t *n_star);
 
 typedef struct hc3d_tts_stats {
   int iterations;            /* Lucy iterations + the final one */

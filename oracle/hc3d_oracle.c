@@ -53,6 +53,7 @@ typedef struct orc_ctx {
   int ndg;
   int64_t ncell4; /* nrg*ntg*npg */
   int limb;       /* run parameter limb (0 or 1) */
+  double inczeta[145]; /* zetainit partial sums of bbfreq (random.f90:79-97) */
 } orc_ctx;
 
 /* Tallies: the fixed-point arrays of hc3d_tallies plus FP64 sums of the
@@ -780,16 +781,53 @@ static double orc_darkening(const orc_ctx *c, double xi) {
   return d->limb_xmu[n] - (d->limb_prob[n] - xi) / (d->limb_prob[n] - d->limb_prob[n - 1]) * delmu;
 }
 
-/* ---- initpspot (ispot=0) with initp_sample, initp_common.f90:1-29 -------- */
-static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
+/* ---- bbfreq, random.f90:49-77 ----------------------------------------------- */
+static double orc_bbfreq(const orc_ctx *c, double teff, orc_rng *rng) {
+  const double z0 = c->inczeta[144] * orc_ran(rng);
+  const double z1 = orc_ran(rng), z2 = orc_ran(rng), z3 = orc_ran(rng), z4 = orc_ran(rng);
+  int i = 1;
+  while (i < 145 && z0 > c->inczeta[i - 1]) i++;
+  return -log(z1 * z2 * z3 * z4) * teff / (double)i;
+}
+
+#define ORC_EMIT_TRIES (1 << 24) /* cap of the emission rejection loops (the GPU library's) */
+
+/* ---- initpspot, initpspot.f90:33-160, with initp_sample (initp_common.f90:1-29)
+ * and the X-ray half of the hot-spot packets (newdisktherm.F90:270-273).
+ * spotph: 1 for a hot-spot packet, 0 for a stellar one; *spot_out (when not
+ * NULL) receives 1 when the packet radiates at the shock temperature.
+ * Returns 0 when the spot rejection ran past the cap. */
+static int orc_initpspot(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, orc_rng *rng, int spotph,
+                         int *spot_out) {
+  const hc3d_sources *S = rp->sources;
+  const int spots = S && S->ispot;
   p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
-  for (;;) {
-    double xran = orc_ran(rng);
-    p->cosb = 1.0 - 2.0 * xran;
-    p->sinb = sqrt(1.0 - p->cosb * p->cosb);
-    if (p->cosb != 0.0 && fabs(p->cosb) < 1.0) break;
+  for (int tries = 0;; tries++) {
+    for (;;) {
+      double xran = orc_ran(rng);
+      p->cosb = 1.0 - 2.0 * xran;
+      p->sinb = sqrt(1.0 - p->cosb * p->cosb);
+      if (p->cosb != 0.0 && fabs(p->cosb) < 1.0) break;
+    }
+    p->lp = ORC_R2P * orc_ran(rng);
+    if (!spots) break;
+    const double cphi = cos(p->lp), sphi = sin(p->lp), sthet = p->sinb, cthet = p->cosb;
+    const double dotsp1 = S->spot1[0] * sthet * cphi + S->spot1[1] * sthet * sphi + S->spot1[2] * cthet;
+    const double dotsp2 = S->spot2[0] * sthet * cphi + S->spot2[1] * sthet * sphi + S->spot2[2] * cthet;
+    if (spotph == 1 && (S->nspot == 1 ? dotsp1 < S->csprad : (dotsp1 < S->csprad && dotsp2 < S->csprad))) {
+      if (tries >= ORC_EMIT_TRIES) return 0;
+      continue;
+    }
+    if (S->fspot < 1.0) {
+      double dellon = p->lp < ORC_PI ? p->lp : ORC_R2P - p->lp;
+      if (S->spot1[2] * p->cosb + S->spot1[3] * p->sinb * cos(dellon) > S->csprad) spotph = 1;
+      if (S->nspot == 2) {
+        dellon = p->lp < ORC_PI ? ORC_PI - p->lp : p->lp - ORC_PI;
+        if (S->spot2[2] * p->cosb + S->spot2[3] * p->sinb * cos(dellon) > S->csprad) spotph = 1;
+      }
+    }
+    break;
   }
-  p->lp = ORC_R2P * orc_ran(rng);
   /* initp_sample: uniform disk (limb = 0) or the Eddington table (darkening) */
   p->cost = c->limb ? orc_darkening(c, orc_ran(rng)) : sqrt(orc_ran(rng));
   p->sint = sqrt(1.0 - p->cost * p->cost);
@@ -797,8 +835,17 @@ static void orc_initpspot(const orc_ctx *c, pkt *p, orc_rng *rng) {
   p->cosp = cos(p->phi);
   p->sinp = sin(p->phi);
   orc_initp_transform(p);
-  /* fspot = 1 without spots: nub = atmosfreq() (initpspot.f90:150-156) */
-  p->nub = orc_atmosfreq(c, rng);
+  /* initpspot.f90:146-160: the hot-spot packets (iplanckst = 1) and the
+   * stellar packets that fall in a spot when fspot < 1 radiate at tshock; the
+   * other stellar packets take the stellar spectrum (atmosfreq) */
+  if (spot_out) *spot_out = spotph;
+  if (spotph) {
+    p->nub = orc_bbfreq(c, S->tshock, rng);
+    if (orc_ran(rng) < 0.5) p->nub = 1.2398 / 0.06 + orc_ran(rng) * (1.2398 / 0.015 - 1.2398 / 0.06);
+  } else {
+    p->nub = orc_atmosfreq(c, rng);
+  }
+  return 1;
 }
 
 /* ---- rep_isrf, rep_isrf.f90:1-41 ------------------------------------------ */
@@ -974,7 +1021,143 @@ static void orc_external_packet(const orc_ctx *c, const hc3d_run_params *rp, pkt
   orc_propagate(c, rp, p, rng, t, tr);
 }
 
-/* ---- one stellar packet: newdisktherm.F90:256-377 with ips = 0 ------------ */
+/* ---- gasdev, random.f90:140-159, its saved deviate kept per packet -------- */
+typedef struct orc_gauss {
+  int have;
+  double next;
+} orc_gauss;
+
+static double orc_gasdev(orc_gauss *g, orc_rng *rng) {
+  if (g->have) {
+    g->have = 0;
+    return g->next;
+  }
+  double v1, v2, rsq;
+  do {
+    v1 = 2.0 * orc_ran(rng) - 1.0;
+    v2 = 2.0 * orc_ran(rng) - 1.0;
+    rsq = v1 * v1 + v2 * v2;
+  } while (!(rsq < 1.0 && rsq > 0.0));
+  const double fac = sqrt(-2.0 * log(rsq) / rsq);
+  g->next = v1 * fac;
+  g->have = 1;
+  return v2 * fac;
+}
+
+/* ---- one disk accretion packet: newdisktherm.F90:209-251 with initpacc
+ * (initpacc.f90:24-119), emit_common (emit_common.f90:25-79), emit_gasacc
+ * (emit_gasacc.f90:26-42) and reemit (reemit.f90:17-34).  The emitting disk
+ * species is picked with the V-band opacities (kapv of hc3d_sources; the
+ * reference uses the opacities of the previous packet's frequency).  Returns
+ * 0 when no emission point was found within the cap or no species could be
+ * picked. */
+static int orc_acc_emit(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, orc_rng *rng, orc_tallies *t,
+                        int *idust_out) {
+  const hc3d_sources *S = rp->sources;
+  orc_gauss g = {0, 0.0};
+  double rp_, xp, yp, zp;
+  int tries = 0;
+  for (;;) {
+    rp_ = 0.0;
+    while (rp_ >= S->rmaxdmax || rp_ <= S->rddustmin) {
+      double winv = orc_ran(rng);
+      while (orc_ran(rng) > 1.0 - sqrt(winv)) {
+        winv = orc_ran(rng);
+        if (++tries > ORC_EMIT_TRIES) return 0;
+      }
+      rp_ = 1.0 / winv;
+      if (++tries > ORC_EMIT_TRIES) return 0;
+    }
+    /* rantheta, random.f90:28-47 */
+    double x, y, r2;
+    do {
+      x = orc_ran(rng);
+      x = x + x - 1.0;
+      y = orc_ran(rng);
+      y = y + y - 1.0;
+      r2 = x * x + y * y;
+    } while (r2 > 1.0 || r2 == 0.0);
+    const double r = sqrt(r2);
+    xp = rp_ * (x / r);
+    yp = rp_ * (y / r);
+    /* sum(fmass*z1*rp**b, mask=is_disk) * gasdev() */
+    zp = ((0.0 + S->zfac[0] * pow(rp_, S->zexp[0])) + S->zfac[1] * pow(rp_, S->zexp[1])) * orc_gasdev(&g, rng);
+    if (zp * zp + rp_ * rp_ < S->rmax * S->rmax) break;
+    if (++tries > ORC_EMIT_TRIES) return 0;
+  }
+  p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
+  const double rsq = xp * xp + yp * yp + zp * zp;
+  const double rtot = sqrt(rsq);
+  int ir = orc_locate(c->g.r2arr, c->g.nrg, rsq);
+  const double cosb = zp / rtot;
+  int it = orc_locate(c->g.costarr, c->g.ntg, cosb);
+  double lp = atan2(yp, xp);
+  if (lp < 0.0) lp = lp + ORC_R2P;
+  int ip = orc_locate(c->g.phiarr, c->g.npg, lp);
+  p->ir = ir < 1 ? 1 : (ir > c->g.nrg - 1 ? c->g.nrg - 1 : ir);
+  p->it = it < 1 ? 1 : (it > c->g.ntg - 1 ? c->g.ntg - 1 : it);
+  p->ip = ip < 1 ? 1 : (ip > c->g.npg - 1 ? c->g.npg - 1 : ip);
+  p->xp = xp; p->yp = yp; p->zp = zp;
+  p->cosb = cosb;
+  p->lp = lp;
+  p->on_wall = 0;
+  const int64_t cell = cidx(c, p->ir, p->it, p->ip);
+  const double d0 = dens(c, cell, 0), d1 = dens(c, cell, 1);
+  int idust2 = -1;
+  if (0.0 + d0 + d1 > 0.0) {
+    /* select_dust (select_dust.f90:16-42) over the thermal disk slots */
+    const double xran = orc_ran(rng);
+    const double opac = (0.0 + S->kapv[0] * d0) + S->kapv[1] * d1;
+    if (opac == 0.0) return 0;
+    double frac = 0.0;
+    const double dd[2] = {d0, d1};
+    for (int id = 0; id < 2 && idust2 < 0; ++id) {
+      frac = frac + S->kapv[id] * dd[id] / opac;
+      if (xran <= frac + (double)1.e-10f) idust2 = id;
+    }
+    if (idust2 < 0) return 0;
+    if (t) {
+      t->fx.dbig[cell]++;
+      t->fx.nabs[cell + c->ncell4 * idust2] += 1;
+    }
+    /* emit_common thermal branch (ilucy = 1): reemit at the species' temperature */
+    p->cost = 1.0 - 2.0 * orc_ran(rng);
+    p->sint = sqrt(1.0 - p->cost * p->cost);
+    p->phi = ORC_R2P * orc_ran(rng);
+    p->cosp = cos(p->phi);
+    p->sinp = sin(p->phi);
+    p->nub = orc_lucydustfreq(c, c->g.tdust[cell + c->ncell4 * idust2], idust2, rng);
+  } else {
+    /* emit_gasacc: the accretion disk temperature of Pringle (1981), eq. 3.23 */
+    const double t0 = S->gas_num / (S->gas_den * pow(rtot * S->rstar * S->rsun, 3.0));
+    const double tgas = pow(t0 * (1.0 - sqrt(1.0 / rtot)), 0.25) / 11605.0;
+    p->nub = orc_bbfreq(c, tgas, rng);
+    p->cost = 1.0 - 2.0 * orc_ran(rng);
+    p->sint = sqrt(1.0 - p->cost * p->cost);
+    p->phi = ORC_R2P * orc_ran(rng);
+    p->cosp = cos(p->phi);
+    p->sinp = sin(p->phi);
+  }
+  p->ux = p->sint * p->cosp; p->uy = p->sint * p->sinp; p->uz = p->cost;
+  p->i_orig = 2;
+  orc_opacset(c, p, p->nub, rp->rstar_cm);
+  *idust_out = idust2;
+  return 1;
+}
+
+static int orc_acc_packet(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, orc_rng *rng, orc_tallies *t,
+                          orc_trace *tr) {
+  int idust2;
+  if (!orc_acc_emit(c, rp, p, rng, t, &idust2)) return 0;
+  trace_add(tr, 0, p->ir, p->it, p->ip, 0, 0, p->xp, p->yp, p->zp);
+  if (rp->ipeel == 1)
+    for (int k = 0; k < rp->npeel; ++k) orc_peeloff(c, rp, p, p->sip, 0, idust2 < 0 ? 0 : idust2, k, t);
+  orc_propagate(c, rp, p, rng, t, tr);
+  return 1;
+}
+
+/* ---- one packet by its global id: newdisktherm.F90:194-449 with ips = 0 --- */
+/* Accretion packets first, then hot-spot, stellar and external packets. */
 static void orc_packet(const orc_ctx *c, const hc3d_run_params *rp, int64_t pid, orc_rng *rng, orc_tallies *t,
                        orc_trace *tr) {
   pkt p;
@@ -984,7 +1167,15 @@ static void orc_packet(const orc_ctx *c, const hc3d_run_params *rp, int64_t pid,
     orc_external_packet(c, rp, &p, rng, t, tr);
     return;
   }
-  orc_initpspot(c, &p, rng);
+  if (rp->sources && pid < rp->n_acc) {
+    if (!orc_acc_packet(c, rp, &p, rng, t, tr)) { t->fx.counters[HC3D_CNT_STUCK]++; t->errors++; }
+    return;
+  }
+  if (!orc_initpspot(c, rp, &p, rng, rp->sources && pid < rp->n_spot ? 1 : 0, NULL)) {
+    t->fx.counters[HC3D_CNT_STUCK]++;
+    t->errors++;
+    return;
+  }
   p.i_orig = 1;
   orc_opacset(c, &p, p.nub, rp->rstar_cm);
   const double coslp = cos(p.lp), sinlp = sin(p.lp);
@@ -1029,6 +1220,64 @@ static void orc_ctx_init(orc_ctx *c, const hc3d_dust_tables *dt, const hc3d_grid
   c->limb = 0;
   c->ndg = g->ndg;
   c->ncell4 = (int64_t)g->nrg * g->ntg * g->npg;
+  /* zetainit (random.f90:79-97): inczeta(i) = sum 1/j^4 over j <= i, added from j = 145 down */
+  for (int i = 0; i < 145; ++i) c->inczeta[i] = 0.0;
+  for (int j = 145; j >= 1; --j) {
+    const double term = 1.0 / (double)(j * j * j * j);
+    for (int i = 145; i >= j; --i) c->inczeta[i - 1] = c->inczeta[i - 1] + term;
+  }
+}
+
+/* The emission of packets [pid0, pid0 + n) of params, without their
+ * transport: out[9 k + 0..8] = kind (1 accretion, 2 hot spot, 3 stellar,
+ * 4 external, -1 dropped), x, y, z, nu, ir, it, ip, and for an accretion
+ * packet the emitting slot (0, 1; -1 the gas) -- for a stellar or hot-spot
+ * packet 1 when it radiates at the shock temperature, else 0. */
+int orc_sample_emission(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run_params *rp, int64_t pid0,
+                        int64_t n, double *out) {
+  orc_ctx c;
+  orc_ctx_init(&c, dt, g);
+  c.limb = rp->limb;
+  for (int64_t k = 0; k < n; ++k) {
+    const int64_t pid = rp->packet_offset + pid0 + k;
+    orc_rng rng;
+    orc_rng_init(&rng, rp->seed, rp->iter, pid);
+    pkt p;
+    memset(&p, 0, sizeof(p));
+    double *o = out + 9 * k;
+    int kind, extra = 0, ok = 1;
+    if (rp->ext_illum && pid >= rp->n_star) {
+      kind = 4;
+      orc_initpout(&c, &p, &rng);
+    } else if (rp->sources && pid < rp->n_acc) {
+      kind = 1;
+      ok = orc_acc_emit(&c, rp, &p, &rng, NULL, &extra);
+    } else {
+      kind = rp->sources && pid < rp->n_spot ? 2 : 3;
+      ok = orc_initpspot(&c, rp, &p, &rng, kind == 2, &extra);
+      p.xp = p.sinb * cos(p.lp); p.yp = p.sinb * sin(p.lp); p.zp = p.cosb;
+    }
+    o[0] = ok ? kind : -1;
+    o[1] = p.xp; o[2] = p.yp; o[3] = p.zp; o[4] = p.nub;
+    o[5] = p.ir; o[6] = p.it; o[7] = p.ip; o[8] = extra;
+  }
+  return 0;
+}
+
+/* n draws of bbfreq(teff), draw k from the counter stream (seed, 1, k). */
+int orc_sample_bbfreq(double teff, uint64_t seed, int64_t n, double *out) {
+  orc_ctx c;
+  memset(&c, 0, sizeof(c));
+  for (int j = 145; j >= 1; --j) {
+    const double term = 1.0 / (double)(j * j * j * j);
+    for (int i = 145; i >= j; --i) c.inczeta[i - 1] = c.inczeta[i - 1] + term;
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    orc_rng rng;
+    orc_rng_init(&rng, seed, 1, k);
+    out[k] = orc_bbfreq(&c, teff, &rng);
+  }
+  return 0;
 }
 
 /* Run packets [pid_begin, pid_end) of params into t (single thread). */

@@ -58,6 +58,8 @@ def lib() -> C.CDLL:
         L.orc_dusttemp.argtypes = [P(DustTables)] + [C.c_double] * 4 + [C.c_int, C.c_double]
         L.orc_dusttemp.restype = C.c_double
         L.orc_tfinal.argtypes = [P(DustTables), P(Grid), dp, C.c_double, C.c_double, dp]
+        L.orc_sample_emission.argtypes = [P(DustTables), P(Grid), P(RunParams), C.c_int64, C.c_int64, dp]
+        L.orc_sample_bbfreq.argtypes = [C.c_double, C.c_uint64, C.c_int64, dp]
         ip = P(C.c_int)
         L.orc_closest_wall_c.argtypes = [C.c_int, dp, ip, C.c_int, dp, ip, dp]
         L.orc_phiface_roots.argtypes = [C.c_double] * 8 + [dp, ip]
@@ -196,4 +198,27 @@ def tfinal(model: hc3d.Model, na: np.ndarray, ltot: float, nphot: float) -> np.n
     out = np.zeros(model.shape4, dtype=np.float64, order="F")
     lib().orc_tfinal(C.byref(t), C.byref(g), na.ctypes.data_as(P(C.c_double)), ltot, nphot,
                      out.ctypes.data_as(P(C.c_double)))
+    return out
+
+
+EMISSION_DTYPE = np.dtype([("kind", "<f8"), ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("nu", "<f8"),
+                           ("ir", "<f8"), ("it", "<f8"), ("ip", "<f8"), ("extra", "<f8")])
+
+
+def sample_emission(model: hc3d.Model, params: RunParams, pid0: int, n: int) -> np.ndarray:
+    """The emission of packets [pid0, pid0 + n) without transport: a record
+    array of kind (1 accretion, 2 hot spot, 3 star, 4 external, -1 dropped),
+    position, frequency, cell and extra (accretion: the emitting disk slot,
+    -1 the gas; star and hot spot: 1 when radiating at the shock temperature)."""
+    t, g = model.tables, model.grid
+    out = np.zeros(9 * n, dtype=np.float64)
+    lib().orc_sample_emission(C.byref(t), C.byref(g), C.byref(params), int(pid0), int(n),
+                              out.ctypes.data_as(P(C.c_double)))
+    return out.view(EMISSION_DTYPE)
+
+
+def sample_bbfreq(teff: float, seed: int, n: int) -> np.ndarray:
+    """n frequencies of the blackbody sampler bbfreq at temperature teff (K/11605)."""
+    out = np.zeros(n, dtype=np.float64)
+    lib().orc_sample_bbfreq(float(teff), int(seed), int(n), out.ctypes.data_as(P(C.c_double)))
     return out

@@ -430,3 +430,128 @@ def diskflux_sed(si, sq, su, sv, si2, sq2, su2, sv2, nums, np_, nmu, nph, ltot_l
     for key, s in (("i", si), ("q", sq), ("u", su), ("v", sv)):
         out[key] = s / rnorm
     return out
+
+
+# ---- disk accretion and hot spots ------------------------------------------------
+GN = 6.67428e-8   # constants.f90:19
+MSOL = 1.989e33   # constants.f90:13
+RSOL = 6.9598e10  # constants.f90:11
+DEG2RAD = PI / 180.0
+RAD2DEG = 180.0 / PI
+
+
+def rho0_disk(massd, fmass, rmaxd, rmind, a, b, z1, rmincgs):
+    """setup_wave.f90:60-92: the disk density scale of one species slot."""
+    z1cgs = rmincgs * z1
+    p = b - a
+    if not (rmaxd > 0.0 and fmass > 0.0):
+        return 0.0
+    const = R2P ** 1.5 * rmincgs ** 2 * z1cgs
+    if p != -2.0 and p != -1.5:
+        den = 1.0 / (p + 2.0) * (rmaxd ** (p + 2.0) - rmind ** (p + 2.0)) - \
+              1.0 / (p + 1.5) * (rmaxd ** (p + 1.5) - rmind ** (p + 1.5))
+    elif p == -2.0:
+        den = math.log(rmaxd / rmind) - 1.0 / (p + 1.5) * (rmaxd ** (p + 1.5) - rmind ** (p + 1.5))
+    else:
+        den = 1.0 / (p + 2.0) * (rmaxd ** (p + 2.0) - rmind ** (p + 2.0)) - math.log(rmaxd / rmind)
+    return massd * MSOL / const / den * fmass
+
+
+def accretion_luminosity(tstar, rstar, massc, massd, rddustmin, rtrunc, rho0, z1, ialpha, alphad, mdotdisk,
+                         l_isrf, itemp, fspot, tspot, nspot, tsub=1600.0):
+    """gridset.f90:72-264 with CDISKACC=YES: the accretion rates of the two
+    disk slots, lacc, lacc2, the luminosity fractions, the shock temperature,
+    the spot size and the mean stellar temperature with its sublimation
+    radius.  Returns a dict."""
+    rmincgs = rstar * RSOL
+    yr = 3600.0 * 24.0 * 365.25
+    lstar = 4.0 * PI * SIGT * tstar ** 4 * rmincgs ** 2
+    vc = math.sqrt(GN * MSOL * massc / rmincgs)
+    mdotcgs = [0.0, 0.0]
+    if ialpha == 1:
+        for i in range(2):
+            mdotcgs[i] = math.sqrt(18.0 * PI ** 3.0) * alphad * vc * rho0[i] * (z1[i] * rmincgs) ** 3.0 / rmincgs
+    else:
+        tot = mdotdisk / (yr / MSOL)
+        ratio = (rho0[0] * (z1[0] * z1[0] * z1[0]) / rho0[1] / (z1[1] * z1[1] * z1[1])) if rho0[1] != 0.0 else math.inf
+        mdotcgs[1] = tot / (1.0 + ratio)
+        mdotcgs[0] = tot - mdotcgs[1]
+    mdot = mdotcgs[0] + mdotcgs[1]
+    lacc = GN * (MSOL * massc) * mdot / 2.0 / (rddustmin * rmincgs)
+    lacc2 = GN * (MSOL * massc) * mdot * (1.0 / rmincgs - 1.0 / (rmincgs * rtrunc)) if massd > 0.0 else 0.0
+    if massd <= 0.0:
+        lacc = 0.0
+    ltot = lacc + lacc2 + lstar + l_isrf
+    out = {"lstar": lstar, "lacc": lacc, "lacc2": lacc2, "ltot": ltot, "accfrac": lacc / ltot,
+           "accfrac2": lacc2 / ltot, "mdot_msun_yr": mdot * yr / MSOL, "tshock_k": 0.0, "thspot_deg": 0.0,
+           "fspot": fspot}
+    if lacc2 > 0.0:
+        if itemp == 0:
+            tshock = tstar * (1.0 + 0.5 * lacc2 / lstar / fspot) ** 0.25
+        else:
+            tshock = tspot
+            fspot = 0.5 * lacc2 / lstar / ((tshock / tstar) ** 4 - 1.0)
+        th = math.acos(1.0 - 2.0 * fspot) if nspot == 1 else math.acos(1.0 - fspot)
+        out.update(tshock_k=tshock, thspot_deg=th * RAD2DEG, fspot=fspot)
+    tave = tstar * (1.0 + 0.5 * lacc2 / lstar) ** 0.25
+    out["tave_k"] = tave
+    out["rminsub"] = (tsub / tave) ** (-2.1)
+    return out
+
+
+def packet_shares(np_, accfrac, accfrac2, isrf_frac):
+    """newdisktherm.F90:143-175 and the loop tests of 209, 256, 258: the
+    number of accretion, hot-spot, stellar and external packets of an
+    iteration of np_ packets (iphot = 1..np_)."""
+    npout = int(isrf_frac * np_)
+    if isrf_frac * np_ - npout > 0.5:
+        npout += 1
+    ns = int(np_ * (1.0 - accfrac - isrf_frac))
+    rn = float(np.float32(np_)) * (1.0 - accfrac - isrf_frac)  # real(np): single precision
+    if rn - ns > 0.5:
+        ns += 1
+    npacc = int(np_ * accfrac)
+    npaccstar = int(accfrac2 * np_)
+    if int(ns * accfrac2) - npaccstar > 0.5:
+        npaccstar += 1
+    if ns + npacc + npout != np_:
+        ns = ns + np_ - (ns + npacc + npout)
+    counts = {"acc": 0, "spot": 0, "star": 0, "ext": 0}
+    for iphot in range(1, np_ + 1):
+        if iphot < npacc:
+            counts["acc"] += 1
+        elif iphot <= npacc + ns:
+            counts["spot" if iphot < npacc + npaccstar else "star"] += 1
+        else:
+            counts["ext"] += 1
+    return counts
+
+
+def inczeta(izmax=145):
+    """zetainit, random.f90:79-97."""
+    z = [0.0] * izmax
+    for j in range(izmax, 0, -1):
+        term = 1.0 / float(j * j * j * j)
+        for i in range(izmax, j - 1, -1):
+            z[i - 1] = z[i - 1] + term
+    return z
+
+
+def bbfreq(teff, u, zeta=None):
+    """random.f90:49-77 with the five uniforms u."""
+    zeta = zeta or inczeta()
+    z0 = zeta[-1] * u[0]
+    i = 1
+    while z0 > zeta[i - 1]:
+        i += 1
+    return -math.log(u[1] * u[2] * u[3] * u[4]) * teff / float(i)
+
+
+def spot_geometry(spotlat, thspot_deg):
+    """spotset.f90:187-206: (scspot, ssspot, cspot, sspot) of both spots and csprad."""
+    th1 = (90.0 - spotlat) * DEG2RAD
+    ph1 = 0.0 * DEG2RAD
+    th2, ph2 = PI - th1, ph1 + PI
+    s1 = (math.sin(th1) * math.cos(ph1), math.sin(th1) * math.sin(ph1), math.cos(th1), math.sin(th1))
+    s2 = (math.sin(th2) * math.cos(ph2), math.sin(th2) * math.sin(ph2), math.cos(th2), math.sin(th2))
+    return s1, s2, math.cos(thspot_deg * DEG2RAD)

@@ -98,7 +98,10 @@ def test_batched_launch_equals_separate_runs(pars, prec):
     separately and the compiler may fuse an FP32 multiply and add in one and
     not the other, so a packet can take a different branch after a last-bit
     difference (a diverged long history touches many cells): its tallies
-    agree to 1e-3 of each array's total and in 90 % of the bins."""
+    agree to 1e-3 of each array's total; the counts (si, nums, nabs, killed)
+    are identical in 90 % of the bins, and the FP32 path-length sums (jmean,
+    dtauabs), whose every crossing may round differently, agree to 1e-4 of the
+    bin in 90 % of the bins."""
     models = [hc3d.Model(p) for p in pars]
     params = [m.run_params(np=6000 + 1000 * k, iter=2, ipeel=0) for k, m in enumerate(models)]
     want = []
@@ -119,7 +122,12 @@ def test_batched_launch_equals_separate_runs(pars, prec):
                 continue
             a, b = got[key].astype(np.float64), want[k][key].astype(np.float64)
             assert np.abs(a - b).sum() <= 1e-3 * np.abs(b).sum() + 2, (k, key)
-            assert np.mean(got[key] == want[k][key]) >= 0.9 or key == "counters", (k, key)
+            if key in ("jmean", "dtauabs"):
+                nz = (a != 0) | (b != 0)
+                close = np.abs(a - b) <= 1e-4 * np.maximum(np.abs(a), np.abs(b))
+                assert np.mean(close[nz]) >= 0.9, (k, key, float(np.mean(close[nz])))
+            elif key != "counters":
+                assert np.mean(got[key] == want[k][key]) >= 0.9, (k, key)
         c.close()
 
 

@@ -41,12 +41,23 @@ def test_missing_key_is_an_error(tmp_path, built):
     assert "NRG" in str(e.value)
 
 
-@pytest.mark.parametrize("key", ["CSPOT", "CDISKACC", "DIFFUSION"])
+@pytest.mark.parametrize("key", ["DIFFUSION", "CHSEQ"])
 def test_unsupported_options_are_rejected(tmp_path, built, key):
     par = configs.write_par(tmp_path, "tiny", **{key: "YES"})
     with pytest.raises(hc3d.Hc3dError) as e:
         hc3d.Model(par)
     assert e.value.code == -7
+
+
+def test_spots_without_accretion_are_rejected(tmp_path, built):
+    """Hot spots take their temperature from the accretion shock: CSPOT=YES
+    without CDISKACC=YES would emit the spots' packets at T = 0."""
+    par = configs.write_par(tmp_path, "tiny", CSPOT="YES")
+    with pytest.raises(hc3d.Hc3dError) as e:
+        hc3d.Model(par)
+    assert e.value.code == -1 and "CDISKACC" in str(e.value)
+    m = hc3d.Model(configs.write_par(tmp_path, "tiny", CDISKACC="YES"))
+    assert m.info.accfrac > 0 and m.sources.ispot == 0
 
 
 def test_external_illumination_needs_its_field(tmp_path, built):
