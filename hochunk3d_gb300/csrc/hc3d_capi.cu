@@ -62,6 +62,11 @@ struct hc3d_ctx {
   int wave_blocks = 0, peel_blocks = 0;
   int64_t queue_records = 1 << 22;  // peel-off events held per wave
   int regen = 1;                    // k_wave regeneration threshold (lanes of a warp)
+  // a peeled iteration run in chunks (hc3d_run_chunk): packets in flight stay in the pool
+  bool chunk_open = false;
+  int64_t carry_alive = 0;
+  uint32_t chunk_key0 = 0, chunk_key1 = 0;
+  int qchunk = 8;                   // k_wave queue slots reserved per atomic
   bool use_waves = true;            // peeled runs use the wavefront form
 };
 
@@ -300,6 +305,7 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   }
   a->limb = p->limb;
   a->regen = c->regen;
+  a->qchunk = c->qchunk;
   // disk accretion and hot-spot packets
   a->n_acc = 0;
   a->n_spot = 0;
@@ -335,6 +341,8 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
 
 // Release the wavefront buffers (after both streams are idle).
 void drop_wave(hc3d_ctx* c) {
+  c->chunk_open = false;  // packets in flight are lost with the pool
+  c->carry_alive = 0;
   if (!c->wave.pool) return;
   cudaStreamSynchronize(c->pstream);
   cudaStreamSynchronize(c->stream);
@@ -358,7 +366,8 @@ int ensure_wave(hc3d_ctx* c) {
   int per_sm_p = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, f64 ? peel_fn_fp64() : peel_fn_mixed(), 256, 0));
   c->peel_blocks = c->sm_count * std::max(1, per_sm_p);
-  c->qcap = std::max<int64_t>(c->queue_records, c->pool_threads);
+  // room for every thread's qchunk reserved slots on top of one record each (see run_waves' E)
+  c->qcap = std::max<int64_t>(c->queue_records, c->pool_threads * (int64_t)(c->qchunk + 1));
   const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
   const size_t rec = f64 ? rec_bytes_fp64() : rec_bytes_mixed();
   int r;
@@ -395,14 +404,19 @@ int wave_events(hc3d_ctx* c, int w) {
 // beside the transport of the next -- in particular beside the long packet
 // histories that leave most of the device idle at the end of a batch.  Before
 // k_wave reuses a queue it waits for the k_peel that read it.
-int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
+//
+// drain = false (a chunk of an iteration, hc3d_run_chunk): the loop stops
+// once every packet of the call has been started; the packets still in
+// flight stay in the pool and continue in the next chunk of the iteration.
+int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a, bool drain = true) {
   int r;
   if ((r = ensure_wave(c))) return r;
   const bool f64 = c->precision == HC3D_PREC_FP64;
   const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
-  CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
-  LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->pstream};
   int64_t alive_prev = 0;
+  if (c->chunk_open) alive_prev = c->carry_alive;
+  else CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
+  LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->pstream};
   unsigned long long work = 0, events_prev = 0;
   CK(cudaMemcpyAsync(&events_prev, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events_prev), cudaMemcpyDeviceToHost,
                      c->stream));
@@ -415,7 +429,8 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     const int64_t remaining = p->np - (int64_t)std::min<unsigned long long>(work, (unsigned long long)p->np);
     const int64_t active = std::min<int64_t>(c->pool_threads, alive_prev + remaining);
     if (active <= 0) break;
-    const int E = (int)std::max<int64_t>(1, std::min<int64_t>(c->qcap / active, 1 << 20));
+    // each appending lane takes at most E records and leaves fewer than qchunk reserved slots unused
+    const int E = (int)std::max<int64_t>(1, std::min<int64_t>(c->qcap / active - c->qchunk, 1 << 20));
     const int q = wave & 1;
     if ((r = wave_events(c, wave))) return r;
     const int ev = 4 * wave;
@@ -450,8 +465,12 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a) {
     events_prev = events;
     alive_prev = alive;
     ++nwave;
-    if (alive == 0 && work >= (unsigned long long)p->np) break;
+    if (work >= (unsigned long long)p->np && (alive == 0 || !drain)) break;
   }
+  c->chunk_open = !drain && alive_prev > 0;
+  c->carry_alive = c->chunk_open ? alive_prev : 0;
+  c->chunk_key0 = a.key0;
+  c->chunk_key1 = a.key1;
   // the first stream waits for the last k_peel, so that what follows on it
   // (tallies, temperatures) sees every ray
   CK(cudaEventRecord(c->join, c->pstream));
@@ -961,6 +980,19 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   return hc3d_zero_tallies(c);
 }
 
+extern "C" int hc3d_set_wave_options(hc3d_ctx* c, int64_t queue_records, int regen, int qchunk) {
+  if (!c || queue_records < 0 || regen < 0 || regen > 32 || qchunk < 0 || qchunk > 64) return HC3D_ERR_INVALID;
+  if (c->chunk_open) return fail(c, HC3D_ERR_STATE, "a chunked iteration has packets in flight");
+  if (queue_records > 0 && queue_records < 1024) return fail(c, HC3D_ERR_INVALID, "queue_records < 1024");
+  if ((queue_records && queue_records != c->queue_records) || (qchunk && qchunk != c->qchunk)) {
+    drop_wave(c);  // reallocated at the next peeled run
+    if (queue_records) c->queue_records = queue_records;
+    if (qchunk) c->qchunk = qchunk;
+  }
+  if (regen) c->regen = regen;
+  return HC3D_OK;
+}
+
 extern "C" int hc3d_set_tdust(hc3d_ctx* c, const double* tdust) {
   if (!c || !tdust) return HC3D_ERR_INVALID;
   if (!c->grid) return fail(c, HC3D_ERR_STATE, "load the grid first");
@@ -1014,6 +1046,8 @@ extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
   c->scales_set = false;
   c->epoch_np = 0;
   c->status_seen = 0;
+  c->chunk_open = false;  // packets of an unfinished chunked iteration are discarded
+  c->carry_alive = 0;
   return HC3D_OK;
 }
 
@@ -1043,6 +1077,9 @@ LaunchCfg transport_cfg(hc3d_ctx* c, int64_t np) {
 
 extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   if (!c) return HC3D_ERR_INVALID;
+  if (c->chunk_open)
+    return fail(c, HC3D_ERR_STATE, "a chunked iteration has packets in flight: end it with hc3d_run_chunk(final = 1) "
+                                   "or discard it with hc3d_zero_tallies()");
   CK(cudaSetDevice(c->device));
   RunArgs a;
   int r = prepare_run(c, p, &a);
@@ -1068,6 +1105,38 @@ extern "C" int hc3d_run_iteration(hc3d_ctx* c, const hc3d_run_params* p) {
   c->last_transport_ms = ms;
   c->last_peel_ms = 0.0;
   c->last_launches = 1;
+  c->epoch_np += p->np;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_run_chunk(hc3d_ctx* c, const hc3d_run_params* p, int64_t np_iteration, int final) {
+  if (!c || !p) return HC3D_ERR_INVALID;
+  if (!p->ipeel || !c->use_waves) {
+    // the per-thread form finishes every packet it starts: a chunk is a run
+    if (np_iteration < p->np) return fail(c, HC3D_ERR_INVALID, "np_iteration < np");
+    if (!c->scales_set && c->grid && c->tables) set_scales(c, np_iteration);
+    return hc3d_run_iteration(c, p);
+  }
+  if (np_iteration < p->np) return fail(c, HC3D_ERR_INVALID, "np_iteration < np");
+  CK(cudaSetDevice(c->device));
+  if (!c->scales_set && !c->chunk_open && c->grid && c->tables) {
+    // the fixed-point scales of the whole iteration (prepare_run keeps them)
+    const TallyDims d = dims_of(p);
+    if (!c->run_tallies || !same_dims(d, c->dims)) {
+      int r = check_params(c, p);
+      if (r) return r;
+      if ((r = alloc_run_tallies(c, d))) return r;
+    }
+    set_scales(c, np_iteration);
+  }
+  RunArgs a;
+  int r = prepare_run(c, p, &a);
+  if (r) return r;
+  if (c->chunk_open && (a.key0 != c->chunk_key0 || a.key1 != c->chunk_key1))
+    return fail(c, HC3D_ERR_STATE, "the chunks of an iteration must share its seed and iteration number");
+  CK(cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), c->stream));
+  if ((r = run_waves(c, p, a, final != 0))) return r;
+  if ((r = finish_run(c))) return r;
   c->epoch_np += p->np;
   return HC3D_OK;
 }
@@ -1156,17 +1225,35 @@ extern "C" int hc3d_run_batch(hc3d_ctx* const* ctxs, const hc3d_run_params* para
 extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tune_result* out) {
   if (!c || !sample || !out || sample->np <= 0) return HC3D_ERR_INVALID;
   if (!c->tables || !c->grid) return fail(c, HC3D_ERR_STATE, "load tables and grid first");
+  if (c->chunk_open) return fail(c, HC3D_ERR_STATE, "a chunked iteration has packets in flight");
   std::memset(out, 0, sizeof *out);
   const bool waves = sample->ipeel && c->use_waves;
   const int64_t q0 = c->queue_records;
   const int b0 = c->block_size, g0 = c->regen;
-  // time the sample under the context's current settings as candidate k
+  // time the sample under the context's current settings as candidate k.
+  // Peeled runs time it as the middle chunk of an iteration (after a chunk
+  // of the same size that fills the pool; the packets in flight are then
+  // discarded), so that the longest histories' tail does not decide the
+  // choice; other runs time the whole sample.
   auto time_one = [&](int k) -> int {
     int r = hc3d_zero_tallies(c);
-    const auto t0 = std::chrono::steady_clock::now();
-    if (!r) r = hc3d_run_iteration(c, sample);
-    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    double ms = 0.0;
+    if (!r && waves) {
+      hc3d_run_params q = *sample;
+      q.packet_offset = sample->packet_offset + sample->np;
+      r = hc3d_run_chunk(c, sample, 2 * sample->np, 0);
+      const auto t0 = std::chrono::steady_clock::now();
+      if (!r) r = hc3d_run_chunk(c, &q, 2 * sample->np, 0);
+      ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (!r) r = hc3d_zero_tallies(c);
+    } else if (!r) {
+      const auto t0 = std::chrono::steady_clock::now();
+      r = hc3d_run_iteration(c, sample);
+      ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
     if (r) {
+      c->chunk_open = false;
+      c->carry_alive = 0;
       if (c->queue_records != q0) drop_wave(c);
       c->queue_records = q0;
       c->block_size = b0;

@@ -124,6 +124,7 @@ struct RunArgs {
   int64_t n_acc, n_spot;     // ids < n_acc: disk accretion; [n_acc, n_spot): hot spot
   int src_on;                // 1: src holds the accretion and spot constants
   int regen;                 // k_wave regeneration threshold: waiting lanes of a warp before they take new packets
+  int qchunk;                // k_wave: peel-off queue slots a lane reserves at a time
   hc3d_sources src;
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
   const double* aperture2;   // [nap]

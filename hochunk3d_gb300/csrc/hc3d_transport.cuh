@@ -2465,7 +2465,7 @@ struct Slot {
 };
 
 template <class R>
-__global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDims d, RunArgs a, Slot<R>* pool,
+__global__ void __launch_bounds__(128, 3) k_wave(DevModel m, DevTallies t, TallyDims d, RunArgs a, Slot<R>* pool,
                                                PeelRec<R>* queue, unsigned long long* qcount, int E,
                                                unsigned int* alive) {
   extern __shared__ double dust_smem[];
@@ -2491,6 +2491,11 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
   // interactions.  The tallies do not depend on it (each packet's stream is
   // keyed by its id).
   bool done = false;  // the batch has no packet left for this lane
+  // Queue slots are reserved a.qchunk at a time, so that the atomic whose
+  // result addresses the record is paid once per qchunk events (in the tail
+  // of a batch, where a few long histories run alone, it is otherwise a
+  // round trip on every event); slots left over are marked empty at the end.
+  unsigned long long slot = 0ull, slot_end = 0ull;
   for (int nrec = 0; nrec < E; ++nrec) {
     const unsigned waiting = __ballot_sync(0xffffffffu, s.stage == 0 && !done);
     const unsigned busy = __ballot_sync(0xffffffffu, s.stage != 0);
@@ -2506,9 +2511,13 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
       rng_init(rng, a.key0, a.key1, s.pid);
     }
     // The event's record is written field by field into its queue slot as
-    // emission or the interaction produces it: the slot's atomic overlaps
-    // that work, and the record occupies no registers across the walk.
-    PeelRec<R>& rec = queue[atomicAdd(qcount, 1ull)];
+    // emission or the interaction produces it: the record occupies no
+    // registers across the walk.
+    if (slot == slot_end) {
+      slot = atomicAdd(qcount, (unsigned long long)a.qchunk);
+      slot_end = slot + (unsigned long long)a.qchunk;
+    }
+    PeelRec<R>& rec = queue[slot++];
     if (s.stage == 0) {
       if (!emit<R>(m, dv, t, a, s.p, rng, rec, tr, L)) continue;  // dropped: the lane takes the next packet
       s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
@@ -2520,6 +2529,7 @@ __global__ void __launch_bounds__(128) k_wave(DevModel m, DevTallies t, TallyDim
     const int st = walk<R>(m, t, d, a, s.p, rng, s.f, L, tr, s.stage == 2);
     s.stage = st == ST_INTERACT ? 1 : 0;
   }
+  for (; slot < slot_end; ++slot) queue[slot].flags = kRecNoPeel;
   s.c0 = rng.c0;
   s.left = rng.left;
   pool[gid] = s;

@@ -196,6 +196,8 @@ SIGNATURES = {
     "hc3d_load_grid": (C.c_int, [C.c_void_p, P(Grid)]),
     "hc3d_zero_tallies": (C.c_int, [C.c_void_p]),
     "hc3d_set_tdust": (C.c_int, [C.c_void_p, dp]),
+    "hc3d_set_wave_options": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_int]),
+    "hc3d_run_chunk": (C.c_int, [C.c_void_p, P(RunParams), C.c_int64, C.c_int]),
     "hc3d_run_iteration": (C.c_int, [C.c_void_p, P(RunParams)]),
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
@@ -602,6 +604,16 @@ class Context:
         self._check(lib().hc3d_lucy_update(self._h, ltot, int(np_), None if td is None else td.ctypes.data_as(dp),
                                            C.byref(rel), C.byref(conv)))
         return td, rel.value, bool(conv.value)
+
+    def run_chunk(self, params: RunParams, np_iteration: int, final: bool) -> None:
+        """One chunk of a peeled iteration of np_iteration packets (hc3d_run_chunk):
+        with final False the packets still in flight continue in the next chunk."""
+        self._check(lib().hc3d_run_chunk(self._h, C.byref(params), int(np_iteration), 1 if final else 0))
+
+    def set_wave_options(self, queue_records: int = 0, regen: int = 0, qchunk: int = 0) -> None:
+        """Queue depth, regeneration threshold and queue-slot chunk of the
+        wavefront form (hc3d_set_wave_options; 0 keeps a setting)."""
+        self._check(lib().hc3d_set_wave_options(self._h, int(queue_records), int(regen), int(qchunk)))
 
     def autotune(self, sample: RunParams) -> dict:
         """Time the sample batch under each candidate setting and keep the fastest (hc3d_autotune)."""

@@ -255,6 +255,22 @@ int hc3d_zero_tallies(hc3d_ctx *ctx);
  * packets are done. */
 int hc3d_run_iteration(hc3d_ctx *ctx, const hc3d_run_params *params);
 
+/* One chunk of a peeled iteration of np_iteration packets: the packets
+ * [packet_offset, packet_offset + np) of params start here, and with final =
+ * 0 the call returns once all of them have started, leaving the packets
+ * still in flight in the context; they continue in the next chunk.  The
+ * chunk with final = 1 runs every packet to its end.  The chunks of an
+ * iteration share its seed and iteration number and accumulate into the same
+ * tallies (the fixed-point scales are set for np_iteration packets); their
+ * tallies equal those of one hc3d_run_iteration of the whole range, bit for
+ * bit.  A long iteration so runs in steps without paying its last, longest
+ * histories at the end of every step.  hc3d_run_iteration, hc3d_autotune and
+ * hc3d_set_wave_options refuse to run while a chunked iteration is in flight;
+ * hc3d_zero_tallies discards it.  Unpeeled runs finish every packet in each
+ * chunk.  No counterpart in the reference (its loop runs one iteration in one
+ * call). */
+int hc3d_run_chunk(hc3d_ctx *ctx, const hc3d_run_params *params, int64_t np_iteration, int final);
+
 /* Copy the device tallies to the non-NULL host buffers of *out. */
 int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies *out);
 
@@ -281,7 +297,8 @@ int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
 
 /* ---- autotuner (no counterpart in the reference) ---------------------------
  * Times the sample batch under each candidate setting and keeps the fastest
- * in the context.  Peeled runs: the peel-off queue depth (2^20 .. 2^23
+ * in the context (peeled runs: as the second of two such chunks of one
+ * iteration, see hc3d_run_chunk).  Peeled runs: the peel-off queue depth (2^20 .. 2^23
  * records), then at the best depth the regeneration threshold of the
  * wavefront kernel (1, 4, 8, 16: how many lanes of a warp must be waiting
  * before they take new packets).  Other runs: the transport block size (64,
@@ -296,6 +313,13 @@ typedef struct hc3d_tune_result {
   double ms[8];              /* wall time of the sample batch */
 } hc3d_tune_result;
 int hc3d_autotune(hc3d_ctx *ctx, const hc3d_run_params *sample, hc3d_tune_result *out);
+
+/* Set the wavefront form's settings by hand (0 keeps a setting): the
+ * peel-off queue depth in records (>= 1024), the regeneration threshold
+ * (1..32 lanes of a warp) and the queue slots a lane reserves per atomic
+ * (1..64).  None of them changes the tallies.  No counterpart in the
+ * reference. */
+int hc3d_set_wave_options(hc3d_ctx *ctx, int64_t queue_records, int regen, int qchunk);
 
 /* n_iter Lucy iterations of params->np packets without peel-off
  * (newtts.F90:294-330 with a fixed count), captured as one CUDA graph and

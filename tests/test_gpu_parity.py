@@ -282,15 +282,24 @@ def test_lucy_graph_equals_the_step_by_step_loop(model_factory, prec):
 @pytest.mark.parametrize("ipeel", [1, 0])
 def test_autotune_keeps_results(model_factory, ipeel):
     """The autotuner times every candidate and keeps the fastest; the tallies
-    of a batch are the same before and after (queue depth and block size do
+    of a batch are the same before and after, and under every setting by hand
+    (queue depth, regeneration threshold, queue-slot chunk and block size do
     not change any packet's history)."""
     m = model_factory("tiny3d")
     ctx = _ctx(m, hc3d.PREC_MIXED)
     p = m.run_params(np=30000, iter=2, ipeel=ipeel)
     ctx.zero(); ctx.run(p); a = ctx.tallies(p)
     res = ctx.autotune(m.run_params(np=20000, iter=7, ipeel=ipeel))
-    assert len(res["candidates"]) == (4 if ipeel else 3) and all(c["ms"] > 0 for c in res["candidates"])
-    ctx.zero(); ctx.run(p); b = ctx.tallies(p)
+    # peeled: 4 queue depths, then the 3 other regeneration thresholds at the best depth
+    assert len(res["candidates"]) == (7 if ipeel else 3) and all(c["ms"] > 0 for c in res["candidates"])
+    if ipeel:
+        assert {c["regen"] for c in res["candidates"]} == {1, 4, 8, 16}
     keys = ("si", "nums", "nabs", "dtauabs", "jmean", "counters") + (("ti", "numt", "image_i") if ipeel else ())
-    for k in keys:
-        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    settings = [{}] + ([{"queue_records": 1 << 20, "regen": 16, "qchunk": 1},
+                        {"queue_records": 1 << 21, "regen": 4, "qchunk": 32}] if ipeel else [])
+    for opt in settings:
+        if opt:
+            ctx.set_wave_options(**opt)
+        ctx.zero(); ctx.run(p); b = ctx.tallies(p)
+        for k in keys:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=f"{k} {opt}")
