@@ -200,6 +200,11 @@ int alloc_run_tallies(hc3d_ctx* c, const TallyDims& d) {
   if ((r = dalloc(c, c->run_allocs, &c->dt.sed, (size_t)9 * d.nsed))) return r;
   if ((r = dalloc(c, c->run_allocs, &c->dt.psed, (size_t)9 * std::max<int64_t>(d.npsed, 1)))) return r;
   if ((r = dalloc(c, c->run_allocs, &c->dt.img, (size_t)4 * std::max<int64_t>(d.nimg, 1)))) return r;
+  c->dt.cube = nullptr;
+  if (d.ncube > 0) {
+    if ((r = dalloc(c, c->run_allocs, &c->dt.cube, (size_t)(kNo + 3) * d.ncube))) return r;
+    CK(cudaMemsetAsync(c->dt.cube, 0, sizeof(unsigned long long) * (kNo + 3) * d.ncube, c->stream));
+  }
   CK(cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * d.nsed, c->stream));
   CK(cudaMemsetAsync(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(d.npsed, 1), c->stream));
   CK(cudaMemsetAsync(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(d.nimg, 1), c->stream));
@@ -210,7 +215,7 @@ int alloc_run_tallies(hc3d_ctx* c, const TallyDims& d) {
 
 bool same_dims(const TallyDims& a, const TallyDims& b) {
   return a.nfreq == b.nfreq && a.nmu == b.nmu && a.nph == b.nph && a.nap == b.nap && a.npeel == b.npeel &&
-         a.nx == b.nx;
+         a.nx == b.nx && a.ncube == b.ncube;
 }
 
 TallyDims dims_of(const hc3d_run_params* p) {
@@ -221,6 +226,7 @@ TallyDims dims_of(const hc3d_run_params* p) {
   d.nsed = (int64_t)p->nfreq * p->nmu * p->nph * p->nap * kNo;
   d.npsed = (int64_t)p->nfreq * d.npeel * p->nap * kNo;
   d.nimg = (int64_t)d.npeel * p->nxhst * p->nxhst;
+  d.ncube = (p->imcube && p->ipeel && p->image) ? d.nimg * p->nfreq : 0;
   return d;
 }
 
@@ -236,6 +242,8 @@ int check_params(hc3d_ctx* c, const hc3d_run_params* p) {
     if (p->nxhst < 1) return fail(c, HC3D_ERR_INVALID, "nxhst must be >= 1");
   }
   if (p->limb != 0 && p->limb != 1) return fail(c, HC3D_ERR_INVALID, "limb must be 0 or 1");
+  if (p->imcube && p->ipeel && !p->image)
+    return fail(c, HC3D_ERR_INVALID, "imcube needs image = 1 (the cube is binned by image pixel)");
   if (p->limb == 1 && c->tables && c->dm.nlimb < 2)
     return fail(c, HC3D_ERR_INVALID, "limb = 1 needs the limb-darkening table (ntab) of hc3d_load_tables");
   if (!(p->numin > 0.0) || !(p->numax > p->numin)) return fail(c, HC3D_ERR_INVALID, "need 0 < numin < numax");
@@ -305,6 +313,7 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   }
   a->limb = p->limb;
   a->regen = c->regen;
+  a->imcube = d.ncube > 0 ? 1 : 0;
   a->qchunk = c->qchunk;
   // disk accretion and hot-spot packets
   a->n_acc = 0;
@@ -1038,6 +1047,8 @@ extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
     CK(cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * c->dims.nsed, c->stream));
     CK(cudaMemsetAsync(c->dt.psed, 0, sizeof(unsigned long long) * 9 * std::max<int64_t>(c->dims.npsed, 1), c->stream));
     CK(cudaMemsetAsync(c->dt.img, 0, sizeof(unsigned long long) * 4 * std::max<int64_t>(c->dims.nimg, 1), c->stream));
+    if (c->dims.ncube > 0)
+      CK(cudaMemsetAsync(c->dt.cube, 0, sizeof(unsigned long long) * (kNo + 3) * c->dims.ncube, c->stream));
   }
   CK(cudaMemsetAsync(c->dt.counters, 0, sizeof(unsigned long long) * 16, c->stream));
   CK(cudaMemsetAsync(c->dt.fault_count, 0, sizeof(unsigned long long), c->stream));
@@ -1351,6 +1362,14 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
     if (c->dims.nimg > 0)
       for (int k = 0; k < 4; ++k)
         if (im[k]) if (int r_ = d2h(c, im[k], c->dt.img + k * c->dims.nimg, sizeof(int64_t) * c->dims.nimg)) return r_;
+    const int64_t nc = c->dims.ncube;
+    if (nc > 0) {
+      if (out->image_m_i)
+        if (int r_ = d2h(c, out->image_m_i, c->dt.cube, sizeof(int64_t) * kNo * nc)) return r_;
+      int64_t* qv[3] = {out->image_m_q, out->image_m_u, out->image_m_v};
+      for (int k = 0; k < 3; ++k)
+        if (qv[k]) if (int r_ = d2h(c, qv[k], c->dt.cube + (kNo + k) * nc, sizeof(int64_t) * nc)) return r_;
+    }
   }
   const DevModel& m = c->dm;
   const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;

@@ -23,6 +23,7 @@ struct TallyDims {
   int64_t nsed;    // nfreq*nmu*nph*nap*no
   int64_t npsed;   // nfreq*npeel*nap*no
   int64_t nimg;    // npeel*nx*nx
+  int64_t ncube;   // npeel*nx*nx*nfreq with the image cube, else 0
 };
 
 // Device tallies (int64 fixed point).  Grid tallies use the compact cell
@@ -31,6 +32,7 @@ struct DevTallies {
   unsigned long long* sed;    // [9][nsed]: si sq su sv si2 sq2 su2 sv2 nums
   unsigned long long* psed;   // [9][npsed]: ti .. numt
   unsigned long long* img;    // [4][nimg]: I Q U V
+  unsigned long long* cube;   // [kNo + 3][ncube]: I of the kNo SED components, then Q U V (image cube)
   unsigned long long* nabs;   // [kSlots][ncell]
   unsigned long long* dtauabs;// [kSlots][ncell]
   unsigned long long* jmean;  // [ncell]
@@ -125,6 +127,7 @@ struct RunArgs {
   int src_on;                // 1: src holds the accretion and spot constants
   int regen;                 // k_wave regeneration threshold: waiting lanes of a warp before they take new packets
   int qchunk;                // k_wave: peel-off queue slots a lane reserves at a time
+  int imcube;                // 1: tally the per-frequency image cube
   hc3d_sources src;
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
   const double* aperture2;   // [nap]

@@ -898,6 +898,7 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   if (P.has("SEDLMIN")) REQ(P.real("SEDLMIN", &lmin, err));
   if (P.has("SEDLMAX")) REQ(P.real("SEDLMAX", &lmax, err));
   if (P.has("IMAGE")) { REQ(P.integer("IMAGE", &iv, err)); m->image = (int)iv; }
+  if (P.has("IMCUBE")) { REQ(P.integer("IMCUBE", &iv, err)); m->imcube = (int)iv; }  // reapar.f90:472
   if (P.has("MAXINT")) REQ(P.integer("MAXINT", &m->maxint, err));
 
   // ---- setup.f90:26-231 ----
@@ -1440,7 +1441,7 @@ hc3d_run_params Model::params_view() const {
   p.thete = thete.data(); p.phie = phie.data(); p.nfreq = nfreq; p.nmu = nmu; p.nph = nph; p.nap = nap;
   p.nxhst = nxhst; p.rmaxi = rmaxi; p.aperture2 = aperture2.data(); p.numin = numin; p.numax = numax;
   p.rstar_cm = rstar * kRsun; p.tstar = tstar_k / 11605.0; p.limb = limb; p.iintmax = 10000;
-  p.max_interactions = maxint; p.image = image;
+  p.max_interactions = maxint; p.image = image; p.imcube = imcube && ipeel && image ? 1 : 0;
   p.ext_illum = iout; p.rmax = rmax;
   set_shares(&p, np);
   return p;

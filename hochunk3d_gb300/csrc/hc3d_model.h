@@ -102,6 +102,7 @@ struct Model {
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;
   int image = 1;
+  int imcube = 0;  // IMCUBE: the per-frequency image cube of the peeled packets
   int64_t maxint = 1000000;
   uint64_t seed = 0;
   std::string atname, pardir;

@@ -1293,6 +1293,14 @@ __device__ void peel_ray(const DevModel& m, const DevTallies& t, const TallyDims
     atomicAdd(t.img + d.nimg + b, fx(dsqp, t.stokes_scale));
     atomicAdd(t.img + 2 * d.nimg + b, fx(dsup, t.stokes_scale));
     atomicAdd(t.img + 3 * d.nimg + b, fx(dsvp, t.stokes_scale));
+    if (a.imcube) {  // peeloff_3d.f90:271-282: I by the three SED components, Q U V
+      const int64_t bc = b + d.nimg * (int64_t)(inub - 1);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) atomicAdd(t.cube + (int64_t)(indx[q] - 1) * d.ncube + bc, fx(dsip, t.stokes_scale));
+      atomicAdd(t.cube + (int64_t)kNo * d.ncube + bc, fx(dsqp, t.stokes_scale));
+      atomicAdd(t.cube + (int64_t)(kNo + 1) * d.ncube + bc, fx(dsup, t.stokes_scale));
+      atomicAdd(t.cube + (int64_t)(kNo + 2) * d.ncube + bc, fx(dsvp, t.stokes_scale));
+    }
   }
 }
 
@@ -1368,6 +1376,13 @@ __device__ __forceinline__ void peel_tally_mixed(const DevTallies& t, const Tall
     const int64_t b = (int64_t)k + (int64_t)a.npeel * ((ix - 1) + (int64_t)a.nx * (iy - 1));
 #pragma unroll
     for (int j = 0; j < 4; ++j) atomicAdd(t.img + j * d.nimg + b, v[j]);
+    if (a.imcube) {  // peeloff_3d.f90:271-282: I by the three SED components, Q U V
+      const int64_t bc = b + d.nimg * (int64_t)(e.inub - 1);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) atomicAdd(t.cube + (int64_t)(indx[q] - 1) * d.ncube + bc, v[0]);
+#pragma unroll
+      for (int j = 1; j < 4; ++j) atomicAdd(t.cube + (int64_t)(kNo + j - 1) * d.ncube + bc, v[j]);
+    }
   }
 }
 

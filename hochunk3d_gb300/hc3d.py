@@ -102,7 +102,7 @@ class RunParams(C.Structure):
         ("rstar_cm", C.c_double), ("tstar", C.c_double), ("limb", C.c_int), ("iintmax", C.c_int),
         ("max_interactions", C.c_int64), ("image", C.c_int),
         ("ext_illum", C.c_int), ("n_star", C.c_int64), ("rmax", C.c_double),
-        ("n_acc", C.c_int64), ("n_spot", C.c_int64), ("sources", C.POINTER(Sources)),
+        ("n_acc", C.c_int64), ("n_spot", C.c_int64), ("sources", C.POINTER(Sources)), ("imcube", C.c_int),
     ]
 
 
@@ -113,6 +113,7 @@ class Tallies(C.Structure):
                                      "nabs", "dtauabs", "jmean")] + [
         ("killed", i32p), ("dbig", i32p), ("counters", C.c_int64 * 16),
         ("stokes_scale", C.c_double), ("square_scale", C.c_double), ("path_scale", C.c_double),
+        ("image_m_i", i64p), ("image_m_q", i64p), ("image_m_u", i64p), ("image_m_v", i64p),
     ]
 
 
@@ -552,6 +553,10 @@ class Context:
             if params.image:
                 for n in ("image_i", "image_q", "image_u", "image_v"):
                     buf(n, img_shape)
+                if params.imcube:  # (npeel, nx, nx, nfreq, no) and (npeel, nx, nx, nfreq)
+                    buf("image_m_i", img_shape + (params.nfreq, NO))
+                    for n in ("image_m_q", "image_m_u", "image_m_v"):
+                        buf(n, img_shape + (params.nfreq,))
         if grid:
             buf("nabs", (nrg, ntg, npg, ndg))
             buf("dtauabs", (nrg, ntg, npg, ndg))

@@ -180,6 +180,8 @@ typedef struct hc3d_run_params {
   int64_t n_spot;         /* global ids in [n_acc, n_spot) are hot-spot packets (iphot < npacc + npaccstar,
                              newdisktherm.F90:258); needs sources */
   const hc3d_sources *sources; /* accretion and spot constants; NULL = neither (n_acc = n_spot = 0) */
+  int imcube;             /* 1 = also the per-frequency image cube image_m_* of the peeled packets
+                             (IMCUBE, peeloff_3d.f90:271-282) in runs with ipeel = 1; needs image */
 } hc3d_run_params;
 
 /* Host copies of the device tallies.  Any pointer may be NULL.  Shapes are
@@ -201,6 +203,9 @@ typedef struct hc3d_tallies {
   double stokes_scale;             /* fixed-point scale of Stokes sums and images */
   double square_scale;             /* fixed-point scale of squared Stokes sums */
   double path_scale;               /* fixed-point scale of dtauabs and jmean */
+  int64_t *image_m_i;              /* (npeel,nxhst,nxhst,nfreq,no) per-frequency image cube, x stokes_scale
+                                      (runs with imcube) */
+  int64_t *image_m_q, *image_m_u, *image_m_v; /* (npeel,nxhst,nxhst,nfreq), x stokes_scale */
 } hc3d_tallies;
 
 /* counters[] of hc3d_tallies (newdisktherm.F90:122-141, propagate.f90:296-318) */

@@ -660,6 +660,15 @@ static void orc_peeloff(const orc_ctx *c, const hc3d_run_params *rp, const pkt *
     int64_t b = (int64_t)peelid + (int64_t)rp->npeel * ((ix - 1) + (int64_t)rp->nxhst * (iy - 1));
     t->fx.image_i[b] += fx_round(sip, ss); t->fx.image_q[b] += fx_round(sqp, ss);
     t->fx.image_u[b] += fx_round(sup, ss); t->fx.image_v[b] += fx_round(svp, ss);
+    if (rp->imcube && t->fx.image_m_i) {
+      /* peeloff_3d.f90:271-282: image_m_i(peelid,ix,iy,inub,indx), image_m_q/u/v(peelid,ix,iy,inub) */
+      const int64_t nim = (int64_t)rp->npeel * rp->nxhst * rp->nxhst, nc = nim * rp->nfreq;
+      const int64_t bc = b + nim * (int64_t)(inub - 1);
+      for (int k = 0; k < 3; ++k) t->fx.image_m_i[bc + nc * (indx[k] - 1)] += fx_round(sip, ss);
+      t->fx.image_m_q[bc] += fx_round(sqp, ss);
+      t->fx.image_m_u[bc] += fx_round(sup, ss);
+      t->fx.image_m_v[bc] += fx_round(svp, ss);
+    }
     if (t->image_i_d) t->image_i_d[b] += sip;
     if (t->image_m2_d) {
       const int64_t n = (int64_t)rp->npeel * rp->nxhst * rp->nxhst;

@@ -91,6 +91,10 @@ class OracleTallies:
             self._add(T.fx, n, self.psed_shape)
         for n in ("image_i", "image_q", "image_u", "image_v"):
             self._add(T.fx, n, self.img_shape)
+        if params.imcube:
+            self._add(T.fx, "image_m_i", self.img_shape + (params.nfreq, NO))
+            for n in ("image_m_q", "image_m_u", "image_m_v"):
+                self._add(T.fx, n, self.img_shape + (params.nfreq,))
         self._add(T.fx, "nabs", self.g4)
         self._add(T.fx, "dtauabs", self.g4)
         self._add(T.fx, "jmean", self.g3)
