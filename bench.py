@@ -653,6 +653,12 @@ def main():
                          "distribution is 1e6,1e8; the default is scaled down to keep the benchmark to minutes)")
     ap.add_argument("--grid-only", action="store_true",
                     help="run only the model-grid measurement (one-off runs at the distribution's photon counts)")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="run only the serving measurement (one-off runs at larger requests)")
+    ap.add_argument("--serve-requests", type=int, default=60, help="requests of the serving measurement")
+    ap.add_argument("--serve-packets", type=int, default=20000,
+                    help="packets of each request's Lucy and peeled iterations (the model-grid distribution is "
+                         "1e6..1e8; the default is scaled down to keep the benchmark to minutes)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default peel-off queue depth")
     ap.add_argument("--profile-chunks", type=int, default=0,
                     help="run this many untimed chunks of one peeled iteration after the set-up (no drain) and "
@@ -683,6 +689,13 @@ def main():
         build_oracle()
     if world > 1:
         torch.distributed.barrier()
+
+    if args.serve_only:
+        with tempfile.TemporaryDirectory() as td:
+            res = serving_latency(Path(td), local, n=args.serve_requests, np_req=args.serve_packets)
+        if rank == 0:
+            print(json.dumps({"serving": res}))
+        return
 
     if args.grid_only:
         with tempfile.TemporaryDirectory() as td:
@@ -949,7 +962,7 @@ def main():
             lo, hi = (float(v) for v in args.grid_packets.split(","))
             grid_runs = model_grid_throughput(Path(td), local, n=args.grid_models, np_lo=lo, np_hi=hi,
                                               one_at_a_time=hi <= 1e6)
-            serving = serving_latency(Path(td), local)
+            serving = serving_latency(Path(td), local, n=args.serve_requests, np_req=args.serve_packets)
         if rank == 0:
             line = {"metric": METRIC, "value": value, "unit": "packets/s", "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
