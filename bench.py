@@ -309,6 +309,34 @@ def model_grid_throughput(tmp: Path, device: int, n: int = 12, slots: int = 4, n
     return out
 
 
+def lucy_scale(tmp: Path, device: int, n_iter: int, np_: int) -> dict:
+    """The Lucy-scale workload (400 x 399 x 128 cells, 100 frequencies): n_iter
+    unpeeled Lucy iterations of np_ packets from the reference's starting
+    temperatures (0.1 K), as one CUDA graph (hc3d_lucy_iterations), with the
+    convergence maximum max dT/T of each iteration."""
+    import torch
+
+    from hochunk3d_gb300 import hc3d
+
+    model = build_model(tmp, "lucy")
+    ctx = hc3d.Context(hc3d.PREC_MIXED, device=device).load(model)
+    warm = model.run_params(np=20000, iter=900, ipeel=0)  # loads the kernels; untimed
+    ctx.zero()
+    ctx.run(warm)
+    ctx.set_tdust(model.tdust)
+    p = model.run_params(np=np_, iter=1, ipeel=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, rel = ctx.lucy_iterations(p, n_iter, model.info.ltot, want_tdust=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    ctx.close()
+    return {"workload": "lucy", "grid": [int(v) for v in model.shape4[:3]], "cells": int(model.info.ncells),
+            "iterations": n_iter, "packets_per_iteration": np_, "seconds": dt,
+            "packets_per_s": n_iter * np_ / dt, "max_rel_change_per_iteration": [float(v) for v in rel],
+            "note": "one CUDA graph of n iterations (tally reset, packet loop, tfinal); temperatures from 0.1 K"}
+
+
 def serving_latency(tmp: Path, device: int, n: int = 60, rate: float = 20.0, slots: int = 8, np_req: int = 20000):
     """Requests of models of the model-grid distribution, each asking for its
     SED and three peel-off inclinations (one Lucy iteration of np_req
@@ -653,6 +681,10 @@ def main():
                          "distribution is 1e6,1e8; the default is scaled down to keep the benchmark to minutes)")
     ap.add_argument("--grid-only", action="store_true",
                     help="run only the model-grid measurement (one-off runs at the distribution's photon counts)")
+    ap.add_argument("--lucy-scale", type=int, default=0,
+                    help="run only the Lucy-scale measurement: this many Lucy iterations of --lucy-scale-packets "
+                         "as one CUDA graph (the configuration's 10 x 1e8)")
+    ap.add_argument("--lucy-scale-packets", type=int, default=100_000_000)
     ap.add_argument("--serve-only", action="store_true",
                     help="run only the serving measurement (one-off runs at larger requests)")
     ap.add_argument("--serve-requests", type=int, default=60, help="requests of the serving measurement")
@@ -689,6 +721,13 @@ def main():
         build_oracle()
     if world > 1:
         torch.distributed.barrier()
+
+    if args.lucy_scale > 0:
+        with tempfile.TemporaryDirectory() as td:
+            res = lucy_scale(Path(td), local, args.lucy_scale, args.lucy_scale_packets)
+        if rank == 0:
+            print(json.dumps({"lucy_scale": res}))
+        return
 
     if args.serve_only:
         with tempfile.TemporaryDirectory() as td:

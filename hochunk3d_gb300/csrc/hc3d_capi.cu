@@ -60,6 +60,8 @@ struct hc3d_ctx {
   WaveBufs wave{};
   int64_t pool_threads = 0, qcap = 0;
   int wave_blocks = 0, peel_blocks = 0;
+  int peel_variant = 0;                   // block shape of the mixed-form peel-off kernel
+  int peel_blocks_v[kPeelVariants] = {};  // its persistent grid per shape
   int64_t queue_records = 1 << 22;  // peel-off events held per wave
   int regen = 1;                    // k_wave regeneration threshold (lanes of a warp)
   // a peeled iteration run in chunks (hc3d_run_chunk): packets in flight stay in the pool
@@ -373,8 +375,13 @@ int ensure_wave(hc3d_ctx* c) {
   c->wave_blocks = c->sm_count * per_sm;
   c->pool_threads = (int64_t)c->wave_blocks * 128;
   int per_sm_p = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, f64 ? peel_fn_fp64() : peel_fn_mixed(), 256, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_p, f64 ? peel_fn_fp64() : peel_fn_mixed(0), 256, 0));
   c->peel_blocks = c->sm_count * std::max(1, per_sm_p);
+  for (int v = 0; v < kPeelVariants; ++v) {
+    int k = 0;
+    if (!f64) CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, peel_fn_mixed(v), peel_threads_mixed(v), 0));
+    c->peel_blocks_v[v] = c->sm_count * std::max(1, k);
+  }
   // room for every thread's qchunk reserved slots on top of one record each (see run_waves' E)
   c->qcap = std::max<int64_t>(c->queue_records, c->pool_threads * (int64_t)(c->qchunk + 1));
   const size_t slot = f64 ? slot_bytes_fp64() : slot_bytes_mixed();
@@ -426,6 +433,11 @@ int run_waves(hc3d_ctx* c, const hc3d_run_params* p, const RunArgs& a, bool drai
   if (c->chunk_open) alive_prev = c->carry_alive;
   else CK(cudaMemsetAsync(c->wave.pool, 0, slot * (size_t)c->pool_threads, c->stream));
   LaunchCfg wc{c->wave_blocks, 128, c->stream}, pc{c->peel_blocks, 256, c->pstream};
+  if (!f64) {
+    pc.variant = c->peel_variant;
+    pc.threads = peel_threads_mixed(c->peel_variant);
+    pc.blocks = c->peel_blocks_v[c->peel_variant];
+  }
   unsigned long long work = 0, events_prev = 0;
   CK(cudaMemcpyAsync(&events_prev, c->dt.counters + HC3D_CNT_EVENTS, sizeof(events_prev), cudaMemcpyDeviceToHost,
                      c->stream));
@@ -989,8 +1001,10 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   return hc3d_zero_tallies(c);
 }
 
-extern "C" int hc3d_set_wave_options(hc3d_ctx* c, int64_t queue_records, int regen, int qchunk) {
-  if (!c || queue_records < 0 || regen < 0 || regen > 32 || qchunk < 0 || qchunk > 64) return HC3D_ERR_INVALID;
+extern "C" int hc3d_set_wave_options(hc3d_ctx* c, int64_t queue_records, int regen, int qchunk, int peel_shape) {
+  if (!c || queue_records < 0 || regen < 0 || regen > 32 || qchunk < 0 || qchunk > 64 || peel_shape < 0 ||
+      peel_shape > kPeelVariants)
+    return HC3D_ERR_INVALID;
   if (c->chunk_open) return fail(c, HC3D_ERR_STATE, "a chunked iteration has packets in flight");
   if (queue_records > 0 && queue_records < 1024) return fail(c, HC3D_ERR_INVALID, "queue_records < 1024");
   if ((queue_records && queue_records != c->queue_records) || (qchunk && qchunk != c->qchunk)) {
@@ -999,6 +1013,7 @@ extern "C" int hc3d_set_wave_options(hc3d_ctx* c, int64_t queue_records, int reg
     if (qchunk) c->qchunk = qchunk;
   }
   if (regen) c->regen = regen;
+  if (peel_shape) c->peel_variant = peel_shape - 1;
   return HC3D_OK;
 }
 
@@ -1240,7 +1255,7 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
   std::memset(out, 0, sizeof *out);
   const bool waves = sample->ipeel && c->use_waves;
   const int64_t q0 = c->queue_records;
-  const int b0 = c->block_size, g0 = c->regen;
+  const int b0 = c->block_size, g0 = c->regen, v0 = c->peel_variant;
   // time the sample under the context's current settings as candidate k.
   // Peeled runs time it as the middle chunk of an iteration (after a chunk
   // of the same size that fills the pool; the packets in flight are then
@@ -1269,11 +1284,14 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
       c->queue_records = q0;
       c->block_size = b0;
       c->regen = g0;
+      c->peel_variant = v0;
       return r;
     }
     out->queue_records[k] = c->queue_records;
     out->block_size[k] = c->block_size;
     out->regen[k] = c->regen;
+    out->peel_shape[k] = c->peel_variant;
+    out->peel_threads[k] = c->precision == HC3D_PREC_MIXED ? peel_threads_mixed(c->peel_variant) : 256;
     out->ms[k] = ms;
     if (k == 0 || ms < out->ms[out->best]) out->best = k;
     return HC3D_OK;
@@ -1299,6 +1317,15 @@ extern "C" int hc3d_autotune(hc3d_ctx* c, const hc3d_run_params* sample, hc3d_tu
       if ((r = time_one(n++))) return r;
     }
     c->regen = out->regen[out->best];
+    if (c->precision == HC3D_PREC_MIXED) {
+      // the peel-off kernel's block shape at the best depth and threshold
+      for (int v = 0; v < kPeelVariants; ++v) {
+        if (v == out->peel_shape[out->best]) continue;
+        c->peel_variant = v;
+        if ((r = time_one(n++))) return r;
+      }
+      c->peel_variant = out->peel_shape[out->best];
+    }
   } else {
     const int blocks[3] = {64, 96, 128};
     for (int k = 0; k < 3; ++k, ++n) {

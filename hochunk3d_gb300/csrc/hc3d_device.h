@@ -141,7 +141,10 @@ struct RunArgs {
 struct LaunchCfg {
   int blocks, threads;
   cudaStream_t stream;
+  int variant = 0;  // block shape of the mixed-form peel-off kernel (see peel_threads_mixed)
 };
+
+constexpr int kPeelVariants = 3;  // block shapes of the mixed-form peel-off kernel
 
 // entry points of the two instantiations
 cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
@@ -175,7 +178,8 @@ size_t rec_bytes_mixed();
 size_t rec_bytes_fp64();
 const void* wave_fn_mixed();
 const void* wave_fn_fp64();
-const void* peel_fn_mixed();
+const void* peel_fn_mixed(int variant);
+int peel_threads_mixed(int variant);
 const void* peel_fn_fp64();
 
 // One model of a batched launch: its device model (dust tables read from

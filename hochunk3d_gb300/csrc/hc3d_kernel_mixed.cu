@@ -39,16 +39,36 @@ cudaError_t launch_wave_transport_mixed(const DevModel& m, const DevTallies& t, 
   return cudaGetLastError();
 }
 
+// the block shapes of k_peel_mixed: (threads, blocks per SM at launch bounds)
+constexpr int kPeelShapes[kPeelVariants][2] = {{256, 2}, {128, 4}, {256, 3}};
+
 cudaError_t launch_wave_peel_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                    const WaveBufs& w, int q, const LaunchCfg& cfg) {
-  dev::k_peel_mixed<float><<<cfg.blocks, dev::kPeelThreads, 0, cfg.stream>>>(
-      m, t, d, a, static_cast<const dev::PeelRec<float>*>(w.queue[q]), w.qcount[q], w.next_ray[q]);
+  const auto* qu = static_cast<const dev::PeelRec<float>*>(w.queue[q]);
+  switch (cfg.variant) {
+    case 1:
+      dev::k_peel_mixed<float, 128, 4><<<cfg.blocks, 128, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
+      break;
+    case 2:
+      dev::k_peel_mixed<float, 256, 3><<<cfg.blocks, 256, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
+      break;
+    default:
+      dev::k_peel_mixed<float, 256, 2><<<cfg.blocks, 256, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
+  }
   return cudaGetLastError();
 }
+
+int peel_threads_mixed(int variant) { return kPeelShapes[variant < 0 || variant >= kPeelVariants ? 0 : variant][0]; }
 
 size_t slot_bytes_mixed() { return sizeof(dev::Slot<float>); }
 size_t rec_bytes_mixed() { return sizeof(dev::PeelRec<float>); }
 const void* wave_fn_mixed() { return (const void*)dev::k_wave<float>; }
-const void* peel_fn_mixed() { return (const void*)dev::k_peel_mixed<float>; }
+const void* peel_fn_mixed(int variant) {
+  switch (variant) {
+    case 1: return (const void*)dev::k_peel_mixed<float, 128, 4>;
+    case 2: return (const void*)dev::k_peel_mixed<float, 256, 3>;
+    default: return (const void*)dev::k_peel_mixed<float, 256, 2>;
+  }
+}
 
 }  // namespace hc3d

@@ -2614,19 +2614,22 @@ static __device__ __noinline__ int prep_rays(const DevModel& m, const PeelRec<fl
   return __popc(okm);
 }
 
-// Two blocks per SM: the walk state of a lane, the set-up stack and the
-// 32-ray tally need about 114 registers; at three blocks (80 registers) the
-// compiler kept part of the walk state in local memory inside the loop.
-template <class R>
-__global__ void __launch_bounds__(kPeelThreads, 2) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
-                                                                  const PeelRec<R>* queue,
-                                                                  const unsigned long long* qcount,
-                                                                  unsigned long long* next_ray) {
+// Instantiated for three block shapes, among which the autotuner picks:
+// 256 threads x 2 blocks per SM and 128 x 4 (the walk state of a lane, the
+// set-up stack and the 32-ray tally need about 118 registers), and 256 x 3
+// (85 registers: part of the walk state goes to local memory).  The smaller
+// blocks retire one by one as the ray pool drains, so the next wave's
+// transport blocks find room sooner.
+template <class R, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
+                                                              const PeelRec<R>* queue,
+                                                              const unsigned long long* qcount,
+                                                              unsigned long long* next_ray) {
   static_assert(sizeof(R) == 4, "the warp-synchronous ray pool is the mixed form");
   __shared__ PeelDir dirs[kMaxPeel];
-  __shared__ PeelEsc esc[kPeelThreads / 32][kPeelBuf];
-  __shared__ PeelRec<float> stage[kPeelThreads / 32][kPeelStage];
-  __shared__ PeelStart prep[kPeelThreads / 32][32];
+  __shared__ PeelEsc esc[THREADS / 32][kPeelBuf];
+  __shared__ PeelRec<float> stage[THREADS / 32][kPeelStage];
+  __shared__ PeelStart prep[THREADS / 32][32];
   static_assert(sizeof(PeelRec<float>) % 4 == 0, "records are staged as 32-bit words");
   for (int k = threadIdx.x; k < a.npeel; k += blockDim.x) dirs[k] = peel_dir(a, k);
   __syncthreads();

@@ -160,8 +160,9 @@ class TtsStats(C.Structure):
 
 
 class TuneResult(C.Structure):
-    _fields_ = [("n", C.c_int), ("best", C.c_int), ("queue_records", C.c_int64 * 8), ("block_size", C.c_int * 8),
-                ("regen", C.c_int * 8), ("ms", C.c_double * 8)]
+    _fields_ = [("n", C.c_int), ("best", C.c_int), ("queue_records", C.c_int64 * 12), ("block_size", C.c_int * 12),
+                ("regen", C.c_int * 12), ("peel_shape", C.c_int * 12), ("peel_threads", C.c_int * 12),
+                ("ms", C.c_double * 12)]
 
 
 class ServerOpts(C.Structure):
@@ -197,7 +198,7 @@ SIGNATURES = {
     "hc3d_load_grid": (C.c_int, [C.c_void_p, P(Grid)]),
     "hc3d_zero_tallies": (C.c_int, [C.c_void_p]),
     "hc3d_set_tdust": (C.c_int, [C.c_void_p, dp]),
-    "hc3d_set_wave_options": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_int]),
+    "hc3d_set_wave_options": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int]),
     "hc3d_run_chunk": (C.c_int, [C.c_void_p, P(RunParams), C.c_int64, C.c_int]),
     "hc3d_run_iteration": (C.c_int, [C.c_void_p, P(RunParams)]),
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
@@ -615,17 +616,20 @@ class Context:
         with final False the packets still in flight continue in the next chunk."""
         self._check(lib().hc3d_run_chunk(self._h, C.byref(params), int(np_iteration), 1 if final else 0))
 
-    def set_wave_options(self, queue_records: int = 0, regen: int = 0, qchunk: int = 0) -> None:
-        """Queue depth, regeneration threshold and queue-slot chunk of the
-        wavefront form (hc3d_set_wave_options; 0 keeps a setting)."""
-        self._check(lib().hc3d_set_wave_options(self._h, int(queue_records), int(regen), int(qchunk)))
+    def set_wave_options(self, queue_records: int = 0, regen: int = 0, qchunk: int = 0, peel_shape: int = 0) -> None:
+        """Queue depth, regeneration threshold, queue-slot chunk and peel-off
+        block shape (1..3) of the wavefront form (hc3d_set_wave_options; 0
+        keeps a setting)."""
+        self._check(lib().hc3d_set_wave_options(self._h, int(queue_records), int(regen), int(qchunk),
+                                                int(peel_shape)))
 
     def autotune(self, sample: RunParams) -> dict:
         """Time the sample batch under each candidate setting and keep the fastest (hc3d_autotune)."""
         r = TuneResult()
         self._check(lib().hc3d_autotune(self._h, C.byref(sample), C.byref(r)))
         return {"candidates": [{"queue_records": int(r.queue_records[k]), "block_size": int(r.block_size[k]),
-                                "regen": int(r.regen[k]), "ms": float(r.ms[k])} for k in range(r.n)],
+                                "regen": int(r.regen[k]), "peel_shape": int(r.peel_shape[k]),
+                                "peel_threads": int(r.peel_threads[k]), "ms": float(r.ms[k])} for k in range(r.n)],
                 "best": int(r.best)}
 
     def lucy_iterations(self, params: RunParams, n_iter: int, ltot: float, want_tdust: bool = True):

@@ -306,25 +306,30 @@ int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
  * iteration, see hc3d_run_chunk).  Peeled runs: the peel-off queue depth (2^20 .. 2^23
  * records), then at the best depth the regeneration threshold of the
  * wavefront kernel (1, 4, 8, 16: how many lanes of a warp must be waiting
- * before they take new packets).  Other runs: the transport block size (64,
- * 96, 128).  The settings do not change the tallies.  The tallies are zeroed
- * afterwards. */
+ * before they take new packets), then in the mixed form the block shape of
+ * the peel-off kernel (256 or 128 threads at the same registers, or 256 at
+ * fewer registers and three blocks per SM).  Other runs: the transport block
+ * size (64, 96, 128).  The settings do not change the tallies.  The tallies
+ * are zeroed afterwards. */
 typedef struct hc3d_tune_result {
-  int n;                     /* candidates timed */
-  int best;                  /* index of the setting the context now uses */
-  int64_t queue_records[8];  /* per candidate */
-  int block_size[8];
-  int regen[8];
-  double ms[8];              /* wall time of the sample batch */
+  int n;                      /* candidates timed */
+  int best;                   /* index of the setting the context now uses */
+  int64_t queue_records[12];  /* per candidate */
+  int block_size[12];         /* transport block size */
+  int regen[12];
+  int peel_shape[12];         /* block shape index of the peel-off kernel */
+  int peel_threads[12];       /* its threads per block */
+  double ms[12];              /* wall time of the sample batch */
 } hc3d_tune_result;
 int hc3d_autotune(hc3d_ctx *ctx, const hc3d_run_params *sample, hc3d_tune_result *out);
 
 /* Set the wavefront form's settings by hand (0 keeps a setting): the
  * peel-off queue depth in records (>= 1024), the regeneration threshold
- * (1..32 lanes of a warp) and the queue slots a lane reserves per atomic
- * (1..64).  None of them changes the tallies.  No counterpart in the
- * reference. */
-int hc3d_set_wave_options(hc3d_ctx *ctx, int64_t queue_records, int regen, int qchunk);
+ * (1..32 lanes of a warp), the queue slots a lane reserves per atomic
+ * (1..64) and the mixed-form peel-off kernel's block shape (1: 256 threads,
+ * 2 blocks per SM; 2: 128 threads, 4 blocks; 3: 256 threads, 3 blocks).
+ * None of them changes the tallies.  No counterpart in the reference. */
+int hc3d_set_wave_options(hc3d_ctx *ctx, int64_t queue_records, int regen, int qchunk, int peel_shape);
 
 /* n_iter Lucy iterations of params->np packets without peel-off
  * (newtts.F90:294-330 with a fixed count), captured as one CUDA graph and
