@@ -2,15 +2,18 @@
 
 Workload: the full-3D precision model (grid 400 x 199 x 64 with a seeded
 3-level fractal envelope, 80 peel-off directions = 20 inclinations x 4
-azimuths, 301^2 broadband Stokes I,Q,U,V images, 50 wavelength bins).  Its
-temperatures are first brought up by two Lucy iterations (untimed set-up).
-One step is one call of disk() for the final, peeled iteration on a batch of
-packets: zero the tallies, run the packet loop, solve the Lucy temperatures.
+azimuths, 301^2 broadband Stokes I,Q,U,V images, 50 wavelength bins), on a
+Lucy temperature field (two GPU Lucy iterations, averaged over azimuth and
+committed; the CPU reference arm uses the same field).  The steps are chunks
+of one final, peeled iteration (hc3d_run_chunk): each starts its batch of
+packets, the packets in flight carry over to the next step, and the last
+timed step runs them all to their end and solves tfinal, so the timed steps
+pay for every history of their packets.
 
   value  packets/s with the model resident in HBM (CUDA events on the
          library's stream around each step; L2 flushed between steps)
-  e2e    the same through the C-ABI with host buffers: run parameters in,
-         every tally and the temperature grid back to host each step
+  e2e    the same through the C-ABI with host buffers, as a second chunked
+         iteration: run parameters in, every tally back to host each step
   roofline  the dominant kernel (transport k_wave or peel-off k_peel_mixed):
          algorithmic bytes per launch (propagation crossings x (4S+16) B, or
          peel crossings x 4S B; S = 3 active species) over its event-timed
@@ -812,44 +815,45 @@ def main():
             ctx.close()
             return
 
-        # The timed steps are chunks of one peeled iteration (hc3d_run_chunk):
-        # step s starts packets [s n, (s+1) n) and returns once all of them
-        # have started; the packets still in flight (the long random walks in
-        # the disk) continue in the next step.  So a step costs what n packets
-        # cost inside a long iteration, as in the published run's 1e8-packet
-        # iteration, instead of charging the longest histories' tail to every
-        # step.  The iteration's last chunk runs the remaining packets to their
-        # end; it is timed apart, with the iteration's tfinal.
+        # The steps are chunks of one peeled iteration (hc3d_run_chunk): step s
+        # starts packets [s n, (s+1) n) and returns once all of them have
+        # started; the packets still in flight (the long random walks in the
+        # disk) continue in the next step.  The last timed step ends the
+        # iteration: it runs every packet still in flight -- those of the
+        # warm-up steps too -- to its end and solves tfinal.  So the timed
+        # steps carry the whole cost of their packets, the longest histories
+        # included, once per iteration as in the published run's 1e8-packet
+        # iteration, instead of once per step.
         n = args.packets
-        chunks_total = args.warmup + args.steps + max(2, args.steps // 2)
-        np_it = n * world * chunks_total
         it_no = 300
-        ctx.zero()
 
-        def chunk(s_, final=False, n_=None):
-            q = model.run_params(np_total=np_it, np=n if n_ is None else n_, iter=it_no, ipeel=1,
+        def chunk(np_it, s_, final=False, n_=None, it_=it_no):
+            q = model.run_params(np_total=np_it, np=n if n_ is None else n_, iter=it_, ipeel=1,
                                  packet_offset=(s_ * world + rank) * n)
             ctx.run_chunk(q, np_it, final)
             return q
 
-        t_it0 = time.perf_counter()
+        np_it = n * world * (args.warmup + args.steps)
+        ctx.zero()
         for w in range(args.warmup):
-            chunk(w)
+            chunk(np_it, w)
         ev = []
         kern_ms = []
         c_prev = ctx.tallies(model.run_params(np=n, ipeel=1), grid=False)["counters"]
-        cross_prop = cross_peel = 0
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         with ClockSampler(local) as clk:
             for s in range(args.steps):
+                last = s == args.steps - 1
                 flush.zero_()
                 torch.cuda.synchronize()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                chunk(args.warmup + s)
+                chunk(np_it, args.warmup + s, final=last)
+                if last:
+                    ctx.lucy_update(model.info.ltot, np_it, want_tdust=False)
                 e1.record(stream)
                 e1.synchronize()
                 ev.append(e0.elapsed_time(e1))
@@ -864,36 +868,33 @@ def main():
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             step_ms = float(t.item())
         value = n * world / (step_ms / 1000.0)
+        steps_detail = {"first_steps_ms": [round(v, 1) for v in ev[:3]], "last_step_ms": round(ev[-1], 1),
+                        "note": "the last step runs the iteration's packets in flight to their end and tfinal"}
+        restore()
 
-        # end to end through the C-ABI with host buffers: the step's run
-        # parameters in (peel-off directions, apertures), the tallies out
+        # end to end through the C-ABI with host buffers: a second chunked
+        # iteration of max(2, steps/2) steps, each with the step's run
+        # parameters in (peel-off directions, apertures) and the tallies out,
+        # its last step ending the iteration
         e2e_times = []
         h2d = d2h = 0
-        for s in range(max(2, args.steps // 2)):
+        k2 = max(2, args.steps // 2)
+        np_it2 = n * world * k2
+        ctx.zero()
+        for s in range(k2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            q = chunk(args.warmup + args.steps + s)
+            q = chunk(np_it2, s, final=s == k2 - 1, it_=it_no + 1)
             T = ctx.tallies(q, grid=False)
+            if s == k2 - 1:
+                ctx.lucy_update(model.info.ltot, np_it2, want_tdust=False)
             torch.cuda.synchronize()
             e2e_times.append(time.perf_counter() - t0)
             d2h = sum(v.nbytes for k, v in T.items() if isinstance(v, np.ndarray))
             h2d = 8 * 4 * model.npeel + 8 * len(model.aperture2)
         e2e = n * world / (sum(e2e_times) / len(e2e_times))
-        # the iteration's end: the packets still in flight run out, then tfinal
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        chunk(chunks_total, final=True, n_=0)
-        ctx.lucy_update(model.info.ltot, np_it, want_tdust=False)
-        e1.record(stream)
-        e1.synchronize()
-        drain_ms = e0.elapsed_time(e1)
-        it_s = time.perf_counter() - t_it0
-        iteration = {"packets": np_it, "chunks": chunks_total, "seconds": it_s, "packets_per_s": np_it / it_s,
-                     "drain_and_tfinal_ms": drain_ms,
-                     "note": "the whole chunked iteration on the host clock: warm-up, timed and e2e chunks, "
-                             "the last chunk (packets in flight run to their end) and tfinal"}
+        iteration = {"packets": np_it, "timed_steps_packets": n * world * args.steps,
+                     "warmup_steps_packets": n * world * args.warmup}
         restore()
 
         # the published run's whole peeled iteration in one call (full-3D: 1e8
@@ -1011,7 +1012,9 @@ def main():
                                "peel_directions": int(model.npeel), "image": [int(model._p.nxhst)] * 2 + [4],
                                "nfreq": int(model._p.nfreq), "packets_per_step": n,
                                "step": f"a chunk of one peeled iteration of {np_it} packets: {n} packets start "
-                                       "in the step; packets in flight at its end continue in the next step",
+                                       "in the step, packets in flight at its end continue in the next step, and "
+                                       "the last step runs them all to their end and solves tfinal",
+                               "steps_detail": steps_detail,
                                "l2": "256 MiB buffer written between timed steps",
                                "temperatures": steps_desc + " (constant over the iteration; tfinal after it)",
                                "autotune": tune},

@@ -2344,6 +2344,28 @@ __device__ __forceinline__ int walk(const DevModel& m, const DevTallies& t, cons
   return ST_INTERACT;
 }
 
+// Mixed form: the peel-off rays of an event deep in an optically thick cell
+// all end inside it.  With s the packet's safe distance (a lower bound on the
+// distance to every wall of the cell) and k the peel-masked opacity of the
+// cell at the event's frequency, every ray's optical depth at its first wall
+// is at least k s; the walk ends a ray whose depth passes taumax = 25
+// (peeloff_3d.f90:118) and tallies nothing for it.  When k s exceeds taumax
+// by 1 %, and s is large against the FP32 resolution of the ray parameter
+// (about 2^-23 |x|), the walk would end every ray at its first wall: the
+// record is marked empty and no ray is walked.  The tallies are unchanged;
+// the peel-off ray and crossing counters count only the rays walked.
+template <class R>
+__device__ __forceinline__ void cull_deep_peel(const DevModel& m, const Pkt<R>& p, int64_t c, PeelRec<R>& rec) {
+  if constexpr (sizeof(R) == 4) {
+    if (p.safe > 0.f) {
+      const float4 q = __ldg(m.rho4p + c);
+      const float op = fmaf(p.kapd[0], q.x, fmaf(p.kapd[1], q.y, fmaf(p.kapd[2], q.z, p.kapd[3] * q.w)));
+      const float r = fabsf(p.x.hi) + fabsf(p.y.hi) + fabsf(p.z.hi);
+      if (p.safe * op > 1.01f * (float)kTauMax && p.safe > r * 1.220703125e-4f) rec.flags |= kRecNoPeel;
+    }
+  }
+}
+
 // One interaction, propagate.f90:70-166: scattering (rec = the state before
 // stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
 template <class R>
@@ -2359,6 +2381,7 @@ __device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& d
   if (ran<R>(rng) <= pick4(p.albedo, idust2)) {  // scattered
     f.iflag = 1; f.iscat++; f.iint++;
     make_rec<R>(rec, p, a, 1, idust2);
+    cull_deep_peel<R>(m, p, c, rec);
     stokes<R>(p, idust2, rng);
     tr.add(5, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
@@ -2376,6 +2399,7 @@ __device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& d
     f.iflag = 0;
     opacset<R>(m, dv, p, p.nub, a);
     make_rec<R>(rec, p, a, 0, idust2);
+    cull_deep_peel<R>(m, p, c, rec);
     f.iint++;
     tr.add(6, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   }
