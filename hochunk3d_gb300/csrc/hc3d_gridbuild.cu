@@ -89,9 +89,17 @@ __device__ double densdisk_dev(const DensParams& P, double rad, double sint, dou
   if (rcoord < P.rgapd2) gapcurve = 0.0;
   double spiral = 1.0;
   if (P.ispiral == 1) {
+    // single-precision factors and phase, integer power by squaring (as the host build)
     double sfact = 1.0;
-    for (int is = 2; is <= P.sn; is += 2) sfact = sfact * ((double)is / ((double)is - 1.0));
-    spiral = 1.0 - P.sw + sfact * P.sw * pow(sin(log(rcoord) / tan(P.pitch) - phi + 0.7854), (double)P.sn);
+    for (int is = 2; is <= P.sn; is += 2) sfact = sfact * (double)((float)is / ((float)is - 1.0f));
+    const double sx = sin(log(rcoord) / tan(P.pitch) - phi + (double)0.7854f);
+    double sp = 1.0, xx = sx;
+    for (unsigned u = (unsigned)P.sn; u;) {
+      if (u & 1u) sp *= xx;
+      u >>= 1;
+      if (u) xx *= xx;
+    }
+    spiral = 1.0 - P.sw + sfact * P.sw * sp;
     if (rcoord < P.rspiral1 || rcoord > P.rspiral2) spiral = 1.0;
   }
   double zmr = zscale * pow(rcoord, bdens);

@@ -371,6 +371,19 @@ double zerod(double mu, double rx) {
 
 // densdisk, densdiskg.f90:1-155: the flared disk with its gap, spiral arms,
 // warp, rim and gap puffs and curves and radial cutoff, at azimuth phi.
+// x**n for an integer n as the Fortran runtime forms it: a product by
+// repeated squaring (the reciprocal for n < 0)
+static double powi(double x, int n) {
+  double r = 1.0;
+  unsigned u = n < 0 ? (unsigned)(-n) : (unsigned)n;
+  while (u) {
+    if (u & 1u) r *= x;
+    u >>= 1;
+    if (u) x *= x;
+  }
+  return n < 0 ? 1.0 / r : r;
+}
+
 double densdisk(const Model& m, double rad, double sint, double cost, double phi, int id) {
   const double rp = rad * sint, zp = rad * cost;
   const double rcoord = m.idiskcurve == 1 ? rad : rp;
@@ -400,9 +413,13 @@ double densdisk(const Model& m, double rad, double sint, double cost, double phi
   // normalised by the product of is/(is-1) over even is
   double spiral = 1.0;
   if (m.ispiral == 1) {
+    // the factors real(is)/(real(is)-1) and the phase 0.7854 are default
+    // (single precision) reals in the Fortran; the integer power is a
+    // product by squaring, as the Fortran runtime forms x**n
     double sfact = 1.0;
-    for (int is = 2; is <= m.sn; is += 2) sfact = sfact * ((double)is / ((double)is - 1.0));
-    spiral = 1.0 - m.sw + sfact * m.sw * std::pow(std::sin(std::log(rcoord) / std::tan(m.pitch) - phi + 0.7854), m.sn);
+    for (int is = 2; is <= m.sn; is += 2) sfact = sfact * (double)((float)is / ((float)is - 1.0f));
+    spiral = 1.0 - m.sw +
+             sfact * m.sw * powi(std::sin(std::log(rcoord) / std::tan(m.pitch) - phi + (double)0.7854f), m.sn);
     if (rcoord < m.rspiral1 || rcoord > m.rspiral2) spiral = 1.0;
   }
   double zmr = zscale * std::pow(rcoord / rmin, bdens);

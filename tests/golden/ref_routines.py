@@ -555,3 +555,106 @@ def spot_geometry(spotlat, thspot_deg):
     s1 = (math.sin(th1) * math.cos(ph1), math.sin(th1) * math.sin(ph1), math.cos(th1), math.sin(th1))
     s2 = (math.sin(th2) * math.cos(ph2), math.sin(th2) * math.sin(ph2), math.cos(th2), math.sin(th2))
     return s1, s2, math.cos(thspot_deg * DEG2RAD)
+
+
+def _rpow(x, y):
+    """x**y for a real exponent as C and Fortran form it: NaN for x < 0 and y
+    not an integer (Python would return a complex number)."""
+    if x < 0.0 and y != int(y):
+        return float("nan")
+    return x ** y
+
+
+def _powi(x, n):
+    """x**n for an integer n, as the Fortran runtime forms it (squaring)."""
+    r, u = 1.0, abs(n)
+    while u:
+        if u & 1:
+            r *= x
+        u >>= 1
+        if u:
+            x *= x
+    return 1.0 / r if n < 0 else r
+
+
+def densdiskg(rad, sint, cost, phi, P, region_out=None):
+    """densdiskg.f90:25-155 for one disk slot.  P holds the slot's scaled
+    parameters (lengths in stellar radii, angles in radians): a, b, z1, rho0,
+    rddust, rmaxd; the gap's agap, bgap, z1gap, rhogap0, rgapd1, rgapd2; and
+    the switches and parameters of the warp, rim and gap puffs and curves,
+    spiral arms and radial cutoff (keys as the Fortran names).  region_out,
+    when given, receives "gap" or "disk": which density law applied."""
+    rp = rad * sint
+    zp = rad * cost
+    rcoord = rad if P["idiskcurve"] == 1 else rp
+    rmin = 1.0
+    ingap = P["igapd"] == 1 and P["rgapd1"] < rcoord < P["rgapd2"]
+    if ingap:
+        adens, bdens, rhodens, zscale = P["agap"], P["bgap"], P["rhogap0"], P["z1gap"]
+    else:
+        adens, bdens, rhodens, zscale = P["a"], P["b"], P["rho0"], P["z1"]
+    if region_out is not None:
+        region_out.append("gap" if ingap else "disk")
+    warp = warp2 = 0.0
+    if P["idiskwarp"] == 1:
+        q = (rcoord - P["rddust"]) / P["warplength"]
+        fall = math.exp(-(q * q))
+        warp = P["warpheight"] * _rpow(math.cos(phi / 2.0), P["wexp"]) * fall
+        if phi >= PI:
+            warp = -warp
+        if P["nspot"] == 2:
+            warp2 = P["warpheight"] * _rpow(math.cos(phi / 2.0 - PI / 2.0), P["wexp"]) * fall
+    rimcurve = 0.0
+    if P["irimcurve"] == 1:
+        rimcurve = P["rimcurveheight"] * math.exp(-_rpow((rcoord - P["rddust"]) / P["rimcurvelength"], P["rimcurveexp"]))
+    rimpuff = 0.0
+    if P["irimpuff"] == 1:
+        q = (rcoord - P["rddust"]) / P["rimlength"]
+        rimpuff = P["rimheight"] * math.exp(-(q * q))
+    if rcoord < P["rddust"]:
+        rimpuff = 0.0
+    gappuff = 0.0
+    if P["igappuff"] == 1 and P["igapd"] == 1:
+        q = (rcoord - P["rgapd2"]) / P["gaplength"]
+        gappuff = P["gapheight"] * math.exp(-(q * q))
+    if rcoord < P["rgapd2"]:
+        gappuff = 0.0
+    gapcurve = 0.0
+    if P["igapcurve"] == 1 and P["igapd"] == 1:
+        gapcurve = P["gapcurveheight"] * math.exp(-_rpow((rcoord - P["rgapd2"]) / P["gapcurvelength"], P["gapcurveexp"]))
+    if rcoord < P["rgapd2"]:
+        gapcurve = 0.0
+    spiral = 1.0
+    if P["ispiral"] == 1:
+        sfact = 1.0
+        for i in range(2, P["sn"] + 1, 2):
+            sfact = sfact * float(np.float32(i) / (np.float32(i) - np.float32(1)))
+        s = math.sin(math.log(rcoord) / math.tan(P["pitch"]) - phi + float(np.float32(0.7854)))
+        spiral = 1.0 - P["sw"] + sfact * P["sw"] * _powi(s, P["sn"])
+        if rcoord < P["rspiral1"] or rcoord > P["rspiral2"]:
+            spiral = 1.0
+    zmr = zscale * (rcoord / rmin) ** bdens
+    if phi < PI / 2.0 or phi > 3.0 * PI / 2.0:
+        if zp > 0.0:
+            zmr = zmr * (1.0 + warp)
+        densfact1 = 1.0 / (1.0 + warp)
+    else:
+        if zp < 0.0:
+            zmr = zmr * (1.0 + warp2)
+        densfact1 = 1.0 / (1.0 + warp2)
+    puff = 1.0 + rimpuff + gappuff - rimcurve - gapcurve
+    densfact = 1.0 / puff * densfact1
+    zmr = zmr * puff
+    if rcoord > P["rmaxd"] or rhodens == 0.0 or rcoord < P["rddust"] or zmr < 1.0e-10:
+        return 0.0
+    gexp = (zp / zmr) * (zp / zmr)
+    if gexp > 1.0e-15:
+        if gexp < 120.0:
+            dens = densfact * spiral * rhodens * (rcoord / rmin) ** (-adens) * math.exp(-0.5 * gexp)
+        else:
+            dens = 0.0
+    else:
+        dens = densfact * spiral * rhodens * (rcoord / rmin) ** (-adens)
+    if P["iradexp"] == 1:
+        dens = dens * math.exp(-rcoord / P["radexp"])
+    return dens
