@@ -144,7 +144,7 @@ struct LaunchCfg {
   int variant = 0;  // block shape of the mixed-form peel-off kernel (see peel_threads_mixed)
 };
 
-constexpr int kPeelVariants = 3;  // block shapes of the mixed-form peel-off kernel
+constexpr int kPeelVariants = 2;  // block shapes of the mixed-form peel-off kernel
 
 // entry points of the two instantiations
 cudaError_t launch_transport_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,

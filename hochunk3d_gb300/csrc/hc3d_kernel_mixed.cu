@@ -40,7 +40,7 @@ cudaError_t launch_wave_transport_mixed(const DevModel& m, const DevTallies& t, 
 }
 
 // the block shapes of k_peel_mixed: (threads, blocks per SM at launch bounds)
-constexpr int kPeelShapes[kPeelVariants][2] = {{256, 2}, {128, 4}, {256, 3}};
+constexpr int kPeelShapes[kPeelVariants][2] = {{256, 2}, {128, 4}};
 
 cudaError_t launch_wave_peel_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                    const WaveBufs& w, int q, const LaunchCfg& cfg) {
@@ -48,9 +48,6 @@ cudaError_t launch_wave_peel_mixed(const DevModel& m, const DevTallies& t, const
   switch (cfg.variant) {
     case 1:
       dev::k_peel_mixed<float, 128, 4><<<cfg.blocks, 128, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
-      break;
-    case 2:
-      dev::k_peel_mixed<float, 256, 3><<<cfg.blocks, 256, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
       break;
     default:
       dev::k_peel_mixed<float, 256, 2><<<cfg.blocks, 256, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
@@ -66,7 +63,6 @@ const void* wave_fn_mixed() { return (const void*)dev::k_wave<float>; }
 const void* peel_fn_mixed(int variant) {
   switch (variant) {
     case 1: return (const void*)dev::k_peel_mixed<float, 128, 4>;
-    case 2: return (const void*)dev::k_peel_mixed<float, 256, 3>;
     default: return (const void*)dev::k_peel_mixed<float, 256, 2>;
   }
 }

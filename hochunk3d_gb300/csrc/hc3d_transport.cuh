@@ -2638,12 +2638,14 @@ static __device__ __noinline__ int prep_rays(const DevModel& m, const PeelRec<fl
   return __popc(okm);
 }
 
-// Instantiated for three block shapes, among which the autotuner picks:
+// Instantiated for two block shapes, between which the autotuner picks:
 // 256 threads x 2 blocks per SM and 128 x 4 (the walk state of a lane, the
-// set-up stack and the 32-ray tally need about 118 registers), and 256 x 3
-// (85 registers: part of the walk state goes to local memory).  The smaller
+// set-up stack and the 32-ray tally need about 118 registers).  The smaller
 // blocks retire one by one as the ray pool drains, so the next wave's
-// transport blocks find room sooner.
+// transport blocks find room sooner.  A shape of 256 x 3 (80 registers,
+// with spills) was slower, and its different register allocation changed
+// which multiply-adds the compiler fused, so its tallies differed in the last
+// bits.
 template <class R, int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                               const PeelRec<R>* queue,

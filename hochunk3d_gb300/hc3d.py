@@ -618,7 +618,7 @@ class Context:
 
     def set_wave_options(self, queue_records: int = 0, regen: int = 0, qchunk: int = 0, peel_shape: int = 0) -> None:
         """Queue depth, regeneration threshold, queue-slot chunk and peel-off
-        block shape (1..3) of the wavefront form (hc3d_set_wave_options; 0
+        block shape (1, 2) of the wavefront form (hc3d_set_wave_options; 0
         keeps a setting)."""
         self._check(lib().hc3d_set_wave_options(self._h, int(queue_records), int(regen), int(qchunk),
                                                 int(peel_shape)))

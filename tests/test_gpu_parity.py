@@ -290,15 +290,15 @@ def test_autotune_keeps_results(model_factory, ipeel):
     p = m.run_params(np=30000, iter=2, ipeel=ipeel)
     ctx.zero(); ctx.run(p); a = ctx.tallies(p)
     res = ctx.autotune(m.run_params(np=20000, iter=7, ipeel=ipeel))
-    # peeled: 4 queue depths, the 3 other regeneration thresholds, the 2 other peel-off block shapes
-    assert len(res["candidates"]) == (9 if ipeel else 3) and all(c["ms"] > 0 for c in res["candidates"])
+    # peeled: 4 queue depths, the 3 other regeneration thresholds, the other peel-off block shape
+    assert len(res["candidates"]) == (8 if ipeel else 3) and all(c["ms"] > 0 for c in res["candidates"])
     if ipeel:
         assert {c["regen"] for c in res["candidates"]} == {1, 4, 8, 16}
         assert {c["peel_threads"] for c in res["candidates"]} == {128, 256}
     keys = ("si", "nums", "nabs", "dtauabs", "jmean", "counters") + (("ti", "numt", "image_i") if ipeel else ())
     settings = [{}] + ([{"queue_records": 1 << 20, "regen": 16, "qchunk": 1, "peel_shape": 2},
-                        {"queue_records": 1 << 21, "regen": 4, "qchunk": 32, "peel_shape": 3},
-                        {"peel_shape": 1}] if ipeel else [])
+                        {"queue_records": 1 << 21, "regen": 4, "qchunk": 32, "peel_shape": 1},
+                        {"peel_shape": 2}] if ipeel else [])
     for opt in settings:
         if opt:
             ctx.set_wave_options(**opt)
