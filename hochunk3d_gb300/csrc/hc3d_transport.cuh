@@ -2351,25 +2351,28 @@ __device__ __forceinline__ int walk(const DevModel& m, const DevTallies& t, cons
 // is at least k s; the walk ends a ray whose depth passes taumax = 25
 // (peeloff_3d.f90:118) and tallies nothing for it.  When k s exceeds taumax
 // by 1 %, and s is large against the FP32 resolution of the ray parameter
-// (about 2^-23 |x|), the walk would end every ray at its first wall: the
-// record is marked empty and no ray is walked.  The tallies are unchanged;
-// the peel-off ray and crossing counters count only the rays walked.
+// (about 2^-23 |x|), the walk would end every ray at its first wall: no
+// record is made and no ray is walked.  The tallies are unchanged; the
+// peel-off ray and crossing counters count only the rays walked.
 template <class R>
-__device__ __forceinline__ void cull_deep_peel(const DevModel& m, const Pkt<R>& p, int64_t c, PeelRec<R>& rec) {
+__device__ __forceinline__ bool deep_peel(const DevModel& m, const Pkt<R>& p, int64_t c) {
   if constexpr (sizeof(R) == 4) {
     if (p.safe > 0.f) {
       const float4 q = __ldg(m.rho4p + c);
       const float op = fmaf(p.kapd[0], q.x, fmaf(p.kapd[1], q.y, fmaf(p.kapd[2], q.z, p.kapd[3] * q.w)));
       const float r = fabsf(p.x.hi) + fabsf(p.y.hi) + fabsf(p.z.hi);
-      if (p.safe * op > 1.01f * (float)kTauMax && p.safe > r * 1.220703125e-4f) rec.flags |= kRecNoPeel;
+      return p.safe * op > 1.01f * (float)kTauMax && p.safe > r * 1.220703125e-4f;
     }
   }
+  return false;
 }
 
 // One interaction, propagate.f90:70-166: scattering (rec = the state before
 // stokes) or absorption and thermal re-emission (rec = the re-emitted packet).
+// Returns whether rec was written: only in peeled runs, and not for an event
+// whose peel-off rays all end in its cell (deep_peel).
 template <class R>
-__device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow<R>& f,
+__device__ __forceinline__ bool interact(const DevModel& m, const DustView<R>& dv, const DevTallies& t, const RunArgs& a, Pkt<R>& p, Rng& rng, Flow<R>& f,
                          Local& L, Tracer& tr, PeelRec<R>& rec) {
   const int64_t c = cidx(m, p.ir, p.it, p.ip);
   const int idust2 = f.idust2;
@@ -2378,10 +2381,11 @@ __device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& d
   // issued before the albedo test so that its latency overlaps the draw
   R tave = R(0);
   if constexpr (sizeof(R) == 8) tave = __ldg(m.tdust + 4 * c + idust2);
+  bool keep;
   if (ran<R>(rng) <= pick4(p.albedo, idust2)) {  // scattered
     f.iflag = 1; f.iscat++; f.iint++;
-    make_rec<R>(rec, p, a, 1, idust2);
-    cull_deep_peel<R>(m, p, c, rec);
+    keep = a.ipeel == 1 && !deep_peel<R>(m, p, c);
+    if (keep) make_rec<R>(rec, p, a, 1, idust2);
     stokes<R>(p, idust2, rng);
     tr.add(5, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
@@ -2398,11 +2402,12 @@ __device__ __forceinline__ void interact(const DevModel& m, const DustView<R>& d
     else p.nub = lucydustfreq<R>(m, tave, idust2, rng);
     f.iflag = 0;
     opacset<R>(m, dv, p, p.nub, a);
-    make_rec<R>(rec, p, a, 0, idust2);
-    cull_deep_peel<R>(m, p, c, rec);
+    keep = a.ipeel == 1 && !deep_peel<R>(m, p, c);
+    if (keep) make_rec<R>(rec, p, a, 0, idust2);
     f.iint++;
     tr.add(6, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
   }
+  return keep;
 }
 
 // every thread of the block calls it, after its last event
@@ -2426,8 +2431,7 @@ __device__ void run_packet(const DevModel& m, const DustView<R>& dv, const DevTa
   f.iflag = 0; f.iscat = 0; f.iint = 0; f.idust2 = 0; f.ntot = 0;
   int st = walk<R>(m, t, d, a, p, rng, f, L, tr, true);
   while (st == ST_INTERACT) {
-    interact<R>(m, dv, t, a, p, rng, f, L, tr, rec);
-    if (a.ipeel == 1) peel_all<R>(m, t, d, a, rec, L);
+    if (interact<R>(m, dv, t, a, p, rng, f, L, tr, rec)) peel_all<R>(m, t, d, a, rec, L);
     st = walk<R>(m, t, d, a, p, rng, f, L, tr, false);
   }
 }
@@ -2570,14 +2574,15 @@ __global__ void __launch_bounds__(128, 3) k_wave(DevModel m, DevTallies t, Tally
       slot = atomicAdd(qcount, (unsigned long long)a.qchunk);
       slot_end = slot + (unsigned long long)a.qchunk;
     }
-    PeelRec<R>& rec = queue[slot++];
+    PeelRec<R>& rec = queue[slot];
     if (s.stage == 0) {
+      ++slot;
       if (!emit<R>(m, dv, t, a, s.p, rng, rec, tr, L)) continue;  // dropped: the lane takes the next packet
       s.f.xpold = s.p.x; s.f.ypold = s.p.y; s.f.zpold = s.p.z;
       s.f.iflag = 0; s.f.iscat = 0; s.f.iint = 0; s.f.idust2 = 0; s.f.ntot = 0;
       s.stage = 2;  // emitted: walk to the first interaction after the record
-    } else {
-      interact<R>(m, dv, t, a, s.p, rng, s.f, L, tr, rec);
+    } else if (interact<R>(m, dv, t, a, s.p, rng, s.f, L, tr, rec)) {
+      ++slot;  // the slot is kept only when the event made a record
     }
     const int st = walk<R>(m, t, d, a, s.p, rng, s.f, L, tr, s.stage == 2);
     s.stage = st == ST_INTERACT ? 1 : 0;
