@@ -27,6 +27,10 @@ Models:
              magnetospheric truncation at 5 R*), two hot spots at latitude
              60 deg covering 5 % of the star, and a gap between 0.1 and
              0.2 AU where the accretion packets are emitted by the gas.
+  tiny_sg -- tiny with very small grains and PAHs: 20 % of the mass of disk
+             1 in small grains (species 5), which re-emit from 18 synthetic
+             emission spectra by the cells' mean intensity; no cavity, so
+             the device slots carry species 1, 2, 3 and 5.
 """
 from __future__ import annotations
 
@@ -116,6 +120,8 @@ CONFIGS = {
                  "MASSD": 0.001, "RATE": 5e-7, "CDISKACC": "YES", "CALPHA": "NO", "ALPHA/MDOT": 3e-7, "RTRUNC": 5.0,
                  "CSPOT": "YES", "SPOTLAT": 60.0, "NSPOT": 2, "CTEMP": "NO", "TSPOT/FSPOT": 0.05,
                  "CGAPD": "YES", "RGAPD1": 0.1, "RGAPD2": 0.2, "RHOSCALE_GAP(1)": 0.0, "RHOSCALE_GAP(2)": 0.0},
+    "tiny_sg": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 2, "NXIMG": 31,
+                "MASSD": 0.001, "RATE": 5e-7, "FSG(1)": 0.2, "CHOLE": "NO", "ISRF_FILE": ISRF_FILE},
     "tiny3d": {"NP": 4000, "NPMIN": 2000, "NIMIN": 2, "NIMAX": 2, "NRG": 40, "NTG": 31, "NPG": 9, "NXIMG": 31,
                "MASSD": 0.0001, "RATE": 5e-7, "NPEEL": 4, "THETE": "30.013,60.013,80.013,120.013",
                "PHIE": "0.0,90.0,180.0,270.0", "CFRACTAL": "YES", "FRACTLEV": 2, "FRACTN": 8},
@@ -145,6 +151,9 @@ def write_fixtures(directory: str | Path) -> Path:
     rc = L.hc3d_write_synthetic_isrf(str(d / ISRF_FILE).encode())
     if rc != 0:
         raise hc3d.Hc3dError(rc, "cannot write external-field fixture")
+    rc = L.hc3d_write_synthetic_draine(str(d).encode())
+    if rc != 0:
+        raise hc3d.Hc3dError(rc, "cannot write small-grain spectra fixtures")
     return d
 
 

@@ -35,6 +35,17 @@ struct hc3d_ctx {
   unsigned char* d_peelmask = nullptr;
   float4* d_rho4p = nullptr;  // (ncell) peel-masked FP32 densities, also dm.rho4p
   int ndg_in = 0;
+  // species (1..8, reference numbering) of the four device slots (hc3d_set_species)
+  int species[kSlots] = {1, 2, 3, 4};
+  // small grains: emission spectra (hc3d_load_sg_tables) and the int_mean result of the last Lucy update
+  bool sg_tables = false;
+  double isrfkap_int = 0.0;
+  std::vector<double> sg_uratio;
+  int* d_imean = nullptr;
+  double* d_imfract = nullptr;
+  double* d_vcell = nullptr;   // (ncell) cell volumes, cm^3 (int_mean)
+  double* d_uratio = nullptr;  // (nemit)
+  bool imean_set = false;
   // tallies
   DevTallies dt{};
   TallyDims dims{};
@@ -77,6 +88,31 @@ namespace {
 int fail(hc3d_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
+}
+
+// the species index (0-based, in the ndg species of the host arrays) device
+// slot s reads; -1 when the host arrays do not describe that species
+int slot_src(const hc3d_ctx* c, int s, int ndg) {
+  const int id = c->species[s] - 1;
+  return id < ndg ? id : -1;
+}
+
+bool has_sg_slots(const hc3d_ctx* c) {
+  for (int s = 0; s < kSlots; ++s)
+    if (c->species[s] >= 5) return true;
+  return false;
+}
+
+// the slot masks of the species map (grid_mod.f90:13-20: species 1, 2, 5, 6
+// are disk species, 5-8 small grains)
+void apply_species(hc3d_ctx* c) {
+  c->dm.disk_mask = c->dm.sg_mask = 0u;
+  for (int s = 0; s < kSlots; ++s) {
+    const int sp = c->species[s];
+    if (sp == 1 || sp == 2 || sp == 5 || sp == 6) c->dm.disk_mask |= 1u << s;
+    if (sp >= 5) c->dm.sg_mask |= 1u << s;
+  }
+  c->dm.sg_on = (c->dm.sg_mask && c->sg_tables) ? 1 : 0;
 }
 
 #define CK(call)                                                                          \
@@ -187,6 +223,57 @@ __global__ void k_peelmask(int64_t ncell, const double* tdust, double tsub, unsi
     peelmask[c] = (unsigned char)mask;
     rho4p[c] = masked_rho(rho4f[c], mask);
   }
+}
+
+// ---- int_mean.f90:19-94 -------------------------------------------------------
+// The mean intensity of each cell in units of the ISRF absorbed by the small
+// grains: the path tally jsg (ds kappa/kappa_V (1 - albedo) over the cell's
+// outer radius, x path_scale) times the outer radius, rstar_cm kappa_V /
+// (4 pi), over vcell and the packets, times ltot, over isrfkap_int.  The
+// spectrum row is where the ratio falls in uratio (nr locate, clamped to
+// 1..nemit), imfract the fraction of the way to the next row in log10 (0
+// where the ratio is 0, 1 on the last row).
+struct IntMeanArgs {
+  int64_t ncell;
+  int nr1;                 // nrg - 1
+  double path_scale, jconst, nphot, ltot, isrfkap_int;
+  int nemit;
+  const double* rarr;      // (nrg)
+  const double* vcell;     // (ncell)
+  const double* uratio;    // (nemit)
+};
+
+__device__ __forceinline__ void int_mean_cell(const IntMeanArgs& a, int64_t c, const unsigned long long* jsg, int* imean,
+                                              double* imfract) {
+  const int ir = (int)(c % a.nr1) + 1;
+  double jm = (double)(long long)jsg[c] / a.path_scale;
+  jm = jm * a.rarr[ir];
+  jm = jm * a.jconst;
+  jm = jm / a.vcell[c] / a.nphot * a.ltot;
+  const double jratio = jm / a.isrfkap_int;
+  int jl = 0, ju = a.nemit + 1;
+  while (ju - jl > 1) {
+    const int jmid = (ju + jl) / 2;
+    if (jratio > a.uratio[jmid - 1]) jl = jmid; else ju = jmid;
+  }
+  if (jl == 0 && jratio == a.uratio[0]) jl = 1;
+  int im = jl;
+  if (im > a.nemit) im = a.nemit;
+  if (im < 1) im = 1;
+  double f;
+  if (jratio == 0.0) f = 0.0;
+  else if (im == a.nemit) f = 1.0;
+  else {
+    const double jr1 = log10(a.uratio[im - 1]), jr2 = log10(a.uratio[im]);
+    f = (log10(jratio) - jr1) / (jr2 - jr1);
+  }
+  imean[c] = im;
+  imfract[c] = f;
+}
+
+__global__ void k_intmean(IntMeanArgs a, const unsigned long long* jsg, int* imean, double* imfract) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.ncell; c += (int64_t)gridDim.x * blockDim.x)
+    int_mean_cell(a, c, jsg, imean, imfract);
 }
 
 int grid_blocks_for(hc3d_ctx* c, int64_t n) {
@@ -316,6 +403,18 @@ int prepare_run(hc3d_ctx* c, const hc3d_run_params* p, RunArgs* a) {
   a->limb = p->limb;
   a->regen = c->regen;
   a->imcube = d.ncube > 0 ? 1 : 0;
+  a->iter1 = p->iter == 1 ? 1 : 0;
+  if (c->dm.sg_on) {
+    c->dm.sg_jfacd = 1.0 / (p->rstar_cm * c->kappav[c->dm.sg_slot]);
+    c->dm.sg_jfac = (float)c->dm.sg_jfacd;
+  }
+  if (c->dm.sg_mask) {
+    if (!c->dm.sg_on) return fail(c, HC3D_ERR_STATE, "a slot holds small grains: load their spectra (hc3d_load_sg_tables)");
+    if (p->iter != 1 && !c->imean_set)
+      return fail(c, HC3D_ERR_STATE,
+                  "small grains after the first iteration re-emit by the mean intensity of the last: run "
+                  "hc3d_lucy_update after an iteration or set it with hc3d_set_imean");
+  }
   a->qchunk = c->qchunk;
   // disk accretion and hot-spot packets
   a->n_acc = 0;
@@ -591,7 +690,111 @@ extern "C" int hc3d_create(hc3d_ctx** out, const hc3d_device_opts* opts) {
     delete c;
     return HC3D_ERR_CUDA;
   }
+  apply_species(c);
   *out = c;
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_set_species(hc3d_ctx* c, const int32_t* species) {
+  if (!c || !species) return HC3D_ERR_INVALID;
+  if (c->tables || c->grid) return fail(c, HC3D_ERR_STATE, "set the species before hc3d_load_tables and hc3d_load_grid");
+  if (species[0] != 1 || species[1] != 2)
+    return fail(c, HC3D_ERR_INVALID, "slots 1 and 2 hold the thermal disk species 1 and 2");
+  if (!(species[2] >= 3 && species[2] <= 8 && species[3] > species[2] && species[3] <= 8))
+    return fail(c, HC3D_ERR_INVALID, "slots 3 and 4 hold two species of 3..8 in increasing order");
+  for (int s = 0; s < kSlots; ++s) c->species[s] = species[s];
+  apply_species(c);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_load_sg_tables(hc3d_ctx* c, const hc3d_sg_tables* t) {
+  if (!c || !t) return HC3D_ERR_INVALID;
+  if (!has_sg_slots(c)) return fail(c, HC3D_ERR_STATE, "no slot holds small grains (hc3d_set_species)");
+  if (!c->tables) return fail(c, HC3D_ERR_STATE, "load the dust tables first");
+  if (c->sg_tables) return fail(c, HC3D_ERR_STATE, "small-grain spectra already loaded in this context");
+  if (t->nemit < 2 || t->nemit > 64 || t->ndraine < 3 || !t->cdf || !t->logcdf || !t->logfreq || !t->uratio)
+    return fail(c, HC3D_ERR_INVALID, "small-grain spectra: bad dimensions or a NULL pointer");
+  if (t->sg_slot < 1 || t->sg_slot > kSlots || c->species[t->sg_slot - 1] < 5)
+    return fail(c, HC3D_ERR_INVALID, "sg_slot must name a slot that holds small grains");
+  if (!(t->isrfkap_int > 0.0) || std::isinf(t->isrfkap_int))
+    return fail(c, HC3D_ERR_INVALID, "isrfkap_int must be positive and finite");
+  for (int j = 1; j < t->nemit; ++j)
+    if (!(t->uratio[j] > t->uratio[j - 1]) || !(t->uratio[0] > 0.0))
+      return fail(c, HC3D_ERR_INVALID, "uratio must be positive and increase");
+  CK(cudaSetDevice(c->device));
+  // rows of one spectrum contiguous on the device: [j * ndraine + i] from the Fortran (nemit, ndraine)
+  const int ne = t->nemit, nd = t->ndraine;
+  std::vector<double> cdf((size_t)ne * nd), lc((size_t)ne * nd);
+  for (int i = 0; i < nd; ++i)
+    for (int j = 0; j < ne; ++j) {
+      cdf[(size_t)j * nd + i] = t->cdf[(size_t)j + (size_t)ne * i];
+      lc[(size_t)j * nd + i] = t->logcdf[(size_t)j + (size_t)ne * i];
+    }
+  std::vector<void*>& own = c->model_allocs;
+  double *d_cdf, *d_lc, *d_lf, *d_ur;
+  int r;
+  if ((r = dupload(c, own, &d_cdf, cdf.data(), cdf.size())) || (r = dupload(c, own, &d_lc, lc.data(), lc.size())) ||
+      (r = dupload(c, own, &d_lf, t->logfreq, (size_t)nd)) || (r = dupload(c, own, &d_ur, t->uratio, (size_t)ne)))
+    return r;
+  CK(cudaStreamSynchronize(c->stream));
+  c->dm.sg_nemit = ne; c->dm.sg_nd = nd;
+  c->dm.sg_cdf = d_cdf; c->dm.sg_logcdf = d_lc; c->dm.sg_logfreq = d_lf;
+  c->d_uratio = d_ur;
+  c->dm.sg_slot = t->sg_slot - 1;
+  c->isrfkap_int = t->isrfkap_int;
+  c->sg_uratio.assign(t->uratio, t->uratio + ne);
+  c->sg_tables = true;
+  apply_species(c);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_get_imean(hc3d_ctx* c, int32_t* imean, double* imfract) {
+  if (!c || (!imean && !imfract)) return HC3D_ERR_INVALID;
+  if (!c->grid || !c->d_imean) return fail(c, HC3D_ERR_STATE, "no slot of the loaded grid holds small grains");
+  if (!c->imean_set) return fail(c, HC3D_ERR_STATE, "int_mean has not run (hc3d_lucy_update) nor been set");
+  CK(cudaSetDevice(c->device));
+  const DevModel& m = c->dm;
+  const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
+  std::vector<int> im((size_t)n);
+  std::vector<double> fr((size_t)n);
+  if (int r_ = d2h(c, im.data(), c->d_imean, sizeof(int) * n)) return r_;
+  if (int r_ = d2h(c, fr.data(), c->d_imfract, sizeof(double) * n)) return r_;
+  if (imean) std::fill(imean, imean + n4, 0);
+  if (imfract) std::fill(imfract, imfract + n4, 0.0);
+  for (int ip = 1; ip < m.npg; ++ip)
+    for (int it = 1; it < m.ntg; ++it)
+      for (int ir = 1; ir < m.nrg; ++ir) {
+        const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+        const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+        if (imean) imean[c4] = im[cc];
+        if (imfract) imfract[c4] = fr[cc];
+      }
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_set_imean(hc3d_ctx* c, const int32_t* imean, const double* imfract) {
+  if (!c || !imean || !imfract) return HC3D_ERR_INVALID;
+  if (!c->grid || !c->d_imean) return fail(c, HC3D_ERR_STATE, "no slot of the loaded grid holds small grains");
+  if (!c->sg_tables) return fail(c, HC3D_ERR_STATE, "load the small-grain spectra first");
+  CK(cudaSetDevice(c->device));
+  const DevModel& m = c->dm;
+  const int64_t n = m.ncell;
+  std::vector<int> im((size_t)n);
+  std::vector<double> fr((size_t)n);
+  for (int ip = 1; ip < m.npg; ++ip)
+    for (int it = 1; it < m.ntg; ++it)
+      for (int ir = 1; ir < m.nrg; ++ir) {
+        const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+        const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+        if (imean[c4] < 1 || imean[c4] > m.sg_nemit || !std::isfinite(imfract[c4]))
+          return fail(c, HC3D_ERR_INVALID, "imean must lie in 1..nemit and imfract be finite");
+        im[cc] = imean[c4];
+        fr[cc] = imfract[c4];
+      }
+  CK(cudaMemcpyAsync(c->d_imean, im.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d_imfract, fr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->imean_set = true;
   return HC3D_OK;
 }
 
@@ -635,6 +838,11 @@ extern "C" int hc3d_reset(hc3d_ctx* c) {
   c->d_peelmask = nullptr;
   c->d_rho4p = nullptr;
   c->ndg_in = 0;
+  for (int s = 0; s < kSlots; ++s) c->species[s] = s + 1;
+  c->sg_tables = false;
+  c->imean_set = false;
+  c->d_imean = nullptr; c->d_imfract = nullptr; c->d_vcell = nullptr; c->d_uratio = nullptr;
+  apply_species(c);
   // the run tallies go; the counters and the fault log stay with the context
   DevTallies keep{};
   keep.counters = c->dt.counters;
@@ -676,12 +884,12 @@ extern "C" int hc3d_load_tables(hc3d_ctx* c, const hc3d_dust_tables* t) {
     // tables own their allocations at the front of model_allocs; rebuild the context tables
     return fail(c, HC3D_ERR_STATE, "tables already loaded in this context");
   }
-  const int ns = std::min(t->ndg, kSlots);
   std::vector<double> nud((size_t)t->nlammax * kSlots), kap(nud.size()), alb(nud.size()), gg(nud.size()),
       pl(nud.size());
   std::vector<double> kB((size_t)t->nT * t->nnu * kSlots), kp((size_t)t->nT * kSlots);
   for (int s = 0; s < kSlots; ++s) {
-    const int src = s < ns ? s : 0;
+    // a slot whose species the tables do not describe repeats slot 1's table (it holds no density)
+    const int src = slot_src(c, s, t->ndg) >= 0 ? slot_src(c, s, t->ndg) : 0;
     const int nl = t->nlambda[src];
     if (nl < 2 || nl > t->nlammax) return fail(c, HC3D_ERR_INVALID, "nlambda out of range");
     c->dm.nlambda[s] = nl;
@@ -890,11 +1098,17 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   // the kernels index cells with 32-bit arithmetic
   if (ncell >= ((int64_t)1 << 31) || 4 * ncell >= ((int64_t)1 << 31))
     return fail(c, HC3D_ERR_INVALID, "grid has 2^29 or more cells");
-  // species slots beyond the device's four must be empty
-  for (int s = kSlots; s < g->ndg; ++s)
+  // the species outside the four device slots must be empty
+  for (int id = 0; id < g->ndg; ++id) {
+    bool mapped = false;
+    for (int s = 0; s < kSlots; ++s) mapped = mapped || c->species[s] == id + 1;
+    if (mapped) continue;
     for (int64_t k = 0; k < n4; ++k)
-      if (g->densarr[k + n4 * s] != 0.0)
-        return fail(c, HC3D_ERR_UNSUPPORTED, "species slots 5-8 (small grains) are not supported");
+      if (g->densarr[k + n4 * id] != 0.0)
+        return fail(c, HC3D_ERR_UNSUPPORTED,
+                    "species " + std::to_string(id + 1) + " holds density but no device slot carries it "
+                    "(hc3d_set_species names the four species the device carries)");
+  }
   for (int64_t k = 0; k < n4 * g->ndg; ++k)
     if (!(g->densarr[k] >= 0.0) || std::isinf(g->densarr[k]))
       return fail(c, HC3D_ERR_INVALID, "densarr holds a negative, NaN or infinite value");
@@ -911,7 +1125,8 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
     af[i] = (float)g->aarr[i];
     bf[i] = (float)g->barr[i];
   }
-  const int ns = std::min(g->ndg, kSlots);
+  int src_of[kSlots];
+  for (int s = 0; s < kSlots; ++s) src_of[s] = slot_src(c, s, g->ndg);
   std::vector<float4> rf(ncell);
   std::vector<double> rd(4 * ncell, 0.0), td(4 * ncell, 0.1 / 11605.0), ma(4 * ncell, 0.0);
   for (int ip = 1; ip < npg; ++ip)
@@ -920,12 +1135,14 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
         const int64_t c4 = (int64_t)(ir - 1) + (int64_t)nrg * ((it - 1) + (int64_t)ntg * (ip - 1));
         const int64_t cc = (int64_t)(ir - 1) + (int64_t)(nrg - 1) * ((it - 1) + (int64_t)(ntg - 1) * (ip - 1));
         float v[4] = {0, 0, 0, 0};
-        for (int s = 0; s < ns; ++s) {
-          const double d = g->densarr[c4 + n4 * s];
+        for (int s = 0; s < kSlots; ++s) {
+          const int id = src_of[s];
+          if (id < 0) continue;
+          const double d = g->densarr[c4 + n4 * id];
           v[s] = (float)d;
           rd[4 * cc + s] = d;
-          td[4 * cc + s] = g->tdust[c4 + n4 * s];
-          ma[4 * cc + s] = g->massarr[c4 + n4 * s];
+          td[4 * cc + s] = g->tdust[c4 + n4 * id];
+          ma[4 * cc + s] = g->massarr[c4 + n4 * id];
         }
         rf[cc] = make_float4(v[0], v[1], v[2], v[3]);
       }
@@ -954,6 +1171,28 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
       (r = dalloc(c, own, &t.jmean, (size_t)ncell)) || (r = dalloc(c, own, &t.killed, (size_t)ncell)) ||
       (r = dalloc(c, own, &t.dbig, (size_t)ncell)))
     return r;
+  // small-grain tallies and the int_mean result, when a slot holds small grains
+  t.dsg = nullptr; t.jsg = nullptr;
+  c->d_imean = nullptr; c->d_imfract = nullptr;
+  c->imean_set = false;
+  c->d_vcell = nullptr;
+  if (has_sg_slots(c)) {
+    std::vector<double> vc((size_t)ncell);
+    for (int ip = 1; ip < npg; ++ip)
+      for (int it = 1; it < ntg; ++it)
+        for (int ir = 1; ir < nrg; ++ir) {
+          const int64_t c4 = (int64_t)(ir - 1) + (int64_t)nrg * ((it - 1) + (int64_t)ntg * (ip - 1));
+          const int64_t cc = (int64_t)(ir - 1) + (int64_t)(nrg - 1) * ((it - 1) + (int64_t)(ntg - 1) * (ip - 1));
+          vc[cc] = g->vcell[c4];
+          if (!(vc[cc] > 0.0)) return fail(c, HC3D_ERR_INVALID, "vcell must be positive (int_mean divides by it)");
+        }
+    if ((r = dalloc(c, own, &t.dsg, (size_t)ncell)) || (r = dalloc(c, own, &t.jsg, (size_t)ncell)) ||
+        (r = dalloc(c, own, &c->d_imean, (size_t)ncell)) || (r = dalloc(c, own, &c->d_imfract, (size_t)ncell)) ||
+        (r = dupload(c, own, &c->d_vcell, vc.data(), vc.size())))
+      return r;
+    CK(cudaMemsetAsync(t.dsg, 0, sizeof(unsigned int) * ncell, c->stream));
+    CK(cudaMemsetAsync(t.jsg, 0, sizeof(unsigned long long) * ncell, c->stream));
+  }
   DevModel& m = c->dm;
   m.nrg = nrg; m.ntg = ntg; m.npg = npg; m.ncell = ncell;
   m.rarr = d_r; m.r2arr = d_r2; m.thetarr = d_th; m.costarr = d_ct; m.phiarr = d_ph; m.tan2d = d_t2; m.tan2f = d_t2f; m.hemi = d_hemi;
@@ -992,6 +1231,7 @@ extern "C" int hc3d_load_grid(hc3d_ctx* c, const hc3d_grid* g) {
   }
   m.aarrd = d_a; m.barrd = d_b; m.aarrf = d_af; m.barrf = d_bf; m.rho4f = d_rf; m.rho4d = d_rd;
   m.peelmask = c->d_peelmask; m.rho4p = c->d_rho4p; m.tdust = c->d_tdust; m.tdustf = c->d_tdustf;
+  m.imean = c->d_imean; m.imfract = c->d_imfract;
   c->ndg_in = g->ndg;
   k_peelmask<<<grid_blocks_for(c, ncell), 256, 0, c->stream>>>(ncell, c->d_tdust, c->tsub, c->d_peelmask, d_rf,
                                                                 c->d_rho4p);
@@ -1023,7 +1263,6 @@ extern "C" int hc3d_set_tdust(hc3d_ctx* c, const double* tdust) {
   CK(cudaSetDevice(c->device));
   const int nrg = c->dm.nrg, ntg = c->dm.ntg, npg = c->dm.npg;
   const int64_t n4 = (int64_t)nrg * ntg * npg, ncell = c->dm.ncell;
-  const int ns = std::min(c->ndg_in, kSlots);
   // the device layout of hc3d_load_grid: 4 slots per compact cell; empty slots keep the floor value
   std::vector<double> td(4 * ncell, 0.1 / 11605.0);
   for (int ip = 1; ip < npg; ++ip)
@@ -1031,8 +1270,10 @@ extern "C" int hc3d_set_tdust(hc3d_ctx* c, const double* tdust) {
       for (int ir = 1; ir < nrg; ++ir) {
         const int64_t c4 = (int64_t)(ir - 1) + (int64_t)nrg * ((it - 1) + (int64_t)ntg * (ip - 1));
         const int64_t cc = (int64_t)(ir - 1) + (int64_t)(nrg - 1) * ((it - 1) + (int64_t)(ntg - 1) * (ip - 1));
-        for (int s = 0; s < ns; ++s) {
-          const double v = tdust[c4 + n4 * s];
+        for (int s = 0; s < kSlots; ++s) {
+          const int id = slot_src(c, s, c->ndg_in);
+          if (id < 0) continue;
+          const double v = tdust[c4 + n4 * id];
           if (!(v >= 0.0) || std::isinf(v)) return fail(c, HC3D_ERR_INVALID, "tdust holds a negative, NaN or infinite value");
           td[4 * cc + s] = v > 0.0 ? v : 0.1 / 11605.0;  // 0: the 0.1 K floor of the starting field
         }
@@ -1057,6 +1298,8 @@ extern "C" int hc3d_zero_tallies(hc3d_ctx* c) {
     CK(cudaMemsetAsync(c->dt.jmean, 0, sizeof(unsigned long long) * n, c->stream));
     CK(cudaMemsetAsync(c->dt.killed, 0, sizeof(unsigned int) * n, c->stream));
     CK(cudaMemsetAsync(c->dt.dbig, 0, sizeof(unsigned int) * n, c->stream));
+    if (c->dt.dsg) CK(cudaMemsetAsync(c->dt.dsg, 0, sizeof(unsigned int) * n, c->stream));
+    if (c->dt.jsg) CK(cudaMemsetAsync(c->dt.jsg, 0, sizeof(unsigned long long) * n, c->stream));
   }
   if (c->run_tallies) {
     CK(cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * c->dims.nsed, c->stream));
@@ -1401,16 +1644,20 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   const DevModel& m = c->dm;
   const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
   const int ndg = c->ndg_in;
+  // device slot s goes to the species it holds in the (nrg,ntg,npg,ndg) layout; slots = 1 for a per-cell tally
   auto scatter = [&](const std::vector<unsigned long long>& src, int slots, int64_t* dst) {
     std::fill(dst, dst + n4 * slots, 0);
-    for (int s = 0; s < std::min(slots, kSlots); ++s)
+    for (int s = 0; s < std::min(slots, kSlots); ++s) {
+      const int id = slots == 1 ? 0 : slot_src(c, s, slots);
+      if (id < 0) continue;
       for (int ip = 1; ip < m.npg; ++ip)
         for (int it = 1; it < m.ntg; ++it)
           for (int ir = 1; ir < m.nrg; ++ir) {
             const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
             const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
-            dst[c4 + n4 * s] = (int64_t)src[(size_t)s * n + cc];
+            dst[c4 + n4 * id] = (int64_t)src[(size_t)s * n + cc];
           }
+    }
   };
   std::vector<unsigned long long> buf;
   if (out->nabs) {
@@ -1444,6 +1691,22 @@ extern "C" int hc3d_get_tallies(hc3d_ctx* c, const hc3d_run_params* p, hc3d_tall
   int r;
   if (out->killed && (r = scatter32(c->dt.killed, out->killed))) return r;
   if (out->dbig && (r = scatter32(c->dt.dbig, out->dbig))) return r;
+  if (out->dsg) {
+    if (c->dt.dsg) {
+      if ((r = scatter32(c->dt.dsg, out->dsg))) return r;
+    } else {
+      std::fill(out->dsg, out->dsg + n4, 0);
+    }
+  }
+  if (out->jsg) {
+    if (c->dt.jsg) {
+      buf.resize((size_t)n);
+      if (int r_ = d2h(c, buf.data(), c->dt.jsg, sizeof(unsigned long long) * n)) return r_;
+      scatter(buf, 1, out->jsg);
+    } else {
+      std::fill(out->jsg, out->jsg + n4, 0);
+    }
+  }
   unsigned long long cnt[16];
   if (int r_ = d2h(c, cnt, c->dt.counters, sizeof(cnt))) return r_;
   for (int k = 0; k < 16; ++k) out->counters[k] = (int64_t)cnt[k];
@@ -1462,24 +1725,47 @@ LucyArgs lucy_args(hc3d_ctx* c, double ltot, int64_t np) {
   a.path_scale = c->dt.path_scale;
   a.tsub = c->tsub;
   a.na_min = 1.0e4;
-  a.nslots = std::min(c->ndg_in, kSlots);
+  a.nslots = 0;  // the slots the host arrays describe (a prefix: the species ascend)
+  for (int s = 0; s < kSlots; ++s)
+    if (slot_src(c, s, c->ndg_in) >= 0) a.nslots = s + 1;
   return a;
 }
 
-// the device temperatures into the reference's (nrg,ntg,npg,ndg) layout
+IntMeanArgs intmean_args(hc3d_ctx* c, double ltot, int64_t np) {
+  IntMeanArgs a{};
+  a.ncell = c->dm.ncell;
+  a.nr1 = c->dm.nrg - 1;
+  a.path_scale = c->dt.path_scale;
+  a.jconst = 1.0 / c->dm.sg_jfacd / (4.0 * 3.1415926535897932384626433);
+  a.nphot = (double)np;
+  a.ltot = ltot;
+  a.isrfkap_int = c->isrfkap_int;
+  a.nemit = c->dm.sg_nemit;
+  a.rarr = c->dm.rarr;
+  a.vcell = c->d_vcell;
+  a.uratio = c->d_uratio;
+  return a;
+}
+
+// the device temperatures into the reference's (nrg,ntg,npg,ndg) layout; the
+// species no slot carries keep the 0.1 K floor of the starting field
 int tdust_to_host(hc3d_ctx* c, double* tdust_out) {
   const DevModel& m = c->dm;
   const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
   std::vector<double> td((size_t)4 * n);
   if (int r_ = d2h(c, td.data(), c->d_tdust, sizeof(double) * td.size())) return r_;
-  for (int s = 0; s < std::min(c->ndg_in, kSlots); ++s)
+  std::fill(tdust_out, tdust_out + n4 * c->ndg_in, 0.1 / 11605.0);
+  for (int s = 0; s < kSlots; ++s) {
+    const int id = slot_src(c, s, c->ndg_in);
+    if (id < 0) continue;
     for (int ip = 1; ip < m.npg; ++ip)
       for (int it = 1; it < m.ntg; ++it)
         for (int ir = 1; ir < m.nrg; ++ir) {
           const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
           const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
-          tdust_out[c4 + n4 * s] = td[4 * cc + s];
+          tdust_out[c4 + n4 * id] = td[4 * cc + s];
         }
+  }
   return HC3D_OK;
 }
 
@@ -1495,6 +1781,12 @@ extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* td
   k_lucy<<<grid_blocks_for(c, a.ncell), 256, 0, c->stream>>>(a, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust, c->d_tdustf,
                                                            c->d_peelmask, c->d_maxrel, c->dm.rho4f, c->d_rho4p);
   CK(cudaGetLastError());
+  if (c->dm.sg_on) {
+    const IntMeanArgs ia = intmean_args(c, ltot, np);
+    k_intmean<<<grid_blocks_for(c, ia.ncell), 256, 0, c->stream>>>(ia, c->dt.jsg, c->d_imean, c->d_imfract);
+    CK(cudaGetLastError());
+    c->imean_set = true;
+  }
   unsigned long long bits = 0;
   CK(cudaMemcpyAsync(&bits, c->d_maxrel, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -1527,7 +1819,9 @@ extern "C" int hc3d_lucy_iterations(hc3d_ctx* c, const hc3d_run_params* p, int n
     c->epoch_np = 0;
     const int r = prepare_run(c, &q, &args[(size_t)k]);
     if (r) return r;
+    if (c->dm.sg_on) c->imean_set = true;  // the graph's int_mean of iteration k feeds iteration k + 1
   }
+  const IntMeanArgs ia = intmean_args(c, ltot, p->np);
   std::vector<void*> tmp;
   unsigned long long* d_rel = nullptr;
   int r = dalloc(c, tmp, &d_rel, (size_t)n_iter);
@@ -1549,6 +1843,8 @@ extern "C" int hc3d_lucy_iterations(hc3d_ctx* c, const hc3d_run_params* p, int n
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.jmean, 0, sizeof(unsigned long long) * n, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.killed, 0, sizeof(unsigned int) * n, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.dbig, 0, sizeof(unsigned int) * n, st);
+    if (e == cudaSuccess && c->dt.dsg) e = cudaMemsetAsync(c->dt.dsg, 0, sizeof(unsigned int) * n, st);
+    if (e == cudaSuccess && c->dt.jsg) e = cudaMemsetAsync(c->dt.jsg, 0, sizeof(unsigned long long) * n, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.sed, 0, sizeof(unsigned long long) * 9 * c->dims.nsed, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dt.counters, 0, sizeof(unsigned long long) * 16, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_work, 0, sizeof(unsigned long long), st);
@@ -1559,6 +1855,10 @@ extern "C" int hc3d_lucy_iterations(hc3d_ctx* c, const hc3d_run_params* p, int n
       k_lucy<<<grid_blocks_for(c, la.ncell), 256, 0, st>>>(la, c->dt.dtauabs, c->dm.rho4d, c->d_massarr, c->d_tdust,
                                                            c->d_tdustf, c->d_peelmask, d_rel + k, c->dm.rho4f,
                                                            c->d_rho4p);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && c->dm.sg_on) {
+      k_intmean<<<grid_blocks_for(c, ia.ncell), 256, 0, st>>>(ia, c->dt.jsg, c->d_imean, c->d_imfract);
       e = cudaGetLastError();
     }
   }

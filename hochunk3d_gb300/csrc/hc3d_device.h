@@ -9,7 +9,7 @@
 
 namespace hc3d {
 
-constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2, envelope, cavity)
+constexpr int kSlots = 4;   // species slots carried on the device (disk1, disk2, and two of species 3-8)
 constexpr int kNo = 8;      // SED components (output.F90:232-239)
 constexpr int kMaxPeel = 256;
 constexpr int kFaultLog = 256;
@@ -38,6 +38,8 @@ struct DevTallies {
   unsigned long long* jmean;  // [ncell]
   unsigned int* killed;       // [ncell]
   unsigned int* dbig;         // [ncell]
+  unsigned int* dsg;          // [ncell] small-grain absorptions (models with small-grain slots)
+  unsigned long long* jsg;    // [ncell] small-grain absorption path, the input of int_mean (same)
   unsigned long long* counters; // [16]
   double stokes_scale, square_scale, path_scale;
   unsigned long long* fault_log;   // [kFaultLog]: packet id | code << 56
@@ -105,6 +107,20 @@ struct DevModel {
   // table u (nud(i0) >= nu > nud(i0+1)) for ln(nu) in bucket b of [dlnlo[u], dlnlo[u] + kDustGuide/dginv[u])
   const short2* dguide;
   float dlnlo[kSlots], dginv[kSlots];
+  // species of the slots (grid_mod.f90:13-20): bit s of disk_mask = slot s holds a disk species
+  // (absorbed packets take origin 2, propagate.f90:114-119), of sg_mask = small grains
+  unsigned disk_mask, sg_mask;
+  // very small grains and PAHs (emit_common.f90:31-53, rep_draine.f90, draine_cdf.f90)
+  int sg_on;              // 1: sg_mask != 0 and the emission spectra are loaded
+  int sg_slot;            // the slot whose opacity weights the jsg path tally
+  float sg_jfac;          // 1 / (rstar_cm kappa_V) of sg_slot: kapd -> kappa/kappa_V
+  double sg_jfacd;
+  int sg_nemit, sg_nd;    // 18 spectra x 1000 frequencies
+  const double* sg_cdf;   // [j * sg_nd + i]: cdf_d(j+1, i+1)
+  const double* sg_logcdf;// [j * sg_nd + i]: logcdf_d(j+1, i+1)
+  const double* sg_logfreq; // (sg_nd)
+  const int* imean;       // (ncell) spectrum row 1..nemit of each cell (int_mean.f90:64-94)
+  const double* imfract;  // (ncell) its interpolation fraction
 };
 
 // One call of the packet loop.
@@ -128,6 +144,7 @@ struct RunArgs {
   int regen;                 // k_wave regeneration threshold: waiting lanes of a warp before they take new packets
   int qchunk;                // k_wave: peel-off queue slots a lane reserves at a time
   int imcube;                // 1: tally the per-frequency image cube
+  int iter1;                 // 1: the first Lucy iteration (small grains emit from spectrum row 2)
   hc3d_sources src;
   const double* peeldir;     // [npeel][4]: coste sinte cospe sinpe
   const double* aperture2;   // [nap]

@@ -327,6 +327,21 @@ void put_err(char* err, size_t len, const std::string& s) {
 }  // namespace
 
 
+extern "C" int hc3d_model_load(hc3d_model* hm, hc3d_ctx* ctx) {
+  if (!hm || !ctx) return HC3D_ERR_INVALID;
+  const Model& m = hm->m;
+  int r;
+  if ((r = hc3d_set_species(ctx, m.slot_species))) return r;
+  hc3d_dust_tables tv = m.tables_view();
+  hc3d_grid gv = m.grid_view();
+  if ((r = hc3d_load_tables(ctx, &tv)) || (r = hc3d_load_grid(ctx, &gv))) return r;
+  if (m.sg_slot >= 0) {
+    hc3d_sg_tables sg;
+    if ((r = hc3d_model_sg_tables(hm, &sg)) || (r = hc3d_load_sg_tables(ctx, &sg))) return r;
+  }
+  return HC3D_OK;
+}
+
 extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* out_dir, const hc3d_device_opts* opts,
                         hc3d_tts_stats* stats, char* err, size_t errlen) {
   if (!par_path || !out_dir) return HC3D_ERR_INVALID;
@@ -352,10 +367,7 @@ extern "C" int hc3d_tts(const char* par_path, const char* par_dir, const char* o
     hc3d_model_destroy(hm);
     return code;
   };
-  hc3d_dust_tables tv = m.tables_view();
-  hc3d_grid gv = m.grid_view();
-  if ((r = hc3d_load_tables(ctx, &tv))) return bail(r);
-  if ((r = hc3d_load_grid(ctx, &gv))) return bail(r);
+  if ((r = hc3d_model_load(hm, ctx))) return bail(r);
   hc3d_run_params p = m.params_view();
   const int ipeelorig = p.ipeel;
   auto io_fail = [&](int code, const char* what) {

@@ -21,15 +21,17 @@ namespace {
 struct DensParams {
   int nrg, ntg, npg;
   int idiskcurve, ienvtype, ihole, ipoly, ifractal;
-  int fractmask[4];
-  double rho0[2], z1[2], a[2], b[2], rmaxd[2], rddust[2];
-  double fmass[4];
+  // species: 4, or 8 with the small grains; the disk species' ids (0, 1 and 4, 5)
+  int ndg, ndisk, disk_id[4];
+  int fractmask[HC3D_NDG];
+  double rho0[HC3D_NDG], z1[HC3D_NDG], a[HC3D_NDG], b[HC3D_NDG], rmaxd[HC3D_NDG], rddust[HC3D_NDG];
+  double fmass[HC3D_NDG];
   double rc, rhoe0, rmine, rmax, envexp, rhodens1, rhoamb;
   double c1e, ex1, z01, c2e, ex2, z02, rhoconst1, rhoconst2, exf;
   double r3;  // rmincgs^3
   // disk structure (densdiskg.f90:25-155) and the envelope gap (densenv.f90:52-58,114-119)
   int igapd, idiskwarp, nspot, irimcurve, irimpuff, igappuff, igapcurve, ispiral, sn, iradexp;
-  double rgapd1, rgapd2, agap[2], bgap[2], rhogap0[2], z1gap[2];
+  double rgapd1, rgapd2, agap[HC3D_NDG], bgap[HC3D_NDG], rhogap0[HC3D_NDG], z1gap[HC3D_NDG];
   double warpheight, wexp, warplength, rimcurveheight, rimcurvelength, rimcurveexp, rimheight, rimlength;
   double gapheight, gaplength, gapcurveheight, gapcurvelength, gapcurveexp;
   double sw, pitch, rspiral1, rspiral2, radexp;
@@ -165,8 +167,8 @@ __device__ double densenv_dev(const DensParams& P, double rad, double costin, do
   if (ingape && P.igapedens == 1) dens = dens * P.fracte;  // scaled density in the gap
   if (rad >= P.rmax) dens = 0.0;
   if (rad <= P.rmine) dens = 0.0;
-  if (id == 3 && inhole == 0) dens = 0.0;
-  if (id == 2 && inhole == 1) dens = 0.0;
+  if (id % 4 == 3 && inhole == 0) dens = 0.0;
+  if (id % 4 == 2 && inhole == 1) dens = 0.0;
   return dens;
 }
 
@@ -174,7 +176,7 @@ struct Walls {
   const double *rarr, *ravearr, *thetarr, *thetavearr, *phiarr, *densvar;
 };
 
-// unnormalised disk mass of each column (both disk species), for diskscl
+// unnormalised disk mass of each column (every disk species), for diskscl
 __global__ void k_disk_colmass(DensParams P, Walls w, double* colmass) {
   const int ncol = (P.nrg - 1) * (P.ntg - 1);
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -185,7 +187,8 @@ __global__ void k_disk_colmass(DensParams P, Walls w, double* colmass) {
   const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
   const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
   const bool phidep = P.idiskwarp || P.ispiral;
-  for (int id = 0; id < 2; ++id) {
+  for (int k = 0; k < P.ndisk; ++k) {
+    const int id = P.disk_id[k];
     double m = 0.0;
     if (P.rho0[id] != 0.0) {
       const double dd0 = phidep ? 0.0 : densdisk_dev(P, rad, sint, cost, 0.0, id);
@@ -195,7 +198,7 @@ __global__ void k_disk_colmass(DensParams P, Walls w, double* colmass) {
           m += dd * (-dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3);
         }
     }
-    colmass[(size_t)id * ncol + col] = m;
+    colmass[(size_t)k * ncol + col] = m;
   }
 }
 
@@ -229,25 +232,28 @@ __global__ void k_density(DensParams P, Walls w, const double* diskscl, double* 
   const double dr3 = pow(w.rarr[ir + 1], 3.0) - pow(w.rarr[ir], 3.0);
   const double thet = w.thetavearr[it], cost = cos(thet), sint = sin(thet);
   const double dcost = cos(w.thetarr[it + 1]) - cos(w.thetarr[it]);
-  double dens_r[4];
+  double dens_r[HC3D_NDG];
   const bool phidep = P.idiskwarp || P.ispiral;
-  for (int id = 0; id < 2; ++id) dens_r[id] = densdisk_dev(P, rad, sint, cost, 0.0, id) * diskscl[id];
-  for (int id = 2; id < 4; ++id) dens_r[id] = densenv_dev(P, rad, cost, sint, id) * P.fmass[id];
+  for (int id = 0; id < P.ndg; ++id)
+    dens_r[id] = id % 4 < 2 ? densdisk_dev(P, rad, sint, cost, 0.0, id) * diskscl[id]
+                            : densenv_dev(P, rad, cost, sint, id) * P.fmass[id];
   double mdisk = 0.0, menv = 0.0;
   for (int ip = 0; ip < P.npg - 1; ++ip) {
     if (phidep)
-      for (int id = 0; id < 2; ++id)
+      for (int k = 0; k < P.ndisk; ++k) {
+        const int id = P.disk_id[k];
         dens_r[id] = densdisk_dev(P, rad, sint, cost, 0.5 * (w.phiarr[ip] + w.phiarr[ip + 1]), id) * diskscl[id];
+      }
     const double vol = -dr3 * dcost * (w.phiarr[ip + 1] - w.phiarr[ip]) / 3.0 * P.r3;
     const int64_t c = (int64_t)ir + (int64_t)P.nrg * (it + (int64_t)P.ntg * ip);
     vcell[c] = vol;
-    for (int id = 0; id < 4; ++id) {
+    for (int id = 0; id < P.ndg; ++id) {
       double d = dens_r[id];
       if (P.ifractal && P.fractmask[id] == 1)
         d *= w.densvar[ir + (int64_t)(P.nrg - 1) * (it + (int64_t)(P.ntg - 1) * ip)];
       densarr[c + n4 * id] = d;
       massarr[c + n4 * id] = pow(d * vol, 0.25);
-      if (id < 2) mdisk += d * vol;
+      if (id % 4 < 2) mdisk += d * vol;
       else menv += d * vol;
     }
   }
@@ -278,16 +284,24 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   const int nrg = m.nrg, ntg = m.ntg, npg = m.npg;
   const int ncol = (nrg - 1) * (ntg - 1);
   const int64_t n4 = m.n4();
-  if (m.ndg != 4 || ncol <= 0) { *err = "model grid not built"; return HC3D_ERR_STATE; }
+  if ((m.ndg != 4 && m.ndg != 8) || ncol <= 0 || m.densarr.size() != (size_t)n4 * m.ndg) {
+    *err = "model grid not built";
+    return HC3D_ERR_STATE;
+  }
+  const int ndg = m.ndg;
   DensParams P;
   std::memset(&P, 0, sizeof P);
   P.nrg = nrg; P.ntg = ntg; P.npg = npg;
   P.idiskcurve = m.idiskcurve; P.ienvtype = m.ienvtype; P.ihole = m.ihole; P.ipoly = m.ipoly;
   P.ifractal = m.ifractal;
-  for (int id = 0; id < 4; ++id) { P.fractmask[id] = m.fractmask[id]; P.fmass[id] = m.fmass[id]; }
-  for (int id = 0; id < 2; ++id) {
+  P.ndg = ndg;
+  P.ndisk = ndg == 8 ? 4 : 2;
+  P.disk_id[0] = 0; P.disk_id[1] = 1; P.disk_id[2] = 4; P.disk_id[3] = 5;
+  for (int id = 0; id < HC3D_NDG; ++id) {
+    P.fractmask[id] = m.fractmask[id]; P.fmass[id] = m.fmass[id];
     P.rho0[id] = m.rho0[id]; P.z1[id] = m.z1[id]; P.a[id] = m.a[id]; P.b[id] = m.b[id];
     P.rmaxd[id] = m.rmaxd[id]; P.rddust[id] = m.rddust[id];
+    P.agap[id] = m.agap[id]; P.bgap[id] = m.bgap[id]; P.rhogap0[id] = m.rhogap0[id]; P.z1gap[id] = m.z1gap[id];
   }
   P.rc = m.rc; P.rhoe0 = m.rhoe0; P.rmine = m.rmine; P.rmax = m.rmax; P.envexp = m.envexp;
   P.rhodens1 = m.rhodens1; P.rhoamb = m.rhoamb;
@@ -297,9 +311,6 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   P.irimpuff = m.irimpuff; P.igappuff = m.igappuff; P.igapcurve = m.igapcurve; P.ispiral = m.ispiral;
   P.sn = m.sn; P.iradexp = m.iradexp;
   P.rgapd1 = m.rgapd1; P.rgapd2 = m.rgapd2;
-  for (int id = 0; id < 2; ++id) {
-    P.agap[id] = m.agap[id]; P.bgap[id] = m.bgap[id]; P.rhogap0[id] = m.rhogap0[id]; P.z1gap[id] = m.z1gap[id];
-  }
   P.warpheight = m.warpheight; P.wexp = m.wexp; P.warplength = m.warplength;
   P.rimcurveheight = m.rimcurveheight; P.rimcurvelength = m.rimcurvelength; P.rimcurveexp = m.rimcurveexp;
   P.rimheight = m.rimheight; P.rimlength = m.rimlength; P.gapheight = m.gapheight; P.gaplength = m.gaplength;
@@ -314,8 +325,9 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
          *d_ta = B.alloc<double>(ntg), *d_p = B.alloc<double>(npg);
   const size_t nvar = m.ifractal ? m.densvar.size() : 1;
   double* d_var = B.alloc<double>(nvar);
-  double *d_dens = B.alloc<double>((size_t)n4 * 4), *d_mass = B.alloc<double>((size_t)n4 * 4),
-         *d_vol = B.alloc<double>((size_t)n4), *d_col = B.alloc<double>((size_t)2 * ncol), *d_s = B.alloc<double>(4);
+  // d_s: the column sums [0, 8), then diskscl [8, 16)
+  double *d_dens = B.alloc<double>((size_t)n4 * ndg), *d_mass = B.alloc<double>((size_t)n4 * ndg),
+         *d_vol = B.alloc<double>((size_t)n4), *d_col = B.alloc<double>((size_t)4 * ncol), *d_s = B.alloc<double>(16);
   if (!d_r || !d_ra || !d_t || !d_ta || !d_p || !d_var || !d_dens || !d_mass || !d_vol || !d_col || !d_s) {
     *err = "device allocation failed";
     return HC3D_ERR_NOMEM;
@@ -329,8 +341,8 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
     return HC3D_ERR_CUDA;
   }
   // zero the wall-index entries (ir = nrg, it = ntg, ip = npg) as the host arrays have them
-  cudaMemset(d_dens, 0, sizeof(double) * n4 * 4);
-  cudaMemset(d_mass, 0, sizeof(double) * n4 * 4);
+  cudaMemset(d_dens, 0, sizeof(double) * n4 * ndg);
+  cudaMemset(d_mass, 0, sizeof(double) * n4 * ndg);
   cudaMemset(d_vol, 0, sizeof(double) * n4);
   Walls w{d_r, d_ra, d_t, d_ta, d_p, d_var};
   cudaEvent_t e0, e1;
@@ -339,23 +351,24 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   const int threads = 128, blocks = (ncol + threads - 1) / threads;
   cudaEventRecord(e0);
   // disk mass normalisation: diskscl = massd * fmass / mass on the grid
-  double diskscl[2] = {1.0, 1.0};
+  double diskscl[HC3D_NDG] = {1, 1, 1, 1, 1, 1, 1, 1};
   if (m.massd > 0.0) {
     k_disk_colmass<<<blocks, threads>>>(P, w, d_col);
-    k_sum_columns<<<1, 256>>>(d_col, ncol, 2, d_s);
-    double tm[2];
-    if (cudaMemcpy(tm, d_s, sizeof(tm), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    k_sum_columns<<<1, 256>>>(d_col, ncol, P.ndisk, d_s);
+    double tm[4];
+    if (cudaMemcpy(tm, d_s, sizeof(double) * P.ndisk, cudaMemcpyDeviceToHost) != cudaSuccess) {
       *err = "disk mass reduction failed";
       return HC3D_ERR_CUDA;
     }
-    for (int id = 0; id < 2; ++id) {
+    for (int k = 0; k < P.ndisk; ++k) {
+      const int id = P.disk_id[k];
       if (m.rho0[id] == 0.0) continue;
-      const double tmp = tm[id] / kMsun;
+      const double tmp = tm[k] / kMsun;
       if (tmp > 0.0) diskscl[id] = m.massd * m.fmass[id] / tmp;
     }
   }
-  cudaMemcpy(d_s + 2, diskscl, sizeof(diskscl), cudaMemcpyHostToDevice);
-  k_density<<<blocks, threads>>>(P, w, d_s + 2, d_dens, d_mass, d_vol, d_col);
+  cudaMemcpy(d_s + 8, diskscl, sizeof(diskscl), cudaMemcpyHostToDevice);
+  k_density<<<blocks, threads>>>(P, w, d_s + 8, d_dens, d_mass, d_vol, d_col);
   k_sum_columns<<<1, 256>>>(d_col, ncol, 2, d_s);
   cudaEventRecord(e1);
   if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
@@ -368,11 +381,11 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   cudaEventDestroy(e1);
   if (ms) *ms = t;
   double sums[2];
-  m.densarr.resize((size_t)n4 * 4);
-  m.massarr.resize((size_t)n4 * 4);
+  m.densarr.resize((size_t)n4 * ndg);
+  m.massarr.resize((size_t)n4 * ndg);
   m.vcell.resize((size_t)n4);
-  if (cudaMemcpy(m.densarr.data(), d_dens, sizeof(double) * n4 * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
-      cudaMemcpy(m.massarr.data(), d_mass, sizeof(double) * n4 * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+  if (cudaMemcpy(m.densarr.data(), d_dens, sizeof(double) * n4 * ndg, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(m.massarr.data(), d_mass, sizeof(double) * n4 * ndg, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(m.vcell.data(), d_vol, sizeof(double) * n4, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(sums, d_s, sizeof(sums), cudaMemcpyDeviceToHost) != cudaSuccess) {
     *err = "download failed";

@@ -668,6 +668,8 @@ static bool isrf_cdf(Model* m, std::string* err) {
   }
   cdf[0] = 0.0;
   for (int i = 1; i < n; ++i) cdf[i] = cdf[i - 1] + 0.5 * (pdf[i] + pdf[i - 1]) * (freq[i] - freq[i - 1]);
+  m->isrf_pdf = pdf;
+  m->isrf_fhz = freq;
   m->isrf_int = cdf[n - 1];
   if (!(m->isrf_int > 0.0)) { *err = "ISRF_FILE integrates to zero"; return false; }
   cdf[0] = 0.0;
@@ -682,6 +684,87 @@ static bool isrf_cdf(Model* m, std::string* err) {
   m->isrf_cdfv = cdf;
   m->isrf_logcdf = logcdf;
   m->isrf_logfreq = logfreq;
+  return true;
+}
+
+// The ISRF weighted by the absorption opacity of the small grains, the unit
+// of the mean-intensity ratio of int_mean (isrf_cdf.f90:199-209): the
+// trapezoid sum of pdf(nu) kappa(nu) kappa_V (1 - albedo(nu)) over the
+// field's rows, the opacity at 1.2398 / (2.9979e14 / nu).  The reference
+// takes species 5's dust; here it is the small-grain species of the first
+// device slot that holds one (sg_slot), whose opacity also weights the
+// device's path tally, so that the ratio is formed from one dust file.  The
+// two agree whenever that species reads species 5's file.
+static void sg_isrf_weight(Model* m) {
+  m->sg_slot = -1;
+  for (int s = 0; s < 4 && m->sg_slot < 0; ++s)
+    if (m->slot_species[s] >= 5) m->sg_slot = s;
+  m->isrfkap_int = 0.0;
+  if (m->sg_slot < 0) return;
+  const int id = m->slot_species[m->sg_slot] - 1;
+  const std::vector<double>& pdf = m->isrf_pdf;
+  const std::vector<double>& freq = m->isrf_fhz;
+  for (size_t i = 1; i < freq.size(); ++i) {
+    const double testnu = 1.2398 / (2.9979e14 / freq[i]);
+    double kappa, albedo;
+    opacset1(*m, id, testnu, &kappa, &albedo);
+    m->isrfkap_int += 0.5 * (pdf[i] + pdf[i - 1]) * (freq[i] - freq[i - 1]) * kappa * m->kappav[id] * (1.0 - albedo);
+  }
+}
+
+// draine_cdf (draine_cdf.f90:1-79): the small grains' emission spectra for
+// 18 ratios U of the mean intensity to the ISRF's, each 1000 rows
+// (lambda [um], j_nu) read from emit_draine_<U>.dat in PARDIR, reordered to
+// increasing frequency 1.2398/lambda, integrated by the trapezoid rule and
+// normalised; row 1 keeps logcdf = -10 and logfreq = 0, as the Fortran sets
+// them.
+static bool draine_cdf(Model* m, std::string* err) {
+  static const char* const names[kNemit] = {"0.50", "1.00", "2.00", "5.00", "10.0", "20.0", "30.0", "1e2", "3e2",
+                                            "1e3",  "3e3",  "1e4",  "3e4",  "1e5",  "3e5",  "1e6",  "3e6", "1e7"};
+  static const float uratio[kNemit] = {0.5f, 1.0f,  2.0f,  5.0f,  10.0f, 20.0f, 30.0f, 1.e2f, 3.e2f,
+                                       1.e3f, 3.e3f, 1.e4f, 3.e4f, 1.e5f, 3.e5f, 1.e6f, 3.e6f, 1.e7f};
+  const int nd = kNdraine;
+  std::vector<double> pdf((size_t)kNemit * nd), freq(nd);
+  for (int j = 0; j < kNemit; ++j) {
+    const std::string path = m->pardir + "/emit_draine_" + names[j] + ".dat";
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) { *err = "FSG > 0: cannot open the small-grain emission spectrum " + path; return false; }
+    for (int i = 0; i < nd; ++i) {
+      double lam, p;
+      if (std::fscanf(f, "%lf %lf", &lam, &p) != 2 || !(lam > 0.0)) {
+        std::fclose(f);
+        *err = path + " holds fewer than 1000 rows of lambda [um] and j_nu";
+        return false;
+      }
+      pdf[(size_t)j * nd + (nd - 1 - i)] = p;
+      freq[nd - 1 - i] = 1.2398 / lam;
+    }
+    std::fclose(f);
+  }
+  for (int i = 1; i < nd; ++i)
+    if (!(freq[i] > freq[i - 1])) { *err = "emit_draine_*.dat: wavelengths must increase down the file"; return false; }
+  m->sg_logcdf.assign((size_t)kNemit * nd, 0.0);
+  m->sg_cdf.assign((size_t)kNemit * nd, 0.0);
+  m->sg_logfreq.assign(nd, 0.0);
+  m->sg_uratio.assign(kNemit, 0.0);
+  std::vector<double> cdf(nd);
+  for (int j = 0; j < kNemit; ++j) {
+    const double* pj = &pdf[(size_t)j * nd];
+    cdf[0] = 0.0;
+    for (int i = 1; i < nd; ++i) cdf[i] = cdf[i - 1] + 0.5 * (pj[i] + pj[i - 1]) * (freq[i] - freq[i - 1]);
+    if (!(cdf[nd - 1] > 0.0)) { *err = std::string("emit_draine_") + names[j] + ".dat integrates to zero"; return false; }
+    // cdf_d and logcdf_d (nemit, ndraine), Fortran order: spectrum j, frequency i at j + nemit i
+    m->sg_logcdf[(size_t)j] = -10.0;
+    m->sg_cdf[(size_t)j] = 0.0;
+    for (int i = 1; i < nd; ++i) {
+      const double v = cdf[i] / cdf[nd - 1];
+      m->sg_cdf[(size_t)j + (size_t)kNemit * i] = v;
+      m->sg_logcdf[(size_t)j + (size_t)kNemit * i] = std::log10(v);
+    }
+    m->sg_uratio[j] = (double)uratio[j];
+  }
+  m->sg_logfreq[0] = 0.0;
+  for (int i = 1; i < nd; ++i) m->sg_logfreq[i] = std::log10(freq[i]);
   return true;
 }
 
@@ -851,9 +934,32 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
   REQ(P.str("DUSTNAME(4)", &sv, err)); m->dustname[3] = sv;
   REQ(P.real("FSG(3)", &fsg[2], err));
   REQ(P.real("FSG(4)", &fsg[3], err));
-  for (int k = 0; k < 4; ++k)
-    if (fsg[k] != 0.0) { *err = "FSG > 0 (small-grain emission) is not supported"; return false; }
-  m->fmass[0] = fmassd1; m->fmass[1] = 1.0 - fmassd1; m->fmass[2] = 1.0; m->fmass[3] = 1.0;
+  for (int k = 0; k < 4; ++k) {
+    if (!(fsg[k] >= 0.0 && fsg[k] <= 1.0)) { *err = "FSG(1..4) must lie in [0, 1]"; return false; }
+    m->fsg[k] = fsg[k];
+  }
+  // the small-grain species 5-8 take the FSG share of their parent's mass
+  // (reapar.f90:259-262,338-339,419-420); their dust files are read when
+  // any FSG is above zero (species 5's opacity weights the ISRF integral)
+  if (m->has_sg()) {
+    for (int d = 5; d <= 8; ++d) {
+      char key[64];
+      snprintf(key, sizeof key, "DUSTNAME(%d)", d);
+      REQ(P.str(key, &sv, err)); m->dustname[d - 1] = sv;
+    }
+    if (m->isrf_file.empty()) {
+      if (!P.has("ISRF_FILE")) {
+        *err = "FSG > 0 needs ISRF_FILE: the small grains' emission spectrum is chosen by the mean intensity "
+               "in units of the ISRF absorbed by them";
+        return false;
+      }
+      REQ(P.str("ISRF_FILE", &sv, err)); m->isrf_file = m->pardir + "/" + sv;
+    }
+  }
+  m->fmass[0] = fmassd1 * (1.0 - fsg[0]); m->fmass[4] = fmassd1 * fsg[0];
+  m->fmass[1] = (1.0 - fmassd1) * (1.0 - fsg[1]); m->fmass[5] = (1.0 - fmassd1) * fsg[1];
+  m->fmass[2] = 1.0 - fsg[2]; m->fmass[6] = fsg[2];
+  m->fmass[3] = 1.0 - fsg[3]; m->fmass[7] = fsg[3];
   for (int d = 0; d < 2; ++d) m->rddust[d] = m->rmind_in[d] = rmind_in[d];
   REQ(P.real("RMAX", &m->rmax, err));
   double rmine_in;
@@ -872,7 +978,7 @@ static bool read_par(Model* m, const ParFile& P, const std::string* par_dir, std
     REQ(P.real("DENSRATIO", &m->densratio, err));
     REQ(P.ints("FRACTMASK", &fm, err));
     REQ(P.integer("IFSEED", &m->ifseed, err));
-    for (size_t k = 0; k < 4 && k < fm.size(); ++k) m->fractmask[k] = (int)fm[k];
+    for (size_t k = 0; k < 4 && k < fm.size(); ++k) m->fractmask[k] = m->fractmask[k + 4] = (int)fm[k];
     if (P.has("FRACTLEV")) { REQ(P.integer("FRACTLEV", &iv, err)); m->fractlev = (int)iv; }
     if (P.has("FRACTN")) { REQ(P.integer("FRACTN", &iv, err)); m->fractn = (int)iv; }
     if (P.has("FRACTCONTRAST")) REQ(P.real("FRACTCONTRAST", &m->fractcontrast, err));
@@ -1017,10 +1123,23 @@ static void envset(Model* m) {
   }
 }
 
+// The small-grain disk species 5 and 6 share the geometry of disk species 1
+// and 2 (reapar.f90:239-268: scale heights, exponents, radii, gap law; the
+// fractal mask of species 5-8 is that of 1-4).  Called after each step that
+// moves the parents' geometry.
+static void sg_geometry(Model* m) {
+  for (int d = 0; d < 2; ++d) {
+    m->z1[d + 4] = m->z1[d]; m->a[d + 4] = m->a[d]; m->b[d + 4] = m->b[d];
+    m->rmaxd[d + 4] = m->rmaxd[d]; m->rddust[d + 4] = m->rddust[d];
+    m->z1gap[d + 4] = m->z1gap[d]; m->agap[d + 4] = m->agap[d]; m->bgap[d + 4] = m->bgap[d];
+    m->rhoscale_gap[d + 4] = m->rhoscale_gap[d];
+  }
+}
+
 // setup_wave, setup_wave.f90:46-80: disk rho0 before gridset rescales it.
 static void setup_rho0(Model* m) {
   const double rmincgs = m->rstar * kRsun;
-  for (int id = 0; id < 2; ++id) {
+  for (int id : {0, 1, 4, 5}) {
     const double z1cgs = rmincgs * m->z1[id];
     const double p = m->b[id] - m->a[id];
     const double rmind = m->rddust[id];
@@ -1256,7 +1375,11 @@ static bool gridset(Model* m, std::string* err) {
 
   // ---- densities (gridset.f90:954-1098) ----
   const auto t_dens = std::chrono::steady_clock::now();
-  m->ndg = 4;  // disk1, disk2, envelope, cavity slots; small-grain slots 5-8 are empty
+  // species: disk 1, disk 2, envelope, cavity, and with FSG > 0 their
+  // small-grain shares 5-8 (grid_mod.f90:13-20)
+  m->ndg = m->has_sg() ? 8 : 4;
+  std::vector<int> disk_ids = {0, 1}, env_ids = {2, 3};
+  if (m->ndg == 8) { disk_ids = {0, 1, 4, 5}; env_ids = {2, 3, 6, 7}; }
   const int64_t n4 = m->n4();
   m->densarr.assign(n4 * m->ndg, 0.0);
   m->massarr.assign(n4 * m->ndg, 0.0);
@@ -1267,7 +1390,7 @@ static bool gridset(Model* m, std::string* err) {
   // the gap's density scale: rho0 times RHOSCALE_GAP times the ratio of the
   // surface densities just outside and just inside the gap's outer wall,
   // integrated over theta and phi with rhogap0 = rho0 (gridset.f90:906-942)
-  for (int id = 0; id < 2; ++id) m->rhogap0[id] = m->rho0[id];
+  for (int id : disk_ids) m->rhogap0[id] = m->rho0[id];
   if (m->igapd) {
     double rhogap[2];
     for (int id = 0; id < 2; ++id) {
@@ -1296,12 +1419,15 @@ static bool gridset(Model* m, std::string* err) {
       rhogap[id] = m->rho0[id] * m->rhoscale_gap[id] * sig[1] / sig[0];
     }
     for (int id = 0; id < 2; ++id) m->rhogap0[id] = rhogap[id];
+    // the small grains' gap scale follows their parent's (gridset.f90:950-951)
+    for (int id = 4; id < 6; ++id)
+      m->rhogap0[id] = m->fmass[id - 4] > 0.0 ? m->fmass[id] / m->fmass[id - 4] * m->rhogap0[id - 4] : 0.0;
   }
   // disk mass normalisation: diskscl = massd*fmass / mass on the grid
-  double diskscl[2] = {1.0, 1.0};
+  double diskscl[HC3D_NDG] = {1, 1, 1, 1, 1, 1, 1, 1};
   if (m->massd > 0.0) {
-    double tmpmass[2] = {0, 0};
-    for (int id = 0; id < 2; ++id) {
+    double tmpmass[HC3D_NDG] = {0};
+    for (int id : disk_ids) {
       if (m->rho0[id] == 0.0) continue;
       for (int ir = 0; ir < nrg - 1; ++ir) {
         const double rad = m->ravearr[ir];
@@ -1332,23 +1458,23 @@ static bool gridset(Model* m, std::string* err) {
     for (int it = 0; it < ntg - 1; ++it) {
       const double thet = m->thetavearr[it], cost = std::cos(thet), sint = std::sin(thet);
       const double dcost = std::cos(m->thetarr[it + 1]) - std::cos(m->thetarr[it]);
-      double dens_r[4];
-      for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, 0.0, id) * diskscl[id];
-      for (int id = 2; id < 4; ++id) dens_r[id] = densenv(*m, rad, thet, cost, sint, id) * m->fmass[id];
+      double dens_r[HC3D_NDG];
+      for (int id : disk_ids) dens_r[id] = densdisk(*m, rad, sint, cost, 0.0, id) * diskscl[id];
+      for (int id : env_ids) dens_r[id] = densenv(*m, rad, thet, cost, sint, id) * m->fmass[id];
       for (int ip = 0; ip < npg - 1; ++ip) {
         if (phidep)
-          for (int id = 0; id < 2; ++id) dens_r[id] = densdisk(*m, rad, sint, cost, phic(ip), id) * diskscl[id];
+          for (int id : disk_ids) dens_r[id] = densdisk(*m, rad, sint, cost, phic(ip), id) * diskscl[id];
         const double dpp = m->phiarr[ip + 1] - m->phiarr[ip];
         const double vol = -dr3 * dcost * dpp / 3.0 * r3;
         const int64_t c = cell(ir, it, ip);
         m->vcell[c] = vol;
-        for (int id = 0; id < 4; ++id) {
+        for (int id = 0; id < m->ndg; ++id) {
           double d = dens_r[id];
           if (m->ifractal && m->fractmask[id] == 1)
             d *= m->densvar[ir + (int64_t)(nrg - 1) * (it + (int64_t)(ntg - 1) * ip)];
           m->densarr[c + n4 * id] = d;
           m->massarr[c + n4 * id] = std::pow(d * vol, 0.25);
-          if (id < 2) m->massdisk += d * vol; else m->massenv += d * vol;
+          if (id % 4 < 2) m->massdisk += d * vol; else m->massenv += d * vol;
         }
       }
     }
@@ -1356,10 +1482,34 @@ static bool gridset(Model* m, std::string* err) {
   m->massdisk /= kMsun;
   m->massenv /= kMsun;
   m->ndg_active = 0;
+  bool filled[HC3D_NDG] = {false};
   for (int id = 0; id < m->ndg; ++id) {
     bool any = false;
     for (int64_t k = 0; k < n4 && !any; ++k) any = m->densarr[k + n4 * id] > 0.0;
+    filled[id] = any;
     if (any) m->ndg_active++;
+  }
+  // The device carries four species slots: disk 1 and disk 2 in slots 1-2
+  // (the accretion source draws among them), and two more.  Without small
+  // grains those are the envelope and the cavity; with them, the species
+  // among 3-8 that hold density, in their order.
+  m->slot_species[0] = 1; m->slot_species[1] = 2; m->slot_species[2] = 3; m->slot_species[3] = 4;
+  if (m->ndg == 8) {
+    std::vector<int> more;
+    for (int id = 2; id < 8; ++id)
+      if (filled[id]) more.push_back(id + 1);
+    if (more.size() > 2) {
+      *err = "FSG > 0: more than four species hold density (disk 1, disk 2 and " + std::to_string(more.size()) +
+             " of envelope, cavity and the small grains); the device carries four species";
+      return false;
+    }
+    for (int cand : {3, 4, 5, 6, 7, 8}) {
+      if (more.size() >= 2) break;
+      if (std::find(more.begin(), more.end(), cand) == more.end()) more.push_back(cand);
+    }
+    std::sort(more.begin(), more.end());
+    m->slot_species[2] = more[0]; m->slot_species[3] = more[1];
+    sg_isrf_weight(m);
   }
   m->density_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_dens).count();
   // initarr(.true.): tdust2 = 0.1 K, tdust = tdust2 (initarr.f90:50,78-84)
@@ -1378,8 +1528,8 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
   if (!P.load(par_path, err)) return false;
   if (!read_par(m, P, par_dir, err)) return false;
   envset(m);
-  // dustinit: one table per slot; identical files are read and integrated once
-  m->ndg = 4;
+  // dustinit: one table per species; identical files are read and integrated once
+  m->ndg = m->has_sg() ? 8 : 4;
   m->nlambda.assign(m->ndg, 0);
   const size_t nl = (size_t)m->nlammax * m->ndg;
   m->nudust.assign(nl, 0); m->kappad.assign(nl, 0); m->adust.assign(nl, 0);
@@ -1412,11 +1562,14 @@ bool build_model(Model* m, const std::string& par_path, const std::string* par_d
   }
   m->tables_host_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tab).count();
   if (!atmosinit(m, m->atname, err)) return false;
-  if (m->iout && !isrf_cdf(m, err)) return false;
+  if ((m->iout || m->has_sg()) && !isrf_cdf(m, err)) return false;
+  if (m->has_sg() && !draine_cdf(m, err)) return false;
+  sg_geometry(m);
   setup_rho0(m);
   for (int d = 0; d < 2; ++d) m->src.kapv[d] = 0.0;
   if (!luminosities(m, err)) return false;
   for (int d = 0; d < 2; ++d) m->src.kapv[d] = m->kappav[d] * (m->rstar * kRsun);
+  sg_geometry(m);
   if (!gridset(m, err)) return false;
   return true;
 }
@@ -1475,6 +1628,9 @@ hc3d_model_info Model::info() const {
   i.lstar = lstar; i.l_isrf = l_isrf; i.isrf_frac = isrf_frac;
   i.lacc = lacc; i.lacc2 = lacc2; i.accfrac = accfrac; i.accfrac2 = accfrac2; i.mdot_msun_yr = mdotdisk;
   i.tshock_k = tshock_k; i.fspot = fspot; i.thspot_deg = thspot_deg; i.tave_k = tave_k;
+  for (int s = 0; s < 4; ++s) i.slot_species[s] = slot_species[s];
+  i.has_sg = sg_slot >= 0 ? 1 : 0;
+  i.ndg = ndg;
   return i;
 }
 
@@ -1524,6 +1680,22 @@ extern "C" int hc3d_model_views(hc3d_model* m, hc3d_dust_tables* t, hc3d_grid* g
   if (g) *g = m->m.grid_view();
   if (p) *p = m->m.params_view();
   if (info) *info = m->m.info();
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_model_sg_tables(hc3d_model* m, hc3d_sg_tables* sg) {
+  if (!m || !sg) return HC3D_ERR_INVALID;
+  const hc3d::Model& M = m->m;
+  if (M.sg_slot < 0) return HC3D_ERR_STATE;
+  std::memset(sg, 0, sizeof *sg);
+  sg->nemit = hc3d::kNemit;
+  sg->ndraine = hc3d::kNdraine;
+  sg->cdf = M.sg_cdf.data();
+  sg->logcdf = M.sg_logcdf.data();
+  sg->logfreq = M.sg_logfreq.data();
+  sg->uratio = M.sg_uratio.data();
+  sg->isrfkap_int = M.isrfkap_int;
+  sg->sg_slot = M.sg_slot + 1;
   return HC3D_OK;
 }
 
@@ -1623,6 +1795,41 @@ extern "C" int hc3d_write_synthetic_isrf(const char* path) {
     std::fprintf(f, " %.4f  %.4f\n", lnu, std::log10(std::max(s, 1.0e-300)));
   }
   std::fclose(f);
+  return HC3D_OK;
+}
+
+extern "C" int hc3d_write_synthetic_draine(const char* dir) {
+  // j_nu of grains heated by U times the ISRF: PAH bands (Gaussians in
+  // lambda at 3.3, 6.2, 7.7, 8.6, 11.3, 12.7 um) plus a modified blackbody
+  // nu^(3+2) / (exp(h nu / k T) - 1) at T = 18 K U^(1/6), both scaling with
+  // U; 1000 rows, lambda log-spaced over 1-1000 um.
+  if (!dir) return HC3D_ERR_INVALID;
+  static const char* const names[hc3d::kNemit] = {"0.50", "1.00", "2.00", "5.00", "10.0", "20.0",
+                                                 "30.0", "1e2",  "3e2",  "1e3",  "3e3",  "1e4",
+                                                 "3e4",  "1e5",  "3e5",  "1e6",  "3e6",  "1e7"};
+  static const double U[hc3d::kNemit] = {0.5, 1, 2, 5, 10, 20, 30, 1e2, 3e2, 1e3, 3e3, 1e4, 3e4, 1e5, 3e5, 1e6, 3e6, 1e7};
+  const double band[6] = {3.3, 6.2, 7.7, 8.6, 11.3, 12.7}, width[6] = {0.04, 0.1, 0.3, 0.15, 0.2, 0.3},
+               amp[6] = {0.5, 1.0, 2.0, 0.6, 1.2, 0.5};
+  const double h = 6.62607015e-27, k = 1.380649e-16, c = 2.99792458e14;  // c in um/s
+  for (int j = 0; j < hc3d::kNemit; ++j) {
+    const std::string path = std::string(dir) + "/emit_draine_" + names[j] + ".dat";
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) return HC3D_ERR_IO;
+    const double T = 18.0 * std::pow(U[j], 1.0 / 6.0);
+    // the continuum's peak nu^5/(e^x - 1) sits near x = 4.97: normalise it to 1 there
+    const double xpk = 4.965, nupk = xpk * k * T / h;
+    const double cpk = std::pow(nupk, 5.0) / std::expm1(xpk);
+    for (int i = 0; i < hc3d::kNdraine; ++i) {
+      const double lam = std::pow(10.0, 3.0 * i / (double)(hc3d::kNdraine - 1));
+      const double nu = c / lam, x = h * nu / (k * T);
+      double cont = x < 700.0 ? std::pow(nu, 5.0) / std::expm1(x) / cpk : 0.0;
+      double pah = 0.0;
+      for (int b = 0; b < 6; ++b) pah += amp[b] * std::exp(-0.5 * std::pow((lam - band[b]) / width[b], 2.0));
+      const double jnu = U[j] * (0.3 * pah + cont) * 1.0e-18 + 1.0e-40;
+      std::fprintf(f, " %12.5f  %12.5e\n", lam, jnu);
+    }
+    std::fclose(f);
+  }
   return HC3D_OK;
 }
 

@@ -42,6 +42,8 @@ class ParFile {
 };
 
 constexpr int kNisrf = 200;  // isrf_mod nisrf
+constexpr int kNemit = 18;     // draine_mod nemit: mean-intensity ratios of the small-grain spectra
+constexpr int kNdraine = 1000; // draine_mod ndraine: frequencies of each spectrum
 constexpr int kNtab = 100;   // tabl_mod ntab (module not shipped; restated)
 
 struct Model {
@@ -78,7 +80,8 @@ struct Model {
   // warp, puffed and curved inner rim and outer gap wall, radial cutoff
   int igapd = 0, ispiral = 0, idiskwarp = 0, irimpuff = 0, igappuff = 0, irimcurve = 0, igapcurve = 0, iradexp = 0;
   double rgapd1 = 0, rgapd2 = 0;
-  double z1gap[2] = {0, 0}, agap[2] = {0, 0}, bgap[2] = {0, 0}, rhoscale_gap[2] = {0, 0}, rhogap0[2] = {0, 0};
+  double z1gap[HC3D_NDG] = {0}, agap[HC3D_NDG] = {0}, bgap[HC3D_NDG] = {0}, rhoscale_gap[HC3D_NDG] = {0},
+         rhogap0[HC3D_NDG] = {0};
   double pitch = 0, sw = 0, rspiral1 = 0, rspiral2 = 0;
   int sn = 0, nspot = 1;
   double warpheight = 0, wexp = 0, warplength = 1;
@@ -99,6 +102,20 @@ struct Model {
   double tshock_k = 0, thspot_deg = 0, tave_k = 0, rmaxdmax = 0;
   hc3d_sources src{};
   bool has_sources() const { return idiskacc || ispot; }
+  // very small grains and PAHs (FSG(1..4) > 0): species 5-8 of the reference
+  // numbering (grid_mod.f90:13-20) hold the small-grain share of disk 1,
+  // disk 2, envelope and cavity; they re-emit from the emission spectra of
+  // draine_cdf.f90 (18 mean-intensity ratios x 1000 frequencies) instead of
+  // at a temperature.  isrfkap_int is the ISRF weighted by the small grains'
+  // absorption opacity (isrf_cdf.f90:191-214), the unit of int_mean's ratio.
+  double fsg[4] = {0, 0, 0, 0};
+  bool has_sg() const { return fsg[0] > 0.0 || fsg[1] > 0.0 || fsg[2] > 0.0 || fsg[3] > 0.0; }
+  int slot_species[4] = {1, 2, 3, 4};  // the species (1..8) each device slot holds
+  std::vector<double> sg_cdf, sg_logcdf;  // (nemit,ndraine) Fortran order
+  std::vector<double> sg_logfreq, sg_uratio;  // (ndraine), (nemit)
+  double isrfkap_int = 0.0;
+  int sg_slot = -1;  // the first device slot holding small grains; -1 = none
+  std::vector<double> isrf_pdf, isrf_fhz;  // the ISRF's pdf on its 200 frequencies in Hz
   // limb-darkening table (tabl_mod) for CLIMB=YES
   std::vector<double> limb_xmu, limb_prob;
   int image = 1;

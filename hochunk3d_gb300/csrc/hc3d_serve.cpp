@@ -149,12 +149,10 @@ int run_request(hc3d_server* s, hc3d_ctx* c, const Request& q, Result* res) {
     s->running--;
     s->cv_mem.notify_all();
   };
-  hc3d_dust_tables tv = m.tables_view();
-  hc3d_grid gv = m.grid_view();
   hc3d_run_params p = m.params_view();
   std::vector<double> td(m.tdust);
   int iter = 0;
-  if ((r = hc3d_reset(c)) || (r = hc3d_load_tables(c, &tv)) || (r = hc3d_load_grid(c, &gv))) {
+  if ((r = hc3d_reset(c)) || (r = hc3d_model_load(hm, c))) {
     ctx_error(c, r, res);
     release();
     hc3d_model_destroy(hm);

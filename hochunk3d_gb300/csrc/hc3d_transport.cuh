@@ -746,6 +746,24 @@ __device__ __forceinline__ unsigned long long fxf(float v, float scale) {
   return (unsigned long long)f2ll(v * scale);
 }
 
+// The small grains' absorption path of a step ds in cell c (models with
+// small-grain slots): ds kappa(nu)/kappa_V (1 - albedo(nu)) of slot sg_slot,
+// over the cell's outer radius like jmean.  int_mean turns it into the mean
+// intensity in units of the ISRF absorbed by the same grains (the tally of
+// the reference's tauint is restated; its source is absent).
+template <class R>
+__device__ __forceinline__ void tally_jsg(const DevModel& m, const DevTallies& t, const Pkt<R>& p, int64_t c, R ds,
+                                          R rout) {
+  if (!m.sg_on) return;
+  if constexpr (sizeof(R) == 4) {
+    const float w = pick4(p.kapd, m.sg_slot) * (1.f - pick4(p.albedo, m.sg_slot)) * m.sg_jfac;
+    atomicAdd(t.jsg + c, fxf(ds * w / rout, (float)t.path_scale));
+  } else {
+    const double w = pick4(p.kapd, m.sg_slot) * (1.0 - pick4(p.albedo, m.sg_slot)) * m.sg_jfacd;
+    atomicAdd(t.jsg + c, fx((double)ds * w / (double)rout, t.path_scale));
+  }
+}
+
 // A lower bound on the distance from a point inside cell (ir, it, ip) to
 // every wall of the cell: the spheres |r - R|, the cones r|sin(theta - theta_w)|
 // = |rho cos(theta_w) - z sin(theta_w)| (rho the cylindrical radius; the
@@ -803,6 +821,7 @@ static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevT
         if (rho.v[s] > 0.f)
           atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fxf(p.kapd[s] * (1.f - p.albedo[s]) * rho.v[s] * ds, ps));
       atomicAdd(t.jmean + c, fxf(ds / __ldg(m.rarrf + p.ir), ps));
+      tally_jsg<float>(m, t, p, c, ds, __ldg(m.rarrf + p.ir));
       path_add(S, ds);
       ray_pos(ray, S, p.x, p.y, p.z);
       tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, dval(p.x), dval(p.y), dval(p.z));
@@ -856,6 +875,7 @@ static __device__ __forceinline__ int tauint_mixed(const DevModel& m, const DevT
       if (rho.v[s] > 0.f)
         atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fxf(p.kapd[s] * (1.f - p.albedo[s]) * rho.v[s] * ds, ps));
     atomicAdd(t.jmean + c, fxf(ds / rout, ps));
+    tally_jsg<float>(m, t, p, c, ds, rout);
     if (stop) {
       path_add(S, ds);
       at();
@@ -929,6 +949,7 @@ __device__ __forceinline__ int tauint(const DevModel& m, const DevTallies& t, Pk
             atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
           }
         atomicAdd(t.jmean + c, fx((double)ds / rout, t.path_scale));
+        tally_jsg<R>(m, t, p, c, ds, (R)rout);
         tr.add(2, p.ir, p.it, p.ip, 0, (double)tau, p.x, p.y, p.z);
         return TI_INTERACT;
       }
@@ -939,6 +960,7 @@ __device__ __forceinline__ int tauint(const DevModel& m, const DevTallies& t, Pk
           atomicAdd(t.dtauabs + (int64_t)s * m.ncell + c, fx((double)v, t.path_scale));
         }
       atomicAdd(t.jmean + c, fx((double)dt / rout, t.path_scale));
+      tally_jsg<R>(m, t, p, c, dt, (R)rout);
       tsum += dtau;
       step_index(m.npg, iface, p.ir, p.it, p.ip);
       p.x += (double)dt * uxd;
@@ -1856,6 +1878,43 @@ __device__ __forceinline__ int locate_dev(const double* xx, int n, double x) {
   return jl;
 }
 
+// ---- rep_draine.f90:1-65: the re-emission frequency of a small grain ---------------
+// One uniform picks the bin of the cumulative spectrum of row im (nr
+// locate3: the bisection without locate's fix-up at the first row), and of
+// row im + 1, each interpolated linearly in log10 cdf against log10 nu; the
+// two log frequencies are mixed by jmf (past the last row, row im alone).
+// FP64 in both forms: one draw per small-grain absorption.
+__device__ __forceinline__ int locate3_dev(const double* xx, int n, double x) {
+  int jl = 0, ju = n + 1;
+  const bool asc = __ldg(xx + n - 1) > __ldg(xx);
+  while (ju - jl > 1) {
+    const int jm = (ju + jl) / 2;
+    if (asc == (x > __ldg(xx + jm - 1))) jl = jm; else ju = jm;
+  }
+  return jl;
+}
+
+__device__ __forceinline__ double draine_logfreq(const DevModel& m, int j, double xran, double lx) {
+  const int nd = m.sg_nd;
+  int i = locate3_dev(m.sg_cdf + (size_t)(j - 1) * nd, nd, xran);
+  if (i == nd) i = nd - 1;
+  if (i == 0) i = 1;
+  const double* lc = m.sg_logcdf + (size_t)(j - 1) * nd;
+  const double l0 = __ldg(lc + i - 1), l1 = __ldg(lc + i);
+  const double f0 = __ldg(m.sg_logfreq + i - 1), f1 = __ldg(m.sg_logfreq + i);
+  return (lx - l0) / (l1 - l0) * (f1 - f0) + f0;
+}
+
+template <class R>
+__device__ __forceinline__ double rep_draine(const DevModel& m, int im, double jmf, Rng& rng) {
+  const double xran = (double)ran<R>(rng);
+  const double lx = log10(xran);
+  const double lf1 = draine_logfreq(m, im, xran, lx);
+  double lf = lf1;
+  if (im + 1 <= m.sg_nemit) lf = lf1 + jmf * (draine_logfreq(m, im + 1, xran, lx) - lf1);
+  return pow(10.0, lf);
+}
+
 // ---- propagate.f90:206-319 escape binning ----------------------------------------
 template <class R>
 __device__ void bin_escape(const DevTallies& t, const TallyDims& d, const RunArgs& a, const Pkt<R>& p, double xpold,
@@ -2388,18 +2447,29 @@ __device__ __forceinline__ bool interact(const DevModel& m, const DustView<R>& d
     if (keep) make_rec<R>(rec, p, a, 1, idust2);
     stokes<R>(p, idust2, rng);
     tr.add(5, p.ir, p.it, p.ip, 0, 0.0, dval(p.x), dval(p.y), dval(p.z));
-  } else {  // absorbed + re-emitted (emit_common thermal branch, reemit)
-    atomicAdd(t.dbig + c, 1u);
-    p.i_orig = (idust2 == 0 || idust2 == 1) ? 2 : 3;
+  } else {  // absorbed + re-emitted (emit_common thermal branch, reemit; small grains: rep_draine, emit_sg)
+    const bool sg = (m.sg_mask >> idust2) & 1u;
+    atomicAdd((sg ? t.dsg : t.dbig) + c, 1u);
+    p.i_orig = ((m.disk_mask >> idust2) & 1u) ? 2 : 3;
     atomicAdd(t.nabs + (int64_t)idust2 * m.ncell + c, 1ull);
     p.sip = R(1); p.sqp = R(0); p.sup = R(0); p.svp = R(0);
+    if (sg) {
+      // emit_common.f90:31-53: the spectrum row of the cell's mean intensity
+      // (row 2, U = 1, in the first iteration), the frequency, then an
+      // isotropic direction (emit_sg.f90)
+      const int im = a.iter1 ? 2 : __ldg(m.imean + c);
+      const double imf = a.iter1 ? 0.0 : __ldg(m.imfract + c);
+      p.nub = (R)rep_draine<R>(m, im, imf, rng);
+    }
     p.cost = R(1) - R(2) * ran<R>(rng);
     p.sint = xsqrt(R(1) - p.cost * p.cost);
     p.phi = (R)kR2p * ran<R>(rng);
     p.cosp = xcos(p.phi);
     p.sinp = xsin(p.phi);
-    if constexpr (sizeof(R) == 4) p.nub = lucy_freq_mixed(m, p.lrow, c, idust2, rng);
-    else p.nub = lucydustfreq<R>(m, tave, idust2, rng);
+    if (!sg) {
+      if constexpr (sizeof(R) == 4) p.nub = lucy_freq_mixed(m, p.lrow, c, idust2, rng);
+      else p.nub = lucydustfreq<R>(m, tave, idust2, rng);
+    }
     f.iflag = 0;
     opacset<R>(m, dv, p, p.nub, a);
     keep = a.ipeel == 1 && !deep_peel<R>(m, p, c);

@@ -114,7 +114,14 @@ class Tallies(C.Structure):
         ("killed", i32p), ("dbig", i32p), ("counters", C.c_int64 * 16),
         ("stokes_scale", C.c_double), ("square_scale", C.c_double), ("path_scale", C.c_double),
         ("image_m_i", i64p), ("image_m_q", i64p), ("image_m_u", i64p), ("image_m_v", i64p),
+        ("dsg", i32p), ("jsg", i64p),
     ]
+
+
+class SgTables(C.Structure):
+    """hc3d_sg_tables: the small grains' emission spectra (draine_cdf.f90) and ISRF integral."""
+    _fields_ = [("nemit", C.c_int), ("ndraine", C.c_int), ("cdf", dp), ("logcdf", dp), ("logfreq", dp),
+                ("uratio", dp), ("isrfkap_int", C.c_double), ("sg_slot", C.c_int)]
 
 
 class LucyBuffers(C.Structure):
@@ -150,6 +157,7 @@ class ModelInfo(C.Structure):
         ("lacc", C.c_double), ("lacc2", C.c_double), ("accfrac", C.c_double), ("accfrac2", C.c_double),
         ("mdot_msun_yr", C.c_double), ("tshock_k", C.c_double), ("fspot", C.c_double),
         ("thspot_deg", C.c_double), ("tave_k", C.c_double),
+        ("slot_species", C.c_int32 * 4), ("has_sg", C.c_int), ("ndg", C.c_int),
     ]
 
 
@@ -194,7 +202,11 @@ SIGNATURES = {
     "hc3d_reset": (C.c_int, [C.c_void_p]),
     "hc3d_get_error": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "hc3d_version": (C.c_char_p, []),
+    "hc3d_set_species": (C.c_int, [C.c_void_p, i32p]),
     "hc3d_load_tables": (C.c_int, [C.c_void_p, P(DustTables)]),
+    "hc3d_load_sg_tables": (C.c_int, [C.c_void_p, P(SgTables)]),
+    "hc3d_get_imean": (C.c_int, [C.c_void_p, i32p, dp]),
+    "hc3d_set_imean": (C.c_int, [C.c_void_p, i32p, dp]),
     "hc3d_load_grid": (C.c_int, [C.c_void_p, P(Grid)]),
     "hc3d_zero_tallies": (C.c_int, [C.c_void_p]),
     "hc3d_set_tdust": (C.c_int, [C.c_void_p, dp]),
@@ -217,12 +229,15 @@ SIGNATURES = {
     "hc3d_model_destroy": (None, [C.c_void_p]),
     "hc3d_model_views": (C.c_int, [C.c_void_p, P(DustTables), P(Grid), P(RunParams), P(ModelInfo)]),
     "hc3d_model_set_tdust": (C.c_int, [C.c_void_p, dp]),
+    "hc3d_model_sg_tables": (C.c_int, [C.c_void_p, P(SgTables)]),
+    "hc3d_model_load": (C.c_int, [C.c_void_p, C.c_void_p]),
     "hc3d_model_densities_gpu": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_char_p, C.c_size_t]),
     "hc3d_model_tables_gpu": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double), C.c_char_p, C.c_size_t]),
     "hc3d_tts": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, P(DeviceOpts), P(TtsStats), C.c_char_p, C.c_size_t]),
     "hc3d_write_synthetic_dust": (C.c_int, [C.c_char_p]),
     "hc3d_write_wavelength_grid": (C.c_int, [C.c_char_p, C.c_double]),
     "hc3d_write_synthetic_isrf": (C.c_int, [C.c_char_p]),
+    "hc3d_write_synthetic_draine": (C.c_int, [C.c_char_p]),
     "hc3d_write_outputs": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies), dp, dp, C.c_char_p]),
     "hc3d_write_grid_unf": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, dp, i32p]),
     "hc3d_star_packets": (C.c_int64, [C.c_double, C.c_int64]),
@@ -240,8 +255,8 @@ SIGNATURES = {
 
 # entry points of libhc3d_host.so (the model set-up, no CUDA)
 HOST_SYMBOLS = ("hc3d_model_create", "hc3d_model_destroy", "hc3d_model_views", "hc3d_model_set_tdust",
-                "hc3d_star_packets", "hc3d_packet_split", "hc3d_write_synthetic_dust", "hc3d_write_wavelength_grid",
-                "hc3d_write_synthetic_isrf")
+                "hc3d_model_sg_tables", "hc3d_star_packets", "hc3d_packet_split", "hc3d_write_synthetic_dust",
+                "hc3d_write_wavelength_grid", "hc3d_write_synthetic_isrf", "hc3d_write_synthetic_draine")
 
 _LIB = None
 _HOST = None
@@ -331,6 +346,7 @@ class Model:
         if rc != 0:
             raise Hc3dError(rc, err.value.decode())
         self._h = h
+        self.par_path = os.fspath(par_path)
         t, g, p, info = DustTables(), Grid(), RunParams(), ModelInfo()
         L.hc3d_model_views(h, C.byref(t), C.byref(g), C.byref(p), C.byref(info))
         self.info = info
@@ -363,6 +379,22 @@ class Model:
         self.ntab = t.ntab
         self.limb_xmu = _arr(t.limb_xmu, t.ntab); self.limb_prob = _arr(t.limb_prob, t.ntab)
         # run parameters
+        # small grains: the species of the four device slots and the emission spectra
+        self.slot_species = np.array(info.slot_species[:], dtype=np.int32)
+        self.sg = None
+        if info.has_sg:
+            sg = SgTables()
+            rc = L.hc3d_model_sg_tables(h, C.byref(sg))
+            if rc != 0:
+                raise Hc3dError(rc, "hc3d_model_sg_tables")
+            ne, nd = sg.nemit, sg.ndraine
+            self.sg_cdf = _arr(sg.cdf, ne * nd).reshape((ne, nd), order="F")
+            self.sg_logcdf = _arr(sg.logcdf, ne * nd).reshape((ne, nd), order="F")
+            self.sg_logfreq = _arr(sg.logfreq, nd)
+            self.sg_uratio = _arr(sg.uratio, ne)
+            self.isrfkap_int = sg.isrfkap_int
+            self.sg_slot = sg.sg_slot
+            self.sg = True
         self.npeel = p.npeel
         self.thete = _arr(p.thete, p.npeel); self.phie = _arr(p.phie, p.npeel)
         self.aperture2 = _arr(p.aperture2, p.nap)
@@ -398,6 +430,25 @@ class Model:
             assert a.flags.f_contiguous
             setattr(g, n, a.ctypes.data_as(dp))
         return g
+
+    @property
+    def sg_tables(self) -> SgTables | None:
+        """hc3d_sg_tables view of the small grains' spectra, or None without small grains."""
+        if not self.sg:
+            return None
+        s = SgTables()
+        s.nemit, s.ndraine = self.sg_cdf.shape
+        for n, a in (("cdf", self.sg_cdf), ("logcdf", self.sg_logcdf)):
+            assert a.flags.f_contiguous
+            setattr(s, n, a.ctypes.data_as(dp))
+        s.logfreq, s.uratio = _ptr(self.sg_logfreq), _ptr(self.sg_uratio)
+        s.isrfkap_int, s.sg_slot = self.isrfkap_int, self.sg_slot
+        return s
+
+    @property
+    def sg_species(self) -> int:
+        """0-based species whose opacity weights the small grains' path tally (-1 without them)."""
+        return int(self.slot_species[self.sg_slot - 1]) - 1 if self.sg else -1
 
     def run_params(self, np_total: int | None = None, **over) -> RunParams:
         """The model's run parameters with fields of RunParams overridden.
@@ -505,10 +556,29 @@ class Context:
 
     def load(self, model: Model) -> "Context":
         t, g = model.tables, model.grid
+        sp = np.ascontiguousarray(model.slot_species, dtype=np.int32)
+        self._check(lib().hc3d_set_species(self._h, _ptr(sp, C.c_int32)))
         self._check(lib().hc3d_load_tables(self._h, C.byref(t)))
         self._check(lib().hc3d_load_grid(self._h, C.byref(g)))
+        if model.sg:
+            s = model.sg_tables
+            self._check(lib().hc3d_load_sg_tables(self._h, C.byref(s)))
         self.model = model
         return self
+
+    def get_imean(self) -> tuple[np.ndarray, np.ndarray]:
+        """(imean, imfract), (nrg,ntg,npg): int_mean's spectrum rows and fractions (hc3d_get_imean)."""
+        shape = self.model.shape3
+        im = np.zeros(shape, dtype=np.int32, order="F")
+        fr = np.zeros(shape, dtype=np.float64, order="F")
+        self._check(lib().hc3d_get_imean(self._h, _ptr(im, C.c_int32), _ptr(fr)))
+        return im, fr
+
+    def set_imean(self, imean: np.ndarray, imfract: np.ndarray) -> None:
+        """Set the cells' spectrum rows and fractions (hc3d_set_imean), (nrg,ntg,npg)."""
+        im = np.asfortranarray(imean, dtype=np.int32)
+        fr = np.asfortranarray(imfract, dtype=np.float64)
+        self._check(lib().hc3d_set_imean(self._h, _ptr(im, C.c_int32), _ptr(fr)))
 
     def reset(self) -> "Context":
         """Drop the loaded model, keeping the stream, packet pool and queue (hc3d_reset)."""
@@ -564,6 +634,8 @@ class Context:
             buf("jmean", (nrg, ntg, npg))
             buf("killed", (nrg, ntg, npg), np.int32, C.c_int32)
             buf("dbig", (nrg, ntg, npg), np.int32, C.c_int32)
+            buf("dsg", (nrg, ntg, npg), np.int32, C.c_int32)
+            buf("jsg", (nrg, ntg, npg))
         self._check(lib().hc3d_get_tallies(self._h, C.byref(params), C.byref(T)))
         res = {k: a.reshape(s, order="F") for k, (a, s) in out.items()}
         res["counters"] = np.array(T.counters[:], dtype=np.int64)

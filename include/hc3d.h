@@ -206,6 +206,10 @@ typedef struct hc3d_tallies {
   int64_t *image_m_i;              /* (npeel,nxhst,nxhst,nfreq,no) per-frequency image cube, x stokes_scale
                                       (runs with imcube) */
   int64_t *image_m_q, *image_m_u, *image_m_v; /* (npeel,nxhst,nxhst,nfreq), x stokes_scale */
+  int32_t *dsg;                    /* (nrg,ntg,npg) small-grain absorptions (propagate.f90:108-113) */
+  int64_t *jsg;                    /* (nrg,ntg,npg) small-grain absorption path, x path_scale: the sum of
+                                      ds kappa(nu)/kappa_V (1 - albedo(nu)) / rarr(ir+1) of the sg_slot
+                                      species over the cell's steps, the input of int_mean */
 } hc3d_tallies;
 
 /* counters[] of hc3d_tallies (newdisktherm.F90:122-141, propagate.f90:296-318) */
@@ -238,8 +242,45 @@ int hc3d_get_error(const hc3d_ctx *ctx, char *buf, size_t len);
 /* Library version string and build architecture, e.g. "hc3d 0.1 sm_103a". */
 const char *hc3d_version(void);
 
+/* The species (reference numbering 1..8, grid_mod.f90:13-20: 1-2 thermal
+ * disk grains, 3 envelope, 4 cavity, 5-8 their very small grains and PAHs)
+ * that the device's four species slots carry: species[0] = 1, species[1] =
+ * 2, species[2] < species[3] in 3..8.  Default {1, 2, 3, 4}.  Call before
+ * hc3d_load_tables and hc3d_load_grid, which read each slot's species from
+ * the (.., ndg) host arrays; a species outside the map must hold no density.
+ * No counterpart in the reference, which carries all eight species. */
+int hc3d_set_species(hc3d_ctx *ctx, const int32_t *species);
+
 /* dustinit/setemiss/atmosinit outputs (dust.f90:314-474, starbarb.f90:3-110) */
 int hc3d_load_tables(hc3d_ctx *ctx, const hc3d_dust_tables *tables);
+
+/* draine_mod (draine_mod.f90, draine_cdf.f90:1-79) and the ISRF integral of
+ * isrf_cdf.f90:191-214: the emission spectra of the very small grains and
+ * PAHs for nemit ratios U of the mean intensity to the ISRF. */
+typedef struct hc3d_sg_tables {
+  int nemit;              /* spectra (18) */
+  int ndraine;            /* frequencies per spectrum (1000) */
+  const double *cdf;      /* (nemit,ndraine) cdf_d: cumulative, normalised, increasing frequency */
+  const double *logcdf;   /* (nemit,ndraine) logcdf_d: log10 cdf_d, -10 at row 1 */
+  const double *logfreq;  /* (ndraine) logfreq_d: log10 frequency (1.2398/lambda[um]), 0 at row 1 */
+  const double *uratio;   /* (nemit) uratio_arr: the U of each spectrum, increasing */
+  double isrfkap_int;     /* ISRF x absorption opacity of the small grains of sg_slot, integrated over frequency */
+  int sg_slot;            /* 1..4: the slot whose opacity weights the jsg tally and isrfkap_int */
+} hc3d_sg_tables;
+/* Load the small-grain spectra into a context whose species map holds small
+ * grains, after hc3d_load_tables.  An absorption by a small-grain slot then
+ * re-emits as emit_common.f90:31-53 does: the frequency from the spectrum of
+ * the cell's U (rep_draine.f90), an unpolarised isotropic direction
+ * (emit_sg.f90); dsg counts it instead of dbig.  hc3d_lucy_update then also
+ * runs int_mean (int_mean.f90:19-94) on the jsg tally. */
+int hc3d_load_sg_tables(hc3d_ctx *ctx, const hc3d_sg_tables *tables);
+/* imean (nrg,ntg,npg): the spectrum row 1..nemit of each cell, and imfract
+ * (nrg,ntg,npg): the fraction of the way to the next row, as int_mean of the
+ * last hc3d_lucy_update left them (get), or as a host computed them (set).
+ * The first iteration (params->iter == 1) uses row 2 with fraction 0 in
+ * every cell (emit_common.f90:34-37); later ones need int_mean's result. */
+int hc3d_get_imean(hc3d_ctx *ctx, int32_t *imean, double *imfract);
+int hc3d_set_imean(hc3d_ctx *ctx, const int32_t *imean, const double *imfract);
 
 /* gridset/initarr outputs (gridset.f90:411-1098, initarr.f90:11-56) */
 int hc3d_load_grid(hc3d_ctx *ctx, const hc3d_grid *grid);

@@ -67,6 +67,10 @@ typedef struct hc3d_model_info {
   double fspot;           /* spot filling factor (1 without spots) */
   double thspot_deg;      /* spot radius, degrees */
   double tave_k;          /* mean stellar temperature with the shock, K; sets rminsub */
+  /* very small grains and PAHs (FSG(1..4) > 0) */
+  int32_t slot_species[4]; /* the species each device slot carries (hc3d_set_species) */
+  int has_sg;             /* 1: a device slot carries small grains; hc3d_model_sg_tables describes them */
+  int ndg;                /* species in the host arrays: 4, or 8 with small grains */
 } hc3d_model_info;
 
 /* Build a model from a .par file.  par_dir overrides PARDIR when non-NULL.
@@ -77,6 +81,15 @@ void hc3d_model_destroy(hc3d_model *m);
 /* Views of the model's arrays (owned by the model; valid until destroy). */
 int hc3d_model_views(hc3d_model *m, hc3d_dust_tables *tables, hc3d_grid *grid, hc3d_run_params *params,
                      hc3d_model_info *info);
+
+/* The small grains' emission spectra and ISRF integral of a model with FSG >
+ * 0 (HC3D_ERR_STATE otherwise), owned by the model. */
+int hc3d_model_sg_tables(hc3d_model *m, hc3d_sg_tables *sg);
+
+/* Load the model into a context: its species map, dust tables, grid and,
+ * with small grains, their spectra (hc3d_set_species, hc3d_load_tables,
+ * hc3d_load_grid, hc3d_load_sg_tables). */
+int hc3d_model_load(hc3d_model *m, hc3d_ctx *ctx);
 
 /* Replace the model's tdust (nrg,ntg,npg,ndg), e.g. after hc3d_lucy_update. */
 int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
@@ -227,6 +240,11 @@ int hc3d_write_wavelength_grid(const char *path, double tstar_k);
 /* Write a synthetic external radiation field in the ISRF_FILE format:
  * three diluted blackbodies (Mathis, Mezger & Panagia 1983 form). */
 int hc3d_write_synthetic_isrf(const char *path);
+/* Write 18 synthetic small-grain emission spectra emit_draine_<U>.dat into
+ * directory dir (draine_cdf.f90's files and format: 1000 rows of lambda [um]
+ * and j_nu, lambda increasing): a PAH band set and a warm continuum whose
+ * temperature rises with U. */
+int hc3d_write_synthetic_draine(const char *dir);
 
 #ifdef __cplusplus
 }

@@ -25,6 +25,13 @@
  *     crossing (gridset.f90:581-604).
  *   - tfinal: the dusttemp fixed point (dusttemp.f90:30-50) with the Lucy
  *     absorbed-path estimator dtauabs in place of the absorption count.
+ *   - the small grains' path tally jsg that int_mean reads: ds times the
+ *     absorption opacity kappa(nu)/kappa_V (1 - albedo) of one small-grain
+ *     species, over the cell's outer radius like the path length.
+ *
+ * The small-grain inputs (spectra, the species whose opacity weights jsg,
+ * the cells' spectrum rows) are module state set by orc_set_sg, read by the
+ * runs that follow: one model at a time.
  *
  * Random numbers: Philox4x32-10 streams keyed by (seed, iter, packet id)
  * replace the L'Ecuyer-Cote stream (random.f90:99-118), in the same order of
@@ -47,6 +54,16 @@
 /* ------------------------------------------------------------------------ */
 /* Inputs, flattened.                                                        */
 /* ------------------------------------------------------------------------ */
+/* very small grains and PAHs (orc_set_sg) */
+typedef struct orc_sg_state {
+  int on;                 /* spectra set */
+  hc3d_sg_tables sg;      /* cdf and logcdf (nemit,ndraine) Fortran order */
+  int jspecies;           /* 0-based species whose opacity weights jsg */
+  const int32_t *imean;   /* (nrg,ntg,npg) spectrum rows 1..nemit, NULL before int_mean */
+  const double *imfract;  /* (nrg,ntg,npg) */
+} orc_sg_state;
+static orc_sg_state g_sg;
+
 typedef struct orc_ctx {
   hc3d_dust_tables dt;
   hc3d_grid g;
@@ -54,6 +71,9 @@ typedef struct orc_ctx {
   int64_t ncell4; /* nrg*ntg*npg */
   int limb;       /* run parameter limb (0 or 1) */
   double inczeta[145]; /* zetainit partial sums of bbfreq (random.f90:79-97) */
+  const orc_sg_state *sg; /* NULL: no small grains */
+  int iter1;      /* the first Lucy iteration: small grains use spectrum row 2 */
+  double jfac;    /* 1 / (rstar_cm kappa_V) of the jsg species */
 } orc_ctx;
 
 /* Tallies: the fixed-point arrays of hc3d_tallies plus FP64 sums of the
@@ -338,6 +358,10 @@ static int orc_tauint(const orc_ctx *c, pkt *p, double tau, orc_tallies *t, orc_
         }
       }
       t->fx.jmean[cell] += fx_round(ds / rout, t->fx.path_scale);
+      if (c->sg && t->fx.jsg) {
+        const int J = c->sg->jspecies;
+        t->fx.jsg[cell] += fx_round(ds * (p->kapd[J] * (1.0 - p->albedo[J]) * c->jfac) / rout, t->fx.path_scale);
+      }
       t->fx.counters[HC3D_CNT_CROSS_PROP]++;
       trace_add(tr, 2, p->ir, p->it, p->ip, 0, tau, p->xp, p->yp, p->zp);
       return TI_INTERACT;
@@ -351,6 +375,10 @@ static int orc_tauint(const orc_ctx *c, pkt *p, double tau, orc_tallies *t, orc_
       }
     }
     t->fx.jmean[cell] += fx_round(dt / rout, t->fx.path_scale);
+    if (c->sg && t->fx.jsg) {
+      const int J = c->sg->jspecies;
+      t->fx.jsg[cell] += fx_round(dt * (p->kapd[J] * (1.0 - p->albedo[J]) * c->jfac) / rout, t->fx.path_scale);
+    }
     t->fx.counters[HC3D_CNT_CROSS_PROP]++;
     tsum += dtau;
     step_index(c, iface, &p->ir, &p->it, &p->ip);
@@ -937,6 +965,37 @@ static void orc_bin_escape(const orc_ctx *c, const hc3d_run_params *rp, const pk
   t->fx.counters[HC3D_CNT_ESCAPED]++;
 }
 
+/* ---- rep_draine.f90:1-65 and locate3.f90 ------------------------------------
+ * The re-emission frequency of a small grain: bin of the uniform xran in the
+ * cumulative spectrum of row jm (locate3: bisection over row jm of cdf_d, no
+ * fix-up at the first element; clamped to 1..ndraine-1), log10 cdf against
+ * log10 nu interpolation, and the same in row jm + 1 mixed by jmf. */
+static int orc_locate3(const double *xx, int n1, int n2, int n3, double x) {
+  int jl = 0, ju = n2 + 1;
+  const int asc = xx[(n3 - 1) + (size_t)n1 * (n2 - 1)] > xx[n3 - 1];
+  while (ju - jl > 1) {
+    const int jm = (ju + jl) / 2;
+    if (asc == (x > xx[(n3 - 1) + (size_t)n1 * (jm - 1)])) jl = jm; else ju = jm;
+  }
+  return jl;
+}
+
+static double orc_draine_logfreq(const hc3d_sg_tables *s, int jm, double xran) {
+  int ifreq = orc_locate3(s->cdf, s->nemit, s->ndraine, jm, xran);
+  if (ifreq == s->ndraine) ifreq = s->ndraine - 1;
+  if (ifreq == 0) ifreq = 1;
+  const double l0 = s->logcdf[(jm - 1) + (size_t)s->nemit * (ifreq - 1)];
+  const double l1 = s->logcdf[(jm - 1) + (size_t)s->nemit * ifreq];
+  return (log10(xran) - l0) / (l1 - l0) * (s->logfreq[ifreq] - s->logfreq[ifreq - 1]) + s->logfreq[ifreq - 1];
+}
+
+static double orc_rep_draine(const hc3d_sg_tables *s, int jm, double jmf, double xran) {
+  const double lf1 = orc_draine_logfreq(s, jm, xran);
+  double lf = lf1;
+  if (jm + 1 <= s->nemit) lf = lf1 + jmf * (orc_draine_logfreq(s, jm + 1, xran) - lf1);
+  return pow(10.0, lf);
+}
+
 static void orc_propagate(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, orc_rng *rng, orc_tallies *t,
                           orc_trace *tr) {
   double xpold = p->xp, ypold = p->yp, zpold = p->zp;
@@ -961,18 +1020,33 @@ static void orc_propagate(const orc_ctx *c, const hc3d_run_params *rp, pkt *p, o
       orc_stokes(p, idust2, rng);
       trace_add(tr, 5, p->ir, p->it, p->ip, 0, 0, p->xp, p->yp, p->zp);
     } else { /* absorbed + re-emitted */
-      t->fx.dbig[cell]++;
+      const int sg = idust2 >= 4; /* is_sg, grid_mod.f90:18 */
+      if (sg) { if (t->fx.dsg) t->fx.dsg[cell]++; }
+      else t->fx.dbig[cell]++;
       p->i_orig = (idust2 == 0 || idust2 == 1 || idust2 == 4 || idust2 == 5) ? 2 : 3;
       t->fx.nabs[cell + c->ncell4 * idust2] += 1;
-      /* emit_common.f90:54-79 thermal branch with ilucy=1, reemit.f90:17-34 */
-      const double tave = c->g.tdust[cell + c->ncell4 * idust2];
       p->sip = 1.0; p->sqp = 0.0; p->sup = 0.0; p->svp = 0.0;
-      p->cost = 1.0 - 2.0 * orc_ran(rng);
-      p->sint = sqrt(1.0 - p->cost * p->cost);
-      p->phi = ORC_R2P * orc_ran(rng);
-      p->cosp = cos(p->phi);
-      p->sinp = sin(p->phi);
-      p->nub = orc_lucydustfreq(c, tave, idust2, rng);
+      if (sg) {
+        /* emit_common.f90:31-53: the spectrum row of the cell (row 2 in the
+         * first iteration), rep_draine, then emit_sg's isotropic direction */
+        const int im = c->iter1 ? 2 : c->sg->imean[cell];
+        const double imf = c->iter1 ? 0.0 : c->sg->imfract[cell];
+        p->nub = orc_rep_draine(&c->sg->sg, im, imf, orc_ran(rng));
+        p->cost = 1.0 - 2.0 * orc_ran(rng);
+        p->sint = sqrt(1.0 - p->cost * p->cost);
+        p->phi = ORC_R2P * orc_ran(rng);
+        p->cosp = cos(p->phi);
+        p->sinp = sin(p->phi);
+      } else {
+        /* emit_common.f90:54-79 thermal branch with ilucy=1, reemit.f90:17-34 */
+        const double tave = c->g.tdust[cell + c->ncell4 * idust2];
+        p->cost = 1.0 - 2.0 * orc_ran(rng);
+        p->sint = sqrt(1.0 - p->cost * p->cost);
+        p->phi = ORC_R2P * orc_ran(rng);
+        p->cosp = cos(p->phi);
+        p->sinp = sin(p->phi);
+        p->nub = orc_lucydustfreq(c, tave, idust2, rng);
+      }
       iflag = 0;
       orc_opacset(c, p, p->nub, rp->rstar_cm);
       if (rp->ipeel == 1)
@@ -1227,6 +1301,9 @@ static void orc_ctx_init(orc_ctx *c, const hc3d_dust_tables *dt, const hc3d_grid
   c->dt = *dt;
   c->g = *g;
   c->limb = 0;
+  c->sg = g_sg.on ? &g_sg : NULL;
+  c->iter1 = 1;
+  c->jfac = 0.0;
   c->ndg = g->ndg;
   c->ncell4 = (int64_t)g->nrg * g->ntg * g->npg;
   /* zetainit (random.f90:79-97): inczeta(i) = sum 1/j^4 over j <= i, added from j = 145 down */
@@ -1289,12 +1366,20 @@ int orc_sample_bbfreq(double teff, uint64_t seed, int64_t n, double *out) {
   return 0;
 }
 
+/* the run parameters the context reads: limb, and for the small grains the
+ * iteration (row 2 in the first) and the jsg weight's kappa_V scale */
+static void orc_ctx_params(orc_ctx *c, const hc3d_run_params *rp) {
+  c->limb = rp->limb;
+  c->iter1 = rp->iter == 1;
+  if (c->sg) c->jfac = 1.0 / (rp->rstar_cm * c->dt.kappav[c->sg->jspecies]);
+}
+
 /* Run packets [pid_begin, pid_end) of params into t (single thread). */
 int orc_run_range(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run_params *rp, orc_tallies *t,
                   int64_t pid_begin, int64_t pid_end) {
   orc_ctx c;
   orc_ctx_init(&c, dt, g);
-  c.limb = rp->limb;
+  orc_ctx_params(&c, rp);
   for (int64_t pid = pid_begin; pid < pid_end; ++pid) {
     orc_rng rng;
     orc_rng_init(&rng, rp->seed, rp->iter, rp->packet_offset + pid);
@@ -1310,7 +1395,7 @@ int orc_trace_packet(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_
                      int *exhausted) {
   orc_ctx c;
   orc_ctx_init(&c, dt, g);
-  c.limb = rp->limb;
+  orc_ctx_params(&c, rp);
   orc_rng rng;
   orc_rng_init(&rng, rp->seed, rp->iter, rp->packet_offset + pid);
   if (uniforms) { rng.inj = uniforms; rng.ninj = nu; rng.pos = 0; }
@@ -1551,6 +1636,58 @@ void orc_tfinal(const hc3d_dust_tables *dt, const hc3d_grid *g, const double *na
           }
           tdust_new[k] = orc_dusttemp(dt, na[k], g->tdust[k], ltot, nphot, id, g->massarr[k]);
         }
+}
+
+/* ---- very small grains ------------------------------------------------------ */
+/* Set (sg != NULL) or clear the small-grain inputs of the runs that follow:
+ * the spectra, the 0-based species whose opacity weights the jsg tally, and
+ * the cells' spectrum rows and fractions (NULL before the first int_mean).
+ * The arrays are not copied. */
+void orc_set_sg(const hc3d_sg_tables *sg, int jspecies, const int32_t *imean, const double *imfract) {
+  memset(&g_sg, 0, sizeof g_sg);
+  if (!sg) return;
+  g_sg.sg = *sg;
+  g_sg.jspecies = jspecies;
+  g_sg.imean = imean;
+  g_sg.imfract = imfract;
+  g_sg.on = 1;
+}
+
+double orc_rep_draine_c(const hc3d_sg_tables *sg, int jm, double jmf, double xran) {
+  return orc_rep_draine(sg, jm, jmf, xran);
+}
+
+/* int_mean (int_mean.f90:19-94) on the jsg tally of nphot packets: the mean
+ * intensity jsg / path_scale x rarr(ir+1) x rstar_cm kappa_V / (4 pi) / vcell
+ * / nphot x ltot in units of isrfkap_int, its row in uratio (nr locate,
+ * clamped to 1..nemit) and the log10 fraction to the next row.  Cells at the
+ * walls' indices (ir = nrg, ...) get row 1, fraction 0. */
+void orc_int_mean(const hc3d_grid *g, const hc3d_sg_tables *sg, const int64_t *jsg, double path_scale,
+                  double rstar_cm, double kappav, double ltot, double nphot, int32_t *imean, double *imfract) {
+  const double jconst = 1.0 / (1.0 / (rstar_cm * kappav)) / (4.0 * ORC_PI);
+  for (int ip = 1; ip <= g->npg; ++ip)
+    for (int it = 1; it <= g->ntg; ++it)
+      for (int ir = 1; ir <= g->nrg; ++ir) {
+        const int64_t k = (int64_t)(ir - 1) + (int64_t)g->nrg * ((it - 1) + (int64_t)g->ntg * (ip - 1));
+        if (ir == g->nrg || it == g->ntg || ip == g->npg) { imean[k] = 1; imfract[k] = 0.0; continue; }
+        double jm = (double)jsg[k] / path_scale;
+        jm = jm * g->rarr[ir];
+        jm = jm * jconst;
+        jm = jm / g->vcell[k] / nphot * ltot;
+        const double jratio = jm / sg->isrfkap_int;
+        int im = orc_locate(sg->uratio, sg->nemit, jratio);
+        if (im > sg->nemit) im = sg->nemit;
+        if (im < 1) im = 1;
+        double f;
+        if (jratio == 0.0) f = 0.0;
+        else if (im == sg->nemit) f = 1.0;
+        else {
+          const double jr1 = log10(sg->uratio[im - 1]), jr2 = log10(sg->uratio[im]);
+          f = (log10(jratio) - jr1) / (jr2 - jr1);
+        }
+        imean[k] = im;
+        imfract[k] = f;
+      }
 }
 
 /* ---- multi-threaded driver (CPU baseline) --------------------------------- */

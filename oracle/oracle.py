@@ -15,7 +15,7 @@ from pathlib import Path
 import numpy as np
 
 from hochunk3d_gb300 import hc3d
-from hochunk3d_gb300.hc3d import NO, P, DustTables, Grid, RunParams, Tallies, TraceRec, TRACE_DTYPE
+from hochunk3d_gb300.hc3d import NO, P, DustTables, Grid, RunParams, SgTables, Tallies, TraceRec, TRACE_DTYPE
 
 ROOT = Path(__file__).resolve().parent
 LIB_PATH = ROOT / "_build" / "libhc3d_oracle.so"
@@ -68,6 +68,14 @@ def lib() -> C.CDLL:
         L.orc_stokes_c.argtypes = [C.c_double, C.c_double, dp, dp, C.c_int]
         L.orc_opacset_c.argtypes = [P(DustTables), P(Grid), C.c_double, dp]
         L.orc_select_dust_c.argtypes = [C.c_int, dp, dp, C.c_double]
+        i32 = P(C.c_int32)
+        L.orc_set_sg.argtypes = [P(SgTables), C.c_int, i32, dp]
+        L.orc_set_sg.restype = None
+        L.orc_rep_draine_c.argtypes = [P(SgTables), C.c_int, C.c_double, C.c_double]
+        L.orc_rep_draine_c.restype = C.c_double
+        L.orc_int_mean.argtypes = [P(Grid), P(SgTables), P(C.c_int64), C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_double, i32, dp]
+        L.orc_int_mean.restype = None
         _LIB = L
     return _LIB
 
@@ -100,6 +108,8 @@ class OracleTallies:
         self._add(T.fx, "jmean", self.g3)
         self._add(T.fx, "killed", self.g3, np.int32, C.c_int32)
         self._add(T.fx, "dbig", self.g3, np.int32, C.c_int32)
+        self._add(T.fx, "dsg", self.g3, np.int32, C.c_int32)
+        self._add(T.fx, "jsg", self.g3)
         for n, shape in (("si_d", self.sed_shape), ("ti_d", self.psed_shape), ("image_i_d", self.img_shape),
                          ("dtauabs_d", self.g4), ("image_m2_d", self.img_shape + (4,))):
             arr = np.zeros(shape, dtype=np.float64, order="F")
@@ -124,9 +134,60 @@ class OracleTallies:
         return r
 
 
-def run(model: hc3d.Model, params: RunParams, nthreads: int = 1, scales=None) -> dict:
-    """Run params.np packets of params on the CPU; int64 tallies summed over threads."""
+# the small-grain inputs of the oracle's runs (module state of hc3d_oracle.c),
+# kept alive here while they are set
+_SG_KEEP: list = []
+
+
+def set_sg(model: hc3d.Model, imean=None, imfract=None) -> None:
+    """Point the oracle's runs at the model's small grains (spectra, the
+    species weighting the jsg tally) and the cells' spectrum rows and
+    fractions (None before the first int_mean), or clear them."""
     L = lib()
+    _SG_KEEP.clear()
+    if not model.sg:
+        L.orc_set_sg(None, -1, None, None)
+        return
+    s = model.sg_tables
+    im = None if imean is None else np.asfortranarray(imean, dtype=np.int32)
+    fr = None if imfract is None else np.asfortranarray(imfract, dtype=np.float64)
+    _SG_KEEP.extend([s, im, fr, model])
+    L.orc_set_sg(C.byref(s), model.sg_species, None if im is None else im.ctypes.data_as(P(C.c_int32)),
+                 None if fr is None else fr.ctypes.data_as(P(C.c_double)))
+
+
+def _sg_for(model: hc3d.Model, params: RunParams, imean, imfract) -> None:
+    if model.sg and params.iter != 1 and imean is None:
+        raise ValueError("small grains after the first iteration need imean and imfract (int_mean)")
+    set_sg(model, imean, imfract)
+
+
+def int_mean(model: hc3d.Model, jsg: np.ndarray, path_scale: float, ltot: float, nphot: float,
+             rstar_cm: float) -> tuple[np.ndarray, np.ndarray]:
+    """int_mean (int_mean.f90:19-94) of the jsg tally: (imean, imfract), (nrg,ntg,npg)."""
+    g, s = model.grid, model.sg_tables
+    j = np.asfortranarray(jsg, dtype=np.int64)
+    im = np.zeros(model.shape3, dtype=np.int32, order="F")
+    fr = np.zeros(model.shape3, dtype=np.float64, order="F")
+    kv = float(model.kappav[model.sg_species])
+    lib().orc_int_mean(C.byref(g), C.byref(s), j.ctypes.data_as(P(C.c_int64)), float(path_scale), float(rstar_cm),
+                       kv, float(ltot), float(nphot), im.ctypes.data_as(P(C.c_int32)),
+                       fr.ctypes.data_as(P(C.c_double)))
+    return im, fr
+
+
+def rep_draine(model: hc3d.Model, jm: int, jmf: float, xran) -> np.ndarray:
+    """Small-grain re-emission frequencies of spectrum row jm mixed by jmf, for the uniforms xran."""
+    s = model.sg_tables
+    return np.array([lib().orc_rep_draine_c(C.byref(s), int(jm), float(jmf), float(x)) for x in np.atleast_1d(xran)])
+
+
+def run(model: hc3d.Model, params: RunParams, nthreads: int = 1, scales=None, imean=None, imfract=None) -> dict:
+    """Run params.np packets of params on the CPU; int64 tallies summed over threads.
+    A model with small grains past the first iteration takes int_mean's
+    imean and imfract."""
+    L = lib()
+    _sg_for(model, params, imean, imfract)
     t, g = model.tables, model.grid
     if nthreads <= 1:
         ot = OracleTallies(model, params, scales)
@@ -150,8 +211,10 @@ def run(model: hc3d.Model, params: RunParams, nthreads: int = 1, scales=None) ->
     return res
 
 
-def trace(model: hc3d.Model, params: RunParams, pid: int, uniforms=None, max_rec: int = 4096):
+def trace(model: hc3d.Model, params: RunParams, pid: int, uniforms=None, max_rec: int = 4096, imean=None,
+          imfract=None):
     L = lib()
+    _sg_for(model, params, imean, imfract)
     t, g = model.tables, model.grid
     ot = OracleTallies(model, params)
     recs = np.zeros(max_rec, dtype=TRACE_DTYPE)

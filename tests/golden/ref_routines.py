@@ -658,3 +658,118 @@ def densdiskg(rad, sint, cost, phi, P, region_out=None):
     if P["iradexp"] == 1:
         dens = dens * math.exp(-rcoord / P["radexp"])
     return dens
+
+
+# ---- very small grains and PAHs ---------------------------------------------------
+U_NAMES = ("0.50", "1.00", "2.00", "5.00", "10.0", "20.0", "30.0", "1e2", "3e2", "1e3", "3e3", "1e4", "3e4",
+           "1e5", "3e5", "1e6", "3e6", "1e7")
+
+
+def draine_cdf(directory, ndraine: int = 1000):
+    """draine_cdf.f90:1-79: (cdf, logcdf) (nemit, ndraine), logfreq (ndraine),
+    uratio (nemit) from the emit_draine_<U>.dat files of directory."""
+    nemit = len(U_NAMES)
+    pdf = np.zeros((nemit, ndraine))
+    freq = np.zeros(ndraine)
+    for j, name in enumerate(U_NAMES):
+        rows = np.loadtxt(f"{directory}/emit_draine_{name}.dat")[:ndraine]
+        for i in range(ndraine):
+            lam, p = rows[i]
+            pdf[j, ndraine - 1 - i] = p
+            freq[ndraine - 1 - i] = 1.2398 / lam
+    cdf = np.zeros((nemit, ndraine))
+    logcdf = np.zeros((nemit, ndraine))
+    logfreq = np.zeros(ndraine)
+    for j in range(nemit):
+        for i in range(1, ndraine):
+            cdf[j, i] = cdf[j, i - 1] + 0.5 * (pdf[j, i] + pdf[j, i - 1]) * (freq[i] - freq[i - 1])
+        total = cdf[j, ndraine - 1]
+        logcdf[j, 0] = -10.0
+        for i in range(1, ndraine):
+            cdf[j, i] = cdf[j, i] / total
+            logcdf[j, i] = math.log10(cdf[j, i])
+            logfreq[i] = math.log10(freq[i])
+    uratio = np.array([float(np.float32(v)) for v in (0.5, 1.0, 2.0, 5.0, 10.0, 20.0, 30.0, 1e2, 3e2, 1e3, 3e3, 1e4,
+                                                        3e4, 1e5, 3e5, 1e6, 3e6, 1e7)])
+    return cdf, logcdf, logfreq, uratio
+
+
+def locate(xx, x) -> int:
+    """nr.f:131-150 (1-based result, with the fix-up at the first element)."""
+    n = len(xx)
+    jl, ju = 0, n + 1
+    asc = xx[n - 1] > xx[0]
+    while ju - jl > 1:
+        jm = (ju + jl) // 2
+        if asc == (x > xx[jm - 1]):
+            jl = jm
+        else:
+            ju = jm
+    if jl == 0 and x == xx[0]:
+        jl = 1
+    return jl
+
+
+def locate3(row, x) -> int:
+    """locate3.f90:1-24 on one row of the table (no fix-up at the first element)."""
+    n = len(row)
+    jl, ju = 0, n + 1
+    asc = row[n - 1] > row[0]
+    while ju - jl > 1:
+        jm = (ju + jl) // 2
+        if asc == (x > row[jm - 1]):
+            jl = jm
+        else:
+            ju = jm
+    return jl
+
+
+def rep_draine(cdf, logcdf, logfreq, jmean: int, jmf: float, xran: float) -> float:
+    """rep_draine.f90:1-65 (jmean 1-based)."""
+    nemit, ndraine = cdf.shape
+
+    def logf(j):
+        ifreq = locate3(cdf[j - 1], xran)
+        if ifreq == ndraine:
+            ifreq = ndraine - 1
+        if ifreq == 0:
+            ifreq = 1
+        return (math.log10(xran) - logcdf[j - 1, ifreq - 1]) / (logcdf[j - 1, ifreq] - logcdf[j - 1, ifreq - 1]) * \
+            (logfreq[ifreq] - logfreq[ifreq - 1]) + logfreq[ifreq - 1]
+
+    lf1 = logf(jmean)
+    lf = lf1 + jmf * (logf(jmean + 1) - lf1) if jmean + 1 <= nemit else lf1
+    return 10.0 ** lf
+
+
+def int_mean_cell(jmean_cell: float, vcell: float, nphot: float, ltot: float, isrfkap_int: float, uratio):
+    """int_mean.f90:30,64-94 for one cell: (imean 1-based, imfract) of the
+    mean intensity jmean_cell (the reference's jmean before its normalisation)."""
+    nemit = len(uratio)
+    jm = jmean_cell / vcell / nphot * ltot
+    jratio = jm / isrfkap_int
+    im = locate(uratio, jratio)
+    if im > nemit:
+        im = nemit
+    if im < 1:
+        im = 1
+    if jratio == 0.0:
+        f = 0.0
+    elif im == nemit:
+        f = 1.0
+    else:
+        jr1, jr2 = math.log10(uratio[im - 1]), math.log10(uratio[im])
+        f = (math.log10(jratio) - jr1) / (jr2 - jr1)
+    return im, f
+
+
+def isrf_sg_integral(freq_hz, pdf, kappa_of, kappav: float) -> float:
+    """isrf_cdf.f90:191-209: the ISRF pdf weighted by the absorption opacity
+    kappa(nu) kappav (1 - albedo(nu)) of the small grains, trapezoid rule;
+    kappa_of(nu) returns (kappa, albedo) at nu in units of 1.2398/lambda[um]."""
+    s = 0.0
+    for i in range(1, len(freq_hz)):
+        testnu = 1.2398 / (2.9979e14 / freq_hz[i])
+        kap, alb = kappa_of(testnu)
+        s = s + 0.5 * (pdf[i] + pdf[i - 1]) * (freq_hz[i] - freq_hz[i - 1]) * kap * kappav * (1.0 - alb)
+    return s
