@@ -85,11 +85,16 @@ double since(const hc3d_server* s) { return std::chrono::duration<double>(clk::n
 // Device bytes a model run holds besides the slot's fixed pool and queue:
 // the grid and temperature arrays and the Lucy tallies the context loads
 // (hc3d_load_grid), the dust tables (hc3d_load_tables) and the SED, peeled
-// SED and image tallies of the peeled iteration.
+// SED and image tallies of the peeled iteration; with small grains their
+// tallies, spectrum rows and the spectra.
 int64_t footprint_bytes(const hc3d::Model& m, int npeel) {
   const int64_t ncell = m.ncells(), n4 = m.n4();
+  const int64_t sg = m.sg_slot >= 0 ? ncell * (4 /*dsg*/ + 8 /*jsg*/ + 4 /*imean*/ + 8 /*imfract*/ + 8 /*vcell*/) +
+                                          (int64_t)2 * hc3d::kNemit * hc3d::kNdraine * 8
+                                    : 0;
   const int64_t grid = ncell * (4 * 4 /*rho f32*/ + 4 * 8 /*rho f64*/ + 2 * 4 * 8 /*tdust, massarr*/ + 4 * 4 /*tdust f32*/ +
-                                1 /*peel mask*/ + 2 * 4 * 8 /*nabs, dtauabs*/ + 8 /*jmean*/ + 2 * 4 /*killed, dbig*/);
+                                1 /*peel mask*/ + 2 * 4 * 8 /*nabs, dtauabs*/ + 8 /*jmean*/ + 2 * 4 /*killed, dbig*/) +
+                       sg;
   const int64_t walls = (int64_t)(m.nrg + m.ntg + m.npg) * 64 + n4 * 8 /*vcell*/;
   const int64_t tables = (int64_t)m.nT * m.nnu * 4 * 12 + (int64_t)m.nlammax * 4 * 5 * 12 + (1 << 20);
   const int64_t sed = (int64_t)m.nfreq * m.nmu * m.nph * m.nap * 8 * 9 * 8;
