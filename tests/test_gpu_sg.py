@@ -6,9 +6,12 @@ through the C-ABI, on the tiny_sg model: the device slots carry species 1,
 * Traces fed identical uniforms: the FP64 kernel's (kind, ir, it, ip, iface)
   sequence equals the oracle's, in the first iteration (spectrum row 2) and
   in a later one with the oracle's int_mean result set on the device.
-* Counter-based runs: FP64 bins identical to the oracle's in >= 95 % of the
-  bins of the SEDs, the images, the absorption counts of both grain kinds
-  and the small grains' path tally.
+* Counter-based runs: FP64 counts (SEDs, absorptions of both grain kinds)
+  and the small grains' path tally identical to the oracle's in >= 95 % of
+  the bins; the peeled SED and image sums, which weigh every re-emission by
+  exp(-tau) at its frequency, to 1e-9 relative in every bin: a small
+  grain's frequency is 10**logfreq, and CUDA's pow and the C library's may
+  differ in the last bit, so the peel-off optical depths of those packets do.
 * hc3d_lucy_update's int_mean on the device equals the oracle's int_mean of
   the device's own path tally: the same spectrum row in every cell, the
   fraction to 1e-12.
@@ -81,11 +84,17 @@ def test_fp64_run_matches_oracle(model_factory, O):
     ctx.close()
     r = O.run(m, p, nthreads=THREADS, imean=im, imfract=fr)
     assert nf == 0 and r["errors"] == 0
-    keys = ("si", "sq", "su", "nums", "ti", "tq", "tu", "numt", "image_i", "nabs", "dbig", "dsg", "jsg")
-    frac = {k: K.same_fraction(t[k], r[k]) for k in keys}
+    keys = ("si", "sq", "su", "nums", "tq", "tu", "numt", "nabs", "dbig", "dsg", "jsg")
+    frac = {k: K.same_fraction(t[k], r[k]) for k in keys + ("ti", "image_i")}
     print("\ntiny_sg identical-bin fractions " + " ".join(f"{k}={v:.4f}" for k, v in frac.items()))
-    low = {k: v for k, v in frac.items() if v < 0.95}
+    low = {k: frac[k] for k in keys if frac[k] < 0.95}
     assert not low, low
+    for k in ("ti", "image_i"):
+        # fixed-point units (x stokes_scale): 1e-9 relative plus 64 units of rounding
+        a, b = t[k].astype(np.float64), r[k].astype(np.float64)
+        worst = np.max(np.abs(a - b) - 1e-9 * np.abs(b))
+        print(f"{k}: largest difference beyond 1e-9 relative: {worst:.3g} units")
+        assert worst <= 64.0, (k, worst)
     assert r["dsg"].sum() > 0 and abs(int(t["dsg"].sum()) - int(r["dsg"].sum())) <= 2 + 0.002 * r["dsg"].sum()
 
 
@@ -130,8 +139,13 @@ def test_mixed_run_chi2_vs_oracle(model_factory, O):
         for c in "iqu":
             c2, dof = rep[f"{tag}_chi2_{c}"], rep[f"{tag}_dof_{c}"]
             assert dof >= 20 and c2 <= 1.2, (tag, c, c2, dof)
-    # the small grains absorb and re-emit at the oracle's rate
-    assert abs(float(t["dsg"].sum()) - float(r["dsg"].sum())) <= 4.0 * np.sqrt(float(r["dsg"].sum()))
+    # the small grains take the oracle's share of the absorptions (the totals
+    # themselves scatter by the packets trapped in the disk midplane, each
+    # absorbed thousands of times)
+    share_t = float(t["dsg"].sum()) / float(t["dsg"].sum() + t["dbig"].sum())
+    share_r = float(r["dsg"].sum()) / float(r["dsg"].sum() + r["dbig"].sum())
+    print(f"small-grain share of absorptions: mixed {share_t:.5f} oracle {share_r:.5f}")
+    assert abs(share_t - share_r) <= 0.02 * share_r
 
 
 def test_lucy_graph_equals_step_loop(model_factory):
