@@ -19,7 +19,6 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/hc3d.h"
 #include "hc3d_lucy.cuh"
@@ -34,12 +33,6 @@ constexpr long long kMaxBlocks = HC3D_NOALLOC_MAX_ELEMENTS / (kThreads * kPerThr
 // bits of non-negative doubles); [kMaxBlocks]: blocks finished;
 // [kMaxBlocks + 1]: the maximum over all blocks.
 static __device__ __align__(256) unsigned long long g_lucy_scratch[kMaxBlocks + 2];
-
-// Device address of g_lucy_scratch per device ordinal, found once per device
-// and kept for the life of the process (a device reset would load the module
-// again elsewhere; the header tells callers not to use the call after one).
-std::mutex g_mu;
-void* g_addr[64] = {};
 
 struct Args {
   int nrg, ntg, npg, ndg;
@@ -135,16 +128,10 @@ extern "C" int hc3d_lucy_update_noalloc(const hc3d_lucy_buffers* b, double* max_
   }
   if (b->device < 0 || b->device >= 64) return HC3D_ERR_INVALID;
   if (cudaSetDevice(b->device) != cudaSuccess) return HC3D_ERR_CUDA;
-  void* addr;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[b->device]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_lucy_scratch) != cudaSuccess || !p) return HC3D_ERR_CUDA;
-      g_addr[b->device] = p;
-    }
-    addr = g_addr[b->device];
-  }
+  // the scratch array's address on this device, looked up on every call (it
+  // allocates nothing), so that a context the host recreated finds it anew
+  void* addr = nullptr;
+  if (cudaGetSymbolAddress(&addr, g_lucy_scratch) != cudaSuccess || !addr) return HC3D_ERR_CUDA;
   unsigned long long* scratch = static_cast<unsigned long long*>(addr);
   cudaStream_t st = static_cast<cudaStream_t>(b->stream);
   if (cudaMemsetAsync(scratch + kMaxBlocks, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess)

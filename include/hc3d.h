@@ -396,12 +396,11 @@ int hc3d_lucy_iterations(hc3d_ctx *ctx, const hc3d_run_params *params, int n_ite
  * completion counter.  Every GPU that loads the library holds that array until
  * the process exits.  Grids are limited to nrg*ntg*npg*ndg <=
  * HC3D_NOALLOC_MAX_ELEMENTS; a larger one returns HC3D_ERR_INVALID with a
- * message on stderr.  The first call on each device looks the array's device
- * address up (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  The address is kept for the life of the
- * process, so the call must not be used on a device after cudaDeviceReset()
- * (or any other end of the primary context it first ran in): the module is
- * then loaded again at another address.  All calls share the array, which keeps the
+ * message on stderr.  Every call looks the array's device address up
+ * (cudaGetSymbolAddress, which allocates nothing) with the device current,
+ * so a context the host recreated after cudaDeviceReset() is found anew; make
+ * the first call on a device before any stream capture (it loads the module
+ * there).  All calls share the array, which keeps the
  * last call's contents, so calls that overlap on the GPU (different streams
  * without ordering between them) race and must not be issued.  The call
  * returns after the update on `stream` is complete. */
