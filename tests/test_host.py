@@ -150,3 +150,10 @@ def test_new_entry_points_reject_bad_arguments(built):
     assert L.hc3d_model_footprint(None) == -1
     L.hc3d_result_free(None)
     L.hc3d_server_destroy(None)
+    # the small-grain entry points
+    assert L.hc3d_set_species(None, None) == -1
+    assert L.hc3d_load_sg_tables(None, None) == -1
+    assert L.hc3d_get_imean(None, None, None) == -1
+    assert L.hc3d_set_imean(None, None, None) == -1
+    assert L.hc3d_model_load(None, None) == -1
+    assert hc3d.host_lib().hc3d_model_sg_tables(None, None) == -1
