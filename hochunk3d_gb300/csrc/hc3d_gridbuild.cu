@@ -261,6 +261,47 @@ __global__ void k_density(DensParams P, Walls w, const double* diskscl, double* 
   colmass[(size_t)ncol + col] = menv;
 }
 
+// ---- the fractal factor (CFRACTAL=YES) --------------------------------------
+// the clump centres of every level, drawn in their one sequence by one thread
+__global__ void k_fractal_points(int nr, int nt, int np, int fractn, int fractlev, int64_t ifseed, double* buf) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) fractal_generate(nr, nt, np, fractn, fractlev, ifseed, buf);
+}
+
+// one block per clump centre: the cells of its box inside the clump set
+// their bit of the cell set; count receives the number of bits newly set
+__global__ void k_fractal_mark(const double* pts, int npts, int nr, int nt, int np, double rad, unsigned* bits,
+                               unsigned long long* count) {
+  const int c = blockIdx.x;
+  if (c >= npts) return;
+  const double r = pts[3 * c], t = pts[3 * c + 1], p = pts[3 * c + 2];
+  const FractalBox B = fractal_box(nr, nt, np, rad, r, t, p);
+  const int64_t nbr = B.r1 - B.r0 + 1, nbt = B.t1 - B.t0 + 1, nbp = B.p1 - B.p0 + 1;
+  const int64_t nbox = nbr > 0 && nbt > 0 && nbp > 0 ? nbr * nbt * nbp : 0;
+  for (int64_t q0 = 0; q0 < nbox; q0 += blockDim.x) {
+    const int64_t q = q0 + threadIdx.x;
+    bool fresh = false;
+    if (q < nbox) {
+      const int ir = B.r0 + (int)(q % nbr);
+      const int it = B.t0 + (int)((q / nbr) % nbt);
+      const int ipp = B.p0 + (int)(q / (nbr * nbt));
+      if (fractal_inside(B, ir, it, ipp, r, t, p)) {
+        const int ip = ((ipp % np) + np) % np;
+        const int64_t k = ir + (int64_t)nr * (it + (int64_t)nt * ip);
+        const unsigned bit = 1u << (k & 31);
+        fresh = (atomicOr(bits + (k >> 5), bit) & bit) == 0u;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, fresh);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
+  }
+}
+
+// densvar: a in the marked cells, b elsewhere
+__global__ void k_fractal_fill(const unsigned* bits, int64_t nc, double a, double b, double* densvar) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nc; k += (int64_t)gridDim.x * blockDim.x)
+    densvar[k] = ((bits[k >> 5] >> (k & 31)) & 1u) ? a : b;
+}
+
 struct DevBufs {
   std::vector<void*> p;
   ~DevBufs() {
@@ -323,8 +364,21 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   DevBufs B;
   double *d_r = B.alloc<double>(nrg), *d_ra = B.alloc<double>(nrg), *d_t = B.alloc<double>(ntg),
          *d_ta = B.alloc<double>(ntg), *d_p = B.alloc<double>(npg);
-  const size_t nvar = m.ifractal ? m.densvar.size() : 1;
+  const int nr1 = nrg - 1, nt1 = ntg - 1, np1 = npg - 1;
+  const int64_t nc = (int64_t)nr1 * nt1 * np1;
+  const size_t nvar = m.ifractal ? (size_t)nc : 1;
   double* d_var = B.alloc<double>(nvar);
+  // the fractal factor's clump centres (all levels) and cell set
+  const int fr_total = m.ifractal ? fractal_total(m.fractn, m.fractlev) : 1;
+  int fr_last = m.fractn;
+  for (int lev = 2; lev <= m.fractlev; ++lev) fr_last *= m.fractn / 8 + 1;
+  double* d_pts = B.alloc<double>(3 * (size_t)fr_total);
+  unsigned* d_bits = B.alloc<unsigned>(m.ifractal ? (size_t)(nc + 31) / 32 : 1);
+  unsigned long long* d_cnt = B.alloc<unsigned long long>(1);
+  if (!d_pts || !d_bits || !d_cnt) {
+    *err = "device allocation failed";
+    return HC3D_ERR_NOMEM;
+  }
   // d_s: the column sums [0, 8), then diskscl [8, 16)
   double *d_dens = B.alloc<double>((size_t)n4 * ndg), *d_mass = B.alloc<double>((size_t)n4 * ndg),
          *d_vol = B.alloc<double>((size_t)n4), *d_col = B.alloc<double>((size_t)4 * ncol), *d_s = B.alloc<double>(16);
@@ -336,7 +390,7 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
     return cudaMemcpy(d, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
   };
   if (!up(d_r, m.rarr, nrg) || !up(d_ra, m.ravearr, nrg - 1) || !up(d_t, m.thetarr, ntg) ||
-      !up(d_ta, m.thetavearr, ntg - 1) || !up(d_p, m.phiarr, npg) || (m.ifractal && !up(d_var, m.densvar, nvar))) {
+      !up(d_ta, m.thetavearr, ntg - 1) || !up(d_p, m.phiarr, npg)) {
     *err = "upload failed";
     return HC3D_ERR_CUDA;
   }
@@ -350,6 +404,37 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   cudaEventCreate(&e1);
   const int threads = 128, blocks = (ncol + threads - 1) / threads;
   cudaEventRecord(e0);
+  // The fractal factor: the clump centres, then the clump radius by
+  // bisection to the volume fraction of the factors (each step marks the
+  // cells inside the clumps and counts them), then the factor of each cell.
+  // The same steps as the host build, so the same cells are marked.
+  if (m.ifractal) {
+    k_fractal_points<<<1, 32>>>(nr1, nt1, np1, m.fractn, m.fractlev, m.ifseed, d_pts);
+    const double* pts = d_pts + 3 * (size_t)(fr_total - fr_last);
+    bool ok = true;
+    auto mark = [&](double rad) -> int64_t {
+      unsigned long long n = 0;
+      ok = ok && cudaMemset(d_bits, 0, sizeof(unsigned) * (size_t)((nc + 31) / 32)) == cudaSuccess &&
+           cudaMemset(d_cnt, 0, sizeof(unsigned long long)) == cudaSuccess;
+      k_fractal_mark<<<fr_last, 256>>>(pts, fr_last, nr1, nt1, np1, rad, d_bits, d_cnt);
+      ok = ok && cudaMemcpy(&n, d_cnt, sizeof n, cudaMemcpyDeviceToHost) == cudaSuccess;
+      return (int64_t)n;
+    };
+    const double fv_target = fractal_target(m);
+    double lo = 0.0, hi = 0.5;
+    for (int k = 0; k < 30; ++k) {
+      const double mid = 0.5 * (lo + hi);
+      if ((double)mark(mid) / (double)nc < fv_target) lo = mid; else hi = mid;
+    }
+    const double fv = std::max((double)mark(hi) / (double)nc, 1.0 / (double)nc);
+    double fa, fb;
+    fractal_factors(m, fv, &fa, &fb);
+    k_fractal_fill<<<(int)std::min<int64_t>((nc + 255) / 256, 4096), 256>>>(d_bits, nc, fa, fb, d_var);
+    if (!ok || cudaGetLastError() != cudaSuccess) {
+      *err = "fractal factor kernels failed";
+      return HC3D_ERR_CUDA;
+    }
+  }
   // disk mass normalisation: diskscl = massd * fmass / mass on the grid
   double diskscl[HC3D_NDG] = {1, 1, 1, 1, 1, 1, 1, 1};
   if (m.massd > 0.0) {
@@ -381,6 +466,13 @@ int densities_gpu(Model& m, int device, double* ms, std::string* err) {
   cudaEventDestroy(e1);
   if (ms) *ms = t;
   double sums[2];
+  if (m.ifractal) {
+    m.densvar.resize((size_t)nc);
+    if (cudaMemcpy(m.densvar.data(), d_var, sizeof(double) * nc, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      *err = "download failed";
+      return HC3D_ERR_CUDA;
+    }
+  }
   m.densarr.resize((size_t)n4 * ndg);
   m.massarr.resize((size_t)n4 * ndg);
   m.vcell.resize((size_t)n4);

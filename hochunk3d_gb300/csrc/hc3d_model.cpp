@@ -506,60 +506,59 @@ double densenv(const Model& m, double rad, double thetin, double costin, double 
 // gridset.f90:842-851) and a share densratio of the mass in clumps; the clump
 // radius is set by bisection to the volume fraction these imply.
 // ---------------------------------------------------------------------------
-static uint64_t splitmix(uint64_t* s) {
-  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
+
+// the final level's clump centres, x = r, t, p in cell-index space, three per centre
+std::vector<double> fractal_points(const Model& m) {
+  const int total = fractal_total(m.fractn, m.fractlev);
+  std::vector<double> buf(3 * (size_t)total);
+  const int n = fractal_generate(m.nrg - 1, m.ntg - 1, m.npg - 1, m.fractn, m.fractlev, m.ifseed, buf.data());
+  int last = m.fractn;
+  for (int lev = 2; lev <= m.fractlev; ++lev) last *= m.fractn / 8 + 1;
+  return std::vector<double>(buf.begin() + 3 * (size_t)(n - last), buf.begin() + 3 * (size_t)n);
 }
-static double u01(uint64_t* s) { return ((double)(splitmix(s) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+
+// the bisection's target volume fraction, and the factors a (clumps), b (the rest) of a volume fraction fv
+double fractal_target(const Model& m) {
+  const double K = m.fractcontrast, fm = m.densratio;
+  return fm / (K * (1.0 - fm) + fm);
+}
+void fractal_factors(const Model& m, double fv, double* a, double* b) {
+  const double K = m.fractcontrast;
+  *b = 1.0 / (K * fv + 1.0 - fv);
+  *a = K * *b;
+}
 
 static void fractal_field(Model* m) {
   const int nr = m->nrg - 1, nt = m->ntg - 1, np = m->npg - 1;
   const int64_t nc = (int64_t)nr * nt * np;
-  uint64_t s = (uint64_t)m->ifseed * 0x2545F4914F6CDD1Dull + 12345;
-  struct C { double r, t, p; };
-  std::vector<C> cur;
-  for (int k = 0; k < m->fractn; ++k) cur.push_back({u01(&s) * nr, u01(&s) * nt, u01(&s) * np});
-  double spread = 0.25;
-  for (int lev = 2; lev <= m->fractlev; ++lev) {
-    std::vector<C> nxt;
-    for (const C& c : cur)
-      for (int k = 0; k < m->fractn / 8 + 1; ++k)
-        nxt.push_back({c.r + (u01(&s) - 0.5) * 2 * spread * nr, c.t + (u01(&s) - 0.5) * 2 * spread * nt,
-                       c.p + (u01(&s) - 0.5) * 2 * spread * np});
-    cur.swap(nxt);
-    spread *= 0.35;
-  }
+  const std::vector<double> cur = fractal_points(*m);
   std::vector<uint8_t> in(nc, 0);
   auto mark = [&](double rad) {
     std::fill(in.begin(), in.end(), 0);
-    const double cr = std::max(0.5, rad * nr), ct = std::max(0.5, rad * nt), cp = std::max(0.5, rad * np);
     int64_t count = 0;
-    for (const C& c : cur) {
-      int r0 = (int)std::floor(c.r - cr), r1 = (int)std::ceil(c.r + cr);
-      int t0 = (int)std::floor(c.t - ct), t1 = (int)std::ceil(c.t + ct);
-      int p0 = (int)std::floor(c.p - cp), p1 = (int)std::ceil(c.p + cp);
-      for (int ir = std::max(0, r0); ir <= std::min(nr - 1, r1); ++ir)
-        for (int it = std::max(0, t0); it <= std::min(nt - 1, t1); ++it)
-          for (int ipp = p0; ipp <= p1; ++ipp) {
-            int ip = ((ipp % np) + np) % np;
-            double dr = (ir + 0.5 - c.r) / cr, dt = (it + 0.5 - c.t) / ct, dp = (ipp + 0.5 - c.p) / cp;
-            int64_t k = ir + (int64_t)nr * (it + (int64_t)nt * ip);
-            if (dr * dr + dt * dt + dp * dp <= 1.0 && !in[k]) { in[k] = 1; ++count; }
+    for (size_t c = 0; c < cur.size(); c += 3) {
+      const FractalBox B = fractal_box(nr, nt, np, rad, cur[c], cur[c + 1], cur[c + 2]);
+      for (int ir = B.r0; ir <= B.r1; ++ir)
+        for (int it = B.t0; it <= B.t1; ++it)
+          for (int ipp = B.p0; ipp <= B.p1; ++ipp) {
+            const int ip = ((ipp % np) + np) % np;
+            if (fractal_inside(B, ir, it, ipp, cur[c], cur[c + 1], cur[c + 2])) {
+              const int64_t k = ir + (int64_t)nr * (it + (int64_t)nt * ip);
+              if (!in[k]) { in[k] = 1; ++count; }
+            }
           }
     }
-    return (double)count / (double)nc;
+    return count;
   };
-  const double K = m->fractcontrast, fm = m->densratio;
-  const double fv_target = fm / (K * (1.0 - fm) + fm);
+  const double fv_target = fractal_target(*m);
   double lo = 0.0, hi = 0.5;
   for (int k = 0; k < 30; ++k) {
     double mid = 0.5 * (lo + hi);
-    if (mark(mid) < fv_target) lo = mid; else hi = mid;
+    if ((double)mark(mid) / (double)nc < fv_target) lo = mid; else hi = mid;
   }
-  const double fv = std::max(mark(hi), 1.0 / (double)nc);
-  const double b = 1.0 / (K * fv + 1.0 - fv), a = K * b;
+  const double fv = std::max((double)mark(hi) / (double)nc, 1.0 / (double)nc);
+  double a, b;
+  fractal_factors(*m, fv, &a, &b);
   m->densvar.assign(nc, 1.0);
   for (int64_t k = 0; k < nc; ++k) m->densvar[k] = in[k] ? a : b;
 }

@@ -1,6 +1,7 @@
 // hc3d_model.h -- host model: the data newtts.F90 builds before calling disk().
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -151,6 +152,112 @@ struct Model {
   int64_t ncells() const { return (int64_t)(nrg - 1) * (ntg - 1) * (npg - 1); }
   int64_t n4() const { return (int64_t)nrg * ntg * npg; }
 };
+
+// The project fractal generator (CFRACTAL=YES): clump centres, the cell box
+// of one clump, its inside test, the bisection's target volume fraction and
+// the density factors (shared by the host build and hc3d_gridbuild.cu).
+struct FractalBox {
+  double cr, ct, cp;       // clump radius in cells along r, theta, phi
+  int r0, r1, t0, t1, p0, p1;  // cell range (r, theta clamped; phi wraps)
+};
+std::vector<double> fractal_points(const Model& m);
+double fractal_target(const Model& m);
+void fractal_factors(const Model& m, double fv, double* a, double* b);
+#ifdef __CUDACC__
+#define HC3D_HD __host__ __device__
+#else
+#define HC3D_HD
+#endif
+// double arithmetic rounded operation by operation on host and device (the
+// device would otherwise contract a * b + c into one rounding)
+HC3D_HD inline double fr_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+HC3D_HD inline double fr_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+// splitmix64 and a uniform in (0, 1) from its top 53 bits
+HC3D_HD inline uint64_t fractal_splitmix(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+HC3D_HD inline double fractal_u01(uint64_t* s) {
+  return fr_mul((double)(fractal_splitmix(s) >> 11) + 0.5, 1.0 / 9007199254740992.0);
+}
+// centres of every level, level by level: fractn at level 1, fractn/8+1
+// children per centre at each next level, spread 0.25 of the index ranges
+// shrinking by 0.35 per level; returns the number of centres written to
+// buf (3 doubles each); the last level's are the final
+// fractn * (fractn/8+1)^(fractlev-1)
+HC3D_HD inline int fractal_generate(int nr, int nt, int np, int fractn, int fractlev, int64_t ifseed, double* buf) {
+  uint64_t s = (uint64_t)ifseed * 0x2545F4914F6CDD1Dull + 12345;
+  int n = 0;
+  for (int k = 0; k < fractn; ++k, ++n) {
+    buf[3 * n] = fr_mul(fractal_u01(&s), nr);
+    buf[3 * n + 1] = fr_mul(fractal_u01(&s), nt);
+    buf[3 * n + 2] = fr_mul(fractal_u01(&s), np);
+  }
+  int beg = 0, cnt = fractn;
+  double spread = 0.25;
+  for (int lev = 2; lev <= fractlev; ++lev) {
+    const int nb = n;
+    for (int c = beg; c < beg + cnt; ++c)
+      for (int k = 0; k < fractn / 8 + 1; ++k, ++n) {
+        const double ds = fr_mul(2.0, spread);
+        buf[3 * n] = fr_add(buf[3 * c], fr_mul(fr_mul(fr_add(fractal_u01(&s), -0.5), ds), nr));
+        buf[3 * n + 1] = fr_add(buf[3 * c + 1], fr_mul(fr_mul(fr_add(fractal_u01(&s), -0.5), ds), nt));
+        buf[3 * n + 2] = fr_add(buf[3 * c + 2], fr_mul(fr_mul(fr_add(fractal_u01(&s), -0.5), ds), np));
+      }
+    beg = nb;
+    cnt = n - nb;
+    spread *= 0.35;
+  }
+  return n;
+}
+// centres of all levels of fractal_generate: fractn (1 + m + m^2 + ...), m = fractn/8+1
+HC3D_HD inline int fractal_total(int fractn, int fractlev) {
+  int n = fractn, lvl = fractn;
+  for (int lev = 2; lev <= fractlev; ++lev) { lvl *= fractn / 8 + 1; n += lvl; }
+  return n;
+}
+// The cells of clump radius rad (a fraction of each index range) around
+// centre (r, t, p): the box the radius spans (at least half a cell).
+HC3D_HD inline FractalBox fractal_box(int nr, int nt, int np, double rad, double r, double t, double p) {
+  FractalBox b;
+  b.cr = fmax(0.5, fr_mul(rad, nr)); b.ct = fmax(0.5, fr_mul(rad, nt)); b.cp = fmax(0.5, fr_mul(rad, np));
+  const int r0 = (int)floor(r - b.cr), r1 = (int)ceil(r + b.cr), t0 = (int)floor(t - b.ct), t1 = (int)ceil(t + b.ct);
+  b.r0 = r0 > 0 ? r0 : 0; b.r1 = r1 < nr - 1 ? r1 : nr - 1;
+  b.t0 = t0 > 0 ? t0 : 0; b.t1 = t1 < nt - 1 ? t1 : nt - 1;
+  b.p0 = (int)floor(p - b.cp); b.p1 = (int)ceil(p + b.cp);
+  return b;
+}
+
+// the inside test of cell (ir, it, ipp) for the clump of box B and centre
+// (r, t, p): dr^2 + dt^2 + dp^2 <= 1 on the cell centre, each product and
+// sum rounded on its own
+HC3D_HD inline bool fractal_inside(const FractalBox& B, int ir, int it, int ipp, double r, double t, double p) {
+#ifdef __CUDA_ARCH__
+  const double dr = __ddiv_rn(__dsub_rn(__dadd_rn((double)ir, 0.5), r), B.cr);
+  const double dt = __ddiv_rn(__dsub_rn(__dadd_rn((double)it, 0.5), t), B.ct);
+  const double dp = __ddiv_rn(__dsub_rn(__dadd_rn((double)ipp, 0.5), p), B.cp);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dr, dr), __dmul_rn(dt, dt)), __dmul_rn(dp, dp)) <= 1.0;
+#else
+  const double dr = ((double)ir + 0.5 - r) / B.cr, dt = ((double)it + 0.5 - t) / B.ct,
+               dp = ((double)ipp + 0.5 - p) / B.cp;
+  const double x = dr * dr, y = dt * dt, z = dp * dp;
+  return (x + y) + z <= 1.0;
+#endif
+}
 
 // setup.f90 + reapar.f90 + dustinit + atmosinit + setup_wave + gridset
 bool build_model(Model* m, const std::string& par_path, const std::string* par_dir, std::string* err);

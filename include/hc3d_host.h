@@ -95,7 +95,8 @@ int hc3d_model_load(hc3d_model *m, hc3d_ctx *ctx);
 int hc3d_model_set_tdust(hc3d_model *m, const double *tdust);
 
 /* The densities of gridset (gridset.f90:954-1098: disk mass normalisation,
- * densdisk, densenv, the fractal factor, cell volumes and (rho V)^(1/4)) on
+ * densdisk, densenv, the fractal factor -- its clump centres and clump
+ * radius too --, cell volumes and (rho V)^(1/4)) on
  * CUDA device `device`, replacing the host-built densarr, massarr, vcell and
  * the grid masses of the model.  *ms receives the device time of the
  * kernels.  Every disk structure option (CGAPD, CSPIRAL, CDISKWARP, CRIMPUFF,
