@@ -1370,10 +1370,9 @@ static bool gridset(Model* m, std::string* err) {
     m->aarr[ip] = std::sin(m->phiarr[ip]);
     m->barr[ip] = -std::cos(m->phiarr[ip]);
   }
-  if (m->ifractal) fractal_field(m);
-
-  // ---- densities (gridset.f90:954-1098) ----
+  // ---- densities (gridset.f90:954-1098), the fractal factor first ----
   const auto t_dens = std::chrono::steady_clock::now();
+  if (m->ifractal) fractal_field(m);
   // species: disk 1, disk 2, envelope, cavity, and with FSG > 0 their
   // small-grain shares 5-8 (grid_mod.f90:13-20)
   m->ndg = m->has_sg() ? 8 : 4;

@@ -69,7 +69,7 @@ struct Model {
   double numin = 0, numax = 0;
   double ltot = 0;
   double massdisk = 0, massenv = 0;
-  double density_host_ms = 0;  // wall time of the host density build
+  double density_host_ms = 0;  // wall time of the host density build, the fractal factor included
   double tables_host_ms = 0;   // wall time of the host setemiss tables
   // external illumination (COUTILLUM, ISRF_SCL, ISRF_AV; isrf_mod)
   int iout = 0;
