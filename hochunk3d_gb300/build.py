@@ -25,7 +25,9 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhc3d.so"
 HOST_LIB = PKG / "libhc3d_host.so"
-HOST_UNITS = ["hc3d_model.cpp"]
+# host units and their extra flags; the fractal factor rounds every product
+# and sum on its own, as the device build of it does
+HOST_UNITS = [("hc3d_model.cpp", []), ("hc3d_fractal.cpp", ["-ffp-contract=off"])]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "libhc3d_oracle.so"
 
@@ -77,13 +79,15 @@ def _run(cmd: list[str]) -> None:
 def build_host_library(verbose: bool = False, force: bool = False) -> Path:
     """Compile the host-only model set-up into libhc3d_host.so (g++, no CUDA)."""
     BUILD.mkdir(exist_ok=True)
-    srcs = [CSRC / u for u in HOST_UNITS]
+    srcs = [CSRC / u for u, _ in HOST_UNITS]
     if force or not HOST_LIB.exists() or any(_stale(HOST_LIB, src) for src in srcs):
+        objs = []
+        for u, extra in HOST_UNITS:
+            obj = BUILD / (Path(u).stem + ".host.o")
+            _run(["g++", "-O2", "-std=c++17", *extra, "-fPIC", "-c", str(CSRC / u), "-o", str(obj)])
+            objs.append(obj)
         tmp = HOST_LIB.with_suffix(".so.tmp")
-        # no contracted multiply-adds: the same results on x86 and Arm hosts, and
-        # the fractal factor's cells equal to the device build's
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-Wl,-soname,libhc3d_host.so", "-o", str(tmp),
-              *map(str, srcs), "-lpthread"])
+        _run(["g++", "-shared", "-Wl,-soname,libhc3d_host.so", "-o", str(tmp), *map(str, objs), "-lpthread"])
         os.replace(tmp, HOST_LIB)
     if verbose:
         print(f"built {HOST_LIB}")

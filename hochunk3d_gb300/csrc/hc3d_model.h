@@ -161,6 +161,7 @@ struct FractalBox {
   int r0, r1, t0, t1, p0, p1;  // cell range (r, theta clamped; phi wraps)
 };
 std::vector<double> fractal_points(const Model& m);
+void fractal_field(Model* m);  // densvar of the host build
 double fractal_target(const Model& m);
 void fractal_factors(const Model& m, double fv, double* a, double* b);
 #ifdef __CUDACC__
