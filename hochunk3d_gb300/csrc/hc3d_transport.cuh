@@ -1609,44 +1609,38 @@ struct PeelWalk {
     tf += dtau;
     pc.cross++;
     if (tf > (float)kTauMax) return ENDED;
-    // Step the cell index, then one density load and one root update for
-    // all kinds of wall: the lanes of a warp that cross different walls share
-    // the load and, for the two polar walls, the one cone solution.
-    int kind;  // 0 sphere, 1 lower polar wall, 2 upper polar wall, 3 azimuthal wall
     if (tn == tr) {
       ir += tr < 0.f ? -1 : 1;
       if (ir == m.nrg) return OUT;
       if (ir == 0) return ENDED;
-      kind = 0;
+      fetch_rho(m);
+      next_sphere(m);
     } else if (tn == th) {
       if (lo1 <= hi1) {  // the lower polar wall: into cell it - 1
         hi1 = lo2;
         hi2 = kInf;
         --it;
         if (it < 1) return GOING;  // caught by the range check of the next step
-        kind = 1;
+        fetch_rho(m);
+        cone_roots(m, it - 1, false, lo1, lo2);
       } else {           // the upper polar wall: into cell it + 1
         lo1 = hi2;
         lo2 = kInf;
         ++it;
         if (it > m.ntg - 1) return GOING;
-        kind = 2;
+        fetch_rho(m);
+        cone_roots(m, it, false, hi1, hi2);
       }
     } else {  // the azimuthal wall, with the wrap at 0 / 2 pi
-      if (up) ip = ip == m.npg - 1 ? 1 : ip + 1;
-      else ip = ip == 1 ? m.npg - 1 : ip - 1;
-      kind = 3;
-    }
-    fetch_rho(m);
-    if (kind == 0) {
-      next_sphere(m);
-    } else if (kind == 3) {
-      tp = plane_root(m, up ? ip : ip - 1);
-    } else {
-      float r1, r2;
-      cone_roots(m, kind == 1 ? it - 1 : it, false, r1, r2);
-      if (kind == 1) { lo1 = r1; lo2 = r2; }
-      else { hi1 = r1; hi2 = r2; }
+      if (up) {
+        ip = ip == m.npg - 1 ? 1 : ip + 1;
+        fetch_rho(m);
+        tp = plane_root(m, ip);
+      } else {
+        ip = ip == 1 ? m.npg - 1 : ip - 1;
+        fetch_rho(m);
+        tp = plane_root(m, ip - 1);
+      }
     }
     return GOING;
   }
