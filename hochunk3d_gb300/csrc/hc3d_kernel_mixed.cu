@@ -40,17 +40,17 @@ cudaError_t launch_wave_transport_mixed(const DevModel& m, const DevTallies& t, 
 }
 
 // the block shapes of k_peel_mixed: (threads, blocks per SM at launch bounds)
-constexpr int kPeelShapes[kPeelVariants][2] = {{256, 2}, {128, 4}};
+constexpr int kPeelShapes[kPeelVariants][2] = {{128, 5}, {192, 3}};
 
 cudaError_t launch_wave_peel_mixed(const DevModel& m, const DevTallies& t, const TallyDims& d, const RunArgs& a,
                                    const WaveBufs& w, int q, const LaunchCfg& cfg) {
   const auto* qu = static_cast<const dev::PeelRec<float>*>(w.queue[q]);
   switch (cfg.variant) {
     case 1:
-      dev::k_peel_mixed<float, 128, 4><<<cfg.blocks, 128, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
+      dev::k_peel_mixed<float, 192, 3><<<cfg.blocks, 192, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
       break;
     default:
-      dev::k_peel_mixed<float, 256, 2><<<cfg.blocks, 256, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
+      dev::k_peel_mixed<float, 128, 5><<<cfg.blocks, 128, 0, cfg.stream>>>(m, t, d, a, qu, w.qcount[q], w.next_ray[q]);
   }
   return cudaGetLastError();
 }
@@ -62,8 +62,8 @@ size_t rec_bytes_mixed() { return sizeof(dev::PeelRec<float>); }
 const void* wave_fn_mixed() { return (const void*)dev::k_wave<float>; }
 const void* peel_fn_mixed(int variant) {
   switch (variant) {
-    case 1: return (const void*)dev::k_peel_mixed<float, 128, 4>;
-    default: return (const void*)dev::k_peel_mixed<float, 256, 2>;
+    case 1: return (const void*)dev::k_peel_mixed<float, 192, 3>;
+    default: return (const void*)dev::k_peel_mixed<float, 128, 5>;
   }
 }
 

@@ -1347,7 +1347,7 @@ constexpr int kPeelThreads = 256;
 constexpr int kPeelBuf = 64;
 constexpr int kPeelChunk = 256;  // rays a warp reserves per atomic, at most
 constexpr int kPeelStage = 4;    // records a warp stages in shared memory
-constexpr int kPeelSub = 8;      // crossings per lane between refills of the ray pool
+constexpr int kPeelSub = 16;     // crossings per lane between refills of the ray pool
 
 // peeloff_3d.f90:155-282 for one ray of the mixed form that reached the grid
 // edge: attenuation, the Stokes rotation of a scattered packet, image pixel
@@ -2714,13 +2714,12 @@ static __device__ __noinline__ int prep_rays(const DevModel& m, const PeelRec<fl
 }
 
 // Instantiated for two block shapes, between which the autotuner picks:
-// 256 threads x 2 blocks per SM and 128 x 4 (the walk state of a lane, the
-// set-up stack and the 32-ray tally need about 118 registers).  The smaller
-// blocks retire one by one as the ray pool drains, so the next wave's
-// transport blocks find room sooner.  A shape of 256 x 3 (80 registers,
-// with spills) was slower, and its different register allocation changed
-// which multiply-adds the compiler fused, so its tallies differed in the last
-// bits.
+// 128 threads x 5 blocks per SM and 192 x 3, both held to 96 registers (the
+// walk state of a lane, the set-up stack and the 32-ray tally would take
+// about 118; the spills are outside the crossing loop).  With one register
+// budget the two compile to the same arithmetic, so their tallies agree bit
+// for bit.  128 x 5 (20 warps per SM) ran 2 % faster than 256 x 2 at 118
+// registers (16 warps); 256 x 3 at 80 registers ran slower.
 template <class R, int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB) k_peel_mixed(DevModel m, DevTallies t, TallyDims d, RunArgs a,
                                                               const PeelRec<R>* queue,

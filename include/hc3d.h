@@ -348,7 +348,7 @@ int hc3d_run_batch(hc3d_ctx *const *ctxs, const hc3d_run_params *params, int n);
  * records), then at the best depth the regeneration threshold of the
  * wavefront kernel (1, 4, 8, 16: how many lanes of a warp must be waiting
  * before they take new packets), then in the mixed form the block shape of
- * the peel-off kernel (256 or 128 threads per block).  Other runs: the transport block
+ * the peel-off kernel (128 or 192 threads per block).  Other runs: the transport block
  * size (64, 96, 128).  The settings do not change the tallies.  The tallies
  * are zeroed afterwards. */
 typedef struct hc3d_tune_result {
@@ -366,8 +366,8 @@ int hc3d_autotune(hc3d_ctx *ctx, const hc3d_run_params *sample, hc3d_tune_result
 /* Set the wavefront form's settings by hand (0 keeps a setting): the
  * peel-off queue depth in records (>= 1024), the regeneration threshold
  * (1..32 lanes of a warp), the queue slots a lane reserves per atomic
- * (1..64) and the mixed-form peel-off kernel's block shape (1: 256 threads,
- * 2 blocks per SM; 2: 128 threads, 4 blocks).
+ * (1..64) and the mixed-form peel-off kernel's block shape (1: 128 threads,
+ * 5 blocks per SM; 2: 192 threads, 3 blocks).
  * None of them changes the tallies.  No counterpart in the reference. */
 int hc3d_set_wave_options(hc3d_ctx *ctx, int64_t queue_records, int regen, int qchunk, int peel_shape);
 

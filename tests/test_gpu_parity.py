@@ -294,7 +294,7 @@ def test_autotune_keeps_results(model_factory, ipeel):
     assert len(res["candidates"]) == (8 if ipeel else 3) and all(c["ms"] > 0 for c in res["candidates"])
     if ipeel:
         assert {c["regen"] for c in res["candidates"]} == {1, 4, 8, 16}
-        assert {c["peel_threads"] for c in res["candidates"]} == {128, 256}
+        assert {c["peel_threads"] for c in res["candidates"]} == {128, 192}
     keys = ("si", "nums", "nabs", "dtauabs", "jmean", "counters") + (("ti", "numt", "image_i") if ipeel else ())
     settings = [{}] + ([{"queue_records": 1 << 20, "regen": 16, "qchunk": 1, "peel_shape": 2},
                         {"queue_records": 1 << 21, "regen": 4, "qchunk": 32, "peel_shape": 1},
