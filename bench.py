@@ -762,8 +762,11 @@ def main():
                       "lucy": f"this run's two Lucy set-up iterations x {args.lucy_packets} packets"}[args.temps]
         model.set_tdust(td_steps)
         ctx.set_tdust(td_steps)
-        # the peel-off queue depth, chosen by timing a sample batch (untimed set-up)
-        tune = ctx.autotune(model.run_params(np=200000, iter=900, ipeel=1)) if not args.no_autotune else None
+        # the wavefront settings, chosen by timing a sample chunk of the timed
+        # steps' size (untimed set-up): a smaller sample favours a shallower
+        # peel-off queue than the steps want
+        tune_np = args.packets if args.packets > 0 else 200000
+        tune = ctx.autotune(model.run_params(np=tune_np, iter=900, ipeel=1)) if not args.no_autotune else None
         stream = torch.cuda.ExternalStream(ctx.stream)
         flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
