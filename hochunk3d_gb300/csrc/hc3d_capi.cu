@@ -1769,6 +1769,31 @@ int tdust_to_host(hc3d_ctx* c, double* tdust_out) {
   return HC3D_OK;
 }
 
+extern "C" int hc3d_set_lucy_tally(hc3d_ctx* c, const int64_t* dtauabs) {
+  if (!c || !dtauabs) return HC3D_ERR_INVALID;
+  if (!c->grid) return fail(c, HC3D_ERR_STATE, "load the grid first");
+  if (!c->scales_set) return fail(c, HC3D_ERR_STATE, "no packets were run since the last hc3d_zero_tallies()");
+  CK(cudaSetDevice(c->device));
+  const DevModel& m = c->dm;
+  const int64_t n = m.ncell, n4 = (int64_t)m.nrg * m.ntg * m.npg;
+  std::vector<unsigned long long> buf((size_t)kSlots * n, 0ull);
+  for (int s = 0; s < kSlots; ++s) {
+    const int id = slot_src(c, s, c->ndg_in);
+    if (id < 0) continue;
+    for (int ip = 1; ip < m.npg; ++ip)
+      for (int it = 1; it < m.ntg; ++it)
+        for (int ir = 1; ir < m.nrg; ++ir) {
+          const int64_t c4 = (int64_t)(ir - 1) + (int64_t)m.nrg * ((it - 1) + (int64_t)m.ntg * (ip - 1));
+          const int64_t cc = (int64_t)(ir - 1) + (int64_t)(m.nrg - 1) * ((it - 1) + (int64_t)(m.ntg - 1) * (ip - 1));
+          buf[(size_t)s * n + cc] = (unsigned long long)dtauabs[c4 + n4 * id];
+        }
+  }
+  CK(cudaMemcpyAsync(c->dt.dtauabs, buf.data(), sizeof(unsigned long long) * buf.size(), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return HC3D_OK;
+}
+
 extern "C" int hc3d_lucy_update(hc3d_ctx* c, double ltot, int64_t np, double* tdust_out, double* max_rel_change,
                                 int* converged) {
   if (!c) return HC3D_ERR_INVALID;

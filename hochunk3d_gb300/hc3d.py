@@ -216,6 +216,7 @@ SIGNATURES = {
     "hc3d_get_tallies": (C.c_int, [C.c_void_p, P(RunParams), P(Tallies)]),
     "hc3d_lucy_update": (C.c_int, [C.c_void_p, C.c_double, C.c_int64, dp, dp, ip_]),
     "hc3d_lucy_update_noalloc": (C.c_int, [P(LucyBuffers), dp, ip_]),
+    "hc3d_set_lucy_tally": (C.c_int, [C.c_void_p, P(C.c_int64)]),
     "hc3d_lucy_iterations": (C.c_int, [C.c_void_p, P(RunParams), C.c_int, C.c_double, dp, dp]),
     "hc3d_autotune": (C.c_int, [C.c_void_p, P(RunParams), P(TuneResult)]),
     "hc3d_run_batch": (C.c_int, [P(C.c_void_p), P(RunParams), C.c_int]),
@@ -682,6 +683,12 @@ class Context:
         self._check(lib().hc3d_lucy_update(self._h, ltot, int(np_), None if td is None else td.ctypes.data_as(dp),
                                            C.byref(rel), C.byref(conv)))
         return td, rel.value, bool(conv.value)
+
+    def set_lucy_tally(self, dtauabs: np.ndarray) -> None:
+        """Replace the absorbed-path tally (hc3d_set_lucy_tally): (nrg,ntg,npg,ndg) int64 at this
+        context's path_scale, e.g. the sum of the shards of an iteration."""
+        a = np.asfortranarray(dtauabs, dtype=np.int64)
+        self._check(lib().hc3d_set_lucy_tally(self._h, a.ctypes.data_as(P(C.c_int64))))
 
     def run_chunk(self, params: RunParams, np_iteration: int, final: bool) -> None:
         """One chunk of a peeled iteration of np_iteration packets (hc3d_run_chunk):

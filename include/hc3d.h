@@ -331,6 +331,16 @@ int hc3d_get_tallies(hc3d_ctx *ctx, const hc3d_run_params *params, hc3d_tallies 
 int hc3d_lucy_update(hc3d_ctx *ctx, double ltot, int64_t np, double *tdust_out,
                      double *max_rel_change, int *converged);
 
+/* Replace the context's absorbed-path tally with dtauabs (nrg,ntg,npg,ndg),
+ * int64 at the context's path_scale (hc3d_get_tallies reports it): the sum
+ * of the shards' tallies when the packets of an iteration ran on several
+ * processes (the reference's MPI_ALLREDUCE of newdisktherm.F90:482), so that
+ * hc3d_lucy_update then solves the temperatures of the whole iteration.  The
+ * shards run their packet ranges with hc3d_run_chunk(final = 1) and the
+ * whole iteration's np_iteration, so that every shard tallies at the same
+ * scales. */
+int hc3d_set_lucy_tally(hc3d_ctx *ctx, const int64_t *dtauabs);
+
 /* The packet loops of n models (1..256) in one persistent launch: ctxs[j]
  * runs params[j] with its own tables, grid and tallies.  Peeled runs
  * (ipeel = 1) walk each event's peel-off rays in the thread that made the

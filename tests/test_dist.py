@@ -1,10 +1,12 @@
-"""Multi-process packet sharding on CPU (gloo, world_size 2).
+"""Multi-process packet sharding on CPU (gloo, world_size 2), through the
+library's sharding module (hochunk3d_gb300/shard.py).
 
 The packet loop shards by packet id (the reference splits np over MPI ranks,
 newtts.F90:185-188).  Tallies are int64 fixed point, so the all-reduce of the
 shards equals the single-process run exactly.  The ranks run the oracle on
-CPU; on GPUs each rank runs the library on its own device with the same
-packet_offset arithmetic.
+CPU as their shard's runner; on GPUs each rank runs shard.run_shard with the
+library on its own device (tests/test_gpu_shard.py checks that runner and
+the temperature update of the summed tallies on one GPU).
 """
 from __future__ import annotations
 
@@ -29,11 +31,10 @@ def _free_port() -> int:
 
 
 def _rank(rank, world, port, directory, n, q, name):
-    import torch
     import torch.distributed as dist
 
     import oracle.oracle as O
-    from hochunk3d_gb300 import hc3d
+    from hochunk3d_gb300 import hc3d, shard
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
@@ -45,14 +46,9 @@ def _rank(rank, world, port, directory, n, q, name):
         q.put(e)
         raise
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    lo, hi = n * rank // world, n * (rank + 1) // world
-    p = m.run_params(np=hi - lo, packet_offset=lo, iter=2, ipeel=1, np_total=n)
-    r = O.run(m, p, scales=hc3d.tally_scales(n))
-    out = {}
-    for k in KEYS + ("counters",):
-        t = torch.from_numpy(np.ascontiguousarray(r[k]).astype(np.int64))
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        out[k] = t.numpy()
+    r = shard.sharded_iteration(lambda p: O.run(m, p, scales=hc3d.tally_scales(n)), m, n, rank, world, iter=2,
+                                ipeel=1)
+    out = {k: np.ascontiguousarray(r[k]).astype(np.int64) for k in KEYS + ("counters",)}
     if rank == 0:
         q.put(out)
     dist.barrier()
@@ -83,3 +79,14 @@ def test_two_rank_shards_sum_to_the_single_run(tmp_path, built, name):
     ref = O.run(m, m.run_params(np=n, iter=2, ipeel=1), scales=hc3d.tally_scales(n))
     for k in KEYS + ("counters",):
         np.testing.assert_array_equal(got[k], np.ascontiguousarray(ref[k]).astype(np.int64), err_msg=k)
+
+
+def test_shard_ranges_cover_the_iteration():
+    from hochunk3d_gb300 import shard
+
+    for n, world in ((1500, 2), (7, 3), (1, 4), (10**8, 8)):
+        spans = [shard.shard_range(n, r, world) for r in range(world)]
+        assert spans[0][0] == 0 and spans[-1][1] == n
+        assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))
+    with pytest.raises(ValueError):
+        shard.shard_range(10, 2, 2)
