@@ -157,3 +157,4 @@ def test_new_entry_points_reject_bad_arguments(built):
     assert L.hc3d_set_imean(None, None, None) == -1
     assert L.hc3d_model_load(None, None) == -1
     assert hc3d.host_lib().hc3d_model_sg_tables(None, None) == -1
+    assert L.hc3d_set_lucy_tally(None, None) == -1
