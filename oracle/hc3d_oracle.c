@@ -39,6 +39,7 @@
  */
 #include <math.h>
 #include <pthread.h>
+#include <time.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1697,7 +1698,15 @@ typedef struct mt_job {
   const hc3d_run_params *rp;
   orc_tallies *t;
   int64_t *next; /* shared: the next packet to claim */
+  double deadline; /* CLOCK_MONOTONIC seconds after which no packet is claimed; 0 = none */
+  int64_t *done;   /* shared: packets claimed */
 } mt_job;
+
+static double orc_now(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
 
 /* Each thread claims packets one at a time from a shared counter, so a few
  * long histories do not leave the other threads idle; the int64 tallies of
@@ -1705,8 +1714,10 @@ typedef struct mt_job {
 static void *mt_main(void *arg) {
   mt_job *j = (mt_job *)arg;
   for (;;) {
+    if (j->deadline > 0.0 && orc_now() > j->deadline) break;
     const int64_t pid = __atomic_fetch_add(j->next, 1, __ATOMIC_RELAXED);
     if (pid >= j->rp->np) break;
+    if (j->done) __atomic_fetch_add(j->done, 1, __ATOMIC_RELAXED);
     orc_run_range(j->dt, j->g, j->rp, j->t, pid, pid + 1);
   }
   return NULL;
@@ -1724,10 +1735,37 @@ int orc_run_mt(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run_pa
   for (int k = 0; k < nthreads; ++k) {
     jobs[k].dt = dt; jobs[k].g = g; jobs[k].rp = rp; jobs[k].t = &tls[k];
     jobs[k].next = &next;
+    jobs[k].deadline = 0.0;
+    jobs[k].done = NULL;
     pthread_create(&th[k], NULL, mt_main, &jobs[k]);
   }
   for (int k = 0; k < nthreads; ++k) pthread_join(th[k], NULL);
   free(th);
   free(jobs);
+  return 0;
+}
+
+/* The packets of params claimed by nthreads threads for `seconds` seconds
+ * (the threads then finish the packets they hold); *done receives the
+ * packets run, the ids [0, *done) of params. */
+int orc_run_mt_timed(const hc3d_dust_tables *dt, const hc3d_grid *g, const hc3d_run_params *rp, orc_tallies *tls,
+                     int nthreads, double seconds, int64_t *done) {
+  if (nthreads < 1) nthreads = 1;
+  pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+  mt_job *jobs = (mt_job *)calloc((size_t)nthreads, sizeof(mt_job));
+  int64_t next = 0, claimed = 0;
+  if (!th || !jobs) { free(th); free(jobs); return -3; }
+  const double deadline = orc_now() + seconds;
+  for (int k = 0; k < nthreads; ++k) {
+    jobs[k].dt = dt; jobs[k].g = g; jobs[k].rp = rp; jobs[k].t = &tls[k];
+    jobs[k].next = &next;
+    jobs[k].deadline = deadline;
+    jobs[k].done = &claimed;
+    pthread_create(&th[k], NULL, mt_main, &jobs[k]);
+  }
+  for (int k = 0; k < nthreads; ++k) pthread_join(th[k], NULL);
+  free(th);
+  free(jobs);
+  if (done) *done = claimed;
   return 0;
 }

@@ -40,6 +40,8 @@ def lib() -> C.CDLL:
         dp = P(C.c_double)
         L.orc_run_range.argtypes = [P(DustTables), P(Grid), P(RunParams), P(OrcTallies), C.c_int64, C.c_int64]
         L.orc_run_mt.argtypes = [P(DustTables), P(Grid), P(RunParams), P(OrcTallies), C.c_int]
+        L.orc_run_mt_timed.argtypes = [P(DustTables), P(Grid), P(RunParams), P(OrcTallies), C.c_int, C.c_double,
+                                       P(C.c_int64)]
         L.orc_trace_packet.argtypes = [P(DustTables), P(Grid), P(RunParams), P(OrcTallies), C.c_int64, dp, C.c_int,
                                        P(TraceRec), C.c_int, P(C.c_int)]
         L.orc_stream.argtypes = [C.c_uint64, C.c_int, C.c_int64, C.c_int, dp]
@@ -209,6 +211,23 @@ def run(model: hc3d.Model, params: RunParams, nthreads: int = 1, scales=None, im
                 if isinstance(v, np.ndarray) and n != "counters":
                     res[n] = res[n] + v
     return res
+
+
+def run_timed(model: hc3d.Model, params: RunParams, nthreads: int, seconds: float) -> tuple[int, dict]:
+    """Packets of params (ids from 0, params.np at most) claimed by nthreads
+    threads for `seconds` seconds, each thread then finishing its packet:
+    (packets run, their tallies' counters)."""
+    L = lib()
+    _sg_for(model, params, None, None)
+    t, g = model.tables, model.grid
+    parts = [OracleTallies(model, params) for _ in range(nthreads)]
+    arr = (OrcTallies * nthreads)(*[p.T for p in parts])
+    done = C.c_int64(0)
+    L.orc_run_mt_timed(C.byref(t), C.byref(g), C.byref(params), arr, nthreads, float(seconds), C.byref(done))
+    counters = np.zeros(16, dtype=np.int64)
+    for k in range(nthreads):
+        counters += np.array(arr[k].fx.counters[:], dtype=np.int64)
+    return int(done.value), {"counters": counters}
 
 
 def trace(model: hc3d.Model, params: RunParams, pid: int, uniforms=None, max_rec: int = 4096, imean=None,
