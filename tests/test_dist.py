@@ -90,3 +90,42 @@ def test_shard_ranges_cover_the_iteration():
         assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))
     with pytest.raises(ValueError):
         shard.shard_range(10, 2, 2)
+
+
+def _reduce_rank(rank, world, port, q):
+    import torch.distributed as dist
+
+    from hochunk3d_gb300 import shard
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    t = {"nabs": np.full((3, 4, 2, 4), rank + 1, dtype=np.int64, order="F"),
+         "killed": np.full((3, 4, 2), 10 * (rank + 1), dtype=np.int32, order="F"),
+         "counters": np.arange(16, dtype=np.int64) * (rank + 1), "path_scale": 2.0 ** 20}
+    t["nabs"][1, 2, 0, 3] = 1 << 40
+    r = shard.allreduce_tallies(t)
+    if rank == 0:
+        q.put({k: v for k, v in r.items()})
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_allreduce_keeps_shapes_and_types():
+    """The int64 sums are exact (2^40 + 2^40 = 2^41), int32 counts stay int32 in
+    their Fortran shape, scalars are left alone."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_reduce_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert got["nabs"].dtype == np.int64 and got["nabs"].shape == (3, 4, 2, 4)
+    assert got["nabs"][0, 0, 0, 0] == 3 and got["nabs"][1, 2, 0, 3] == 2 << 40
+    assert got["killed"].dtype == np.int32 and np.all(got["killed"] == 30)
+    np.testing.assert_array_equal(got["counters"], np.arange(16) * 3)
+    assert got["path_scale"] == 2.0 ** 20
